@@ -1,0 +1,422 @@
+"""Benchmark of the GW-transient likelihood hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One step = one launch sequence of the fused likelihood over one batch of
+parameter points (default workload ``tf2_128s``: 3.5PN aligned-spin TaylorF2,
+H1/L1/V1, 128 s at 4096 Hz = 262145 bins, 4096 points per launch) with the
+data, PSD and tables resident in HBM.  ``value`` is the mixed-precision
+throughput in likelihood evaluations per second, timed with CUDA events on the
+launching stream; the L2 is flushed (256 MiB write) before every timed
+launch.  ``e2e`` is the same metric through the public API
+(``GravitationalWaveTransient.log_likelihood_ratio_batch`` with host numpy
+arrays: parameter conversion, host->device copy, launch, device->host copy).
+The plain float64 kernel (the drop-in) is timed on the same workload for the
+ratio, and |dlnL| of the mixed results against it is reported.
+
+``--impl reference`` times the reference algorithm on the host cores (the
+oracle's numpy restatement of bilby's path, one process per core) on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "lnL evals/s, served mixed-precision vs plain FP64 @|ΔlnL|≤1e-3; p50/p99 ms"
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tf2_128s")
+    ap.add_argument("--batch", type=int, default=0, help="points per launch (default: the workload's)")
+    ap.add_argument("--fp64-batch", type=int, default=512, help="points per launch of the float64 comparison")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas: each rank evaluates its own batch)
+# ---------------------------------------------------------------------------
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("nccl")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload construction through the library's own API
+# ---------------------------------------------------------------------------
+def build_likelihood(w, precision="mixed"):
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.source import sinegaussian, taylorf2_aligned
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    model = sinegaussian if w.model == "sinegaussian" else taylorf2_aligned
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=model,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency)
+                            if w.model == "taylorf2" else None)
+    ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+    return GravitationalWaveTransient(ifos, wfg, precision=precision)
+
+
+def algorithmic_counts(w, B):
+    """Per-launch algorithmic work of the mixed kernel.
+
+    bytes: compulsory HBM traffic of one launch -- the per-bin tables read once
+    (float-float phase basis 64 B/bin for TaylorF2, 8 B/bin/detector weights),
+    the parameter block in and the partial sums out.
+    ops: FP32/INT issue slots per (point, bin) of the inner loop: 8 float-float
+    multiply-accumulates of 11 ops + 3 for the reduction, and per detector 14
+    ops (2 integer multiplies, conversion, 2 roundings, 2 SFU, 4 FMA, ...).
+    """
+    n_in = w.n_bins - int(math.ceil(w.minimum_frequency * w.duration))
+    D = len(w.detectors)
+    if w.model == "taylorf2":
+        table = n_in * (64 + 8 * D)
+        ops_per_pb = 8 * 11 + 3 + 14 * D
+    else:
+        table = n_in * (4 + 12 * D)
+        ops_per_pb = 12 + 16 * D
+    chunks = int(math.ceil(n_in / 512))
+    bytes_launch = table + 15 * 8 * B + chunks * B * D * 2 * 8
+    return bytes_launch, ops_per_pb * n_in * B
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's numpy restatement of the reference path
+# ---------------------------------------------------------------------------
+_CPU = {}
+
+
+def _cpu_init(name):
+    from bilby_gb300.workloads import WORKLOADS
+    from oracle import data as OD
+    w = WORKLOADS[name]
+    _CPU["w"] = w
+    _CPU["dets"] = OD.build_workload(w)
+    _CPU["src"] = OD.source_for(w.model, w.minimum_frequency)
+
+
+def _cpu_eval(p):
+    from oracle import restate as R
+    return R.log_likelihood_ratio(_CPU["dets"], _CPU["src"], p)
+
+
+class CpuBaseline:
+    """The oracle (numpy restatement of bilby's log_likelihood_ratio) on all
+    host cores: one spawned process per core, OMP_NUM_THREADS=1."""
+
+    def __init__(self, name):
+        from bilby_gb300.workloads import WORKLOADS, draw_points, point
+        self.name = name
+        self.w = WORKLOADS[name]
+        self.cores = len(os.sched_getaffinity(0))
+        os.environ["OMP_NUM_THREADS"] = "1"
+        _cpu_init(name)
+        self.params = draw_points(self.w, 4096, np.random.default_rng(123))
+        self.point = point
+        t0 = time.perf_counter()
+        _cpu_eval(point(self.params, 0))
+        self.per_eval = time.perf_counter() - t0
+        self.pool = mp.get_context("spawn").Pool(self.cores, initializer=_cpu_init, initargs=(name,))
+        self.pool.map(_cpu_eval, [point(self.params, i) for i in range(self.cores)])
+        self.offset = 0
+
+    def sample(self, target_seconds):
+        n = max(self.cores, int(target_seconds * self.cores / max(self.per_eval, 1e-6)))
+        n = min(n, 4096)
+        pts = [self.point(self.params, (self.offset + i) % 4096) for i in range(n)]
+        self.offset += n
+        t0 = time.perf_counter()
+        self.pool.map(_cpu_eval, pts, chunksize=max(1, n // (4 * self.cores)))
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": "evals/s", "cores": self.cores, "kind": "port",
+                "sample": f"{n} prior draws of {self.name} through the oracle (numpy restatement of bilby's "
+                          f"log_likelihood_ratio), {self.cores} processes, OMP_NUM_THREADS=1, {dt:.1f} s"}
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def cpu_baseline(name, target_seconds):
+    cb = CpuBaseline(name)
+    try:
+        return cb.sample(target_seconds)
+    finally:
+        cb.close()
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    from bilby_gb300.workloads import WORKLOADS
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    cb = CpuBaseline(args.workload)
+    values = []
+    for s in range(args.warmup + args.steps):
+        r = cb.sample(max(2.0, 90.0 / max(1, args.warmup + args.steps)))
+        if s >= args.warmup:
+            values.append(r["value"])
+    cb.close()
+    v = float(np.median(values))
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": w.name, "batch": w.batch, "detectors": list(w.detectors),
+                       "n_bins": w.n_bins, "model": w.model},
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from bilby_gb300 import _build, _capi
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import WORKLOADS, draw_points
+
+    w = WORKLOADS[args.workload]
+    B = args.batch or w.batch
+    torch.cuda.set_device(local)
+    _build.build()
+    dist = Dist(world)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload, args.cpu_seconds)   # spawned before any CUDA work of this process
+    like = build_likelihood(w, precision="mixed")
+    an = like.analysis
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    n_blocks = args.warmup + args.steps
+    rng = np.random.default_rng(w.draw_seed + 7919 * rank)
+    host_params = [draw_points(w, B, rng) for _ in range(n_blocks)]
+    blocks = [torch.from_numpy(params_block(p)).cuda() for p in host_params]
+    out = torch.empty(B, dtype=torch.float64, device="cuda")
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    an.set_profiling(True)
+
+    def timed(precision, bl, n_steps, warm):
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
+        kms = []
+        for s in range(warm):
+            an.log_likelihood_ratio_device(bl[s % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(), precision, sptr)
+        torch.cuda.synchronize()
+        an.last_kernel_ms()
+        dist.barrier()
+        torch.cuda.synchronize()
+        for s in range(n_steps):
+            flush.fill_(float(s))
+            ev0[s].record(stream)
+            an.log_likelihood_ratio_device(bl[(warm + s) % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(),
+                                           precision, sptr)
+            ev1[s].record(stream)
+            kms.append(an.last_kernel_ms())
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+        return ms, kms
+
+    # -- headline: mixed precision, resident inputs ----------------------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, kms = timed("mixed", blocks, args.steps, args.warmup)
+    clk = clocks.stop()
+    total_ms = dist.max(float(np.sum(ms)))
+    value = world * B * args.steps / (total_ms / 1e3)
+
+    # -- plain float64 kernel on the same workload (smaller batch) and |dlnL| --
+    Bf = min(args.fp64_batch, B)
+    fblocks = [b[:, :Bf].contiguous() for b in blocks[:3]]
+    fms, _ = timed("fp64", fblocks, 3, 1)
+    fp64_value = Bf * 3 / (float(np.sum(fms)) / 1e3)
+    res64 = torch.empty(Bf, dtype=torch.float64, device="cuda")
+    resmx = torch.empty(Bf, dtype=torch.float64, device="cuda")
+    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, res64.data_ptr(), "fp64", sptr)
+    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, resmx.data_ptr(), "mixed", sptr)
+    torch.cuda.synchronize()
+    an.last_kernel_ms()
+    dlnl = float((res64 - resmx).abs().max().item())
+
+    # -- end to end through the public API with host buffers --------------------
+    e2e_times = []
+    for s in range(args.warmup + args.steps):
+        p = host_params[s % n_blocks]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = like.log_likelihood_ratio_batch(p)
+        t1 = time.perf_counter()
+        if s >= args.warmup:
+            e2e_times.append(t1 - t0)
+        assert res.shape == (B,)
+    e2e_total = dist.max(float(np.sum(e2e_times)))
+    e2e_value = world * B * args.steps / e2e_total
+
+    # -- roofline of the dominant kernel ---------------------------------------
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bytes_launch, ops_launch = algorithmic_counts(w, B)
+    kernel_ms = float(np.mean(kms))
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    props = torch.cuda.get_device_properties(local)
+    issue_peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12  # Tops/s, FP32 lanes at the sampled clock
+    an.set_profiling(False)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"{w.name}_mixed_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath))
+        traffic = t.get("dram_bytes_per_launch_scaled_to", {}).get(str(B))
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float phase, 0.64 fixed-point time shift)",
+            "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection)",
+            "config": {"workload": w.name, "model": w.model, "detectors": list(w.detectors), "n_bins": w.n_bins,
+                       "duration_s": w.duration, "sampling_frequency": w.sampling_frequency, "batch": B,
+                       "parallelism": f"replicas x{world}", "l2": "flushed before every timed launch (256 MiB write)"},
+            "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+            "fp64": {"value": fp64_value, "unit": "evals/s", "batch": Bf},
+            "mixed_over_fp64": value / world / fp64_value,
+            "max_abs_dlnl_mixed_vs_fp64": dlnl,
+            "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": 8 * _capi.NPARAM * B,
+                    "d2h_bytes_per_step": 8 * B},
+            "gpu_launches": 3 * args.steps * world,
+            "roofline": {"bound": "hbm", "achieved": bytes_launch / (kernel_ms / 1e3) / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": bytes_launch / (kernel_ms / 1e3) / 1e9 / hbm_peak,
+                         "traffic": traffic, "kernel": f"k_mixed_{'tf2' if w.model == 'taylorf2' else 'sg'}",
+                         "kernel_ms": kernel_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "note": "tables are L2/shared-memory resident and reused by every point of the launch; "
+                                 "the kernel is bound by FP32/INT/SFU issue, see compute"},
+            "compute": {"bound": "fp32_issue", "achieved": ops_launch / (kernel_ms / 1e3) / 1e12,
+                        "peak": issue_peak, "unit": "Tops/s",
+                        "frac": ops_launch / (kernel_ms / 1e3) / 1e12 / issue_peak,
+                        "peak_source": "152 SMs x 128 FP32 lanes x sampled SM clock"},
+            "clocks": clk,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    dist.close()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+"""Python owner of one device-resident analysis handle (``gwl_analysis``).
+
+An :class:`Analysis` is built from plain arrays (what bilby's
+``Interferometer`` objects expose) and evaluates ``log_likelihood_ratio``
+for batches of parameter points through the C ABI.  The likelihood class in
+:mod:`bilby_gb300.likelihood` and the serving loop in
+:mod:`bilby_gb300.serving` sit on top of it.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi
+
+PRECISIONS = {"fp64": _capi.PRECISION_FP64, "mixed": _capi.PRECISION_MIXED}
+
+
+@dataclass
+class DetectorData:
+    """The per-detector inputs of the likelihood (one ``Interferometer``)."""
+    name: str
+    vertex: np.ndarray        # geometry.vertex (m)
+    tensor: np.ndarray        # geometry.detector_tensor (3x3)
+    start_time: float         # strain_data.start_time
+    strain: np.ndarray        # masked frequency_domain_strain (complex128)
+    psd: np.ndarray           # power_spectral_density_array
+    mask: np.ndarray          # frequency_mask (bool)
+
+
+def params_block(params: dict, n: int | None = None) -> np.ndarray:
+    """Pack a dict of scalars / arrays into the [NPARAM, B] float64 block.
+    Slots the model does not use may be absent (filled with zeros)."""
+    if n is None:
+        n = 1
+        for v in params.values():
+            s = np.shape(v)
+            if len(s):
+                n = max(n, s[0])
+    block = np.zeros((_capi.NPARAM, n), dtype=np.float64)
+    for key, slot in _capi.SLOT.items():
+        if key in params and params[key] is not None:
+            block[slot] = np.broadcast_to(np.asarray(params[key], dtype=np.float64), (n,))
+    return block
+
+
+class Analysis:
+    """A device-resident analysis: data, PSD, geometry and derived tables."""
+
+    def __init__(self, model: str, frequency: np.ndarray, detectors: list[DetectorData], duration: float,
+                 sampling_frequency: float, minimum_frequency: float = 20.0):
+        self._lib = _capi.load()
+        self.model = model
+        self.model_id = {"sinegaussian": _capi.MODEL_SINEGAUSSIAN, "taylorf2": _capi.MODEL_TAYLORF2}[model]
+        self.n_detectors = len(detectors)
+        if not 1 <= self.n_detectors <= _capi.MAX_DETECTORS:
+            raise ValueError(f"between 1 and {_capi.MAX_DETECTORS} detectors are supported")
+        self.frequency = np.ascontiguousarray(frequency, dtype=np.float64)
+        self.n_bins = len(self.frequency)
+        self.duration = float(duration)
+        self.sampling_frequency = float(sampling_frequency)
+        keep: list = []
+        arr = (_capi.GwlDetector * self.n_detectors)()
+        for i, d in enumerate(detectors):
+            if len(d.strain) != self.n_bins or len(d.psd) != self.n_bins or len(d.mask) != self.n_bins:
+                raise ValueError(f"detector {d.name}: strain/psd/mask length differs from the frequency array")
+            arr[i] = _capi.make_detector_struct(d.name, d.vertex, d.tensor, d.start_time, d.strain, d.psd,
+                                                d.mask, keep)
+        desc = _capi.GwlAnalysisDesc()
+        desc.model = self.model_id
+        desc.n_detectors = self.n_detectors
+        desc.n_bins = self.n_bins
+        desc.duration = self.duration
+        desc.sampling_frequency = self.sampling_frequency
+        desc.minimum_frequency = float(minimum_frequency)
+        desc.frequency = _capi.dptr(self.frequency)
+        desc.detectors = arr
+        handle = ctypes.c_void_p()
+        _capi.check(self._lib.gwl_analysis_create(ctypes.byref(desc), ctypes.byref(handle)), "gwl_analysis_create")
+        self._h = handle
+        self._host_out = None
+        self.time_marginalization = False
+        self.phase_marginalization = False
+        self.distance_marginalization = False
+
+    # -- configuration -----------------------------------------------------
+    def set_time_marginalization(self, enable: bool, jitter: bool, t_min: float, t_max: float):
+        _capi.check(self._lib.gwl_set_time_marginalization(self._h, int(enable), int(jitter), float(t_min),
+                                                           float(t_max)), "gwl_set_time_marginalization")
+        self.time_marginalization = bool(enable)
+
+    def set_phase_marginalization(self, enable: bool):
+        _capi.check(self._lib.gwl_set_phase_marginalization(self._h, int(enable)), "gwl_set_phase_marginalization")
+        self.phase_marginalization = bool(enable)
+
+    def set_distance_marginalization(self, enable: bool, tx=None, ty=None, coeffs=None, bbox=None,
+                                     reference_distance=0.0):
+        if not enable:
+            _capi.check(self._lib.gwl_set_distance_marginalization(self._h, 0, None, 0, None, 0, None, None, 0.0))
+            self.distance_marginalization = False
+            return
+        tx = np.ascontiguousarray(tx, dtype=np.float64)
+        ty = np.ascontiguousarray(ty, dtype=np.float64)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        bb = np.ascontiguousarray(bbox, dtype=np.float64)
+        if c.size != (len(tx) - 4) * (len(ty) - 4):
+            raise ValueError("spline coefficient count does not match the knot vectors")
+        _capi.check(self._lib.gwl_set_distance_marginalization(
+            self._h, 1, _capi.dptr(tx), len(tx), _capi.dptr(ty), len(ty), _capi.dptr(c), _capi.dptr(bb),
+            float(reference_distance)), "gwl_set_distance_marginalization")
+        self.distance_marginalization = True
+
+    # -- queries -----------------------------------------------------------
+    def noise_log_likelihood(self) -> float:
+        out = ctypes.c_double()
+        _capi.check(self._lib.gwl_noise_log_likelihood(self._h, ctypes.byref(out)), "gwl_noise_log_likelihood")
+        return out.value
+
+    def resident_bytes(self) -> int:
+        out = ctypes.c_size_t()
+        _capi.check(self._lib.gwl_analysis_resident_bytes(self._h, ctypes.byref(out)))
+        return int(out.value)
+
+    def log_likelihood_ratio_host(self, block: np.ndarray, precision: str = "fp64") -> np.ndarray:
+        """Host parameter block [NPARAM, B] -> host float64 [B] (synchronous)."""
+        block = np.ascontiguousarray(block, dtype=np.float64)
+        if block.ndim != 2 or block.shape[0] != _capi.NPARAM:
+            raise ValueError("parameter block must have shape (NPARAM, B)")
+        B = block.shape[1]
+        out = np.empty(B, dtype=np.float64)
+        _capi.check(self._lib.gwl_eval_host(self._h, _capi.dptr(block), B, PRECISIONS[precision], _capi.dptr(out)),
+                    "gwl_eval_host")
+        return out
+
+    def log_likelihood_ratio_device(self, block_ptr: int, B: int, out_ptr: int, precision: str = "fp64",
+                                    stream: int = 0):
+        """Device pointers in / out, asynchronous on ``stream`` (a cudaStream_t as int)."""
+        _capi.check(self._lib.gwl_eval_device(self._h, ctypes.c_void_p(block_ptr), int(B), PRECISIONS[precision],
+                                              ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)),
+                    "gwl_eval_device")
+
+    def inner_products_device(self, block_ptr: int, B: int, dh_ptr: int, hh_ptr: int, precision: str = "fp64",
+                              stream: int = 0):
+        _capi.check(self._lib.gwl_inner_products_device(
+            self._h, ctypes.c_void_p(block_ptr), int(B), PRECISIONS[precision], ctypes.c_void_p(dh_ptr),
+            ctypes.c_void_p(hh_ptr), ctypes.c_void_p(stream)), "gwl_inner_products_device")
+
+    def set_profiling(self, enable: bool):
+        _capi.check(self._lib.gwl_set_profiling(self._h, int(enable)), "gwl_set_profiling")
+
+    def last_kernel_ms(self) -> float:
+        ms = ctypes.c_float()
+        _capi.check(self._lib.gwl_profile_last_kernel_ms(self._h, ctypes.byref(ms)), "gwl_profile_last_kernel_ms")
+        return float(ms.value)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.gwl_analysis_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

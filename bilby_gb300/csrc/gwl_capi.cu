@@ -1,0 +1,767 @@
+// Host runtime behind include/gwlnl.h: builds the device-resident tables of an
+// analysis, owns its work space and sequences the kernels of one evaluation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gwl_internal.h"
+#include "gwl_math.cuh"
+
+namespace gwl {
+
+static thread_local std::string t_last_error;
+
+void set_error(const std::string& msg) { t_last_error = msg; }
+
+#define GWL_CUDA(expr)                                                                   \
+  do {                                                                                   \
+    cudaError_t _e = (expr);                                                             \
+    if (_e != cudaSuccess) {                                                             \
+      set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));                     \
+      return GWL_ERR_CUDA;                                                               \
+    }                                                                                    \
+  } while (0)
+
+// Compensated (Kahan-Babuska) float64 accumulator for the set-up sums.
+struct KahanSum {
+  double s = 0.0, c = 0.0;
+  void add(double x) {
+    const double t = s + x;
+    if (std::fabs(s) >= std::fabs(x)) c += (s - t) + x; else c += (x - t) + s;
+    s = t;
+  }
+  double value() const { return s + c; }
+};
+
+}  // namespace gwl
+
+using namespace gwl;
+
+struct gwl_analysis {
+  int model = 0, n_det = 0;
+  int64_t n_bins = 0, n_pad = 0, k_lo = 0, k_hi = 0, k_base = 0, k_fmin = 0;
+  int64_t n_chunks_plain = 0, n_chunks_mixed = 0;
+  double duration = 0, fs = 0, fmin = 0, step = 0, start0 = 0;
+  DetGeom geom[kMaxDet];
+  std::vector<std::vector<double>> host_strain;  // kept for the noise log-likelihood
+  double noise_lnl = 0.0;
+  // device tables
+  double* freq = nullptr;
+  float* freq_f = nullptr;
+  float2* basis = nullptr;
+  double* strain[kMaxDet] = {};
+  double* inv_psd[kMaxDet] = {};
+  float2* w[kMaxDet] = {};
+  float* v[kMaxDet] = {};
+  double* hh_prefix[kMaxDet] = {};
+  double w_scale[kMaxDet] = {}, v_scale[kMaxDet] = {};
+  // marginalisation
+  int time_marg = 0, jitter = 0, phase_marg = 0, dist_marg = 0;
+  double t_min = 0, t_max = 0;
+  double* tx = nullptr;
+  double* ty = nullptr;
+  double* tc = nullptr;
+  int nx = 0, ny = 0;
+  double bbox[4] = {0, 0, 0, 0};
+  double ref_dist = 0;
+  // work space
+  int64_t ws_B = 0;
+  double* d_params = nullptr;
+  double* d_out = nullptr;
+  PointRec* d_rec = nullptr;
+  double* d_part = nullptr;
+  size_t part_bytes = 0;
+  double* d_tm = nullptr;
+  size_t tm_bytes = 0;
+  double* h_params = nullptr;  // pinned staging for gwl_eval_host
+  double* h_out = nullptr;
+  int* d_status = nullptr;
+  cudaStream_t stream = nullptr;
+  size_t resident = 0;
+  // optional CUDA events around the dominant kernel of each evaluation
+  int profiling = 0;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  int ev_pending = 0;
+  std::vector<void*> tables;  // everything allocated for the tables
+  std::mutex mu;
+};
+
+namespace {
+
+template <class T>
+int dev_alloc(gwl_analysis* a, T** p, size_t count, bool table = true) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GWL_ERR_MEMORY : GWL_ERR_CUDA;
+  }
+  if (table) {
+    a->tables.push_back(*p);
+    a->resident += count * sizeof(T);
+  }
+  return GWL_OK;
+}
+
+template <class T>
+int upload(gwl_analysis* a, T** dst, const std::vector<T>& src) {
+  int rc = dev_alloc(a, dst, src.size());
+  if (rc) return rc;
+  GWL_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return GWL_OK;
+}
+
+void free_workspace(gwl_analysis* a) {
+  cudaFree(a->d_params);
+  cudaFree(a->d_out);
+  cudaFree(a->d_rec);
+  cudaFree(a->d_part);
+  cudaFree(a->d_tm);
+  cudaFreeHost(a->h_params);
+  cudaFreeHost(a->h_out);
+  a->h_params = a->h_out = nullptr;
+  a->d_params = a->d_out = a->d_part = a->d_tm = nullptr;
+  a->d_rec = nullptr;
+  a->ws_B = 0;
+  a->part_bytes = a->tm_bytes = 0;
+}
+
+float2 split_ff(double x) {
+  const float hi = (float)x;
+  const float lo = (float)(x - (double)hi);
+  return make_float2(hi, lo);
+}
+
+LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
+  LaunchArgs L;
+  std::memset(&L, 0, sizeof(L));
+  L.model = a->model;
+  L.n_det = a->n_det;
+  L.precision = precision;
+  L.B = B;
+  L.n_bins = a->n_bins;
+  L.k_lo = a->k_lo;
+  L.k_hi = a->k_hi;
+  L.k_base = a->k_base;
+  L.chunk = precision == GWL_PRECISION_FP64 ? kChunkPlain : kChunkMixed;
+  L.n_chunks = precision == GWL_PRECISION_FP64 ? a->n_chunks_plain : a->n_chunks_mixed;
+  L.duration = a->duration;
+  L.step = a->step;
+  L.fmin = a->fmin;
+  L.k_fmin = a->k_fmin;
+  for (int d = 0; d < a->n_det; ++d) {
+    L.det[d] = a->geom[d];
+    L.strain[d] = a->strain[d];
+    L.inv_psd[d] = a->inv_psd[d];
+    L.w[d] = a->w[d];
+    L.v[d] = a->v[d];
+    L.hh_prefix[d] = a->hh_prefix[d];
+    L.w_scale[d] = a->w_scale[d];
+    L.v_scale[d] = a->v_scale[d];
+  }
+  L.freq = a->freq;
+  L.freq_f = a->freq_f;
+  L.basis = a->basis;
+  L.status = a->d_status;
+  L.time_marg = a->time_marg;
+  L.phase_marg = a->phase_marg;
+  L.dist_marg = a->dist_marg;
+  L.jitter = a->jitter;
+  L.t_min = a->t_min;
+  L.t_max = a->t_max;
+  L.delta_tc = 2.0 / a->fs;
+  L.start_time0 = a->start0;
+  L.n_fft = a->n_bins - 1;
+  L.tx = a->tx;
+  L.ty = a->ty;
+  L.tc = a->tc;
+  L.nx = a->nx;
+  L.ny = a->ny;
+  for (int q = 0; q < 4; ++q) L.bbox[q] = a->bbox[q];
+  L.ref_dist = a->ref_dist;
+  return L;
+}
+
+int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
+  const size_t part = (size_t)std::max(a->n_chunks_plain, a->n_chunks_mixed) * B * a->n_det * kPartStride *
+                      sizeof(double);
+  size_t tm = 0;
+  if (a->time_marg) tm = time_marg_work_bytes(L);
+  if (B <= a->ws_B && part <= a->part_bytes && tm <= a->tm_bytes) return GWL_OK;
+  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  free_workspace(a);
+  int rc;
+  if ((rc = dev_alloc(a, &a->d_params, (size_t)GWL_NPARAM * B, false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_out, (size_t)B, false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_rec, (size_t)B, false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_part, part / sizeof(double), false))) return rc;
+  if (tm) {
+    if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_tm), tm, false))) return rc;
+  }
+  GWL_CUDA(cudaMallocHost(&a->h_params, sizeof(double) * GWL_NPARAM * B));
+  GWL_CUDA(cudaMallocHost(&a->h_out, sizeof(double) * B));
+  a->ws_B = B;
+  a->part_bytes = part;
+  a->tm_bytes = tm;
+  return GWL_OK;
+}
+
+int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, double* d_out, double* d_dh,
+             double* d_hh, cudaStream_t s) {
+  if (precision != GWL_PRECISION_FP64 && precision != GWL_PRECISION_MIXED) {
+    set_error("precision must be GWL_PRECISION_FP64 or GWL_PRECISION_MIXED");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (B <= 0) return GWL_OK;
+  LaunchArgs L = make_args(a, B, precision);
+  int rc = ensure_workspace(a, B, L);
+  if (rc) return rc;
+  L.params = d_params;
+  L.rec = a->d_rec;
+  L.part = a->d_part;
+  L.out = d_out;
+  L.dh_out = d_dh;
+  L.hh_out = d_hh;
+  L.tm_work = a->d_tm;
+  GWL_CUDA(launch_prologue(L, s));
+  if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+  if (a->time_marg && d_out) {
+    GWL_CUDA(launch_time_marginalized(L, s));
+    if (a->profiling) {
+      GWL_CUDA(cudaEventRecord(a->ev_end, s));
+      a->ev_pending = 1;
+    }
+    return GWL_OK;
+  }
+  if (precision == GWL_PRECISION_FP64) {
+    GWL_CUDA(launch_plain(L, s));
+  } else {
+    GWL_CUDA(launch_mixed(L, s));
+  }
+  if (a->profiling) {
+    GWL_CUDA(cudaEventRecord(a->ev_end, s));
+    a->ev_pending = 1;
+  }
+  GWL_CUDA(launch_finalize(L, s));
+  return GWL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gwl_last_error(void) { return t_last_error.c_str(); }
+
+const char* gwl_version(void) { return "bilby_gb300 gwlnl 0.1 (sm_103a)"; }
+
+int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
+  if (!desc || !out) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  if (desc->model != GWL_MODEL_SINEGAUSSIAN && desc->model != GWL_MODEL_TAYLORF2) {
+    set_error("unsupported source model");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  if (desc->n_detectors < 1 || desc->n_detectors > kMaxDet || desc->n_bins < 3 || !desc->frequency ||
+      !desc->detectors || !(desc->duration > 0) || !(desc->sampling_frequency > 0)) {
+    set_error("invalid analysis description (detectors 1..4, n_bins >= 3, positive duration and rate)");
+    return GWL_ERR_ARGUMENT;
+  }
+  auto* a = new gwl_analysis();
+  a->model = desc->model;
+  a->n_det = desc->n_detectors;
+  a->n_bins = desc->n_bins;
+  a->duration = desc->duration;
+  a->fs = desc->sampling_frequency;
+  a->fmin = desc->minimum_frequency;
+  const int64_t N = desc->n_bins;
+  const double* f = desc->frequency;
+  // The kernels take f_k = k * step (bilby's linspace(0, fs/2, N) grid).
+  a->step = f[N - 1] / (double)(N - 1);
+  for (int64_t k = 0; k < N; ++k) {
+    if (std::fabs(f[k] - k * a->step) > 1e-9 * std::max(1.0, f[N - 1])) {
+      set_error("frequency_array is not the uniform grid k * df starting at 0");
+      delete a;
+      return GWL_ERR_UNSUPPORTED;
+    }
+  }
+  // in-band hull over all detectors
+  int64_t lo = N, hi = -1;
+  for (int d = 0; d < a->n_det; ++d) {
+    const gwl_detector& det = desc->detectors[d];
+    if (!det.strain || !det.psd || !det.mask) {
+      set_error("detector arrays must be non-null");
+      delete a;
+      return GWL_ERR_ARGUMENT;
+    }
+    for (int64_t k = 0; k < N; ++k)
+      if (det.mask[k]) {
+        lo = std::min(lo, k);
+        hi = std::max(hi, k);
+      }
+    std::memcpy(a->geom[d].vertex, det.vertex, sizeof(det.vertex));
+    std::memcpy(a->geom[d].tensor, det.tensor, sizeof(det.tensor));
+    a->geom[d].start_time = det.start_time;
+  }
+  if (hi < lo) {
+    set_error("frequency masks select no bins");
+    delete a;
+    return GWL_ERR_ARGUMENT;
+  }
+  a->start0 = a->geom[0].start_time;
+  a->k_lo = lo;
+  a->k_hi = hi + 1;
+  a->k_base = (lo / kBinAlign) * kBinAlign;
+  const int64_t span = a->k_hi - a->k_base;
+  a->n_chunks_plain = (span + kChunkPlain - 1) / kChunkPlain;
+  a->n_chunks_mixed = (span + kChunkMixed - 1) / kChunkMixed;
+  a->n_pad = std::max({N + 1, a->k_base + a->n_chunks_plain * kChunkPlain, a->k_base + a->n_chunks_mixed * kChunkMixed});
+  a->n_pad = (a->n_pad + 15) / 16 * 16;
+  a->k_fmin = N;
+  for (int64_t k = 0; k < N; ++k)
+    if (f[k] >= a->fmin) {
+      a->k_fmin = k;
+      break;
+    }
+  const int64_t P = a->n_pad;
+  int rc = GWL_OK;
+  cudaError_t ce = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+    delete a;
+    return GWL_ERR_CUDA;
+  }
+  if ((rc = dev_alloc(a, &a->d_status, 1))) goto fail;
+  if (cudaMemset(a->d_status, 0, sizeof(int)) != cudaSuccess) {
+    rc = GWL_ERR_CUDA;
+    goto fail;
+  }
+  {
+    std::vector<double> hf(P, 0.0);
+    std::vector<float> hff(P, 0.0f);
+    for (int64_t k = 0; k < N; ++k) {
+      hf[k] = f[k];
+      hff[k] = (float)f[k];
+    }
+    if ((rc = upload(a, &a->freq, hf))) goto fail;
+    if (a->model == GWL_MODEL_SINEGAUSSIAN && (rc = upload(a, &a->freq_f, hff))) goto fail;
+    if (a->model == GWL_MODEL_TAYLORF2) {
+      // float-float phase basis: f^-5/3, f^-1, f^-2/3, f^-1/3, ln f, f^1/3, f^1/3 ln f, f^2/3
+      std::vector<float2> basis((size_t)P * kNumBasis, make_float2(0.f, 0.f));
+      for (int64_t k = 0; k < N; ++k) {
+        const double x = f[k];
+        if (!(x > 0)) continue;
+        const double c3 = std::cbrt(x), lx = std::log(x);
+        const double inv3 = 1.0 / c3;
+        const double vals[kNumBasis] = {inv3 * inv3 * inv3 * inv3 * inv3, 1.0 / x, inv3 * inv3, inv3,
+                                        lx, c3, c3 * lx, c3 * c3};
+        for (int b = 0; b < kNumBasis; ++b) basis[(size_t)k * kNumBasis + b] = split_ff(vals[b]);
+      }
+      if ((rc = upload(a, &a->basis, basis))) goto fail;
+    }
+    a->noise_lnl = 0.0;
+    for (int d = 0; d < a->n_det; ++d) {
+      const gwl_detector& det = desc->detectors[d];
+      std::vector<double> s(2 * P, 0.0), ip(P, 0.0);
+      KahanSum dd;
+      for (int64_t k = 0; k < N; ++k) {
+        if (!det.mask[k]) continue;
+        s[2 * k] = det.strain[2 * k];
+        s[2 * k + 1] = det.strain[2 * k + 1];
+        const double S = det.psd[k];
+        ip[k] = (std::isfinite(S) && S > 0) ? 1.0 / S : 0.0;
+        // base.py:402-411: |<d|d>| / 2 with <a|b> = 4/T sum conj(a) b / S
+        dd.add((s[2 * k] * s[2 * k] + s[2 * k + 1] * s[2 * k + 1]) * ip[k]);
+      }
+      a->noise_lnl -= std::fabs(4.0 / a->duration * dd.value() / 2.0);
+      if ((rc = upload(a, &a->strain[d], s))) goto fail;
+      if ((rc = upload(a, &a->inv_psd[d], ip))) goto fail;
+      // mixed-precision weights, scaled into float32 range
+      std::vector<double> wr(P, 0.0), wi(P, 0.0);
+      double wmax = 0.0, vmax = 0.0;
+      for (int64_t k = 0; k < N; ++k) {
+        if (ip[k] == 0.0) continue;
+        const double amp = a->model == GWL_MODEL_TAYLORF2 ? std::pow(f[k], -7.0 / 6.0) : 1.0;
+        wr[k] = amp * s[2 * k] * ip[k];
+        wi[k] = amp * s[2 * k + 1] * ip[k];
+        wmax = std::max(wmax, std::max(std::fabs(wr[k]), std::fabs(wi[k])));
+        vmax = std::max(vmax, ip[k]);
+      }
+      a->w_scale[d] = wmax > 0 ? wmax : 1.0;
+      a->v_scale[d] = vmax > 0 ? vmax : 1.0;
+      std::vector<float2> wf(P, make_float2(0.f, 0.f));
+      std::vector<float> vf(P, 0.f);
+      for (int64_t k = 0; k < N; ++k) {
+        wf[k] = make_float2((float)(wr[k] / a->w_scale[d]), (float)(wi[k] / a->w_scale[d]));
+        vf[k] = (float)(ip[k] / a->v_scale[d]);
+      }
+      if ((rc = upload(a, &a->w[d], wf))) goto fail;
+      if (a->model == GWL_MODEL_SINEGAUSSIAN) {
+        if ((rc = upload(a, &a->v[d], vf))) goto fail;
+      } else {
+        // <h|h> prefix sums of f^(-7/3) / S over the analysis grid
+        std::vector<double> pre(N + 1, 0.0);
+        KahanSum acc;
+        for (int64_t k = 0; k < N; ++k) {
+          if (ip[k] != 0.0 && f[k] > 0) acc.add(std::pow(f[k], -7.0 / 3.0) * ip[k]);
+          pre[k + 1] = acc.value();
+        }
+        if ((rc = upload(a, &a->hh_prefix[d], pre))) goto fail;
+      }
+    }
+  }
+  *out = a;
+  return GWL_OK;
+fail:
+  for (void* p : a->tables) cudaFree(p);
+  if (a->stream) cudaStreamDestroy(a->stream);
+  delete a;
+  return rc ? rc : GWL_ERR_CUDA;
+}
+
+int gwl_analysis_destroy(gwl_analysis* a) {
+  if (!a) return GWL_OK;
+  {
+    std::lock_guard<std::mutex> g(a->mu);
+    cudaStreamSynchronize(a->stream);
+    free_workspace(a);
+    for (void* p : a->tables) cudaFree(p);
+    a->tables.clear();
+    if (a->ev_begin) cudaEventDestroy(a->ev_begin);
+    if (a->ev_end) cudaEventDestroy(a->ev_end);
+    cudaStreamDestroy(a->stream);
+  }
+  delete a;
+  return GWL_OK;
+}
+
+int gwl_analysis_resident_bytes(const gwl_analysis* a, size_t* bytes) {
+  if (!a || !bytes) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *bytes = a->resident;
+  return GWL_OK;
+}
+
+int gwl_set_profiling(gwl_analysis* a, int enable) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (enable && !a->ev_begin) {
+    GWL_CUDA(cudaEventCreate(&a->ev_begin));
+    GWL_CUDA(cudaEventCreate(&a->ev_end));
+  }
+  a->profiling = enable ? 1 : 0;
+  a->ev_pending = 0;
+  return GWL_OK;
+}
+
+int gwl_profile_last_kernel_ms(gwl_analysis* a, float* ms) {
+  if (!a || !ms) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->profiling || !a->ev_pending) {
+    set_error("no profiled evaluation pending (enable gwl_set_profiling first)");
+    return GWL_ERR_STATE;
+  }
+  GWL_CUDA(cudaEventSynchronize(a->ev_end));
+  GWL_CUDA(cudaEventElapsedTime(ms, a->ev_begin, a->ev_end));
+  a->ev_pending = 0;
+  return GWL_OK;
+}
+
+int gwl_noise_log_likelihood(gwl_analysis* a, double* out) {
+  if (!a || !out) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *out = a->noise_lnl;
+  return GWL_OK;
+}
+
+int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double t_min, double t_max) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (enable) {
+    if (!(t_max > t_min)) {
+      set_error("time prior must have t_max > t_min");
+      return GWL_ERR_ARGUMENT;
+    }
+    if ((a->n_bins - 1) % 2 != 0) {
+      set_error("time marginalisation needs an even FFT length (n_bins - 1)");
+      return GWL_ERR_UNSUPPORTED;
+    }
+  }
+  a->time_marg = enable ? 1 : 0;
+  a->jitter = jitter ? 1 : 0;
+  a->t_min = t_min;
+  a->t_max = t_max;
+  return GWL_OK;
+}
+
+int gwl_set_phase_marginalization(gwl_analysis* a, int enable) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  a->phase_marg = enable ? 1 : 0;
+  return GWL_OK;
+}
+
+int gwl_set_distance_marginalization(gwl_analysis* a, int enable, const double* tx, int32_t nx, const double* ty,
+                                     int32_t ny, const double* c, const double bbox[4], double reference_distance) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!enable) {
+    a->dist_marg = 0;
+    return GWL_OK;
+  }
+  if (!tx || !ty || !c || !bbox || nx < 8 || ny < 8 || !(reference_distance > 0)) {
+    set_error("distance spline needs knots (>= 8 per axis), coefficients, a box and a positive reference distance");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<double> vx(tx, tx + nx), vy(ty, ty + ny), vc(c, c + (size_t)(nx - 4) * (ny - 4));
+  int rc;
+  if ((rc = upload(a, &a->tx, vx))) return rc;
+  if ((rc = upload(a, &a->ty, vy))) return rc;
+  if ((rc = upload(a, &a->tc, vc))) return rc;
+  a->nx = nx;
+  a->ny = ny;
+  for (int q = 0; q < 4; ++q) a->bbox[q] = bbox[q];
+  a->ref_dist = reference_distance;
+  a->dist_marg = 1;
+  return GWL_OK;
+}
+
+int gwl_eval_device(gwl_analysis* a, const double* params, int64_t B, int32_t precision, double* out, void* stream) {
+  if (!a || (B > 0 && (!params || !out))) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  return run_eval(a, params, B, precision, out, nullptr, nullptr, static_cast<cudaStream_t>(stream));
+}
+
+int gwl_inner_products_device(gwl_analysis* a, const double* params, int64_t B, int32_t precision, double* d_inner_h,
+                              double* h_inner_h, void* stream) {
+  if (!a || (B > 0 && (!params || !d_inner_h || !h_inner_h))) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  const int saved = a->time_marg;
+  a->time_marg = 0;
+  const int rc = run_eval(a, params, B, precision, nullptr, d_inner_h, h_inner_h, static_cast<cudaStream_t>(stream));
+  a->time_marg = saved;
+  return rc;
+}
+
+int gwl_eval_host(gwl_analysis* a, const double* params, int64_t B, int32_t precision, double* out) {
+  if (!a || (B > 0 && (!params || !out))) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (B <= 0) return GWL_OK;
+  std::lock_guard<std::mutex> g(a->mu);
+  LaunchArgs L = make_args(a, B, precision);
+  int rc = ensure_workspace(a, B, L);
+  if (rc) return rc;
+  // stage through pinned buffers so that both copies are true async DMA
+  std::memcpy(a->h_params, params, sizeof(double) * GWL_NPARAM * B);
+  GWL_CUDA(cudaMemcpyAsync(a->d_params, a->h_params, sizeof(double) * GWL_NPARAM * B, cudaMemcpyHostToDevice,
+                           a->stream));
+  rc = run_eval(a, a->d_params, B, precision, a->d_out, nullptr, nullptr, a->stream);
+  if (rc) return rc;
+  GWL_CUDA(cudaMemcpyAsync(a->h_out, a->d_out, sizeof(double) * B, cudaMemcpyDeviceToHost, a->stream));
+  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  std::memcpy(out, a->h_out, sizeof(double) * B);
+  int status = 0;
+  GWL_CUDA(cudaMemcpy(&status, a->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status != kDevStatusOk) {
+    cudaMemset(a->d_status, 0, sizeof(int));
+    set_error("a bounded device wait gave up (bulk copy did not complete)");
+    return GWL_ERR_TIMEOUT;
+  }
+  return GWL_OK;
+}
+
+int gwl_source_polarizations(int32_t model, const double* frequency, int64_t n, const double* params,
+                             double minimum_frequency, double* plus, double* cross) {
+  if (!frequency || !params || !plus || !cross || n <= 0) {
+    set_error("null argument or empty grid");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (model != GWL_MODEL_SINEGAUSSIAN && model != GWL_MODEL_TAYLORF2) {
+    set_error("unsupported source model");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  double *df = nullptr, *dp = nullptr, *dplus = nullptr, *dcross = nullptr;
+  int rc = GWL_OK;
+  cudaError_t e;
+  if ((e = cudaMalloc(&df, n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dp, GWL_NPARAM * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dplus, 2 * n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dcross, 2 * n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(df, frequency, n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(dp, params, GWL_NPARAM * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = launch_source_polarizations(model, df, n, dp, minimum_frequency, dplus, dcross, 0)) != cudaSuccess)
+    goto cuda_fail;
+  if ((e = cudaMemcpy(plus, dplus, 2 * n * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(cross, dcross, 2 * n * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess) goto cuda_fail;
+  goto done;
+cuda_fail:
+  set_error(std::string("source polarisations: ") + cudaGetErrorString(e));
+  rc = GWL_ERR_CUDA;
+done:
+  cudaFree(df);
+  cudaFree(dp);
+  cudaFree(dplus);
+  cudaFree(dcross);
+  return rc;
+}
+
+int gwl_detector_response(const gwl_detector* det, const double* frequency, int64_t n, const double* plus,
+                          const double* cross, const double* params, double* response) {
+  if (!det || !frequency || !plus || !cross || !params || !response || n <= 0 || !det->mask) {
+    set_error("null argument or empty grid");
+    return GWL_ERR_ARGUMENT;
+  }
+  DetGeom g;
+  std::memcpy(g.vertex, det->vertex, sizeof(g.vertex));
+  std::memcpy(g.tensor, det->tensor, sizeof(g.tensor));
+  g.start_time = det->start_time;
+  std::vector<double> masked_plus(2 * n), masked_cross(2 * n);
+  for (int64_t k = 0; k < n; ++k) {
+    const double m = det->mask[k] ? 1.0 : 0.0;
+    masked_plus[2 * k] = plus[2 * k] * m;
+    masked_plus[2 * k + 1] = plus[2 * k + 1] * m;
+    masked_cross[2 * k] = cross[2 * k] * m;
+    masked_cross[2 * k + 1] = cross[2 * k + 1] * m;
+  }
+  double *df = nullptr, *dp = nullptr, *dplus = nullptr, *dcross = nullptr, *dr = nullptr;
+  int rc = GWL_OK;
+  cudaError_t e;
+  if ((e = cudaMalloc(&df, n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dp, GWL_NPARAM * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dplus, 2 * n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dcross, 2 * n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&dr, 2 * n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(df, frequency, n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(dp, params, GWL_NPARAM * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(dplus, masked_plus.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    goto cuda_fail;
+  if ((e = cudaMemcpy(dcross, masked_cross.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    goto cuda_fail;
+  if ((e = launch_detector_response(g, df, n, dplus, dcross, dp, dr, 0)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(response, dr, 2 * n * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess) goto cuda_fail;
+  goto done;
+cuda_fail:
+  set_error(std::string("detector response: ") + cudaGetErrorString(e));
+  rc = GWL_ERR_CUDA;
+done:
+  cudaFree(df);
+  cudaFree(dp);
+  cudaFree(dplus);
+  cudaFree(dcross);
+  cudaFree(dr);
+  return rc;
+}
+
+int gwl_distance_lookup_table(const double* distance, const double* prior, int32_t n, double ref_dist,
+                              const double* dh_axis, int32_t n_dh, const double* hh_axis, int32_t n_hh,
+                              int phase_marginalization, double* table) {
+  if (!distance || !prior || !dh_axis || !hh_axis || !table || n < 2 || n_dh < 1 || n_hh < 1 || !(ref_dist > 0)) {
+    set_error("invalid lookup-table arguments");
+    return GWL_ERR_ARGUMENT;
+  }
+  const double dd = distance[1] - distance[0];
+  std::vector<double> sc(n), sc2(n), wt(n);
+  KahanSum norm;
+  for (int k = 0; k < n; ++k) {
+    sc[k] = ref_dist / distance[k];
+    sc2[k] = sc[k] * sc[k];
+    wt[k] = prior[k] * dd;
+    norm.add(wt[k]);
+  }
+  // logsumexp(0 / d, b = prior * dd) = log(sum b)
+  const double log_norm = std::log(norm.value());
+  double *d_dh = nullptr, *d_hh = nullptr, *d_sc = nullptr, *d_sc2 = nullptr, *d_wt = nullptr, *d_li = nullptr,
+         *d_tab = nullptr;
+  int rc = GWL_OK;
+  cudaError_t e;
+  const size_t tab = (size_t)n_dh * n_hh;
+  if ((e = cudaMalloc(&d_dh, n_dh * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&d_hh, n_hh * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&d_sc, n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&d_sc2, n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&d_wt, n * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMalloc(&d_tab, tab * sizeof(double))) != cudaSuccess) goto cuda_fail;
+  if (phase_marginalization && (e = cudaMalloc(&d_li, (size_t)n_dh * n * sizeof(double))) != cudaSuccess)
+    goto cuda_fail;
+  if ((e = cudaMemcpy(d_dh, dh_axis, n_dh * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(d_hh, hh_axis, n_hh * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(d_sc, sc.data(), n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(d_sc2, sc2.data(), n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = cudaMemcpy(d_wt, wt.data(), n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) goto cuda_fail;
+  if ((e = launch_distance_table(d_dh, n_dh, d_hh, n_hh, d_sc, d_sc2, d_wt, n, d_li, phase_marginalization, log_norm,
+                                 d_tab)) != cudaSuccess)
+    goto cuda_fail;
+  if ((e = cudaMemcpy(table, d_tab, tab * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess) goto cuda_fail;
+  goto done;
+cuda_fail:
+  set_error(std::string("distance lookup table: ") + cudaGetErrorString(e));
+  rc = GWL_ERR_CUDA;
+done:
+  cudaFree(d_dh);
+  cudaFree(d_hh);
+  cudaFree(d_sc);
+  cudaFree(d_sc2);
+  cudaFree(d_wt);
+  cudaFree(d_li);
+  cudaFree(d_tab);
+  return rc;
+}
+
+int gwl_host_math(int what, const double* x, const double* y, int64_t n, const double* tx, int32_t nx,
+                  const double* ty, int32_t ny, const double* c, const double bbox[4], double* out) {
+  if (!x || !out || n < 0) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (what == 0) {
+    for (int64_t i = 0; i < n; ++i) out[i] = gwl::ln_i0(x[i]);
+    return GWL_OK;
+  }
+  if (what == 1) {
+    if (!y || !tx || !ty || !c || !bbox || nx < 8 || ny < 8) {
+      set_error("spline evaluation needs knots, coefficients and a box");
+      return GWL_ERR_ARGUMENT;
+    }
+    for (int64_t i = 0; i < n; ++i) out[i] = gwl::bicubic_eval(tx, nx, ty, ny, c, bbox, x[i], y[i]);
+    return GWL_OK;
+  }
+  set_error("unknown host_math selector");
+  return GWL_ERR_ARGUMENT;
+}
+
+}  // extern "C"

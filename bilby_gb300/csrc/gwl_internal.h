@@ -1,0 +1,103 @@
+// Internal declarations shared by the host runtime (gwl_capi.cu) and the
+// kernel translation units.  Not part of the public ABI (include/gwlnl.h).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gwlnl.h"
+
+namespace gwl {
+
+constexpr int kMaxDet = GWL_MAX_DETECTORS;
+constexpr int kPointsPerCta = 128;     // one thread per parameter point
+constexpr int kChunkPlain = 256;       // bins per CTA, float64 kernels
+constexpr int kChunkMixed = 512;       // bins per CTA, mixed-precision kernels
+constexpr int kBinAlign = 16;          // chunk starts are multiples of this many bins
+constexpr int kNumBasis = 8;           // TaylorF2 phase basis functions of f
+constexpr int kPartStride = 6;         // doubles per (chunk, point, detector) partial record
+constexpr int kDevStatusOk = 0;
+constexpr int kDevStatusTimeout = 1;
+constexpr int kDevStatusBadInput = 2;
+constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
+
+// Per-point quantities computed once per evaluation by the float64 prologue.
+struct PointRec {
+  double fp[kMaxDet], fx[kMaxDet], dt[kMaxDet];  // antenna patterns; (t_geo - t_start) + delay
+  uint32_t xfix[kMaxDet][2];                     // frac(dt * df) as 0.64 fixed point {lo, hi}
+  double amp;          // TaylorF2 amplitude prefactor A0 | sine-Gaussian plus factor
+  double amp2;         // sine-Gaussian cross factor
+  double sg_f0, sg_a;  // sine-Gaussian centre frequency, pi^2 tau^2
+  double m_sec, eta, f_isco, cos_i, phase, dist, jitter;
+  double a[8], l[8];                 // TaylorF2 phase coefficients
+  float c_hi[kNumBasis + 1];         // TaylorF2 phase basis coefficients in cycles (float-float)
+  float c_lo[kNumBasis + 1];         // index kNumBasis: frac of the constant term
+  int64_t k_start, k_end;            // TaylorF2 band [k_start, k_end) on the analysis grid
+  int32_t valid;                     // 0: waveform undefined (lnL = nan_to_num(-inf))
+};
+
+struct DetGeom {
+  double vertex[3];
+  double tensor[9];
+  double start_time;
+};
+
+// Everything a kernel needs, passed by value.
+struct LaunchArgs {
+  int model, n_det, precision;
+  int64_t B;
+  int64_t n_bins, k_lo, k_hi, k_base;   // in-band hull [k_lo, k_hi); chunk origin k_base
+  int64_t n_chunks;                     // chunks over [k_base, k_hi)
+  int chunk;                            // bins per chunk
+  double duration, step, fmin;
+  int64_t k_fmin;                       // first bin with f >= minimum_frequency
+  DetGeom det[kMaxDet];
+  const double* freq;                   // [n_pad] float64 frequency array
+  const float* freq_f;                  // [n_pad] float32 copy (sine-Gaussian mixed)
+  const double* strain[kMaxDet];        // [2*n_pad] masked strain
+  const double* inv_psd[kMaxDet];       // [n_pad] mask / S
+  const float2* w[kMaxDet];             // [n_pad] mixed data weights (scaled)
+  const float* v[kMaxDet];              // [n_pad] mixed inverse PSD (scaled)
+  const double* hh_prefix[kMaxDet];     // [n_bins + 1] TaylorF2 <h|h> prefix sums
+  double w_scale[kMaxDet], v_scale[kMaxDet];
+  const float2* basis;                  // [n_pad][kNumBasis] float-float phase basis
+  const double* params;                 // [GWL_NPARAM][B]
+  PointRec* rec;                        // [B]
+  double* part;                         // [n_chunks][B][n_det][kPartStride]
+  double* out;                          // [B]
+  double* dh_out;                       // optional [2B] complex <d|h> totals
+  double* hh_out;                       // optional [B] <h|h> totals
+  int* status;                          // device status word
+  // marginalisation
+  int time_marg, phase_marg, dist_marg, jitter;
+  double t_min, t_max, delta_tc, start_time0;
+  int64_t n_fft;                        // time-marginalisation FFT length (n_bins - 1)
+  const double* tx; const double* ty; const double* tc;  // distance spline
+  int nx, ny;
+  double bbox[4];
+  double ref_dist;
+  double* tm_work;                      // time-marginalisation work space
+};
+
+// Kernel launchers (defined in gwl_kernels.cu / gwl_marg.cu).
+cudaError_t launch_prologue(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
+size_t time_marg_work_bytes(const LaunchArgs& a);
+cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,
+                                        double fmin, double* plus, double* cross, cudaStream_t s);
+cudaError_t launch_detector_response(const DetGeom& g, const double* freq, int64_t n, const double* plus,
+                                     const double* cross, const double* params, double* resp, cudaStream_t s);
+
+cudaError_t launch_distance_table(const double* dh_axis, int n_dh, const double* hh_axis, int n_hh,
+                                  const double* scaling, const double* scaling2, const double* weight, int n,
+                                  double* lni0_work, int phase, double log_norm, double* table);
+
+void set_error(const std::string& msg);
+
+}  // namespace gwl

@@ -1,0 +1,430 @@
+// Time marginalisation (bilby/gw/likelihood/base.py:325-330, 794-820,
+// 1027-1035), composed with phase (ln I0) and distance (bicubic table)
+// marginalisation.
+//
+// One CTA per parameter point:
+//   A. the fused integrand z_k = 4/T sum_det h_det,k conj(d_k) / S_k for
+//      k < L = n_bins - 1, written in bit-reversed order into shared memory
+//      (mixed precision, float32) or into this CTA's slot of an L2-resident
+//      work buffer (float64; 16 B * L does not fit in shared memory);
+//   B. an in-place radix-2 decimation-in-time FFT of length L (numpy's sign
+//      convention, exp(-2 pi i m k / L));
+//   C. the time samples inside the geocent_time prior, paired with FFT index
+//      j exactly as the reference pairs them (times[j] = start + (j+1) 2/fs
+//      + jitter), the per-sample marginalised log-likelihood, and a
+//      logsumexp weighted by prior(t_j) * delta_tc, reduced in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+
+#include "gwl_device.cuh"
+#include "gwl_internal.h"
+#include "gwl_math.cuh"
+
+namespace gwl {
+
+constexpr int kTmThreads = 512;
+
+template <bool MIXED>
+struct TmTypes;
+template <>
+struct TmTypes<true> {
+  using C = float2;
+  using R = float;
+};
+template <>
+struct TmTypes<false> {
+  using C = double2;
+  using R = double;
+};
+
+__device__ __forceinline__ uint32_t bit_reverse(uint32_t k, int log2n) { return __brev(k) >> (32 - log2n); }
+
+// float64 source polarisations of the plain kernels at one frequency.
+__device__ __forceinline__ bool plain_pols(const LaunchArgs& a, const PointRec& r, double f, double2& hp, double2& hx) {
+  if (a.model == GWL_MODEL_SINEGAUSSIAN) {
+    const double pi2 = 9.869604401089358;
+    const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
+    const double neg = exp(-(fm * fm) * pi2 * r.a[3]);
+    const double pos = exp(-(fpl * fpl) * pi2 * r.a[3]);
+    hp = make_double2(r.a[0] * (neg + pos) / r.a[1], 0.0);
+    hx = make_double2(0.0, -(r.a[0] * (neg - pos) / r.a[2]));
+    return true;
+  }
+  if (f < a.fmin || f >= r.f_isco) return false;
+  const double v = cbrt(kPi * r.m_sec * f), lnv = log(v);
+  double s = 0.0, vk = 1.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    s = s + (r.a[q] + r.l[q] * lnv) * vk;
+    vk = vk * v;
+  }
+  const double psi = (-2.0 * r.phase - kPi / 4) + 3.0 / (128.0 * r.eta) * s / (v * v * v * v * v);
+  const double amp = r.amp * pow(f, -7.0 / 6.0);
+  double sp, cp;
+  sincos(psi, &sp, &cp);
+  const double ere = amp * cp, eim = -amp * sp, ci = r.cos_i, pf = (1.0 + ci * ci) / 2.0;
+  hp = make_double2(pf * ere, pf * eim);
+  hx = make_double2(ci * eim, -ci * ere);
+  return true;
+}
+
+// Block-wide reductions over kTmThreads threads in a fixed tree order.
+__device__ double block_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kTmThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kTmThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = red[threadIdx.x] + red[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+template <int D, bool MIXED>
+__global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const typename TmTypes<MIXED>::C* twiddle,
+                                                          int log2L) {
+  using C = typename TmTypes<MIXED>::C;
+  using R = typename TmTypes<MIXED>::R;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[kTmThreads];
+  const int64_t L = a.n_fft;
+  const double norm = 4.0 / a.duration;
+  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+    C* buf = MIXED ? reinterpret_cast<C*>(smem) : reinterpret_cast<C*>(a.tm_work) + (size_t)blockIdx.x * L;
+    const PointRec& r = a.rec[i];
+    // ---- A: integrand --------------------------------------------------
+    double hh_part = 0.0;
+    if constexpr (MIXED) {
+      float gre[D], gim[D], cre[D], cim[D];
+      uint32_t xl[D], xh[D];
+      float ch[kNumBasis + 1], cl[kNumBasis + 1];
+      for (int d = 0; d < D; ++d) {
+        xl[d] = r.xfix[d][0];
+        xh[d] = r.xfix[d][1];
+        if (a.model == GWL_MODEL_TAYLORF2) {
+          const double ci = r.cos_i;
+          const double s = norm * r.amp * a.w_scale[d];
+          gre[d] = (float)(s * r.fp[d] * (1.0 + ci * ci) / 2.0);
+          gim[d] = (float)(-s * r.fx[d] * ci);
+        } else {
+          cre[d] = (float)(norm * a.w_scale[d] * r.fp[d] * r.amp);
+          cim[d] = (float)(norm * a.w_scale[d] * r.fx[d] * r.amp2);
+        }
+      }
+      for (int b = 0; b <= kNumBasis; ++b) {
+        ch[b] = r.c_hi[b];
+        cl[b] = r.c_lo[b];
+      }
+      const float f0h = (float)r.sg_f0, f0l = (float)(r.sg_f0 - (double)f0h);
+      const float gah = (float)r.sg_a, gal = (float)(r.sg_a - (double)gah);
+      float hh1[D], hh2[D];
+      for (int d = 0; d < D; ++d) hh1[d] = hh2[d] = 0.f;
+      for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
+        float zr = 0.f, zi = 0.f;
+        const bool in_hull = k >= a.k_lo && k < a.k_hi;
+        if (r.valid && in_hull) {
+          if (a.model == GWL_MODEL_TAYLORF2) {
+            if (k >= r.k_start && k < r.k_end) {
+              const float4* bp = reinterpret_cast<const float4*>(a.basis + k * kNumBasis);
+              float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+              for (int q = 0; q < kNumBasis / 2; ++q) {
+                const float4 v = bp[q];
+                ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+                ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
+              }
+              const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+                float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
+                ph -= rintf(ph);
+                float sn, cs;
+                __sincosf(ph * 6.283185307179586f, &sn, &cs);
+                const float2 w = a.w[d][k];
+                const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+                // h conj(d) / S = G conj(e^{i Phi} w)
+                zr += gre[d] * er + gim[d] * ei;
+                zi += gim[d] * er - gre[d] * ei;
+              }
+            }
+          } else {
+            const float f = a.freq_f[k];
+            const float g1 = gauss_ff(f, f0h, f0l, gah, gal, -1.0f);
+            const float g2 = gauss_ff(f, f0h, f0l, gah, gal, 1.0f);
+            const float hp = g1 + g2, hx = g1 - g2;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+              const float ph = __int2float_rn((int)top) * 2.3283064365386963e-10f;
+              float sn, cs;
+              __sincosf(ph * 6.283185307179586f, &sn, &cs);
+              const float2 w = a.w[d][k];
+              const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+              // (C hp - i E hx) conj(e)
+              const float ar = cre[d] * hp, ai = -cim[d] * hx;
+              zr += ar * er + ai * ei;
+              zi += ai * er - ar * ei;
+              const float vv = a.v[d][k];
+              hh1[d] = __fmaf_rn(hp * hp, vv, hh1[d]);
+              hh2[d] = __fmaf_rn(hx * hx, vv, hh2[d]);
+            }
+          }
+        }
+        buf[bit_reverse((uint32_t)k, log2L)] = make_float2(zr, zi);
+      }
+      if (a.model == GWL_MODEL_SINEGAUSSIAN) {
+        for (int d = 0; d < D; ++d) {
+          const double A = r.fp[d] * r.amp, Cx = r.fx[d] * r.amp2;
+          hh_part += norm * a.v_scale[d] * (A * A * hh1[d] + Cx * Cx * hh2[d]);
+        }
+      }
+    } else {
+      double w2[D];
+      for (int d = 0; d < D; ++d) w2[d] = 2.0 * kPi * r.dt[d];
+      for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
+        double zr = 0.0, zi = 0.0;
+        double2 hp, hx;
+        if (r.valid && k >= a.k_lo && k < a.k_hi) {
+          const double f = a.freq[k];
+          if (plain_pols(a, r, f, hp, hx)) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const double is = a.inv_psd[d][k];
+              if (is == 0.0) continue;
+              const double sre = hp.x * r.fp[d] + hx.x * r.fx[d];
+              const double sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+              double sn, cs;
+              sincos(w2[d] * f, &sn, &cs);
+              const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+              const double2 dd = reinterpret_cast<const double2*>(a.strain[d])[k];
+              // base.py:326-329: signal * conj(d) / S
+              zr += (hre * dd.x + him * dd.y) * is;
+              zi += (him * dd.x - hre * dd.y) * is;
+              hh_part += (hre * hre + him * him) * is;
+            }
+          }
+        }
+        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(norm * zr, norm * zi);
+      }
+      hh_part *= norm;
+    }
+    // The last bin (index L) only enters <h|h>; the FFT uses bins 0..L-1.
+    if (!MIXED && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
+      double2 hp, hx;
+      const double f = a.freq[L];
+      if (plain_pols(a, r, f, hp, hx)) {
+        for (int d = 0; d < D; ++d) {
+          const double is = a.inv_psd[d][L];
+          const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+          hh_part += norm * (sre * sre + sim * sim) * is;
+        }
+      }
+    }
+    if (MIXED && a.model == GWL_MODEL_SINEGAUSSIAN && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
+      const double f = a.freq[L];
+      const double pi2 = 9.869604401089358;
+      const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
+      const double g1 = exp(-(fm * fm) * pi2 * r.a[3]), g2 = exp(-(fpl * fpl) * pi2 * r.a[3]);
+      for (int d = 0; d < D; ++d) {
+        const double A = r.fp[d] * r.amp, Cx = r.fx[d] * r.amp2;
+        hh_part += norm * a.inv_psd[d][L] * (A * A * (g1 + g2) * (g1 + g2) + Cx * Cx * (g1 - g2) * (g1 - g2));
+      }
+    }
+    __syncthreads();
+    // ---- B: in-place radix-2 FFT -----------------------------------------
+    for (int s = 1; s <= log2L; ++s) {
+      const int64_t half = (int64_t)1 << (s - 1);
+      const int64_t tstride = L >> s;  // twiddle index stride W_L^(pos * L / len)
+      for (int64_t b = threadIdx.x; b < L / 2; b += blockDim.x) {
+        const int64_t pos = b & (half - 1);
+        const int64_t i0 = ((b >> (s - 1)) << s) + pos;
+        const int64_t i1 = i0 + half;
+        const C w = twiddle[pos * tstride];
+        const C x1 = buf[i1];
+        const C x0 = buf[i0];
+        const R tr = w.x * x1.x - w.y * x1.y;
+        const R ti = w.x * x1.y + w.y * x1.x;
+        C y0, y1;
+        y0.x = x0.x + tr;
+        y0.y = x0.y + ti;
+        y1.x = x0.x - tr;
+        y1.y = x0.y - ti;
+        buf[i0] = y0;
+        buf[i1] = y1;
+      }
+      __syncthreads();
+    }
+    // ---- C: prior window, marginalised lnL per time sample, logsumexp ----
+    double hh = block_sum(hh_part, red);
+    if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
+      hh = 0.0;
+      for (int d = 0; d < D; ++d) {
+        const double ci = r.cos_i;
+        const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
+        const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+        hh += norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
+      }
+    }
+    const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
+    const double prob = 1.0 / (a.t_max - a.t_min);
+    const double jit = r.jitter;
+    // candidate window from the real-valued bounds, checked exactly below
+    const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
+    const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
+    const int64_t j_lo = (int64_t)fmax(0.0, jl), j_hi = (int64_t)fmin((double)(L - 1), jh);
+    double best = -INFINITY;
+    for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
+      const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
+      const double t = (a.start_time0 + lin) + jit;
+      if (!(t >= a.t_min && t <= a.t_max)) continue;
+      const C x = buf[j];
+      const double xr = (double)x.x, xi = (double)x.y;
+      double l;
+      if (a.dist_marg) {
+        const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+        const double sr = r.dist / a.ref_dist;
+        const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
+        l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
+      } else if (a.phase_marg) {
+        l = ln_i0(sqrt(xr * xr + xi * xi)) - hh / 2;
+      } else {
+        l = xr - hh / 2;
+      }
+      best = fmax(best, l);
+    }
+    const double amax = block_max(best, red);
+    double acc = 0.0;
+    if (isfinite(amax)) {
+      for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
+        const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
+        const double t = (a.start_time0 + lin) + jit;
+        if (!(t >= a.t_min && t <= a.t_max)) continue;
+        const C x = buf[j];
+        const double xr = (double)x.x, xi = (double)x.y;
+        double l;
+        if (a.dist_marg) {
+          const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+          const double sr = r.dist / a.ref_dist;
+          const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
+          l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
+        } else if (a.phase_marg) {
+          l = ln_i0(sqrt(xr * xr + xi * xi)) - hh / 2;
+        } else {
+          l = xr - hh / 2;
+        }
+        acc += prob * a.delta_tc * exp(l - amax);
+      }
+    }
+    const double total = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+      double lnl;
+      if (!r.valid) lnl = -1.7976931348623157e308;
+      else if (!isfinite(amax)) lnl = amax;
+      else lnl = amax + log(total);
+      a.out[i] = lnl;
+    }
+    __syncthreads();
+  }
+}
+
+namespace {
+
+struct TwiddleCache {
+  int64_t L = 0;
+  double2* d64 = nullptr;
+  float2* d32 = nullptr;
+};
+TwiddleCache g_twiddle;
+
+cudaError_t ensure_twiddles(int64_t L) {
+  if (g_twiddle.L == L) return cudaSuccess;
+  cudaFree(g_twiddle.d64);
+  cudaFree(g_twiddle.d32);
+  g_twiddle = TwiddleCache();
+  const int64_t H = L / 2;
+  double2* h64 = new double2[H];
+  float2* h32 = new float2[H];
+  for (int64_t t = 0; t < H; ++t) {
+    // exp(-2 pi i t / L), argument reduced to an exact rational of pi
+    const double ang = -2.0 * 3.141592653589793 * (double)t / (double)L;
+    h64[t] = make_double2(std::cos(ang), std::sin(ang));
+    h32[t] = make_float2((float)h64[t].x, (float)h64[t].y);
+  }
+  cudaError_t e = cudaMalloc(&g_twiddle.d64, H * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc(&g_twiddle.d32, H * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(g_twiddle.d64, h64, H * sizeof(double2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(g_twiddle.d32, h32, H * sizeof(float2), cudaMemcpyHostToDevice);
+  delete[] h64;
+  delete[] h32;
+  if (e == cudaSuccess) g_twiddle.L = L;
+  return e;
+}
+
+int log2_exact(int64_t L) {
+  int s = 0;
+  while (((int64_t)1 << s) < L) ++s;
+  return ((int64_t)1 << s) == L ? s : -1;
+}
+
+int tm_grid_fp64() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? 2 * sms : 304;
+}
+
+}  // namespace
+
+size_t time_marg_work_bytes(const LaunchArgs& a) {
+  // float64 integrand / FFT slots, one per resident CTA
+  return (size_t)tm_grid_fp64() * (size_t)a.n_fft * sizeof(double2);
+}
+
+template <int D>
+static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
+  if (a.precision == GWL_PRECISION_MIXED) {
+    const size_t smem = (size_t)a.n_fft * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(k_time_marg<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)a.B;
+    k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d32, log2L);
+  } else {
+    const unsigned grid = (unsigned)std::min<int64_t>(a.B, tm_grid_fp64());
+    k_time_marg<D, false><<<grid, kTmThreads, 0, s>>>(a, g_twiddle.d64, log2L);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
+  const int log2L = log2_exact(a.n_fft);
+  if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
+  if (a.precision == GWL_PRECISION_MIXED && (size_t)a.n_fft * sizeof(float2) > 200 * 1024)
+    return cudaErrorInvalidValue;
+  cudaError_t e = ensure_twiddles(a.n_fft);
+  if (e != cudaSuccess) return e;
+  switch (a.n_det) {
+    case 1: return launch_tm_d<1>(a, s, log2L);
+    case 2: return launch_tm_d<2>(a, s, log2L);
+    case 3: return launch_tm_d<3>(a, s, log2L);
+    default: return launch_tm_d<4>(a, s, log2L);
+  }
+}
+
+}  // namespace gwl

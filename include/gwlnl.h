@@ -1,0 +1,203 @@
+/*
+ * gwlnl.h -- C ABI of the GB300 gravitational-wave transient likelihood.
+ *
+ * One analysis handle holds, resident in device memory, everything that
+ * bilby's GravitationalWaveTransient reads from its Interferometer objects
+ * (masked strain, PSD, frequency mask, detector geometry) plus the tables the
+ * kernels derive from them.  A batch call evaluates log_likelihood_ratio for
+ * B parameter points in one fused launch sequence; the strain h(f) is never
+ * written to device memory.
+ *
+ * The entry points replace, for the sine-Gaussian and TaylorF2 source models
+ * and identity calibration, the reference call chain
+ *
+ *   GravitationalWaveTransient.__init__          bilby/gw/likelihood/base.py:150-229
+ *   GravitationalWaveTransient.noise_log_likelihood  base.py:402-417
+ *   GravitationalWaveTransient.log_likelihood_ratio  base.py:419-477
+ *     -> WaveformGenerator.frequency_domain_strain   bilby/gw/waveform_generator.py:113-209
+ *     -> Interferometer.get_detector_response        bilby/gw/detector/interferometer.py:303-368
+ *     -> noise_weighted_inner_product                bilby/gw/utils.py:118-138
+ *     -> time / phase / distance marginalisation     base.py:775-820
+ *
+ * Conventions: every function returns a gwl_status (0 = success); no C++
+ * exception crosses the ABI; gwl_last_error() returns a description of the
+ * last failure on the calling thread.  Arrays are plain pointers with
+ * explicit sizes; complex arrays are interleaved (re, im) float64.
+ * One handle is used by one host thread at a time.
+ */
+#ifndef GWLNL_H
+#define GWLNL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GWL_OK = 0,
+  GWL_ERR_ARGUMENT = 1,      /* invalid argument (maps to ValueError) */
+  GWL_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  GWL_ERR_MEMORY = 3,        /* device allocation failed or HBM budget exceeded */
+  GWL_ERR_UNSUPPORTED = 4,   /* model / option not implemented (NotImplementedError) */
+  GWL_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
+  GWL_ERR_STATE = 6          /* handle not configured for the request */
+} gwl_status;
+
+typedef enum {
+  GWL_MODEL_SINEGAUSSIAN = 1, /* bilby/gw/source.py:1153-1209 */
+  GWL_MODEL_TAYLORF2 = 2      /* 3.5PN aligned-spin TaylorF2 (published PN phase) */
+} gwl_model;
+
+typedef enum {
+  GWL_PRECISION_FP64 = 0,  /* plain fused float64 kernels: the drop-in */
+  GWL_PRECISION_MIXED = 1  /* float-float phase + fixed-point time shift, float32 products */
+} gwl_precision;
+
+/* Parameter slots of the [GWL_NPARAM][B] float64 parameter block. */
+typedef enum {
+  GWL_P_RA = 0,
+  GWL_P_DEC,
+  GWL_P_PSI,
+  GWL_P_GEOCENT_TIME,
+  GWL_P_TIME_JITTER,
+  GWL_P_HRSS,
+  GWL_P_Q,
+  GWL_P_FREQUENCY,
+  GWL_P_MASS_1,
+  GWL_P_MASS_2,
+  GWL_P_CHI_1,
+  GWL_P_CHI_2,
+  GWL_P_LUMINOSITY_DISTANCE,
+  GWL_P_THETA_JN,
+  GWL_P_PHASE,
+  GWL_NPARAM
+} gwl_param;
+
+#define GWL_MAX_DETECTORS 4
+
+/* One Interferometer, as the likelihood reads it
+ * (interferometer.py:551-564, strain_data.py:143-233, detector/geometry.py:201-270). */
+typedef struct {
+  char name[8];
+  double vertex[3];        /* geometry.vertex, metres, geocentric */
+  double tensor[9];        /* geometry.detector_tensor, row major */
+  double start_time;       /* strain_data.start_time (GPS s) */
+  const double *strain;    /* [2*n_bins] masked frequency_domain_strain, host */
+  const double *psd;       /* [n_bins] power_spectral_density_array, host (+inf allowed) */
+  const uint8_t *mask;     /* [n_bins] frequency_mask, host */
+} gwl_detector;
+
+typedef struct {
+  int32_t model;               /* gwl_model */
+  int32_t n_detectors;         /* 1..GWL_MAX_DETECTORS */
+  int64_t n_bins;              /* len(frequency_array) */
+  double duration;             /* waveform_generator.duration */
+  double sampling_frequency;   /* waveform_generator.sampling_frequency */
+  double minimum_frequency;    /* TaylorF2 waveform argument (Hz) */
+  const double *frequency;     /* [n_bins] frequency_array, host */
+  const gwl_detector *detectors;
+} gwl_analysis_desc;
+
+typedef struct gwl_analysis gwl_analysis;
+
+/* Create a device-resident analysis (base.py:150-229 minus marginalisation
+ * set-up).  Copies and derives every table; the caller's arrays may be freed
+ * on return. */
+int gwl_analysis_create(const gwl_analysis_desc *desc, gwl_analysis **out);
+int gwl_analysis_destroy(gwl_analysis *a);
+
+/* Bytes of device memory the analysis holds (tables, not per-batch work space). */
+int gwl_analysis_resident_bytes(const gwl_analysis *a, size_t *bytes);
+
+/* noise_log_likelihood(): -sum_det |<d|d>| / 2 over masked bins (base.py:402-417). */
+int gwl_noise_log_likelihood(gwl_analysis *a, double *out);
+
+/* Time marginalisation (base.py:183-195, 325-330, 794-820, 1027-1035).
+ * The geocent_time prior must be Uniform(t_min, t_max); jitter != 0 shifts
+ * the time grid by each point's GWL_P_TIME_JITTER.  Requires the analysis
+ * grid to have an even number of FFT points (n_bins - 1). */
+int gwl_set_time_marginalization(gwl_analysis *a, int enable, int jitter, double t_min, double t_max);
+
+/* Phase marginalisation (base.py:202-205, 786-792): ln I0(|<d|h>|) - <h|h>/2. */
+int gwl_set_phase_marginalization(gwl_analysis *a, int enable);
+
+/* Distance marginalisation (base.py:207-223, 775-784, 879-934): the caller
+ * passes the interpolating bicubic B-spline of the lookup table that
+ * BoundedRectBivariateSpline builds (core/utils/calculus.py:221-262), as
+ * knots tx[nx], ty[ny] and coefficients c[(nx-4)*(ny-4)] (row major over x),
+ * its bounding box, and the reference distance.  Outside the box the
+ * result is -inf. */
+int gwl_set_distance_marginalization(gwl_analysis *a, int enable, const double *tx, int32_t nx,
+                                     const double *ty, int32_t ny, const double *c,
+                                     const double bbox[4], double reference_distance);
+
+/* log_likelihood_ratio for B points.
+ *   params: device pointer to a [GWL_NPARAM][B] float64 block (slot-major)
+ *   out:    device pointer to B float64 results
+ *   stream: cudaStream_t (NULL = legacy default stream)
+ * Asynchronous on `stream`.  Work space is allocated on the first call for
+ * a given B and reused. */
+int gwl_eval_device(gwl_analysis *a, const double *params, int64_t B, int32_t precision,
+                    double *out, void *stream);
+
+/* Same, with host parameter and result buffers: copies the parameter block
+ * in, evaluates and copies the results out, then synchronises. */
+int gwl_eval_host(gwl_analysis *a, const double *params, int64_t B, int32_t precision, double *out);
+
+/* Per-point inner products for B points (device pointers): d_inner_h
+ * (interleaved complex, summed over detectors) and optimal_snr_squared,
+ * i.e. the _CalculatedSNRs totals of base.py:109-148 before marginalisation. */
+int gwl_inner_products_device(gwl_analysis *a, const double *params, int64_t B, int32_t precision,
+                              double *d_inner_h, double *h_inner_h, void *stream);
+
+/* Source polarisations {plus, cross} of one parameter point on a frequency
+ * grid (host in, host out, float64): source.py:1153-1209 for the
+ * sine-Gaussian; the TaylorF2 model for GWL_MODEL_TAYLORF2.  `params` is one
+ * [GWL_NPARAM] vector.  plus / cross are [2*n] interleaved complex. */
+int gwl_source_polarizations(int32_t model, const double *frequency, int64_t n, const double *params,
+                             double minimum_frequency, double *plus, double *cross);
+
+/* Detector response of given polarisations (interferometer.py:303-368 with
+ * identity calibration), host in / host out, float64. */
+int gwl_detector_response(const gwl_detector *det, const double *frequency, int64_t n,
+                          const double *plus, const double *cross, const double *params,
+                          double *response);
+
+/* The distance-marginalisation lookup table of base.py:994-1018 (host in /
+ * host out, float64, built on the GPU): for the n-point distance grid with
+ * prior density `prior`, reference distance `ref_dist` and the reference
+ * axes of base.py:899-914 (n_dh <d|h> values, n_hh <h|h> values),
+ *   table[i][j] = logsumexp_k(dh'_jk - hh_i s_k^2 / 2, b = prior_k dd) - log_norm,
+ * s_k = ref_dist / d_k, dh'_jk = dh_j s_k (or ln I0(|dh_j s_k|) with phase
+ * marginalisation).  `table` is [n_hh][n_dh] row major. */
+int gwl_distance_lookup_table(const double *distance, const double *prior, int32_t n, double ref_dist,
+                              const double *dh_axis, int32_t n_dh, const double *hh_axis, int32_t n_hh,
+                              int phase_marginalization, double *table);
+
+/* Evaluate host+device float64 helpers on the host (ln I0 of x, or the
+ * bicubic spline): a test hook that needs no GPU.  what = 0: out[i] =
+ * ln_i0(x[i]); what = 1: out[i] = spline(x[i], y[i]) with the knots and
+ * coefficients passed as in gwl_set_distance_marginalization. */
+int gwl_host_math(int what, const double *x, const double *y, int64_t n, const double *tx, int32_t nx,
+                  const double *ty, int32_t ny, const double *c, const double bbox[4], double *out);
+
+/* Measurement hooks: with profiling enabled, each evaluation records CUDA
+ * events on its stream around its dominant kernel (the fused likelihood or
+ * time-marginalisation kernel); gwl_profile_last_kernel_ms waits for the
+ * last one and returns its duration in milliseconds. */
+int gwl_set_profiling(gwl_analysis *a, int enable);
+int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
+
+/* Description of the last error on this thread ("" if none). */
+const char *gwl_last_error(void);
+
+/* Library version string. */
+const char *gwl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GWLNL_H */

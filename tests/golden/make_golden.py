@@ -1,0 +1,184 @@
+"""Generate the golden fixtures in this directory (and the packaged detector
+noise-curve tables) by running the reference bilby, imported in place from
+its source tree, on the seeded workloads of ``bilby_gb300.workloads``.
+
+Run from the repository root, where the reference tree is available:
+
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py --quick    # skip the marginalised cases
+
+Outputs
+-------
+``bilby_gb300/noise_curves.npz``
+    The two bundled sensitivity curves the workloads use
+    (bilby/gw/detector/noise_curves/aLIGO_O4_high_asd.txt and AdV_psd.txt),
+    as float64 (frequency, value) arrays.
+``tests/golden/known_answer.json``
+    The reference's own known answer for H1, 4 s at 2048 Hz, seed 500
+    (test/gw/likelihood_test.py:195-201), recomputed by the reference here.
+``tests/golden/<workload>.npz``
+    Prior draws and the reference's ``log_likelihood_ratio`` for each draw,
+    the reference's ``noise_log_likelihood``, and a checksum of the strain it
+    generated, so a test can check that the oracle regenerates the same data.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_harness  # noqa: E402
+from oracle.taylorf2 import taylorf2_aligned  # noqa: E402
+from bilby_gb300.workloads import WORKLOADS, DISTANCE_PRIOR, draw_points, point  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def export_noise_curves():
+    out = {}
+    for stem in ("aLIGO_O4_high_asd", "AdV_psd"):
+        tab = np.genfromtxt(ref_harness.asd_file_path(stem + ".txt")).T
+        out[stem + "_frequency"] = tab[0].astype(np.float64)
+        out[stem + "_value"] = tab[1].astype(np.float64)
+    np.savez_compressed(os.path.join(ROOT, "bilby_gb300", "noise_curves.npz"), **out)
+
+
+def build_reference(bilby, w, source):
+    bilby.core.utils.random.seed(w.seed)
+    ifos = bilby.gw.detector.InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(
+        sampling_frequency=w.sampling_frequency, duration=w.duration, start_time=w.start_time)
+    wfg = bilby.gw.waveform_generator.WaveformGenerator(
+        duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+        frequency_domain_source_model=source,
+        waveform_arguments=dict(minimum_frequency=w.minimum_frequency) if w.model == "taylorf2" else {})
+    # InterferometerList.inject_signal without its signal-duration check, which
+    # needs lalsimulation (interferometer.py:370-410); the injection itself is
+    # interferometer.py:493-510.
+    pols = wfg.frequency_domain_strain(dict(w.injection))
+    for ifo in ifos:
+        ifo.inject_signal_from_waveform_polarizations(parameters=dict(w.injection), injection_polarizations=pols)
+    return ifos, wfg
+
+
+def strain_checksum(ifos):
+    return np.array([[np.sum(np.abs(ifo.strain_data.frequency_domain_strain) ** 2) * 1e42,
+                      np.sum(ifo.strain_data.frequency_domain_strain.real) * 1e21]
+                     for ifo in ifos])
+
+
+def make_priors(bilby, w, time=False, phase=False, distance=False):
+    priors = bilby.core.prior.PriorDict()
+    tc = w.injection["geocent_time"]
+    if time:
+        priors["geocent_time"] = bilby.core.prior.Uniform(tc - 0.1, tc + 0.1, name="geocent_time")
+    if phase:
+        priors["phase"] = bilby.core.prior.Uniform(0, 2 * np.pi, name="phase", boundary="periodic")
+    if distance:
+        priors["luminosity_distance"] = bilby.core.prior.PowerLaw(
+            DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"], DISTANCE_PRIOR["maximum"],
+            name="luminosity_distance")
+    return priors
+
+
+def run_plain(bilby, name, n_fixed, n_random):
+    w = WORKLOADS[name]
+    source = bilby.gw.source.sinegaussian if w.model == "sinegaussian" else taylorf2_aligned
+    ifos, wfg = build_reference(bilby, w, source)
+    like = bilby.gw.likelihood.GravitationalWaveTransient(interferometers=ifos, waveform_generator=wfg)
+    rng = np.random.default_rng(w.draw_seed)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    n = n_fixed + n_random
+    t0 = time.perf_counter()
+    lnl = np.array([like.log_likelihood_ratio(point(params, i)) for i in range(n)])
+    dt = (time.perf_counter() - t0) / n
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), lnl=lnl,
+                        noise_lnl=float(like.noise_log_likelihood()),
+                        checksum=strain_checksum(ifos), **{"p_" + k: v for k, v in params.items()})
+    print(f"{name}: {n} points, {dt * 1e3:.2f} ms/eval in the reference, noise lnL {like.noise_log_likelihood()}")
+
+
+MARG_COMBOS = ["t", "p", "d", "tp", "td", "pd", "tpd"]
+
+
+def run_marginalised(bilby, name, n_points):
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in MARG_COMBOS:
+        ifos, wfg = build_reference(bilby, w, taylorf2_aligned)
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, t, p, d)
+        like = bilby.gw.likelihood.GravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors,
+            time_marginalization=t, phase_marginalization=p, distance_marginalization=d)
+        t0 = time.perf_counter()
+        vals = []
+        for i in range(n_points):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            if not t:
+                q.pop("time_jitter")
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name}[{combo}]: {(time.perf_counter() - t0) / n_points * 1e3:.2f} ms/eval")
+        if combo == "tpd":
+            out["noise_lnl"] = float(like.noise_log_likelihood())
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
+def known_answer(bilby):
+    """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
+    there needs IMRPhenomPv2 from lalsimulation)."""
+    bilby.core.utils.random.seed(500)
+    ifos = bilby.gw.detector.InterferometerList(["H1"])
+    ifos.set_strain_data_from_power_spectral_densities(sampling_frequency=2048.0, duration=4.0)
+    wfg = bilby.gw.waveform_generator.WaveformGenerator(
+        duration=4.0, sampling_frequency=2048.0, frequency_domain_source_model=bilby.gw.source.sinegaussian)
+    like = bilby.gw.likelihood.GravitationalWaveTransient(interferometers=ifos, waveform_generator=wfg)
+    nll = float(like.noise_log_likelihood())
+    with open(os.path.join(HERE, "known_answer.json"), "w") as f:
+        json.dump({"H1_seed500_4s_2048Hz_noise_log_likelihood": nll,
+                   "reference_test_value": -4014.1787704539474}, f, indent=1)
+    print("known answer", nll)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true")
+    args = ap.parse_args()
+    bilby = ref_harness.import_bilby()
+    export_noise_curves()
+    known_answer(bilby)
+    run_plain(bilby, "sg_4s", 32, 32)
+    run_plain(bilby, "tf2_128s", 4, 4)
+    if not args.quick:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)  # the reference caches its distance table in the working directory
+            try:
+                run_marginalised(bilby, "tf2_marg_8s_2k", 8)
+            finally:
+                os.chdir(cwd)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,141 @@
+"""Marginalised likelihoods on the GPU against the reference's own values
+(tests/golden/tf2_marg_8s_2k.npz, generated by the reference with the oracle's
+TaylorF2 as its source model) and against brute-force integrals of the
+non-marginalised likelihood (the pattern of the reference's
+test/gw/likelihood/marginalization_test.py:383-430).
+
+Tolerances: float64 kernels |dlnL| <= 1e-8 * max(1, |lnL|); mixed precision
+|dlnL| <= 1e-3.
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import golden
+from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, point
+
+pytestmark = pytest.mark.gpu
+
+COMBOS = ["t", "p", "d", "tp", "td", "pd", "tpd"]
+
+
+def make_likelihood(w, combo, precision, table_path):
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.prior import PowerLaw, Uniform
+    from bilby_gb300.source import taylorf2_aligned
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+    tc = w.injection["geocent_time"]
+    priors = {}
+    if "t" in combo:
+        priors["geocent_time"] = Uniform(tc - 0.1, tc + 0.1)
+    if "p" in combo:
+        priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
+    if "d" in combo:
+        priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
+                                                 DISTANCE_PRIOR["maximum"])
+    like = GravitationalWaveTransient(ifos, wfg, priors=priors, time_marginalization="t" in combo,
+                                      phase_marginalization="p" in combo, distance_marginalization="d" in combo,
+                                      distance_marginalization_lookup_table=str(table_path), precision=precision)
+    return like, priors
+
+
+def golden_points(w, priors, combo):
+    z = golden(w.name)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        if "t" not in combo:
+            q.pop("time_jitter")
+        pts.append(q)
+    return pts, z["lnl_" + combo]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("combo", COMBOS)
+def test_marginalized_vs_reference_golden(gpu, tmp_path, combo, precision):
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    like, priors = make_likelihood(w, combo, precision, tmp_path / "table.npz")
+    pts, ref = golden_points(w, priors, combo)
+    single = np.array([like.log_likelihood_ratio(q) for q in pts])
+    batch = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    assert np.array_equal(single, batch)
+    if precision == "fp64":
+        tol = 1e-8 * np.maximum(1.0, np.abs(ref))
+        assert np.all(np.abs(single - ref) <= tol), (combo, single - ref)
+    else:
+        assert np.max(np.abs(single - ref)) <= 1e-3, (combo, single - ref)
+
+
+def test_priors_mutated_like_the_reference(gpu, tmp_path):
+    """base.py:183-223: marginalised parameters are fixed in the caller's dict."""
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    like, priors = make_likelihood(w, "tpd", "fp64", tmp_path / "table.npz")
+    assert priors["geocent_time"] == w.start_time
+    assert priors["phase"] == 0.0
+    assert isinstance(priors["luminosity_distance"], float)
+    assert "time_jitter" in priors
+    assert like.marginalized_parameters == ["geocent_time", "phase", "luminosity_distance"]
+    # the cached table is reused by a second likelihood with the same prior
+    like2, _ = make_likelihood(w, "tpd", "fp64", tmp_path / "table.npz")
+    assert np.array_equal(like2._dist_margd_loglikelihood_array, like._dist_margd_loglikelihood_array)
+
+
+def test_distance_table_matches_the_reference_construction(gpu):
+    """base.py:994-1018 restated row by row for a subset of rows."""
+    from scipy.special import logsumexp
+    from bilby_gb300 import _capi
+    from bilby_gb300.likelihood import d_inner_h_ref_axis, optimal_snr_squared_ref_axis
+    from bilby_gb300.prior import PowerLaw
+    prior = PowerLaw(2.0, 100.0, 5000.0)
+    dist = np.linspace(prior.minimum, prior.maximum, 10000)
+    parr = np.array([prior.prob(d) for d in dist])
+    ref_dist = prior.rescale(0.5)
+    for phase in (False, True):
+        table = _capi.distance_lookup_table(dist, parr, ref_dist, phase)
+        scaling = ref_dist / dist
+        dh = np.outer(d_inner_h_ref_axis(800, phase), scaling)
+        if phase:
+            from scipy.special import i0e
+            dh = np.log(i0e(np.abs(dh))) + np.abs(dh)
+        hh = np.outer(optimal_snr_squared_ref_axis(400), scaling ** 2)
+        dd = dist[1] - dist[0]
+        log_norm = logsumexp(0 / dist, b=parr * dd)
+        for ii in (0, 57, 199, 311, 399):
+            row = logsumexp(dh - hh[ii] / 2, b=parr * dd, axis=-1) - log_norm
+            assert np.allclose(table[ii], row, rtol=1e-12, atol=1e-9), (phase, ii)
+
+
+def test_phase_marginalization_vs_brute_force(gpu, tmp_path):
+    """ln of the phase-averaged likelihood equals the marginalised value."""
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    plain, _ = make_likelihood(w, "", "fp64", tmp_path / "t0.npz")
+    marg, _ = make_likelihood(w, "p", "fp64", tmp_path / "t1.npz")
+    z = golden(w.name)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    params.pop("time_jitter")
+    # the injection itself, where the likelihood is large
+    params = {k: np.r_[v, w.injection[k]] for k, v in params.items()}
+    phases = np.linspace(0, 2 * np.pi, 1001)[:-1]
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        batch = {k: np.full(len(phases), v) for k, v in q.items()}
+        batch["phase"] = phases
+        lnl = plain.log_likelihood_ratio_batch(batch)
+        brute = np.log(np.mean(np.exp(lnl - lnl.max()))) + lnl.max()
+        q["phase"] = 0.0
+        assert abs(marg.log_likelihood_ratio(q) - brute) < 1e-6 * max(1.0, abs(brute))
