@@ -452,9 +452,12 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
         const uint32_t k = (uint32_t)(k0 + j);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          float ph = fixed_phase_cycles(k, xl[d], xh[d]);
+          // The sine-Gaussian's phase is linear in k, so the error of the
+          // hardware sin/cos approximation would repeat coherently from bin
+          // to bin: use the accurate sincospi on the exact fraction.
+          const float ph = fixed_phase_cycles(k, xl[d], xh[d]);
           float sn, cs;
-          __sincosf(ph * 6.283185307179586f, &sn, &cs);
+          sincospif(2.0f * ph, &sn, &cs);
           const float2 w = s_w[d][j];
           const float ere = w.x * cs - w.y * sn, eim = w.x * sn + w.y * cs;
           const float vv = s_v[d][j];

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
               const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
               const float ph = __int2float_rn((int)top) * 2.3283064365386963e-10f;
               float sn, cs;
-              __sincosf(ph * 6.283185307179586f, &sn, &cs);
+              sincospif(2.0f * ph, &sn, &cs);  // linear phase: avoid coherent approximation error
               const float2 w = a.w[d][k];
               const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
               // (C hp - i E hx) conj(e)

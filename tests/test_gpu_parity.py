@@ -4,7 +4,10 @@ data, through the C ABI.
 
 Tolerances (written here, used below):
 * plain float64 kernels: |dlnL| <= 1e-9 * max(1, |Re<d|h>|, <h|h>/2);
-* mixed-precision kernels: |dlnL| <= 1e-3 against the float64 oracle.
+* mixed-precision kernels: |dlnL| <= 1e-3 against the float64 oracle; for
+  sine-Gaussian templates far louder than any signal in the data
+  (<h|h> ~ 1e5, lnL ~ -1e5) float32 terms bound the error relatively instead:
+  |dlnL| <= 1e-3 + 2e-8 * max(1, |Re<d|h>|, <h|h>/2).
 """
 import numpy as np
 import pytest
@@ -15,6 +18,8 @@ from tests.gpu_helpers import (FP64_RTOL, MIXED_ATOL, WORKLOADS, device_analysis
 from oracle import data as OD
 
 pytestmark = pytest.mark.gpu
+
+SG_MIXED_RTOL = 2e-8
 
 
 @pytest.fixture(scope="module")
@@ -67,7 +72,7 @@ def test_sine_gaussian_vs_reference_golden(sg, precision):
     if precision == "fp64":
         assert np.all(np.abs(got - ref) <= FP64_RTOL * scale), np.max(np.abs(got - ref) / scale)
     else:
-        assert np.max(np.abs(got - ref)) <= MIXED_ATOL
+        assert np.all(np.abs(got - ref) <= MIXED_ATOL + SG_MIXED_RTOL * scale), np.abs(got - ref)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -81,7 +86,9 @@ def test_sine_gaussian_many_points(sg, precision):
     if precision == "fp64":
         assert np.all(np.abs(g - ref) <= FP64_RTOL * scale), np.max(np.abs(g - ref) / scale)
     else:
-        assert np.max(np.abs(g - ref)) <= MIXED_ATOL, np.max(np.abs(g - ref))
+        assert np.all(np.abs(g - ref) <= MIXED_ATOL + SG_MIXED_RTOL * scale), np.max(np.abs(g - ref))
+        quiet = scale < 1e4
+        assert np.max(np.abs(g - ref)[quiet]) <= MIXED_ATOL
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -160,3 +167,22 @@ def test_source_polarizations_match_oracle(gpu):
     scale = np.max(np.abs(ref["plus"]))
     assert np.max(np.abs(plus - ref["plus"])) <= 1e-9 * scale
     assert np.max(np.abs(cross - ref["cross"])) <= 1e-9 * scale
+
+
+@pytest.mark.parametrize("fixture", ["tf2", "sg"])
+def test_mixed_at_the_injection(fixture, request):
+    """The loudest points (on and around the injection, where <d|h> is
+    largest) keep |dlnL| <= 1e-3 in mixed precision."""
+    w, dets, an = request.getfixturevalue(fixture)
+    keys = [k for k in w.injection]
+    rng = np.random.default_rng(4)
+    n = 16
+    params = {k: np.full(n, float(w.injection[k])) for k in keys}
+    params["geocent_time"] = params["geocent_time"] + rng.normal(0, 2e-4, n) * (np.arange(n) > 0)
+    params["psi"] = params["psi"] + rng.normal(0, 0.05, n) * (np.arange(n) > 0)
+    got = an.log_likelihood_ratio_host(params_block(params), "mixed")
+    exact = an.log_likelihood_ratio_host(params_block(params), "fp64")
+    ref, scale = oracle_plain(dets, w, params, range(0, n, 4))
+    assert ref[0] > 20.0, ref[0]  # a loud signal
+    assert np.all(np.abs(exact[::4] - ref) <= FP64_RTOL * scale)
+    assert np.max(np.abs(got - exact)) <= MIXED_ATOL, np.abs(got - exact)
