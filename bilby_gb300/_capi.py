@@ -50,6 +50,11 @@ class GwlAnalysisDesc(ctypes.Structure):
                 ("detectors", ctypes.POINTER(GwlDetector))]
 
 
+class GwlBatchItem(ctypes.Structure):
+    _fields_ = [("analysis", ctypes.c_void_p), ("params", ctypes.c_void_p), ("B", ctypes.c_int64),
+                ("out", ctypes.c_void_p)]
+
+
 # every symbol include/gwlnl.h declares, with (restype, argtypes)
 SIGNATURES = {
     "gwl_analysis_create": (ctypes.c_int, [ctypes.POINTER(GwlAnalysisDesc), ctypes.POINTER(ctypes.c_void_p)]),
@@ -78,6 +83,12 @@ SIGNATURES = {
                                      ctypes.c_int32, c_double_p, ctypes.c_int32, c_double_p, c_double_p, c_double_p]),
     "gwl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "gwl_profile_last_kernel_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "gwl_batcher_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
+    "gwl_batcher_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gwl_batcher_use_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gwl_batcher_eval": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GwlBatchItem), ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_void_p]),
+    "gwl_batcher_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "gwl_last_error": (ctypes.c_char_p, []),
     "gwl_version": (ctypes.c_char_p, []),
 }

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -55,6 +56,8 @@ struct gwl_analysis {
   double* freq = nullptr;
   float* freq_f = nullptr;
   float2* basis = nullptr;
+  float* anchors = nullptr;
+  int64_t n_anchors = 0;
   double* strain[kMaxDet] = {};
   double* inv_psd[kMaxDet] = {};
   float2* w[kMaxDet] = {};
@@ -138,6 +141,60 @@ float2 split_ff(double x) {
   return make_float2(hi, lo);
 }
 
+// n-th derivative of f^alpha
+double dpow(double f, double alpha, int n) {
+  double c = 1.0;
+  for (int i = 0; i < n; ++i) c *= (alpha - i);
+  return c * std::pow(f, alpha - n);
+}
+
+// n-th derivative of ln f
+double dlog(double f, int n) {
+  if (n == 0) return std::log(f);
+  double c = ((n - 1) % 2 == 0) ? 1.0 : -1.0;
+  for (int i = 1; i < n; ++i) c *= i;
+  return c * std::pow(f, -(double)n);
+}
+
+// Taylor coefficients in the bin index of the eight TaylorF2 phase basis
+// functions (f^-5/3, f^-1, f^-2/3, f^-1/3, ln f, f^1/3, f^1/3 ln f, f^2/3)
+// at frequency f: T[n][b] = phi_b^(n)(f) * df^n / n!.
+void basis_taylor(double f, double df, double T[kAnchorOrders][kNumBasis]) {
+  double fact = 1.0, dfn = 1.0;
+  for (int n = 0; n < kAnchorOrders; ++n) {
+    if (n > 0) {
+      fact *= n;
+      dfn *= df;
+    }
+    const double s = dfn / fact;
+    T[n][0] = dpow(f, -5.0 / 3.0, n) * s;
+    T[n][1] = dpow(f, -1.0, n) * s;
+    T[n][2] = dpow(f, -2.0 / 3.0, n) * s;
+    T[n][3] = dpow(f, -1.0 / 3.0, n) * s;
+    T[n][4] = dlog(f, n) * s;
+    T[n][5] = dpow(f, 1.0 / 3.0, n) * s;
+    double leib = 0.0, binom = 1.0;  // Leibniz rule for f^1/3 ln f
+    for (int i = 0; i <= n; ++i) {
+      if (i > 0) binom = binom * (n - i + 1) / i;
+      leib += binom * dpow(f, 1.0 / 3.0, n - i) * dlog(f, i);
+    }
+    T[n][6] = leib * s;
+    T[n][7] = dpow(f, 2.0 / 3.0, n) * s;
+  }
+}
+
+int g_sm_count = 0;
+
+int sm_count() {
+  if (g_sm_count == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm_count <= 0) g_sm_count = 152;
+  }
+  return g_sm_count;
+}
+
 LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   LaunchArgs L;
   std::memset(&L, 0, sizeof(L));
@@ -151,6 +208,13 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.k_base = a->k_base;
   L.chunk = precision == GWL_PRECISION_FP64 ? kChunkPlain : kChunkMixed;
   L.n_chunks = precision == GWL_PRECISION_FP64 ? a->n_chunks_plain : a->n_chunks_mixed;
+  L.n_groups = L.n_chunks;
+  if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) {
+    // split-K: each CTA walks a strided set of chunks;
+    // a fixed number of chunks per group, so that the summation order of a
+    // point (and so its result) is the same for every batch size
+    L.n_groups = (a->n_chunks_mixed + kChunksPerGroup - 1) / kChunksPerGroup;
+  }
   L.duration = a->duration;
   L.step = a->step;
   L.fmin = a->fmin;
@@ -168,6 +232,8 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.freq = a->freq;
   L.freq_f = a->freq_f;
   L.basis = a->basis;
+  L.anchors = a->anchors;
+  L.n_anchors = a->n_anchors;
   L.status = a->d_status;
   L.time_marg = a->time_marg;
   L.phase_marg = a->phase_marg;
@@ -249,6 +315,55 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     a->ev_pending = 1;
   }
   GWL_CUDA(launch_finalize(L, s));
+  return GWL_OK;
+}
+
+}  // namespace
+
+// Batches of several analyses in one launch sequence (a persistent kernel per
+// detector count), optionally replayed from captured CUDA graphs.
+struct gwl_batcher {
+  LaunchArgs* d_args = nullptr;
+  LaunchArgs* h_args = nullptr;
+  int cap_items = 0;
+  int64_t* d_off = nullptr;
+  int64_t* h_off = nullptr;
+  int4* d_units = nullptr;
+  int4* h_units = nullptr;
+  int64_t cap_units = 0;
+  int* d_counter = nullptr;
+  PointRec* d_rec = nullptr;
+  int64_t cap_points = 0;
+  double* d_part = nullptr;
+  size_t cap_part = 0;  // doubles
+  int* d_status = nullptr;
+  cudaEvent_t staged = nullptr;
+  bool staged_pending = false;
+  int use_graphs = 0;
+  std::map<std::vector<int64_t>, cudaGraphExec_t> graphs;
+  std::mutex mu;
+};
+
+namespace {
+
+void drop_graphs(gwl_batcher* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+template <class T>
+int grow(T** dptr, T** hptr, size_t have, size_t need) {
+  if (need <= have) return GWL_OK;
+  if (dptr) {
+    cudaFree(*dptr);
+    *dptr = nullptr;
+    GWL_CUDA(cudaMalloc(reinterpret_cast<void**>(dptr), need * sizeof(T)));
+  }
+  if (hptr) {
+    cudaFreeHost(*hptr);
+    *hptr = nullptr;
+    GWL_CUDA(cudaMallocHost(reinterpret_cast<void**>(hptr), need * sizeof(T)));
+  }
   return GWL_OK;
 }
 
@@ -366,6 +481,22 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
         for (int b = 0; b < kNumBasis; ++b) basis[(size_t)k * kNumBasis + b] = split_ff(vals[b]);
       }
       if ((rc = upload(a, &a->basis, basis))) goto fail;
+      // Taylor tables of the basis every kAnchorStep bins (f = k * df)
+      a->n_anchors = N / kAnchorStep + 2;
+      std::vector<float> anc((size_t)a->n_anchors * kAnchorFloats, 0.f);
+      for (int64_t q = 1; q < a->n_anchors; ++q) {
+        const double fa = (double)(q * kAnchorStep) * a->step;
+        double T[kAnchorOrders][kNumBasis];
+        basis_taylor(fa, a->step, T);
+        float* dst = anc.data() + (size_t)q * kAnchorFloats;
+        for (int n = 0; n < kAnchorOrders; ++n)
+          for (int b = 0; b < kNumBasis; ++b) {
+            const float2 v = split_ff(T[n][b]);
+            dst[n * kNumBasis + b] = v.x;
+            if (n < kAnchorFF) dst[kAnchorOrders * kNumBasis + n * kNumBasis + b] = v.y;
+          }
+      }
+      if ((rc = upload(a, &a->anchors, anc))) goto fail;
     }
     a->noise_lnl = 0.0;
     for (int d = 0; d < a->n_det; ++d) {
@@ -685,6 +816,213 @@ done:
   cudaFree(dcross);
   cudaFree(dr);
   return rc;
+}
+
+int gwl_batcher_create(gwl_batcher** out) {
+  if (!out) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  auto* b = new gwl_batcher();
+  cudaError_t e = cudaMalloc(&b->d_counter, 8 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    set_error(std::string("gwl_batcher_create: ") + cudaGetErrorString(e));
+    cudaFree(b->d_counter);
+    cudaFree(b->d_status);
+    delete b;
+    return GWL_ERR_CUDA;
+  }
+  *out = b;
+  return GWL_OK;
+}
+
+int gwl_batcher_destroy(gwl_batcher* b) {
+  if (!b) return GWL_OK;
+  {
+    std::lock_guard<std::mutex> g(b->mu);
+    cudaDeviceSynchronize();
+    drop_graphs(b);
+    cudaFree(b->d_args);
+    cudaFreeHost(b->h_args);
+    cudaFree(b->d_off);
+    cudaFreeHost(b->h_off);
+    cudaFree(b->d_units);
+    cudaFreeHost(b->h_units);
+    cudaFree(b->d_counter);
+    cudaFree(b->d_rec);
+    cudaFree(b->d_part);
+    cudaFree(b->d_status);
+    cudaEventDestroy(b->staged);
+  }
+  delete b;
+  return GWL_OK;
+}
+
+int gwl_batcher_use_graphs(gwl_batcher* b, int enable) {
+  if (!b) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(b->mu);
+  b->use_graphs = enable ? 1 : 0;
+  if (!enable) drop_graphs(b);
+  return GWL_OK;
+}
+
+int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int32_t precision, void* stream) {
+  if (!b || (n > 0 && !items) || n < 0) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (n == 0) return GWL_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  bool fused = precision == GWL_PRECISION_MIXED;
+  for (int q = 0; q < n; ++q) {
+    const gwl_batch_item& it = items[q];
+    if (!it.analysis || it.B < 0 || (it.B > 0 && (!it.params || !it.out))) {
+      set_error("batch item with a null analysis, params or out");
+      return GWL_ERR_ARGUMENT;
+    }
+    const gwl_analysis* a = it.analysis;
+    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->n_det > kMultiMaxDet) fused = false;
+  }
+  if (!fused) {
+    // other models / precisions / time marginalisation: one launch sequence per item
+    for (int q = 0; q < n; ++q) {
+      gwl_analysis* a = items[q].analysis;
+      std::lock_guard<std::mutex> g(a->mu);
+      const int rc = run_eval(a, items[q].params, items[q].B, precision, items[q].out, nullptr, nullptr, s);
+      if (rc) return rc;
+    }
+    return GWL_OK;
+  }
+  std::lock_guard<std::mutex> g(b->mu);
+  // sizes
+  int64_t total = 0, n_units = 0;
+  size_t part = 0;
+  std::vector<LaunchArgs> largs(n);
+  std::vector<int64_t> key;
+  key.reserve(2 * n + 1);
+  key.push_back(n);
+  int64_t units_d[kMaxDet + 2] = {0, 0, 0, 0, 0, 0};
+  for (int q = 0; q < n; ++q) {
+    gwl_analysis* a = items[q].analysis;
+    largs[q] = make_args(a, items[q].B, GWL_PRECISION_MIXED);
+    total += items[q].B;
+    part += (size_t)largs[q].n_groups * a->n_det * kPartStride * items[q].B;
+    const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
+    units_d[a->n_det] += tiles * largs[q].n_groups;
+    key.push_back(reinterpret_cast<int64_t>(a));
+    key.push_back(items[q].B);
+  }
+  for (int D = 1; D <= kMultiMaxDet; ++D) n_units += units_d[D];
+  // capacity (growing invalidates captured graphs: their pointers change)
+  if (b->staged_pending) {
+    GWL_CUDA(cudaEventSynchronize(b->staged));
+    b->staged_pending = false;
+  }
+  const bool need_grow = n > b->cap_items || n_units > b->cap_units || total > b->cap_points || part > b->cap_part;
+  if (need_grow) {
+    GWL_CUDA(cudaDeviceSynchronize());
+    drop_graphs(b);
+    int rc;
+    if ((rc = grow(&b->d_args, &b->h_args, b->cap_items, (size_t)n))) return rc;
+    if ((rc = grow(&b->d_off, &b->h_off, b->cap_items + 1, (size_t)n + 1))) return rc;
+    b->cap_items = std::max(b->cap_items, (int)n);
+    if ((rc = grow(&b->d_units, &b->h_units, b->cap_units, (size_t)n_units))) return rc;
+    b->cap_units = std::max(b->cap_units, n_units);
+    if ((rc = grow<PointRec>(&b->d_rec, nullptr, b->cap_points, (size_t)total))) return rc;
+    b->cap_points = std::max(b->cap_points, total);
+    if ((rc = grow<double>(&b->d_part, nullptr, b->cap_part, part))) return rc;
+    b->cap_part = std::max(b->cap_part, part);
+  }
+  // per-item launch arguments, point offsets and work units (grouped by detector count)
+  int64_t off = 0;
+  size_t poff = 0;
+  int64_t ucur[kMaxDet + 2];
+  int64_t ubeg[kMaxDet + 2];
+  ubeg[0] = ubeg[1] = 0;
+  for (int D = 1; D <= kMultiMaxDet; ++D) ubeg[D + 1] = ubeg[D] + units_d[D];
+  for (int D = 0; D <= kMultiMaxDet + 1; ++D) ucur[D] = ubeg[D];
+  for (int q = 0; q < n; ++q) {
+    gwl_analysis* a = items[q].analysis;
+    LaunchArgs& L = largs[q];
+    L.params = items[q].params;
+    L.out = items[q].out;
+    L.rec = b->d_rec + off;
+    L.part = b->d_part + poff;
+    L.status = b->d_status;
+    b->h_args[q] = L;
+    b->h_off[q] = off;
+    const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
+    for (int64_t t = 0; t < tiles; ++t)
+      for (int64_t gg = 0; gg < L.n_groups; ++gg) b->h_units[ucur[a->n_det]++] = make_int4(q, (int)t, (int)gg, 0);
+    off += items[q].B;
+    poff += (size_t)L.n_groups * a->n_det * kPartStride * items[q].B;
+  }
+  b->h_off[n] = off;
+  MultiArgs m;
+  m.args = b->d_args;
+  m.offsets = b->d_off;
+  m.n_items = n;
+  m.total_points = total;
+  m.units = b->d_units;
+  for (int D = 0; D <= kMultiMaxDet + 1; ++D) m.unit_begin[D] = ubeg[D];
+  m.counter = b->d_counter;
+  int ctas[kMaxDet + 2] = {0, 0, 0, 0, 0, 0};
+  for (int D = 1; D <= kMultiMaxDet; ++D)
+    if (units_d[D] > 0)
+      ctas[D] = (int)std::min<int64_t>(units_d[D], (int64_t)sm_count() * multi_tf2_ctas_per_sm(D));
+  auto enqueue = [&]() -> int {
+    GWL_CUDA(cudaMemcpyAsync(b->d_args, b->h_args, n * sizeof(LaunchArgs), cudaMemcpyHostToDevice, s));
+    GWL_CUDA(cudaMemcpyAsync(b->d_off, b->h_off, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    GWL_CUDA(cudaMemcpyAsync(b->d_units, b->h_units, n_units * sizeof(int4), cudaMemcpyHostToDevice, s));
+    GWL_CUDA(cudaMemsetAsync(b->d_counter, 0, 8 * sizeof(int), s));
+    GWL_CUDA(launch_multi(m, ctas, s));
+    return GWL_OK;
+  };
+  if (b->use_graphs && s != nullptr) {  // the legacy default stream cannot be captured
+    auto hit = b->graphs.find(key);
+    if (hit == b->graphs.end()) {
+      cudaGraph_t graph;
+      GWL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue();
+      cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      if (rc) return rc;
+      if (ce != cudaSuccess) {
+        set_error(std::string("graph capture: ") + cudaGetErrorString(ce));
+        return GWL_ERR_CUDA;
+      }
+      cudaGraphExec_t exec;
+      ce = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        set_error(std::string("graph instantiate: ") + cudaGetErrorString(ce));
+        return GWL_ERR_CUDA;
+      }
+      hit = b->graphs.emplace(key, exec).first;
+    }
+    GWL_CUDA(cudaGraphLaunch(hit->second, s));
+  } else {
+    const int rc = enqueue();
+    if (rc) return rc;
+  }
+  GWL_CUDA(cudaEventRecord(b->staged, s));
+  b->staged_pending = true;
+  return GWL_OK;
+}
+
+int gwl_batcher_status(gwl_batcher* b, int* device_status) {
+  if (!b || !device_status) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  GWL_CUDA(cudaMemcpy(device_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (*device_status) cudaMemset(b->d_status, 0, sizeof(int));
+  return GWL_OK;
 }
 
 int gwl_distance_lookup_table(const double* distance, const double* prior, int32_t n, double ref_dist,

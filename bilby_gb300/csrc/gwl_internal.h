@@ -18,7 +18,12 @@ constexpr int kChunkPlain = 256;       // bins per CTA, float64 kernels
 constexpr int kChunkMixed = 512;       // bins per CTA, mixed-precision kernels
 constexpr int kBinAlign = 16;          // chunk starts are multiples of this many bins
 constexpr int kNumBasis = 8;           // TaylorF2 phase basis functions of f
-constexpr int kPartStride = 6;         // doubles per (chunk, point, detector) partial record
+constexpr int kPartStride = 6;         // partial-sum components per (group, detector, point)
+constexpr int kAnchorStep = 8;         // bins between TaylorF2 phase anchors in the table
+constexpr int kAnchorOrders = 7;       // Taylor orders 0..6 of the phase about an anchor
+constexpr int kAnchorFF = 4;           // orders 0..3 kept in float-float
+constexpr int kAnchorFloats = 96;      // per anchor: hi[7][8], lo[4][8], padding
+constexpr int kChunksPerGroup = 4;     // chunks walked by one split-K CTA of the TaylorF2 mixed kernel
 constexpr int kDevStatusOk = 0;
 constexpr int kDevStatusTimeout = 1;
 constexpr int kDevStatusBadInput = 2;
@@ -51,6 +56,7 @@ struct LaunchArgs {
   int64_t B;
   int64_t n_bins, k_lo, k_hi, k_base;   // in-band hull [k_lo, k_hi); chunk origin k_base
   int64_t n_chunks;                     // chunks over [k_base, k_hi)
+  int64_t n_groups;                     // CTAs along the bin axis; CTA g walks chunks g, g + G, ...
   int chunk;                            // bins per chunk
   double duration, step, fmin;
   int64_t k_fmin;                       // first bin with f >= minimum_frequency
@@ -64,9 +70,11 @@ struct LaunchArgs {
   const double* hh_prefix[kMaxDet];     // [n_bins + 1] TaylorF2 <h|h> prefix sums
   double w_scale[kMaxDet], v_scale[kMaxDet];
   const float2* basis;                  // [n_pad][kNumBasis] float-float phase basis
+  const float* anchors;                 // [n_anchors][kAnchorFloats] Taylor tables of the basis
+  int64_t n_anchors;
   const double* params;                 // [GWL_NPARAM][B]
   PointRec* rec;                        // [B]
-  double* part;                         // [n_chunks][B][n_det][kPartStride]
+  double* part;                         // [n_groups][n_det][kPartStride][B] (point fastest)
   double* out;                          // [B]
   double* dh_out;                       // optional [2B] complex <d|h> totals
   double* hh_out;                       // optional [B] <h|h> totals
@@ -82,7 +90,23 @@ struct LaunchArgs {
   double* tm_work;                      // time-marginalisation work space
 };
 
+// A batch over several analyses evaluated by one persistent launch: per item
+// (one analysis and its points) a LaunchArgs; work units (item, point tile,
+// chunk group) are pulled by the persistent CTAs from an atomic counter.
+struct MultiArgs {
+  const LaunchArgs* args;   // [n_items]
+  const int64_t* offsets;   // [n_items + 1] first global point of each item
+  int n_items;
+  int64_t total_points;
+  const int4* units;        // [n_units] {item, tile, group, 0}, grouped by detector count
+  int64_t unit_begin[5];    // units of analyses with D detectors: [unit_begin[D], unit_begin[D + 1])
+  int* counter;             // [4], zeroed before the launch
+};
+
 // Kernel launchers (defined in gwl_kernels.cu / gwl_marg.cu).
+constexpr int kMultiMaxDet = 3;
+cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s);
+int multi_tf2_ctas_per_sm(int D);
 cudaError_t launch_prologue(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);

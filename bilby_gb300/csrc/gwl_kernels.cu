@@ -25,9 +25,7 @@ __device__ __forceinline__ double par(const LaunchArgs& a, int slot, int64_t i) 
 // ---------------------------------------------------------------------------
 // prologue: per-point float64 set-up (sky frame, antenna, delays, model scalars)
 // ---------------------------------------------------------------------------
-__global__ void k_prologue(LaunchArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.B) return;
+__device__ void prologue_point(const LaunchArgs& a, int64_t i) {
   PointRec r;
   memset(&r, 0, sizeof(r));
   const double ra = par(a, GWL_P_RA, i), dec = par(a, GWL_P_DEC, i), psi = par(a, GWL_P_PSI, i);
@@ -121,6 +119,12 @@ __global__ void k_prologue(LaunchArgs a) {
   a.rec[i] = r;
 }
 
+__global__ void k_prologue(LaunchArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.B) return;
+  prologue_point(a, i);
+}
+
 // ---------------------------------------------------------------------------
 // plain float64 kernels
 // ---------------------------------------------------------------------------
@@ -144,7 +148,6 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
   if (i >= a.B) return;
   const PointRec& r = a.rec[i];
-  double* out = a.part + (((int64_t)blockIdx.y * a.B + i) * D) * kPartStride;
   double dre[D], dim[D], hh[D], fp[D], fx[D], w2[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -185,9 +188,10 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
   }
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    out[d * kPartStride + 0] = dre[d];
-    out[d * kPartStride + 1] = dim[d];
-    out[d * kPartStride + 2] = hh[d];
+    double* out = a.part + (((int64_t)blockIdx.y * D + d) * kPartStride) * a.B + i;
+    out[0 * a.B] = dre[d];
+    out[1 * a.B] = dim[d];
+    out[2 * a.B] = hh[d];
   }
 }
 
@@ -211,7 +215,6 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_tf2(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
   if (i >= a.B) return;
   const PointRec& r = a.rec[i];
-  double* out = a.part + (((int64_t)blockIdx.y * a.B + i) * D) * kPartStride;
   double dre[D], dim[D], hh[D], fp[D], fx[D], w2[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -270,9 +273,10 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_tf2(LaunchArgs a) {
   }
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    out[d * kPartStride + 0] = dre[d];
-    out[d * kPartStride + 1] = dim[d];
-    out[d * kPartStride + 2] = hh[d];
+    double* out = a.part + (((int64_t)blockIdx.y * D + d) * kPartStride) * a.B + i;
+    out[0 * a.B] = dre[d];
+    out[1 * a.B] = dim[d];
+    out[2 * a.B] = hh[d];
   }
 }
 
@@ -288,92 +292,220 @@ __device__ __forceinline__ float fixed_phase_cycles(uint32_t k, uint32_t xlo, ui
 
 constexpr int kFlush = 64;  // bins summed in float32 before folding into float64
 
-// TaylorF2, mixed precision.  Shared memory per chunk: the float-float phase
-// basis (64 B/bin) and each detector's weights f^(-7/6) d / S (8 B/bin/det),
-// brought in by 1-D bulk async copies completed on one mbarrier.
+// TaylorF2, mixed precision.
+//
+// Phase: about anchor bins k_a (every J bins, J from the Taylor-remainder
+// bound below) the phase in cycles Phi(k_a + j) = sum_n A_n j^n is a degree-6
+// polynomial whose coefficients A_n = sum_b c_b T_n,b(k_a) come from the
+// per-analysis Taylor tables of the basis functions (orders 0..3 in
+// float-float).  Its forward differences are converted to 0.64 fixed point
+// (cycles modulo one) and the phase is stepped bin by bin with wrapping
+// 64-bit integer adds, which are exact: no rounding error accumulates along
+// the interval.  The detector time shift k * frac(dt df) is another exact
+// 0.64 fixed-point sequence.  Only the final sin/cos and the complex
+// multiply-accumulate with the weights w = f^(-7/6) d / S are float32.
+//
+// Work split (split-K): CTA (tile, g) holds 128 points and walks chunks
+// g, g + G, ... of 512 bins; each chunk's weights come in by 1-D bulk async
+// copies into a double-buffered shared-memory stage.  One partial sum per
+// (g, detector, point) is written, point fastest.
+
+// ff helpers for the anchor set-up (all float32 operations, error-free transforms)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl) {
+  const float s = __fadd_rn(hi, bh);
+  const float bb = __fsub_rn(s, hi);
+  float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+  e = __fadd_rn(e, __fadd_rn(lo, bl));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+__device__ __forceinline__ void ff_scale(float& hi, float& lo, float k) {
+  const float p = __fmul_rn(hi, k);
+  const float e = __fmaf_rn(hi, k, -p);
+  hi = p;
+  lo = __fmaf_rn(lo, k, e);
+}
+
+// (hi + lo) modulo one cycle as 0.64 fixed point
+__device__ __forceinline__ uint64_t to_fixed(float hi, float lo) {
+  float r = __fsub_rn(hi, rintf(hi));
+  if (r >= 0.5f) r -= 1.0f;
+  float q = __fsub_rn(lo, rintf(lo));
+  if (q >= 0.5f) q -= 1.0f;
+  const long long a = __float2ll_rn(r * 18446744073709551616.0f);
+  const long long b = __float2ll_rn(q * 18446744073709551616.0f);
+  return (uint64_t)(a + b);
+}
+
+// Largest anchor interval J (power of two, 8..256 bins) for which, at a chunk
+// starting at bin k0 with Newtonian phase magnitude N cycles there, the
+// degree-6 Taylor remainder stays below 1e-9 cycle and the float32 orders
+// 4..6 below 1e-2 * 6e-8 cycle (factor 8 of margin for the PN terms).
+// 256 keeps the fixed-point quantisation C(J,6) 2^-65 below 1e-8 cycle.
+__device__ __forceinline__ int anchor_interval(float n_cycles, float k0) {
+  int J = 256;
+  while (J > 8) {
+    const float x = (float)J / k0;
+    const float x2 = x * x, x4 = x2 * x2, x7 = x4 * x2 * x;
+    if (n_cycles * x7 <= 3.1e-11f && n_cycles * x4 <= 4.5e-4f) break;
+    J >>= 1;
+  }
+  return J;
+}
+
+// One work unit: the points of tile `tile` over the chunks g, g + G, ...
+// `it_global` counts the chunks this CTA has consumed so far (all units): it
+// selects the shared-memory stage and the mbarrier phase.
 template <int D>
-__global__ void __launch_bounds__(kPointsPerCta) k_mixed_tf2(LaunchArgs a) {
+__device__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s_w, uint64_t* bar,
+                         unsigned long long* s_kmax, int64_t& it_global) {
   constexpr int CH = kChunkMixed;
-  extern __shared__ __align__(128) unsigned char smem[];
-  float2* s_basis = reinterpret_cast<float2*>(smem);                     // [CH][8]
-  float2* s_w = reinterpret_cast<float2*>(smem + CH * kNumBasis * 8);   // [D][CH]
-  __shared__ uint64_t bar;
-  __shared__ int s_any;
-  const int64_t k0 = a.k_base + (int64_t)blockIdx.y * CH;
-  const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
+  const int64_t i = tile * kPointsPerCta + threadIdx.x;
+  const int64_t G = a.n_groups;
   const bool have = i < a.B;
   int64_t ks = 0, ke = 0;
-  int valid = 0;
+  bool valid = false;
   if (have) {
-    valid = a.rec[i].valid;
+    valid = a.rec[i].valid != 0;
     ks = a.rec[i].k_start;
     ke = a.rec[i].k_end;
   }
-  const int64_t jb = max((int64_t)0, ks - k0);
-  const int64_t je = min((int64_t)CH, ke - k0);
-  const bool work = have && valid && jb < je;
-  if (threadIdx.x == 0) s_any = 0;
+  if (threadIdx.x == 0) *s_kmax = 0ull;
   __syncthreads();
-  if (work) s_any = 1;
+  if (have && valid && ke > ks) atomicMax(s_kmax, (unsigned long long)ke);
   __syncthreads();
+  const int64_t kmax = (int64_t)*s_kmax;
+  // chunks of this group that can contribute: k0 < kmax
+  const int64_t c_end = min(a.n_chunks, (kmax - a.k_base + CH - 1) / CH);
+  const int64_t nit = c_end > g ? (c_end - g + G - 1) / G : 0;
+
+  float ch[kNumBasis + 1], cl[kNumBasis + 1];
+  uint64_t X[D];
+  float c0 = 0.f;
+  if (have && valid) {
+    const PointRec& r = a.rec[i];
+#pragma unroll
+    for (int b = 0; b <= kNumBasis; ++b) {
+      ch[b] = r.c_hi[b];
+      cl[b] = r.c_lo[b];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) X[d] = ((uint64_t)r.xfix[d][1] << 32) | r.xfix[d][0];
+    c0 = fabsf(r.c_hi[0]);
+  }
   double tre[D], tim[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) tre[d] = tim[d] = 0.0;
-  if (s_any) {
-    if (threadIdx.x == 0) {
-      mbar_init(&bar, 1);
-      mbar_fence_init();
+
+  const uint32_t stage_bytes = D * CH * 8;
+  const int64_t it0 = it_global;
+  if (nit > 0 && threadIdx.x == 0) {
+    const int s0 = (int)(it0 & 1);
+    const int64_t k0 = a.k_base + g * CH;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[s0], stage_bytes);
+#pragma unroll
+    for (int d = 0; d < D; ++d) bulk_g2s(s_w + s0 * D * CH + d * CH, a.w[d] + k0, CH * 8, &bar[s0]);
+  }
+  int64_t done = 0;
+  for (int64_t it = 0; it < nit; ++it) {
+    const int64_t itg = it0 + it;
+    const int s = (int)(itg & 1);
+    const int64_t c = g + it * G;
+    if (it + 1 < nit && threadIdx.x == 0) {
+      // the other stage was released by the barrier at the end of the previous iteration
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const int64_t k1 = a.k_base + (c + G) * CH;
+      float2* dst = s_w + (s ^ 1) * D * CH;
+      mbar_expect_tx(&bar[s ^ 1], stage_bytes);
+#pragma unroll
+      for (int d = 0; d < D; ++d) bulk_g2s(dst + d * CH, a.w[d] + k1, CH * 8, &bar[s ^ 1]);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const uint32_t bytes_basis = CH * kNumBasis * 8;
-      const uint32_t bytes_w = CH * 8;
-      mbar_expect_tx(&bar, bytes_basis + D * bytes_w);
-      bulk_g2s(s_basis, a.basis + k0 * kNumBasis, bytes_basis, &bar);
+    const bool arrived = mbar_wait_bounded(&bar[s], (uint32_t)((itg >> 1) & 1), a.status, kWaitLimit);
+    done = it + 1;
+    if (!__syncthreads_and(arrived)) break;
+    const float2* w = s_w + s * D * CH;
+    const int64_t k0 = a.k_base + c * CH;
+    if (have && valid && k0 < ke && k0 + CH > ks) {
+      // this point's own anchor interval for the chunk: the result of a
+      // point never depends on the other points of the batch
+      const int J = anchor_interval(c0 * __powf((float)k0 * (float)a.step, -5.0f / 3.0f),
+                                    (float)max(k0, (int64_t)8));
+      uint64_t D0 = 0, D1 = 0, D2 = 0, D3 = 0, D4 = 0, D5 = 0, D6 = 0;
+      uint64_t L[D];
 #pragma unroll
-      for (int d = 0; d < D; ++d) bulk_g2s(s_w + d * CH, a.w[d] + k0, bytes_w, &bar);
-    }
-    const bool arrived = mbar_wait_bounded(&bar, 0, a.status, kWaitLimit);
-    if (arrived && work) {
-      const PointRec& r = a.rec[i];
-      float ch[kNumBasis + 1], cl[kNumBasis + 1];
-#pragma unroll
-      for (int b = 0; b <= kNumBasis; ++b) {
-        ch[b] = r.c_hi[b];
-        cl[b] = r.c_lo[b];
-      }
-      uint32_t xl[D], xh[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        xl[d] = r.xfix[d][0];
-        xh[d] = r.xfix[d][1];
-      }
-      for (int64_t jf = jb; jf < je; jf += kFlush) {
-        const int jend = (int)min(je, jf + kFlush);
+      for (int d = 0; d < D; ++d) L[d] = 0;
+      const int jlast = (int)min((int64_t)CH, ke - k0);
+      for (int jf = 0; jf < jlast; jf += kFlush) {
         float are[D], aim[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
-        for (int j = (int)jf; j < jend; ++j) {
-          const float4* bp = reinterpret_cast<const float4*>(s_basis + j * kNumBasis);
-          float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+        const int jfe = min(jf + kFlush, jlast);
+        for (int j = jf; j < jfe; ++j) {
+          const int64_t k = k0 + j;
+          if ((j & (J - 1)) == 0) {
+            // Taylor coefficients of the phase about k (cycles per bin)
+            const float* an = a.anchors + (k / kAnchorStep) * kAnchorFloats;
+            float Ah[kAnchorFF], Al[kAnchorFF], Af[kAnchorOrders - kAnchorFF];
 #pragma unroll
-          for (int q = 0; q < kNumBasis / 2; ++q) {
-            const float4 v = bp[q];
-            ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
-            ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
-          }
-          const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
-          const uint32_t k = (uint32_t)(k0 + j);
+            for (int n = 0; n < kAnchorFF; ++n) {
+              float sh = n == 0 ? ch[kNumBasis] : 0.f, sl = n == 0 ? cl[kNumBasis] : 0.f;
 #pragma unroll
-          for (int d = 0; d < D; ++d) {
-            float ph = base + fixed_phase_cycles(k, xl[d], xh[d]);
-            ph -= rintf(ph);
-            float sn, cs;
-            __sincosf(ph * 6.283185307179586f, &sn, &cs);
-            const float2 w = s_w[d * CH + j];
-            are[d] = __fmaf_rn(w.x, cs, __fmaf_rn(-w.y, sn, are[d]));
-            aim[d] = __fmaf_rn(w.x, sn, __fmaf_rn(w.y, cs, aim[d]));
+              for (int b = 0; b < kNumBasis; ++b)
+                ff_mac(sh, sl, ch[b], cl[b], __ldg(an + n * kNumBasis + b),
+                       __ldg(an + kAnchorOrders * kNumBasis + n * kNumBasis + b));
+              Ah[n] = sh;
+              Al[n] = sl;
+            }
+#pragma unroll
+            for (int n = kAnchorFF; n < kAnchorOrders; ++n) {
+              float sf = 0.f;
+#pragma unroll
+              for (int b = 0; b < kNumBasis; ++b) sf = __fmaf_rn(ch[b], __ldg(an + n * kNumBasis + b), sf);
+              Af[n - kAnchorFF] = sf;
+            }
+            // forward differences Delta_m = m! sum_n S(n, m) A_n (Stirling numbers of the second kind)
+            const float A4 = Af[0], A5 = Af[1], A6 = Af[2];
+            float d1h = Ah[1], d1l = Al[1];
+            ff_add(d1h, d1l, Ah[2], Al[2]);
+            ff_add(d1h, d1l, Ah[3], Al[3]);
+            ff_add(d1h, d1l, A4 + A5 + A6, 0.f);
+            float d2h = Ah[2], d2l = Al[2];
+            ff_scale(d2h, d2l, 2.f);
+            float t3h = Ah[3], t3l = Al[3];
+            ff_scale(t3h, t3l, 6.f);
+            ff_add(d2h, d2l, t3h, t3l);
+            ff_add(d2h, d2l, 14.f * A4 + 30.f * A5 + 62.f * A6, 0.f);
+            float d3h = Ah[3], d3l = Al[3];
+            ff_scale(d3h, d3l, 6.f);
+            ff_add(d3h, d3l, 36.f * A4 + 150.f * A5 + 540.f * A6, 0.f);
+            D0 = to_fixed(Ah[0], Al[0]);
+            D1 = to_fixed(d1h, d1l);
+            D2 = to_fixed(d2h, d2l);
+            D3 = to_fixed(d3h, d3l);
+            D4 = to_fixed(24.f * A4 + 240.f * A5 + 1560.f * A6, 0.f);
+            D5 = to_fixed(120.f * A5 + 1800.f * A6, 0.f);
+            D6 = to_fixed(720.f * A6, 0.f);
+#pragma unroll
+            for (int d = 0; d < D; ++d) L[d] = (uint64_t)k * X[d];
           }
+          if (k >= ks) {
+            const uint32_t base = (uint32_t)(D0 >> 32);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const uint32_t top = base + (uint32_t)(L[d] >> 32);
+              const float ph = __int2float_rn((int)top) * 1.4629180792671596e-09f;  // 2 pi 2^-32
+              float sn, cs;
+              __sincosf(ph, &sn, &cs);
+              const float2 wv = w[d * CH + j];
+              are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
+              aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+            }
+          }
+#pragma unroll
+          for (int d = 0; d < D; ++d) L[d] += X[d];
+          D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
         }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -382,15 +514,31 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_tf2(LaunchArgs a) {
         }
       }
     }
+    __syncthreads();
   }
+  it_global = it0 + done;
   if (have) {
-    double* out = a.part + (((int64_t)blockIdx.y * a.B + i) * D) * kPartStride;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      out[d * kPartStride + 0] = tre[d];
-      out[d * kPartStride + 1] = tim[d];
+      a.part[((g * D + d) * kPartStride + 0) * a.B + i] = tre[d];
+      a.part[((g * D + d) * kPartStride + 1) * a.B + i] = tim[d];
     }
   }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kPointsPerCta) k_mixed_tf2(LaunchArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar[2];
+  __shared__ unsigned long long s_kmax;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  int64_t it_global = 0;
+  tf2_unit<D>(a, blockIdx.x, blockIdx.y, reinterpret_cast<float2*>(smem), bar, &s_kmax, it_global);
 }
 
 // Sine-Gaussian, mixed precision.  Shared memory per chunk: float32
@@ -476,11 +624,10 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
     }
   }
   if (have) {
-    double* out = a.part + (((int64_t)blockIdx.y * a.B + i) * D) * kPartStride;
 #pragma unroll
     for (int d = 0; d < D; ++d)
 #pragma unroll
-      for (int q = 0; q < 6; ++q) out[d * kPartStride + q] = t[d][q];
+      for (int q = 0; q < 6; ++q) a.part[(((int64_t)blockIdx.y * D + d) * kPartStride + q) * a.B + i] = t[d][q];
   }
 }
 
@@ -495,10 +642,10 @@ __device__ void detector_totals(const LaunchArgs& a, int64_t i, const PointRec& 
   double sdr = 0.0, sdi = 0.0, shh = 0.0;
   for (int d = 0; d < a.n_det; ++d) {
     double p[kPartStride] = {0, 0, 0, 0, 0, 0};
-    for (int64_t c = 0; c < a.n_chunks; ++c) {
-      const double* q = a.part + ((c * a.B + i) * a.n_det + d) * kPartStride;
+    for (int64_t c = 0; c < a.n_groups; ++c) {
+      const double* q = a.part + ((c * a.n_det + d) * kPartStride) * a.B + i;
       const int nq = a.precision == GWL_PRECISION_FP64 ? 3 : (a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : 2);
-      for (int t = 0; t < nq; ++t) p[t] += q[t];
+      for (int t = 0; t < nq; ++t) p[t] += q[(int64_t)t * a.B];
     }
     double dr, di, h;
     if (a.precision == GWL_PRECISION_FP64) {
@@ -542,9 +689,7 @@ __device__ double distance_marginalized(const LaunchArgs& a, double dh_re, doubl
   return bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, x, hh_ref);
 }
 
-__global__ void k_finalize(LaunchArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.B) return;
+__device__ void finalize_point(const LaunchArgs& a, int64_t i) {
   const PointRec& r = a.rec[i];
   double dr, di, hh;
   detector_totals(a, i, r, &dr, &di, &hh);
@@ -565,6 +710,12 @@ __global__ void k_finalize(LaunchArgs a) {
     lnl = dr - hh / 2;  // base.py:475
   }
   a.out[i] = lnl;
+}
+
+__global__ void k_finalize(LaunchArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.B) return;
+  finalize_point(a, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -596,13 +747,13 @@ cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s) {
 
 template <int D>
 static cudaError_t set_mixed_smem() {
-  const int bytes = kChunkMixed * kNumBasis * 8 + D * kChunkMixed * 8;
+  const int bytes = 2 * D * kChunkMixed * 8;
   return cudaFuncSetAttribute(k_mixed_tf2<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
-  dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_chunks);
   if (a.model == GWL_MODEL_SINEGAUSSIAN) {
+    dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_chunks);
     GWL_DISPATCH_D(k_mixed_sg, grid, kPointsPerCta, 0, s, a);
   } else {
     static bool configured = false;
@@ -614,7 +765,8 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
       if ((e = set_mixed_smem<4>()) != cudaSuccess) return e;
       configured = true;
     }
-    const int smem = kChunkMixed * kNumBasis * 8 + a.n_det * kChunkMixed * 8;
+    dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_groups);
+    const int smem = 2 * a.n_det * kChunkMixed * 8;
     GWL_DISPATCH_D(k_mixed_tf2, grid, kPointsPerCta, smem, s, a);
   }
   return cudaGetLastError();
@@ -623,6 +775,101 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
   const int threads = 128;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// several analyses in one launch sequence
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_item(const int64_t* off, int n, int64_t p) {
+  int lo = 0, hi = n - 1;  // largest item with off[item] <= p
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (off[mid] <= p) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_multi_prologue(MultiArgs m) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= m.total_points) return;
+  const int it = find_item(m.offsets, m.n_items, p);
+  prologue_point(m.args[it], p - m.offsets[it]);
+}
+
+__global__ void k_multi_finalize(MultiArgs m) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= m.total_points) return;
+  const int it = find_item(m.offsets, m.n_items, p);
+  finalize_point(m.args[it], p - m.offsets[it]);
+}
+
+// Persistent: each CTA pulls work units of analyses with D detectors (units
+// [unit_begin[D], unit_begin[D+1])) until none is left.  Every unit covers at
+// most kChunksPerGroup chunks, so units of short and long analyses cost about
+// the same.  One kernel per detector count keeps the register allocation of
+// the single-analysis kernel.
+template <int D>
+__global__ void __launch_bounds__(kPointsPerCta, 5) k_multi_tf2(MultiArgs m) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar[2];
+  __shared__ unsigned long long s_kmax;
+  __shared__ int64_t s_unit;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  int64_t it_global = 0;
+  float2* s_w = reinterpret_cast<float2*>(smem);
+  const int64_t ub = m.unit_begin[D], ue = m.unit_begin[D + 1];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_unit = ub + atomicAdd(m.counter + D, 1);
+    __syncthreads();
+    const int64_t u = s_unit;
+    if (u >= ue) break;
+    const int4 wu = m.units[u];
+    tf2_unit<D>(m.args[wu.x], wu.y, wu.z, s_w, bar, &s_kmax, it_global);
+  }
+}
+
+template <int D>
+static int ctas_per_sm_d() {
+  static int n = 0;
+  if (n == 0) {
+    const int smem = 2 * D * kChunkMixed * 8;
+    if (cudaFuncSetAttribute(k_multi_tf2<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_multi_tf2<D>, kPointsPerCta, smem) != cudaSuccess || n < 1)
+      n = 1;
+  }
+  return n;
+}
+
+int multi_tf2_ctas_per_sm(int D) {
+  switch (D) {
+    case 1: return ctas_per_sm_d<1>();
+    case 2: return ctas_per_sm_d<2>();
+    default: return ctas_per_sm_d<3>();
+  }
+}
+
+cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s) {
+  const int threads = 128;
+  const unsigned pblocks = (unsigned)((m.total_points + threads - 1) / threads);
+  k_multi_prologue<<<pblocks, threads, 0, s>>>(m);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  for (int D = 1; D <= kMultiMaxDet; ++D) {
+    if (ctas[D] <= 0) continue;
+    const int smem = 2 * D * kChunkMixed * 8;
+    if (D == 1) k_multi_tf2<1><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
+    if (D == 2) k_multi_tf2<2><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
+    if (D == 3) k_multi_tf2<3><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  k_multi_finalize<<<pblocks, threads, 0, s>>>(m);
   return cudaGetLastError();
 }
 

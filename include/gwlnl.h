@@ -183,6 +183,35 @@ int gwl_distance_lookup_table(const double *distance, const double *prior, int32
 int gwl_host_math(int what, const double *x, const double *y, int64_t n, const double *tx, int32_t nx,
                   const double *ty, int32_t ny, const double *c, const double bbox[4], double *out);
 
+/* ---- several analyses in one launch --------------------------------------
+ * A batcher evaluates, in one launch sequence, batches of points that belong
+ * to different analyses (configurations of uneven duration, sampling rate
+ * and detector count): a persistent kernel per detector count pulls work
+ * units (analysis, 128-point tile, group of chunks) from an atomic counter.
+ * With graphs enabled, the launch sequence of each batch shape (analyses and
+ * point counts) is captured once in a CUDA graph and replayed.  Mixed
+ * precision TaylorF2 analyses without time marginalisation take the fused
+ * path; any other item is evaluated by its own launch sequence.  A batcher
+ * holds its own work space, so one batcher serves one stream at a time.
+ * This extends base.py:419-477 to many analyses at once; it has no single
+ * counterpart in the reference, whose likelihood evaluates one point of one
+ * analysis per call. */
+typedef struct gwl_batcher gwl_batcher;
+
+typedef struct {
+  gwl_analysis *analysis;
+  const double *params;   /* device [GWL_NPARAM][B] */
+  int64_t B;
+  double *out;            /* device [B] */
+} gwl_batch_item;
+
+int gwl_batcher_create(gwl_batcher **out);
+int gwl_batcher_destroy(gwl_batcher *b);
+int gwl_batcher_use_graphs(gwl_batcher *b, int enable);
+int gwl_batcher_eval(gwl_batcher *b, const gwl_batch_item *items, int32_t n, int32_t precision, void *stream);
+/* Reads and clears the batcher's device status word (non-zero: a bounded wait gave up). */
+int gwl_batcher_status(gwl_batcher *b, int *device_status);
+
 /* Measurement hooks: with profiling enabled, each evaluation records CUDA
  * events on its stream around its dominant kernel (the fused likelihood or
  * time-marginalisation kernel); gwl_profile_last_kernel_ms waits for the
