@@ -50,43 +50,12 @@ def parse():
     ap.add_argument("--fp64-batch", type=int, default=512, help="points per launch of the float64 comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the 64-analysis uneven batch")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving run")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the serving run")
+    ap.add_argument("--n-analyses", type=int, default=64)
+    ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     return ap.parse_args()
-
-
-# ---------------------------------------------------------------------------
-# distributed plumbing (replicas: each rank evaluates its own batch)
-# ---------------------------------------------------------------------------
-def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
-
-
-class Dist:
-    def __init__(self, world):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch.distributed as td
-            td.init_process_group("nccl")
-            self.td = td
-
-    def barrier(self):
-        if self.world > 1:
-            self.td.barrier()
-
-    def max(self, x: float) -> float:
-        if self.world == 1:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.td.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------
@@ -146,6 +115,7 @@ class ClockSampler:
 # workload construction through the library's own API
 # ---------------------------------------------------------------------------
 def build_likelihood(w, precision="mixed"):
+    """A likelihood for workload ``w`` built through the library's public API."""
     from bilby_gb300 import random as grandom
     from bilby_gb300.detector import InterferometerList
     from bilby_gb300.likelihood import GravitationalWaveTransient
@@ -184,6 +154,146 @@ def algorithmic_counts(w, B):
     chunks = int(math.ceil(n_in / 512))
     bytes_launch = table + 15 * 8 * B + chunks * B * D * 2 * 8
     return bytes_launch, ops_per_pb * n_in * B
+
+
+# ---------------------------------------------------------------------------
+# uneven batching (many analyses in one launch) and serving
+# ---------------------------------------------------------------------------
+def bench_uneven(likes, ws, steps, warmup, seed=17):
+    """One batched launch over all analyses per step (CUDA graph replay); L2 flushed before each."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.batching import Batcher
+    from bilby_gb300.workloads import draw_points
+    rng = np.random.default_rng(seed)
+    stream = torch.cuda.Stream()
+    bat = Batcher(use_graphs=True)
+    blocks = [torch.from_numpy(params_block(draw_points(w, w.batch, rng))).cuda() for w in ws]
+    outs = [torch.empty(w.batch, dtype=torch.float64, device="cuda") for w in ws]
+    items = [(lk.analysis, b.data_ptr(), b.shape[1], o.data_ptr()) for lk, b, o in zip(likes, blocks, outs)]
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        bat.eval_device(items, "mixed", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bat.eval_device(items, "mixed", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    bat.check()
+    pts = sum(w.batch for w in ws)
+    pbd = sum(w.batch * (w.n_bins - int(w.minimum_frequency * w.duration)) * len(w.detectors) for w in ws)
+    bat.close()
+    return {"analyses": len(ws), "points_per_launch": pts, "value": pts * steps / (sum(ms) / 1e3),
+            "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+            "point_bin_detector_per_s": pbd * steps / (sum(ms) / 1e3),
+            "launch": "one persistent kernel per detector count, CUDA-graph replay"}
+
+
+def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
+    """Time + phase + distance marginalisation (length-L FFT per point, ln I0,
+    bicubic distance table) on the 8 s TaylorF2 workload."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.prior import PowerLaw, Uniform
+    from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, draw_points
+    w = WORKLOADS[name]
+    base = build_likelihood(w, precision="mixed")
+    tc = w.injection["geocent_time"]
+    priors = dict(geocent_time=Uniform(tc - 0.1, tc + 0.1), phase=Uniform(0, 2 * np.pi, boundary="periodic"),
+                  luminosity_distance=PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
+                                               DISTANCE_PRIOR["maximum"]))
+    import tempfile
+    t0 = time.perf_counter()
+    like = GravitationalWaveTransient(base.interferometers, base.waveform_generator, priors=priors,
+                                      time_marginalization=True, phase_marginalization=True,
+                                      distance_marginalization=True, precision="mixed",
+                                      distance_marginalization_lookup_table=os.path.join(tempfile.mkdtemp(), "t.npz"))
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(seed)
+    p = draw_points(w, w.batch, rng)
+    p["geocent_time"] = np.full(w.batch, priors["geocent_time"])
+    p["phase"] = np.zeros(w.batch)
+    p["luminosity_distance"] = np.full(w.batch, priors["luminosity_distance"])
+    block = torch.from_numpy(params_block(p)).cuda()
+    out = torch.empty(w.batch, dtype=torch.float64, device="cuda")
+    an = like.analysis
+    stream = torch.cuda.current_stream()
+    res = {}
+    for precision, B in (("mixed", w.batch), ("fp64", fp64_batch)):
+        for _ in range(warmup):
+            an.log_likelihood_ratio_device(block.data_ptr(), B, out.data_ptr(), precision, stream.cuda_stream)
+        torch.cuda.synchronize()
+        ms = []
+        n = steps if precision == "mixed" else 3
+        bl = block[:, :B].contiguous()
+        for _ in range(n):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            an.log_likelihood_ratio_device(bl.data_ptr(), B, out.data_ptr(), precision, stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        res[precision] = {"value": B * n / (sum(ms) / 1e3), "unit": "evals/s", "batch": B,
+                          "ms_per_launch": float(np.mean(ms))}
+    m = torch.empty(fp64_batch, dtype=torch.float64, device="cuda")
+    f = torch.empty(fp64_batch, dtype=torch.float64, device="cuda")
+    bl = block[:, :fp64_batch].contiguous()
+    an.log_likelihood_ratio_device(bl.data_ptr(), fp64_batch, m.data_ptr(), "mixed", stream.cuda_stream)
+    an.log_likelihood_ratio_device(bl.data_ptr(), fp64_batch, f.data_ptr(), "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    return {"workload": name, "n_bins": w.n_bins, "fft_length": w.n_bins - 1, "marginalization": "time+phase+distance",
+            "mixed": res["mixed"], "fp64": res["fp64"], "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+            "max_abs_dlnl_mixed_vs_fp64": float((m - f).abs().max().item()),
+            "setup_s_incl_distance_table": setup_s}
+
+
+def bench_serving(likes, ws, seconds, capacity, n_clients=200, seed=23):
+    """200 clients with Poisson arrivals (rate for ~80% load), batches
+    log-uniform in [64, 8192] points from the analyses above."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.serving import LikelihoodServer
+    from bilby_gb300.workloads import draw_points
+    rng = np.random.default_rng(seed)
+    srv = LikelihoodServer(hbm_budget_bytes=160e9, max_points_per_step=1 << 16, n_streams=2)
+    for q, lk in enumerate(likes):
+        srv.add_analysis(q, lk)
+    mean_b = (8192 - 64) / math.log(128)
+    rate = 0.8 * capacity / mean_b                # requests per second, all clients together
+    pool = []
+    for q in range(len(ws)):                      # pre-drawn parameter blocks per analysis
+        pool.append(params_block(draw_points(ws[q], 8192, rng)))
+    srv.start()
+    # warm-up: compile paths and allocate work space
+    for q in range(len(ws)):
+        srv.submit(q, pool[q][:, :64]).result(120)
+    srv.stats = type(srv.stats)()
+    futs = []
+    t0 = time.perf_counter()
+    t_next = t0
+    while t_next - t0 < seconds:
+        t_next += rng.exponential(1.0 / rate)
+        now = time.perf_counter()
+        if t_next > now:
+            time.sleep(t_next - now)
+        q = int(rng.integers(0, len(ws)))
+        b = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
+        off = int(rng.integers(0, 8192 - b + 1))
+        futs.append(srv.submit(q, pool[q][:, off:off + b], client=int(rng.integers(0, n_clients))))
+    for f in futs:
+        f.result(300)
+    srv.stop()
+    out = srv.stats.summary()
+    out.update({"clients": n_clients, "arrival_rate_per_s": rate, "target_load": 0.8,
+                "batch": "log-uniform [64, 8192]", "streams": 2, "hbm_budget_gb": 160})
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -286,7 +396,8 @@ def run_ours(args, rank, world, local):
     B = args.batch or w.batch
     torch.cuda.set_device(local)
     _build.build()
-    dist = Dist(world)
+    from bilby_gb300.replicas import ReplicaGroup
+    dist = ReplicaGroup(world, backend="nccl")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload, args.cpu_seconds)   # spawned before any CUDA work of this process
@@ -359,6 +470,22 @@ def run_ours(args, rank, world, local):
     e2e_total = dist.max(float(np.sum(e2e_times)))
     e2e_value = world * B * args.steps / e2e_total
 
+    # -- many analyses in one launch, then the serving loop ---------------------
+    uneven = served = None
+    if world == 1 and (not args.no_uneven or not args.no_serving):
+        from bilby_gb300.workloads import uneven_analyses
+        uws = uneven_analyses(args.n_analyses)
+        ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
+        uneven = bench_uneven(ulikes, uws, max(3, args.steps // 2), args.warmup)
+        if not args.no_serving:
+            served = bench_serving(ulikes, uws, args.serve_seconds, uneven["value"])
+        if args.no_uneven:
+            uneven = None
+
+    marg = None
+    if world == 1 and not args.no_marg:
+        marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup)
+
     # -- roofline of the dominant kernel ---------------------------------------
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
@@ -403,6 +530,12 @@ def run_ours(args, rank, world, local):
                         "peak_source": "152 SMs x 128 FP32 lanes x sampled SM clock"},
             "clocks": clk,
         }
+        if marg is not None:
+            line["marginalized"] = marg
+        if uneven is not None:
+            line["uneven"] = uneven
+        if served is not None:
+            line["served"] = served
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -410,6 +543,7 @@ def run_ours(args, rank, world, local):
 
 
 def main():
+    from bilby_gb300.replicas import dist_info
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":

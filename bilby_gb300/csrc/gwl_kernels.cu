@@ -25,7 +25,7 @@ __device__ __forceinline__ double par(const LaunchArgs& a, int slot, int64_t i) 
 // ---------------------------------------------------------------------------
 // prologue: per-point float64 set-up (sky frame, antenna, delays, model scalars)
 // ---------------------------------------------------------------------------
-__device__ void prologue_point(const LaunchArgs& a, int64_t i) {
+__device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
   PointRec r;
   memset(&r, 0, sizeof(r));
   const double ra = par(a, GWL_P_RA, i), dec = par(a, GWL_P_DEC, i), psi = par(a, GWL_P_PSI, i);
@@ -327,6 +327,11 @@ __device__ __forceinline__ void ff_scale(float& hi, float& lo, float k) {
   lo = __fmaf_rn(lo, k, e);
 }
 
+// a0 x0 + a1 x1 + a2 x2 with a fixed operation order (no compiler contraction)
+__device__ __forceinline__ float lin3(float a0, float x0, float a1, float x1, float a2, float x2) {
+  return __fmaf_rn(a2, x2, __fmaf_rn(a1, x1, __fmul_rn(a0, x0)));
+}
+
 // (hi + lo) modulo one cycle as 0.64 fixed point
 __device__ __forceinline__ uint64_t to_fixed(float hi, float lo) {
   float r = __fsub_rn(hi, rintf(hi));
@@ -358,7 +363,7 @@ __device__ __forceinline__ int anchor_interval(float n_cycles, float k0) {
 // `it_global` counts the chunks this CTA has consumed so far (all units): it
 // selects the shared-memory stage and the mbarrier phase.
 template <int D>
-__device__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s_w, uint64_t* bar,
+__device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s_w, uint64_t* bar,
                          unsigned long long* s_kmax, int64_t& it_global) {
   constexpr int CH = kChunkMixed;
   const int64_t i = tile * kPointsPerCta + threadIdx.x;
@@ -470,23 +475,23 @@ __device__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s
             float d1h = Ah[1], d1l = Al[1];
             ff_add(d1h, d1l, Ah[2], Al[2]);
             ff_add(d1h, d1l, Ah[3], Al[3]);
-            ff_add(d1h, d1l, A4 + A5 + A6, 0.f);
+            ff_add(d1h, d1l, __fadd_rn(__fadd_rn(A4, A5), A6), 0.f);
             float d2h = Ah[2], d2l = Al[2];
             ff_scale(d2h, d2l, 2.f);
             float t3h = Ah[3], t3l = Al[3];
             ff_scale(t3h, t3l, 6.f);
             ff_add(d2h, d2l, t3h, t3l);
-            ff_add(d2h, d2l, 14.f * A4 + 30.f * A5 + 62.f * A6, 0.f);
+            ff_add(d2h, d2l, lin3(14.f, A4, 30.f, A5, 62.f, A6), 0.f);
             float d3h = Ah[3], d3l = Al[3];
             ff_scale(d3h, d3l, 6.f);
-            ff_add(d3h, d3l, 36.f * A4 + 150.f * A5 + 540.f * A6, 0.f);
+            ff_add(d3h, d3l, lin3(36.f, A4, 150.f, A5, 540.f, A6), 0.f);
             D0 = to_fixed(Ah[0], Al[0]);
             D1 = to_fixed(d1h, d1l);
             D2 = to_fixed(d2h, d2l);
             D3 = to_fixed(d3h, d3l);
-            D4 = to_fixed(24.f * A4 + 240.f * A5 + 1560.f * A6, 0.f);
-            D5 = to_fixed(120.f * A5 + 1800.f * A6, 0.f);
-            D6 = to_fixed(720.f * A6, 0.f);
+            D4 = to_fixed(lin3(24.f, A4, 240.f, A5, 1560.f, A6), 0.f);
+            D5 = to_fixed(__fmaf_rn(1800.f, A6, __fmul_rn(120.f, A5)), 0.f);
+            D6 = to_fixed(__fmul_rn(720.f, A6), 0.f);
 #pragma unroll
             for (int d = 0; d < D; ++d) L[d] = (uint64_t)k * X[d];
           }
@@ -495,7 +500,7 @@ __device__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s
 #pragma unroll
             for (int d = 0; d < D; ++d) {
               const uint32_t top = base + (uint32_t)(L[d] >> 32);
-              const float ph = __int2float_rn((int)top) * 1.4629180792671596e-09f;  // 2 pi 2^-32
+              const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
               float sn, cs;
               __sincosf(ph, &sn, &cs);
               const float2 wv = w[d * CH + j];
@@ -527,7 +532,7 @@ __device__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s
 }
 
 template <int D>
-__global__ void __launch_bounds__(kPointsPerCta) k_mixed_tf2(LaunchArgs a) {
+__global__ void __launch_bounds__(kPointsPerCta, 5) k_mixed_tf2(LaunchArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar[2];
   __shared__ unsigned long long s_kmax;
@@ -689,7 +694,7 @@ __device__ double distance_marginalized(const LaunchArgs& a, double dh_re, doubl
   return bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, x, hh_ref);
 }
 
-__device__ void finalize_point(const LaunchArgs& a, int64_t i) {
+__device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i) {
   const PointRec& r = a.rec[i];
   double dr, di, hh;
   detector_totals(a, i, r, &dr, &di, &hh);

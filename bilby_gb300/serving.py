@@ -1,0 +1,387 @@
+"""Serving: one process owns the GPU and evaluates likelihood-batch requests
+from many concurrent sampler clients with continuous batching.
+
+* Analyses are registered once (data, PSD and tables stay resident) and are
+  admitted against an HBM budget; a registration that would exceed it is
+  refused with ``MemoryError``.
+* Requests (analysis, batch of points) queue up; whenever one of the
+  ``n_streams`` step slots is free the scheduler packs pending requests (FIFO,
+  up to ``max_points_per_step`` points and the remaining work-space budget)
+  into one step: one batched launch over all their analyses on that slot's
+  CUDA stream.  Requests that arrive while steps are running are admitted as
+  slots free up; up to ``n_streams`` steps are on the device at once.
+* Each request's result is bit-identical whether it ran alone or in a mix
+  (the batched kernels never mix points of different requests).
+* Latency (submission to result) is recorded per request; ``stats()``
+  reports p50 / p99 and throughput.
+
+The device work goes through a backend; :class:`GpuBackend` uses the CUDA
+batcher, and a CPU stand-in with the same interface lets the scheduling,
+admission and failure paths be tested without a GPU.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import threading
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+
+
+class AdmissionError(MemoryError):
+    """An analysis or a request does not fit in the HBM budget."""
+
+
+@dataclass
+class Request:
+    key: object
+    block: np.ndarray            # [NPARAM, B] float64
+    future: cf.Future
+    t_submit: float
+    client: object = None
+
+    @property
+    def n(self) -> int:
+        return self.block.shape[1]
+
+
+@dataclass
+class _Step:
+    slot: int
+    requests: list
+    handle: object
+    t_launch: float
+    points: int = 0
+
+
+@dataclass
+class ServerStats:
+    latencies: list = field(default_factory=list)
+    points_done: int = 0
+    steps: int = 0
+    step_points: list = field(default_factory=list)
+    t_first: float | None = None
+    t_last: float | None = None
+    failed: int = 0
+
+    def summary(self) -> dict:
+        lat = np.array(self.latencies) * 1e3
+        span = (self.t_last - self.t_first) if self.t_first is not None and self.t_last is not None else 0.0
+        return {"requests": len(self.latencies), "failed": self.failed, "points": self.points_done,
+                "steps": self.steps,
+                "mean_points_per_step": float(np.mean(self.step_points)) if self.step_points else 0.0,
+                "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                "evals_per_s": self.points_done / span if span > 0 else None}
+
+
+class GpuBackend:
+    """Device side of the server: one CUDA stream, one batcher and pinned
+    staging per step slot."""
+
+    def __init__(self, n_slots: int, precision: str = "mixed", use_graphs: bool = False):
+        import torch
+        from .batching import Batcher
+        self.torch = torch
+        self.precision = precision
+        self.streams = [torch.cuda.Stream() for _ in range(n_slots)]
+        self.batchers = [Batcher(use_graphs=use_graphs) for _ in range(n_slots)]
+
+    @staticmethod
+    def resident_bytes(analysis) -> int:
+        return analysis.resident_bytes()
+
+    @staticmethod
+    def step_bytes(analysis, n_points: int) -> int:
+        """Device work space of n points of an analysis in one step."""
+        groups = max(1, -(-analysis.n_bins // 512))
+        return n_points * (8 * _capi.NPARAM + 8 + 640) + groups * analysis.n_detectors * 6 * 8 * n_points
+
+    def launch(self, slot: int, items):
+        """items: [(Analysis, host block)] -> handle; asynchronous."""
+        torch = self.torch
+        stream = self.streams[slot]
+        with torch.cuda.stream(stream):
+            dev, host_in, host_out = [], [], []
+            for an, block in items:
+                h = torch.from_numpy(block).pin_memory()
+                host_in.append(h)
+                d = h.to("cuda", non_blocking=True)
+                dev.append((an, d))
+            outs = self.batchers[slot].eval_tensors(dev, self.precision, stream)
+            for o in outs:
+                ho = torch.empty(o.shape, dtype=o.dtype, pin_memory=True)
+                ho.copy_(o, non_blocking=True)
+                host_out.append(ho)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return (ev, host_out, (dev, host_in, outs), None, slot)
+
+    @staticmethod
+    def ready(handle) -> bool:
+        return handle[0].query()
+
+    def results(self, handle):
+        ev, host_out, _, _, slot = handle
+        ev.synchronize()
+        self.batchers[slot].check()
+        return [h.numpy().copy() for h in host_out]
+
+
+class LikelihoodServer:
+    def __init__(self, hbm_budget_bytes: float = 160e9, max_points_per_step: int = 1 << 16, n_streams: int = 2,
+                 backend=None, precision: str = "mixed", use_graphs: bool = False, poll_s: float = 5e-5):
+        self.budget = float(hbm_budget_bytes)
+        self.max_points = int(max_points_per_step)
+        self.n_streams = int(n_streams)
+        self.backend = backend if backend is not None else GpuBackend(n_streams, precision, use_graphs)
+        self.poll_s = poll_s
+        self.analyses: dict = {}
+        self.resident = 0
+        self.pending: deque = deque()
+        self.inflight: list = []
+        self.cv = threading.Condition()
+        self.stats = ServerStats()
+        self._thread = None
+        self._running = False
+        self._busy_slots: set = set()
+
+    # -- analyses ----------------------------------------------------------
+    def add_analysis(self, key, analysis):
+        """Register a device-resident analysis (an ``Analysis`` or a likelihood
+        holding one); refused with AdmissionError beyond the HBM budget."""
+        an = getattr(analysis, "analysis", analysis)
+        size = self.backend.resident_bytes(an)
+        with self.cv:
+            if key in self.analyses:
+                raise ValueError(f"analysis {key!r} is already registered")
+            if self.resident + size + self.backend.step_bytes(an, 1) > self.budget:
+                raise AdmissionError(f"analysis {key!r} ({size / 1e9:.3f} GB) does not fit in the "
+                                     f"{self.budget / 1e9:.1f} GB budget ({self.resident / 1e9:.3f} GB resident)")
+            self.analyses[key] = an
+            self.resident += size
+
+    def remove_analysis(self, key):
+        with self.cv:
+            an = self.analyses.pop(key)
+            self.resident -= self.backend.resident_bytes(an)
+
+    # -- requests ----------------------------------------------------------
+    def submit(self, key, block, client=None) -> cf.Future:
+        """Queue a batch: ``block`` is a [NPARAM, B] float64 array (see
+        ``analysis.params_block``).  Returns a Future of the B log-likelihood ratios."""
+        fut: cf.Future = cf.Future()
+        try:
+            if key not in self.analyses:
+                raise KeyError(f"unknown analysis {key!r}")
+            block = np.ascontiguousarray(block, dtype=np.float64)
+            if block.ndim != 2 or block.shape[0] != _capi.NPARAM or block.shape[1] < 1:
+                raise ValueError(f"request block must have shape ({_capi.NPARAM}, B>=1), got {block.shape}")
+            if self.backend.step_bytes(self.analyses[key], block.shape[1]) > self.budget - self.resident:
+                raise AdmissionError("request larger than the work-space budget")
+        except Exception as e:  # malformed request: fail it alone
+            fut.set_exception(e)
+            with self.cv:
+                self.stats.failed += 1
+            return fut
+        req = Request(key, block, fut, time.perf_counter(), client)
+        with self.cv:
+            self.pending.append(req)
+            self.cv.notify()
+        return fut
+
+    def cancel_client(self, client):
+        """Drop the queued requests of a client that went away (their futures are cancelled)."""
+        with self.cv:
+            keep = deque()
+            for r in self.pending:
+                if r.client is client:
+                    r.future.cancel()
+                else:
+                    keep.append(r)
+            self.pending = keep
+
+    # -- scheduler ---------------------------------------------------------
+    def _take(self):
+        """FIFO requests for one step, within the point and work-space limits."""
+        take, pts, ws = [], 0, 0
+        room = self.budget - self.resident
+        while self.pending:
+            r = self.pending[0]
+            if r.future.cancelled():
+                self.pending.popleft()
+                continue
+            need = self.backend.step_bytes(self.analyses[r.key], r.n)
+            if take and (pts + r.n > self.max_points or ws + need > room):
+                break
+            self.pending.popleft()
+            take.append(r)
+            pts += r.n
+            ws += need
+        return take, pts
+
+    def _retire(self, step: _Step):
+        try:
+            res = self.backend.results(step.handle)
+            now = time.perf_counter()
+            for r, out in zip(step.requests, res):
+                if not r.future.cancelled():
+                    r.future.set_result(out)
+                self.stats.latencies.append(now - r.t_submit)
+            self.stats.points_done += step.points
+            self.stats.t_last = now
+        except Exception as e:
+            for r in step.requests:
+                if not r.future.done():
+                    r.future.set_exception(e)
+            self.stats.failed += len(step.requests)
+
+    def _loop(self):
+        while True:
+            with self.cv:
+                if not self._running and not self.pending and not self.inflight:
+                    return
+            # retire finished steps
+            done = [s for s in self.inflight if self.backend.ready(s.handle)]
+            for s in done:
+                self.inflight.remove(s)
+                self._busy_slots.discard(s.slot)
+                self._retire(s)
+            launched = False
+            with self.cv:
+                if len(self.inflight) < self.n_streams and self.pending:
+                    slot = min(set(range(self.n_streams)) - self._busy_slots)
+                    take, pts = self._take()
+                    if take:
+                        self._busy_slots.add(slot)
+                    else:
+                        slot = None
+                elif not self.pending and not self.inflight:
+                    if not self._running:
+                        continue
+                    self.cv.wait(timeout=0.01)
+                    continue
+                else:
+                    take = None
+            if take:
+                if self.stats.t_first is None:
+                    self.stats.t_first = min(r.t_submit for r in take)
+                try:
+                    handle = self.backend.launch(slot, [(self.analyses[r.key], r.block) for r in take])
+                    self.inflight.append(_Step(slot, take, handle, time.perf_counter(), pts))
+                    self.stats.steps += 1
+                    self.stats.step_points.append(pts)
+                    launched = True
+                except Exception as e:
+                    self._busy_slots.discard(slot)
+                    for r in take:
+                        r.future.set_exception(e)
+                    self.stats.failed += len(take)
+            if not launched and self.inflight:
+                time.sleep(self.poll_s)
+
+    def start(self):
+        self._running = True
+        self._thread = threading.Thread(target=self._loop, name="gwl-server", daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self, timeout: float = 60.0):
+        with self.cv:
+            self._running = False
+            self.cv.notify_all()
+        if self._thread is not None:
+            self._thread.join(timeout)
+            if self._thread.is_alive():
+                raise TimeoutError("server thread did not drain in time")
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+
+# ---------------------------------------------------------------------------
+# local IPC front end for sampler processes
+# ---------------------------------------------------------------------------
+def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
+    """Accept client processes on ``address`` (a Unix socket path or
+    (host, port)); each connection sends ``("eval", key, block)`` messages and
+    receives ``("ok", results)`` or ``("error", message)``.  Returns the
+    listener (close it to stop accepting)."""
+    from multiprocessing.connection import Listener
+    listener = Listener(address, authkey=authkey)
+
+    def handle(conn):
+        token = object()
+        try:
+            while True:
+                msg = conn.recv()
+                if not isinstance(msg, tuple) or len(msg) != 3 or msg[0] != "eval":
+                    conn.send(("error", "malformed message"))
+                    continue
+                fut = server.submit(msg[1], msg[2], client=token)
+                try:
+                    conn.send(("ok", fut.result()))
+                except Exception as e:
+                    conn.send(("error", f"{type(e).__name__}: {e}"))
+        except (EOFError, OSError):
+            server.cancel_client(token)   # the client went away mid-request
+        finally:
+            conn.close()
+
+    def accept():
+        while True:
+            try:
+                conn = listener.accept()
+            except OSError:
+                return
+            threading.Thread(target=handle, args=(conn,), daemon=True).start()
+
+    threading.Thread(target=accept, daemon=True).start()
+    return listener
+
+
+class ServedLikelihood:
+    """A sampler-side likelihood that sends each call to the serving process:
+    ``log_likelihood_ratio(parameters)`` evaluates one point,
+    ``log_likelihood_ratio_batch(params)`` a batch (dict of arrays)."""
+
+    def __init__(self, address, key, noise_log_likelihood: float = 0.0, authkey: bytes = b"gwlnl"):
+        self.address, self.key, self.authkey = address, key, authkey
+        self._noise = noise_log_likelihood
+        self._conn = None
+
+    def _connection(self):
+        if self._conn is None:
+            from multiprocessing.connection import Client
+            self._conn = Client(self.address, authkey=self.authkey)
+        return self._conn
+
+    def __getstate__(self):
+        st = dict(self.__dict__)
+        st["_conn"] = None
+        return st
+
+    def log_likelihood_ratio_batch(self, params) -> np.ndarray:
+        from .analysis import params_block
+        conn = self._connection()
+        conn.send(("eval", self.key, params_block(params)))
+        status, payload = conn.recv()
+        if status != "ok":
+            raise RuntimeError(payload)
+        return payload
+
+    def log_likelihood_ratio(self, parameters) -> float:
+        return float(self.log_likelihood_ratio_batch(parameters)[0])
+
+    def noise_log_likelihood(self) -> float:
+        return self._noise
+
+    def log_likelihood(self, parameters) -> float:
+        return self.log_likelihood_ratio(parameters) + self._noise

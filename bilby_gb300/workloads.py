@@ -42,6 +42,7 @@ class Workload:
     distance_marginalization: bool = False
     minimum_frequency: float = 20.0
     start_time: float = START_TIME
+    mass_range: tuple = (10.0, 40.0)   # component masses (Msun) of the TaylorF2 prior draws
 
     @property
     def n_bins(self) -> int:
@@ -57,7 +58,7 @@ WORKLOADS = {
     "tf2_128s": Workload(
         "tf2_128s", "taylorf2", ("H1", "L1", "V1"), 4096.0, 128.0, seed=3, draw_seed=3, batch=4096,
         injection=dict(mass_1=1.5, mass_2=1.3, chi_1=0.02, chi_2=-0.01, luminosity_distance=100.0,
-                       theta_jn=0.4, phase=1.3, geocent_time=START_TIME + 124.0, **_SKY)),
+                       theta_jn=0.4, phase=1.3, geocent_time=START_TIME + 124.0, **_SKY), mass_range=(1.0, 2.0)),
     "tf2_marg_8s": Workload(
         "tf2_marg_8s", "taylorf2", ("H1", "L1"), 4096.0, 8.0, seed=4, draw_seed=4, batch=8192,
         injection=dict(mass_1=30.0, mass_2=25.0, chi_1=0.02, chi_2=-0.01, luminosity_distance=800.0,
@@ -84,7 +85,7 @@ def draw_points(w: Workload, n: int, rng=None, fixed_extrinsic: bool = False) ->
         out["Q"] = rng.uniform(3, 30, n)
         out["frequency"] = rng.uniform(50, 500, n)
     else:
-        lo, hi = (1.0, 2.0) if w.name == "tf2_128s" else (10.0, 40.0)
+        lo, hi = w.mass_range
         m1 = rng.uniform(lo, hi, n)
         m2 = rng.uniform(lo, hi, n)
         out["mass_1"] = np.maximum(m1, m2)
@@ -113,3 +114,28 @@ def draw_points(w: Workload, n: int, rng=None, fixed_extrinsic: bool = False) ->
 def point(params: dict, i: int) -> dict:
     """The ``i``-th point of a batch as a plain dict of Python floats."""
     return {k: float(v[i]) for k, v in params.items()}
+
+
+# Mixed-duration TaylorF2 analyses (uneven batching): component-mass ranges
+# whose inspirals from 20 Hz fit the segment, with the segment's injection.
+_MASS_BY_DURATION = {4: (10.0, 40.0), 8: (10.0, 40.0), 16: (5.0, 10.0), 32: (2.5, 5.0), 64: (1.5, 3.0),
+                     128: (1.0, 2.0)}
+
+
+def uneven_analyses(n: int = 64, seed: int = 5) -> list:
+    """``n`` TaylorF2 analyses: duration U{4,8,16,32,64,128} s, sampling rate
+    U{2048, 4096} Hz, 2 or 3 detectors, batch log-uniform in [256, 4096]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(n):
+        T = float(rng.choice([4, 8, 16, 32, 64, 128]))
+        fs = float(rng.choice([2048, 4096]))
+        D = int(rng.choice([2, 3]))
+        B = int(round(np.exp(rng.uniform(np.log(256), np.log(4096)))))
+        lo, hi = _MASS_BY_DURATION[int(T)]
+        m1, m2 = sorted(rng.uniform(lo, hi, 2))[::-1]
+        inj = dict(mass_1=m1, mass_2=m2, chi_1=0.01, chi_2=-0.01, luminosity_distance=float(rng.uniform(100, 400)),
+                   theta_jn=0.4, phase=1.3, geocent_time=START_TIME + T - 2.0, **_SKY)
+        out.append(Workload(f"uneven_{q}", "taylorf2", ("H1", "L1", "V1")[:D], fs, T, seed=1000 + q,
+                            draw_seed=2000 + q, batch=B, injection=inj, mass_range=(lo, hi)))
+    return out
