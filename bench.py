@@ -136,23 +136,27 @@ def build_likelihood(w, precision="mixed"):
 def algorithmic_counts(w, B):
     """Per-launch algorithmic work of the mixed kernel.
 
-    bytes: compulsory HBM traffic of one launch -- the per-bin tables read once
-    (float-float phase basis 64 B/bin for TaylorF2, 8 B/bin/detector weights),
-    the parameter block in and the partial sums out.
-    ops: FP32/INT issue slots per (point, bin) of the inner loop: 8 float-float
-    multiply-accumulates of 11 ops + 3 for the reduction, and per detector 14
-    ops (2 integer multiplies, conversion, 2 roundings, 2 SFU, 4 FMA, ...).
+    bytes: compulsory HBM traffic of one launch -- the per-bin tables read
+    once (weights 8 B/bin/detector; for TaylorF2 also the anchor Taylor tables,
+    48 B/bin), the parameter block in and the partial sums out.
+    ops: issue slots per (point, bin) of the inner loop.  TaylorF2: six
+    wrapping 64-bit adds stepping the phase (12) and per detector a 32-bit add,
+    a 64-bit add for the time shift, conversion, scaling, two SFU ops, the
+    weight load and four FMAs (12).  Sine-Gaussian: the two float-float
+    Gaussians and per detector the shift, sincospi and six accumulations.
     """
     n_in = w.n_bins - int(math.ceil(w.minimum_frequency * w.duration))
     D = len(w.detectors)
     if w.model == "taylorf2":
-        table = n_in * (64 + 8 * D)
-        ops_per_pb = 8 * 11 + 3 + 14 * D
+        table = n_in * (48 + 8 * D)
+        ops_per_pb = 12 + 12 * D
+        groups = int(math.ceil(math.ceil(n_in / 512) / 4))
+        partial = groups * B * D * 2 * 8
     else:
         table = n_in * (4 + 12 * D)
-        ops_per_pb = 12 + 16 * D
-    chunks = int(math.ceil(n_in / 512))
-    bytes_launch = table + 15 * 8 * B + chunks * B * D * 2 * 8
+        ops_per_pb = 60 + 30 * D
+        partial = int(math.ceil(n_in / 512)) * B * D * 6 * 8
+    bytes_launch = table + 15 * 8 * B + partial
     return bytes_launch, ops_per_pb * n_in * B
 
 

@@ -290,7 +290,8 @@ __device__ __forceinline__ float fixed_phase_cycles(uint32_t k, uint32_t xlo, ui
   return __int2float_rn((int)top) * 2.3283064365386963e-10f;  // 2^-32
 }
 
-constexpr int kFlush = 64;  // bins summed in float32 before folding into float64
+constexpr int kFlush = 64;  // bins summed in float32 before folding into float64 (sine-Gaussian)
+constexpr int kFold = 8;    // bins summed in float32 before folding into float-float (TaylorF2)
 
 // TaylorF2, mixed precision.
 //
@@ -327,6 +328,16 @@ __device__ __forceinline__ void ff_scale(float& hi, float& lo, float k) {
   lo = __fmaf_rn(lo, k, e);
 }
 
+// hi + lo += x with TwoSum (Knuth): the float-float accumulation of the
+// 8-bin float32 partial sums
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
 // a0 x0 + a1 x1 + a2 x2 with a fixed operation order (no compiler contraction)
 __device__ __forceinline__ float lin3(float a0, float x0, float a1, float x1, float a2, float x2) {
   return __fmaf_rn(a2, x2, __fmaf_rn(a1, x1, __fmul_rn(a0, x0)));
@@ -348,15 +359,61 @@ __device__ __forceinline__ uint64_t to_fixed(float hi, float lo) {
 // degree-6 Taylor remainder stays below 1e-9 cycle and the float32 orders
 // 4..6 below 1e-2 * 6e-8 cycle (factor 8 of margin for the PN terms).
 // 256 keeps the fixed-point quantisation C(J,6) 2^-65 below 1e-8 cycle.
+// Returns 0 when even J = 8 violates the bound (low bins of short segments,
+// where f changes by a large fraction per bin): the chunk then evaluates the
+// phase at every bin in float-float from the per-bin basis table.
 __device__ __forceinline__ int anchor_interval(float n_cycles, float k0) {
-  int J = 256;
-  while (J > 8) {
+  for (int J = 256; J >= 8; J >>= 1) {
     const float x = (float)J / k0;
     const float x2 = x * x, x4 = x2 * x2, x7 = x4 * x2 * x;
-    if (n_cycles * x7 <= 3.1e-11f && n_cycles * x4 <= 4.5e-4f) break;
-    J >>= 1;
+    if (n_cycles * x7 <= 3.1e-11f && n_cycles * x4 <= 4.5e-4f) return J;
   }
-  return J;
+  return 0;
+}
+
+// A chunk where no anchor interval meets the Taylor bound: the phase of every
+// bin in float-float from the per-bin basis table (sum_b c_b phi_b(f_k)),
+// the time shift exact in 0.64 fixed point.
+template <int D>
+__device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* w, int64_t k0, int64_t ks, int jlast,
+                                             const float* ch, const float* cl, const uint64_t* X, float* ahi,
+                                             float* alo, float* bhi, float* blo) {
+  constexpr int CH = kChunkMixed;
+  for (int jb = 0; jb < jlast; jb += kFold) {
+    float are[D], aim[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
+    const int je = min(jb + kFold, jlast);
+    for (int j = jb; j < je; ++j) {
+      const int64_t k = k0 + j;
+      if (k < ks) continue;
+      const float4* bp = reinterpret_cast<const float4*>(a.basis + k * kNumBasis);
+      float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+      for (int q = 0; q < kNumBasis / 2; ++q) {
+        const float4 v = __ldg(bp + q);
+        ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+        ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
+      }
+      const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
+      const uint32_t bu = (uint32_t)__float2int_rn(__fmul_rn(base, 4294967296.0f));
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d]) >> 32);
+        const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);
+        float sn, cs;
+        __sincosf(ph, &sn, &cs);
+        const float2 wv = w[d * CH + j];
+        are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
+        aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      two_sum_acc(ahi[d], alo[d], are[d]);
+      two_sum_acc(bhi[d], blo[d], aim[d]);
+    }
+  }
 }
 
 // One work unit: the points of tile `tile` over the chunks g, g + G, ...
@@ -442,14 +499,16 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
 #pragma unroll
       for (int d = 0; d < D; ++d) L[d] = 0;
       const int jlast = (int)min((int64_t)CH, ke - k0);
-      for (int jf = 0; jf < jlast; jf += kFlush) {
-        float are[D], aim[D];
+      // 8-bin float32 partial sums folded into float-float accumulators
+      float ahi[D], alo[D], bhi[D], blo[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
-        const int jfe = min(jf + kFlush, jlast);
-        for (int j = jf; j < jfe; ++j) {
-          const int64_t k = k0 + j;
-          if ((j & (J - 1)) == 0) {
+      for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
+      if (J == 0) {
+        direct_chunk<D>(a, w, k0, ks, jlast, ch, cl, X, ahi, alo, bhi, blo);
+      } else {
+        for (int jb = 0; jb < jlast; jb += kFold) {
+          if ((jb & (J - 1)) == 0) {
+            const int64_t k = k0 + jb;
             // Taylor coefficients of the phase about k (cycles per bin)
             const float* an = a.anchors + (k / kAnchorStep) * kAnchorFloats;
             float Ah[kAnchorFF], Al[kAnchorFF], Af[kAnchorOrders - kAnchorFF];
@@ -495,28 +554,39 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
 #pragma unroll
             for (int d = 0; d < D; ++d) L[d] = (uint64_t)k * X[d];
           }
-          if (k >= ks) {
-            const uint32_t base = (uint32_t)(D0 >> 32);
+          float are[D], aim[D];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-              const uint32_t top = base + (uint32_t)(L[d] >> 32);
-              const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
-              float sn, cs;
-              __sincosf(ph, &sn, &cs);
-              const float2 wv = w[d * CH + j];
-              are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
-              aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+          for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
+          const int je = min(jb + kFold, jlast);
+          for (int j = jb; j < je; ++j) {
+            if (k0 + j >= ks) {
+              const uint32_t base = (uint32_t)(D0 >> 32);
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                const uint32_t top = base + (uint32_t)(L[d] >> 32);
+                const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
+                float sn, cs;
+                __sincosf(ph, &sn, &cs);
+                const float2 wv = w[d * CH + j];
+                are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
+                aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+              }
             }
+#pragma unroll
+            for (int d = 0; d < D; ++d) L[d] += X[d];
+            D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
           }
 #pragma unroll
-          for (int d = 0; d < D; ++d) L[d] += X[d];
-          D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
+          for (int d = 0; d < D; ++d) {
+            two_sum_acc(ahi[d], alo[d], are[d]);
+            two_sum_acc(bhi[d], blo[d], aim[d]);
+          }
         }
+      }
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          tre[d] += are[d];
-          tim[d] += aim[d];
-        }
+      for (int d = 0; d < D; ++d) {
+        tre[d] += (double)ahi[d] + (double)alo[d];
+        tim[d] += (double)bhi[d] + (double)blo[d];
       }
     }
     __syncthreads();
