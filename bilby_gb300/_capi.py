@@ -70,6 +70,8 @@ SIGNATURES = {
     "gwl_eval_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.c_void_p]),
     "gwl_eval_host": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int64, ctypes.c_int32, c_double_p]),
+    "gwl_eval_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "gwl_inner_products_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "gwl_source_polarizations": (ctypes.c_int, [ctypes.c_int32, c_double_p, ctypes.c_int64, c_double_p,

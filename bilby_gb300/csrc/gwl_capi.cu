@@ -320,6 +320,25 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
 
 }  // namespace
 
+namespace gwl {
+
+// Launch arguments of a mixed-precision TaylorF2 evaluation of B points for an
+// entry point that supplies its own work space; also the bytes it needs for
+// the per-point records and the partial sums.  Allocates nothing.
+int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg) {
+    set_error("the allocation-free entry point serves mixed-precision TaylorF2 analyses without time "
+              "marginalisation");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  *L = make_args(a, B, GWL_PRECISION_MIXED);
+  *rec_bytes = (size_t)B * sizeof(PointRec);
+  *part_bytes = (size_t)L->n_groups * a->n_det * kPartStride * (size_t)B * sizeof(double);
+  return GWL_OK;
+}
+
+}  // namespace gwl
+
 // Batches of several analyses in one launch sequence (a persistent kernel per
 // detector count), optionally replayed from captured CUDA graphs.
 struct gwl_batcher {

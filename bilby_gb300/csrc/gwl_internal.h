@@ -123,5 +123,6 @@ cudaError_t launch_distance_table(const double* dh_axis, int n_dh, const double*
                                   double* lni0_work, int phase, double log_norm, double* table);
 
 void set_error(const std::string& msg);
+int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes);
 
 }  // namespace gwl

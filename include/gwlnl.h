@@ -212,6 +212,21 @@ int gwl_batcher_eval(gwl_batcher *b, const gwl_batch_item *items, int32_t n, int
 /* Reads and clears the batcher's device status word (non-zero: a bounded wait gave up). */
 int gwl_batcher_status(gwl_batcher *b, int *device_status);
 
+/* log_likelihood_ratio for B points without allocating device memory, for
+ * callers that cannot let a library call cudaMalloc (an application that
+ * reserves the GPU's memory for its own pool, or a latency-critical loop
+ * that must not pay cudaMalloc's device-wide synchronisation).  It has no
+ * counterpart in the reference.  Mixed-precision TaylorF2 analyses without
+ * time marginalisation only (GWL_ERR_UNSUPPORTED otherwise).  params / out
+ * are device pointers as for gwl_eval_device; asynchronous on `stream`; the
+ * device status word is not read back.  The work space is a static 32 MiB
+ * device buffer shared by all calls: B is limited to what fits (about 1,800
+ * points for 128 s at 4096 Hz with 3 detectors, about 40,000 for 8 s at
+ * 2048 Hz with 2 detectors); larger B returns GWL_ERR_ARGUMENT.  The first
+ * call on a device looks up the buffer's address -- make it before any
+ * stream capture.  Calls that overlap on the GPU race on the buffer. */
+int gwl_eval_device_noalloc(gwl_analysis *a, const double *params, int64_t B, double *out, void *stream);
+
 /* Measurement hooks: with profiling enabled, each evaluation records CUDA
  * events on its stream around its dominant kernel (the fused likelihood or
  * time-marginalisation kernel); gwl_profile_last_kernel_ms waits for the
