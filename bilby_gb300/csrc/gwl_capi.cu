@@ -70,6 +70,9 @@ struct gwl_analysis {
   double* tx = nullptr;
   double* ty = nullptr;
   double* tc = nullptr;
+  float* tx_f = nullptr;
+  float* ty_f = nullptr;
+  float* tc_f = nullptr;
   int nx = 0, ny = 0;
   double bbox[4] = {0, 0, 0, 0};
   double ref_dist = 0;
@@ -80,6 +83,8 @@ struct gwl_analysis {
   PointRec* d_rec = nullptr;
   double* d_part = nullptr;
   size_t part_bytes = 0;
+  int32_t* d_order = nullptr;       // [ws_B] point ordering of the mixed TaylorF2 kernel
+  int32_t* d_order_hist = nullptr;  // [2 * kOrderMaxKeys]
   double* d_tm = nullptr;
   size_t tm_bytes = 0;
   double* h_params = nullptr;  // pinned staging for gwl_eval_host
@@ -125,12 +130,15 @@ void free_workspace(gwl_analysis* a) {
   cudaFree(a->d_out);
   cudaFree(a->d_rec);
   cudaFree(a->d_part);
+  cudaFree(a->d_order);
+  cudaFree(a->d_order_hist);
   cudaFree(a->d_tm);
   cudaFreeHost(a->h_params);
   cudaFreeHost(a->h_out);
   a->h_params = a->h_out = nullptr;
   a->d_params = a->d_out = a->d_part = a->d_tm = nullptr;
   a->d_rec = nullptr;
+  a->d_order = a->d_order_hist = nullptr;
   a->ws_B = 0;
   a->part_bytes = a->tm_bytes = 0;
 }
@@ -201,6 +209,8 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.model = a->model;
   L.n_det = a->n_det;
   L.precision = precision;
+  // real-part partials suffice unless |<d|h>| (phase marginalisation) is needed
+  L.cplx = (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) ? (a->phase_marg || a->time_marg) : 1;
   L.B = B;
   L.n_bins = a->n_bins;
   L.k_lo = a->k_lo;
@@ -247,6 +257,9 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.tx = a->tx;
   L.ty = a->ty;
   L.tc = a->tc;
+  L.tx_f = a->tx_f;
+  L.ty_f = a->ty_f;
+  L.tc_f = a->tc_f;
   L.nx = a->nx;
   L.ny = a->ny;
   for (int q = 0; q < 4; ++q) L.bbox[q] = a->bbox[q];
@@ -267,6 +280,8 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
   if ((rc = dev_alloc(a, &a->d_out, (size_t)B, false))) return rc;
   if ((rc = dev_alloc(a, &a->d_rec, (size_t)B, false))) return rc;
   if ((rc = dev_alloc(a, &a->d_part, part / sizeof(double), false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_order, (size_t)B, false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_order_hist, (size_t)2 * kOrderMaxKeys, false))) return rc;
   if (tm) {
     if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_tm), tm, false))) return rc;
   }
@@ -295,7 +310,17 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.dh_out = d_dh;
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
+  if (d_dh) L.cplx = 1;  // complex <d|h> requested
+  const bool ordered = precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2 && !(a->time_marg && d_out);
+  if (ordered) {
+    // group the points by band end (see LaunchArgs::order)
+    L.order = a->d_order;
+    L.order_hist = a->d_order_hist;
+    order_layout(L.n_chunks, &L.order_keys, &L.order_shift);
+    GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * 2 * L.order_keys, s));
+  }
   GWL_CUDA(launch_prologue(L, s));
+  if (ordered) GWL_CUDA(launch_order(L, s));
   if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
   if (a->time_marg && d_out) {
     GWL_CUDA(launch_time_marginalized(L, s));
@@ -355,6 +380,9 @@ struct gwl_batcher {
   int64_t cap_points = 0;
   double* d_part = nullptr;
   size_t cap_part = 0;  // doubles
+  int32_t* d_order = nullptr;  // [cap_points]
+  int32_t* d_hist = nullptr;   // [cap_hist] per item 2 * order_keys
+  size_t cap_hist = 0;
   int* d_status = nullptr;
   cudaEvent_t staged = nullptr;
   bool staged_pending = false;
@@ -695,6 +723,10 @@ int gwl_set_distance_marginalization(gwl_analysis* a, int enable, const double* 
   if ((rc = upload(a, &a->tx, vx))) return rc;
   if ((rc = upload(a, &a->ty, vy))) return rc;
   if ((rc = upload(a, &a->tc, vc))) return rc;
+  std::vector<float> fx(vx.begin(), vx.end()), fy(vy.begin(), vy.end()), fc(vc.begin(), vc.end());
+  if ((rc = upload(a, &a->tx_f, fx))) return rc;
+  if ((rc = upload(a, &a->ty_f, fy))) return rc;
+  if ((rc = upload(a, &a->tc_f, fc))) return rc;
   a->nx = nx;
   a->ny = ny;
   for (int q = 0; q < 4; ++q) a->bbox[q] = bbox[q];
@@ -873,6 +905,8 @@ int gwl_batcher_destroy(gwl_batcher* b) {
     cudaFree(b->d_counter);
     cudaFree(b->d_rec);
     cudaFree(b->d_part);
+    cudaFree(b->d_order);
+    cudaFree(b->d_hist);
     cudaFree(b->d_status);
     cudaEventDestroy(b->staged);
   }
@@ -921,29 +955,32 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
   std::lock_guard<std::mutex> g(b->mu);
   // sizes
   int64_t total = 0, n_units = 0;
-  size_t part = 0;
+  size_t part = 0, hist = 0;
   std::vector<LaunchArgs> largs(n);
   std::vector<int64_t> key;
   key.reserve(2 * n + 1);
   key.push_back(n);
-  int64_t units_d[kMaxDet + 2] = {0, 0, 0, 0, 0, 0};
+  int64_t units_d[kMultiClasses] = {0, 0, 0, 0, 0, 0, 0, 0};  // per kernel class 2 D + cplx
   for (int q = 0; q < n; ++q) {
     gwl_analysis* a = items[q].analysis;
     largs[q] = make_args(a, items[q].B, GWL_PRECISION_MIXED);
+    order_layout(largs[q].n_chunks, &largs[q].order_keys, &largs[q].order_shift);
+    hist += 2 * (size_t)largs[q].order_keys;
     total += items[q].B;
     part += (size_t)largs[q].n_groups * a->n_det * kPartStride * items[q].B;
     const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
-    units_d[a->n_det] += tiles * largs[q].n_groups;
+    units_d[2 * a->n_det + largs[q].cplx] += tiles * largs[q].n_groups;
     key.push_back(reinterpret_cast<int64_t>(a));
     key.push_back(items[q].B);
   }
-  for (int D = 1; D <= kMultiMaxDet; ++D) n_units += units_d[D];
+  for (int c = 0; c < kMultiClasses; ++c) n_units += units_d[c];
   // capacity (growing invalidates captured graphs: their pointers change)
   if (b->staged_pending) {
     GWL_CUDA(cudaEventSynchronize(b->staged));
     b->staged_pending = false;
   }
-  const bool need_grow = n > b->cap_items || n_units > b->cap_units || total > b->cap_points || part > b->cap_part;
+  const bool need_grow = n > b->cap_items || n_units > b->cap_units || total > b->cap_points || part > b->cap_part ||
+                         hist > b->cap_hist;
   if (need_grow) {
     GWL_CUDA(cudaDeviceSynchronize());
     drop_graphs(b);
@@ -954,18 +991,21 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     if ((rc = grow(&b->d_units, &b->h_units, b->cap_units, (size_t)n_units))) return rc;
     b->cap_units = std::max(b->cap_units, n_units);
     if ((rc = grow<PointRec>(&b->d_rec, nullptr, b->cap_points, (size_t)total))) return rc;
+    if ((rc = grow<int32_t>(&b->d_order, nullptr, b->cap_points, (size_t)total))) return rc;
     b->cap_points = std::max(b->cap_points, total);
+    if ((rc = grow<int32_t>(&b->d_hist, nullptr, b->cap_hist, hist))) return rc;
+    b->cap_hist = std::max(b->cap_hist, hist);
     if ((rc = grow<double>(&b->d_part, nullptr, b->cap_part, part))) return rc;
     b->cap_part = std::max(b->cap_part, part);
   }
   // per-item launch arguments, point offsets and work units (grouped by detector count)
   int64_t off = 0;
-  size_t poff = 0;
-  int64_t ucur[kMaxDet + 2];
-  int64_t ubeg[kMaxDet + 2];
-  ubeg[0] = ubeg[1] = 0;
-  for (int D = 1; D <= kMultiMaxDet; ++D) ubeg[D + 1] = ubeg[D] + units_d[D];
-  for (int D = 0; D <= kMultiMaxDet + 1; ++D) ucur[D] = ubeg[D];
+  size_t poff = 0, hoff = 0;
+  int64_t ucur[kMultiClasses + 1];
+  int64_t ubeg[kMultiClasses + 1];
+  ubeg[0] = 0;
+  for (int c = 0; c < kMultiClasses; ++c) ubeg[c + 1] = ubeg[c] + units_d[c];
+  for (int c = 0; c <= kMultiClasses; ++c) ucur[c] = ubeg[c];
   for (int q = 0; q < n; ++q) {
     gwl_analysis* a = items[q].analysis;
     LaunchArgs& L = largs[q];
@@ -973,12 +1013,16 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     L.out = items[q].out;
     L.rec = b->d_rec + off;
     L.part = b->d_part + poff;
+    L.order = b->d_order + off;
+    L.order_hist = b->d_hist + hoff;
+    hoff += 2 * (size_t)L.order_keys;
     L.status = b->d_status;
     b->h_args[q] = L;
     b->h_off[q] = off;
     const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
     for (int64_t t = 0; t < tiles; ++t)
-      for (int64_t gg = 0; gg < L.n_groups; ++gg) b->h_units[ucur[a->n_det]++] = make_int4(q, (int)t, (int)gg, 0);
+      for (int64_t gg = 0; gg < L.n_groups; ++gg)
+        b->h_units[ucur[2 * a->n_det + L.cplx]++] = make_int4(q, (int)t, (int)gg, 0);
     off += items[q].B;
     poff += (size_t)L.n_groups * a->n_det * kPartStride * items[q].B;
   }
@@ -989,17 +1033,19 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
   m.n_items = n;
   m.total_points = total;
   m.units = b->d_units;
-  for (int D = 0; D <= kMultiMaxDet + 1; ++D) m.unit_begin[D] = ubeg[D];
+  for (int c = 0; c <= kMultiClasses; ++c) m.unit_begin[c] = ubeg[c];
   m.counter = b->d_counter;
-  int ctas[kMaxDet + 2] = {0, 0, 0, 0, 0, 0};
-  for (int D = 1; D <= kMultiMaxDet; ++D)
-    if (units_d[D] > 0)
-      ctas[D] = (int)std::min<int64_t>(units_d[D], (int64_t)sm_count() * multi_tf2_ctas_per_sm(D));
+  m.ordered = 1;
+  int ctas[kMultiClasses] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 2; c < kMultiClasses; ++c)
+    if (units_d[c] > 0)
+      ctas[c] = (int)std::min<int64_t>(units_d[c], (int64_t)sm_count() * multi_tf2_ctas_per_sm(c));
   auto enqueue = [&]() -> int {
     GWL_CUDA(cudaMemcpyAsync(b->d_args, b->h_args, n * sizeof(LaunchArgs), cudaMemcpyHostToDevice, s));
     GWL_CUDA(cudaMemcpyAsync(b->d_off, b->h_off, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     GWL_CUDA(cudaMemcpyAsync(b->d_units, b->h_units, n_units * sizeof(int4), cudaMemcpyHostToDevice, s));
     GWL_CUDA(cudaMemsetAsync(b->d_counter, 0, 8 * sizeof(int), s));
+    GWL_CUDA(cudaMemsetAsync(b->d_hist, 0, hoff * sizeof(int32_t), s));
     GWL_CUDA(launch_multi(m, ctas, s));
     return GWL_OK;
   };

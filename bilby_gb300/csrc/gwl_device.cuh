@@ -54,17 +54,24 @@ __device__ __forceinline__ double pymod(double x, double y) {
   return r;
 }
 
+// Sines and cosines of the sky frame of one point (shared by its detectors).
+struct SkyTrig {
+  double sphi, cphi, sth, cth, sps, cps;
+};
+
+__device__ __forceinline__ SkyTrig sky_trig(double ra, double dec, double psi, double gmst_mod) {
+  SkyTrig t;
+  sincos(ra - gmst_mod, &t.sphi, &t.cphi);
+  sincos(kPi / 2 - dec, &t.sth, &t.cth);
+  sincos(psi, &t.sps, &t.cps);
+  return t;
+}
+
 // Antenna patterns F+, Fx (bilby/gw/geometry.py:118-186 + 261-279) and the
 // geocentre-to-detector delay (geometry.py:282-343) for one detector.
-__device__ __forceinline__ void antenna_and_delay(const double* tensor, const double* vertex, double ra,
-                                                  double dec, double psi, double gmst_mod, double* fplus,
-                                                  double* fcross, double* delay) {
-  const double phi = ra - gmst_mod;
-  const double theta = kPi / 2 - dec;
-  double sphi, cphi, sth, cth, sps, cps;
-  sincos(phi, &sphi, &cphi);
-  sincos(theta, &sth, &cth);
-  sincos(psi, &sps, &cps);
+__device__ __forceinline__ void antenna_and_delay(const double* tensor, const double* vertex, const SkyTrig& t,
+                                                  double* fplus, double* fcross, double* delay) {
+  const double sphi = t.sphi, cphi = t.cphi, sth = t.sth, cth = t.cth, sps = t.sps, cps = t.cps;
   const double u[3] = {cphi * cth, cth * sphi, -sth};
   const double v[3] = {-sphi, cphi, 0.0};
   double m[3], n[3];
@@ -87,6 +94,12 @@ __device__ __forceinline__ void antenna_and_delay(const double* tensor, const do
   *fcross = fx;
   const double om[3] = {sth * cphi, sth * sphi, cth};
   *delay = (om[0] * (0.0 - vertex[0]) + om[1] * (0.0 - vertex[1]) + om[2] * (0.0 - vertex[2])) / kSpeedOfLight;
+}
+
+__device__ __forceinline__ void antenna_and_delay(const double* tensor, const double* vertex, double ra,
+                                                  double dec, double psi, double gmst_mod, double* fplus,
+                                                  double* fcross, double* delay) {
+  antenna_and_delay(tensor, vertex, sky_trig(ra, dec, psi, gmst_mod), fplus, fcross, delay);
 }
 
 // TaylorF2 phase coefficients a_k, l_k of

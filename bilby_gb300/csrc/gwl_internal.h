@@ -24,6 +24,7 @@ constexpr int kAnchorOrders = 7;       // Taylor orders 0..6 of the phase about 
 constexpr int kAnchorFF = 4;           // orders 0..3 kept in float-float
 constexpr int kAnchorFloats = 96;      // per anchor: hi[7][8], lo[4][8], padding
 constexpr int kChunksPerGroup = 4;     // chunks walked by one split-K CTA of the TaylorF2 mixed kernel
+constexpr int kOrderMaxKeys = 4096;    // buckets of the point ordering by band end
 constexpr int kDevStatusOk = 0;
 constexpr int kDevStatusTimeout = 1;
 constexpr int kDevStatusBadInput = 2;
@@ -33,6 +34,8 @@ constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier befor
 struct PointRec {
   double fp[kMaxDet], fx[kMaxDet], dt[kMaxDet];  // antenna patterns; (t_geo - t_start) + delay
   uint32_t xfix[kMaxDet][2];                     // frac(dt * df) as 0.64 fixed point {lo, hi}
+  uint32_t qfix[kMaxDet][2];                     // TaylorF2 real-part kernel: arg(conj(Q_d)) / 2 pi, 0.64 fixed
+  double qabs[kMaxDet];                          // |Q_d|, Q_d = Fp (1 + cos^2 i) / 2 - i Fx cos i
   double amp;          // TaylorF2 amplitude prefactor A0 | sine-Gaussian plus factor
   double amp2;         // sine-Gaussian cross factor
   double sg_f0, sg_a;  // sine-Gaussian centre frequency, pi^2 tau^2
@@ -53,6 +56,7 @@ struct DetGeom {
 // Everything a kernel needs, passed by value.
 struct LaunchArgs {
   int model, n_det, precision;
+  int cplx;                             // TaylorF2 mixed: 1 = complex <d|h> partials, 0 = real part only
   int64_t B;
   int64_t n_bins, k_lo, k_hi, k_base;   // in-band hull [k_lo, k_hi); chunk origin k_base
   int64_t n_chunks;                     // chunks over [k_base, k_hi)
@@ -79,11 +83,19 @@ struct LaunchArgs {
   double* dh_out;                       // optional [2B] complex <d|h> totals
   double* hh_out;                       // optional [B] <h|h> totals
   int* status;                          // device status word
+  // optional point ordering (TaylorF2 mixed): thread slot s of the bin-walking
+  // kernel evaluates point order[s]; points are grouped by the chunk that
+  // holds their band end, longest first, so that the 128 points of a CTA stop
+  // at nearly the same bin.  nullptr: slot s evaluates point s.
+  int32_t* order;                       // [B]
+  int32_t* order_hist;                  // [2 * order_keys]: counts (then bases), cursors; zeroed before use
+  int order_keys, order_shift;
   // marginalisation
   int time_marg, phase_marg, dist_marg, jitter;
   double t_min, t_max, delta_tc, start_time0;
   int64_t n_fft;                        // time-marginalisation FFT length (n_bins - 1)
   const double* tx; const double* ty; const double* tc;  // distance spline
+  const float* tx_f; const float* ty_f; const float* tc_f; // float32 copy (mixed precision)
   int nx, ny;
   double bbox[4];
   double ref_dist;
@@ -98,19 +110,23 @@ struct MultiArgs {
   const int64_t* offsets;   // [n_items + 1] first global point of each item
   int n_items;
   int64_t total_points;
-  const int4* units;        // [n_units] {item, tile, group, 0}, grouped by detector count
-  int64_t unit_begin[5];    // units of analyses with D detectors: [unit_begin[D], unit_begin[D + 1])
-  int* counter;             // [4], zeroed before the launch
+  const int4* units;        // [n_units] {item, tile, group, 0}, grouped by kernel class
+  int64_t unit_begin[9];    // units of class q = 2 D + cplx: [unit_begin[q], unit_begin[q + 1])
+  int* counter;             // [8], zeroed before the launch
+  int ordered;              // items carry a point ordering (LaunchArgs::order)
 };
 
 // Kernel launchers (defined in gwl_kernels.cu / gwl_marg.cu).
 constexpr int kMultiMaxDet = 3;
+constexpr int kMultiClasses = 2 * (kMultiMaxDet + 1);  // kernel class q = 2 * detectors + cplx
 cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s);
-int multi_tf2_ctas_per_sm(int D);
+int multi_tf2_ctas_per_sm(int q);
 cudaError_t launch_prologue(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
+void order_layout(int64_t n_chunks, int* keys, int* shift);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,

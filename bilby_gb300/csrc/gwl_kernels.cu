@@ -23,6 +23,16 @@ __device__ __forceinline__ double par(const LaunchArgs& a, int slot, int64_t i) 
 }
 
 // ---------------------------------------------------------------------------
+// point ordering: bucket of a point = the chunk that holds its band end
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int order_key(const LaunchArgs& a, const PointRec& r) {
+  if (!r.valid || r.k_end <= r.k_start) return 0;
+  int64_t c = (r.k_end - a.k_base + a.chunk - 1) / a.chunk;
+  c = c < 0 ? 0 : (c > a.n_chunks ? a.n_chunks : c);
+  return (int)(c >> a.order_shift);
+}
+
+// ---------------------------------------------------------------------------
 // prologue: per-point float64 set-up (sky frame, antenna, delays, model scalars)
 // ---------------------------------------------------------------------------
 __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
@@ -35,9 +45,10 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
   tgeo = tgeo + r.jitter;
   const double gmst = pymod(gmst_radians(tgeo), kTwoPi);
   bool ok = isfinite(ra) && isfinite(dec) && isfinite(psi) && isfinite(tgeo);
+  const SkyTrig sky = sky_trig(ra, dec, psi, gmst);
   for (int d = 0; d < a.n_det; ++d) {
     double fp, fx, delay;
-    antenna_and_delay(a.det[d].tensor, a.det[d].vertex, ra, dec, psi, gmst, &fp, &fx, &delay);
+    antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky, &fp, &fx, &delay);
     r.fp[d] = fp;
     r.fx[d] = fx;
     // interferometer.py:355-358: subtract the two GPS times first, then add the delay.
@@ -76,25 +87,50 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
     r.m_sec = m * kMtsunSI;
     r.eta = m1 * m2 / (m * m);
     r.f_isco = 1.0 / (6.0 * sqrt(6.0) * kPi * r.m_sec);
-    const double mc_sec = pow(r.eta, 0.6) * m * kMtsunSI;
     r.dist = dl;
-    r.amp = sqrt(5.0 / 24.0) * pow(kPi, -2.0 / 3.0) * pow(mc_sec, 5.0 / 6.0) * kSpeedOfLight / (dl * 1e6 * kPcSI);
+    // Mc^(5/6) = eta^(1/2) M^(5/6) and M^(5/6) = M (cbrt(pi) / u)^(1/2) with u = (pi M)^(1/3)
+    const double u = cbrt(kPi * r.m_sec);
+    const double mc56 = sqrt(r.eta) * r.m_sec * sqrt(1.4645918875615231 / u);
+    // sqrt(5/24) pi^(-2/3)
+    r.amp = 0.45643546458763845 * 0.46619407703541166 * mc56 * kSpeedOfLight / (dl * 1e6 * kPcSI);
     r.cos_i = cos(theta_jn);
     r.phase = phase;
+    // Re <d|h>_d = |Q_d| Re sum w e^{i (phase_k + alpha_d)}, alpha_d = arg(conj(Q_d)): the real-part
+    // kernel carries alpha_d as a constant phase offset of detector d
+    for (int d = 0; d < a.n_det; ++d) {
+      const double qr = r.fp[d] * (1.0 + r.cos_i * r.cos_i) / 2.0, qi = -r.fx[d] * r.cos_i;
+      r.qabs[d] = hypot(qr, qi);
+      uint64_t u = 0;
+      if (!a.cplx) {
+        const double x = atan2(-qi, qr) / kTwoPi;
+        double scaled = ldexp(x - floor(x), 64);
+        if (!(scaled < 18446744073709551616.0)) scaled = 0.0;
+        u = (uint64_t)scaled;
+      }
+      r.qfix[d][0] = (uint32_t)(u & 0xffffffffull);
+      r.qfix[d][1] = (uint32_t)(u >> 32);
+    }
     taylorf2_coefficients(m1, m2, chi1, chi2, r.a, r.l);
     ok = ok && m1 > 0 && m2 > 0 && dl > 0 && isfinite(r.amp) && isfinite(phase) && isfinite(chi1) &&
          isfinite(chi2);
-    // band [k_start, k_end): f >= minimum_frequency and f < f_isco
-    int64_t lo = 0, hi = a.n_bins;  // first k with freq[k] >= f_isco
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) / 2;
-      if (a.freq[mid] >= r.f_isco) hi = mid; else lo = mid + 1;
+    // band [k_start, k_end): f >= minimum_frequency and f < f_isco; k_end is
+    // the first k with freq[k] >= f_isco: guessed from the uniform grid and
+    // corrected against the frequency array (binary search if that fails)
+    int64_t ke = (int64_t)fmin(fmax(ceil(r.f_isco / a.step), 0.0), (double)a.n_bins);
+    for (int q = 0; q < 4 && ke > 0 && a.freq[ke - 1] >= r.f_isco; ++q) --ke;
+    for (int q = 0; q < 4 && ke < a.n_bins && a.freq[ke] < r.f_isco; ++q) ++ke;
+    if ((ke > 0 && a.freq[ke - 1] >= r.f_isco) || (ke < a.n_bins && a.freq[ke] < r.f_isco)) {
+      int64_t lo = 0, hi = a.n_bins;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (a.freq[mid] >= r.f_isco) hi = mid; else lo = mid + 1;
+      }
+      ke = lo;
     }
-    r.k_end = lo;
+    r.k_end = ke;
     r.k_start = a.k_fmin;
     // Psi / (2 pi) = sum_b c_b phi_b(f) + c_const with v = u f^(1/3), u = (pi M)^(1/3)
     const double P = 3.0 / (128.0 * r.eta) / kTwoPi;
-    const double u = cbrt(kPi * r.m_sec);
     const double lnu = log(u);
     double c[kNumBasis];
     c[0] = P * r.a[0] / (u * u * u * u * u);   // f^(-5/3)
@@ -117,12 +153,63 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
   }
   r.valid = ok ? 1 : 0;
   a.rec[i] = r;
+  if (a.order_hist) atomicAdd(&a.order_hist[order_key(a, r)], 1);
 }
 
 __global__ void k_prologue(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.B) return;
   prologue_point(a, i);
+}
+
+// Counts per bucket -> first slot of each bucket, buckets in descending order
+// (longest bands first).  One CTA of kOrderThreads threads per analysis.
+constexpr int kOrderThreads = 256;
+
+__device__ void order_scan(const LaunchArgs& a) {
+  __shared__ int s_part[kOrderThreads];
+  const int n = a.order_keys, t = threadIdx.x;
+  const int per = (n + kOrderThreads - 1) / kOrderThreads;
+  int32_t* h = a.order_hist;
+  int local = 0;
+  for (int q = 0; q < per; ++q) {
+    const int p = t * per + q;
+    if (p < n) local += h[n - 1 - p];
+  }
+  s_part[t] = local;
+  __syncthreads();
+  for (int off = 1; off < kOrderThreads; off <<= 1) {
+    const int v = t >= off ? s_part[t - off] : 0;
+    __syncthreads();
+    s_part[t] += v;
+    __syncthreads();
+  }
+  int run = s_part[t] - local;
+  for (int q = 0; q < per; ++q) {
+    const int p = t * per + q;
+    if (p < n) {
+      const int key = n - 1 - p;
+      const int c = h[key];
+      h[key] = run;
+      run += c;
+    }
+  }
+}
+
+// Slot of point i within its bucket (any order inside a bucket: the result of
+// a point does not depend on the slot it is evaluated in).
+__device__ __forceinline__ void order_scatter(const LaunchArgs& a, int64_t i) {
+  const int key = order_key(a, a.rec[i]);
+  const int pos = a.order_hist[key] + atomicAdd(&a.order_hist[a.order_keys + key], 1);
+  if (pos >= 0 && pos < a.B) a.order[pos] = (int32_t)i;
+  else atomicExch(a.status, kDevStatusBadInput);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_scan(LaunchArgs a) { order_scan(a); }
+
+__global__ void k_order_scatter(LaunchArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.B) order_scatter(a, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -371,13 +458,31 @@ __device__ __forceinline__ int anchor_interval(float n_cycles, float k0) {
   return 0;
 }
 
+// One bin of the anchored phase recurrence: detector d's phase (top 32 bits
+// of the 0.64 fixed-point cycle count) is base + lh[d] (lh[0] = 0), then the
+// weighted e^{+i phase} accumulation.  w points at the bin's weight of
+// detector 0; detector d's weight is CH entries further per detector.
+template <int D, bool CPLX>
+__device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const float2* w, float* are, float* aim) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const uint32_t top = d == 0 ? base : base + lh[d];
+    const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
+    float sn, cs;
+    __sincosf(ph, &sn, &cs);
+    const float2 wv = w[d * kChunkMixed];
+    are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
+    if (CPLX) aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+  }
+}
+
 // A chunk where no anchor interval meets the Taylor bound: the phase of every
 // bin in float-float from the per-bin basis table (sum_b c_b phi_b(f_k)),
 // the time shift exact in 0.64 fixed point.
-template <int D>
+template <int D, bool CPLX>
 __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* w, int64_t k0, int64_t ks, int jlast,
-                                             const float* ch, const float* cl, const uint64_t* X, float* ahi,
-                                             float* alo, float* bhi, float* blo) {
+                                             const float* ch, const float* cl, const uint64_t* X, const uint64_t* Q,
+                                             float* ahi, float* alo, float* bhi, float* blo) {
   constexpr int CH = kChunkMixed;
   for (int jb = 0; jb < jlast; jb += kFold) {
     float are[D], aim[D];
@@ -399,19 +504,19 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* 
       const uint32_t bu = (uint32_t)__float2int_rn(__fmul_rn(base, 4294967296.0f));
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d]) >> 32);
+        const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d] + Q[d]) >> 32);
         const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);
         float sn, cs;
         __sincosf(ph, &sn, &cs);
         const float2 wv = w[d * CH + j];
         are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
-        aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+        if (CPLX) aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
       }
     }
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       two_sum_acc(ahi[d], alo[d], are[d]);
-      two_sum_acc(bhi[d], blo[d], aim[d]);
+      if (CPLX) two_sum_acc(bhi[d], blo[d], aim[d]);
     }
   }
 }
@@ -419,13 +524,14 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* 
 // One work unit: the points of tile `tile` over the chunks g, g + G, ...
 // `it_global` counts the chunks this CTA has consumed so far (all units): it
 // selects the shared-memory stage and the mbarrier phase.
-template <int D>
+template <int D, bool CPLX>
 __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s_w, uint64_t* bar,
                          unsigned long long* s_kmax, int64_t& it_global) {
   constexpr int CH = kChunkMixed;
-  const int64_t i = tile * kPointsPerCta + threadIdx.x;
+  const int64_t slot = tile * kPointsPerCta + threadIdx.x;
+  const int64_t i = slot < a.B && a.order ? (int64_t)a.order[slot] : slot;
   const int64_t G = a.n_groups;
-  const bool have = i < a.B;
+  const bool have = slot < a.B && i >= 0 && i < a.B;
   int64_t ks = 0, ke = 0;
   bool valid = false;
   if (have) {
@@ -445,6 +551,11 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
   float ch[kNumBasis + 1], cl[kNumBasis + 1];
   uint64_t X[D];
   float c0 = 0.f;
+  // constant phase offset of detector d (real-part kernel), read when needed
+  const auto qoff = [&](int d) -> uint64_t {
+    if (CPLX) return 0;
+    return ((uint64_t)a.rec[i].qfix[d][1] << 32) | a.rec[i].qfix[d][0];
+  };
   if (have && valid) {
     const PointRec& r = a.rec[i];
 #pragma unroll
@@ -495,20 +606,34 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
       const int J = anchor_interval(c0 * __powf((float)k0 * (float)a.step, -5.0f / 3.0f),
                                     (float)max(k0, (int64_t)8));
       uint64_t D0 = 0, D1 = 0, D2 = 0, D3 = 0, D4 = 0, D5 = 0, D6 = 0;
-      uint64_t L[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) L[d] = 0;
       const int jlast = (int)min((int64_t)CH, ke - k0);
       // 8-bin float32 partial sums folded into float-float accumulators
       float ahi[D], alo[D], bhi[D], blo[D];
 #pragma unroll
       for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
       if (J == 0) {
-        direct_chunk<D>(a, w, k0, ks, jlast, ch, cl, X, ahi, alo, bhi, blo);
+        uint64_t Q[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) Q[d] = qoff(d);
+        direct_chunk<D, CPLX>(a, w, k0, ks, jlast, ch, cl, X, Q, ahi, alo, bhi, blo);
       } else {
+        // detector 0's time shift rides in the phase recurrence (a linear
+        // term: D0 += k X0, D1 += X0); detector d > 0 adds its shift relative
+        // to detector 0, R_d = X_d - X_0, whose top 32 bits are taken exactly
+        // at the start of every 8-bin block and stepped in 32 bits inside it
+        // (error at most 4.5 * 2^-32 cycle)
+        const uint64_t X0 = X[0];
+        uint64_t R[D], L64[D];
+        uint32_t r32[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          R[d] = X[d] - X0;
+          r32[d] = (uint32_t)((R[d] + 0x80000000ull) >> 32);
+          L64[d] = 0;
+        }
         for (int jb = 0; jb < jlast; jb += kFold) {
+          const int64_t k = k0 + jb;
           if ((jb & (J - 1)) == 0) {
-            const int64_t k = k0 + jb;
             // Taylor coefficients of the phase about k (cycles per bin)
             const float* an = a.anchors + (k / kAnchorStep) * kAnchorFloats;
             float Ah[kAnchorFF], Al[kAnchorFF], Af[kAnchorOrders - kAnchorFF];
@@ -544,49 +669,54 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
             float d3h = Ah[3], d3l = Al[3];
             ff_scale(d3h, d3l, 6.f);
             ff_add(d3h, d3l, lin3(36.f, A4, 150.f, A5, 540.f, A6), 0.f);
-            D0 = to_fixed(Ah[0], Al[0]);
-            D1 = to_fixed(d1h, d1l);
+            const uint64_t q0 = qoff(0);
+            D0 = to_fixed(Ah[0], Al[0]) + (uint64_t)k * X0 + q0;
+            D1 = to_fixed(d1h, d1l) + X0;
             D2 = to_fixed(d2h, d2l);
             D3 = to_fixed(d3h, d3l);
             D4 = to_fixed(lin3(24.f, A4, 240.f, A5, 1560.f, A6), 0.f);
             D5 = to_fixed(__fmaf_rn(1800.f, A6, __fmul_rn(120.f, A5)), 0.f);
             D6 = to_fixed(__fmul_rn(720.f, A6), 0.f);
 #pragma unroll
-            for (int d = 0; d < D; ++d) L[d] = (uint64_t)k * X[d];
+            for (int d = 1; d < D; ++d) L64[d] = (uint64_t)k * R[d] + (qoff(d) - q0);
           }
+          uint32_t lh[D];
+#pragma unroll
+          for (int d = 0; d < D; ++d) lh[d] = (uint32_t)(L64[d] >> 32);
           float are[D], aim[D];
 #pragma unroll
           for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
-          const int je = min(jb + kFold, jlast);
-          for (int j = jb; j < je; ++j) {
-            if (k0 + j >= ks) {
-              const uint32_t base = (uint32_t)(D0 >> 32);
+          if (jb + kFold <= jlast && k >= ks) {
+            // a whole block inside the band
 #pragma unroll
-              for (int d = 0; d < D; ++d) {
-                const uint32_t top = base + (uint32_t)(L[d] >> 32);
-                const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
-                float sn, cs;
-                __sincosf(ph, &sn, &cs);
-                const float2 wv = w[d * CH + j];
-                are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
-                aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
-              }
+            for (int j = 0; j < kFold; ++j) {
+              tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + jb + j, are, aim);
+#pragma unroll
+              for (int d = 1; d < D; ++d) lh[d] += r32[d];
+              D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
             }
+          } else {
+            const int je = min(jb + kFold, jlast);
+            for (int j = jb; j < je; ++j) {
+              if (k0 + j >= ks) tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + j, are, aim);
 #pragma unroll
-            for (int d = 0; d < D; ++d) L[d] += X[d];
-            D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
+              for (int d = 1; d < D; ++d) lh[d] += r32[d];
+              D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
+            }
           }
+#pragma unroll
+          for (int d = 1; d < D; ++d) L64[d] += R[d] * (uint64_t)kFold;
 #pragma unroll
           for (int d = 0; d < D; ++d) {
             two_sum_acc(ahi[d], alo[d], are[d]);
-            two_sum_acc(bhi[d], blo[d], aim[d]);
+            if (CPLX) two_sum_acc(bhi[d], blo[d], aim[d]);
           }
         }
       }
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         tre[d] += (double)ahi[d] + (double)alo[d];
-        tim[d] += (double)bhi[d] + (double)blo[d];
+        if (CPLX) tim[d] += (double)bhi[d] + (double)blo[d];
       }
     }
     __syncthreads();
@@ -596,12 +726,12 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       a.part[((g * D + d) * kPartStride + 0) * a.B + i] = tre[d];
-      a.part[((g * D + d) * kPartStride + 1) * a.B + i] = tim[d];
+      if (CPLX) a.part[((g * D + d) * kPartStride + 1) * a.B + i] = tim[d];
     }
   }
 }
 
-template <int D>
+template <int D, bool CPLX>
 __global__ void __launch_bounds__(kPointsPerCta, 5) k_mixed_tf2(LaunchArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar[2];
@@ -613,7 +743,7 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_mixed_tf2(LaunchArgs a) {
   }
   __syncthreads();
   int64_t it_global = 0;
-  tf2_unit<D>(a, blockIdx.x, blockIdx.y, reinterpret_cast<float2*>(smem), bar, &s_kmax, it_global);
+  tf2_unit<D, CPLX>(a, blockIdx.x, blockIdx.y, reinterpret_cast<float2*>(smem), bar, &s_kmax, it_global);
 }
 
 // Sine-Gaussian, mixed precision.  Shared memory per chunk: float32
@@ -711,17 +841,40 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double neg_huge() { return -1.7976931348623157e308; }  // nan_to_num(-inf)
 
-__device__ void detector_totals(const LaunchArgs& a, int64_t i, const PointRec& r, double* dh_re, double* dh_im,
-                                double* hh) {
+// p[t] = sum over groups c = 0, 1, ... (in that order) of the partial sums
+// of detector d; the loads of 8 (or 4) groups are issued before their adds.
+template <int NQ>
+__device__ __forceinline__ void sum_groups(const LaunchArgs& a, int64_t i, int d, int64_t G, double* p) {
+  constexpr int U = NQ <= 3 ? 8 : 4;
+  const int64_t gs = (int64_t)a.n_det * kPartStride * a.B;
+  const double* q = a.part + ((int64_t)d * kPartStride) * a.B + i;
+  int64_t c = 0;
+  for (; c + U <= G; c += U) {
+    double v[U][NQ];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int t = 0; t < NQ; ++t) v[u][t] = q[(c + u) * gs + (int64_t)t * a.B];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int t = 0; t < NQ; ++t) p[t] += v[u][t];
+  }
+  for (; c < G; ++c)
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) p[t] += q[c * gs + (int64_t)t * a.B];
+}
+
+__device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const PointRec& r, double* dh_re,
+                                double* dh_im, double* hh) {
   const double norm = 4.0 / a.duration;
   double sdr = 0.0, sdi = 0.0, shh = 0.0;
   for (int d = 0; d < a.n_det; ++d) {
     double p[kPartStride] = {0, 0, 0, 0, 0, 0};
-    for (int64_t c = 0; c < a.n_groups; ++c) {
-      const double* q = a.part + ((c * a.n_det + d) * kPartStride) * a.B + i;
-      const int nq = a.precision == GWL_PRECISION_FP64 ? 3 : (a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : 2);
-      for (int t = 0; t < nq; ++t) p[t] += q[(int64_t)t * a.B];
-    }
+    if (a.precision == GWL_PRECISION_FP64) sum_groups<3>(a, i, d, G, p);
+    else if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<6>(a, i, d, G, p);
+    else if (a.cplx) sum_groups<2>(a, i, d, G, p);
+    else sum_groups<1>(a, i, d, G, p);
     double dr, di, h;
     if (a.precision == GWL_PRECISION_FP64) {
       dr = norm * p[0];
@@ -739,9 +892,15 @@ __device__ void detector_totals(const LaunchArgs& a, int64_t i, const PointRec& 
       const double ci = r.cos_i;
       const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
       const double s = norm * a.w_scale[d] * r.amp;
-      // (qr - i qi) * (p0 + i p1)
-      dr = s * (qr * p[0] + qi * p[1]);
-      di = s * (qr * p[1] - qi * p[0]);
+      if (a.cplx) {
+        // (qr - i qi) * (p0 + i p1)
+        dr = s * (qr * p[0] + qi * p[1]);
+        di = s * (qr * p[1] - qi * p[0]);
+      } else {
+        // p0 = Re sum w e^{i (phase + alpha_d)} (see PointRec::qfix)
+        dr = s * r.qabs[d] * p[0];
+        di = 0.0;
+      }
       const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
       const double* pre = a.hh_prefix[d];
       h = norm * r.amp * r.amp * (qr * qr + qi * qi) * (pre[k1] - pre[k0]);
@@ -764,10 +923,44 @@ __device__ double distance_marginalized(const LaunchArgs& a, double dh_re, doubl
   return bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, x, hh_ref);
 }
 
-__device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i) {
+// Components of a partial-sum record: <d|h> re/im and <h|h> (float64 kernels),
+// the six sums of the sine-Gaussian mixed kernel, re/im for TaylorF2 mixed.
+__device__ __host__ __forceinline__ int part_components(const LaunchArgs& a) {
+  return a.precision == GWL_PRECISION_FP64 ? 3 : (a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : (a.cplx ? 2 : 1));
+}
+
+// One (point, detector, component) chain: the partial sums of all groups
+// added in group order (loads of 8 groups in flight) into group 0's slot.
+__device__ __forceinline__ void reduce_chain(const LaunchArgs& a, int64_t i, int d, int t) {
+  const int64_t G = a.n_groups;
+  const int64_t gs = (int64_t)a.n_det * kPartStride * a.B;
+  double* q = a.part + ((int64_t)d * kPartStride + t) * a.B + i;
+  double p = 0.0;
+  int64_t c = 0;
+  for (; c + 8 <= G; c += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = q[(c + u) * gs];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) p += v[u];
+  }
+  for (; c < G; ++c) p += q[c * gs];
+  q[0] = p;
+}
+
+__global__ void k_reduce_parts(LaunchArgs a) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nq = part_components(a);
+  if (idx >= a.B * a.n_det * nq) return;
+  const int64_t i = idx % a.B, r = idx / a.B;
+  reduce_chain(a, i, (int)(r / nq), (int)(r % nq));
+}
+
+// G: the groups still to be summed (1 after k_reduce_parts)
+__device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int64_t G) {
   const PointRec& r = a.rec[i];
   double dr, di, hh;
-  detector_totals(a, i, r, &dr, &di, &hh);
+  detector_totals(a, i, G, r, &dr, &di, &hh);
   if (a.dh_out) {
     a.dh_out[2 * i] = dr;
     a.dh_out[2 * i + 1] = di;
@@ -790,14 +983,18 @@ __device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i) {
 __global__ void k_finalize(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.B) return;
-  finalize_point(a, i);
+  finalize_point(a, i, 1);
 }
 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+// The per-point float64 steps run one warp per CTA so that a batch of a few
+// thousand points spreads over all SMs (their float64 pipes bound them).
+constexpr int kPointThreads = 32;
+
 cudaError_t launch_prologue(const LaunchArgs& a, cudaStream_t s) {
-  const int threads = 128;
+  const int threads = kPointThreads;
   k_prologue<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
   return cudaGetLastError();
 }
@@ -821,9 +1018,16 @@ cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s) {
 }
 
 template <int D>
+constexpr auto k_mixed_tf2_c = k_mixed_tf2<D, true>;
+template <int D>
+constexpr auto k_mixed_tf2_r = k_mixed_tf2<D, false>;
+
+template <int D>
 static cudaError_t set_mixed_smem() {
   const int bytes = 2 * D * kChunkMixed * 8;
-  return cudaFuncSetAttribute(k_mixed_tf2<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  const cudaError_t e = cudaFuncSetAttribute(k_mixed_tf2<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_mixed_tf2<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
@@ -842,14 +1046,41 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
     }
     dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_groups);
     const int smem = 2 * a.n_det * kChunkMixed * 8;
-    GWL_DISPATCH_D(k_mixed_tf2, grid, kPointsPerCta, smem, s, a);
+    if (a.cplx) {
+      GWL_DISPATCH_D(k_mixed_tf2_c, grid, kPointsPerCta, smem, s, a);
+    } else {
+      GWL_DISPATCH_D(k_mixed_tf2_r, grid, kPointsPerCta, smem, s, a);
+    }
   }
   return cudaGetLastError();
 }
 
+// Group sums in parallel over (point, detector, component), then the
+// per-point totals and marginalisation.
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
-  const int threads = 128;
+  const int64_t chains = a.B * a.n_det * part_components(a);
+  k_reduce_parts<<<(unsigned)((chains + 127) / 128), 128, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int threads = kPointThreads;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+void order_layout(int64_t n_chunks, int* keys, int* shift) {
+  int sh = 0;
+  while ((n_chunks >> sh) + 1 > kOrderMaxKeys) ++sh;
+  *shift = sh;
+  *keys = (int)(n_chunks >> sh) + 1;
+}
+
+// Bases of the buckets counted by the prologue, then each point's slot.
+cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s) {
+  k_order_scan<<<1, kOrderThreads, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int threads = 128;
+  k_order_scatter<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -872,20 +1103,46 @@ __global__ void k_multi_prologue(MultiArgs m) {
   prologue_point(m.args[it], p - m.offsets[it]);
 }
 
+__global__ void __launch_bounds__(kOrderThreads) k_multi_order_scan(MultiArgs m) {
+  const LaunchArgs& a = m.args[blockIdx.x];
+  if (a.order_hist) order_scan(a);
+}
+
+__global__ void k_multi_order_scatter(MultiArgs m) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= m.total_points) return;
+  const int it = find_item(m.offsets, m.n_items, p);
+  if (m.args[it].order_hist) order_scatter(m.args[it], p - m.offsets[it]);
+}
+
+// thread per (global point, detector, component): TaylorF2 mixed items, two
+// components, at most kMultiMaxDet detectors
+__global__ void k_multi_reduce(MultiArgs m) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m.total_points * kMultiMaxDet * 2) return;
+  const int64_t p = idx % m.total_points, r = idx / m.total_points;
+  const int d = (int)(r / 2), t = (int)(r % 2);
+  const int it = find_item(m.offsets, m.n_items, p);
+  const LaunchArgs& a = m.args[it];
+  if (d < a.n_det && t < part_components(a)) reduce_chain(a, p - m.offsets[it], d, t);
+}
+
 __global__ void k_multi_finalize(MultiArgs m) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= m.total_points) return;
   const int it = find_item(m.offsets, m.n_items, p);
-  finalize_point(m.args[it], p - m.offsets[it]);
+  finalize_point(m.args[it], p - m.offsets[it], 1);
 }
 
-// Persistent: each CTA pulls work units of analyses with D detectors (units
-// [unit_begin[D], unit_begin[D+1])) until none is left.  Every unit covers at
+// Persistent: each CTA pulls work units of kernel class q = 2 D + CPLX
+// (analyses with D detectors and that partial-sum kind; units
+// [unit_begin[q], unit_begin[q + 1])) until none is left.  Every unit covers at
 // most kChunksPerGroup chunks, so units of short and long analyses cost about
-// the same.  One kernel per detector count keeps the register allocation of
-// the single-analysis kernel.
-template <int D>
+// the same.  One kernel per class keeps the register allocation of the
+// single-analysis kernel.
+template <int D, bool CPLX>
 __global__ void __launch_bounds__(kPointsPerCta, 5) k_multi_tf2(MultiArgs m) {
+  constexpr int q = 2 * D + (CPLX ? 1 : 0);
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar[2];
   __shared__ unsigned long long s_kmax;
@@ -897,53 +1154,72 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_multi_tf2(MultiArgs m) {
   }
   int64_t it_global = 0;
   float2* s_w = reinterpret_cast<float2*>(smem);
-  const int64_t ub = m.unit_begin[D], ue = m.unit_begin[D + 1];
+  const int64_t ub = m.unit_begin[q], ue = m.unit_begin[q + 1];
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) s_unit = ub + atomicAdd(m.counter + D, 1);
+    if (threadIdx.x == 0) s_unit = ub + atomicAdd(m.counter + q, 1);
     __syncthreads();
     const int64_t u = s_unit;
     if (u >= ue) break;
     const int4 wu = m.units[u];
-    tf2_unit<D>(m.args[wu.x], wu.y, wu.z, s_w, bar, &s_kmax, it_global);
+    tf2_unit<D, CPLX>(m.args[wu.x], wu.y, wu.z, s_w, bar, &s_kmax, it_global);
   }
 }
 
-template <int D>
+template <int D, bool CPLX>
 static int ctas_per_sm_d() {
   static int n = 0;
   if (n == 0) {
     const int smem = 2 * D * kChunkMixed * 8;
-    if (cudaFuncSetAttribute(k_multi_tf2<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_multi_tf2<D, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_multi_tf2<D>, kPointsPerCta, smem) != cudaSuccess || n < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_multi_tf2<D, CPLX>, kPointsPerCta, smem) != cudaSuccess ||
+        n < 1)
       n = 1;
   }
   return n;
 }
 
-int multi_tf2_ctas_per_sm(int D) {
-  switch (D) {
-    case 1: return ctas_per_sm_d<1>();
-    case 2: return ctas_per_sm_d<2>();
-    default: return ctas_per_sm_d<3>();
+int multi_tf2_ctas_per_sm(int q) {
+  switch (q) {
+    case 2: return ctas_per_sm_d<1, false>();
+    case 3: return ctas_per_sm_d<1, true>();
+    case 4: return ctas_per_sm_d<2, false>();
+    case 5: return ctas_per_sm_d<2, true>();
+    case 6: return ctas_per_sm_d<3, false>();
+    default: return ctas_per_sm_d<3, true>();
   }
 }
 
 cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s) {
-  const int threads = 128;
+  const int threads = kPointThreads;
   const unsigned pblocks = (unsigned)((m.total_points + threads - 1) / threads);
   k_multi_prologue<<<pblocks, threads, 0, s>>>(m);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  for (int D = 1; D <= kMultiMaxDet; ++D) {
-    if (ctas[D] <= 0) continue;
-    const int smem = 2 * D * kChunkMixed * 8;
-    if (D == 1) k_multi_tf2<1><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
-    if (D == 2) k_multi_tf2<2><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
-    if (D == 3) k_multi_tf2<3><<<(unsigned)ctas[D], kPointsPerCta, smem, s>>>(m);
+  if (m.ordered) {
+    k_multi_order_scan<<<(unsigned)m.n_items, kOrderThreads, 0, s>>>(m);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_multi_order_scatter<<<(unsigned)((m.total_points + 127) / 128), 128, 0, s>>>(m);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  for (int q = 2; q < kMultiClasses; ++q) {
+    if (ctas[q] <= 0) continue;
+    const int smem = 2 * (q / 2) * kChunkMixed * 8;
+    const unsigned g = (unsigned)ctas[q];
+    switch (q) {
+      case 2: k_multi_tf2<1, false><<<g, kPointsPerCta, smem, s>>>(m); break;
+      case 3: k_multi_tf2<1, true><<<g, kPointsPerCta, smem, s>>>(m); break;
+      case 4: k_multi_tf2<2, false><<<g, kPointsPerCta, smem, s>>>(m); break;
+      case 5: k_multi_tf2<2, true><<<g, kPointsPerCta, smem, s>>>(m); break;
+      case 6: k_multi_tf2<3, false><<<g, kPointsPerCta, smem, s>>>(m); break;
+      default: k_multi_tf2<3, true><<<g, kPointsPerCta, smem, s>>>(m); break;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  const int64_t chains = m.total_points * kMultiMaxDet * 2;
+  k_multi_reduce<<<(unsigned)((chains + 127) / 128), 128, 0, s>>>(m);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   k_multi_finalize<<<pblocks, threads, 0, s>>>(m);
   return cudaGetLastError();
 }

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   using C = typename TmTypes<MIXED>::C;
   using R = typename TmTypes<MIXED>::R;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double red[kTmThreads];
+  __shared__ double red[2 * kTmThreads];
   const int64_t L = a.n_fft;
   const double norm = 4.0 / a.duration;
   for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
@@ -248,26 +248,45 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
     }
     __syncthreads();
-    // ---- B: in-place radix-2 FFT -----------------------------------------
-    for (int s = 1; s <= log2L; ++s) {
-      const int64_t half = (int64_t)1 << (s - 1);
-      const int64_t tstride = L >> s;  // twiddle index stride W_L^(pos * L / len)
-      for (int64_t b = threadIdx.x; b < L / 2; b += blockDim.x) {
-        const int64_t pos = b & (half - 1);
-        const int64_t i0 = ((b >> (s - 1)) << s) + pos;
-        const int64_t i1 = i0 + half;
-        const C w = twiddle[pos * tstride];
-        const C x1 = buf[i1];
-        const C x0 = buf[i0];
-        const R tr = w.x * x1.x - w.y * x1.y;
-        const R ti = w.x * x1.y + w.y * x1.x;
+    // ---- B: in-place FFT, radix-4 passes (two radix-2 stages each) -------
+    int stage = 1;
+    if (log2L & 1) {  // one radix-2 stage first when log2 L is odd
+      for (int64_t bf = threadIdx.x; bf < L / 2; bf += blockDim.x) {
+        const int64_t i0 = 2 * bf, i1 = i0 + 1;
+        const C x0 = buf[i0], x1 = buf[i1];
         C y0, y1;
-        y0.x = x0.x + tr;
-        y0.y = x0.y + ti;
-        y1.x = x0.x - tr;
-        y1.y = x0.y - ti;
+        y0.x = x0.x + x1.x;
+        y0.y = x0.y + x1.y;
+        y1.x = x0.x - x1.x;
+        y1.y = x0.y - x1.y;
         buf[i0] = y0;
         buf[i1] = y1;
+      }
+      __syncthreads();
+      stage = 2;
+    }
+    for (; stage < log2L; stage += 2) {
+      const int64_t h = (int64_t)1 << (stage - 1);  // half-length of the first of the two stages
+      const int64_t s1 = L / (2 * h), s2 = L / (4 * h);  // twiddle strides of the two stages
+      for (int64_t bf = threadIdx.x; bf < L / 4; bf += blockDim.x) {
+        const int64_t pos = bf & (h - 1);
+        const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
+        const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
+        const C w1 = twiddle[pos * s1], w2 = twiddle[pos * s2], w3 = twiddle[(pos + h) * s2];
+        const C x0 = buf[i0], x1 = buf[i1], x2 = buf[i2], x3 = buf[i3];
+        C a0, a1, a2, a3, y0, y1, y2, y3;
+        R tr = w1.x * x1.x - w1.y * x1.y, ti = w1.x * x1.y + w1.y * x1.x;
+        a0.x = x0.x + tr; a0.y = x0.y + ti; a1.x = x0.x - tr; a1.y = x0.y - ti;
+        tr = w1.x * x3.x - w1.y * x3.y; ti = w1.x * x3.y + w1.y * x3.x;
+        a2.x = x2.x + tr; a2.y = x2.y + ti; a3.x = x2.x - tr; a3.y = x2.y - ti;
+        tr = w2.x * a2.x - w2.y * a2.y; ti = w2.x * a2.y + w2.y * a2.x;
+        y0.x = a0.x + tr; y0.y = a0.y + ti; y2.x = a0.x - tr; y2.y = a0.y - ti;
+        tr = w3.x * a3.x - w3.y * a3.y; ti = w3.x * a3.y + w3.y * a3.x;
+        y1.x = a1.x + tr; y1.y = a1.y + ti; y3.x = a1.x - tr; y3.y = a1.y - ti;
+        buf[i0] = y0;
+        buf[i1] = y1;
+        buf[i2] = y2;
+        buf[i3] = y3;
       }
       __syncthreads();
     }
@@ -285,43 +304,41 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
     const double prob = 1.0 / (a.t_max - a.t_min);
     const double jit = r.jitter;
+    const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+    const double sr = r.dist / a.ref_dist;
     // candidate window from the real-valued bounds, checked exactly below
     const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
     const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
     const int64_t j_lo = (int64_t)fmax(0.0, jl), j_hi = (int64_t)fmin((double)(L - 1), jh);
-    double best = -INFINITY;
+    // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
+    double m = -INFINITY, acc = 0.0;
     for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
       const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
       const double t = (a.start_time0 + lin) + jit;
       if (!(t >= a.t_min && t <= a.t_max)) continue;
       const C x = buf[j];
-      const double xr = (double)x.x, xi = (double)x.y;
       double l;
-      if (a.dist_marg) {
-        const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
-        const double sr = r.dist / a.ref_dist;
-        const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
-        l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
-      } else if (a.phase_marg) {
-        l = ln_i0(sqrt(xr * xr + xi * xi)) - hh / 2;
-      } else {
-        l = xr - hh / 2;
-      }
-      best = fmax(best, l);
-    }
-    const double amax = block_max(best, red);
-    double acc = 0.0;
-    if (isfinite(amax)) {
-      for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
-        const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
-        const double t = (a.start_time0 + lin) + jit;
-        if (!(t >= a.t_min && t <= a.t_max)) continue;
-        const C x = buf[j];
-        const double xr = (double)x.x, xi = (double)x.y;
-        double l;
+      if constexpr (MIXED) {
+        // float32 per-sample work; the large terms combine in float64
+        const float xr = x.x, xi = x.y;
         if (a.dist_marg) {
-          const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
-          const double sr = r.dist / a.ref_dist;
+          const float dx = a.phase_marg ? sqrtf(xr * xr + xi * xi) * (float)sr : xr * (float)sr;
+          l = (double)bicubic_eval_f(a.tx_f, a.nx, a.ty_f, a.ny, a.tc_f, a.bbox, dx, (float)hh_ref);
+        } else if (a.phase_marg) {
+          const float ax = sqrtf(xr * xr + xi * xi);
+          l = ((double)ax + (double)ln_i0_minus_x(ax)) - hh / 2;
+        } else {
+          l = (double)xr - hh / 2;
+        }
+        if (l > m) {
+          acc = isfinite(m) ? acc * (double)__expf((float)(m - l)) + 1.0 : 1.0;
+          m = l;
+        } else if (isfinite(l)) {
+          acc += (double)__expf((float)(l - m));
+        }
+      } else {
+        const double xr = x.x, xi = x.y;
+        if (a.dist_marg) {
           const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
           l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
         } else if (a.phase_marg) {
@@ -329,11 +346,34 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         } else {
           l = xr - hh / 2;
         }
-        acc += prob * a.delta_tc * exp(l - amax);
+        if (l > m) {
+          acc = isfinite(m) ? acc * exp(m - l) + 1.0 : 1.0;
+          m = l;
+        } else if (isfinite(l)) {
+          acc += exp(l - m);
+        }
       }
     }
-    const double total = block_sum(acc, red);
+    // combine (m, acc) pairs over the block in a fixed tree order
+    double* redm = red;
+    double* reds = red + kTmThreads;
+    redm[threadIdx.x] = m;
+    reds[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kTmThreads / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        const double m1 = redm[threadIdx.x], m2 = redm[threadIdx.x + w];
+        const double s1 = reds[threadIdx.x], s2 = reds[threadIdx.x + w];
+        const double mm = fmax(m1, m2);
+        double ss = 0.0;
+        if (isfinite(mm)) ss = (isfinite(m1) ? s1 * exp(m1 - mm) : 0.0) + (isfinite(m2) ? s2 * exp(m2 - mm) : 0.0);
+        redm[threadIdx.x] = mm;
+        reds[threadIdx.x] = ss;
+      }
+      __syncthreads();
+    }
     if (threadIdx.x == 0) {
+      const double amax = redm[0], total = reds[0] * prob * a.delta_tc;
       double lnl;
       if (!r.valid) lnl = -1.7976931348623157e308;
       else if (!isfinite(amax)) lnl = amax;

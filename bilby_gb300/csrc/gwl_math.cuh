@@ -89,4 +89,67 @@ __host__ __device__ inline double bicubic_eval(const double* tx, int nx, const d
   return s;
 }
 
+// ln I0(x) - x for x >= 0 in float32 (the large part x is added in float64
+// by the caller): the library Bessel function below 80, the large-argument
+// expansion (A&S 9.7.1) above.
+__device__ inline float ln_i0_minus_x(float x) {
+  if (x < 80.0f) return logf(cyl_bessel_i0f(x)) - x;
+  const float inv = 1.0f / (8.0f * x);
+  const float sum = 1.0f + inv * (1.0f + inv * (4.5f + inv * 37.5f));
+  return -0.5f * logf(6.2831853f * x) + logf(sum);
+}
+
+__device__ inline void bspline_values_f(const float* t, int k, float x, int L, float* h) {
+  float hh[4];
+  h[0] = 1.0f;
+  for (int j = 1; j <= k; ++j) {
+    for (int i = 0; i < j; ++i) hh[i] = h[i];
+    h[0] = 0.0f;
+    for (int i = 1; i <= j; ++i) {
+      const int li = L + i;
+      const int lj = li - j;
+      if (t[li] == t[lj]) {
+        h[i] = 0.0f;
+      } else {
+        const float f = hh[i - 1] / (t[li] - t[lj]);
+        h[i - 1] += f * (t[li] - x);
+        h[i] = f * (x - t[lj]);
+      }
+    }
+  }
+}
+
+__device__ inline int bspline_interval_f(const float* t, int n, int k, float& x) {
+  const float tb = t[k], te = t[n - k - 1];
+  if (x < tb) x = tb;
+  if (x > te) x = te;
+  int lo = k, hi = n - k - 2;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (t[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// float32 copy of bicubic_eval (same knots and coefficients rounded to float)
+__device__ inline float bicubic_eval_f(const float* tx, int nx, const float* ty, int ny, const float* c,
+                                       const double* bbox, float x, float y) {
+  if (!((double)x >= bbox[0] && (double)x <= bbox[1] && (double)y >= bbox[2] && (double)y <= bbox[3]))
+    return -INFINITY;
+  const int Lx = bspline_interval_f(tx, nx, 3, x);
+  const int Ly = bspline_interval_f(ty, ny, 3, y);
+  float hx[4], hy[4];
+  bspline_values_f(tx, 3, x, Lx, hx);
+  bspline_values_f(ty, 3, y, Ly, hy);
+  const int ncy = ny - 4;
+  float s = 0.0f;
+  for (int i = 0; i < 4; ++i) {
+    const float* row = c + (size_t)(Lx - 3 + i) * ncy + (Ly - 3);
+    float r = 0.0f;
+    for (int j = 0; j < 4; ++j) r += row[j] * hy[j];
+    s += r * hx[i];
+  }
+  return s;
+}
+
 }  // namespace gwl
