@@ -56,11 +56,13 @@ struct gwl_analysis {
   double* freq = nullptr;
   float* freq_f = nullptr;
   float2* basis = nullptr;
+  double4* ftab = nullptr;  // float64 TaylorF2: {f^(1/3), ln(f) / 3, f^(-5/3), f^(-7/6)} per bin
   float* anchors = nullptr;
   int64_t n_anchors = 0;
   double* strain[kMaxDet] = {};
   double* inv_psd[kMaxDet] = {};
   float2* w[kMaxDet] = {};
+  uint2* wp[kMaxDet] = {};  // TaylorF2: the same weights in polar form {float |w|, arg(w) as 0.32 fixed cycles}
   float* v[kMaxDet] = {};
   double* hh_prefix[kMaxDet] = {};
   double w_scale[kMaxDet] = {}, v_scale[kMaxDet] = {};
@@ -234,6 +236,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.strain[d] = a->strain[d];
     L.inv_psd[d] = a->inv_psd[d];
     L.w[d] = a->w[d];
+    L.wp[d] = a->wp[d];
     L.v[d] = a->v[d];
     L.hh_prefix[d] = a->hh_prefix[d];
     L.w_scale[d] = a->w_scale[d];
@@ -242,6 +245,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.freq = a->freq;
   L.freq_f = a->freq_f;
   L.basis = a->basis;
+  L.ftab = a->ftab;
   L.anchors = a->anchors;
   L.n_anchors = a->n_anchors;
   L.status = a->d_status;
@@ -528,6 +532,14 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
         for (int b = 0; b < kNumBasis; ++b) basis[(size_t)k * kNumBasis + b] = split_ff(vals[b]);
       }
       if ((rc = upload(a, &a->basis, basis))) goto fail;
+      // float64 powers of f for the plain kernel
+      std::vector<double4> ft((size_t)P, make_double4(0.0, 0.0, 0.0, 0.0));
+      for (int64_t k = 0; k < N; ++k) {
+        const double x = f[k];
+        if (!(x > 0)) continue;
+        ft[k] = make_double4(std::cbrt(x), std::log(x) / 3.0, std::pow(x, -5.0 / 3.0), std::pow(x, -7.0 / 6.0));
+      }
+      if ((rc = upload(a, &a->ftab, ft))) goto fail;
       // Taylor tables of the basis every kAnchorStep bins (f = k * df)
       a->n_anchors = N / kAnchorStep + 2;
       std::vector<float> anc((size_t)a->n_anchors * kAnchorFloats, 0.f);
@@ -582,6 +594,24 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
         vf[k] = (float)(ip[k] / a->v_scale[d]);
       }
       if ((rc = upload(a, &a->w[d], wf))) goto fail;
+      if (a->model == GWL_MODEL_TAYLORF2) {
+        std::vector<uint2> wpol(P, make_uint2(0u, 0u));
+        for (int64_t k = 0; k < N; ++k) {
+          const double x = wr[k] / a->w_scale[d], y = wi[k] / a->w_scale[d];
+          // odd bins carry -|w| at arg(w) + 1/2 cycle (the same term): a mean
+          // error of the float32 cosine then cancels between neighbouring bins
+          // instead of adding up coherently with the positive magnitudes
+          const bool odd = (k & 1) != 0;
+          const float mag = (float)(odd ? -std::hypot(x, y) : std::hypot(x, y));
+          double cyc = std::atan2(y, x) / (2.0 * M_PI) + (odd ? 0.5 : 0.0);
+          cyc -= std::floor(cyc);
+          const uint32_t th = (uint32_t)(uint64_t)std::llround(cyc * 4294967296.0);  // 2^32 wraps to 0
+          uint32_t mb;
+          std::memcpy(&mb, &mag, 4);
+          wpol[k] = make_uint2(mb, th);
+        }
+        if ((rc = upload(a, &a->wp[d], wpol))) goto fail;
+      }
       if (a->model == GWL_MODEL_SINEGAUSSIAN) {
         if ((rc = upload(a, &a->v[d], vf))) goto fail;
       } else {

@@ -70,10 +70,12 @@ struct LaunchArgs {
   const double* strain[kMaxDet];        // [2*n_pad] masked strain
   const double* inv_psd[kMaxDet];       // [n_pad] mask / S
   const float2* w[kMaxDet];             // [n_pad] mixed data weights (scaled)
+  const uint2* wp[kMaxDet];             // [n_pad] TaylorF2: polar weights {float |w| bits, arg(w) 0.32 cycles}
   const float* v[kMaxDet];              // [n_pad] mixed inverse PSD (scaled)
   const double* hh_prefix[kMaxDet];     // [n_bins + 1] TaylorF2 <h|h> prefix sums
   double w_scale[kMaxDet], v_scale[kMaxDet];
   const float2* basis;                  // [n_pad][kNumBasis] float-float phase basis
+  const double4* ftab;                  // [n_pad] {f^(1/3), ln(f) / 3, f^(-5/3), f^(-7/6)} (float64 TaylorF2)
   const float* anchors;                 // [n_anchors][kAnchorFloats] Taylor tables of the basis
   int64_t n_anchors;
   const double* params;                 // [GWL_NPARAM][B]

@@ -215,6 +215,14 @@ __global__ void k_order_scatter(LaunchArgs a) {
 // ---------------------------------------------------------------------------
 // plain float64 kernels
 // ---------------------------------------------------------------------------
+// (c + i s) *= (rc + i rs): one bin of a uniform-grid rotation.  Over a
+// chunk of kChunkPlain bins its rounding error stays near 1e-13 rad.
+__device__ __forceinline__ void rotate(double& c, double& s, double rc, double rs) {
+  const double t = c * rc - s * rs;
+  s = c * rs + s * rc;
+  c = t;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
   constexpr int CH = kChunkPlain;
@@ -246,6 +254,13 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
   if (r.valid) {
     const double f0 = r.sg_f0, amp = r.a[0], dplus = r.a[1], dcross = r.a[2], tau2 = r.a[3];
     const double pi2 = 9.869604401089358;
+    // e^{i w f} on the chunk's uniform grid by rotation from its first bin
+    double zc[D], zs[D], rc[D], rs[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      sincos(w2[d] * s_f[0], &zs[d], &zc[d]);
+      sincos(w2[d] * a.step, &rs[d], &rc[d]);
+    }
     for (int j = 0; j < CH; ++j) {
       const double f = s_f[j];
       // source.py:1199-1207
@@ -261,8 +276,7 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
         // interferometer.py:341-362
         const double sre = hp * fp[d];
         const double sim = hx_im * fx[d];
-        double sn, cs;
-        sincos(w2[d] * f, &sn, &cs);  // exp(-i w f) = cs - i sn
+        const double sn = zs[d], cs = zc[d];  // exp(-i w f) = cs - i sn
         const double hre = sre * cs + sim * sn;
         const double him = sim * cs - sre * sn;
         const double2 dd = s_d[d][j];
@@ -271,6 +285,8 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
         dim[d] += (hre * dd.y - him * dd.x) * is;
         hh[d] += (hre * hre + him * him) * is;
       }
+#pragma unroll
+      for (int d = 0; d < D; ++d) rotate(zc[d], zs[d], rc[d], rs[d]);
     }
   }
 #pragma unroll
@@ -282,16 +298,23 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_sg(LaunchArgs a) {
   }
 }
 
+// TaylorF2, float64.  Per bin: v = u f^(1/3), ln v = ln u + ln(f) / 3 and
+// the f^(-5/3), f^(-7/6) factors from the per-analysis table, the 3.5PN phase
+// by Horner's rule, one sincos, and each detector's time shift e^{-2 pi i f dt}
+// by rotation on the chunk's uniform grid.  <h|h> comes from the analysis's
+// prefix sums of f^(-7/3) / S (finalize), so only <d|h> is summed here.
 template <int D>
 __global__ void __launch_bounds__(kPointsPerCta) k_plain_tf2(LaunchArgs a) {
   constexpr int CH = kChunkPlain;
   __shared__ double s_f[CH];
+  __shared__ double4 s_t[CH];
   __shared__ double2 s_d[D][CH];
   __shared__ double s_is[D][CH];
   const int64_t k0 = a.k_base + (int64_t)blockIdx.y * CH;
   for (int j = threadIdx.x; j < CH; j += blockDim.x) {
     const int64_t k = k0 + j;
     s_f[j] = a.freq[k];
+    s_t[j] = a.ftab[k];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       s_d[d][j] = reinterpret_cast<const double2*>(a.strain[d])[k];
@@ -302,60 +325,64 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_tf2(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
   if (i >= a.B) return;
   const PointRec& r = a.rec[i];
-  double dre[D], dim[D], hh[D], fp[D], fx[D], w2[D];
+  double dre[D], dim[D], fp[D], fx[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    dre[d] = dim[d] = hh[d] = 0.0;
+    dre[d] = dim[d] = 0.0;
     fp[d] = r.fp[d];
     fx[d] = r.fx[d];
-    w2[d] = 2.0 * kPi * r.dt[d];
   }
-  if (r.valid) {
-    double ak[8], lk[8];
+  if (r.valid && k0 < r.k_end && k0 + CH > r.k_start) {
+    double ak[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      ak[k] = r.a[k];
-      lk[k] = r.l[k];
-    }
-    const double pim = kPi * r.m_sec, amp0 = r.amp, ci = r.cos_i, f_isco = r.f_isco;
-    const double pref = 3.0 / (128.0 * r.eta), cphase = -2.0 * r.phase - kPi / 4;
+    for (int k = 0; k < 8; ++k) ak[k] = r.a[k];
+    const double l5 = r.l[5], l6 = r.l[6];
+    const double u = cbrt(kPi * r.m_sec), lnu = log(u);
+    const double amp0 = r.amp, ci = r.cos_i, f_isco = r.f_isco;
+    const double pu5 = 3.0 / (128.0 * r.eta) / (u * u * u * u * u), cphase = -2.0 * r.phase - kPi / 4;
     const double pfac = (1.0 + ci * ci) / 2.0;
+    double zc[D], zs[D], rc[D], rs[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double w2 = 2.0 * kPi * r.dt[d];
+      sincos(w2 * s_f[0], &zs[d], &zc[d]);
+      sincos(w2 * a.step, &rs[d], &rc[d]);
+    }
     for (int j = 0; j < CH; ++j) {
       const double f = s_f[j];
-      if (f < a.fmin || f >= f_isco) continue;
-      // the TaylorF2 model (oracle/taylorf2.py) evaluated in float64
-      const double v = cbrt(pim * f);
-      const double lnv = log(v);
-      double s = 0.0, vk = 1.0;
+      if (f >= a.fmin && f < f_isco) {
+        // the TaylorF2 model (oracle/taylorf2.py) evaluated in float64
+        const double4 t = s_t[j];
+        const double v = u * t.x;
+        const double lnv = lnu + t.y;
+        double s = ak[7];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        s = s + (ak[k] + lk[k] * lnv) * vk;
-        vk = vk * v;
-      }
-      const double v5 = v * v * v * v * v;
-      const double psi = cphase + pref * s / v5;
-      const double amp = amp0 * pow(f, -7.0 / 6.0);
-      double sp, cp;
-      sincos(psi, &sp, &cp);  // exp(-i psi) = cp - i sp
-      const double ere = amp * cp, eim = -amp * sp;
-      // h_+ = pfac * e, h_x = -i ci * e
-      const double hpre = pfac * ere, hpim = pfac * eim;
-      const double hxre = ci * eim, hxim = -ci * ere;
+        for (int k = 6; k >= 0; --k) s = s * v + ak[k];
+        const double v5 = v * v * v * v * v;
+        s = s + lnv * (l5 + l6 * v) * v5;
+        const double psi = cphase + pu5 * s * t.z;
+        const double amp = amp0 * t.w;
+        double sp, cp;
+        sincos(psi, &sp, &cp);  // exp(-i psi) = cp - i sp
+        const double ere = amp * cp, eim = -amp * sp;
+        // h_+ = pfac * e, h_x = -i ci * e
+        const double hpre = pfac * ere, hpim = pfac * eim;
+        const double hxre = ci * eim, hxim = -ci * ere;
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const double is = s_is[d][j];
-        if (is == 0.0) continue;
-        const double sre = hpre * fp[d] + hxre * fx[d];
-        const double sim = hpim * fp[d] + hxim * fx[d];
-        double sn, cs;
-        sincos(w2[d] * f, &sn, &cs);
-        const double hre = sre * cs + sim * sn;
-        const double him = sim * cs - sre * sn;
-        const double2 dd = s_d[d][j];
-        dre[d] += (hre * dd.x + him * dd.y) * is;
-        dim[d] += (hre * dd.y - him * dd.x) * is;
-        hh[d] += (hre * hre + him * him) * is;
+        for (int d = 0; d < D; ++d) {
+          const double is = s_is[d][j];
+          const double sre = hpre * fp[d] + hxre * fx[d];
+          const double sim = hpim * fp[d] + hxim * fx[d];
+          const double sn = zs[d], cs = zc[d];  // exp(-i w f) = cs - i sn
+          const double hre = sre * cs + sim * sn;
+          const double him = sim * cs - sre * sn;
+          const double2 dd = s_d[d][j];
+          dre[d] += (hre * dd.x + him * dd.y) * is;
+          dim[d] += (hre * dd.y - him * dd.x) * is;
+        }
       }
+#pragma unroll
+      for (int d = 0; d < D; ++d) rotate(zc[d], zs[d], rc[d], rs[d]);
     }
   }
 #pragma unroll
@@ -363,7 +390,6 @@ __global__ void __launch_bounds__(kPointsPerCta) k_plain_tf2(LaunchArgs a) {
     double* out = a.part + (((int64_t)blockIdx.y * D + d) * kPartStride) * a.B + i;
     out[0 * a.B] = dre[d];
     out[1 * a.B] = dim[d];
-    out[2 * a.B] = hh[d];
   }
 }
 
@@ -459,20 +485,27 @@ __device__ __forceinline__ int anchor_interval(float n_cycles, float k0) {
 }
 
 // One bin of the anchored phase recurrence: detector d's phase (top 32 bits
-// of the 0.64 fixed-point cycle count) is base + lh[d] (lh[0] = 0), then the
-// weighted e^{+i phase} accumulation.  w points at the bin's weight of
-// detector 0; detector d's weight is CH entries further per detector.
+// of the 0.64 fixed-point cycle count) is base + lh[d] (lh[0] = 0); with the
+// polar weight w = |w| e^{i theta} (theta in 0.32 fixed cycles) the terms are
+// Re w e^{i phase} = |w| cos(phase + theta) and Im = |w| sin(phase + theta).
+// w points at the bin's weight of detector 0; detector d's weight is
+// kChunkMixed entries further per detector.
 template <int D, bool CPLX>
-__device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const float2* w, float* are, float* aim) {
+__device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const uint2* w, float* are, float* aim) {
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    const uint32_t top = d == 0 ? base : base + lh[d];
+    const uint2 wv = w[d * kChunkMixed];
+    const uint32_t top = (d == 0 ? base : base + lh[d]) + wv.y;
     const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
-    float sn, cs;
-    __sincosf(ph, &sn, &cs);
-    const float2 wv = w[d * kChunkMixed];
-    are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
-    if (CPLX) aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+    const float mag = __uint_as_float(wv.x);
+    if (CPLX) {
+      float sn, cs;
+      __sincosf(ph, &sn, &cs);
+      are[d] = __fmaf_rn(mag, cs, are[d]);
+      aim[d] = __fmaf_rn(mag, sn, aim[d]);
+    } else {
+      are[d] = __fmaf_rn(mag, __cosf(ph), are[d]);
+    }
   }
 }
 
@@ -480,7 +513,7 @@ __device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const
 // bin in float-float from the per-bin basis table (sum_b c_b phi_b(f_k)),
 // the time shift exact in 0.64 fixed point.
 template <int D, bool CPLX>
-__device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* w, int64_t k0, int64_t ks, int jlast,
+__device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const uint2* w, int64_t k0, int64_t ks, int jlast,
                                              const float* ch, const float* cl, const uint64_t* X, const uint64_t* Q,
                                              float* ahi, float* alo, float* bhi, float* blo) {
   constexpr int CH = kChunkMixed;
@@ -504,13 +537,14 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* 
       const uint32_t bu = (uint32_t)__float2int_rn(__fmul_rn(base, 4294967296.0f));
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d] + Q[d]) >> 32);
+        const uint2 wv = w[d * CH + j];
+        const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d] + Q[d]) >> 32) + wv.y;
         const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);
         float sn, cs;
         __sincosf(ph, &sn, &cs);
-        const float2 wv = w[d * CH + j];
-        are[d] = __fmaf_rn(wv.x, cs, __fmaf_rn(-wv.y, sn, are[d]));
-        if (CPLX) aim[d] = __fmaf_rn(wv.x, sn, __fmaf_rn(wv.y, cs, aim[d]));
+        const float mag = __uint_as_float(wv.x);
+        are[d] = __fmaf_rn(mag, cs, are[d]);
+        if (CPLX) aim[d] = __fmaf_rn(mag, sn, aim[d]);
       }
     }
 #pragma unroll
@@ -525,7 +559,7 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const float2* 
 // `it_global` counts the chunks this CTA has consumed so far (all units): it
 // selects the shared-memory stage and the mbarrier phase.
 template <int D, bool CPLX>
-__device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, float2* s_w, uint64_t* bar,
+__device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, uint2* s_w, uint64_t* bar,
                          unsigned long long* s_kmax, int64_t& it_global) {
   constexpr int CH = kChunkMixed;
   const int64_t slot = tile * kPointsPerCta + threadIdx.x;
@@ -579,7 +613,7 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&bar[s0], stage_bytes);
 #pragma unroll
-    for (int d = 0; d < D; ++d) bulk_g2s(s_w + s0 * D * CH + d * CH, a.w[d] + k0, CH * 8, &bar[s0]);
+    for (int d = 0; d < D; ++d) bulk_g2s(s_w + s0 * D * CH + d * CH, a.wp[d] + k0, CH * 8, &bar[s0]);
   }
   int64_t done = 0;
   for (int64_t it = 0; it < nit; ++it) {
@@ -590,15 +624,15 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
       // the other stage was released by the barrier at the end of the previous iteration
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       const int64_t k1 = a.k_base + (c + G) * CH;
-      float2* dst = s_w + (s ^ 1) * D * CH;
+      uint2* dst = s_w + (s ^ 1) * D * CH;
       mbar_expect_tx(&bar[s ^ 1], stage_bytes);
 #pragma unroll
-      for (int d = 0; d < D; ++d) bulk_g2s(dst + d * CH, a.w[d] + k1, CH * 8, &bar[s ^ 1]);
+      for (int d = 0; d < D; ++d) bulk_g2s(dst + d * CH, a.wp[d] + k1, CH * 8, &bar[s ^ 1]);
     }
     const bool arrived = mbar_wait_bounded(&bar[s], (uint32_t)((itg >> 1) & 1), a.status, kWaitLimit);
     done = it + 1;
     if (!__syncthreads_and(arrived)) break;
-    const float2* w = s_w + s * D * CH;
+    const uint2* w = s_w + s * D * CH;
     const int64_t k0 = a.k_base + c * CH;
     if (have && valid && k0 < ke && k0 + CH > ks) {
       // this point's own anchor interval for the chunk: the result of a
@@ -743,7 +777,7 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_mixed_tf2(LaunchArgs a) {
   }
   __syncthreads();
   int64_t it_global = 0;
-  tf2_unit<D, CPLX>(a, blockIdx.x, blockIdx.y, reinterpret_cast<float2*>(smem), bar, &s_kmax, it_global);
+  tf2_unit<D, CPLX>(a, blockIdx.x, blockIdx.y, reinterpret_cast<uint2*>(smem), bar, &s_kmax, it_global);
 }
 
 // Sine-Gaussian, mixed precision.  Shared memory per chunk: float32
@@ -871,15 +905,25 @@ __device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const
   double sdr = 0.0, sdi = 0.0, shh = 0.0;
   for (int d = 0; d < a.n_det; ++d) {
     double p[kPartStride] = {0, 0, 0, 0, 0, 0};
-    if (a.precision == GWL_PRECISION_FP64) sum_groups<3>(a, i, d, G, p);
-    else if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<6>(a, i, d, G, p);
+    if (a.precision == GWL_PRECISION_FP64) {
+      if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<3>(a, i, d, G, p);
+      else sum_groups<2>(a, i, d, G, p);
+    } else if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<6>(a, i, d, G, p);
     else if (a.cplx) sum_groups<2>(a, i, d, G, p);
     else sum_groups<1>(a, i, d, G, p);
     double dr, di, h;
-    if (a.precision == GWL_PRECISION_FP64) {
+    if (a.precision == GWL_PRECISION_FP64 && a.model == GWL_MODEL_SINEGAUSSIAN) {
       dr = norm * p[0];
       di = norm * p[1];
       h = norm * p[2];
+    } else if (a.precision == GWL_PRECISION_FP64) {
+      // <h|h> = A0^2 |Q|^2 sum_band f^(-7/3) / S
+      dr = norm * p[0];
+      di = norm * p[1];
+      const double ci = r.cos_i;
+      const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
+      const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+      h = norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
     } else if (a.model == GWL_MODEL_SINEGAUSSIAN) {
       // conj(h) = (Fp P hp + i Fx X hx) e^{+i theta}; sums S1 = sum hp e w, S2 = sum hx e w
       const double P = r.amp, X = r.amp2, ws = a.w_scale[d], vs = a.v_scale[d];
@@ -926,7 +970,8 @@ __device__ double distance_marginalized(const LaunchArgs& a, double dh_re, doubl
 // Components of a partial-sum record: <d|h> re/im and <h|h> (float64 kernels),
 // the six sums of the sine-Gaussian mixed kernel, re/im for TaylorF2 mixed.
 __device__ __host__ __forceinline__ int part_components(const LaunchArgs& a) {
-  return a.precision == GWL_PRECISION_FP64 ? 3 : (a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : (a.cplx ? 2 : 1));
+  if (a.precision == GWL_PRECISION_FP64) return a.model == GWL_MODEL_SINEGAUSSIAN ? 3 : 2;
+  return a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : (a.cplx ? 2 : 1);
 }
 
 // One (point, detector, component) chain: the partial sums of all groups
@@ -1153,7 +1198,7 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_multi_tf2(MultiArgs m) {
     mbar_fence_init();
   }
   int64_t it_global = 0;
-  float2* s_w = reinterpret_cast<float2*>(smem);
+  uint2* s_w = reinterpret_cast<uint2*>(smem);
   const int64_t ub = m.unit_begin[q], ue = m.unit_begin[q + 1];
   for (;;) {
     __syncthreads();

@@ -71,6 +71,35 @@ __device__ __forceinline__ bool plain_pols(const LaunchArgs& a, const PointRec& 
   return true;
 }
 
+// The same TaylorF2 polarisations from the per-bin power table f^(1/3),
+// ln(f) / 3, f^(-5/3), f^(-7/6); u = (pi M)^(1/3), pu5 = 3 / (128 eta u^5).
+__device__ __forceinline__ bool tf2_pols_tab(const LaunchArgs& a, const PointRec& r, int64_t k, double f, double u,
+                                             double lnu, double pu5, double2& hp, double2& hx) {
+  if (f < a.fmin || f >= r.f_isco) return false;
+  const double4 t = a.ftab[k];
+  const double v = u * t.x, lnv = lnu + t.y;
+  double s = r.a[7];
+#pragma unroll
+  for (int q = 6; q >= 0; --q) s = s * v + r.a[q];
+  const double v5 = v * v * v * v * v;
+  s = s + lnv * (r.l[5] + r.l[6] * v) * v5;
+  const double psi = (-2.0 * r.phase - kPi / 4) + pu5 * s * t.z;
+  const double amp = r.amp * t.w;
+  double sp, cp;
+  sincos(psi, &sp, &cp);
+  const double ere = amp * cp, eim = -amp * sp, ci = r.cos_i, pf = (1.0 + ci * ci) / 2.0;
+  hp = make_double2(pf * ere, pf * eim);
+  hx = make_double2(ci * eim, -ci * ere);
+  return true;
+}
+
+// (c + i s) *= (rc + i rs)
+__device__ __forceinline__ void tm_rotate(double& c, double& s, double rc, double rs) {
+  const double t = c * rc - s * rs;
+  s = c * rs + s * rc;
+  c = t;
+}
+
 // Block-wide reductions over kTmThreads threads in a fixed tree order.
 __device__ double block_max(double v, double* red) {
   red[threadIdx.x] = v;
@@ -196,22 +225,29 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         }
       }
     } else {
-      double w2[D];
-      for (int d = 0; d < D; ++d) w2[d] = 2.0 * kPi * r.dt[d];
+      // e^{i w f_k} for this thread's bins k = tid, tid + T, ... by rotation
+      double zc[D], zs[D], rc[D], rs[D];
+      for (int d = 0; d < D; ++d) {
+        const double w2 = 2.0 * kPi * r.dt[d];
+        sincos(w2 * ((double)threadIdx.x * a.step), &zs[d], &zc[d]);
+        sincos(w2 * ((double)blockDim.x * a.step), &rs[d], &rc[d]);
+      }
+      const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+      const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+      const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
       for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
         double zr = 0.0, zi = 0.0;
         double2 hp, hx;
         if (r.valid && k >= a.k_lo && k < a.k_hi) {
           const double f = a.freq[k];
-          if (plain_pols(a, r, f, hp, hx)) {
+          if (tf2 ? tf2_pols_tab(a, r, k, f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx)) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
               const double is = a.inv_psd[d][k];
               if (is == 0.0) continue;
               const double sre = hp.x * r.fp[d] + hx.x * r.fx[d];
               const double sim = hp.y * r.fp[d] + hx.y * r.fx[d];
-              double sn, cs;
-              sincos(w2[d] * f, &sn, &cs);
+              const double sn = zs[d], cs = zc[d];
               const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
               const double2 dd = reinterpret_cast<const double2*>(a.strain[d])[k];
               // base.py:326-329: signal * conj(d) / S
@@ -222,6 +258,8 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
           }
         }
         buf[bit_reverse((uint32_t)k, log2L)] = make_double2(norm * zr, norm * zi);
+#pragma unroll
+        for (int d = 0; d < D; ++d) tm_rotate(zc[d], zs[d], rc[d], rs[d]);
       }
       hh_part *= norm;
     }
