@@ -176,6 +176,7 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
     outs = [torch.empty(w.batch, dtype=torch.float64, device="cuda") for w in ws]
     items = [(lk.analysis, b.data_ptr(), b.shape[1], o.data_ptr()) for lk, b, o in zip(likes, blocks, outs)]
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    tuned = [lk.analysis.autotune(b.data_ptr(), b.shape[1], stream.cuda_stream)[0] for lk, b in zip(likes, blocks)]
     torch.cuda.synchronize()
     for _ in range(warmup):
         bat.eval_device(items, "mixed", stream.cuda_stream)
@@ -193,11 +194,40 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
     bat.check()
     pts = sum(w.batch for w in ws)
     pbd = sum(w.batch * (w.n_bins - int(w.minimum_frequency * w.duration)) * len(w.detectors) for w in ws)
+    value = pts * steps / (sum(ms) / 1e3)
+    # the plain float64 kernel on the same analyses (the first fp64_points points
+    # of each): one launch sequence per analysis, L2 flushed before each step
+    fp64_points = 64
+    sub_blocks = [b[:, :fp64_points].contiguous() for b in blocks]
+    sub = [(lk.analysis, b, b.shape[1], torch.empty(b.shape[1], dtype=torch.float64, device="cuda"))
+           for lk, b in zip(likes, sub_blocks)]
+    sub_items = [(an, b.data_ptr(), n, o.data_ptr()) for an, b, n, o in sub]
+    bat.eval_device(sub_items, "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms64 = []
+    for s in range(2):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bat.eval_device(sub_items, "fp64", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms64.append(e0.elapsed_time(e1))
+    pts64 = sum(n for _, _, n, _ in sub)
+    value64 = pts64 * len(ms64) / (sum(ms64) / 1e3)
+    dl = 0.0
+    for (_, _, n, o64), o in zip(sub, outs):
+        dl = max(dl, float((o64 - o[:n]).abs().max()))
     bat.close()
-    return {"analyses": len(ws), "points_per_launch": pts, "value": pts * steps / (sum(ms) / 1e3),
+    return {"analyses": len(ws), "points_per_launch": pts, "value": value,
             "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
             "point_bin_detector_per_s": pbd * steps / (sum(ms) / 1e3),
-            "launch": "one persistent kernel per detector count, CUDA-graph replay"}
+            "launch": "one persistent kernel per kernel class (detectors x partial kind), CUDA-graph replay",
+            "autotuned_chunks_per_group": {str(c): tuned.count(c) for c in sorted(set(tuned))},
+            "fp64": {"value": value64, "unit": "evals/s", "points_per_step": pts64,
+                     "sample": f"the first {fp64_points} points of every analysis, one launch sequence per analysis"},
+            "mixed_over_fp64": value / value64, "max_abs_dlnl_mixed_vs_fp64": dl}
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
@@ -415,6 +445,8 @@ def run_ours(args, rank, world, local):
     blocks = [torch.from_numpy(params_block(p)).cuda() for p in host_params]
     out = torch.empty(B, dtype=torch.float64, device="cuda")
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    # launch shape for this workload (outside the timed region)
+    tuned_cpg, _ = an.autotune(blocks[0].data_ptr(), B, sptr)
     an.set_profiling(True)
 
     def timed(precision, bl, n_steps, warm):
@@ -514,7 +546,8 @@ def run_ours(args, rank, world, local):
             "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection)",
             "config": {"workload": w.name, "model": w.model, "detectors": list(w.detectors), "n_bins": w.n_bins,
                        "duration_s": w.duration, "sampling_frequency": w.sampling_frequency, "batch": B,
-                       "parallelism": f"replicas x{world}", "l2": "flushed before every timed launch (256 MiB write)"},
+                       "parallelism": f"replicas x{world}", "l2": "flushed before every timed launch (256 MiB write)",
+                       "autotuned_chunks_per_group": tuned_cpg},
             "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
             "fp64": {"value": fp64_value, "unit": "evals/s", "batch": Bf},
             "mixed_over_fp64": value / world / fp64_value,

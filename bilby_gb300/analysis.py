@@ -155,6 +155,27 @@ class Analysis:
         _capi.check(self._lib.gwl_profile_last_kernel_ms(self._h, ctypes.byref(ms)), "gwl_profile_last_kernel_ms")
         return float(ms.value)
 
+    # -- launch-shape tuning ---------------------------------------------------
+    def autotune(self, block_ptr: int, B: int, stream: int = 0) -> tuple[int, float]:
+        """Pick the split-K depth of the mixed TaylorF2 kernel by timing each
+        candidate on B device points (block [NPARAM, B] at ``block_ptr``);
+        returns (chunks per group, median ms of the launch sequence)."""
+        c = ctypes.c_int32()
+        ms = ctypes.c_double()
+        _capi.check(self._lib.gwl_autotune(self._h, ctypes.c_void_p(block_ptr), int(B), ctypes.c_void_p(stream),
+                                           ctypes.byref(c), ctypes.byref(ms)), "gwl_autotune")
+        return int(c.value), float(ms.value)
+
+    @property
+    def chunks_per_group(self) -> int:
+        c = ctypes.c_int32()
+        _capi.check(self._lib.gwl_get_chunks_per_group(self._h, ctypes.byref(c)), "gwl_get_chunks_per_group")
+        return int(c.value)
+
+    @chunks_per_group.setter
+    def chunks_per_group(self, value: int):
+        _capi.check(self._lib.gwl_set_chunks_per_group(self._h, int(value)), "gwl_set_chunks_per_group")
+
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

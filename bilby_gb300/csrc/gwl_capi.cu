@@ -79,6 +79,7 @@ struct gwl_analysis {
   double bbox[4] = {0, 0, 0, 0};
   double ref_dist = 0;
   // work space
+  int chunks_per_group = kChunksPerGroup;  // split-K depth of the TaylorF2 mixed kernel (gwl_autotune)
   int64_t ws_B = 0;
   double* d_params = nullptr;
   double* d_out = nullptr;
@@ -225,7 +226,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     // split-K: each CTA walks a strided set of chunks;
     // a fixed number of chunks per group, so that the summation order of a
     // point (and so its result) is the same for every batch size
-    L.n_groups = (a->n_chunks_mixed + kChunksPerGroup - 1) / kChunksPerGroup;
+    L.n_groups = (a->n_chunks_mixed + a->chunks_per_group - 1) / a->chunks_per_group;
   }
   L.duration = a->duration;
   L.step = a->step;
@@ -691,6 +692,81 @@ int gwl_profile_last_kernel_ms(gwl_analysis* a, float* ms) {
   return GWL_OK;
 }
 
+int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream, int32_t* chunks_per_group,
+                 double* best_ms) {
+  if (!a || !params || B <= 0) {
+    set_error("gwl_autotune: null argument or empty batch");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg) {
+    // nothing to tune: the other launch shapes are fixed
+    if (chunks_per_group) *chunks_per_group = a->chunks_per_group;
+    if (best_ms) *best_ms = 0.0;
+    return GWL_OK;
+  }
+  cudaEvent_t e0, e1;
+  GWL_CUDA(cudaEventCreate(&e0));
+  GWL_CUDA(cudaEventCreate(&e1));
+  const int candidates[] = {2, 3, 4, 6, 8, 12, 16};
+  const int keep = a->chunks_per_group;
+  int best = keep;
+  float best_t = 0.f;
+  int rc = GWL_OK;
+  LaunchArgs L0 = make_args(a, B, GWL_PRECISION_MIXED);
+  if ((rc = ensure_workspace(a, B, L0))) goto done;
+  for (int c : candidates) {
+    if (c > a->n_chunks_mixed && c != candidates[0]) break;
+    a->chunks_per_group = c;
+    // one untimed run, then the median of three timed runs of the whole launch sequence
+    if ((rc = run_eval(a, params, B, GWL_PRECISION_MIXED, a->d_out, nullptr, nullptr, s))) goto done;
+    float t[3];
+    for (int r = 0; r < 3; ++r) {
+      if (cudaEventRecord(e0, s) != cudaSuccess) { rc = GWL_ERR_CUDA; goto done; }
+      if ((rc = run_eval(a, params, B, GWL_PRECISION_MIXED, a->d_out, nullptr, nullptr, s))) goto done;
+      if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess) {
+        rc = GWL_ERR_CUDA;
+        goto done;
+      }
+    }
+    std::sort(t, t + 3);
+    if (best_t == 0.f || t[1] < best_t) {
+      best_t = t[1];
+      best = c;
+    }
+  }
+done:
+  a->chunks_per_group = rc == GWL_OK ? best : keep;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == GWL_OK) {
+    if (chunks_per_group) *chunks_per_group = best;
+    if (best_ms) *best_ms = best_t;
+  }
+  return rc;
+}
+
+int gwl_get_chunks_per_group(gwl_analysis* a, int32_t* chunks_per_group) {
+  if (!a || !chunks_per_group) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *chunks_per_group = a->chunks_per_group;
+  return GWL_OK;
+}
+
+int gwl_set_chunks_per_group(gwl_analysis* a, int32_t chunks_per_group) {
+  if (!a || chunks_per_group < 1 || chunks_per_group > 1024) {
+    set_error("chunks_per_group must be in [1, 1024]");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  a->chunks_per_group = chunks_per_group;
+  return GWL_OK;
+}
+
 int gwl_noise_log_likelihood(gwl_analysis* a, double* out) {
   if (!a || !out) {
     set_error("null argument");
@@ -1002,6 +1078,7 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     units_d[2 * a->n_det + largs[q].cplx] += tiles * largs[q].n_groups;
     key.push_back(reinterpret_cast<int64_t>(a));
     key.push_back(items[q].B);
+    key.push_back(largs[q].n_groups);  // changes when the analysis is re-tuned
   }
   for (int c = 0; c < kMultiClasses; ++c) n_units += units_d[c];
   // capacity (growing invalidates captured graphs: their pointers change)

@@ -401,6 +401,17 @@ class GravitationalWaveTransient(_Base):
         block = params_block(self._prepare(arrays))
         return self.analysis.log_likelihood_ratio_host(block, precision)
 
+    def autotune(self, parameters) -> tuple[int, float]:
+        """Choose the mixed kernel's launch shape for batches like ``parameters``
+        (a mapping of names to equal-length arrays): returns the chosen
+        split-K depth and the median milliseconds of one launch sequence."""
+        import torch
+        arrays = {k: np.asarray(v, dtype=np.float64) for k, v in parameters.items()}
+        block = torch.from_numpy(params_block(self._prepare(arrays))).cuda()
+        res = self.analysis.autotune(block.data_ptr(), block.shape[1], torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return res
+
     # ------------------------------------------------------------------
     def __repr__(self):
         return (f"{self.__class__.__name__}(interferometers={[i.name for i in self.interferometers]},\n\t"

@@ -234,6 +234,19 @@ int gwl_eval_device_noalloc(gwl_analysis *a, const double *params, int64_t B, do
 int gwl_set_profiling(gwl_analysis *a, int enable);
 int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
 
+/* Autotuner (no counterpart in the reference, which has no launch shapes):
+ * times the mixed-precision TaylorF2 launch sequence on the caller's B device
+ * points for each split-K depth (chunks of 512 bins walked by one CTA; 2, 3,
+ * 4, 6, 8, 12, 16), keeps the fastest for this analysis and returns it with
+ * its median time.  Synchronous on `stream`.  The depth sets the order in
+ * which a point's chunk sums are added, so results are bit-reproducible for a
+ * fixed depth and move by float64 rounding only (~1e-16 relative) when it
+ * changes.  Other models and time marginalisation have nothing to tune. */
+int gwl_autotune(gwl_analysis *a, const double *params, int64_t B, void *stream, int32_t *chunks_per_group,
+                 double *best_ms);
+int gwl_get_chunks_per_group(gwl_analysis *a, int32_t *chunks_per_group);
+int gwl_set_chunks_per_group(gwl_analysis *a, int32_t chunks_per_group);
+
 /* Description of the last error on this thread ("" if none). */
 const char *gwl_last_error(void);
 
