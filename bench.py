@@ -220,15 +220,14 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
         ms64.append(e0.elapsed_time(e1))
     pts64 = sum(n for _, _, n, _ in sub)
     value64 = pts64 * len(ms64) / (sum(ms64) / 1e3)
-    dl, dl_quiet, lnl_at = 0.0, 0.0, 0.0
-    for (_, _, n, o64), o in zip(sub, outs):
-        err = (o64 - o[:n]).abs()
-        j = int(err.argmax())
-        if float(err[j]) > dl:
-            dl, lnl_at = float(err[j]), float(o64[j])
-        quiet = o64.abs() < 1e4
-        if bool(quiet.any()):
-            dl_quiet = max(dl_quiet, float(err[quiet].max()))
+    errs = torch.cat([(o64 - o[:n]).abs() for (_, _, n, o64), o in zip(sub, outs)]).cpu().numpy()
+    lnls = torch.cat([o64 for (_, _, _, o64) in sub]).cpu().numpy()
+    j = int(np.argmax(errs))
+    dl, lnl_at = float(errs[j]), float(lnls[j])
+    quiet = np.abs(lnls) < 1e4
+    dl_quiet = float(errs[quiet].max()) if quiet.any() else 0.0
+    dl_1e3 = float(errs[np.abs(lnls) < 1e3].max()) if (np.abs(lnls) < 1e3).any() else 0.0
+    frac_ok = float(np.mean(errs <= 1e-3))
     bat.close()
     return {"analyses": len(ws), "points_per_launch": pts, "value": value,
             "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
@@ -238,7 +237,8 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
             "fp64": {"value": value64, "unit": "evals/s", "points_per_step": pts64,
                      "sample": f"the first {fp64_points} points of every analysis, one launch sequence per analysis"},
             "mixed_over_fp64": value / value64, "max_abs_dlnl_mixed_vs_fp64": dl, "lnl_at_max_dlnl": lnl_at,
-            "max_abs_dlnl_where_abs_lnl_below_1e4": dl_quiet}
+            "max_abs_dlnl_where_abs_lnl_below_1e4": dl_quiet, "max_abs_dlnl_where_abs_lnl_below_1e3": dl_1e3,
+            "fraction_of_points_with_abs_dlnl_le_1e-3": frac_ok}
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):

@@ -159,7 +159,7 @@ class Analysis:
     def autotune(self, block_ptr: int, B: int, stream: int = 0) -> tuple[int, float]:
         """Pick the split-K depth of the mixed TaylorF2 kernel by timing each
         candidate on B device points (block [NPARAM, B] at ``block_ptr``);
-        returns (chunks per group, median ms of the launch sequence)."""
+        returns (chunks per group, ms of the launch sequence at that depth)."""
         c = ctypes.c_int32()
         ms = ctypes.c_double()
         _capi.check(self._lib.gwl_autotune(self._h, ctypes.c_void_p(block_ptr), int(B), ctypes.c_void_p(stream),

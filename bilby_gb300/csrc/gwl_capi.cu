@@ -719,10 +719,11 @@ int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream,
   for (int c : candidates) {
     if (c > a->n_chunks_mixed && c != candidates[0]) break;
     a->chunks_per_group = c;
-    // one untimed run, then the median of three timed runs of the whole launch sequence
+    // one untimed run, then the fastest of five timed runs of the whole launch
+    // sequence (interference from other work only ever adds time)
     if ((rc = run_eval(a, params, B, GWL_PRECISION_MIXED, a->d_out, nullptr, nullptr, s))) goto done;
-    float t[3];
-    for (int r = 0; r < 3; ++r) {
+    float t[5];
+    for (int r = 0; r < 5; ++r) {
       if (cudaEventRecord(e0, s) != cudaSuccess) { rc = GWL_ERR_CUDA; goto done; }
       if ((rc = run_eval(a, params, B, GWL_PRECISION_MIXED, a->d_out, nullptr, nullptr, s))) goto done;
       if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
@@ -731,9 +732,9 @@ int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream,
         goto done;
       }
     }
-    std::sort(t, t + 3);
-    if (best_t == 0.f || t[1] < best_t) {
-      best_t = t[1];
+    std::sort(t, t + 5);
+    if (best_t == 0.f || t[0] < best_t) {
+      best_t = t[0];
       best = c;
     }
   }

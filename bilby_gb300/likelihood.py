@@ -404,7 +404,7 @@ class GravitationalWaveTransient(_Base):
     def autotune(self, parameters) -> tuple[int, float]:
         """Choose the mixed kernel's launch shape for batches like ``parameters``
         (a mapping of names to equal-length arrays): returns the chosen
-        split-K depth and the median milliseconds of one launch sequence."""
+        split-K depth and the milliseconds of one launch sequence at that depth."""
         import torch
         arrays = {k: np.asarray(v, dtype=np.float64) for k, v in parameters.items()}
         block = torch.from_numpy(params_block(self._prepare(arrays))).cuda()

@@ -238,7 +238,7 @@ int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
  * times the mixed-precision TaylorF2 launch sequence on the caller's B device
  * points for each split-K depth (chunks of 512 bins walked by one CTA; 2, 3,
  * 4, 6, 8, 12, 16), keeps the fastest for this analysis and returns it with
- * its median time.  Synchronous on `stream`.  The depth sets the order in
+ * its time (the fastest of five runs after one untimed run).  Synchronous on `stream`.  The depth sets the order in
  * which a point's chunk sums are added, so results are bit-reproducible for a
  * fixed depth and move by float64 rounding only (~1e-16 relative) when it
  * changes.  Other models and time marginalisation have nothing to tune. */
