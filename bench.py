@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the serving run")
     ap.add_argument("--n-analyses", type=int, default=64)
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
+    ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
     return ap.parse_args()
 
 
@@ -239,6 +240,43 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
             "mixed_over_fp64": value / value64, "max_abs_dlnl_mixed_vs_fp64": dl, "lnl_at_max_dlnl": lnl_at,
             "max_abs_dlnl_where_abs_lnl_below_1e4": dl_quiet, "max_abs_dlnl_where_abs_lnl_below_1e3": dl_1e3,
             "fraction_of_points_with_abs_dlnl_le_1e-3": frac_ok}
+
+
+def bench_relbin(name, steps, warmup, batch=65536, seed=31):
+    """Relative binning (bilby/gw/likelihood/relative.py) on the GPU: fiducial
+    = the injection, default chi = 1 and epsilon = 0.5; float64 throughout."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.relative import RelativeBinningGravitationalWaveTransient
+    from bilby_gb300.workloads import WORKLOADS, draw_points
+    w = WORKLOADS[name]
+    base = build_likelihood(w, precision="fp64")
+    t0 = time.perf_counter()
+    like = RelativeBinningGravitationalWaveTransient(base.interferometers, base.waveform_generator,
+                                                     fiducial_parameters=dict(w.injection))
+    setup_s = time.perf_counter() - t0
+    an = like.analysis
+    rng = np.random.default_rng(seed)
+    blocks = [torch.from_numpy(params_block(draw_points(w, batch, rng))).cuda() for _ in range(2)]
+    out = torch.empty(batch, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for s in range(warmup):
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return {"workload": name, "bins": int(like.number_of_bins), "batch": batch,
+            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+            "precision": "fp64", "setup_s": setup_s,
+            "launch": "prologue + one warp per point over the bin edges"}
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
@@ -529,6 +567,10 @@ def run_ours(args, rank, world, local):
         if args.no_uneven:
             uneven = None
 
+    relbin = None
+    if world == 1 and not args.no_relbin:
+        relbin = bench_relbin("tf2_128s", max(3, args.steps // 2), args.warmup)
+
     marg = None
     if world == 1 and not args.no_marg:
         marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup)
@@ -584,6 +626,8 @@ def run_ours(args, rank, world, local):
         }
         if marg is not None:
             line["marginalized"] = marg
+        if relbin is not None:
+            line["relative_binning"] = relbin
         if uneven is not None:
             line["uneven"] = uneven
         if served is not None:

@@ -112,6 +112,25 @@ class Analysis:
             float(reference_distance)), "gwl_set_distance_marginalization")
         self.distance_marginalization = True
 
+    def set_relative_binning(self, enable: bool, edge_index=None, h0_inverse=None, summary=None):
+        """Relative binning: ``edge_index`` [n_edges] increasing grid indices,
+        ``h0_inverse`` [n_det, n_edges] complex 1 / h0 at the edges,
+        ``summary`` [n_det, n_edges - 1, 6] (a0 re, a0 im, a1 re, a1 im, b0, b1)."""
+        if not enable:
+            _capi.check(self._lib.gwl_set_relative_binning(self._h, 0, 0, None, None, None),
+                        "gwl_set_relative_binning")
+            self.relative_binning = False
+            return
+        idx = np.ascontiguousarray(edge_index, dtype=np.int64)
+        h = np.ascontiguousarray(np.asarray(h0_inverse, dtype=np.complex128).view(np.float64))
+        sm = np.ascontiguousarray(summary, dtype=np.float64)
+        if h.size != 2 * self.n_detectors * len(idx) or sm.size != 6 * self.n_detectors * (len(idx) - 1):
+            raise ValueError("relative-binning arrays do not match the detectors and bin edges")
+        _capi.check(self._lib.gwl_set_relative_binning(
+            self._h, 1, len(idx), idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _capi.dptr(h),
+            _capi.dptr(sm)), "gwl_set_relative_binning")
+        self.relative_binning = True
+
     # -- queries -----------------------------------------------------------
     def noise_log_likelihood(self) -> float:
         out = ctypes.c_double()

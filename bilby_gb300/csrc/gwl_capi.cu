@@ -78,6 +78,13 @@ struct gwl_analysis {
   int nx = 0, ny = 0;
   double bbox[4] = {0, 0, 0, 0};
   double ref_dist = 0;
+  // relative binning
+  int relbin = 0;
+  int rb_edges = 0;
+  int64_t* rb_index = nullptr;
+  double* rb_freq = nullptr;
+  double2* rb_h0inv[kMaxDet] = {};
+  double* rb_sum[kMaxDet] = {};
   // work space
   int chunks_per_group = kChunksPerGroup;  // split-K depth of the TaylorF2 mixed kernel (gwl_autotune)
   int64_t ws_B = 0;
@@ -100,6 +107,7 @@ struct gwl_analysis {
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   int ev_pending = 0;
   std::vector<void*> tables;  // everything allocated for the tables
+  std::vector<double> h_freq;  // host copy of the frequency array
   std::mutex mu;
 };
 
@@ -269,6 +277,14 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.ny = a->ny;
   for (int q = 0; q < 4; ++q) L.bbox[q] = a->bbox[q];
   L.ref_dist = a->ref_dist;
+  L.relbin = a->relbin;
+  L.rb_edges = a->rb_edges;
+  L.rb_index = a->rb_index;
+  L.rb_freq = a->rb_freq;
+  for (int d = 0; d < a->n_det; ++d) {
+    L.rb_h0inv[d] = a->rb_h0inv[d];
+    L.rb_sum[d] = a->rb_sum[d];
+  }
   return L;
 }
 
@@ -315,6 +331,17 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.dh_out = d_dh;
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
+  if (a->relbin) {
+    // relative binning: per-point set-up, then one warp per point over the bins
+    GWL_CUDA(launch_prologue(L, s));
+    if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+    GWL_CUDA(launch_relbin(L, s));
+    if (a->profiling) {
+      GWL_CUDA(cudaEventRecord(a->ev_end, s));
+      a->ev_pending = 1;
+    }
+    return GWL_OK;
+  }
   if (d_dh) L.cplx = 1;  // complex <d|h> requested
   const bool ordered = precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2 && !(a->time_marg && d_out);
   if (ordered) {
@@ -356,9 +383,9 @@ namespace gwl {
 // entry point that supplies its own work space; also the bytes it needs for
 // the per-point records and the partial sums.  Allocates nothing.
 int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes) {
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin) {
     set_error("the allocation-free entry point serves mixed-precision TaylorF2 analyses without time "
-              "marginalisation");
+              "marginalisation or relative binning");
     return GWL_ERR_UNSUPPORTED;
   }
   *L = make_args(a, B, GWL_PRECISION_MIXED);
@@ -519,6 +546,7 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
       hff[k] = (float)f[k];
     }
     if ((rc = upload(a, &a->freq, hf))) goto fail;
+    a->h_freq.assign(f, f + N);
     if (a->model == GWL_MODEL_SINEGAUSSIAN && (rc = upload(a, &a->freq_f, hff))) goto fail;
     if (a->model == GWL_MODEL_TAYLORF2) {
       // float-float phase basis: f^-5/3, f^-1, f^-2/3, f^-1/3, ln f, f^1/3, f^1/3 ln f, f^2/3
@@ -700,7 +728,7 @@ int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream,
   }
   std::lock_guard<std::mutex> g(a->mu);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin) {
     // nothing to tune: the other launch shapes are fixed
     if (chunks_per_group) *chunks_per_group = a->chunks_per_group;
     if (best_ms) *best_ms = 0.0;
@@ -792,6 +820,10 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
+    if (a->relbin) {
+      set_error("time marginalisation is not available with relative binning");
+      return GWL_ERR_UNSUPPORTED;
+    }
   }
   a->time_marg = enable ? 1 : 0;
   a->jitter = jitter ? 1 : 0;
@@ -839,6 +871,51 @@ int gwl_set_distance_marginalization(gwl_analysis* a, int enable, const double* 
   for (int q = 0; q < 4; ++q) a->bbox[q] = bbox[q];
   a->ref_dist = reference_distance;
   a->dist_marg = 1;
+  return GWL_OK;
+}
+
+int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const int64_t* edge_index,
+                             const double* h0_inverse, const double* summary) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!enable) {
+    a->relbin = 0;
+    return GWL_OK;
+  }
+  if (a->time_marg) {
+    set_error("time marginalisation is not available with relative binning");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  if (n_edges < 2 || !edge_index || !h0_inverse || !summary) {
+    set_error("relative binning needs at least two bin edges, 1 / h0 at the edges and the summary data");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<int64_t> idx(edge_index, edge_index + n_edges);
+  std::vector<double> fe(n_edges);
+  for (int32_t e = 0; e < n_edges; ++e) {
+    if (idx[e] < 0 || idx[e] >= a->n_bins || (e > 0 && idx[e] <= idx[e - 1])) {
+      set_error("bin edges must be increasing grid indices inside the frequency array");
+      return GWL_ERR_ARGUMENT;
+    }
+    fe[e] = a->h_freq[idx[e]];
+  }
+  int rc;
+  if ((rc = upload(a, &a->rb_index, idx))) return rc;
+  if ((rc = upload(a, &a->rb_freq, fe))) return rc;
+  const size_t nb = (size_t)(n_edges - 1);
+  for (int d = 0; d < a->n_det; ++d) {
+    std::vector<double2> h(n_edges);
+    for (int32_t e = 0; e < n_edges; ++e)
+      h[e] = make_double2(h0_inverse[((size_t)d * n_edges + e) * 2], h0_inverse[((size_t)d * n_edges + e) * 2 + 1]);
+    std::vector<double> sm(summary + (size_t)d * nb * 6, summary + (size_t)(d + 1) * nb * 6);
+    if ((rc = upload(a, &a->rb_h0inv[d], h))) return rc;
+    if ((rc = upload(a, &a->rb_sum[d], sm))) return rc;
+  }
+  a->rb_edges = n_edges;
+  a->relbin = 1;
   return GWL_OK;
 }
 
@@ -1047,7 +1124,7 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
       return GWL_ERR_ARGUMENT;
     }
     const gwl_analysis* a = it.analysis;
-    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->n_det > kMultiMaxDet) fused = false;
+    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->n_det > kMultiMaxDet) fused = false;
   }
   if (!fused) {
     // other models / precisions / time marginalisation: one launch sequence per item

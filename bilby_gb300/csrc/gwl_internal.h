@@ -102,6 +102,14 @@ struct LaunchArgs {
   double bbox[4];
   double ref_dist;
   double* tm_work;                      // time-marginalisation work space
+  // relative binning: the model at the bin edges, its ratio to the fiducial
+  // response, and the per-bin summary data of each detector
+  int relbin;
+  int rb_edges;
+  const int64_t* rb_index;              // [rb_edges] grid index of each edge
+  const double* rb_freq;                // [rb_edges] edge frequencies
+  const double2* rb_h0inv[kMaxDet];     // [rb_edges] 1 / h0_d(f_e)
+  const double* rb_sum[kMaxDet];        // [rb_edges - 1][6]: a0 re, a0 im, a1 re, a1 im, b0, b1
 };
 
 // A batch over several analyses evaluated by one persistent launch: per item
@@ -128,6 +136,7 @@ cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);

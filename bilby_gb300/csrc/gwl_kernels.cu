@@ -1001,11 +1001,9 @@ __global__ void k_reduce_parts(LaunchArgs a) {
   reduce_chain(a, i, (int)(r / nq), (int)(r % nq));
 }
 
-// G: the groups still to be summed (1 after k_reduce_parts)
-__device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int64_t G) {
-  const PointRec& r = a.rec[i];
-  double dr, di, hh;
-  detector_totals(a, i, G, r, &dr, &di, &hh);
+// lnL of point i from its totals <d|h> = dr + i di and <h|h> (base.py:448-477
+// without time marginalisation), with the optional outputs of the totals.
+__device__ void finish_point(const LaunchArgs& a, const PointRec& r, int64_t i, double dr, double di, double hh) {
   if (a.dh_out) {
     a.dh_out[2 * i] = dr;
     a.dh_out[2 * i + 1] = di;
@@ -1023,6 +1021,121 @@ __device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int6
     lnl = dr - hh / 2;  // base.py:475
   }
   a.out[i] = lnl;
+}
+
+// G: the groups still to be summed (1 after k_reduce_parts)
+__device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int64_t G) {
+  const PointRec& r = a.rec[i];
+  double dr, di, hh;
+  detector_totals(a, i, G, r, &dr, &di, &hh);
+  finish_point(a, r, i, dr, di, hh);
+}
+
+// ---------------------------------------------------------------------------
+// relative binning (bilby/gw/likelihood/relative.py:365-402)
+// ---------------------------------------------------------------------------
+// One warp per point.  Lane l evaluates the model at edge e = 31 q + l (q-th
+// pass), projects it on each detector, multiplies by 1 / h0_d(f_e) and takes
+// the ratio at edge e + 1 from lane l + 1; lanes 0..30 then add bin e's terms
+//   <d|h> += a0 conj(r0) + a1 conj(r1),  <h|h> += b0 |r0|^2 + 2 b1 Re(r0 conj(r1))
+// with r0 = (r_{e+1} + r_e) / 2 and r1 = (r_{e+1} - r_e) / (f_{e+1} - f_e).
+// float64 throughout.
+constexpr int kRelbinWarps = 4;
+
+template <int D>
+__global__ void __launch_bounds__(32 * kRelbinWarps) k_relbin(LaunchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kRelbinWarps + (threadIdx.x >> 5);
+  if (i >= a.B) return;  // uniform over the warp
+  const PointRec& r = a.rec[i];
+  const int nE = a.rb_edges, nB = nE - 1;
+  double dre = 0.0, dim = 0.0, hh = 0.0;
+  if (r.valid) {
+    double fp[D], fx[D], w2[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      fp[d] = r.fp[d];
+      fx[d] = r.fx[d];
+      w2[d] = 2.0 * kPi * r.dt[d];
+    }
+    const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+    const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+    const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+    const double ci = r.cos_i, pfac = (1.0 + ci * ci) / 2.0;
+    for (int base = 0; base < nB; base += 31) {
+      const int e = base + lane;
+      double rr[D], ri[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) rr[d] = ri[d] = 0.0;
+      if (e < nE) {
+        const double f = a.rb_freq[e];
+        double hpr = 0.0, hpi = 0.0, hxr = 0.0, hxi = 0.0;
+        if (tf2) {
+          if (f >= a.fmin && f < r.f_isco) {
+            const double4 t = a.ftab[a.rb_index[e]];
+            const double v = u * t.x, lnv = lnu + t.y;
+            double sm = r.a[7];
+#pragma unroll
+            for (int q = 6; q >= 0; --q) sm = sm * v + r.a[q];
+            const double v5 = v * v * v * v * v;
+            sm = sm + lnv * (r.l[5] + r.l[6] * v) * v5;
+            const double psi = (-2.0 * r.phase - kPi / 4) + pu5 * sm * t.z;
+            const double amp = r.amp * t.w;
+            double sp, cp;
+            sincos(psi, &sp, &cp);
+            const double ere = amp * cp, eim = -amp * sp;
+            hpr = pfac * ere;
+            hpi = pfac * eim;
+            hxr = ci * eim;
+            hxi = -ci * ere;
+          }
+        } else {
+          // source.py:1199-1207
+          const double pi2 = 9.869604401089358;
+          const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
+          const double neg = exp(-(fm * fm) * pi2 * r.a[3]);
+          const double pos = exp(-(fpl * fpl) * pi2 * r.a[3]);
+          hpr = r.a[0] * (neg + pos) / r.a[1];
+          hxi = -(r.a[0] * (neg - pos) / r.a[2]);
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          // interferometer.py:341-362 at explicit frequencies (no mask)
+          const double sre = hpr * fp[d] + hxr * fx[d];
+          const double sim = hpi * fp[d] + hxi * fx[d];
+          double sn, cs;
+          sincos(w2[d] * f, &sn, &cs);
+          const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+          const double2 g = a.rb_h0inv[d][e];
+          rr[d] = hre * g.x - him * g.y;
+          ri[d] = hre * g.y + him * g.x;
+        }
+      }
+      const bool bin = lane < 31 && e < nB;
+      const double width = bin ? a.rb_freq[e + 1] - a.rb_freq[e] : 1.0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double nr = __shfl_down_sync(0xffffffffu, rr[d], 1);
+        const double ni = __shfl_down_sync(0xffffffffu, ri[d], 1);
+        if (bin) {
+          const double r0r = (nr + rr[d]) / 2, r0i = (ni + ri[d]) / 2;
+          const double r1r = (nr - rr[d]) / width, r1i = (ni - ri[d]) / width;
+          const double* sd = a.rb_sum[d] + (size_t)e * 6;
+          const double a0r = sd[0], a0i = sd[1], a1r = sd[2], a1i = sd[3], b0 = sd[4], b1 = sd[5];
+          dre += a0r * r0r + a0i * r0i + a1r * r1r + a1i * r1i;
+          dim += a0i * r0r - a0r * r0i + a1i * r1r - a1r * r1i;
+          hh += b0 * (r0r * r0r + r0i * r0i) + 2.0 * b1 * (r0r * r1r + r0i * r1i);
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      dre += __shfl_xor_sync(0xffffffffu, dre, off);
+      dim += __shfl_xor_sync(0xffffffffu, dim, off);
+      hh += __shfl_xor_sync(0xffffffffu, hh, off);
+    }
+  }
+  if (lane == 0) finish_point(a, r, i, dre, dim, hh);
 }
 
 __global__ void k_finalize(LaunchArgs a) {
@@ -1109,6 +1222,12 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const int threads = kPointThreads;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s) {
+  const unsigned grid = (unsigned)((a.B + kRelbinWarps - 1) / kRelbinWarps);
+  GWL_DISPATCH_D(k_relbin, grid, 32 * kRelbinWarps, 0, s, a);
   return cudaGetLastError();
 }
 

@@ -38,6 +38,17 @@ def taylorf2_aligned(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_d
     return {"plus": plus, "cross": cross}
 
 
+def taylorf2_aligned_relative_binning(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
+                                      theta_jn, phase, **kwargs):
+    """``taylorf2_aligned`` with bilby's relative-binning source convention
+    (bilby/gw/source.py:724-761): ``fiducial=1`` evaluates on the full grid,
+    otherwise on the ``frequency_bin_edges`` waveform argument."""
+    fiducial = kwargs.pop("fiducial", 0)
+    edges = kwargs.pop("frequency_bin_edges", None)
+    grid = frequency_array if (fiducial == 1 or edges is None) else edges
+    return taylorf2_aligned(grid, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
+
+
 def model_of(source_model) -> str:
     """Which fused kernel serves ``source_model`` ('sinegaussian' | 'taylorf2').
 
@@ -47,7 +58,8 @@ def model_of(source_model) -> str:
     module = getattr(source_model, "__module__", "") or ""
     if source_model is sinegaussian or (name == "sinegaussian" and module.endswith("gw.source")):
         return "sinegaussian"
-    if source_model is taylorf2_aligned or name == "taylorf2_aligned":
+    if source_model in (taylorf2_aligned, taylorf2_aligned_relative_binning) or name in (
+            "taylorf2_aligned", "taylorf2_aligned_relative_binning"):
         return "taylorf2"
     raise NotImplementedError(
         f"source model {module}.{name} has no GPU kernel (supported: sinegaussian, taylorf2_aligned)")

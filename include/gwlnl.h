@@ -234,6 +234,20 @@ int gwl_eval_device_noalloc(gwl_analysis *a, const double *params, int64_t B, do
 int gwl_set_profiling(gwl_analysis *a, int enable);
 int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
 
+/* Relative binning (replaces the per-evaluation part of
+ * RelativeBinningGravitationalWaveTransient, bilby/gw/likelihood/relative.py:
+ * calculate_snrs 365-402 through compute_waveform_ratio_per_interferometer;
+ * the bins and summary data of setup_bins 178-230 and compute_summary_data
+ * 319-363 are computed by the caller).  With it enabled, every evaluation of
+ * this analysis evaluates the model at the n_edges bin edges (increasing
+ * grid indices edge_index), forms the ratio to the fiducial response through
+ * h0_inverse ([n_det][n_edges][2]: 1 / h0_d(f_e), re/im) and sums the per-bin
+ * summary data ([n_det][n_edges - 1][6]: a0 re, a0 im, a1 re, a1 im, b0, b1)
+ * in float64 for either precision.  Phase and distance marginalisation
+ * apply; time marginalisation is refused (GWL_ERR_UNSUPPORTED). */
+int gwl_set_relative_binning(gwl_analysis *a, int enable, int32_t n_edges, const int64_t *edge_index,
+                             const double *h0_inverse, const double *summary);
+
 /* Autotuner (no counterpart in the reference, which has no launch shapes):
  * times the mixed-precision TaylorF2 launch sequence on the caller's B device
  * points for each split-K depth (chunks of 512 bins walked by one CTA; 2, 3,

@@ -131,3 +131,16 @@ def taylorf2_aligned(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_d
     plus[band] = amp * (1.0 + ci * ci) / 2.0 * e
     cross[band] = -1j * amp * ci * e
     return {"plus": plus, "cross": cross}
+
+
+def taylorf2_aligned_relative_binning(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
+                                      theta_jn, phase, **kwargs):
+    """The same model with the relative-binning source convention of bilby
+    (bilby/gw/source.py:724-761): ``fiducial=1`` evaluates on the full grid,
+    otherwise on ``frequency_bin_edges`` from the waveform arguments."""
+    fiducial = kwargs.pop("fiducial", 0)
+    edges = kwargs.pop("frequency_bin_edges", None)
+    if fiducial == 1 or edges is None:
+        return taylorf2_aligned(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
+                                theta_jn, phase, **kwargs)
+    return taylorf2_aligned(edges, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)

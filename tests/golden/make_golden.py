@@ -20,6 +20,10 @@ Outputs
     Prior draws and the reference's ``log_likelihood_ratio`` for each draw,
     the reference's ``noise_log_likelihood``, and a checksum of the strain it
     generated, so a test can check that the oracle regenerates the same data.
+``tests/golden/tf2_128s_relbin.npz``
+    The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
+    (fiducial = the injection): its bin edges, summary data and lnL ratios
+    without marginalisation, with phase and with distance marginalisation.
 """
 from __future__ import annotations
 
@@ -36,7 +40,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import ref_harness  # noqa: E402
-from oracle.taylorf2 import taylorf2_aligned  # noqa: E402
+from oracle.taylorf2 import taylorf2_aligned, taylorf2_aligned_relative_binning  # noqa: E402
 from bilby_gb300.workloads import WORKLOADS, DISTANCE_PRIOR, draw_points, point  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -145,6 +149,50 @@ def run_marginalised(bilby, name, n_points):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
+RELBIN_COMBOS = ["none", "p", "d"]
+
+
+def run_relbin(bilby, name, n_fixed, n_random):
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 1)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    n = n_fixed + n_random
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in RELBIN_COMBOS:
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_relative_binning,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+        p, d = "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, False, p, d)
+        like = bilby.gw.likelihood.RelativeBinningGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, fiducial_parameters=dict(w.injection),
+            priors=priors if (p or d) else None, phase_marginalization=p, distance_marginalization=d)
+        t0 = time.perf_counter()
+        vals = []
+        for i in range(n):
+            q = point(params, i)
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} relbin[{combo}]: {like.number_of_bins} bins, "
+              f"{(time.perf_counter() - t0) / n * 1e3:.2f} ms/eval")
+        if combo == "none":
+            out["bin_inds"] = like.bin_inds
+            out["bin_freqs"] = like.bin_freqs
+            for q, ifo in enumerate(ifos):
+                a0, a1, b0, b1 = like.summary_data[ifo.name]
+                out[f"summary_{q}"] = np.stack([a0, a1, b0, b1])
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}_relbin.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -164,8 +212,18 @@ def known_answer(bilby):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--relbin-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.relbin_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_relbin(bilby, "tf2_128s", 8, 8)
+            finally:
+                os.chdir(cwd)
+        return
     export_noise_curves()
     known_answer(bilby)
     run_plain(bilby, "sg_4s", 32, 32)
@@ -176,6 +234,7 @@ def main():
             os.chdir(tmp)  # the reference caches its distance table in the working directory
             try:
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
+                run_relbin(bilby, "tf2_128s", 8, 8)
             finally:
                 os.chdir(cwd)
 
