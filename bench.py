@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--n-analyses", type=int, default=64)
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
+    ap.add_argument("--no-multiband", action="store_true", help="skip the multi-banding workload")
     return ap.parse_args()
 
 
@@ -277,6 +278,44 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
             "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
             "precision": "fp64", "setup_s": setup_s,
             "launch": "prologue + one warp per point over the bin edges"}
+
+
+def bench_multiband(name, steps, warmup, batch=16384, seed=37):
+    """Multi-banding (bilby/gw/likelihood/multiband.py, linear interpolation
+    of <h|h>) on the GPU: reference chirp mass 0.87 (the 1+1 Msun prior
+    corner); float64 throughout."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    from bilby_gb300.workloads import WORKLOADS, draw_points
+    w = WORKLOADS[name]
+    base = build_likelihood(w, precision="fp64")
+    t0 = time.perf_counter()
+    like = MBGravitationalWaveTransient(base.interferometers, base.waveform_generator, reference_chirp_mass=0.87)
+    setup_s = time.perf_counter() - t0
+    an = like.analysis
+    rng = np.random.default_rng(seed)
+    blocks = [torch.from_numpy(params_block(draw_points(w, batch, rng))).cuda() for _ in range(2)]
+    out = torch.empty(batch, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for s in range(warmup):
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return {"workload": name, "bands": int(like.number_of_bands),
+            "banded_frequencies": int(len(like.banded_frequency_points)), "batch": batch,
+            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+            "precision": "fp64", "setup_s": setup_s,
+            "launch": "prologue + one warp per point over the banded frequencies"}
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
@@ -571,6 +610,10 @@ def run_ours(args, rank, world, local):
     if world == 1 and not args.no_relbin:
         relbin = bench_relbin("tf2_128s", max(3, args.steps // 2), args.warmup)
 
+    multiband = None
+    if world == 1 and not args.no_multiband:
+        multiband = bench_multiband("tf2_128s", max(3, args.steps // 4), args.warmup)
+
     marg = None
     if world == 1 and not args.no_marg:
         marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup)
@@ -628,6 +671,8 @@ def run_ours(args, rank, world, local):
             line["marginalized"] = marg
         if relbin is not None:
             line["relative_binning"] = relbin
+        if multiband is not None:
+            line["multiband"] = multiband
         if uneven is not None:
             line["uneven"] = uneven
         if served is not None:

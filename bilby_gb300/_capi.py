@@ -88,6 +88,10 @@ SIGNATURES = {
     "gwl_set_relative_binning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32,
                                                 ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                                 ctypes.POINTER(ctypes.c_double)]),
+    "gwl_set_multiband": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                         ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.POINTER(ctypes.c_double)]),
     "gwl_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                     ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)]),
     "gwl_get_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),

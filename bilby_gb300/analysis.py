@@ -131,6 +131,32 @@ class Analysis:
             _capi.dptr(sm)), "gwl_set_relative_binning")
         self.relative_binning = True
 
+    def set_multiband(self, enable: bool, frequencies=None, linear=None, quadratic=None, band_start=None,
+                      band_df=None):
+        """Multi-banding: ``frequencies`` [K] banded frequencies, ``linear``
+        [n_det, K] complex and ``quadratic`` [n_det, K] real coefficients;
+        band b holds frequencies [band_start[b], band_start[b + 1]) spaced by
+        band_df[b]."""
+        if not enable:
+            _capi.check(self._lib.gwl_set_multiband(self._h, 0, 0, None, None, None, 0, None, None),
+                        "gwl_set_multiband")
+            self.multiband = False
+            return
+        f = np.ascontiguousarray(frequencies, dtype=np.float64)
+        lin = np.ascontiguousarray(np.asarray(linear, dtype=np.complex128).view(np.float64))
+        quad = np.ascontiguousarray(quadratic, dtype=np.float64)
+        if lin.size != 2 * self.n_detectors * len(f) or quad.size != self.n_detectors * len(f):
+            raise ValueError("multi-banding coefficients do not match the detectors and banded frequencies")
+        bs = np.ascontiguousarray(band_start, dtype=np.int64)
+        bd = np.ascontiguousarray(band_df, dtype=np.float64)
+        if len(bs) != len(bd) + 1:
+            raise ValueError("band_start needs one more entry than band_df")
+        _capi.check(self._lib.gwl_set_multiband(self._h, 1, len(f), _capi.dptr(f), _capi.dptr(lin),
+                                                _capi.dptr(quad), len(bd),
+                                                bs.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _capi.dptr(bd)),
+                    "gwl_set_multiband")
+        self.multiband = True
+
     # -- queries -----------------------------------------------------------
     def noise_log_likelihood(self) -> float:
         out = ctypes.c_double()

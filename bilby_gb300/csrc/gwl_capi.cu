@@ -85,6 +85,16 @@ struct gwl_analysis {
   double* rb_freq = nullptr;
   double2* rb_h0inv[kMaxDet] = {};
   double* rb_sum[kMaxDet] = {};
+  // multi-banding
+  int multiband = 0;
+  int64_t mb_points = 0;
+  double* mb_freq = nullptr;
+  double4* mb_pow = nullptr;
+  double2* mb_lin[kMaxDet] = {};
+  double* mb_quad[kMaxDet] = {};
+  int mb_bands = 0;
+  int64_t* mb_band_start = nullptr;
+  double* mb_band_df = nullptr;
   // work space
   int chunks_per_group = kChunksPerGroup;  // split-K depth of the TaylorF2 mixed kernel (gwl_autotune)
   int64_t ws_B = 0;
@@ -285,6 +295,17 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.rb_h0inv[d] = a->rb_h0inv[d];
     L.rb_sum[d] = a->rb_sum[d];
   }
+  L.multiband = a->multiband;
+  L.mb_points = a->mb_points;
+  L.mb_freq = a->mb_freq;
+  L.mb_pow = a->mb_pow;
+  for (int d = 0; d < a->n_det; ++d) {
+    L.mb_lin[d] = a->mb_lin[d];
+    L.mb_quad[d] = a->mb_quad[d];
+  }
+  L.mb_bands = a->mb_bands;
+  L.mb_band_start = a->mb_band_start;
+  L.mb_band_df = a->mb_band_df;
   return L;
 }
 
@@ -331,11 +352,16 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.dh_out = d_dh;
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
-  if (a->relbin) {
-    // relative binning: per-point set-up, then one warp per point over the bins
+  if (a->relbin || a->multiband) {
+    // relative binning / multi-banding: per-point set-up, then one warp per
+    // point over the bin edges or banded frequencies
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
-    GWL_CUDA(launch_relbin(L, s));
+    if (a->relbin) {
+      GWL_CUDA(launch_relbin(L, s));
+    } else {
+      GWL_CUDA(launch_multiband(L, s));
+    }
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
       a->ev_pending = 1;
@@ -383,9 +409,9 @@ namespace gwl {
 // entry point that supplies its own work space; also the bytes it needs for
 // the per-point records and the partial sums.  Allocates nothing.
 int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes) {
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband) {
     set_error("the allocation-free entry point serves mixed-precision TaylorF2 analyses without time "
-              "marginalisation or relative binning");
+              "marginalisation, relative binning or multi-banding");
     return GWL_ERR_UNSUPPORTED;
   }
   *L = make_args(a, B, GWL_PRECISION_MIXED);
@@ -728,7 +754,7 @@ int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream,
   }
   std::lock_guard<std::mutex> g(a->mu);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband) {
     // nothing to tune: the other launch shapes are fixed
     if (chunks_per_group) *chunks_per_group = a->chunks_per_group;
     if (best_ms) *best_ms = 0.0;
@@ -820,8 +846,8 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
-    if (a->relbin) {
-      set_error("time marginalisation is not available with relative binning");
+    if (a->relbin || a->multiband) {
+      set_error("time marginalisation is not available with relative binning or multi-banding");
       return GWL_ERR_UNSUPPORTED;
     }
   }
@@ -885,8 +911,8 @@ int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const
     a->relbin = 0;
     return GWL_OK;
   }
-  if (a->time_marg) {
-    set_error("time marginalisation is not available with relative binning");
+  if (a->time_marg || a->multiband) {
+    set_error("relative binning excludes time marginalisation and multi-banding");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_edges < 2 || !edge_index || !h0_inverse || !summary) {
@@ -916,6 +942,69 @@ int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const
   }
   a->rb_edges = n_edges;
   a->relbin = 1;
+  return GWL_OK;
+}
+
+int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const double* frequencies,
+                      const double* linear, const double* quadratic, int32_t n_bands, const int64_t* band_start,
+                      const double* band_df) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!enable) {
+    a->multiband = 0;
+    return GWL_OK;
+  }
+  if (a->time_marg || a->relbin) {
+    set_error("multi-banding excludes time marginalisation and relative binning");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  if (n_points < 1 || !frequencies || !linear || !quadratic || n_bands < 1 || !band_start || !band_df) {
+    set_error("multi-banding needs the banded frequencies, both coefficient sets and the band layout");
+    return GWL_ERR_ARGUMENT;
+  }
+  for (int32_t b = 0; b < n_bands; ++b) {
+    if (band_start[b] < 0 || band_start[b + 1] < band_start[b] || band_start[b + 1] > n_points ||
+        !(band_df[b] > 0)) {
+      set_error("band layout must be increasing start indices within the banded frequencies, positive spacings");
+      return GWL_ERR_ARGUMENT;
+    }
+    // the frequencies of a band must be uniform with its spacing (the kernel rotates from point to point)
+    for (int64_t k = band_start[b] + 1; k < band_start[b + 1]; ++k) {
+      const double step = frequencies[k] - frequencies[k - 1];
+      if (std::fabs(step - band_df[b]) > 1e-9 * band_df[b]) {
+        set_error("the frequencies of a band must be uniformly spaced by its spacing");
+        return GWL_ERR_ARGUMENT;
+      }
+    }
+  }
+  std::vector<double> fr(frequencies, frequencies + n_points);
+  std::vector<double4> pw(n_points, make_double4(0.0, 0.0, 0.0, 0.0));
+  for (int64_t k = 0; k < n_points; ++k) {
+    const double x = fr[k];
+    if (!(x > 0) || !std::isfinite(x)) continue;
+    pw[k] = make_double4(std::cbrt(x), std::log(x) / 3.0, std::pow(x, -5.0 / 3.0), std::pow(x, -7.0 / 6.0));
+  }
+  int rc;
+  if ((rc = upload(a, &a->mb_freq, fr))) return rc;
+  if ((rc = upload(a, &a->mb_pow, pw))) return rc;
+  for (int d = 0; d < a->n_det; ++d) {
+    std::vector<double2> lin(n_points);
+    for (int64_t k = 0; k < n_points; ++k)
+      lin[k] = make_double2(linear[((size_t)d * n_points + k) * 2], linear[((size_t)d * n_points + k) * 2 + 1]);
+    std::vector<double> quad(quadratic + (size_t)d * n_points, quadratic + (size_t)(d + 1) * n_points);
+    if ((rc = upload(a, &a->mb_lin[d], lin))) return rc;
+    if ((rc = upload(a, &a->mb_quad[d], quad))) return rc;
+  }
+  std::vector<int64_t> bs(band_start, band_start + n_bands + 1);
+  std::vector<double> bd(band_df, band_df + n_bands);
+  if ((rc = upload(a, &a->mb_band_start, bs))) return rc;
+  if ((rc = upload(a, &a->mb_band_df, bd))) return rc;
+  a->mb_bands = n_bands;
+  a->mb_points = n_points;
+  a->multiband = 1;
   return GWL_OK;
 }
 
@@ -1124,7 +1213,8 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
       return GWL_ERR_ARGUMENT;
     }
     const gwl_analysis* a = it.analysis;
-    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->n_det > kMultiMaxDet) fused = false;
+    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband || a->n_det > kMultiMaxDet)
+      fused = false;
   }
   if (!fused) {
     // other models / precisions / time marginalisation: one launch sequence per item

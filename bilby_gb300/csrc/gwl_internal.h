@@ -110,6 +110,17 @@ struct LaunchArgs {
   const double* rb_freq;                // [rb_edges] edge frequencies
   const double2* rb_h0inv[kMaxDet];     // [rb_edges] 1 / h0_d(f_e)
   const double* rb_sum[kMaxDet];        // [rb_edges - 1][6]: a0 re, a0 im, a1 re, a1 im, b0, b1
+  // multi-banding: the model at the banded frequencies, weighted by the
+  // per-detector linear (complex) and quadratic (real) coefficients
+  int multiband;
+  int64_t mb_points;
+  const double* mb_freq;                // [mb_points] banded frequencies
+  const double4* mb_pow;                // [mb_points] {f^(1/3), ln(f) / 3, f^(-5/3), f^(-7/6)}
+  const double2* mb_lin[kMaxDet];       // [mb_points]
+  const double* mb_quad[kMaxDet];       // [mb_points]
+  int mb_bands;
+  const int64_t* mb_band_start;         // [mb_bands + 1] first banded index of each band (and the end)
+  const double* mb_band_df;             // [mb_bands] frequency spacing of each band
 };
 
 // A batch over several analyses evaluated by one persistent launch: per item
@@ -137,6 +148,7 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);

@@ -1138,6 +1138,120 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_relbin(LaunchArgs a) {
   if (lane == 0) finish_point(a, r, i, dre, dim, hh);
 }
 
+// The float64 TaylorF2 or sine-Gaussian polarisations at one frequency, the
+// TaylorF2 powers of f from a table entry t.
+struct PointModel {
+  bool tf2;
+  double u, lnu, pu5, ci, pfac;
+};
+
+__device__ __forceinline__ PointModel point_model(const LaunchArgs& a, const PointRec& r) {
+  PointModel m;
+  m.tf2 = a.model == GWL_MODEL_TAYLORF2;
+  m.u = m.tf2 ? cbrt(kPi * r.m_sec) : 0.0;
+  m.lnu = m.tf2 ? log(m.u) : 0.0;
+  m.pu5 = m.tf2 ? 3.0 / (128.0 * r.eta) / (m.u * m.u * m.u * m.u * m.u) : 0.0;
+  m.ci = r.cos_i;
+  m.pfac = (1.0 + m.ci * m.ci) / 2.0;
+  return m;
+}
+
+__device__ __forceinline__ void model_at(const LaunchArgs& a, const PointRec& r, const PointModel& m, double f,
+                                         const double4& t, double& hpr, double& hpi, double& hxr, double& hxi) {
+  hpr = hpi = hxr = hxi = 0.0;
+  if (m.tf2) {
+    if (f >= a.fmin && f < r.f_isco) {
+      const double v = m.u * t.x, lnv = m.lnu + t.y;
+      double sm = r.a[7];
+#pragma unroll
+      for (int q = 6; q >= 0; --q) sm = sm * v + r.a[q];
+      const double v5 = v * v * v * v * v;
+      sm = sm + lnv * (r.l[5] + r.l[6] * v) * v5;
+      const double psi = (-2.0 * r.phase - kPi / 4) + m.pu5 * sm * t.z;
+      const double amp = r.amp * t.w;
+      double sp, cp;
+      sincos(psi, &sp, &cp);
+      const double ere = amp * cp, eim = -amp * sp;
+      hpr = m.pfac * ere;
+      hpi = m.pfac * eim;
+      hxr = m.ci * eim;
+      hxi = -m.ci * ere;
+    }
+  } else {
+    const double pi2 = 9.869604401089358;
+    const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
+    const double neg = exp(-(fm * fm) * pi2 * r.a[3]);
+    const double pos = exp(-(fpl * fpl) * pi2 * r.a[3]);
+    hpr = r.a[0] * (neg + pos) / r.a[1];
+    hxi = -(r.a[0] * (neg - pos) / r.a[2]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// multi-banding (bilby/gw/likelihood/multiband.py:741-819, linear
+// interpolation of <h|h>): one warp per point, lanes striding over the banded
+// frequencies; <d|h> = conj(sum_k s_k L_k), <h|h> = sum_k |s_k|^2 Q_k with the
+// detector response s_k at banded frequency k.  float64 throughout.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband(LaunchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kRelbinWarps + (threadIdx.x >> 5);
+  if (i >= a.B) return;  // uniform over the warp
+  const PointRec& r = a.rec[i];
+  double sr = 0.0, si = 0.0, hh = 0.0;
+  if (r.valid) {
+    double fp[D], fx[D], w2[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      fp[d] = r.fp[d];
+      fx[d] = r.fx[d];
+      w2[d] = 2.0 * kPi * r.dt[d];
+    }
+    const PointModel m = point_model(a, r);
+    // inside a band the banded frequencies are uniform (spacing df_b): this
+    // lane's e^{i w f} advances by e^{i w 32 df_b} from point to point
+    for (int b = 0; b < a.mb_bands; ++b) {
+      const int64_t k0 = a.mb_band_start[b] + lane, k1 = a.mb_band_start[b + 1];
+      if (k0 >= k1) continue;
+      double zc[D], zs[D], rc[D], rs[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        sincos(w2[d] * a.mb_freq[k0], &zs[d], &zc[d]);
+        sincos(w2[d] * (32.0 * a.mb_band_df[b]), &rs[d], &rc[d]);
+      }
+      for (int64_t k = k0; k < k1; k += 32) {
+        const double f = a.mb_freq[k];
+        double hpr, hpi, hxr, hxi;
+        model_at(a, r, m, f, a.mb_pow[k], hpr, hpi, hxr, hxi);
+        if (hpr != 0.0 || hpi != 0.0 || hxr != 0.0 || hxi != 0.0) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const double sre = hpr * fp[d] + hxr * fx[d];
+            const double sim = hpi * fp[d] + hxi * fx[d];
+            const double sn = zs[d], cs = zc[d];
+            const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+            const double2 L = a.mb_lin[d][k];
+            sr += hre * L.x - him * L.y;
+            si += hre * L.y + him * L.x;
+            hh += (hre * hre + him * him) * a.mb_quad[d][k];
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) rotate(zc[d], zs[d], rc[d], rs[d]);
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, off);
+      si += __shfl_xor_sync(0xffffffffu, si, off);
+      hh += __shfl_xor_sync(0xffffffffu, hh, off);
+    }
+  }
+  // <d|h> = conj(sum s L)
+  if (lane == 0) finish_point(a, r, i, sr, -si, hh);
+}
+
 __global__ void k_finalize(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.B) return;
@@ -1222,6 +1336,12 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const int threads = kPointThreads;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s) {
+  const unsigned grid = (unsigned)((a.B + kRelbinWarps - 1) / kRelbinWarps);
+  GWL_DISPATCH_D(k_multiband, grid, 32 * kRelbinWarps, 0, s, a);
   return cudaGetLastError();
 }
 

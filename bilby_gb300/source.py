@@ -49,6 +49,16 @@ def taylorf2_aligned_relative_binning(frequency_array, mass_1, mass_2, chi_1, ch
     return taylorf2_aligned(grid, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
 
 
+def taylorf2_aligned_frequency_sequence(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
+                                        theta_jn, phase, **kwargs):
+    """``taylorf2_aligned`` on the ``frequencies`` waveform argument, the
+    convention of bilby's frequency-sequence source models used by the
+    multi-banded likelihood (bilby/gw/likelihood/multiband.py:451-481)."""
+    frequencies = kwargs.pop("frequencies", None)
+    grid = frequency_array if frequencies is None else frequencies
+    return taylorf2_aligned(grid, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
+
+
 def model_of(source_model) -> str:
     """Which fused kernel serves ``source_model`` ('sinegaussian' | 'taylorf2').
 
@@ -58,8 +68,8 @@ def model_of(source_model) -> str:
     module = getattr(source_model, "__module__", "") or ""
     if source_model is sinegaussian or (name == "sinegaussian" and module.endswith("gw.source")):
         return "sinegaussian"
-    if source_model in (taylorf2_aligned, taylorf2_aligned_relative_binning) or name in (
-            "taylorf2_aligned", "taylorf2_aligned_relative_binning"):
+    if source_model in (taylorf2_aligned, taylorf2_aligned_relative_binning, taylorf2_aligned_frequency_sequence) \
+            or name in ("taylorf2_aligned", "taylorf2_aligned_relative_binning", "taylorf2_aligned_frequency_sequence"):
         return "taylorf2"
     raise NotImplementedError(
         f"source model {module}.{name} has no GPU kernel (supported: sinegaussian, taylorf2_aligned)")

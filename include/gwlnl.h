@@ -248,6 +248,21 @@ int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
 int gwl_set_relative_binning(gwl_analysis *a, int enable, int32_t n_edges, const int64_t *edge_index,
                              const double *h0_inverse, const double *summary);
 
+/* Multi-banding (replaces MBGravitationalWaveTransient.calculate_snrs with
+ * linear interpolation of <h|h>, bilby/gw/likelihood/multiband.py:741-819;
+ * the bands and coefficients of setup_multibanding 317-640 are computed by
+ * the caller).  With it enabled, every evaluation of this analysis evaluates
+ * the model at the n_points banded frequencies, projects it on each detector
+ * and forms <d|h> = conj(sum_k s_k L_k) and <h|h> = sum_k |s_k|^2 Q_k with
+ * linear ([n_det][n_points][2], complex) and quadratic ([n_det][n_points])
+ * coefficients, in float64 for either precision.  The banded frequencies
+ * come in n_bands runs: band b holds indices [band_start[b], band_start[b+1])
+ * uniformly spaced by band_df[b] (1 / T^(b)).  Phase and distance
+ * marginalisation apply; time marginalisation is refused. */
+int gwl_set_multiband(gwl_analysis *a, int enable, int64_t n_points, const double *frequencies,
+                      const double *linear, const double *quadratic, int32_t n_bands, const int64_t *band_start,
+                      const double *band_df);
+
 /* Autotuner (no counterpart in the reference, which has no launch shapes):
  * times the mixed-precision TaylorF2 launch sequence on the caller's B device
  * points for each split-K depth (chunks of 512 bins walked by one CTA; 2, 3,

@@ -144,3 +144,14 @@ def taylorf2_aligned_relative_binning(frequency_array, mass_1, mass_2, chi_1, ch
         return taylorf2_aligned(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
                                 theta_jn, phase, **kwargs)
     return taylorf2_aligned(edges, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
+
+
+def taylorf2_aligned_frequency_sequence(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance,
+                                        theta_jn, phase, **kwargs):
+    """The same model on the ``frequencies`` waveform argument, the convention
+    of bilby's frequency-sequence source models used by the multi-banded
+    likelihood (bilby/gw/source.py, ``binary_black_hole_frequency_sequence``;
+    bilby/gw/likelihood/multiband.py:437-439)."""
+    frequencies = kwargs.pop("frequencies")
+    return taylorf2_aligned(frequencies, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                            **kwargs)

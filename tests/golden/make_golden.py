@@ -20,6 +20,11 @@ Outputs
     Prior draws and the reference's ``log_likelihood_ratio`` for each draw,
     the reference's ``noise_log_likelihood``, and a checksum of the strain it
     generated, so a test can check that the oracle regenerates the same data.
+``tests/golden/tf2_128s_multiband.npz``
+    The reference's ``MBGravitationalWaveTransient`` on tf2_128s (reference
+    chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
+    frequencies, linear and quadratic coefficients and lnL ratios without
+    marginalisation, with phase and with distance marginalisation.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -40,7 +45,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import ref_harness  # noqa: E402
-from oracle.taylorf2 import taylorf2_aligned, taylorf2_aligned_relative_binning  # noqa: E402
+from oracle.taylorf2 import (taylorf2_aligned, taylorf2_aligned_frequency_sequence,  # noqa: E402
+                             taylorf2_aligned_relative_binning)
 from bilby_gb300.workloads import WORKLOADS, DISTANCE_PRIOR, draw_points, point  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -193,6 +199,54 @@ def run_relbin(bilby, name, n_fixed, n_random):
     np.savez_compressed(os.path.join(HERE, f"{name}_relbin.npz"), **out)
 
 
+MB_KEYS = ["durations", "fb_dfb", "Nbs", "Mbs", "Ks_Ke", "banded_frequency_points", "start_end_idxs",
+           "unique_to_original_frequencies"]
+
+
+def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 2)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    n = n_fixed + n_random
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in RELBIN_COMBOS:
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_frequency_sequence,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+        p, d = "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, False, p, d)
+        like = bilby.gw.likelihood.MBGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, reference_chirp_mass=reference_chirp_mass,
+            priors=priors if (p or d) else None, phase_marginalization=p, distance_marginalization=d)
+        t0 = time.perf_counter()
+        vals = []
+        for i in range(n):
+            q = point(params, i)
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} multiband[{combo}]: {len(like.banded_frequency_points)} banded points, "
+              f"{(time.perf_counter() - t0) / n * 1e3:.2f} ms/eval")
+        if combo == "none":
+            for key in MB_KEYS:
+                out["mb_" + key] = np.asarray(getattr(like, key))
+            for key in ("time_offset", "delta_f_end", "maximum_banding_frequency"):
+                out["mb_" + key] = float(getattr(like, key))
+            out["mb_waveform_frequencies"] = np.asarray(wfg.waveform_arguments["frequencies"])
+            for q, ifo in enumerate(ifos):
+                out[f"mb_linear_coeffs_{q}"] = np.asarray(like.linear_coeffs[ifo.name])
+                out[f"mb_quadratic_coeffs_{q}"] = np.asarray(like.quadratic_coeffs[ifo.name])
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}_multiband.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -213,8 +267,18 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--relbin-only", action="store_true")
+    ap.add_argument("--multiband-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.multiband_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_multiband(bilby, "tf2_128s", 8, 8)
+            finally:
+                os.chdir(cwd)
+        return
     if args.relbin_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -235,6 +299,7 @@ def main():
             try:
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
                 run_relbin(bilby, "tf2_128s", 8, 8)
+                run_multiband(bilby, "tf2_128s", 8, 8)
             finally:
                 os.chdir(cwd)
 

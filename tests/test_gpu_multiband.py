@@ -1,0 +1,80 @@
+"""Multi-banding on the GPU against the reference's own MBGravitationalWaveTransient
+(tests/golden/tf2_128s_multiband.npz, written by the reference with the
+oracle's TaylorF2 as its source model): lnL ratios without marginalisation,
+with phase and with distance marginalisation; batch equals single; the
+unsupported options are refused.
+
+Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
+table, as for the full likelihood)."""
+import numpy as np
+import pytest
+
+from tests.conftest import golden
+from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, point
+
+pytestmark = pytest.mark.gpu
+
+
+def make(combo, tmp_path, **kw):
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    from bilby_gb300.prior import PowerLaw, Uniform
+    from bilby_gb300.source import taylorf2_aligned_frequency_sequence
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    w = WORKLOADS["tf2_128s"]
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned_frequency_sequence,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+    priors = {}
+    if "p" in combo:
+        priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
+    if "d" in combo:
+        priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
+                                                 DISTANCE_PRIOR["maximum"])
+    like = MBGravitationalWaveTransient(ifos, wfg, reference_chirp_mass=0.87, priors=priors or None,
+                                        phase_marginalization="p" in combo, distance_marginalization="d" in combo,
+                                        distance_marginalization_lookup_table=str(tmp_path / "table.npz"), **kw)
+    return like, priors
+
+
+@pytest.mark.parametrize("combo", ["none", "p", "d"])
+def test_lnl_matches_the_reference(gpu, tmp_path, combo):
+    like, priors = make(combo, tmp_path)
+    z = golden("tf2_128s_multiband")
+    assert len(like.banded_frequency_points) == len(z["mb_banded_frequency_points"])
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        pts.append(q)
+    ref = z["lnl_" + combo]
+    single = np.array([like.log_likelihood_ratio(q) for q in pts])
+    batch = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    assert np.array_equal(single, batch)
+    rtol = 1e-8 if "d" in combo else 1e-9
+    assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
+
+
+def test_weights_round_trip(gpu, tmp_path):
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    like, _ = make("none", tmp_path)
+    again = MBGravitationalWaveTransient(like.interferometers, like.waveform_generator, weights=like.weights)
+    z = golden("tf2_128s_multiband")
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    a = like.log_likelihood_ratio_batch(params)
+    b = again.log_likelihood_ratio_batch(params)
+    assert np.array_equal(a, b)
+
+
+def test_unsupported_options_are_refused(gpu, tmp_path):
+    with pytest.raises(NotImplementedError):
+        make("none", tmp_path, linear_interpolation=False)

@@ -1,0 +1,94 @@
+"""Multi-banding without a GPU: the oracle's per-evaluation restatement on the
+reference's own bands and coefficients reproduces the reference's lnL, and the
+product's host set-up (bands, banded frequencies, linear and quadratic
+coefficients; bilby/gw/likelihood/multiband.py:317-601) reproduces the
+reference's arrays on the same data (tests/golden/tf2_128s_multiband.npz)."""
+import numpy as np
+import pytest
+
+from tests.conftest import golden
+from oracle import data as OD
+from oracle import multiband as MB
+from oracle import restate as R
+from bilby_gb300.workloads import WORKLOADS, point
+
+
+@pytest.fixture(scope="module")
+def mb():
+    w = WORKLOADS["tf2_128s"]
+    dets = OD.build_workload(w)
+    z = golden("tf2_128s_multiband")
+    weights = {k[3:]: z[k] for k in z.files if k.startswith("mb_")}
+    return w, dets, z, weights
+
+
+@pytest.mark.parametrize("combo", ["none", "p"])
+def test_oracle_reproduces_the_reference(mb, combo):
+    w, dets, z, weights = mb
+    assert np.allclose(OD.strain_checksum(dets), z["checksum"], rtol=1e-14, atol=0)
+    src = OD.source_for(w.model, w.minimum_frequency)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    marg = R.Marginalization(phase="p" in combo)
+    got = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "p" in combo:
+            q["phase"] = 0.0
+        got.append(MB.log_likelihood_ratio(dets, src, weights, q, marg))
+    ref = z["lnl_" + combo]
+    assert np.all(np.abs(np.array(got) - ref) <= 1e-10 * np.maximum(1.0, np.abs(ref)))
+
+
+class _StrainData:
+    def __init__(self, det, fmin=20.0, fmax=2048.0):
+        self.frequency_array = det.frequency
+        self.frequency_mask = det.mask
+        self.frequency_domain_strain = det.masked_strain
+        self.duration = det.duration
+        self.start_time = det.start_time
+        self.minimum_frequency = fmin
+        self.maximum_frequency = fmax
+
+
+class _Ifo:
+    def __init__(self, det):
+        self.name = det.name
+        self.strain_data = _StrainData(det)
+        self.power_spectral_density_array = det.psd
+        self.minimum_frequency = 20.0
+        self.maximum_frequency = 2048.0
+
+
+class _Gen:
+    def __init__(self):
+        self.waveform_arguments = {}
+
+
+def test_host_setup_reproduces_the_reference(mb):
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    w, dets, z, weights = mb
+    like = object.__new__(MBGravitationalWaveTransient)
+    like.interferometers = [_Ifo(d) for d in dets]
+    like.waveform_generator = _Gen()
+    like._prior = None
+    like.time_reference = "geocent"
+    like.reference_chirp_mass = 0.87
+    like.highest_mode = 2
+    like.linear_interpolation = True
+    like.accuracy_factor = 5
+    like.time_offset = None
+    like.delta_f_end = None
+    like.maximum_banding_frequency = None
+    like.minimum_banding_duration = 0.
+    like.setup_multibanding()
+    assert like.time_offset == weights["time_offset"] and like.delta_f_end == weights["delta_f_end"]
+    assert like.maximum_banding_frequency == weights["maximum_banding_frequency"]
+    for key in ("durations", "fb_dfb", "Nbs", "Mbs", "Ks_Ke", "banded_frequency_points", "start_end_idxs",
+                "unique_to_original_frequencies"):
+        assert np.array_equal(np.asarray(getattr(like, key)), weights[key]), key
+    assert np.array_equal(like.waveform_generator.waveform_arguments["frequencies"], weights["waveform_frequencies"])
+    for q, d in enumerate(dets):
+        lin, ref = like.linear_coeffs[d.name], weights[f"linear_coeffs_{q}"]
+        assert np.max(np.abs(lin - ref)) <= 1e-12 * np.max(np.abs(ref))
+        quad, ref = like.quadratic_coeffs[d.name], weights[f"quadratic_coeffs_{q}"]
+        assert np.max(np.abs(quad - ref)) <= 1e-12 * np.max(np.abs(ref))
