@@ -25,6 +25,9 @@ Outputs
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
     frequencies, linear and quadratic coefficients and lnL ratios without
     marginalisation, with phase and with distance marginalisation.
+``tests/golden/sky_frames.npz``
+    The reference's ``get_sky_frame_parameters`` (base.py:1091-1137) for
+    detector-pair frames and detector time references on random points.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -247,6 +250,33 @@ def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
     np.savez_compressed(os.path.join(HERE, f"{name}_multiband.npz"), **out)
 
 
+FRAME_CASES = [("H1L1", "geocent"), ("H1L1", "H1"), ("sky", "L1"), ("L1V1", "V1")]
+
+
+def run_frames(bilby, n=16):
+    w = WORKLOADS["sg_4s"]
+    rng = np.random.default_rng(77)
+    out = {}
+    pts = dict(zenith=np.arccos(rng.uniform(-1, 1, n)), azimuth=rng.uniform(0, 2 * np.pi, n),
+               ra=rng.uniform(0, 2 * np.pi, n), dec=np.arcsin(rng.uniform(-1, 1, n)),
+               t=w.start_time + rng.uniform(0.5, 3.5, n))
+    out.update({"p_" + k: v for k, v in pts.items()})
+    for q, (frame, tref) in enumerate(FRAME_CASES):
+        ifos, wfg = build_reference(bilby, w, bilby.gw.source.sinegaussian)
+        like = bilby.gw.likelihood.GravitationalWaveTransient(interferometers=ifos, waveform_generator=wfg,
+                                                              reference_frame=frame, time_reference=tref)
+        key = "geocent_time" if "geocent" in tref else f"{tref}_time"
+        res = np.zeros((n, 3))
+        for i in range(n):
+            par = dict(zenith=pts["zenith"][i], azimuth=pts["azimuth"][i], ra=pts["ra"][i], dec=pts["dec"][i])
+            par[key] = pts["t"][i]
+            r = like.get_sky_frame_parameters(par)
+            res[i] = [r["ra"], r["dec"], r["geocent_time"]]
+        out[f"frame_{q}"] = res
+    np.savez_compressed(os.path.join(HERE, "sky_frames.npz"), **out)
+    print("sky frames", len(FRAME_CASES), "cases")
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -268,8 +298,12 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--relbin-only", action="store_true")
     ap.add_argument("--multiband-only", action="store_true")
+    ap.add_argument("--frames-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.frames_only:
+        run_frames(bilby)
+        return
     if args.multiband_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -291,6 +325,7 @@ def main():
     export_noise_curves()
     known_answer(bilby)
     run_plain(bilby, "sg_4s", 32, 32)
+    run_frames(bilby)
     run_plain(bilby, "tf2_128s", 4, 4)
     if not args.quick:
         cwd = os.getcwd()
