@@ -137,6 +137,15 @@ struct MultiArgs {
   int ordered;              // items carry a point ordering (LaunchArgs::order)
 };
 
+// One compiled prior (gwl_priors_create): device copy of a gwl_prior with
+// device table pointers.
+struct PriorEntry {
+  int kind, target, column, table_n;
+  double p[4];
+  const double* x;
+  const double* y;
+};
+
 // Kernel launchers (defined in gwl_kernels.cu / gwl_marg.cu).
 constexpr int kMultiMaxDet = 3;
 constexpr int kMultiClasses = 2 * (kMultiMaxDet + 1);  // kernel class q = 2 * detectors + cplx

@@ -401,6 +401,24 @@ class GravitationalWaveTransient(_Base):
         block = params_block(self._prepare(arrays))
         return self.analysis.log_likelihood_ratio_host(block, precision)
 
+    def log_likelihood_ratio_from_unit_cube(self, unit, device_priors, precision=None, out=None):
+        """lnL ratios of a batch given as unit-cube samples: ``unit`` is a CUDA
+        float64 tensor [len(device_priors.keys), B]; the priors' inverse CDFs and
+        the mass / inclination conversions run on the device
+        (``bilby_gb300.priors_device.DevicePriors``), then the likelihood, all
+        on torch's current stream with no host work per point.  Needs the sky
+        frame and geocentre time (no detector-frame sampling)."""
+        import torch
+        if self._frame is not None or self.time_reference != "geocent":
+            raise NotImplementedError("unit-cube batches need reference_frame='sky' and geocentre time")
+        block = device_priors.rescale(unit)
+        n = block.shape[1]
+        res = out if out is not None else torch.empty(n, dtype=torch.float64, device=block.device)
+        stream = torch.cuda.current_stream(block.device).cuda_stream
+        self.analysis.log_likelihood_ratio_device(block.data_ptr(), n, res.data_ptr(), precision or self.precision,
+                                                  stream)
+        return res
+
     def autotune(self, parameters) -> tuple[int, float]:
         """Choose the mixed kernel's launch shape for batches like ``parameters``
         (a mapping of names to equal-length arrays): returns the chosen

@@ -60,3 +60,53 @@ class DeltaFunction(Prior):
 
     def prob(self, val):
         return np.where(val == self.peak, np.inf, 0.0)
+
+
+class LogUniform(PowerLaw):
+    """analytical.py:265-290: a power law with alpha = -1."""
+
+    def __init__(self, minimum, maximum, **kwargs):
+        super().__init__(-1, minimum, maximum, **kwargs)
+
+
+class Sine(Prior):
+    """analytical.py:450-507: p(x) proportional to sin x on [0, pi] by default."""
+
+    def __init__(self, minimum=0.0, maximum=np.pi, **kwargs):
+        super().__init__(minimum, maximum, **kwargs)
+
+    def rescale(self, val):
+        norm = 1 / (np.cos(self.minimum) - np.cos(self.maximum))
+        return np.arccos(np.cos(self.minimum) - val / norm)
+
+    def prob(self, val):
+        return np.sin(val) / 2 * self.is_in_prior_range(val)
+
+
+class Cosine(Prior):
+    """analytical.py:390-447: p(x) proportional to cos x on [-pi/2, pi/2] by default."""
+
+    def __init__(self, minimum=-np.pi / 2, maximum=np.pi / 2, **kwargs):
+        super().__init__(minimum, maximum, **kwargs)
+
+    def rescale(self, val):
+        norm = 1 / (np.sin(self.maximum) - np.sin(self.minimum))
+        return np.arcsin(val / norm + np.sin(self.minimum))
+
+    def prob(self, val):
+        return np.cos(val) / 2 * self.is_in_prior_range(val)
+
+
+class Gaussian(Prior):
+    """analytical.py:510-576."""
+
+    def __init__(self, mu, sigma, **kwargs):
+        super().__init__(-np.inf, np.inf, **kwargs)
+        self.mu, self.sigma = mu, sigma
+
+    def rescale(self, val):
+        from scipy.special import erfinv
+        return self.mu + erfinv(2 * val - 1) * 2 ** 0.5 * self.sigma
+
+    def prob(self, val):
+        return np.exp(-(self.mu - val) ** 2 / (2 * self.sigma ** 2)) / (2 * np.pi) ** 0.5 / self.sigma

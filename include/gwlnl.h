@@ -263,6 +263,50 @@ int gwl_set_multiband(gwl_analysis *a, int enable, int64_t n_points, const doubl
                       const double *linear, const double *quadratic, int32_t n_bands, const int64_t *band_start,
                       const double *band_df);
 
+/* On-device prior rescaling and parameter conversion for the batch path
+ * (replaces, for the supported priors, PriorDict.rescale, bilby/core/prior/
+ * dict.py, with the inverse CDFs of bilby/core/prior/analytical.py,
+ * interpolated.py and bilby/gw/prior.py, followed by the mass and
+ * inclination conversions of convert_to_lal_binary_black_hole_parameters,
+ * bilby/gw/conversion.py:182-283, 849-990).  A program of n entries maps
+ * unit-cube samples ([n_columns][B], device) to the [GWL_NPARAM][B]
+ * parameter block (device) in one launch; entries with column < 0 are
+ * constants (DeltaFunction). */
+enum {
+  GWL_PRIOR_DELTA = 0,       /* p[0] = peak */
+  GWL_PRIOR_UNIFORM = 1,     /* p = minimum, maximum */
+  GWL_PRIOR_POWERLAW = 2,    /* p = alpha, minimum, maximum (alpha = -1: log-uniform) */
+  GWL_PRIOR_SINE = 3,        /* p = minimum, maximum */
+  GWL_PRIOR_COSINE = 4,      /* p = minimum, maximum */
+  GWL_PRIOR_GAUSSIAN = 5,    /* p = mu, sigma */
+  GWL_PRIOR_TRUNCATED_GAUSSIAN = 6, /* p = mu, sigma, minimum, normalisation */
+  GWL_PRIOR_TABLE_LINEAR = 7,  /* linear interpolation of the inverse CDF: x = CDF grid, y = values */
+  GWL_PRIOR_TABLE_BSPLINE = 8  /* cubic B-spline inverse CDF: x = knots, y = coefficients,
+                                  p = value below / above the knot range, equal-mass folding flag, last x */
+};
+/* Conversion targets beyond the parameter slots. */
+enum {
+  GWL_T_CHIRP_MASS = 100,
+  GWL_T_MASS_RATIO = 101,
+  GWL_T_TOTAL_MASS = 102,
+  GWL_T_COS_THETA_JN = 103
+};
+typedef struct gwl_prior {
+  int32_t kind;          /* GWL_PRIOR_* */
+  int32_t target;        /* a GWL_P_* slot or a GWL_T_* conversion input */
+  int32_t column;        /* unit-cube column, or -1 for a constant */
+  int32_t table_n;       /* table length (GWL_PRIOR_TABLE_*) */
+  double p[4];
+  const double *table_x; /* host arrays, copied by gwl_priors_create */
+  const double *table_y;
+} gwl_prior;
+typedef struct gwl_priors gwl_priors;
+int gwl_priors_create(const gwl_prior *entries, int32_t n, gwl_priors **out);
+int gwl_priors_destroy(gwl_priors *p);
+/* unit: device [n_columns][B]; params: device [GWL_NPARAM][B] (slots without
+ * an entry are left as they are) */
+int gwl_priors_rescale(gwl_priors *p, const double *unit, int64_t B, double *params, void *stream);
+
 /* Autotuner (no counterpart in the reference, which has no launch shapes):
  * times the mixed-precision TaylorF2 launch sequence on the caller's B device
  * points for each split-K depth (chunks of 512 bins walked by one CTA; 2, 3,

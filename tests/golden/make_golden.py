@@ -25,6 +25,10 @@ Outputs
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
     frequencies, linear and quadratic coefficients and lnL ratios without
     marginalisation, with phase and with distance marginalisation.
+``tests/golden/priors.npz``
+    The reference's ``PriorDict.rescale`` of fixed unit-cube samples for the
+    GW prior kinds the device rescaler supports, followed by
+    ``convert_to_lal_binary_black_hole_parameters``.
 ``tests/golden/sky_frames.npz``
     The reference's ``get_sky_frame_parameters`` (base.py:1091-1137) for
     detector-pair frames and detector time references on random points.
@@ -250,6 +254,52 @@ def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
     np.savez_compressed(os.path.join(HERE, f"{name}_multiband.npz"), **out)
 
 
+def run_priors(bilby, n=256):
+    from bilby.core.prior import (Cosine, Gaussian, LogUniform, PowerLaw, PriorDict, Sine, TruncatedGaussian,
+                                  Uniform)
+    from bilby.gw.conversion import convert_to_lal_binary_black_hole_parameters
+    from bilby.gw.prior import AlignedSpin, UniformInComponentsChirpMass, UniformInComponentsMassRatio
+    tc = WORKLOADS["tf2_128s"].injection["geocent_time"]
+    cases = {
+        "a": dict(chirp_mass=UniformInComponentsChirpMass(0.87, 1.74), mass_ratio=UniformInComponentsMassRatio(0.5, 1.0),
+                  chi_1=AlignedSpin(a_prior=Uniform(0, 0.05)), chi_2=Uniform(-0.05, 0.05),
+                  luminosity_distance=PowerLaw(2, 20, 200), dec=Cosine(), ra=Uniform(0, 2 * np.pi),
+                  theta_jn=Sine(), psi=Uniform(0, np.pi), phase=Uniform(0, 2 * np.pi),
+                  geocent_time=Uniform(tc - 0.1, tc + 0.1), hrss=LogUniform(1e-23, 1e-21), Q=Gaussian(10, 2),
+                  frequency=TruncatedGaussian(200, 50, 50, 500)),
+        "b": dict(chirp_mass=UniformInComponentsChirpMass(5, 30),
+                  mass_ratio=UniformInComponentsMassRatio(0.125, 1.0, equal_mass=True),
+                  cos_theta_jn=Uniform(-1, 1), luminosity_distance=PowerLaw(-1, 100, 1000)),
+    }
+    rng = np.random.default_rng(99)
+    out = {}
+    for name, d in cases.items():
+        priors = PriorDict(d)
+        keys = list(priors.keys())
+        u = rng.uniform(size=(len(keys), n))
+        vals = priors.rescale(keys, u)
+        params = {k: np.asarray(v, dtype=np.float64) for k, v in zip(keys, vals)}
+        conv, _ = convert_to_lal_binary_black_hole_parameters(dict(params))
+        out[f"{name}_keys"] = np.array(keys)
+        out[f"{name}_unit"] = u
+        # the device program compiled from the reference's own prior objects
+        from bilby_gb300.priors_device import compile_program
+        prog = compile_program(priors, keys)
+        out[f"{name}_prog_head"] = np.array([[k, t, c] for k, t, c, _, _, _ in prog], dtype=np.int64)
+        out[f"{name}_prog_p"] = np.array([pp for _, _, _, pp, _, _ in prog], dtype=np.float64)
+        for j, (_, _, _, _, tx, ty) in enumerate(prog):
+            if tx is not None:
+                out[f"{name}_prog_tx_{j}"] = tx
+                out[f"{name}_prog_ty_{j}"] = ty
+        for k in keys:
+            out[f"{name}_v_{k}"] = params[k]
+        for k in ("mass_1", "mass_2", "theta_jn"):
+            if k in conv:
+                out[f"{name}_c_{k}"] = np.asarray(conv[k], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "priors.npz"), **out)
+    print("priors", {k: len(v) for k, v in cases.items()})
+
+
 FRAME_CASES = [("H1L1", "geocent"), ("H1L1", "H1"), ("sky", "L1"), ("L1V1", "V1")]
 
 
@@ -299,8 +349,12 @@ def main():
     ap.add_argument("--relbin-only", action="store_true")
     ap.add_argument("--multiband-only", action="store_true")
     ap.add_argument("--frames-only", action="store_true")
+    ap.add_argument("--priors-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.priors_only:
+        run_priors(bilby)
+        return
     if args.frames_only:
         run_frames(bilby)
         return
