@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
     ap.add_argument("--no-multiband", action="store_true", help="skip the multi-banding workload")
+    ap.add_argument("--no-roq", action="store_true", help="skip the ROQ workload")
     return ap.parse_args()
 
 
@@ -316,6 +317,63 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
             "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
             "precision": "fp64", "setup_s": setup_s,
             "launch": "prologue + one warp per point over the banded frequencies"}
+
+
+def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, seed=41):
+    """Reduced-order quadrature on the GPU (bilby/gw/likelihood/roq.py, one
+    basis).  ROQ bases are data files the container does not have, so a
+    seeded random basis of the stated size stands in: the cost of an
+    evaluation depends on the numbers of nodes and time samples, not on the
+    basis values.  float64 throughout."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.roq import ROQGravitationalWaveTransient
+    from bilby_gb300.source import taylorf2_aligned_roq
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    from bilby_gb300.workloads import WORKLOADS, draw_points
+    w = WORKLOADS[name]
+    base = build_likelihood(w, precision="fp64")
+    ifos = base.interferometers
+    rng = np.random.default_rng(seed)
+    fm = np.asarray(ifos[0].strain_data.frequency_array)[np.asarray(ifos[0].strain_data.frequency_mask)]
+    lin = rng.standard_normal((len(fm), n_linear)) + 1j * rng.standard_normal((len(fm), n_linear))
+    quad = rng.standard_normal((len(fm), n_quadratic))
+    nl = np.sort(rng.choice(fm, n_linear, replace=False))
+    nq = np.sort(rng.choice(fm, n_quadratic, replace=False))
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned_roq,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency,
+                                                    frequency_nodes_linear=nl, frequency_nodes_quadratic=nq))
+    tc = w.injection["geocent_time"]
+    t0 = time.perf_counter()
+    like = ROQGravitationalWaveTransient(ifos, wfg, {"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
+                                         linear_matrix=lin, quadratic_matrix=quad)
+    setup_s = time.perf_counter() - t0
+    an = like.analysis
+    p = draw_points(w, batch, rng)
+    p["geocent_time"] = tc + rng.uniform(-0.1, 0.1, batch)
+    blocks = [torch.from_numpy(params_block(p)).cuda() for _ in range(2)]
+    out = torch.empty(batch, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for s in range(warmup):
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return {"workload": name, "linear_nodes": n_linear, "quadratic_nodes": n_quadratic,
+            "time_samples": int(len(like.weights["time_samples"])), "batch": batch,
+            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+            "precision": "fp64", "setup_s": setup_s, "basis": "seeded random basis of the stated size",
+            "launch": "prologue + one warp per point over the nodes"}
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
@@ -614,6 +672,10 @@ def run_ours(args, rank, world, local):
     if world == 1 and not args.no_multiband:
         multiband = bench_multiband("tf2_128s", max(3, args.steps // 4), args.warmup)
 
+    roq = None
+    if world == 1 and not args.no_roq:
+        roq = bench_roq("tf2_marg_8s_2k", max(3, args.steps // 2), args.warmup)
+
     marg = None
     if world == 1 and not args.no_marg:
         marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup)
@@ -673,6 +735,8 @@ def run_ours(args, rank, world, local):
             line["relative_binning"] = relbin
         if multiband is not None:
             line["multiband"] = multiband
+        if roq is not None:
+            line["roq"] = roq
         if uneven is not None:
             line["uneven"] = uneven
         if served is not None:

@@ -92,6 +92,10 @@ SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
                                          ctypes.POINTER(ctypes.c_double)]),
+    "gwl_set_roq": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.c_int64,
+                                   ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_double)]),
     "gwl_priors_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "gwl_priors_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "gwl_priors_rescale": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

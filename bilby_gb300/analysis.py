@@ -157,6 +157,28 @@ class Analysis:
                     "gwl_set_multiband")
         self.multiband = True
 
+    def set_roq(self, enable: bool, nodes_linear=None, nodes_quadratic=None, time_start_index=0, time_step=0.0,
+                linear_weights=None, quadratic_weights=None):
+        """Reduced-order quadrature: ``linear_weights`` [n_det, n_time,
+        n_linear] complex on the time grid (time_start_index + k) time_step,
+        ``quadratic_weights`` [n_det, n_quadratic] real."""
+        if not enable:
+            _capi.check(self._lib.gwl_set_roq(self._h, 0, 0, None, 0, None, 0, 0, 0.0, None, None), "gwl_set_roq")
+            self.roq = False
+            return
+        fl = np.ascontiguousarray(nodes_linear, dtype=np.float64)
+        fq = np.ascontiguousarray(nodes_quadratic, dtype=np.float64)
+        wl = np.ascontiguousarray(np.asarray(linear_weights, dtype=np.complex128))
+        wq = np.ascontiguousarray(quadratic_weights, dtype=np.float64)
+        if wl.ndim != 3 or wl.shape[0] != self.n_detectors or wl.shape[2] != len(fl) or \
+                wq.shape != (self.n_detectors, len(fq)):
+            raise ValueError("ROQ weights do not match the detectors and nodes")
+        wlf = wl.view(np.float64)
+        _capi.check(self._lib.gwl_set_roq(self._h, 1, len(fl), _capi.dptr(fl), len(fq), _capi.dptr(fq),
+                                          wl.shape[1], int(time_start_index), float(time_step), _capi.dptr(wlf),
+                                          _capi.dptr(wq)), "gwl_set_roq")
+        self.roq = True
+
     # -- queries -----------------------------------------------------------
     def noise_log_likelihood(self) -> float:
         out = ctypes.c_double()

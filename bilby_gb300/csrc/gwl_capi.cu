@@ -95,6 +95,17 @@ struct gwl_analysis {
   int mb_bands = 0;
   int64_t* mb_band_start = nullptr;
   double* mb_band_df = nullptr;
+  // reduced-order quadrature
+  int roq = 0;
+  int roq_nl = 0, roq_nq = 0;
+  int64_t roq_time_start = 0, roq_n_time = 0;
+  double roq_dt = 0.0;
+  double* roq_fl = nullptr;
+  double* roq_fq = nullptr;
+  double4* roq_pl = nullptr;
+  double4* roq_pq = nullptr;
+  double2* roq_wl[kMaxDet] = {};
+  double* roq_wq[kMaxDet] = {};
   // work space
   int chunks_per_group = kChunksPerGroup;  // split-K depth of the TaylorF2 mixed kernel (gwl_autotune)
   int64_t ws_B = 0;
@@ -306,6 +317,20 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.mb_bands = a->mb_bands;
   L.mb_band_start = a->mb_band_start;
   L.mb_band_df = a->mb_band_df;
+  L.roq = a->roq;
+  L.roq_nl = a->roq_nl;
+  L.roq_nq = a->roq_nq;
+  L.roq_time_start = a->roq_time_start;
+  L.roq_n_time = a->roq_n_time;
+  L.roq_dt = a->roq_dt;
+  L.roq_fl = a->roq_fl;
+  L.roq_fq = a->roq_fq;
+  L.roq_pl = a->roq_pl;
+  L.roq_pq = a->roq_pq;
+  for (int d = 0; d < a->n_det; ++d) {
+    L.roq_wl[d] = a->roq_wl[d];
+    L.roq_wq[d] = a->roq_wq[d];
+  }
   return L;
 }
 
@@ -352,15 +377,17 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.dh_out = d_dh;
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
-  if (a->relbin || a->multiband) {
-    // relative binning / multi-banding: per-point set-up, then one warp per
-    // point over the bin edges or banded frequencies
+  if (a->relbin || a->multiband || a->roq) {
+    // relative binning / multi-banding / ROQ: per-point set-up, then one warp
+    // per point over the bin edges, banded frequencies or nodes
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
     if (a->relbin) {
       GWL_CUDA(launch_relbin(L, s));
-    } else {
+    } else if (a->multiband) {
       GWL_CUDA(launch_multiband(L, s));
+    } else {
+      GWL_CUDA(launch_roq(L, s));
     }
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
@@ -409,9 +436,9 @@ namespace gwl {
 // entry point that supplies its own work space; also the bytes it needs for
 // the per-point records and the partial sums.  Allocates nothing.
 int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes) {
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband || a->roq) {
     set_error("the allocation-free entry point serves mixed-precision TaylorF2 analyses without time "
-              "marginalisation, relative binning or multi-banding");
+              "marginalisation, relative binning, multi-banding or ROQ");
     return GWL_ERR_UNSUPPORTED;
   }
   *L = make_args(a, B, GWL_PRECISION_MIXED);
@@ -754,7 +781,7 @@ int gwl_autotune(gwl_analysis* a, const double* params, int64_t B, void* stream,
   }
   std::lock_guard<std::mutex> g(a->mu);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband) {
+  if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband || a->roq) {
     // nothing to tune: the other launch shapes are fixed
     if (chunks_per_group) *chunks_per_group = a->chunks_per_group;
     if (best_ms) *best_ms = 0.0;
@@ -846,8 +873,8 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
-    if (a->relbin || a->multiband) {
-      set_error("time marginalisation is not available with relative binning or multi-banding");
+    if (a->relbin || a->multiband || a->roq) {
+      set_error("time marginalisation is not available with relative binning, multi-banding or ROQ");
       return GWL_ERR_UNSUPPORTED;
     }
   }
@@ -911,8 +938,8 @@ int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const
     a->relbin = 0;
     return GWL_OK;
   }
-  if (a->time_marg || a->multiband) {
-    set_error("relative binning excludes time marginalisation and multi-banding");
+  if (a->time_marg || a->multiband || a->roq) {
+    set_error("relative binning excludes time marginalisation, multi-banding and ROQ");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_edges < 2 || !edge_index || !h0_inverse || !summary) {
@@ -957,8 +984,8 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
     a->multiband = 0;
     return GWL_OK;
   }
-  if (a->time_marg || a->relbin) {
-    set_error("multi-banding excludes time marginalisation and relative binning");
+  if (a->time_marg || a->relbin || a->roq) {
+    set_error("multi-banding excludes time marginalisation, relative binning and ROQ");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_points < 1 || !frequencies || !linear || !quadratic || n_bands < 1 || !band_start || !band_df) {
@@ -1005,6 +1032,64 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   a->mb_bands = n_bands;
   a->mb_points = n_points;
   a->multiband = 1;
+  return GWL_OK;
+}
+
+namespace {
+std::vector<double4> node_powers(const std::vector<double>& f) {
+  std::vector<double4> pw(f.size(), make_double4(0.0, 0.0, 0.0, 0.0));
+  for (size_t k = 0; k < f.size(); ++k) {
+    const double x = f[k];
+    if (!(x > 0) || !std::isfinite(x)) continue;
+    pw[k] = make_double4(std::cbrt(x), std::log(x) / 3.0, std::pow(x, -5.0 / 3.0), std::pow(x, -7.0 / 6.0));
+  }
+  return pw;
+}
+}  // namespace
+
+int gwl_set_roq(gwl_analysis* a, int enable, int32_t n_linear, const double* nodes_linear, int32_t n_quadratic,
+                const double* nodes_quadratic, int64_t n_time, int64_t time_start_index, double time_step,
+                const double* linear_weights, const double* quadratic_weights) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!enable) {
+    a->roq = 0;
+    return GWL_OK;
+  }
+  if (a->time_marg || a->relbin || a->multiband) {
+    set_error("ROQ excludes time marginalisation, relative binning and multi-banding");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  if (n_linear < 1 || n_quadratic < 1 || n_time < 5 || !(time_step > 0) || time_start_index < 0 || !nodes_linear ||
+      !nodes_quadratic || !linear_weights || !quadratic_weights) {
+    set_error("ROQ needs nodes, at least five time samples with a positive step and both weight sets");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<double> fl(nodes_linear, nodes_linear + n_linear), fq(nodes_quadratic, nodes_quadratic + n_quadratic);
+  int rc;
+  if ((rc = upload(a, &a->roq_fl, fl))) return rc;
+  if ((rc = upload(a, &a->roq_fq, fq))) return rc;
+  if ((rc = upload(a, &a->roq_pl, node_powers(fl)))) return rc;
+  if ((rc = upload(a, &a->roq_pq, node_powers(fq)))) return rc;
+  const size_t per = (size_t)n_time * n_linear;
+  for (int d = 0; d < a->n_det; ++d) {
+    std::vector<double2> wl(per);
+    for (size_t k = 0; k < per; ++k)
+      wl[k] = make_double2(linear_weights[((size_t)d * per + k) * 2], linear_weights[((size_t)d * per + k) * 2 + 1]);
+    std::vector<double> wq(quadratic_weights + (size_t)d * n_quadratic,
+                           quadratic_weights + (size_t)(d + 1) * n_quadratic);
+    if ((rc = upload(a, &a->roq_wl[d], wl))) return rc;
+    if ((rc = upload(a, &a->roq_wq[d], wq))) return rc;
+  }
+  a->roq_nl = n_linear;
+  a->roq_nq = n_quadratic;
+  a->roq_n_time = n_time;
+  a->roq_time_start = time_start_index;
+  a->roq_dt = time_step;
+  a->roq = 1;
   return GWL_OK;
 }
 
@@ -1213,7 +1298,8 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
       return GWL_ERR_ARGUMENT;
     }
     const gwl_analysis* a = it.analysis;
-    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband || a->n_det > kMultiMaxDet)
+    if (a->model != GWL_MODEL_TAYLORF2 || a->time_marg || a->relbin || a->multiband || a->roq ||
+        a->n_det > kMultiMaxDet)
       fused = false;
   }
   if (!fused) {

@@ -121,6 +121,18 @@ struct LaunchArgs {
   int mb_bands;
   const int64_t* mb_band_start;         // [mb_bands + 1] first banded index of each band (and the end)
   const double* mb_band_df;             // [mb_bands] frequency spacing of each band
+  // reduced-order quadrature: the model at the linear and quadratic nodes,
+  // time-dependent linear weights on the grid (t_start + k) dt, k < n_time
+  int roq;
+  int roq_nl, roq_nq;
+  int64_t roq_time_start, roq_n_time;
+  double roq_dt;
+  const double* roq_fl;                 // [roq_nl] linear nodes
+  const double* roq_fq;                 // [roq_nq] quadratic nodes
+  const double4* roq_pl;                // [roq_nl] TaylorF2 powers of the linear nodes
+  const double4* roq_pq;                // [roq_nq] and of the quadratic nodes
+  const double2* roq_wl[kMaxDet];       // [roq_n_time][roq_nl]
+  const double* roq_wq[kMaxDet];        // [roq_nq]
 };
 
 // A batch over several analyses evaluated by one persistent launch: per item
@@ -158,6 +170,7 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);

@@ -1188,6 +1188,100 @@ __device__ __forceinline__ void model_at(const LaunchArgs& a, const PointRec& r,
 }
 
 // ---------------------------------------------------------------------------
+// reduced-order quadrature (bilby/gw/likelihood/roq.py:467-602, one basis,
+// no time marginalisation): one warp per point.  Lanes stride over the
+// linear nodes, accumulating for each detector the five sums
+//   D_m = sum_j conj(h_d(F_j)) W_d[c + m - 2][j],  m = 0..4,
+// at the time samples around the detector's arrival time (c the closest
+// sample below it), then over the quadratic nodes for
+//   <h|h> += sum_j |h_d(G_j)|^2 w_d[j].
+// Lane 0 interpolates the five D_m to the arrival time (LIGO-T2100224).  The
+// detector time shift lives in the weights, so h carries no e^{-2 pi i f dt}.
+// float64 throughout.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(32 * kRelbinWarps) k_roq(LaunchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kRelbinWarps + (threadIdx.x >> 5);
+  if (i >= a.B) return;  // uniform over the warp
+  const PointRec& r = a.rec[i];
+  double dr = 0.0, di = 0.0, hh = 0.0;
+  if (r.valid) {
+    double fp[D], fx[D], ar[D][5], ai[D][5];
+    int64_t row[D][5];
+    bool inb[D];
+    const double t0 = (double)a.roq_time_start * a.roq_dt;
+    const double step = (double)(a.roq_time_start + 1) * a.roq_dt - t0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      fp[d] = r.fp[d];
+      fx[d] = r.fx[d];
+      // roq.py:552-575: the five samples around the arrival time
+      const int64_t c = (int64_t)floor((r.dt[d] - t0) / step);
+      inb[d] = c - 2 >= 0 && c + 2 < a.roq_n_time;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const int64_t k = c + m - 2;
+        row[d][m] = k < 0 ? 0 : (k > a.roq_n_time - 1 ? a.roq_n_time - 1 : k);
+        ar[d][m] = ai[d][m] = 0.0;
+      }
+    }
+    const PointModel pm = point_model(a, r);
+    for (int j = lane; j < a.roq_nl; j += 32) {
+      double hpr, hpi, hxr, hxi;
+      model_at(a, r, pm, a.roq_fl[j], a.roq_pl[j], hpr, hpi, hxr, hxi);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double hr = hpr * fp[d] + hxr * fx[d], hi = hpi * fp[d] + hxi * fx[d];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          const double2 w = a.roq_wl[d][row[d][m] * a.roq_nl + j];
+          // conj(h) w
+          ar[d][m] += hr * w.x + hi * w.y;
+          ai[d][m] += hr * w.y - hi * w.x;
+        }
+      }
+    }
+    for (int j = lane; j < a.roq_nq; j += 32) {
+      double hpr, hpi, hxr, hxi;
+      model_at(a, r, pm, a.roq_fq[j], a.roq_pq[j], hpr, hpi, hxr, hxi);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double hr = hpr * fp[d] + hxr * fx[d], hi = hpi * fp[d] + hxi * fx[d];
+        hh += (hr * hr + hi * hi) * a.roq_wq[d][j];
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      hh += __shfl_xor_sync(0xffffffffu, hh, off);
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          ar[d][m] += __shfl_xor_sync(0xffffffffu, ar[d][m], off);
+          ai[d][m] += __shfl_xor_sync(0xffffffffu, ai[d][m], off);
+        }
+    }
+    // roq.py:577-602 on the (clipped) sample times; out of range: + log(0)
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double ts0 = (double)(a.roq_time_start + row[d][0]) * a.roq_dt;
+      const double ts1 = (double)(a.roq_time_start + row[d][1]) * a.roq_dt;
+      const double ts3 = (double)(a.roq_time_start + row[d][3]) * a.roq_dt;
+      const double aa = (ts3 - r.dt[d]) / fmax(ts1 - ts0, 1e-12);
+      const double bb = 1.0 - aa;
+      const double cc = (aa * aa * aa - aa) / 6.0, dd = (bb * bb * bb - bb) / 6.0;
+      const double r1r = (-ar[d][0] + 8.0 * ar[d][1] - 14.0 * ar[d][2] + 8.0 * ar[d][3] - ar[d][4]) / 4.0;
+      const double r1i = (-ai[d][0] + 8.0 * ai[d][1] - 14.0 * ai[d][2] + 8.0 * ai[d][3] - ai[d][4]) / 4.0;
+      const double r2r = ar[d][2] - 2.0 * ar[d][3] + ar[d][4], r2i = ai[d][2] - 2.0 * ai[d][3] + ai[d][4];
+      dr += aa * ar[d][2] + bb * ar[d][3] + cc * r1r + dd * r2r + (inb[d] ? 0.0 : -INFINITY);
+      di += aa * ai[d][2] + bb * ai[d][3] + cc * r1i + dd * r2i;
+    }
+  }
+  if (lane == 0) finish_point(a, r, i, dr, di, hh);
+}
+
+// ---------------------------------------------------------------------------
 // multi-banding (bilby/gw/likelihood/multiband.py:741-819, linear
 // interpolation of <h|h>): one warp per point, lanes striding over the banded
 // frequencies; <d|h> = conj(sum_k s_k L_k), <h|h> = sum_k |s_k|^2 Q_k with the
@@ -1336,6 +1430,12 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const int threads = kPointThreads;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s) {
+  const unsigned grid = (unsigned)((a.B + kRelbinWarps - 1) / kRelbinWarps);
+  GWL_DISPATCH_D(k_roq, grid, 32 * kRelbinWarps, 0, s, a);
   return cudaGetLastError();
 }
 

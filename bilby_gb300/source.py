@@ -59,6 +59,23 @@ def taylorf2_aligned_frequency_sequence(frequency_array, mass_1, mass_2, chi_1, 
     return taylorf2_aligned(grid, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
 
 
+def taylorf2_aligned_roq(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                         **kwargs):
+    """``taylorf2_aligned`` with bilby's ROQ source convention
+    (bilby/gw/source.py:802-900): {"linear": ..., "quadratic": ...} at the
+    frequency nodes of the waveform arguments."""
+    if "frequency_nodes" in kwargs:
+        nodes = kwargs.pop("frequency_nodes")
+        li, qi = kwargs.pop("linear_indices"), kwargs.pop("quadratic_indices")
+        pols = taylorf2_aligned(nodes, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase, **kwargs)
+        return {"linear": {m: v[li] for m, v in pols.items()}, "quadratic": {m: v[qi] for m, v in pols.items()}}
+    fl, fq = kwargs.pop("frequency_nodes_linear"), kwargs.pop("frequency_nodes_quadratic")
+    return {"linear": taylorf2_aligned(fl, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                                       **kwargs),
+            "quadratic": taylorf2_aligned(fq, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                                          **kwargs)}
+
+
 def model_of(source_model) -> str:
     """Which fused kernel serves ``source_model`` ('sinegaussian' | 'taylorf2').
 
@@ -68,8 +85,10 @@ def model_of(source_model) -> str:
     module = getattr(source_model, "__module__", "") or ""
     if source_model is sinegaussian or (name == "sinegaussian" and module.endswith("gw.source")):
         return "sinegaussian"
-    if source_model in (taylorf2_aligned, taylorf2_aligned_relative_binning, taylorf2_aligned_frequency_sequence) \
-            or name in ("taylorf2_aligned", "taylorf2_aligned_relative_binning", "taylorf2_aligned_frequency_sequence"):
+    if source_model in (taylorf2_aligned, taylorf2_aligned_relative_binning, taylorf2_aligned_frequency_sequence,
+                        taylorf2_aligned_roq) \
+            or name in ("taylorf2_aligned", "taylorf2_aligned_relative_binning", "taylorf2_aligned_frequency_sequence",
+                        "taylorf2_aligned_roq"):
         return "taylorf2"
     raise NotImplementedError(
         f"source model {module}.{name} has no GPU kernel (supported: sinegaussian, taylorf2_aligned)")

@@ -263,6 +263,24 @@ int gwl_set_multiband(gwl_analysis *a, int enable, int64_t n_points, const doubl
                       const double *linear, const double *quadratic, int32_t n_bands, const int64_t *band_start,
                       const double *band_df);
 
+/* Reduced-order quadrature (replaces ROQGravitationalWaveTransient.
+ * calculate_snrs for one linear and one quadratic basis without time
+ * marginalisation, bilby/gw/likelihood/roq.py:467-602; the weights of
+ * _set_weights 736-1007 are computed by the caller).  With it enabled, every
+ * evaluation evaluates the model at the n_linear linear and n_quadratic
+ * quadratic frequency nodes, projects it on each detector (antenna patterns
+ * only: the time shift lives in the weights), contracts the linear part with
+ * the weights of the five time samples around the detector's arrival time
+ * (time sample k at (time_start_index + k) * time_step, k < n_time;
+ * linear_weights [n_det][n_time][n_linear][2]) and interpolates them to the
+ * arrival time (LIGO-T2100224); <h|h> = sum_j |h(G_j)|^2 w_j
+ * (quadratic_weights [n_det][n_quadratic]).  float64 for either precision;
+ * an arrival time within two samples of the grid's ends gives lnL = -inf, as
+ * in the reference. */
+int gwl_set_roq(gwl_analysis *a, int enable, int32_t n_linear, const double *nodes_linear, int32_t n_quadratic,
+                const double *nodes_quadratic, int64_t n_time, int64_t time_start_index, double time_step,
+                const double *linear_weights, const double *quadratic_weights);
+
 /* On-device prior rescaling and parameter conversion for the batch path
  * (replaces, for the supported priors, PriorDict.rescale, bilby/core/prior/
  * dict.py, with the inverse CDFs of bilby/core/prior/analytical.py,

@@ -155,3 +155,23 @@ def taylorf2_aligned_frequency_sequence(frequency_array, mass_1, mass_2, chi_1, 
     frequencies = kwargs.pop("frequencies")
     return taylorf2_aligned(frequencies, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
                             **kwargs)
+
+
+def taylorf2_aligned_roq(frequency_array, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                         **kwargs):
+    """The same model with the ROQ source convention of bilby
+    (bilby/gw/source.py:802-900): polarisations at the linear and quadratic
+    frequency nodes, {"linear": {...}, "quadratic": {...}}."""
+    if "frequency_nodes" in kwargs:
+        nodes = kwargs.pop("frequency_nodes")
+        li = kwargs.pop("linear_indices")
+        qi = kwargs.pop("quadratic_indices")
+        pols = taylorf2_aligned(nodes, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                                **kwargs)
+        return {"linear": {m: v[li] for m, v in pols.items()}, "quadratic": {m: v[qi] for m, v in pols.items()}}
+    fl = kwargs.pop("frequency_nodes_linear")
+    fq = kwargs.pop("frequency_nodes_quadratic")
+    return {"linear": taylorf2_aligned(fl, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                                       **kwargs),
+            "quadratic": taylorf2_aligned(fq, mass_1, mass_2, chi_1, chi_2, luminosity_distance, theta_jn, phase,
+                                          **kwargs)}

@@ -25,6 +25,12 @@ Outputs
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
     frequencies, linear and quadratic coefficients and lnL ratios without
     marginalisation, with phase and with distance marginalisation.
+``tests/golden/tf2_marg_8s_2k_roq.npz``
+    The reference's ``ROQGravitationalWaveTransient`` on tf2_marg_8s_2k with the
+    seeded synthetic basis of ``oracle/roq_basis.py``: its time grid, the rows
+    of the linear weights the stored points read, the quadratic weights, the
+    frequency nodes, and lnL ratios without marginalisation, with phase and
+    with distance marginalisation.
 ``tests/golden/priors.npz``
     The reference's ``PriorDict.rescale`` of fixed unit-cube samples for the
     GW prior kinds the device rescaler supports, followed by
@@ -53,7 +59,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import ref_harness  # noqa: E402
 from oracle.taylorf2 import (taylorf2_aligned, taylorf2_aligned_frequency_sequence,  # noqa: E402
-                             taylorf2_aligned_relative_binning)
+                             taylorf2_aligned_relative_binning, taylorf2_aligned_roq)
 from bilby_gb300.workloads import WORKLOADS, DISTANCE_PRIOR, draw_points, point  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -254,6 +260,65 @@ def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
     np.savez_compressed(os.path.join(HERE, f"{name}_multiband.npz"), **out)
 
 
+def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
+    from oracle import roq_basis
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 3)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    params.pop("time_jitter", None)
+    n = n_fixed + n_random
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in RELBIN_COMBOS:
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+        nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_roq,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency, frequency_nodes_linear=nl,
+                                    frequency_nodes_quadratic=nq))
+        p, d = "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, True, p, d)
+        like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, linear_matrix=bl.T,
+            quadratic_matrix=bq.T, phase_marginalization=p, distance_marginalization=d)
+        t0 = time.perf_counter()
+        vals = []
+        for i in range(n):
+            q = point(params, i)
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} roq[{combo}]: {len(nl)} linear / {len(nq)} quadratic nodes, "
+              f"{(time.perf_counter() - t0) / n * 1e3:.2f} ms/eval")
+        if combo == "none":
+            ts = np.asarray(like.weights["time_samples"])
+            out["roq_time_meta"] = np.array([ts[0], ts[1] - ts[0], len(ts)])
+            out["roq_nodes_linear"] = nl
+            out["roq_nodes_quadratic"] = nq
+            # only the rows of the linear weights these points read (five
+            # time samples per point and detector): the whole table is MBs
+            for q, ifo in enumerate(ifos):
+                rows = set()
+                for i in range(n):
+                    pt = point(params, i)
+                    dt = ifo.time_delay_from_geocenter(pt["ra"], pt["dec"], pt["geocent_time"])
+                    t_ifo = pt["geocent_time"] - ifo.strain_data.start_time + dt
+                    c = int(np.floor((t_ifo - ts[0]) / (ts[1] - ts[0])))
+                    rows.update(min(max(c + k, 0), len(ts) - 1) for k in range(-2, 3))
+                rows = np.array(sorted(rows))
+                out[f"roq_linear_rows_{q}"] = rows
+                out[f"roq_linear_{q}"] = np.asarray(like.weights[ifo.name + "_linear"][0])[rows]
+                out[f"roq_quadratic_{q}"] = np.asarray(like.weights[ifo.name + "_quadratic"][0])
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}_roq.npz"), **out)
+
+
 def run_priors(bilby, n=256):
     from bilby.core.prior import (Cosine, Gaussian, LogUniform, PowerLaw, PriorDict, Sine, TruncatedGaussian,
                                   Uniform)
@@ -350,8 +415,18 @@ def main():
     ap.add_argument("--multiband-only", action="store_true")
     ap.add_argument("--frames-only", action="store_true")
     ap.add_argument("--priors-only", action="store_true")
+    ap.add_argument("--roq-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.roq_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_roq(bilby)
+            finally:
+                os.chdir(cwd)
+        return
     if args.priors_only:
         run_priors(bilby)
         return
@@ -364,6 +439,7 @@ def main():
             os.chdir(tmp)
             try:
                 run_multiband(bilby, "tf2_128s", 8, 8)
+                run_roq(bilby)
             finally:
                 os.chdir(cwd)
         return
@@ -389,6 +465,7 @@ def main():
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)
+                run_roq(bilby)
             finally:
                 os.chdir(cwd)
 

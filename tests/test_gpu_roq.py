@@ -1,0 +1,88 @@
+"""ROQ on the GPU against the reference's own ROQGravitationalWaveTransient
+(tests/golden/tf2_marg_8s_2k_roq.npz: the reference's weights for a seeded
+synthetic basis, stored for the time samples the points read, and its lnL
+ratios without marginalisation, with phase and with distance
+marginalisation).  The rows of the linear weights that were not stored are
+NaN, so reading any other time sample would show.
+
+Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
+table, as for the full likelihood)."""
+import numpy as np
+import pytest
+
+from tests.conftest import golden
+from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, point
+
+pytestmark = pytest.mark.gpu
+
+
+def golden_weights(z, names):
+    t0, dt, n = z["roq_time_meta"]
+    start = int(round(t0 / dt))
+    weights = {"time_samples": np.arange(start, start + int(n)) * dt,
+               "frequency_nodes_linear": [z["roq_nodes_linear"]],
+               "frequency_nodes_quadratic": [z["roq_nodes_quadratic"]]}
+    for q, name in enumerate(names):
+        w = np.full((int(n), len(z["roq_nodes_linear"])), np.nan + 0j)
+        w[z[f"roq_linear_rows_{q}"]] = z[f"roq_linear_{q}"]
+        weights[name + "_linear"] = [w]
+        weights[name + "_quadratic"] = [z[f"roq_quadratic_{q}"]]
+    return weights
+
+
+def make(combo, tmp_path, **kw):
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.prior import PowerLaw, Uniform
+    from bilby_gb300.roq import ROQGravitationalWaveTransient
+    from bilby_gb300.source import taylorf2_aligned_roq
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned_roq,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    from bilby_gb300.source import taylorf2_aligned
+    from bilby_gb300.waveform_generator import WaveformGenerator as WG
+    inj = WG(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+             frequency_domain_source_model=taylorf2_aligned, waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    ifos.inject_signal(waveform_generator=inj, parameters=dict(w.injection))
+    tc = w.injection["geocent_time"]
+    priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1)}
+    if "p" in combo:
+        priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
+    if "d" in combo:
+        priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
+                                                 DISTANCE_PRIOR["maximum"])
+    z = golden("tf2_marg_8s_2k_roq")
+    like = ROQGravitationalWaveTransient(ifos, wfg, priors, weights=golden_weights(z, [i.name for i in ifos]),
+                                         phase_marginalization="p" in combo, distance_marginalization="d" in combo,
+                                         distance_marginalization_lookup_table=str(tmp_path / "table.npz"), **kw)
+    return like, priors, z
+
+
+@pytest.mark.parametrize("combo", ["none", "p", "d"])
+def test_lnl_matches_the_reference(gpu, tmp_path, combo):
+    like, priors, z = make(combo, tmp_path)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        pts.append(q)
+    ref = z["lnl_" + combo]
+    single = np.array([like.log_likelihood_ratio(q) for q in pts])
+    batch = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    assert np.array_equal(single, batch)
+    rtol = 1e-8 if "d" in combo else 1e-9
+    assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
+
+
+def test_time_marginalisation_is_refused(gpu, tmp_path):
+    with pytest.raises(NotImplementedError):
+        make("none", tmp_path, time_marginalization=True)
