@@ -509,6 +509,34 @@ __device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const
   }
 }
 
+// A whole 8-bin block of the anchored recurrence.  DEG is the degree of the
+// phase polynomial about the anchor: with DEG < 6 the higher differences are
+// zero, so the adds skipped here would only add zero.
+template <int D, bool CPLX, int DEG>
+__device__ __forceinline__ void tf2_block8(uint64_t& D0, uint64_t& D1, uint64_t& D2, uint64_t& D3, uint64_t& D4,
+                                           uint64_t& D5, uint64_t D6, uint32_t* lh, const uint32_t* r32,
+                                           const uint2* w, float* are, float* aim) {
+#pragma unroll
+  for (int j = 0; j < kFold; ++j) {
+    tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + j, are, aim);
+#pragma unroll
+    for (int d = 1; d < D; ++d) lh[d] += r32[d];
+    D0 += D1; D1 += D2; D2 += D3; D3 += D4;
+    if (DEG >= 5) D4 += D5;
+    if (DEG >= 6) D5 += D6;
+  }
+}
+
+// Degree of the phase polynomial about an anchor: the lowest of 4, 5, 6 whose
+// Taylor remainder N x^(deg + 1) stays within the bound of anchor_interval
+// (N the Newtonian phase in cycles at the anchor, x = J / k).
+__device__ __forceinline__ int anchor_degree(float n_cycles, float x) {
+  const float x5 = x * x * x * x * x;
+  if (n_cycles * x5 <= 3.1e-11f) return 4;
+  if (n_cycles * x5 * x <= 3.1e-11f) return 5;
+  return 6;
+}
+
 // A chunk where no anchor interval meets the Taylor bound: the phase of every
 // bin in float-float from the per-bin basis table (sum_b c_b phi_b(f_k)),
 // the time shift exact in 0.64 fixed point.
@@ -665,9 +693,11 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
           r32[d] = (uint32_t)((R[d] + 0x80000000ull) >> 32);
           L64[d] = 0;
         }
+        int deg = 6;
         for (int jb = 0; jb < jlast; jb += kFold) {
           const int64_t k = k0 + jb;
           if ((jb & (J - 1)) == 0) {
+            deg = anchor_degree(c0 * __powf((float)k * (float)a.step, -5.0f / 3.0f), (float)J / (float)k);
             // Taylor coefficients of the phase about k (cycles per bin)
             const float* an = a.anchors + (k / kAnchorStep) * kAnchorFloats;
             float Ah[kAnchorFF], Al[kAnchorFF], Af[kAnchorOrders - kAnchorFF];
@@ -689,7 +719,8 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
               Af[n - kAnchorFF] = sf;
             }
             // forward differences Delta_m = m! sum_n S(n, m) A_n (Stirling numbers of the second kind)
-            const float A4 = Af[0], A5 = Af[1], A6 = Af[2];
+            // of the polynomial truncated at degree deg
+            const float A4 = Af[0], A5 = deg >= 5 ? Af[1] : 0.f, A6 = deg >= 6 ? Af[2] : 0.f;
             float d1h = Ah[1], d1l = Al[1];
             ff_add(d1h, d1l, Ah[2], Al[2]);
             ff_add(d1h, d1l, Ah[3], Al[3]);
@@ -722,12 +753,12 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
           for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
           if (jb + kFold <= jlast && k >= ks) {
             // a whole block inside the band
-#pragma unroll
-            for (int j = 0; j < kFold; ++j) {
-              tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + jb + j, are, aim);
-#pragma unroll
-              for (int d = 1; d < D; ++d) lh[d] += r32[d];
-              D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
+            if (deg == 4) {
+              tf2_block8<D, CPLX, 4>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
+            } else if (deg == 5) {
+              tf2_block8<D, CPLX, 5>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
+            } else {
+              tf2_block8<D, CPLX, 6>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
             }
           } else {
             const int je = min(jb + kFold, jlast);
