@@ -80,8 +80,11 @@ class ServerStats:
 
 
 class GpuBackend:
-    """Device side of the server: one CUDA stream, one batcher and pinned
-    staging per step slot."""
+    """Device side of the server: per step slot one CUDA stream, one batcher
+    and a staging arena (pinned host and device buffers for the parameter
+    blocks and results of a step, grown on demand and reused), so that a step
+    costs one host memcpy per request, one host-to-device and one
+    device-to-host copy, and the batched launch."""
 
     def __init__(self, n_slots: int, precision: str = "mixed", use_graphs: bool = False):
         import torch
@@ -90,6 +93,7 @@ class GpuBackend:
         self.precision = precision
         self.streams = [torch.cuda.Stream() for _ in range(n_slots)]
         self.batchers = [Batcher(use_graphs=use_graphs) for _ in range(n_slots)]
+        self._arenas = [None] * n_slots
 
     @staticmethod
     def resident_bytes(analysis) -> int:
@@ -101,35 +105,53 @@ class GpuBackend:
         groups = max(1, -(-analysis.n_bins // 512))
         return n_points * (8 * _capi.NPARAM + 8 + 640) + groups * analysis.n_detectors * 6 * 8 * n_points
 
-    def launch(self, slot: int, items):
-        """items: [(Analysis, host block)] -> handle; asynchronous."""
+    def _arena(self, slot: int, n_points: int):
         torch = self.torch
+        a = self._arenas[slot]
+        if a is None or a[0] < n_points:
+            cap = max(n_points, 4096)
+            a = (cap,
+                 torch.empty(_capi.NPARAM * cap, dtype=torch.float64, pin_memory=True),
+                 torch.empty(_capi.NPARAM * cap, dtype=torch.float64, device="cuda"),
+                 torch.empty(cap, dtype=torch.float64, device="cuda"),
+                 torch.empty(cap, dtype=torch.float64, pin_memory=True))
+            self._arenas[slot] = a
+        return a
+
+    def launch(self, slot: int, items):
+        """items: [(Analysis, host block)] -> handle; asynchronous.  The slot's
+        arena is free: the scheduler hands a slot out only after its previous
+        step was retired."""
+        torch = self.torch
+        n_total = sum(b.shape[1] for _, b in items)
+        _, pin_in, dev_in, dev_out, pin_out = self._arena(slot, n_total)
+        host = pin_in.numpy()
+        raw, spans, off = [], [], 0
+        for an, block in items:
+            n = block.shape[1]
+            host[_capi.NPARAM * off:_capi.NPARAM * (off + n)].reshape(_capi.NPARAM, n)[...] = block
+            raw.append((an, dev_in.data_ptr() + 8 * _capi.NPARAM * off, n, dev_out.data_ptr() + 8 * off))
+            spans.append((off, n))
+            off += n
         stream = self.streams[slot]
         with torch.cuda.stream(stream):
-            dev, host_in, host_out = [], [], []
-            for an, block in items:
-                h = torch.from_numpy(block).pin_memory()
-                host_in.append(h)
-                d = h.to("cuda", non_blocking=True)
-                dev.append((an, d))
-            outs = self.batchers[slot].eval_tensors(dev, self.precision, stream)
-            for o in outs:
-                ho = torch.empty(o.shape, dtype=o.dtype, pin_memory=True)
-                ho.copy_(o, non_blocking=True)
-                host_out.append(ho)
+            dev_in[:_capi.NPARAM * off].copy_(pin_in[:_capi.NPARAM * off], non_blocking=True)
+            self.batchers[slot].eval_device(raw, self.precision, stream.cuda_stream)
+            pin_out[:off].copy_(dev_out[:off], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
-        return (ev, host_out, (dev, host_in, outs), None, slot)
+        return (ev, spans, pin_out, None, slot)
 
     @staticmethod
     def ready(handle) -> bool:
         return handle[0].query()
 
     def results(self, handle):
-        ev, host_out, _, _, slot = handle
+        ev, spans, pin_out, _, slot = handle
         ev.synchronize()
         self.batchers[slot].check()
-        return [h.numpy().copy() for h in host_out]
+        out = pin_out.numpy()
+        return [out[o:o + n].copy() for o, n in spans]
 
 
 class LikelihoodServer:
