@@ -77,7 +77,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "10",
                  "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -618,8 +618,10 @@ def run_ours(args, rank, world, local):
         return ms, kms
 
     # -- headline: mixed precision, resident inputs ----------------------------
+    # clocks sampled every 10 ms from the warm-up through the timed steps
     clocks = ClockSampler(local)
     clocks.start()
+    time.sleep(0.05)
     ms, kms = timed("mixed", blocks, args.steps, args.warmup)
     clk = clocks.stop()
     total_ms = dist.max(float(np.sum(ms)))
