@@ -199,6 +199,7 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
     bat.check()
+    refined = bat.last_refined(stream.cuda_stream)
     pts = sum(w.batch for w in ws)
     pbd = sum(w.batch * (w.n_bins - int(w.minimum_frequency * w.duration)) * len(w.detectors) for w in ws)
     value = pts * steps / (sum(ms) / 1e3)
@@ -236,6 +237,7 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
             "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
             "point_bin_detector_per_s": pbd * steps / (sum(ms) / 1e3),
             "launch": "one persistent kernel per kernel class (detectors x partial kind), CUDA-graph replay",
+            "refined_points_per_launch": refined,
             "autotuned_chunks_per_group": {str(c): tuned.count(c) for c in sorted(set(tuned))},
             "fp64": {"value": value64, "unit": "evals/s", "points_per_step": pts64,
                      "sample": f"the first {fp64_points} points of every analysis, one launch sequence per analysis"},
@@ -624,6 +626,7 @@ def run_ours(args, rank, world, local):
     time.sleep(0.05)
     ms, kms = timed("mixed", blocks, args.steps, args.warmup)
     clk = clocks.stop()
+    refined = an.last_refined(sptr)  # points of the last timed batch whose sums were recomputed
     total_ms = dist.max(float(np.sum(ms)))
     value = world * B * args.steps / (total_ms / 1e3)
 
@@ -717,7 +720,8 @@ def run_ours(args, rank, world, local):
             "max_abs_dlnl_mixed_vs_fp64": dlnl,
             "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": 8 * _capi.NPARAM * B,
                     "d2h_bytes_per_step": 8 * B},
-            "gpu_launches": (6 if w.model == "taylorf2" else 4) * args.steps * world,
+            "gpu_launches": (7 if w.model == "taylorf2" else 4) * args.steps * world,
+            "refined_points_per_launch": refined,
             "roofline": {"bound": "hbm", "achieved": bytes_launch / (kernel_ms / 1e3) / 1e9, "peak": hbm_peak,
                          "unit": "GB/s", "frac": bytes_launch / (kernel_ms / 1e3) / 1e9 / hbm_peak,
                          "traffic": traffic, "kernel": f"k_mixed_{'tf2' if w.model == 'taylorf2' else 'sg'}",

@@ -104,6 +104,10 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)]),
     "gwl_get_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     "gwl_set_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "gwl_set_refinement": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "gwl_get_refinement": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "gwl_last_refined": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "gwl_batcher_last_refined": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "gwl_batcher_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "gwl_batcher_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "gwl_batcher_use_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

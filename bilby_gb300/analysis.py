@@ -243,6 +243,25 @@ class Analysis:
     def chunks_per_group(self, value: int):
         _capi.check(self._lib.gwl_set_chunks_per_group(self._h, int(value)), "gwl_set_chunks_per_group")
 
+    @property
+    def refinement_tolerance(self) -> float:
+        """Error control of the mixed-precision TaylorF2 result: points whose
+        |Delta lnL| bound exceeds this are recomputed with error-free sums
+        (gwl_set_refinement); <= 0 turns it off."""
+        t = ctypes.c_double()
+        _capi.check(self._lib.gwl_get_refinement(self._h, ctypes.byref(t)), "gwl_get_refinement")
+        return float(t.value)
+
+    @refinement_tolerance.setter
+    def refinement_tolerance(self, value: float):
+        _capi.check(self._lib.gwl_set_refinement(self._h, float(value)), "gwl_set_refinement")
+
+    def last_refined(self, stream: int = 0) -> int:
+        """Points refined by the last mixed-precision evaluation (waits for ``stream``)."""
+        n = ctypes.c_int64()
+        _capi.check(self._lib.gwl_last_refined(self._h, ctypes.c_void_p(stream), ctypes.byref(n)), "gwl_last_refined")
+        return int(n.value)
+
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

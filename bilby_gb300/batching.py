@@ -71,6 +71,13 @@ class Batcher:
         if st.value:
             raise TimeoutError("a bounded device wait gave up during a batched evaluation")
 
+    def last_refined(self, stream: int = 0) -> int:
+        """Points the last batched launch refined (see Analysis.refinement_tolerance); waits for ``stream``."""
+        n = ctypes.c_int64()
+        _capi.check(self._lib.gwl_batcher_last_refined(self._h, ctypes.c_void_p(stream), ctypes.byref(n)),
+                    "gwl_batcher_last_refined")
+        return int(n.value)
+
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

@@ -65,6 +65,10 @@ struct gwl_analysis {
   uint2* wp[kMaxDet] = {};  // TaylorF2: the same weights in polar form {float |w|, arg(w) as 0.32 fixed cycles}
   float* v[kMaxDet] = {};
   double* hh_prefix[kMaxDet] = {};
+  double* rf_p2[kMaxDet] = {};  // TaylorF2: prefix sums of |w|^2 and of |w| over signal-dominated bins
+  double* rf_p1[kMaxDet] = {};
+  double refine_tol = kRefineDefaultTol;  // mixed-precision refinement tolerance (<= 0: off)
+  float4* cos_tab = nullptr;  // TaylorF2: float-float cos / sin of 2 pi q / kCosTable (accurate kernel)
   double w_scale[kMaxDet] = {}, v_scale[kMaxDet] = {};
   // marginalisation
   int time_marg = 0, jitter = 0, phase_marg = 0, dist_marg = 0;
@@ -115,13 +119,15 @@ struct gwl_analysis {
   double* d_part = nullptr;
   size_t part_bytes = 0;
   int32_t* d_order = nullptr;       // [ws_B] point ordering of the mixed TaylorF2 kernel
-  int32_t* d_order_hist = nullptr;  // [2 * kOrderMaxKeys]
+  int32_t* d_order_hist = nullptr;  // [4 * kOrderMaxKeys + 1]: bucket counts and cursors, then the marked count
+  int* last_rf_count = nullptr;     // marked points of the last mixed TaylorF2 evaluation (device)
   double* d_tm = nullptr;
   size_t tm_bytes = 0;
   double* h_params = nullptr;  // pinned staging for gwl_eval_host
   double* h_out = nullptr;
   int* d_status = nullptr;
   cudaStream_t stream = nullptr;
+  SideStream side;  // the accurate kernel beside the fast one
   size_t resident = 0;
   // optional CUDA events around the dominant kernel of each evaluation
   int profiling = 0;
@@ -171,6 +177,7 @@ void free_workspace(gwl_analysis* a) {
   a->d_params = a->d_out = a->d_part = a->d_tm = nullptr;
   a->d_rec = nullptr;
   a->d_order = a->d_order_hist = nullptr;
+  a->last_rf_count = nullptr;
   a->ws_B = 0;
   a->part_bytes = a->tm_bytes = 0;
 }
@@ -269,9 +276,14 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.wp[d] = a->wp[d];
     L.v[d] = a->v[d];
     L.hh_prefix[d] = a->hh_prefix[d];
+    L.rf_p2[d] = a->rf_p2[d];
+    L.rf_p1[d] = a->rf_p1[d];
     L.w_scale[d] = a->w_scale[d];
     L.v_scale[d] = a->v_scale[d];
   }
+  // the list and its count are set by the entry point that launches k_refine
+  L.rf_tol = (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) ? a->refine_tol : 0.0;
+  L.cos_tab = a->cos_tab;
   L.freq = a->freq;
   L.freq_f = a->freq_f;
   L.basis = a->basis;
@@ -348,7 +360,7 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
   if ((rc = dev_alloc(a, &a->d_rec, (size_t)B, false))) return rc;
   if ((rc = dev_alloc(a, &a->d_part, part / sizeof(double), false))) return rc;
   if ((rc = dev_alloc(a, &a->d_order, (size_t)B, false))) return rc;
-  if ((rc = dev_alloc(a, &a->d_order_hist, (size_t)2 * kOrderMaxKeys, false))) return rc;
+  if ((rc = dev_alloc(a, &a->d_order_hist, (size_t)4 * kOrderMaxKeys + 1, false))) return rc;
   if (tm) {
     if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_tm), tm, false))) return rc;
   }
@@ -401,8 +413,12 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     // group the points by band end (see LaunchArgs::order)
     L.order = a->d_order;
     L.order_hist = a->d_order_hist;
-    order_layout(L.n_chunks, &L.order_keys, &L.order_shift);
-    GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * 2 * L.order_keys, s));
+    if (a->time_marg && d_out) L.rf_tol = 0.0;  // the time-marginalised kernel has its own integrand
+    ordering_with_marks(L);
+    a->last_rf_count = L.rf_count;
+    GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * (2 * L.order_keys + 1), s));
+  } else {
+    L.rf_tol = 0.0;
   }
   GWL_CUDA(launch_prologue(L, s));
   if (ordered) GWL_CUDA(launch_order(L, s));
@@ -415,6 +431,12 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     }
     return GWL_OK;
   }
+  const bool acc = precision == GWL_PRECISION_MIXED && L.rf_tol > 0;
+  if (acc) {
+    // the marked points in the accurate kernel on the side stream, beside the fast kernel
+    GWL_CUDA(side_fork(a->side, s));
+    GWL_CUDA(launch_mixed_acc(L, a->side.stream));
+  }
   if (precision == GWL_PRECISION_FP64) {
     GWL_CUDA(launch_plain(L, s));
   } else {
@@ -424,6 +446,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     GWL_CUDA(cudaEventRecord(a->ev_end, s));
     a->ev_pending = 1;
   }
+  if (acc) GWL_CUDA(side_join(a->side, s));
   GWL_CUDA(launch_finalize(L, s));
   return GWL_OK;
 }
@@ -471,6 +494,7 @@ struct gwl_batcher {
   int* d_status = nullptr;
   cudaEvent_t staged = nullptr;
   bool staged_pending = false;
+  SideStream side;  // the accurate kernels beside the fast ones
   int use_graphs = 0;
   std::map<std::vector<int64_t>, cudaGraphExec_t> graphs;
   std::mutex mu;
@@ -581,8 +605,11 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
   const int64_t P = a->n_pad;
   int rc = GWL_OK;
   cudaError_t ce = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = side_stream_create(&a->side);
   if (ce != cudaSuccess) {
     set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+    if (a->stream) cudaStreamDestroy(a->stream);
+    side_stream_destroy(&a->side);
     delete a;
     return GWL_ERR_CUDA;
   }
@@ -638,6 +665,14 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
           }
       }
       if ((rc = upload(a, &a->anchors, anc))) goto fail;
+      // float-float cos and sin of 2 pi q / kCosTable for the accurate kernel
+      std::vector<float4> ct(kCosTable);
+      for (int q = 0; q < kCosTable; ++q) {
+        const double x = 2.0 * M_PI * q / kCosTable, c = std::cos(x), sn = std::sin(x);
+        const float ch = (float)c, sh = (float)sn;
+        ct[q] = make_float4(ch, (float)(c - (double)ch), sh, (float)(sn - (double)sh));
+      }
+      if ((rc = upload(a, &a->cos_tab, ct))) goto fail;
     }
     a->noise_lnl = 0.0;
     for (int d = 0; d < a->n_det; ++d) {
@@ -705,6 +740,25 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
           pre[k + 1] = acc.value();
         }
         if ((rc = upload(a, &a->hh_prefix[d], pre))) goto fail;
+        // refinement bound: prefix sums of the scaled weight magnitudes |w|^2,
+        // and of |w| where the whitened data power 4 |d|^2 / (T S) exceeds
+        // kRefineLoudPower (bins dominated by a signal, whose phase a template
+        // can follow coherently)
+        std::vector<double> p2(N + 1, 0.0), p1(N + 1, 0.0);
+        KahanSum acc2, acc1;
+        for (int64_t k = 0; k < N; ++k) {
+          if (ip[k] != 0.0) {
+            const double x = wr[k] / a->w_scale[d], y = wi[k] / a->w_scale[d];
+            const double m2 = x * x + y * y;
+            acc2.add(m2);
+            const double pw = 4.0 / a->duration * (s[2 * k] * s[2 * k] + s[2 * k + 1] * s[2 * k + 1]) * ip[k];
+            if (pw > kRefineLoudPower) acc1.add(std::sqrt(m2));
+          }
+          p2[k + 1] = acc2.value();
+          p1[k + 1] = acc1.value();
+        }
+        if ((rc = upload(a, &a->rf_p2[d], p2))) goto fail;
+        if ((rc = upload(a, &a->rf_p1[d], p1))) goto fail;
       }
     }
   }
@@ -713,6 +767,7 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
 fail:
   for (void* p : a->tables) cudaFree(p);
   if (a->stream) cudaStreamDestroy(a->stream);
+  side_stream_destroy(&a->side);
   delete a;
   return rc ? rc : GWL_ERR_CUDA;
 }
@@ -727,6 +782,7 @@ int gwl_analysis_destroy(gwl_analysis* a) {
     a->tables.clear();
     if (a->ev_begin) cudaEventDestroy(a->ev_begin);
     if (a->ev_end) cudaEventDestroy(a->ev_end);
+    side_stream_destroy(&a->side);
     cudaStreamDestroy(a->stream);
   }
   delete a;
@@ -846,6 +902,40 @@ int gwl_set_chunks_per_group(gwl_analysis* a, int32_t chunks_per_group) {
   }
   std::lock_guard<std::mutex> g(a->mu);
   a->chunks_per_group = chunks_per_group;
+  return GWL_OK;
+}
+
+int gwl_set_refinement(gwl_analysis* a, double tolerance) {
+  if (!a || !std::isfinite(tolerance)) {
+    set_error("refinement tolerance must be finite (<= 0 turns refinement off)");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  a->refine_tol = tolerance;
+  return GWL_OK;
+}
+
+int gwl_get_refinement(gwl_analysis* a, double* tolerance) {
+  if (!a || !tolerance) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *tolerance = a->refine_tol;
+  return GWL_OK;
+}
+
+int gwl_last_refined(gwl_analysis* a, void* stream, int64_t* count) {
+  if (!a || !count) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *count = 0;
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->last_rf_count) return GWL_OK;
+  int n = 0;
+  GWL_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  GWL_CUDA(cudaMemcpy(&n, a->last_rf_count, sizeof(int), cudaMemcpyDeviceToHost));
+  *count = n;
   return GWL_OK;
 }
 
@@ -1233,14 +1323,16 @@ int gwl_batcher_create(gwl_batcher** out) {
     return GWL_ERR_ARGUMENT;
   }
   auto* b = new gwl_batcher();
-  cudaError_t e = cudaMalloc(&b->d_counter, 8 * sizeof(int));
+  cudaError_t e = cudaMalloc(&b->d_counter, kMultiCounters * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = side_stream_create(&b->side);
   if (e != cudaSuccess) {
     set_error(std::string("gwl_batcher_create: ") + cudaGetErrorString(e));
     cudaFree(b->d_counter);
     cudaFree(b->d_status);
+    side_stream_destroy(&b->side);
     delete b;
     return GWL_ERR_CUDA;
   }
@@ -1267,6 +1359,7 @@ int gwl_batcher_destroy(gwl_batcher* b) {
     cudaFree(b->d_hist);
     cudaFree(b->d_status);
     cudaEventDestroy(b->staged);
+    side_stream_destroy(&b->side);
   }
   delete b;
   return GWL_OK;
@@ -1321,11 +1414,12 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
   key.reserve(2 * n + 1);
   key.push_back(n);
   int64_t units_d[kMultiClasses] = {0, 0, 0, 0, 0, 0, 0, 0};  // per kernel class 2 D + cplx
+  bool acc_class[kMultiClasses] = {false, false, false, false, false, false, false, false};
   for (int q = 0; q < n; ++q) {
     gwl_analysis* a = items[q].analysis;
     largs[q] = make_args(a, items[q].B, GWL_PRECISION_MIXED);
-    order_layout(largs[q].n_chunks, &largs[q].order_keys, &largs[q].order_shift);
-    hist += 2 * (size_t)largs[q].order_keys;
+    ordering_with_marks(largs[q]);
+    hist += 2 * (size_t)largs[q].order_keys + 1;
     total += items[q].B;
     part += (size_t)largs[q].n_groups * a->n_det * kPartStride * items[q].B;
     const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
@@ -1333,6 +1427,8 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     key.push_back(reinterpret_cast<int64_t>(a));
     key.push_back(items[q].B);
     key.push_back(largs[q].n_groups);  // changes when the analysis is re-tuned
+    key.push_back(largs[q].rf_tol > 0);  // the accurate kernel and the histogram layout
+    if (largs[q].rf_tol > 0) acc_class[2 * a->n_det + largs[q].cplx] = true;
   }
   for (int c = 0; c < kMultiClasses; ++c) n_units += units_d[c];
   // capacity (growing invalidates captured graphs: their pointers change)
@@ -1376,8 +1472,10 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     L.part = b->d_part + poff;
     L.order = b->d_order + off;
     L.order_hist = b->d_hist + hoff;
-    hoff += 2 * (size_t)L.order_keys;
+    L.rf_count = L.order_hist + 2 * L.order_keys;  // this item's marked points
+    hoff += 2 * (size_t)L.order_keys + 1;
     L.status = b->d_status;
+    L.rf_total = b->d_counter + 2 * kMultiClasses;
     b->h_args[q] = L;
     b->h_off[q] = off;
     const int64_t tiles = (items[q].B + kPointsPerCta - 1) / kPointsPerCta;
@@ -1398,16 +1496,19 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
   m.counter = b->d_counter;
   m.ordered = 1;
   int ctas[kMultiClasses] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int c = 2; c < kMultiClasses; ++c)
+  int ctas_acc[kMultiClasses] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 2; c < kMultiClasses; ++c) {
     if (units_d[c] > 0)
-      ctas[c] = (int)std::min<int64_t>(units_d[c], (int64_t)sm_count() * multi_tf2_ctas_per_sm(c));
+      ctas[c] = (int)std::min<int64_t>(units_d[c], (int64_t)sm_count() * multi_tf2_ctas_per_sm(c, false));
+    if (units_d[c] > 0 && acc_class[c]) ctas_acc[c] = sm_count() * multi_tf2_ctas_per_sm(c, true);
+  }
   auto enqueue = [&]() -> int {
     GWL_CUDA(cudaMemcpyAsync(b->d_args, b->h_args, n * sizeof(LaunchArgs), cudaMemcpyHostToDevice, s));
     GWL_CUDA(cudaMemcpyAsync(b->d_off, b->h_off, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     GWL_CUDA(cudaMemcpyAsync(b->d_units, b->h_units, n_units * sizeof(int4), cudaMemcpyHostToDevice, s));
-    GWL_CUDA(cudaMemsetAsync(b->d_counter, 0, 8 * sizeof(int), s));
+    GWL_CUDA(cudaMemsetAsync(b->d_counter, 0, kMultiCounters * sizeof(int), s));
     GWL_CUDA(cudaMemsetAsync(b->d_hist, 0, hoff * sizeof(int32_t), s));
-    GWL_CUDA(launch_multi(m, ctas, s));
+    GWL_CUDA(launch_multi(m, ctas, ctas_acc, s, &b->side));
     return GWL_OK;
   };
   if (b->use_graphs && s != nullptr) {  // the legacy default stream cannot be captured
@@ -1438,6 +1539,21 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
   }
   GWL_CUDA(cudaEventRecord(b->staged, s));
   b->staged_pending = true;
+  return GWL_OK;
+}
+
+int gwl_batcher_last_refined(gwl_batcher* b, void* stream, int64_t* count) {
+  if (!b || !count) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *count = 0;
+  std::lock_guard<std::mutex> g(b->mu);
+  if (!b->d_counter) return GWL_OK;
+  int n = 0;
+  GWL_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  GWL_CUDA(cudaMemcpy(&n, b->d_counter + 2 * kMultiClasses, sizeof(int), cudaMemcpyDeviceToHost));
+  *count = n;
   return GWL_OK;
 }
 

@@ -29,6 +29,17 @@ constexpr int kDevStatusOk = 0;
 constexpr int kDevStatusTimeout = 1;
 constexpr int kDevStatusBadInput = 2;
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
+// Refinement of the TaylorF2 mixed-precision result (see LaunchArgs::rf_tol):
+// the error bound of a point is kRefineL2 * L2 + kRefineL1 * L1, with L2 the
+// Euclidean norm of its per-bin terms |<d|h>_k| and L1 their sum over the
+// bins where the data are signal-dominated (whitened power 4 |d|^2 / (T S)
+// above kRefineLoudPower).  The coefficients hold with a margin of 2.5 to 4
+// over the measured error of the fast kernel on short, loud analyses.
+constexpr double kRefineL2 = 1e-6;
+constexpr double kRefineL1 = 1e-7;
+constexpr double kRefineLoudPower = 10.0;
+constexpr double kRefineDefaultTol = 5e-4;
+constexpr int kCosTable = 1024;        // angles of the float-float cos / sin table of the accurate kernel
 
 // Per-point quantities computed once per evaluation by the float64 prologue.
 struct PointRec {
@@ -45,6 +56,7 @@ struct PointRec {
   float c_lo[kNumBasis + 1];         // index kNumBasis: frac of the constant term
   int64_t k_start, k_end;            // TaylorF2 band [k_start, k_end) on the analysis grid
   int32_t valid;                     // 0: waveform undefined (lnL = nan_to_num(-inf))
+  int32_t refine;                    // TaylorF2 mixed: error bound above the tolerance (LaunchArgs::rf_tol)
 };
 
 struct DetGeom {
@@ -85,6 +97,18 @@ struct LaunchArgs {
   double* dh_out;                       // optional [2B] complex <d|h> totals
   double* hh_out;                       // optional [B] <h|h> totals
   int* status;                          // device status word
+  // error control of the TaylorF2 mixed-precision sums: the prologue bounds
+  // each point's error from the prefix sums rf_p2 (|w|^2) and rf_p1 (|w| over
+  // signal-dominated bins); a point whose bound exceeds rf_tol is marked
+  // (PointRec::refine), counted in rf_count and ordered into the first slots,
+  // which the accurate variant of the bin-walking kernel evaluates (float-float
+  // cosine from cos_tab, TwoSum accumulation per bin).  rf_tol <= 0: off.
+  const double* rf_p2[kMaxDet];         // [n_bins + 1]
+  const double* rf_p1[kMaxDet];         // [n_bins + 1]
+  double rf_tol;
+  int* rf_count;                        // marked points of this analysis (zeroed with the ordering histogram)
+  int* rf_total;                        // optional: marked points of the whole launch
+  const float4* cos_tab;                // [kCosTable] {cos hi, cos lo, sin hi, sin lo} of 2 pi q / kCosTable
   // optional point ordering (TaylorF2 mixed): thread slot s of the bin-walking
   // kernel evaluates point order[s]; points are grouped by the chunk that
   // holds their band end, longest first, so that the 128 points of a CTA stop
@@ -92,6 +116,7 @@ struct LaunchArgs {
   int32_t* order;                       // [B]
   int32_t* order_hist;                  // [2 * order_keys]: counts (then bases), cursors; zeroed before use
   int order_keys, order_shift;
+  int order_half;                       // keys of marked points (PointRec::refine) are offset by this
   // marginalisation
   int time_marg, phase_marg, dist_marg, jitter;
   double t_min, t_max, delta_tc, start_time0;
@@ -145,7 +170,8 @@ struct MultiArgs {
   int64_t total_points;
   const int4* units;        // [n_units] {item, tile, group, 0}, grouped by kernel class
   int64_t unit_begin[9];    // units of class q = 2 D + cplx: [unit_begin[q], unit_begin[q + 1])
-  int* counter;             // [8], zeroed before the launch
+  int* counter;             // [kMultiCounters], zeroed before the launch: units taken per class by the
+                            // fast kernels, then by the accurate kernels, then the marked points
   int ordered;              // items carry a point ordering (LaunchArgs::order)
 };
 
@@ -158,20 +184,41 @@ struct PriorEntry {
   const double* y;
 };
 
+// A second, high-priority stream on which the accurate kernel runs beside the
+// fast one: forked from the launching stream after the ordering and joined
+// before the reduction (both capturable in a CUDA graph).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+cudaError_t side_stream_create(SideStream* s);
+void side_stream_destroy(SideStream* s);
+cudaError_t side_fork(SideStream& side, cudaStream_t s);   // side waits for the work enqueued so far on s
+cudaError_t side_join(SideStream& side, cudaStream_t s);   // s waits for the work enqueued so far on side
+
 // Kernel launchers (defined in gwl_kernels.cu / gwl_marg.cu).
 constexpr int kMultiMaxDet = 3;
 constexpr int kMultiClasses = 2 * (kMultiMaxDet + 1);  // kernel class q = 2 * detectors + cplx
-cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s);
-int multi_tf2_ctas_per_sm(int q);
+constexpr int kMultiCounters = 2 * kMultiClasses + 1;  // unit counters (fast, accurate), then the marked points
+cudaError_t launch_multi(const MultiArgs& m, const int* ctas, const int* ctas_acc, cudaStream_t s, SideStream* side);
+int multi_tf2_ctas_per_sm(int q, bool acc);
 cudaError_t launch_prologue(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_plain(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
+// The accurate kernel for the marked points (nothing when rf_tol <= 0).
+cudaError_t launch_mixed_acc(const LaunchArgs& a, cudaStream_t s);
+
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
+// Ordering of a mixed TaylorF2 launch: the band-end keys, doubled when points
+// can be marked for the accurate kernel (rf_tol > 0; their keys take the upper
+// half); the marked count follows the 2 * order_keys histogram words (zeroed
+// with them: 2 * order_keys + 1 words in all).  order_hist, if set, must hold them.
+void ordering_with_marks(LaunchArgs& L);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,

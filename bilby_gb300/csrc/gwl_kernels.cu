@@ -24,13 +24,15 @@ __device__ __forceinline__ double par(const LaunchArgs& a, int slot, int64_t i) 
 }
 
 // ---------------------------------------------------------------------------
-// point ordering: bucket of a point = the chunk that holds its band end
+// point ordering: bucket of a point = the chunk that holds its band end;
+// points marked for the accurate kernel take the upper half of the keys, so
+// that (buckets in descending order) they fill the first slots
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int order_key(const LaunchArgs& a, const PointRec& r) {
   if (!r.valid || r.k_end <= r.k_start) return 0;
   int64_t c = (r.k_end - a.k_base + a.chunk - 1) / a.chunk;
   c = c < 0 ? 0 : (c > a.n_chunks ? a.n_chunks : c);
-  return (int)(c >> a.order_shift);
+  return (int)(c >> a.order_shift) + (r.refine ? a.order_half : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -153,6 +155,22 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
     r.c_lo[kNumBasis] = s.lo;
   }
   r.valid = ok ? 1 : 0;
+  if (a.rf_tol > 0 && r.valid && a.model == GWL_MODEL_TAYLORF2) {
+    // error bound of the fast mixed-precision sums (kRefineL2): norms of the
+    // per-bin terms |<d|h>_k| = 4/T A0 |Q_d| f^(-7/6) |d_k| / S_k over the band
+    const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+    double l2 = 0.0, l1 = 0.0;
+    for (int d = 0; d < a.n_det; ++d) {
+      const double s = 4.0 / a.duration * a.w_scale[d] * r.amp * r.qabs[d];
+      l2 += s * s * (a.rf_p2[d][k1] - a.rf_p2[d][k0]);
+      l1 += s * (a.rf_p1[d][k1] - a.rf_p1[d][k0]);
+    }
+    if (kRefineL2 * sqrt(fmax(l2, 0.0)) + kRefineL1 * l1 > a.rf_tol) {
+      r.refine = 1;
+      atomicAdd(a.rf_count, 1);
+      if (a.rf_total) atomicAdd(a.rf_total, 1);
+    }
+  }
   a.rec[i] = r;
   if (a.order_hist) atomicAdd(&a.order_hist[order_key(a, r)], 1);
 }
@@ -450,6 +468,41 @@ __device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const
   }
 }
 
+// Accurate variant, for the points the prologue marks (LaunchArgs::rf_tol).
+// The hardware cosine's error is a smooth function of the angle, so it adds up
+// coherently where a template follows a loud signal in the data, and so do the
+// roundings of float32 sums of 8 such terms.  Here cos and sin of 2 pi u 2^-32
+// are float-float pairs hi + lo: the table entry at the nearest 1/kCosTable
+// cycle (float-float of the float64 values) rotated by the remainder r,
+// |r| <= pi / kCosTable, with cos r - 1 = -r^2/2 + r^4/24 and sin r = r - r^3/6
+// (truncation below 3e-15); each term is added into the chunk's float-float
+// sum by TwoSum.  What remains is rounding of single terms (the weight
+// magnitude, the product), independent from bin to bin.
+static_assert(kCosTable == 1024, "cos_sin_fixed splits the angle as 10 + 22 bits");
+
+template <bool SIN>
+__device__ __forceinline__ void cos_sin_fixed(const float4* tab, uint32_t u, float& ch, float& cl, float& sh,
+                                              float& sl) {
+  const uint32_t q = (u + (1u << 21)) >> 22;  // nearest table angle (q = kCosTable wraps to entry 0)
+  const float r = __fmul_rn((float)(int32_t)(u - (q << 22)), 1.4629180792671596e-09f);  // |u - q 2^22| <= 2^21: exact
+  const float4 t = tab[q & (kCosTable - 1)];
+  const float z = __fmul_rn(r, r);
+  const float cm1 = __fmul_rn(z, __fmaf_rn(z, 1.0f / 24.0f, -0.5f));
+  const float sr = __fmul_rn(r, __fmaf_rn(z, -1.0f / 6.0f, 1.0f));
+  ch = t.x;
+  cl = __fadd_rn(t.y, __fmaf_rn(t.x, cm1, -__fmul_rn(t.z, sr)));
+  if (SIN) {
+    sh = t.z;
+    sl = __fadd_rn(t.w, __fmaf_rn(t.z, cm1, __fmul_rn(t.x, sr)));
+  }
+}
+
+// hi + lo += m (c_hi + c_lo)
+__device__ __forceinline__ void acc_ff(float& hi, float& lo, float m, float c_hi, float c_lo) {
+  two_sum_acc(hi, lo, __fmul_rn(m, c_hi));
+  lo = __fmaf_rn(m, c_lo, lo);
+}
+
 // A whole 8-bin block of the anchored recurrence.  DEG is the degree of the
 // phase polynomial about the anchor: with DEG < 6 the higher differences are
 // zero, so the adds skipped here would only add zero.
@@ -492,8 +545,7 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const uint2* w
         ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
         ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
       }
-      const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
-      const uint32_t bu = (uint32_t)__float2int_rn(__fmul_rn(base, 4294967296.0f));
+      const uint32_t bu = (uint32_t)((to_fixed(s_hi, s_lo) + 0x80000000ull) >> 32);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const uint2 wv = w[d * CH + j];
@@ -516,15 +568,17 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const uint2* w
 
 // One work unit: the points of tile `tile` over the chunks g, g + G, ...
 // `it_global` counts the chunks this CTA has consumed so far (all units): it
-// selects the shared-memory stage and the mbarrier phase.
+// selects the shared-memory stage and the mbarrier phase.  The first n_acc
+// slots hold the points marked by the prologue (the ordering puts them
+// first): the accurate kernel evaluates them, this one skips them.
 template <int D, bool CPLX>
 __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t g, uint2* s_w, uint64_t* bar,
-                         unsigned long long* s_kmax, int64_t& it_global) {
+                         unsigned long long* s_kmax, int64_t& it_global, int64_t n_acc) {
   constexpr int CH = kChunkMixed;
   const int64_t slot = tile * kPointsPerCta + threadIdx.x;
   const int64_t i = slot < a.B && a.order ? (int64_t)a.order[slot] : slot;
   const int64_t G = a.n_groups;
-  const bool have = slot < a.B && i >= 0 && i < a.B;
+  const bool have = slot < a.B && i >= 0 && i < a.B && slot >= n_acc;
   int64_t ks = 0, ke = 0;
   bool valid = false;
   if (have) {
@@ -706,7 +760,102 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_mixed_tf2(LaunchArgs a) {
   }
   __syncthreads();
   int64_t it_global = 0;
-  tf2_unit<D, CPLX>(a, blockIdx.x, blockIdx.y, reinterpret_cast<uint2*>(smem), bar, &s_kmax, it_global);
+  const int64_t n_acc = a.rf_count ? *a.rf_count : 0;
+  tf2_unit<D, CPLX>(a, blockIdx.x, blockIdx.y, reinterpret_cast<uint2*>(smem), bar, &s_kmax, it_global, n_acc);
+}
+
+__device__ __forceinline__ void load_cos_table(float4* tab, const float4* src) {
+  for (int q = threadIdx.x; q < kCosTable; q += blockDim.x) tab[q] = src[q];
+}
+
+// Accurate variant: one (marked point, chunk group) unit per warp.  Lane l
+// takes bins k0 + l + 32 j of each chunk g, g + G, ... of the group (the
+// chunks the fast kernel's CTA g walks), within the point's band.  Every bin's
+// phase is evaluated in float-float from the basis table, so the lanes are
+// independent (no recurrence to carry) and a point's 512-bin chunk costs 16
+// bins of latency; the angle is summed in 64-bit fixed point (phase, time
+// shift, detector offset, weight angle) and rounded once to 0.32; cos / sin
+// from cos_sin_fixed; each term added by TwoSum; the lanes' sums reduced in
+// float64 in a fixed order.  Writes the group's partial sums of the point.
+constexpr int kAccThreads = 256;
+
+template <int D, bool CPLX>
+__device__ void acc_unit(const LaunchArgs& a, int64_t i, int64_t g, const float4* tab) {
+  const int lane = threadIdx.x & 31;
+  const PointRec& r = a.rec[i];
+  const int64_t ks = r.k_start, ke = r.k_end;
+  float ch[kNumBasis + 1], cl[kNumBasis + 1];
+#pragma unroll
+  for (int b = 0; b <= kNumBasis; ++b) {
+    ch[b] = r.c_hi[b];
+    cl[b] = r.c_lo[b];
+  }
+  uint64_t X[D], Q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    X[d] = ((uint64_t)r.xfix[d][1] << 32) | r.xfix[d][0];
+    Q[d] = CPLX ? 0ull : (((uint64_t)r.qfix[d][1] << 32) | r.qfix[d][0]);
+  }
+  float ahi[D], alo[D], bhi[D], blo[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
+  for (int64_t c = g; c < a.n_chunks; c += a.n_groups) {
+    const int64_t k0 = a.k_base + c * kChunkMixed;
+    if (k0 >= ke) break;
+    if (k0 + kChunkMixed <= ks) continue;
+    for (int j = lane; j < kChunkMixed; j += 32) {
+      const int64_t k = k0 + j;
+      if (k < ks || k >= ke) continue;
+      const float4* bp = reinterpret_cast<const float4*>(a.basis + k * kNumBasis);
+      float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+      for (int q = 0; q < kNumBasis / 2; ++q) {
+        const float4 v = __ldg(bp + q);
+        ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+        ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
+      }
+      const uint64_t base = to_fixed(s_hi, s_lo);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const uint2 wv = __ldg(a.wp[d] + k);
+        const uint64_t full = base + (uint64_t)k * X[d] + Q[d] + ((uint64_t)wv.y << 32);
+        float c_h, c_l, s_h, s_l;
+        cos_sin_fixed<CPLX>(tab, (uint32_t)((full + 0x80000000ull) >> 32), c_h, c_l, s_h, s_l);
+        const float mag = __uint_as_float(wv.x);
+        acc_ff(ahi[d], alo[d], mag, c_h, c_l);
+        if (CPLX) acc_ff(bhi[d], blo[d], mag, s_h, s_l);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double re = (double)ahi[d] + (double)alo[d];
+    double im = CPLX ? (double)bhi[d] + (double)blo[d] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      if (CPLX) im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+      a.part[((g * D + d) * kPartStride + 0) * a.B + i] = re;
+      if (CPLX) a.part[((g * D + d) * kPartStride + 1) * a.B + i] = im;
+    }
+  }
+}
+
+// The marked points (first rf_count slots of the ordering), all their groups;
+// the count is read on the device, so the launch shape does not depend on it.
+template <int D, bool CPLX>
+__global__ void __launch_bounds__(kAccThreads) k_mixed_tf2_acc(LaunchArgs a) {
+  __shared__ float4 tab[kCosTable];
+  const int wpc = kAccThreads / 32;
+  const int64_t units = (int64_t)*a.rf_count * a.n_groups;
+  if ((int64_t)blockIdx.x * wpc >= units) return;
+  load_cos_table(tab, a.cos_tab);
+  __syncthreads();
+  const int64_t nw = (int64_t)gridDim.x * wpc;
+  for (int64_t u = (int64_t)blockIdx.x * wpc + (threadIdx.x >> 5); u < units; u += nw)
+    acc_unit<D, CPLX>(a, a.order[u / a.n_groups], u % a.n_groups, tab);
 }
 
 // Sine-Gaussian, mixed precision.  Shared memory per chunk: float32
@@ -1281,6 +1430,7 @@ __global__ void k_finalize(LaunchArgs a) {
   finalize_point(a, i, 1);
 }
 
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -1316,13 +1466,53 @@ template <int D>
 constexpr auto k_mixed_tf2_c = k_mixed_tf2<D, true>;
 template <int D>
 constexpr auto k_mixed_tf2_r = k_mixed_tf2<D, false>;
+template <int D>
+constexpr auto k_mixed_tf2_acc_c = k_mixed_tf2_acc<D, true>;
+template <int D>
+constexpr auto k_mixed_tf2_acc_r = k_mixed_tf2_acc<D, false>;
+
+// resident CTAs per SM of the accurate kernel, per detector count
+static int acc_ctas_per_sm[kMaxDet + 1] = {};
 
 template <int D>
 static cudaError_t set_mixed_smem() {
   const int bytes = 2 * D * kChunkMixed * 8;
-  const cudaError_t e = cudaFuncSetAttribute(k_mixed_tf2<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = cudaFuncSetAttribute(k_mixed_tf2<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_mixed_tf2<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if ((e = cudaFuncSetAttribute(k_mixed_tf2<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) !=
+      cudaSuccess)
+    return e;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mixed_tf2_acc<D, false>, kAccThreads, 0) != cudaSuccess ||
+      n < 1)
+    n = 1;
+  acc_ctas_per_sm[D] = n;
+  return cudaSuccess;
+}
+
+static int sm_count_k() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+// shared-memory limits and occupancies of the mixed TaylorF2 kernels, once
+static cudaError_t configure_mixed() {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e;
+    if ((e = set_mixed_smem<1>()) != cudaSuccess) return e;
+    if ((e = set_mixed_smem<2>()) != cudaSuccess) return e;
+    if ((e = set_mixed_smem<3>()) != cudaSuccess) return e;
+    if ((e = set_mixed_smem<4>()) != cudaSuccess) return e;
+    configured = true;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
@@ -1330,21 +1520,32 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
     dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_chunks);
     GWL_DISPATCH_D(k_mixed_sg, grid, kPointsPerCta, 0, s, a);
   } else {
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e;
-      if ((e = set_mixed_smem<1>()) != cudaSuccess) return e;
-      if ((e = set_mixed_smem<2>()) != cudaSuccess) return e;
-      if ((e = set_mixed_smem<3>()) != cudaSuccess) return e;
-      if ((e = set_mixed_smem<4>()) != cudaSuccess) return e;
-      configured = true;
-    }
+    const cudaError_t ce = configure_mixed();
+    if (ce != cudaSuccess) return ce;
     dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_groups);
     const int smem = 2 * a.n_det * kChunkMixed * 8;
     if (a.cplx) {
       GWL_DISPATCH_D(k_mixed_tf2_c, grid, kPointsPerCta, smem, s, a);
     } else {
       GWL_DISPATCH_D(k_mixed_tf2_r, grid, kPointsPerCta, smem, s, a);
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_acc(const LaunchArgs& a, cudaStream_t s) {
+  if (a.model != GWL_MODEL_TAYLORF2 || !(a.rf_tol > 0) || !a.rf_count || !a.order || a.B <= 0) return cudaSuccess;
+  {
+    const cudaError_t ce = configure_mixed();
+    if (ce != cudaSuccess) return ce;
+    // the marked points (first slots of the ordering), one warp per (point, group)
+    const int64_t warps = a.B * a.n_groups;
+    const unsigned g_acc = (unsigned)min((warps + kAccThreads / 32 - 1) / (kAccThreads / 32),
+                                         (int64_t)sm_count_k() * acc_ctas_per_sm[min(a.n_det, kMaxDet)]);
+    if (a.cplx) {
+      GWL_DISPATCH_D(k_mixed_tf2_acc_c, g_acc, kAccThreads, 0, s, a);
+    } else {
+      GWL_DISPATCH_D(k_mixed_tf2_acc_r, g_acc, kAccThreads, 0, s, a);
     }
   }
   return cudaGetLastError();
@@ -1385,6 +1586,15 @@ void order_layout(int64_t n_chunks, int* keys, int* shift) {
   while ((n_chunks >> sh) + 1 > kOrderMaxKeys) ++sh;
   *shift = sh;
   *keys = (int)(n_chunks >> sh) + 1;
+}
+
+void ordering_with_marks(LaunchArgs& L) {
+  int keys = 0, shift = 0;
+  order_layout(L.n_chunks, &keys, &shift);
+  L.order_shift = shift;
+  L.order_half = L.rf_tol > 0 ? keys : 0;
+  L.order_keys = L.rf_tol > 0 ? 2 * keys : keys;
+  L.rf_count = L.order_hist ? L.order_hist + 2 * L.order_keys : nullptr;
 }
 
 // Bases of the buckets counted by the prologue, then each point's slot.
@@ -1475,14 +1685,47 @@ __global__ void __launch_bounds__(kPointsPerCta, 5) k_multi_tf2(MultiArgs m) {
     const int64_t u = s_unit;
     if (u >= ue) break;
     const int4 wu = m.units[u];
-    tf2_unit<D, CPLX>(m.args[wu.x], wu.y, wu.z, s_w, bar, &s_kmax, it_global);
+    const LaunchArgs& a = m.args[wu.x];
+    tf2_unit<D, CPLX>(a, wu.y, wu.z, s_w, bar, &s_kmax, it_global, a.rf_count ? *a.rf_count : 0);
   }
 }
 
+// Accurate variant for the items of class (D, CPLX): the warps of the grid
+// take the (marked point, group) units of each item in turn, continuing the
+// round-robin from item to item.
 template <int D, bool CPLX>
+__global__ void __launch_bounds__(kAccThreads) k_multi_tf2_acc(MultiArgs m) {
+  __shared__ float4 tab[kCosTable];
+  const int wpc = kAccThreads / 32;
+  const int64_t nw = (int64_t)gridDim.x * wpc, w = (int64_t)blockIdx.x * wpc + (threadIdx.x >> 5);
+  bool loaded = false;
+  int64_t base = 0;  // units of the earlier items of the class
+  for (int it = 0; it < m.n_items; ++it) {
+    const LaunchArgs& a = m.args[it];
+    if (a.n_det != D || (a.cplx != 0) != CPLX || !a.rf_count || !(a.rf_tol > 0)) continue;
+    const int64_t units = (int64_t)*a.rf_count * a.n_groups;
+    if (units == 0) continue;
+    if (!loaded) {  // uniform over the CTA: every thread sees the same items and counts
+      load_cos_table(tab, a.cos_tab);
+      __syncthreads();
+      loaded = true;
+    }
+    for (int64_t u = ((w - base) % nw + nw) % nw; u < units; u += nw)
+      acc_unit<D, CPLX>(a, a.order[u / a.n_groups], u % a.n_groups, tab);
+    base += units;
+  }
+}
+
+template <int D, bool CPLX, bool ACC>
 static int ctas_per_sm_d() {
   static int n = 0;
   if (n == 0) {
+    if (ACC) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_multi_tf2_acc<D, CPLX>, kAccThreads, 0) != cudaSuccess ||
+          n < 1)
+        n = 1;
+      return n;
+    }
     const int smem = 2 * D * kChunkMixed * 8;
     if (cudaFuncSetAttribute(k_multi_tf2<D, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return 1;
@@ -1493,18 +1736,47 @@ static int ctas_per_sm_d() {
   return n;
 }
 
-int multi_tf2_ctas_per_sm(int q) {
+int multi_tf2_ctas_per_sm(int q, bool acc) {
   switch (q) {
-    case 2: return ctas_per_sm_d<1, false>();
-    case 3: return ctas_per_sm_d<1, true>();
-    case 4: return ctas_per_sm_d<2, false>();
-    case 5: return ctas_per_sm_d<2, true>();
-    case 6: return ctas_per_sm_d<3, false>();
-    default: return ctas_per_sm_d<3, true>();
+    case 2: return acc ? ctas_per_sm_d<1, false, true>() : ctas_per_sm_d<1, false, false>();
+    case 3: return acc ? ctas_per_sm_d<1, true, true>() : ctas_per_sm_d<1, true, false>();
+    case 4: return acc ? ctas_per_sm_d<2, false, true>() : ctas_per_sm_d<2, false, false>();
+    case 5: return acc ? ctas_per_sm_d<2, true, true>() : ctas_per_sm_d<2, true, false>();
+    case 6: return acc ? ctas_per_sm_d<3, false, true>() : ctas_per_sm_d<3, false, false>();
+    default: return acc ? ctas_per_sm_d<3, true, true>() : ctas_per_sm_d<3, true, false>();
   }
 }
 
-cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s) {
+cudaError_t side_stream_create(SideStream* side) {
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithPriority(&side->stream, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
+  if ((e = cudaEventCreateWithFlags(&side->fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+  return cudaEventCreateWithFlags(&side->join, cudaEventDisableTiming);
+}
+
+void side_stream_destroy(SideStream* side) {
+  if (side->stream) cudaStreamSynchronize(side->stream);
+  if (side->fork) cudaEventDestroy(side->fork);
+  if (side->join) cudaEventDestroy(side->join);
+  if (side->stream) cudaStreamDestroy(side->stream);
+  *side = SideStream();
+}
+
+cudaError_t side_fork(SideStream& side, cudaStream_t s) {
+  cudaError_t e = cudaEventRecord(side.fork, s);
+  if (e != cudaSuccess) return e;
+  return cudaStreamWaitEvent(side.stream, side.fork, 0);
+}
+
+cudaError_t side_join(SideStream& side, cudaStream_t s) {
+  cudaError_t e = cudaEventRecord(side.join, side.stream);
+  if (e != cudaSuccess) return e;
+  return cudaStreamWaitEvent(s, side.join, 0);
+}
+
+cudaError_t launch_multi(const MultiArgs& m, const int* ctas, const int* ctas_acc, cudaStream_t s, SideStream* side) {
   const int threads = kPointThreads;
   const unsigned pblocks = (unsigned)((m.total_points + threads - 1) / threads);
   k_multi_prologue<<<pblocks, threads, 0, s>>>(m);
@@ -1514,6 +1786,24 @@ cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s) {
     k_multi_order_scan<<<(unsigned)m.n_items, kOrderThreads, 0, s>>>(m);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_multi_order_scatter<<<(unsigned)((m.total_points + 127) / 128), 128, 0, s>>>(m);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  // the accurate kernels on the side stream, beside the fast ones
+  bool any_acc = false;
+  for (int q = 2; q < kMultiClasses; ++q) any_acc = any_acc || ctas_acc[q] > 0;
+  cudaStream_t sa = any_acc && side ? side->stream : s;
+  if (any_acc && side && (e = side_fork(*side, s)) != cudaSuccess) return e;
+  for (int q = 2; q < kMultiClasses; ++q) {
+    if (ctas_acc[q] <= 0) continue;
+    const unsigned ga = (unsigned)ctas_acc[q];
+    switch (q) {
+      case 2: k_multi_tf2_acc<1, false><<<ga, kAccThreads, 0, sa>>>(m); break;
+      case 3: k_multi_tf2_acc<1, true><<<ga, kAccThreads, 0, sa>>>(m); break;
+      case 4: k_multi_tf2_acc<2, false><<<ga, kAccThreads, 0, sa>>>(m); break;
+      case 5: k_multi_tf2_acc<2, true><<<ga, kAccThreads, 0, sa>>>(m); break;
+      case 6: k_multi_tf2_acc<3, false><<<ga, kAccThreads, 0, sa>>>(m); break;
+      default: k_multi_tf2_acc<3, true><<<ga, kAccThreads, 0, sa>>>(m); break;
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   for (int q = 2; q < kMultiClasses; ++q) {
@@ -1530,6 +1820,7 @@ cudaError_t launch_multi(const MultiArgs& m, const int* ctas, cudaStream_t s) {
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  if (any_acc && side && (e = side_join(*side, s)) != cudaSuccess) return e;
   const int64_t chains = m.total_points * kMultiMaxDet * 2;
   k_multi_reduce<<<(unsigned)((chains + 127) / 128), 128, 0, s>>>(m);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

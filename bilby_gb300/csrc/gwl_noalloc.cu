@@ -6,9 +6,12 @@
 // run its likelihood calls on a latency-critical path where the device-wide
 // synchronisation of cudaMalloc / cudaFree is not acceptable.  For them
 // gwl_eval_device_noalloc runs the mixed-precision TaylorF2 launch sequence
-// (per-point prologue, fused likelihood kernel, finalize) with its work space
-// -- the per-point records, the split-K partial sums and the device status
-// word -- in one statically allocated device buffer of kNoAllocScratchBytes
+// (per-point prologue, band-end ordering, fused likelihood kernel and its
+// accurate variant for the points whose error bound exceeds the tolerance,
+// finalize) with its work space -- the device status word, the ordering
+// histogram with the count of marked points, the per-point records, the
+// split-K partial sums and the ordering -- in one statically allocated device
+// buffer of kNoAllocScratchBytes
 // that every GPU loading this library holds until the process exits.
 //
 // The caller passes the parameter block and the result buffer.  The first
@@ -76,15 +79,21 @@ extern "C" int gwl_eval_device_noalloc(gwl_analysis* a, const double* params, in
   size_t rec_bytes = 0, part_bytes = 0;
   int rc = noalloc_launch_args(a, B, &L, &rec_bytes, &part_bytes);
   if (rc) return rc;
-  const size_t rec_off = kAlign;  // the status word occupies the first aligned slot
+  // the status word, then the ordering histogram and the marked count: one memset clears them
+  ordering_with_marks(L);
+  const size_t head_bytes = sizeof(int) + sizeof(int32_t) * (2 * (size_t)L.order_keys + 1);
+  const size_t rec_off = align_up(head_bytes);
   const size_t part_off = rec_off + align_up(rec_bytes);
-  const size_t need = part_off + part_bytes;
+  const size_t order_off = part_off + align_up(part_bytes);
+  const size_t order_bytes = (size_t)B * sizeof(int32_t);
+  const size_t need = order_off + order_bytes;
   if (need > kNoAllocScratchBytes) {
-    const size_t per_point = rec_bytes / (size_t)B + part_bytes / (size_t)B;
+    const size_t per_point = rec_bytes / (size_t)B + part_bytes / (size_t)B + sizeof(int32_t);
     set_error("gwl_eval_device_noalloc: " + std::to_string(B) + " points need " + std::to_string(need) +
               " bytes of scratch, more than the " + std::to_string(kNoAllocScratchBytes) +
               "-byte static buffer; at most about " +
-              std::to_string((kNoAllocScratchBytes - 2 * kAlign) / per_point) + " points fit for this analysis");
+              std::to_string((kNoAllocScratchBytes - rec_off - 3 * kAlign) / per_point) +
+              " points fit for this analysis");
     return GWL_ERR_ARGUMENT;
   }
   unsigned char* scratch = static_cast<unsigned char*>(base);
@@ -96,10 +105,15 @@ extern "C" int gwl_eval_device_noalloc(gwl_analysis* a, const double* params, in
   L.part = reinterpret_cast<double*>(scratch + part_off);
   L.dh_out = nullptr;
   L.hh_out = nullptr;
-  // The buffer keeps the previous call's contents: the status word must start
-  // at zero; the records and partial sums are fully written before being read.
-  if ((e = cudaMemsetAsync(L.status, 0, sizeof(int), s)) != cudaSuccess ||
-      (e = launch_prologue(L, s)) != cudaSuccess || (e = launch_mixed(L, s)) != cudaSuccess ||
+  L.order_hist = reinterpret_cast<int32_t*>(scratch + sizeof(int));
+  L.rf_count = L.order_hist + 2 * L.order_keys;
+  L.order = reinterpret_cast<int32_t*>(scratch + order_off);
+  // The buffer keeps the previous call's contents: the status word, the
+  // histogram and the marked count must start at zero; the records, partial
+  // sums and ordering are fully written before being read.
+  if ((e = cudaMemsetAsync(scratch, 0, head_bytes, s)) != cudaSuccess ||
+      (e = launch_prologue(L, s)) != cudaSuccess || (e = launch_order(L, s)) != cudaSuccess ||
+      (e = launch_mixed(L, s)) != cudaSuccess || (e = launch_mixed_acc(L, s)) != cudaSuccess ||
       (e = launch_finalize(L, s)) != cudaSuccess) {
     set_error(std::string("gwl_eval_device_noalloc: ") + cudaGetErrorString(e));
     return GWL_ERR_CUDA;

@@ -338,6 +338,25 @@ int gwl_autotune(gwl_analysis *a, const double *params, int64_t B, void *stream,
 int gwl_get_chunks_per_group(gwl_analysis *a, int32_t *chunks_per_group);
 int gwl_set_chunks_per_group(gwl_analysis *a, int32_t chunks_per_group);
 
+/* Error control of the mixed-precision TaylorF2 result (no counterpart in the
+ * reference, which evaluates in float64 only).  The prologue bounds each
+ * point's |Delta lnL| from prefix sums of the data weights:
+ * 1e-6 L2 + 1e-7 L1, with L2 the Euclidean norm of the per-bin terms
+ * |<d|h>_k| over the point's band and L1 their sum over the bins where the
+ * data are signal-dominated (whitened power above 10), the place where the
+ * error of the hardware cosine adds up coherently.  Points whose bound
+ * exceeds `tolerance` (default 5e-4) are ordered first and evaluated by an
+ * accurate variant of the kernel (float-float cosine from a table, TwoSum
+ * accumulation of every term); tolerance <= 0 turns this off.  The choice
+ * depends only on the point and the analysis, so a point's result does not
+ * depend on the batch it is evaluated in.  gwl_last_refined waits for
+ * `stream` and returns how many points the last mixed evaluation of `a`
+ * marked; gwl_batcher_last_refined the same for the batcher's last launch. */
+int gwl_set_refinement(gwl_analysis *a, double tolerance);
+int gwl_get_refinement(gwl_analysis *a, double *tolerance);
+int gwl_last_refined(gwl_analysis *a, void *stream, int64_t *count);
+int gwl_batcher_last_refined(gwl_batcher *b, void *stream, int64_t *count);
+
 /* Description of the last error on this thread ("" if none). */
 const char *gwl_last_error(void);
 

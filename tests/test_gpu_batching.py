@@ -54,10 +54,10 @@ def test_batched_equals_single(mix, graphs):
 
 
 def test_batched_fp64_and_mixed_agree(mix):
-    """Mixed vs float64 through the batcher: |dlnL| <= 1e-3 for |lnL| < 1e4;
-    for templates far louder than the data (<h|h> ~ 1e5-1e6, which these
-    10-40 Msun draws at 20-200 Mpc reach) float32 sin/cos and products bound
-    the error relatively: |dlnL| <= 1e-3 + 2e-8 |lnL|."""
+    """Mixed vs float64 through the batcher: |dlnL| <= 1e-3 for every point,
+    including templates far louder than the data (<h|h> ~ 1e5-1e6, which these
+    10-40 Msun draws at 20-200 Mpc reach), whose sums the refinement step
+    recomputes."""
     from bilby_gb300.batching import Batcher
     ws, likes, blocks = mix
     bat = Batcher()
@@ -66,7 +66,5 @@ def test_batched_fp64_and_mixed_agree(mix):
     fp64 = bat.eval_host(items, "fp64")
     for q in range(len(items)):
         err = np.abs(mixed[q] - fp64[q])
-        assert np.all(err <= 1e-3 + 2e-8 * np.abs(fp64[q])), err
-        quiet = np.abs(fp64[q]) < 1e4
-        assert np.all(err[quiet] <= 1e-3), err[quiet]
+        assert np.all(err <= 1e-3), (err.max(), fp64[q][np.argmax(err)])
     bat.close()
