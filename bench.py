@@ -498,6 +498,13 @@ def _cpu_eval(p):
     return R.log_likelihood_ratio(_CPU["dets"], _CPU["src"], p)
 
 
+def _cpu_eval_timed(p):
+    """Seconds one evaluation takes inside its worker process."""
+    t0 = time.perf_counter()
+    _cpu_eval(p)
+    return time.perf_counter() - t0
+
+
 class CpuBaseline:
     """The oracle (numpy restatement of bilby's log_likelihood_ratio) on all
     host cores: one spawned process per core, OMP_NUM_THREADS=1."""
@@ -524,9 +531,12 @@ class CpuBaseline:
         pts = [self.point(self.params, (self.offset + i) % 4096) for i in range(n)]
         self.offset += n
         t0 = time.perf_counter()
-        self.pool.map(_cpu_eval, pts, chunksize=max(1, n // (4 * self.cores)))
+        lat = np.array(self.pool.map(_cpu_eval_timed, pts, chunksize=max(1, n // (4 * self.cores))))
         dt = time.perf_counter() - t0
         return {"value": n / dt, "unit": "evals/s", "cores": self.cores, "kind": "port",
+                "latency_ms_p50": float(np.percentile(lat, 50) * 1e3),
+                "latency_ms_p99": float(np.percentile(lat, 99) * 1e3),
+                "latency_note": "one evaluation inside its worker, all workers busy",
                 "sample": f"{n} prior draws of {self.name} through the oracle (numpy restatement of bilby's "
                           f"log_likelihood_ratio), {self.cores} processes, OMP_NUM_THREADS=1, {dt:.1f} s"}
 
