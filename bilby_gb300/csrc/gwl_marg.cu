@@ -26,6 +26,7 @@
 namespace gwl {
 
 constexpr int kTmThreads = 512;
+constexpr int kTmTwiddleRows = 128;  // two-level twiddle tables: L / 2 <= 128 * 128
 
 template <bool MIXED>
 struct TmTypes;
@@ -132,8 +133,31 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   using R = typename TmTypes<MIXED>::R;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[2 * kTmThreads];
+  // mixed: the FFT twiddles exp(-2 pi i q / L), q < L / 2, as products of two
+  // shared-memory tables (q = 128 q1 + q2), instead of loads from global memory
+  __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
   const int64_t L = a.n_fft;
   const double norm = 4.0 / a.duration;
+  if constexpr (MIXED) {
+    const int64_t half = L / 2;
+    for (int q = threadIdx.x; q < kTmTwiddleRows; q += blockDim.x) {
+      const int64_t qh = (int64_t)q * kTmTwiddleRows;
+      tw_hi[q] = qh < half ? reinterpret_cast<const float2*>(twiddle)[qh] : make_float2(1.f, 0.f);
+      tw_lo[q] = q < half ? reinterpret_cast<const float2*>(twiddle)[q] : make_float2(1.f, 0.f);
+    }
+    __syncthreads();
+  }
+  const auto tw = [&](int64_t q) -> C {
+    if constexpr (MIXED) {
+      const float2 h = tw_hi[q / kTmTwiddleRows], l = tw_lo[q % kTmTwiddleRows];
+      C w;
+      w.x = h.x * l.x - h.y * l.y;
+      w.y = h.x * l.y + h.y * l.x;
+      return w;
+    } else {
+      return twiddle[q];
+    }
+  };
   for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
     C* buf = MIXED ? reinterpret_cast<C*>(smem) : reinterpret_cast<C*>(a.tm_work) + (size_t)blockIdx.x * L;
     const PointRec& r = a.rec[i];
@@ -164,7 +188,62 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       const float gah = (float)r.sg_a, gal = (float)(r.sg_a - (double)gah);
       float hh1[D], hh2[D];
       for (int d = 0; d < D; ++d) hh1[d] = hh2[d] = 0.f;
-      for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
+      if (a.model == GWL_MODEL_TAYLORF2) {
+        // The basis values and weights of this thread's next bin are loaded
+        // before the current bin is evaluated, so that their L2 latency
+        // overlaps the float-float phase (the tables span n_pad >= L bins).
+        const int64_t ks = max(r.k_start, a.k_lo), ke = min(r.k_end, a.k_hi);
+        const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
+        float4 vb[kNumBasis / 2];
+        float2 vw[D];
+        int64_t k = threadIdx.x;
+        if (r.valid && k >= ks && k < ke) {
+#pragma unroll
+          for (int q = 0; q < kNumBasis / 2; ++q) vb[q] = __ldg(basis4 + k * (kNumBasis / 2) + q);
+#pragma unroll
+          for (int d = 0; d < D; ++d) vw[d] = __ldg(a.w[d] + k);
+        }
+        for (; k < L; k += blockDim.x) {
+          const int64_t kn = k + blockDim.x;
+          float4 nb[kNumBasis / 2];
+          float2 nw[D];
+          if (r.valid && kn >= ks && kn < ke) {
+#pragma unroll
+            for (int q = 0; q < kNumBasis / 2; ++q) nb[q] = __ldg(basis4 + kn * (kNumBasis / 2) + q);
+#pragma unroll
+            for (int d = 0; d < D; ++d) nw[d] = __ldg(a.w[d] + kn);
+          }
+          float zr = 0.f, zi = 0.f;
+          if (r.valid && k >= ks && k < ke) {
+            float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+            for (int q = 0; q < kNumBasis / 2; ++q) {
+              ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], vb[q].x, vb[q].y);
+              ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], vb[q].z, vb[q].w);
+            }
+            const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+              float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
+              ph -= rintf(ph);
+              float sn, cs;
+              __sincosf(ph * 6.283185307179586f, &sn, &cs);
+              const float2 w = vw[d];
+              const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+              // h conj(d) / S = G conj(e^{i Phi} w)
+              zr += gre[d] * er + gim[d] * ei;
+              zi += gim[d] * er - gre[d] * ei;
+            }
+          }
+          buf[bit_reverse((uint32_t)k, log2L)] = make_float2(zr, zi);
+#pragma unroll
+          for (int q = 0; q < kNumBasis / 2; ++q) vb[q] = nb[q];
+#pragma unroll
+          for (int d = 0; d < D; ++d) vw[d] = nw[d];
+        }
+      }
+      for (int64_t k = threadIdx.x; a.model != GWL_MODEL_TAYLORF2 && k < L; k += blockDim.x) {
         float zr = 0.f, zi = 0.f;
         const bool in_hull = k >= a.k_lo && k < a.k_hi;
         if (r.valid && in_hull) {
@@ -310,7 +389,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const int64_t pos = bf & (h - 1);
         const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
         const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
-        const C w1 = twiddle[pos * s1], w2 = twiddle[pos * s2], w3 = twiddle[(pos + h) * s2];
+        const C w1 = tw(pos * s1), w2 = tw(pos * s2), w3 = tw((pos + h) * s2);
         const C x0 = buf[i0], x1 = buf[i1], x2 = buf[i2], x3 = buf[i3];
         C a0, a1, a2, a3, y0, y1, y2, y3;
         R tr = w1.x * x1.x - w1.y * x1.y, ti = w1.x * x1.y + w1.y * x1.x;
@@ -493,7 +572,8 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
   const int log2L = log2_exact(a.n_fft);
   if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
-  if (a.precision == GWL_PRECISION_MIXED && (size_t)a.n_fft * sizeof(float2) > 200 * 1024)
+  if (a.precision == GWL_PRECISION_MIXED && ((size_t)a.n_fft * sizeof(float2) > 200 * 1024 ||
+                                             a.n_fft / 2 > (int64_t)kTmTwiddleRows * kTmTwiddleRows))
     return cudaErrorInvalidValue;
   cudaError_t e = ensure_twiddles(a.n_fft);
   if (e != cudaSuccess) return e;
