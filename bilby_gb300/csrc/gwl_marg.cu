@@ -147,6 +147,14 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     }
     __syncthreads();
   }
+  // mixed: the distance spline's knots in shared memory, after the FFT buffer
+  float* s_tx = reinterpret_cast<float*>(smem + (MIXED ? L * sizeof(float2) : 0));
+  float* s_ty = s_tx + a.nx;
+  if (MIXED && a.dist_marg) {
+    for (int q = threadIdx.x; q < a.nx; q += blockDim.x) s_tx[q] = a.tx_f[q];
+    for (int q = threadIdx.x; q < a.ny; q += blockDim.x) s_ty[q] = a.ty_f[q];
+    __syncthreads();
+  }
   const auto tw = [&](int64_t q) -> C {
     if constexpr (MIXED) {
       const float2 h = tw_hi[q / kTmTwiddleRows], l = tw_lo[q % kTmTwiddleRows];
@@ -189,58 +197,37 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       float hh1[D], hh2[D];
       for (int d = 0; d < D; ++d) hh1[d] = hh2[d] = 0.f;
       if (a.model == GWL_MODEL_TAYLORF2) {
-        // The basis values and weights of this thread's next bin are loaded
-        // before the current bin is evaluated, so that their L2 latency
-        // overlaps the float-float phase (the tables span n_pad >= L bins).
-        const int64_t ks = max(r.k_start, a.k_lo), ke = min(r.k_end, a.k_hi);
+        // zero the buffer with coalesced stores, then write the in-band bins
+        // (a few thousand of the L) to their bit-reversed slots
+        float4* b4 = reinterpret_cast<float4*>(buf);
+        for (int64_t q = threadIdx.x; q < L / 2; q += blockDim.x) b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
         const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
-        float4 vb[kNumBasis / 2];
-        float2 vw[D];
-        int64_t k = threadIdx.x;
-        if (r.valid && k >= ks && k < ke) {
+        for (int64_t k = ks + threadIdx.x; r.valid && k < ke; k += blockDim.x) {
+          float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
 #pragma unroll
-          for (int q = 0; q < kNumBasis / 2; ++q) vb[q] = __ldg(basis4 + k * (kNumBasis / 2) + q);
-#pragma unroll
-          for (int d = 0; d < D; ++d) vw[d] = __ldg(a.w[d] + k);
-        }
-        for (; k < L; k += blockDim.x) {
-          const int64_t kn = k + blockDim.x;
-          float4 nb[kNumBasis / 2];
-          float2 nw[D];
-          if (r.valid && kn >= ks && kn < ke) {
-#pragma unroll
-            for (int q = 0; q < kNumBasis / 2; ++q) nb[q] = __ldg(basis4 + kn * (kNumBasis / 2) + q);
-#pragma unroll
-            for (int d = 0; d < D; ++d) nw[d] = __ldg(a.w[d] + kn);
+          for (int q = 0; q < kNumBasis / 2; ++q) {
+            const float4 v = __ldg(basis4 + k * (kNumBasis / 2) + q);
+            ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+            ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
           }
+          const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
           float zr = 0.f, zi = 0.f;
-          if (r.valid && k >= ks && k < ke) {
-            float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
 #pragma unroll
-            for (int q = 0; q < kNumBasis / 2; ++q) {
-              ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], vb[q].x, vb[q].y);
-              ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], vb[q].z, vb[q].w);
-            }
-            const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-              const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
-              float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
-              ph -= rintf(ph);
-              float sn, cs;
-              __sincosf(ph * 6.283185307179586f, &sn, &cs);
-              const float2 w = vw[d];
-              const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
-              // h conj(d) / S = G conj(e^{i Phi} w)
-              zr += gre[d] * er + gim[d] * ei;
-              zi += gim[d] * er - gre[d] * ei;
-            }
+          for (int d = 0; d < D; ++d) {
+            const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+            float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
+            ph -= rintf(ph);
+            float sn, cs;
+            __sincosf(ph * 6.283185307179586f, &sn, &cs);
+            const float2 w = __ldg(a.w[d] + k);
+            const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+            // h conj(d) / S = G conj(e^{i Phi} w)
+            zr += gre[d] * er + gim[d] * ei;
+            zi += gim[d] * er - gre[d] * ei;
           }
           buf[bit_reverse((uint32_t)k, log2L)] = make_float2(zr, zi);
-#pragma unroll
-          for (int q = 0; q < kNumBasis / 2; ++q) vb[q] = nb[q];
-#pragma unroll
-          for (int d = 0; d < D; ++d) vw[d] = nw[d];
         }
       }
       for (int64_t k = threadIdx.x; a.model != GWL_MODEL_TAYLORF2 && k < L; k += blockDim.x) {
@@ -408,9 +395,9 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       __syncthreads();
     }
     // ---- C: prior window, marginalised lnL per time sample, logsumexp ----
-    double hh = block_sum(hh_part, red);
+    double hh = 0.0;
+    if (!(MIXED && a.model == GWL_MODEL_TAYLORF2)) hh = block_sum(hh_part, red);
     if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
-      hh = 0.0;
       for (int d = 0; d < D; ++d) {
         const double ci = r.cos_i;
         const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
@@ -440,7 +427,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const float xr = x.x, xi = x.y;
         if (a.dist_marg) {
           const float dx = a.phase_marg ? sqrtf(xr * xr + xi * xi) * (float)sr : xr * (float)sr;
-          l = (double)bicubic_eval_f(a.tx_f, a.nx, a.ty_f, a.ny, a.tc_f, a.bbox, dx, (float)hh_ref);
+          l = (double)bicubic_eval_f(s_tx, a.nx, s_ty, a.ny, a.tc_f, a.bbox, dx, (float)hh_ref);
         } else if (a.phase_marg) {
           const float ax = sqrtf(xr * xr + xi * xi);
           l = ((double)ax + (double)ln_i0_minus_x(ax)) - hh / 2;
@@ -471,23 +458,58 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         }
       }
     }
-    // combine (m, acc) pairs over the block in a fixed tree order
+    // combine (m, acc) pairs over the block in a fixed order
     double* redm = red;
     double* reds = red + kTmThreads;
-    redm[threadIdx.x] = m;
-    reds[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = kTmThreads / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) {
-        const double m1 = redm[threadIdx.x], m2 = redm[threadIdx.x + w];
-        const double s1 = reds[threadIdx.x], s2 = reds[threadIdx.x + w];
+    if constexpr (MIXED) {
+      // within warps by xor-shuffles (the combination is symmetric, so every
+      // lane ends with the same pair), then the warps' pairs in warp 0; the
+      // exponentials of the non-positive differences in float32
+      const auto comb = [](double& m1, double& s1, double m2, double s2) {
         const double mm = fmax(m1, m2);
         double ss = 0.0;
-        if (isfinite(mm)) ss = (isfinite(m1) ? s1 * exp(m1 - mm) : 0.0) + (isfinite(m2) ? s2 * exp(m2 - mm) : 0.0);
-        redm[threadIdx.x] = mm;
-        reds[threadIdx.x] = ss;
+        if (isfinite(mm))
+          ss = (isfinite(m1) ? s1 * (double)__expf((float)(m1 - mm)) : 0.0) +
+               (isfinite(m2) ? s2 * (double)__expf((float)(m2 - mm)) : 0.0);
+        m1 = mm;
+        s1 = ss;
+      };
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) comb(m, acc, __shfl_xor_sync(0xffffffffu, m, o), __shfl_xor_sync(0xffffffffu, acc, o));
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      if (lane == 0) {
+        redm[warp] = m;
+        reds[warp] = acc;
       }
       __syncthreads();
+      if (warp == 0) {
+        m = lane < kTmThreads / 32 ? redm[lane] : -INFINITY;
+        acc = lane < kTmThreads / 32 ? reds[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          comb(m, acc, __shfl_xor_sync(0xffffffffu, m, o), __shfl_xor_sync(0xffffffffu, acc, o));
+        if (lane == 0) {
+          redm[0] = m;
+          reds[0] = acc;
+        }
+      }
+      __syncthreads();
+    } else {
+      redm[threadIdx.x] = m;
+      reds[threadIdx.x] = acc;
+      __syncthreads();
+      for (int w = kTmThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+          const double m1 = redm[threadIdx.x], m2 = redm[threadIdx.x + w];
+          const double s1 = reds[threadIdx.x], s2 = reds[threadIdx.x + w];
+          const double mm = fmax(m1, m2);
+          double ss = 0.0;
+          if (isfinite(mm)) ss = (isfinite(m1) ? s1 * exp(m1 - mm) : 0.0) + (isfinite(m2) ? s2 * exp(m2 - mm) : 0.0);
+          redm[threadIdx.x] = mm;
+          reds[threadIdx.x] = ss;
+        }
+        __syncthreads();
+      }
     }
     if (threadIdx.x == 0) {
       const double amax = redm[0], total = reds[0] * prob * a.delta_tc;
@@ -557,7 +579,8 @@ size_t time_marg_work_bytes(const LaunchArgs& a) {
 template <int D>
 static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
   if (a.precision == GWL_PRECISION_MIXED) {
-    const size_t smem = (size_t)a.n_fft * sizeof(float2);
+    // the FFT buffer, then the distance spline's knots
+    const size_t smem = (size_t)a.n_fft * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0);
     cudaError_t e = cudaFuncSetAttribute(k_time_marg<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)a.B;
@@ -572,7 +595,8 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
   const int log2L = log2_exact(a.n_fft);
   if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
-  if (a.precision == GWL_PRECISION_MIXED && ((size_t)a.n_fft * sizeof(float2) > 200 * 1024 ||
+  if (a.precision == GWL_PRECISION_MIXED &&
+      ((size_t)a.n_fft * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0) > 200 * 1024 ||
                                              a.n_fft / 2 > (int64_t)kTmTwiddleRows * kTmTwiddleRows))
     return cudaErrorInvalidValue;
   cudaError_t e = ensure_twiddles(a.n_fft);
