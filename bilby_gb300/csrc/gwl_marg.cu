@@ -133,6 +133,9 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   using R = typename TmTypes<MIXED>::R;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[2 * kTmThreads];
+  __shared__ float s_coef[2 * kMaxDet];
+  __shared__ double s_scal[6];
+  __shared__ long long s_jr[2];
   // mixed: the FFT twiddles exp(-2 pi i q / L), q < L / 2, as products of two
   // shared-memory tables (q = 128 q1 + q2), instead of loads from global memory
   __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     __syncthreads();
   }
   // mixed: the distance spline's knots in shared memory, after the FFT buffer
-  float* s_tx = reinterpret_cast<float*>(smem + (MIXED ? L * sizeof(float2) : 0));
+  float* s_tx = reinterpret_cast<float*>(smem + (MIXED ? (L + L / 16) * sizeof(float2) : 0));
   float* s_ty = s_tx + a.nx;
   if (MIXED && a.dist_marg) {
     for (int q = threadIdx.x; q < a.nx; q += blockDim.x) s_tx[q] = a.tx_f[q];
@@ -166,27 +169,38 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       return twiddle[q];
     }
   };
+  // mixed: one padding slot after every 16 elements of the shared-memory
+  // buffer, so that the strided accesses of the FFT passes spread over the banks
+  const auto P = [](int64_t q) -> int64_t { return MIXED ? q + (q >> 4) : q; };
   for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
     C* buf = MIXED ? reinterpret_cast<C*>(smem) : reinterpret_cast<C*>(a.tm_work) + (size_t)blockIdx.x * L;
     const PointRec& r = a.rec[i];
     // ---- A: integrand --------------------------------------------------
     double hh_part = 0.0;
     if constexpr (MIXED) {
+      // per-point float32 coefficients, computed once (float64 issues slowly) and shared
+      if (threadIdx.x == 0) {
+        for (int d = 0; d < D; ++d) {
+          if (a.model == GWL_MODEL_TAYLORF2) {
+            const double ci = r.cos_i;
+            const double s = norm * r.amp * a.w_scale[d];
+            s_coef[2 * d] = (float)(s * r.fp[d] * (1.0 + ci * ci) / 2.0);
+            s_coef[2 * d + 1] = (float)(-s * r.fx[d] * ci);
+          } else {
+            s_coef[2 * d] = (float)(norm * a.w_scale[d] * r.fp[d] * r.amp);
+            s_coef[2 * d + 1] = (float)(norm * a.w_scale[d] * r.fx[d] * r.amp2);
+          }
+        }
+      }
+      __syncthreads();
       float gre[D], gim[D], cre[D], cim[D];
       uint32_t xl[D], xh[D];
       float ch[kNumBasis + 1], cl[kNumBasis + 1];
       for (int d = 0; d < D; ++d) {
         xl[d] = r.xfix[d][0];
         xh[d] = r.xfix[d][1];
-        if (a.model == GWL_MODEL_TAYLORF2) {
-          const double ci = r.cos_i;
-          const double s = norm * r.amp * a.w_scale[d];
-          gre[d] = (float)(s * r.fp[d] * (1.0 + ci * ci) / 2.0);
-          gim[d] = (float)(-s * r.fx[d] * ci);
-        } else {
-          cre[d] = (float)(norm * a.w_scale[d] * r.fp[d] * r.amp);
-          cim[d] = (float)(norm * a.w_scale[d] * r.fx[d] * r.amp2);
-        }
+        gre[d] = cre[d] = s_coef[2 * d];
+        gim[d] = cim[d] = s_coef[2 * d + 1];
       }
       for (int b = 0; b <= kNumBasis; ++b) {
         ch[b] = r.c_hi[b];
@@ -200,7 +214,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         // zero the buffer with coalesced stores, then write the in-band bins
         // (a few thousand of the L) to their bit-reversed slots
         float4* b4 = reinterpret_cast<float4*>(buf);
-        for (int64_t q = threadIdx.x; q < L / 2; q += blockDim.x) b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int64_t q = threadIdx.x; q < (L + L / 16) / 2; q += blockDim.x) b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
         const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
         const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
@@ -227,7 +241,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             zr += gre[d] * er + gim[d] * ei;
             zi += gim[d] * er - gre[d] * ei;
           }
-          buf[bit_reverse((uint32_t)k, log2L)] = make_float2(zr, zi);
+          buf[P(bit_reverse((uint32_t)k, log2L))] = make_float2(zr, zi);
         }
       }
       for (int64_t k = threadIdx.x; a.model != GWL_MODEL_TAYLORF2 && k < L; k += blockDim.x) {
@@ -282,7 +296,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             }
           }
         }
-        buf[bit_reverse((uint32_t)k, log2L)] = make_float2(zr, zi);
+        buf[P(bit_reverse((uint32_t)k, log2L))] = make_float2(zr, zi);
       }
       if (a.model == GWL_MODEL_SINEGAUSSIAN) {
         for (int d = 0; d < D; ++d) {
@@ -357,17 +371,53 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     if (log2L & 1) {  // one radix-2 stage first when log2 L is odd
       for (int64_t bf = threadIdx.x; bf < L / 2; bf += blockDim.x) {
         const int64_t i0 = 2 * bf, i1 = i0 + 1;
-        const C x0 = buf[i0], x1 = buf[i1];
+        const C x0 = buf[P(i0)], x1 = buf[P(i1)];
         C y0, y1;
         y0.x = x0.x + x1.x;
         y0.y = x0.y + x1.y;
         y1.x = x0.x - x1.x;
         y1.y = x0.y - x1.y;
-        buf[i0] = y0;
-        buf[i1] = y1;
+        buf[P(i0)] = y0;
+        buf[P(i1)] = y1;
       }
       __syncthreads();
       stage = 2;
+    }
+    if constexpr (MIXED) {
+      // radix-16 passes (four radix-2 stages in registers): fewer shared-memory
+      // round trips and barriers; the stage-j twiddles of a group depend only
+      // on (k mod 2^j)
+      for (; stage + 3 <= log2L; stage += 4) {
+        const int64_t h0 = (int64_t)1 << (stage - 1);
+        for (int64_t gi = threadIdx.x; gi < L / 16; gi += blockDim.x) {
+          const int64_t pos = gi & (h0 - 1);
+          const int64_t b0 = ((gi >> (stage - 1)) << (stage + 3)) + pos;
+          C x[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) x[k] = buf[P(b0 + k * h0)];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int64_t stride = L / (2 * (h0 << j));
+            C w[8];
+#pragma unroll
+            for (int m = 0; m < (1 << j); ++m) w[m] = tw((pos + m * h0) * stride);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              if (k & (1 << j)) continue;
+              const int k2 = k | (1 << j);
+              const C ww = w[k & ((1 << j) - 1)];
+              const R tr = ww.x * x[k2].x - ww.y * x[k2].y, ti = ww.x * x[k2].y + ww.y * x[k2].x;
+              x[k2].x = x[k].x - tr;
+              x[k2].y = x[k].y - ti;
+              x[k].x = x[k].x + tr;
+              x[k].y = x[k].y + ti;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 16; ++k) buf[P(b0 + k * h0)] = x[k];
+        }
+        __syncthreads();
+      }
     }
     for (; stage < log2L; stage += 2) {
       const int64_t h = (int64_t)1 << (stage - 1);  // half-length of the first of the two stages
@@ -377,7 +427,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
         const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
         const C w1 = tw(pos * s1), w2 = tw(pos * s2), w3 = tw((pos + h) * s2);
-        const C x0 = buf[i0], x1 = buf[i1], x2 = buf[i2], x3 = buf[i3];
+        const C x0 = buf[P(i0)], x1 = buf[P(i1)], x2 = buf[P(i2)], x3 = buf[P(i3)];
         C a0, a1, a2, a3, y0, y1, y2, y3;
         R tr = w1.x * x1.x - w1.y * x1.y, ti = w1.x * x1.y + w1.y * x1.x;
         a0.x = x0.x + tr; a0.y = x0.y + ti; a1.x = x0.x - tr; a1.y = x0.y - ti;
@@ -387,40 +437,50 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         y0.x = a0.x + tr; y0.y = a0.y + ti; y2.x = a0.x - tr; y2.y = a0.y - ti;
         tr = w3.x * a3.x - w3.y * a3.y; ti = w3.x * a3.y + w3.y * a3.x;
         y1.x = a1.x + tr; y1.y = a1.y + ti; y3.x = a1.x - tr; y3.y = a1.y - ti;
-        buf[i0] = y0;
-        buf[i1] = y1;
-        buf[i2] = y2;
-        buf[i3] = y3;
+        buf[P(i0)] = y0;
+        buf[P(i1)] = y1;
+        buf[P(i2)] = y2;
+        buf[P(i3)] = y3;
       }
       __syncthreads();
     }
     // ---- C: prior window, marginalised lnL per time sample, logsumexp ----
     double hh = 0.0;
     if (!(MIXED && a.model == GWL_MODEL_TAYLORF2)) hh = block_sum(hh_part, red);
-    if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
-      for (int d = 0; d < D; ++d) {
-        const double ci = r.cos_i;
-        const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
-        const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
-        hh += norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
-      }
-    }
-    const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
-    const double prob = 1.0 / (a.t_max - a.t_min);
     const double jit = r.jitter;
-    const double hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
-    const double sr = r.dist / a.ref_dist;
-    // candidate window from the real-valued bounds, checked exactly below
-    const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
-    const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
-    const int64_t j_lo = (int64_t)fmax(0.0, jl), j_hi = (int64_t)fmin((double)(L - 1), jh);
+    // per-point scalars, computed once (float64 issues slowly) and shared
+    if (threadIdx.x == 0) {
+      const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
+      s_scal[3] = step;
+      s_scal[4] = 1.0 / (a.t_max - a.t_min);
+      if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
+        for (int d = 0; d < D; ++d) {
+          const double ci = r.cos_i;
+          const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
+          const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+          hh += norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
+        }
+      }
+      s_scal[0] = hh;
+      s_scal[1] = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+      s_scal[2] = r.dist / a.ref_dist;
+      // candidate window from the real-valued bounds, checked exactly below
+      const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
+      const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
+      s_jr[0] = (long long)fmax(0.0, jl);
+      s_jr[1] = (long long)fmin((double)(L - 1), jh);
+    }
+    __syncthreads();
+    hh = s_scal[0];
+    const double hh_ref = s_scal[1], sr = s_scal[2], step = s_scal[3], prob = s_scal[4];
+    const int64_t j_lo = s_jr[0], j_hi = s_jr[1];
     // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
     double m = -INFINITY, acc = 0.0;
     for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
       const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
       const double t = (a.start_time0 + lin) + jit;
       if (!(t >= a.t_min && t <= a.t_max)) continue;
-      const C x = buf[j];
+      const C x = buf[P(j)];
       double l;
       if constexpr (MIXED) {
         // float32 per-sample work; the large terms combine in float64
@@ -462,35 +522,28 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     double* redm = red;
     double* reds = red + kTmThreads;
     if constexpr (MIXED) {
-      // within warps by xor-shuffles (the combination is symmetric, so every
-      // lane ends with the same pair), then the warps' pairs in warp 0; the
-      // exponentials of the non-positive differences in float32
-      const auto comb = [](double& m1, double& s1, double m2, double s2) {
-        const double mm = fmax(m1, m2);
-        double ss = 0.0;
-        if (isfinite(mm))
-          ss = (isfinite(m1) ? s1 * (double)__expf((float)(m1 - mm)) : 0.0) +
-               (isfinite(m2) ? s2 * (double)__expf((float)(m2 - mm)) : 0.0);
-        m1 = mm;
-        s1 = ss;
-      };
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) comb(m, acc, __shfl_xor_sync(0xffffffffu, m, o), __shfl_xor_sync(0xffffffffu, acc, o));
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      if (lane == 0) {
-        redm[warp] = m;
-        reds[warp] = acc;
-      }
+      // warp 0 alone combines the threads' pairs (float64 issues slowly, so
+      // the other warps leave it the pipe): the maximum over the pairs, then
+      // sum acc_t exp(m_t - max) in float32; lane q takes pairs q, q + 32, ...
+      // and the lanes combine by xor-shuffles, a fixed order
+      redm[threadIdx.x] = m;
+      reds[threadIdx.x] = acc;
       __syncthreads();
-      if (warp == 0) {
-        m = lane < kTmThreads / 32 ? redm[lane] : -INFINITY;
-        acc = lane < kTmThreads / 32 ? reds[lane] : 0.0;
+      if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double mx = -INFINITY;
+        for (int q = lane; q < kTmThreads; q += 32) mx = fmax(mx, redm[q]);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-          comb(m, acc, __shfl_xor_sync(0xffffffffu, m, o), __shfl_xor_sync(0xffffffffu, acc, o));
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        float sm = 0.f;
+        if (isfinite(mx))
+          for (int q = lane; q < kTmThreads; q += 32)
+            if (isfinite(redm[q])) sm += (float)reds[q] * __expf((float)(redm[q] - mx));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
         if (lane == 0) {
-          redm[0] = m;
-          reds[0] = acc;
+          redm[0] = mx;
+          reds[0] = (double)sm;
         }
       }
       __syncthreads();
@@ -580,7 +633,8 @@ template <int D>
 static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
   if (a.precision == GWL_PRECISION_MIXED) {
     // the FFT buffer, then the distance spline's knots
-    const size_t smem = (size_t)a.n_fft * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0);
+    const size_t smem = (size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) +
+                        (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0);
     cudaError_t e = cudaFuncSetAttribute(k_time_marg<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)a.B;
@@ -596,7 +650,8 @@ cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
   const int log2L = log2_exact(a.n_fft);
   if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
   if (a.precision == GWL_PRECISION_MIXED &&
-      ((size_t)a.n_fft * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0) > 200 * 1024 ||
+      ((size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0) >
+           200 * 1024 ||
                                              a.n_fft / 2 > (int64_t)kTmTwiddleRows * kTmTwiddleRows))
     return cudaErrorInvalidValue;
   cudaError_t e = ensure_twiddles(a.n_fft);
