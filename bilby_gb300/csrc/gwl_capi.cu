@@ -310,6 +310,10 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.ny = a->ny;
   for (int q = 0; q < 4; ++q) L.bbox[q] = a->bbox[q];
   L.ref_dist = a->ref_dist;
+  L.tm_step = a->duration / (double)(a->n_bins - 1);  // linspace(0, T, L + 1) spacing, L = n_bins - 1
+  L.tm_inv_step = (double)(a->n_bins - 1) / a->duration;
+  L.tm_prob = a->t_max > a->t_min ? 1.0 / (a->t_max - a->t_min) : 0.0;
+  L.inv_ref_dist = a->ref_dist > 0 ? 1.0 / a->ref_dist : 0.0;
   L.relbin = a->relbin;
   L.rb_edges = a->rb_edges;
   L.rb_index = a->rb_index;

@@ -120,6 +120,7 @@ struct LaunchArgs {
   // marginalisation
   int time_marg, phase_marg, dist_marg, jitter;
   double t_min, t_max, delta_tc, start_time0;
+  double tm_step, tm_inv_step, tm_prob, inv_ref_dist;  // T / L, L / T, 1 / (t_max - t_min), 1 / ref_dist
   int64_t n_fft;                        // time-marginalisation FFT length (n_bins - 1)
   const double* tx; const double* ty; const double* tc;  // distance spline
   const float* tx_f; const float* ty_f; const float* tc_f; // float32 copy (mixed precision)

@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   __shared__ float s_coef[2 * kMaxDet];
   __shared__ double s_scal[6];
   __shared__ long long s_jr[2];
+  __shared__ SplineRowF s_row;
   // mixed: the FFT twiddles exp(-2 pi i q / L), q < L / 2, as products of two
   // shared-memory tables (q = 128 q1 + q2), instead of loads from global memory
   __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
@@ -449,26 +450,46 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     if (!(MIXED && a.model == GWL_MODEL_TAYLORF2)) hh = block_sum(hh_part, red);
     const double jit = r.jitter;
     // per-point scalars, computed once (float64 issues slowly) and shared
+    if (MIXED && a.model == GWL_MODEL_TAYLORF2 && threadIdx.x < D) {
+      // <h|h> of detector d from the prefix sums, one thread per detector
+      const int d = threadIdx.x;
+      const double ci = r.cos_i;
+      const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
+      const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+      red[d] = norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
+    }
+    if (MIXED && a.model == GWL_MODEL_TAYLORF2) __syncthreads();
     if (threadIdx.x == 0) {
-      const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
-      s_scal[3] = step;
-      s_scal[4] = 1.0 / (a.t_max - a.t_min);
-      if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
-        for (int d = 0; d < D; ++d) {
-          const double ci = r.cos_i;
-          const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
-          const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
-          hh += norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
-        }
+      if constexpr (MIXED) {
+        // the divisions precomputed on the host (LaunchArgs::tm_step ...)
+        if (a.model == GWL_MODEL_TAYLORF2)
+          for (int d = 0; d < D; ++d) hh += red[d];
+        const double sr = r.dist * a.inv_ref_dist;
+        s_scal[0] = hh;
+        s_scal[1] = hh * sr * sr;
+        s_scal[2] = sr;
+        s_scal[3] = a.tm_step;
+        s_scal[4] = a.tm_prob;
+        // candidate window from the real-valued bounds, checked exactly below
+        const double jl = floor((a.t_min - a.start_time0 - jit) * a.tm_inv_step) - 3.0;
+        const double jh = ceil((a.t_max - a.start_time0 - jit) * a.tm_inv_step) + 2.0;
+        s_jr[0] = (long long)fmax(0.0, jl);
+        s_jr[1] = (long long)fmin((double)(L - 1), jh);
+        // the distance spline's row at this point's <h|h>
+        if (a.dist_marg) s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)s_scal[1]);
+      } else {
+        const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
+        s_scal[3] = step;
+        s_scal[4] = 1.0 / (a.t_max - a.t_min);
+        s_scal[0] = hh;
+        s_scal[1] = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+        s_scal[2] = r.dist / a.ref_dist;
+        // candidate window from the real-valued bounds, checked exactly below
+        const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
+        const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
+        s_jr[0] = (long long)fmax(0.0, jl);
+        s_jr[1] = (long long)fmin((double)(L - 1), jh);
       }
-      s_scal[0] = hh;
-      s_scal[1] = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
-      s_scal[2] = r.dist / a.ref_dist;
-      // candidate window from the real-valued bounds, checked exactly below
-      const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
-      const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
-      s_jr[0] = (long long)fmax(0.0, jl);
-      s_jr[1] = (long long)fmin((double)(L - 1), jh);
     }
     __syncthreads();
     hh = s_scal[0];
@@ -487,7 +508,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const float xr = x.x, xi = x.y;
         if (a.dist_marg) {
           const float dx = a.phase_marg ? sqrtf(xr * xr + xi * xi) * (float)sr : xr * (float)sr;
-          l = (double)bicubic_eval_f(s_tx, a.nx, s_ty, a.ny, a.tc_f, a.bbox, dx, (float)hh_ref);
+          l = (double)bicubic_eval_row_f(s_tx, a.nx, a.ny, a.tc_f, a.bbox, dx, s_row);
         } else if (a.phase_marg) {
           const float ax = sqrtf(xr * xr + xi * xi);
           l = ((double)ax + (double)ln_i0_minus_x(ax)) - hh / 2;

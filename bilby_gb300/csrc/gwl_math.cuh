@@ -152,4 +152,42 @@ __device__ inline float bicubic_eval_f(const float* tx, int nx, const float* ty,
   return s;
 }
 
+// bicubic_eval_f split for many x at one y: the y-axis interval and B-spline
+// values once (SplineRowF), then per x the same interval search, values and
+// sums in the same order (the <d|h> axis is log-spaced, so the search stays).
+struct SplineRowF {
+  int Ly;
+  int inside;  // y within the table's bounding box
+  float hy[4];
+};
+
+__device__ inline SplineRowF bicubic_row_f(const float* ty, int ny, const double* bbox, float y) {
+  SplineRowF row;
+  row.inside = (double)y >= bbox[2] && (double)y <= bbox[3];
+  row.Ly = 3;
+  row.hy[0] = row.hy[1] = row.hy[2] = row.hy[3] = 0.f;
+  if (row.inside) {
+    row.Ly = bspline_interval_f(ty, ny, 3, y);
+    bspline_values_f(ty, 3, y, row.Ly, row.hy);
+  }
+  return row;
+}
+
+__device__ inline float bicubic_eval_row_f(const float* tx, int nx, int ny, const float* c, const double* bbox,
+                                           float x, const SplineRowF& row) {
+  if (!((double)x >= bbox[0] && (double)x <= bbox[1] && row.inside)) return -INFINITY;
+  const int Lx = bspline_interval_f(tx, nx, 3, x);
+  float hx[4];
+  bspline_values_f(tx, 3, x, Lx, hx);
+  const int ncy = ny - 4;
+  float s = 0.0f;
+  for (int i = 0; i < 4; ++i) {
+    const float* rowc = c + (size_t)(Lx - 3 + i) * ncy + (row.Ly - 3);
+    float r = 0.0f;
+    for (int j = 0; j < 4; ++j) r += rowc[j] * row.hy[j];
+    s += r * hx[i];
+  }
+  return s;
+}
+
 }  // namespace gwl
