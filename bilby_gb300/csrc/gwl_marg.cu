@@ -459,14 +459,17 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       red[d] = norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
     }
     if (MIXED && a.model == GWL_MODEL_TAYLORF2) __syncthreads();
-    if (threadIdx.x == 0) {
-      if constexpr (MIXED) {
-        // the divisions precomputed on the host (LaunchArgs::tm_step ...)
-        if (a.model == GWL_MODEL_TAYLORF2)
-          for (int d = 0; d < D; ++d) hh += red[d];
-        const double sr = r.dist * a.inv_ref_dist;
+    if (MIXED && (threadIdx.x == 0 || threadIdx.x == 32)) {
+      // the divisions precomputed on the host (LaunchArgs::tm_step ...);
+      // thread 0 the scalars and the window, thread 32 (another warp) the
+      // distance spline's row at this point's <h|h>, at the same time
+      if (a.model == GWL_MODEL_TAYLORF2)
+        for (int d = 0; d < D; ++d) hh += red[d];
+      const double sr = r.dist * a.inv_ref_dist;
+      const double hh_ref = hh * sr * sr;
+      if (threadIdx.x == 0) {
         s_scal[0] = hh;
-        s_scal[1] = hh * sr * sr;
+        s_scal[1] = hh_ref;
         s_scal[2] = sr;
         s_scal[3] = a.tm_step;
         s_scal[4] = a.tm_prob;
@@ -475,21 +478,22 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const double jh = ceil((a.t_max - a.start_time0 - jit) * a.tm_inv_step) + 2.0;
         s_jr[0] = (long long)fmax(0.0, jl);
         s_jr[1] = (long long)fmin((double)(L - 1), jh);
-        // the distance spline's row at this point's <h|h>
-        if (a.dist_marg) s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)s_scal[1]);
-      } else {
-        const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
-        s_scal[3] = step;
-        s_scal[4] = 1.0 / (a.t_max - a.t_min);
-        s_scal[0] = hh;
-        s_scal[1] = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
-        s_scal[2] = r.dist / a.ref_dist;
-        // candidate window from the real-valued bounds, checked exactly below
-        const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
-        const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
-        s_jr[0] = (long long)fmax(0.0, jl);
-        s_jr[1] = (long long)fmin((double)(L - 1), jh);
+      } else if (a.dist_marg) {
+        s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)hh_ref);
       }
+    }
+    if (!MIXED && threadIdx.x == 0) {
+      const double step = a.duration / (double)L;  // linspace(0, T, L + 1) spacing
+      s_scal[3] = step;
+      s_scal[4] = 1.0 / (a.t_max - a.t_min);
+      s_scal[0] = hh;
+      s_scal[1] = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+      s_scal[2] = r.dist / a.ref_dist;
+      // candidate window from the real-valued bounds, checked exactly below
+      const double jl = floor((a.t_min - a.start_time0 - jit) / step) - 3.0;
+      const double jh = ceil((a.t_max - a.start_time0 - jit) / step) + 2.0;
+      s_jr[0] = (long long)fmax(0.0, jl);
+      s_jr[1] = (long long)fmin((double)(L - 1), jh);
     }
     __syncthreads();
     hh = s_scal[0];
@@ -543,29 +547,30 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     double* redm = red;
     double* reds = red + kTmThreads;
     if constexpr (MIXED) {
-      // warp 0 alone combines the threads' pairs (float64 issues slowly, so
-      // the other warps leave it the pipe): the maximum over the pairs, then
-      // sum acc_t exp(m_t - max) in float32; lane q takes pairs q, q + 32, ...
-      // and the lanes combine by xor-shuffles, a fixed order
-      redm[threadIdx.x] = m;
-      reds[threadIdx.x] = acc;
+      // all warps: the maximum of the threads' m as float32 (any reference
+      // near the maximum serves), then sum acc_t exp(m_t - M) in float32; both
+      // by xor-shuffles within warps and a fixed-order sum of the 16 warps
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      float mf = (float)m;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
+      float* redf = reinterpret_cast<float*>(reds);
+      if (lane == 0) redf[warp] = mf;
       __syncthreads();
-      if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        double mx = -INFINITY;
-        for (int q = lane; q < kTmThreads; q += 32) mx = fmax(mx, redm[q]);
+      float M = redf[0];
+      for (int w = 1; w < kTmThreads / 32; ++w) M = fmaxf(M, redf[w]);
+      float sm = 0.f;
+      if (isfinite(M) && isfinite(m)) sm = (float)acc * __expf((float)(m - (double)M));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        float sm = 0.f;
-        if (isfinite(mx))
-          for (int q = lane; q < kTmThreads; q += 32)
-            if (isfinite(redm[q])) sm += (float)reds[q] * __expf((float)(redm[q] - mx));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
-        if (lane == 0) {
-          redm[0] = mx;
-          reds[0] = (double)sm;
-        }
+      for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
+      __syncthreads();
+      if (lane == 0) redf[warp] = sm;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float total = 0.f;
+        for (int w = 0; w < kTmThreads / 32; ++w) total += redf[w];
+        redm[0] = isfinite(M) ? (double)M : -INFINITY;
+        reds[0] = (double)total;
       }
       __syncthreads();
     } else {
@@ -590,7 +595,8 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       double lnl;
       if (!r.valid) lnl = -1.7976931348623157e308;
       else if (!isfinite(amax)) lnl = amax;
-      else lnl = amax + log(total);
+      // mixed: the logarithm of the O(1..1e3) sum in float32 (error ~1e-7)
+      else lnl = amax + (MIXED ? (double)logf((float)total) : log(total));
       a.out[i] = lnl;
     }
     __syncthreads();
