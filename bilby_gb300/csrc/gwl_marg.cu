@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   // mixed: the FFT twiddles exp(-2 pi i q / L), q < L / 2, as products of two
   // shared-memory tables (q = 128 q1 + q2), instead of loads from global memory
   __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
+  __shared__ float2 s_w16[16];
   const int64_t L = a.n_fft;
   const double norm = 4.0 / a.duration;
   if constexpr (MIXED) {
@@ -148,6 +149,12 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       const int64_t qh = (int64_t)q * kTmTwiddleRows;
       tw_hi[q] = qh < half ? reinterpret_cast<const float2*>(twiddle)[qh] : make_float2(1.f, 0.f);
       tw_lo[q] = q < half ? reinterpret_cast<const float2*>(twiddle)[q] : make_float2(1.f, 0.f);
+    }
+    // the 16th roots of unity exp(-2 pi i m / 16) (the table holds q < L / 2)
+    if (threadIdx.x < 8) {
+      const float2 t = reinterpret_cast<const float2*>(twiddle)[(int64_t)threadIdx.x * (L / 16)];
+      s_w16[threadIdx.x] = t;
+      s_w16[threadIdx.x + 8] = make_float2(-t.x, -t.y);
     }
     __syncthreads();
   }
@@ -212,37 +219,59 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       float hh1[D], hh2[D];
       for (int d = 0; d < D; ++d) hh1[d] = hh2[d] = 0.f;
       if (a.model == GWL_MODEL_TAYLORF2) {
-        // zero the buffer with coalesced stores, then write the in-band bins
-        // (a few thousand of the L) to their bit-reversed slots
-        float4* b4 = reinterpret_cast<float4*>(buf);
-        for (int64_t q = threadIdx.x; q < (L + L / 16) / 2; q += blockDim.x) b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        __syncthreads();
+        // The integrand fused with the first four FFT stages.  After them the
+        // positions 16 b .. 16 b + 15 hold the 16-point DFT of the bins
+        // q + j L/16 (j < 16), q = bitrev(b) over log2(L) - 4 bits.  The band
+        // holds a few thousand of the L bins, so a residue q has 0-3 of its 16
+        // bins in it: a thread takes blocks b, evaluates their in-band bins,
+        // and writes the 16 outputs (zeros when none); consecutive threads
+        // write consecutive blocks.
+        const int64_t R = L >> 4;
+        const int lr = log2L - 4;
         const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
         const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
-        for (int64_t k = ks + threadIdx.x; r.valid && k < ke; k += blockDim.x) {
-          float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+        for (int64_t bb = threadIdx.x; bb < R; bb += blockDim.x) {
+          const int64_t q = (int64_t)bit_reverse((uint32_t)bb, lr);
+          float yr[16], yi[16];
 #pragma unroll
-          for (int q = 0; q < kNumBasis / 2; ++q) {
-            const float4 v = __ldg(basis4 + k * (kNumBasis / 2) + q);
-            ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
-            ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
-          }
-          const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
-          float zr = 0.f, zi = 0.f;
+          for (int v = 0; v < 16; ++v) yr[v] = yi[v] = 0.f;
+          // in-band j: ks <= q + j R < ke
+          const int j0 = r.valid ? (int)max((int64_t)0, (ks - q + R - 1) / R) : 16;
+          const int j1 = r.valid ? (int)min((int64_t)16, (ke - q + R - 1) / R) : 0;
+          for (int j = j0; j < j1; ++j) {
+            const int64_t k = q + (int64_t)j * R;
+            float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
 #pragma unroll
-          for (int d = 0; d < D; ++d) {
-            const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
-            float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
-            ph -= rintf(ph);
-            float sn, cs;
-            __sincosf(ph * 6.283185307179586f, &sn, &cs);
-            const float2 w = __ldg(a.w[d] + k);
-            const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
-            // h conj(d) / S = G conj(e^{i Phi} w)
-            zr += gre[d] * er + gim[d] * ei;
-            zi += gim[d] * er - gre[d] * ei;
+            for (int qq = 0; qq < kNumBasis / 2; ++qq) {
+              const float4 v = __ldg(basis4 + k * (kNumBasis / 2) + qq);
+              ff_mac(s_hi, s_lo, ch[2 * qq], cl[2 * qq], v.x, v.y);
+              ff_mac(s_hi, s_lo, ch[2 * qq + 1], cl[2 * qq + 1], v.z, v.w);
+            }
+            const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
+            float zr = 0.f, zi = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+              float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
+              ph -= rintf(ph);
+              float sn, cs;
+              __sincosf(ph * 6.283185307179586f, &sn, &cs);
+              const float2 w = __ldg(a.w[d] + k);
+              const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+              // h conj(d) / S = G conj(e^{i Phi} w)
+              zr += gre[d] * er + gim[d] * ei;
+              zi += gim[d] * er - gre[d] * ei;
+            }
+            // Y[v] += z exp(-2 pi i j v / 16)
+#pragma unroll
+            for (int v = 0; v < 16; ++v) {
+              const float2 t = s_w16[(j * v) & 15];
+              yr[v] += zr * t.x - zi * t.y;
+              yi[v] += zr * t.y + zi * t.x;
+            }
           }
-          buf[P(bit_reverse((uint32_t)k, log2L))] = make_float2(zr, zi);
+#pragma unroll
+          for (int v = 0; v < 16; ++v) buf[P(16 * bb + v)] = make_float2(yr[v], yi[v]);
         }
       }
       for (int64_t k = threadIdx.x; a.model != GWL_MODEL_TAYLORF2 && k < L; k += blockDim.x) {
@@ -369,7 +398,9 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     __syncthreads();
     // ---- B: in-place FFT, radix-4 passes (two radix-2 stages each) -------
     int stage = 1;
-    if (log2L & 1) {  // one radix-2 stage first when log2 L is odd
+    if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
+      stage = 5;  // stages 1-4 ran with the integrand
+    } else if (log2L & 1) {  // one radix-2 stage first when log2 L is odd
       for (int64_t bf = threadIdx.x; bf < L / 2; bf += blockDim.x) {
         const int64_t i0 = 2 * bf, i1 = i0 + 1;
         const C x0 = buf[P(i0)], x1 = buf[P(i1)];
@@ -442,6 +473,22 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         buf[P(i1)] = y1;
         buf[P(i2)] = y2;
         buf[P(i3)] = y3;
+      }
+      __syncthreads();
+    }
+    if (stage == log2L) {  // a last radix-2 stage (half-length L / 2, twiddle exp(-2 pi i q / L))
+      const int64_t h = L / 2;
+      for (int64_t q = threadIdx.x; q < h; q += blockDim.x) {
+        const C w = tw(q);
+        const C x0 = buf[P(q)], x1 = buf[P(q + h)];
+        const R tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
+        C y0, y1;
+        y0.x = x0.x + tr;
+        y0.y = x0.y + ti;
+        y1.x = x0.x - tr;
+        y1.y = x0.y - ti;
+        buf[P(q)] = y0;
+        buf[P(q + h)] = y1;
       }
       __syncthreads();
     }
