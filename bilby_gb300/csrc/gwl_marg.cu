@@ -429,10 +429,17 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
           for (int k = 0; k < 16; ++k) x[k] = buf[P(b0 + k * h0)];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
+            // exp(-2 pi i (pos + m h0) L / (2 h0 2^j) / L) = tw(pos stride) * exp(-2 pi i m / 2^(j+1))
             const int64_t stride = L / (2 * (h0 << j));
+            const C w0 = tw(pos * stride);
             C w[8];
+            w[0] = w0;
 #pragma unroll
-            for (int m = 0; m < (1 << j); ++m) w[m] = tw((pos + m * h0) * stride);
+            for (int m = 1; m < (1 << j); ++m) {
+              const float2 u = s_w16[m << (3 - j)];
+              w[m].x = w0.x * u.x - w0.y * u.y;
+              w[m].y = w0.x * u.y + w0.y * u.x;
+            }
 #pragma unroll
             for (int k = 0; k < 16; ++k) {
               if (k & (1 << j)) continue;
