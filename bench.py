@@ -286,7 +286,8 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
 def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     """Multi-banding (bilby/gw/likelihood/multiband.py, linear interpolation
     of <h|h>) on the GPU: reference chirp mass 0.87 (the 1+1 Msun prior
-    corner); float64 throughout."""
+    corner); the float64 kernel and the mixed-precision one, with |dlnL|
+    between them on the first batch."""
     import torch
     from bilby_gb300.analysis import params_block
     from bilby_gb300.multiband import MBGravitationalWaveTransient
@@ -302,22 +303,34 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     out = torch.empty(batch, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    for s in range(warmup):
-        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
+    res = {}
+    for precision in ("fp64", "mixed"):
+        for s in range(warmup):
+            an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), precision,
+                                           stream.cuda_stream)
+        torch.cuda.synchronize()
+        ms = []
+        for s in range(steps):
+            flush.fill_(float(s))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), precision,
+                                           stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        res[precision] = {"value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s",
+                          "ms_per_launch": float(np.mean(ms))}
+    o64 = torch.empty(batch, dtype=torch.float64, device="cuda")
+    omx = torch.empty(batch, dtype=torch.float64, device="cuda")
+    an.log_likelihood_ratio_device(blocks[0].data_ptr(), batch, o64.data_ptr(), "fp64", stream.cuda_stream)
+    an.log_likelihood_ratio_device(blocks[0].data_ptr(), batch, omx.data_ptr(), "mixed", stream.cuda_stream)
     torch.cuda.synchronize()
-    ms = []
-    for s in range(steps):
-        flush.fill_(float(s))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        an.log_likelihood_ratio_device(blocks[s % 2].data_ptr(), batch, out.data_ptr(), "fp64", stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
     return {"workload": name, "bands": int(like.number_of_bands),
             "banded_frequencies": int(len(like.banded_frequency_points)), "batch": batch,
-            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
-            "precision": "fp64", "setup_s": setup_s,
+            "value": res["fp64"]["value"], "unit": "evals/s", "ms_per_launch": res["fp64"]["ms_per_launch"],
+            "precision": "fp64", "mixed": res["mixed"], "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+            "max_abs_dlnl_mixed_vs_fp64": float((omx - o64).abs().max().item()), "setup_s": setup_s,
             "launch": "prologue + one warp per point over the banded frequencies"}
 
 

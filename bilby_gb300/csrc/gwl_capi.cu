@@ -99,6 +99,10 @@ struct gwl_analysis {
   int mb_bands = 0;
   int64_t* mb_band_start = nullptr;
   double* mb_band_df = nullptr;
+  float2* mb_basis = nullptr;
+  float2* mb_lw[kMaxDet] = {};
+  double mb_lw_scale[kMaxDet] = {};
+  double* mb_qprefix[kMaxDet] = {};
   // reduced-order quadrature
   int roq = 0;
   int roq_nl = 0, roq_nq = 0;
@@ -333,6 +337,12 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.mb_bands = a->mb_bands;
   L.mb_band_start = a->mb_band_start;
   L.mb_band_df = a->mb_band_df;
+  L.mb_basis = a->mb_basis;
+  for (int d = 0; d < a->n_det; ++d) {
+    L.mb_lw[d] = a->mb_lw[d];
+    L.mb_lw_scale[d] = a->mb_lw_scale[d];
+    L.mb_qprefix[d] = a->mb_qprefix[d];
+  }
   L.roq = a->roq;
   L.roq_nl = a->roq_nl;
   L.roq_nq = a->roq_nq;
@@ -395,13 +405,19 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.tm_work = a->d_tm;
   if (a->relbin || a->multiband || a->roq) {
     // relative binning / multi-banding / ROQ: per-point set-up, then one warp
-    // per point over the bin edges, banded frequencies or nodes
+    // per point over the bin edges, banded frequencies or nodes (no marking
+    // for the accurate kernel: it serves the full-grid TaylorF2 kernels)
+    L.rf_tol = 0.0;
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
     if (a->relbin) {
       GWL_CUDA(launch_relbin(L, s));
     } else if (a->multiband) {
-      GWL_CUDA(launch_multiband(L, s));
+      if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) {
+        GWL_CUDA(launch_multiband_mixed(L, s));
+      } else {
+        GWL_CUDA(launch_multiband(L, s));
+      }
     } else {
       GWL_CUDA(launch_roq(L, s));
     }
@@ -1111,6 +1127,18 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   int rc;
   if ((rc = upload(a, &a->mb_freq, fr))) return rc;
   if ((rc = upload(a, &a->mb_pow, pw))) return rc;
+  // mixed precision: float-float phase basis at the banded frequencies (the
+  // functions of the analysis grid's basis table)
+  std::vector<float2> mbb((size_t)n_points * kNumBasis, make_float2(0.f, 0.f));
+  for (int64_t k = 0; k < n_points; ++k) {
+    const double x = fr[k];
+    if (!(x > 0) || !std::isfinite(x)) continue;
+    const double c3 = std::cbrt(x), lx = std::log(x), inv3 = 1.0 / c3;
+    const double vals[kNumBasis] = {inv3 * inv3 * inv3 * inv3 * inv3, 1.0 / x, inv3 * inv3, inv3, lx, c3, c3 * lx,
+                                    c3 * c3};
+    for (int b = 0; b < kNumBasis; ++b) mbb[(size_t)k * kNumBasis + b] = split_ff(vals[b]);
+  }
+  if ((rc = upload(a, &a->mb_basis, mbb))) return rc;
   for (int d = 0; d < a->n_det; ++d) {
     std::vector<double2> lin(n_points);
     for (int64_t k = 0; k < n_points; ++k)
@@ -1118,6 +1146,27 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
     std::vector<double> quad(quadratic + (size_t)d * n_points, quadratic + (size_t)(d + 1) * n_points);
     if ((rc = upload(a, &a->mb_lin[d], lin))) return rc;
     if ((rc = upload(a, &a->mb_quad[d], quad))) return rc;
+    // mixed precision: L f^(-7/6) scaled into float32 range, and prefix sums of f^(-7/3) quad
+    std::vector<double> lr(n_points, 0.0), li(n_points, 0.0), qp(n_points + 1, 0.0);
+    double lmax = 0.0;
+    KahanSum acc;
+    for (int64_t k = 0; k < n_points; ++k) {
+      const double x = fr[k];
+      if (x > 0 && std::isfinite(x)) {
+        const double a76 = std::pow(x, -7.0 / 6.0);
+        lr[k] = lin[k].x * a76;
+        li[k] = lin[k].y * a76;
+        lmax = std::max(lmax, std::max(std::fabs(lr[k]), std::fabs(li[k])));
+        acc.add(a76 * a76 * quad[k]);
+      }
+      qp[k + 1] = acc.value();
+    }
+    a->mb_lw_scale[d] = lmax > 0 ? lmax : 1.0;
+    std::vector<float2> lw(n_points);
+    for (int64_t k = 0; k < n_points; ++k)
+      lw[k] = make_float2((float)(lr[k] / a->mb_lw_scale[d]), (float)(li[k] / a->mb_lw_scale[d]));
+    if ((rc = upload(a, &a->mb_lw[d], lw))) return rc;
+    if ((rc = upload(a, &a->mb_qprefix[d], qp))) return rc;
   }
   std::vector<int64_t> bs(band_start, band_start + n_bands + 1);
   std::vector<double> bd(band_df, band_df + n_bands);

@@ -147,6 +147,13 @@ struct LaunchArgs {
   int mb_bands;
   const int64_t* mb_band_start;         // [mb_bands + 1] first banded index of each band (and the end)
   const double* mb_band_df;             // [mb_bands] frequency spacing of each band
+  // mixed precision: the float-float phase basis at the banded frequencies, the
+  // linear coefficients times f^(-7/6) in float32 (scaled by mb_lw_scale), and
+  // prefix sums of f^(-7/3) times the quadratic coefficients
+  const float2* mb_basis;               // [mb_points][kNumBasis]
+  const float2* mb_lw[kMaxDet];         // [mb_points]
+  double mb_lw_scale[kMaxDet];
+  const double* mb_qprefix[kMaxDet];    // [mb_points + 1]
   // reduced-order quadrature: the model at the linear and quadratic nodes,
   // time-dependent linear weights on the grid (t_start + k) dt, k < n_time
   int roq;
@@ -213,6 +220,7 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_multiband_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 // Ordering of a mixed TaylorF2 launch: the band-end keys, doubled when points

@@ -155,7 +155,7 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
     r.c_lo[kNumBasis] = s.lo;
   }
   r.valid = ok ? 1 : 0;
-  if (a.rf_tol > 0 && r.valid && a.model == GWL_MODEL_TAYLORF2) {
+  if (a.rf_tol > 0 && a.rf_count && r.valid && a.model == GWL_MODEL_TAYLORF2) {
     // error bound of the fast mixed-precision sums (kRefineL2): norms of the
     // per-bin terms |<d|h>_k| = 4/T A0 |Q_d| f^(-7/6) |d_k| / S_k over the band
     const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
@@ -1424,6 +1424,134 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband(LaunchArgs a) {
   if (lane == 0) finish_point(a, r, i, sr, -si, hh);
 }
 
+// Multi-banding in mixed precision: one warp per point, lanes over the banded
+// frequencies of each band.  The phase of every banded frequency comes from
+// the float-float basis at that frequency (mb_basis) reduced to 0.64 fixed
+// point; detector d's time shift f dt_d is exact in 0.64 fixed point per band
+// (frac(f_b0 dt_d) + i frac(df_b dt_d), f = f_b0 + i df_b); cos / sin by the
+// hardware approximation; the linear coefficients times f^(-7/6) in float32;
+// 8-term float32 partials folded into float-float, then float64 over the
+// warp.  <h|h> needs no per-frequency work: A^2 |Q_d|^2 times the prefix sum
+// of f^(-7/3) quad over the point's band.
+template <int D>
+__global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kRelbinWarps + (threadIdx.x >> 5);
+  if (i >= a.B) return;  // uniform over the warp
+  const PointRec& r = a.rec[i];
+  double sr = 0.0, si = 0.0, hh = 0.0;
+  if (r.valid) {
+    // the point's band among the banded frequencies: fmin <= f < f_isco
+    int64_t kb0 = 0, kb1 = a.mb_points;
+    {
+      int64_t lo = 0, hi = a.mb_points;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (a.mb_freq[mid] >= a.fmin) hi = mid; else lo = mid + 1;
+      }
+      kb0 = lo;
+      lo = kb0;
+      hi = a.mb_points;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if (a.mb_freq[mid] >= r.f_isco) hi = mid; else lo = mid + 1;
+      }
+      kb1 = lo;
+    }
+    float ch[kNumBasis + 1], cl[kNumBasis + 1];
+#pragma unroll
+    for (int b = 0; b <= kNumBasis; ++b) {
+      ch[b] = r.c_hi[b];
+      cl[b] = r.c_lo[b];
+    }
+    float ahi[D], alo[D], bhi[D], blo[D], pre[D], pim[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = pre[d] = pim[d] = 0.f;
+    int n_acc = 0;
+    for (int b = 0; b < a.mb_bands; ++b) {
+      const int64_t bs = a.mb_band_start[b];
+      const int64_t k_lo = max(bs, kb0), k_hi = min(a.mb_band_start[b + 1], kb1);
+      if (k_lo >= k_hi) continue;  // uniform over the warp
+      // detector d's shift in this band, 0.64 fixed point: lane d computes it
+      uint64_t Yl = 0, Xl = 0;
+      if (lane < D) {
+        const double dt = r.dt[lane];
+        const double y = a.mb_freq[bs] * dt, x = a.mb_band_df[b] * dt;
+        double fy = ldexp(y - floor(y), 64), fx = ldexp(x - floor(x), 64);
+        if (!(fy < 18446744073709551616.0)) fy = 0.0;
+        if (!(fx < 18446744073709551616.0)) fx = 0.0;
+        Yl = (uint64_t)fy;
+        Xl = (uint64_t)fx;
+      }
+      uint64_t Y[D], X[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        Y[d] = __shfl_sync(0xffffffffu, Yl, d);
+        X[d] = __shfl_sync(0xffffffffu, Xl, d);
+      }
+      for (int64_t k = k_lo + lane; k < k_hi; k += 32) {
+        const float4* bp = reinterpret_cast<const float4*>(a.mb_basis + k * kNumBasis);
+        float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+        for (int q = 0; q < kNumBasis / 2; ++q) {
+          const float4 v = __ldg(bp + q);
+          ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+          ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
+        }
+        const uint64_t base = to_fixed(s_hi, s_lo);
+        const uint64_t idx = (uint64_t)(k - bs);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const uint64_t full = base + Y[d] + idx * X[d];
+          const uint32_t top = (uint32_t)((full + 0x80000000ull) >> 32);
+          const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
+          float sn, cs;
+          __sincosf(ph, &sn, &cs);
+          const float2 L = __ldg(a.mb_lw[d] + k);
+          // h_d L with h_d proportional to exp(-i phase)
+          pre[d] = __fmaf_rn(cs, L.x, __fmaf_rn(sn, L.y, pre[d]));
+          pim[d] = __fmaf_rn(cs, L.y, __fmaf_rn(-sn, L.x, pim[d]));
+        }
+        if (++n_acc == 8) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            two_sum_acc(ahi[d], alo[d], pre[d]);
+            two_sum_acc(bhi[d], blo[d], pim[d]);
+            pre[d] = pim[d] = 0.f;
+          }
+          n_acc = 0;
+        }
+      }
+    }
+    double P_re[D], P_im[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      two_sum_acc(ahi[d], alo[d], pre[d]);
+      two_sum_acc(bhi[d], blo[d], pim[d]);
+      P_re[d] = (double)ahi[d] + (double)alo[d];
+      P_im[d] = (double)bhi[d] + (double)blo[d];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        P_re[d] += __shfl_xor_sync(0xffffffffu, P_re[d], off);
+        P_im[d] += __shfl_xor_sync(0xffffffffu, P_im[d], off);
+      }
+    }
+    if (lane == 0) {
+      // sum_d A Q_d P_d scale_d, Q_d = Fp (1 + c^2) / 2 - i Fx c
+      const double ci = r.cos_i, pfac = (1.0 + ci * ci) / 2.0;
+      for (int d = 0; d < D; ++d) {
+        const double qr = r.fp[d] * pfac, qi = -r.fx[d] * ci;
+        const double pr = P_re[d] * a.mb_lw_scale[d], pm = P_im[d] * a.mb_lw_scale[d];
+        sr += r.amp * (qr * pr - qi * pm);
+        si += r.amp * (qr * pm + qi * pr);
+        hh += r.amp * r.amp * (qr * qr + qi * qi) * (a.mb_qprefix[d][kb1] - a.mb_qprefix[d][kb0]);
+      }
+    }
+  }
+  // <d|h> = conj(sum h L)
+  if (lane == 0) finish_point(a, r, i, sr, -si, hh);
+}
+
 __global__ void k_finalize(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.B) return;
@@ -1566,6 +1694,12 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
 cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s) {
   const unsigned grid = (unsigned)((a.B + kRelbinWarps - 1) / kRelbinWarps);
   GWL_DISPATCH_D(k_roq, grid, 32 * kRelbinWarps, 0, s, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_multiband_mixed(const LaunchArgs& a, cudaStream_t s) {
+  const unsigned grid = (unsigned)((a.B + kRelbinWarps - 1) / kRelbinWarps);
+  GWL_DISPATCH_D(k_multiband_mixed, grid, 32 * kRelbinWarps, 0, s, a);
   return cudaGetLastError();
 }
 
