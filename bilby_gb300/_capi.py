@@ -105,6 +105,9 @@ SIGNATURES = {
     "gwl_get_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
     "gwl_set_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "gwl_set_refinement": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "gwl_host_buffers": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                        ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]),
+    "gwl_eval_host_staged": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]),
     "gwl_get_refinement": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "gwl_last_refined": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "gwl_batcher_last_refined": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),

@@ -9,6 +9,7 @@ for batches of parameter points through the C ABI.  The likelihood class in
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -52,6 +53,7 @@ class Analysis:
     def __init__(self, model: str, frequency: np.ndarray, detectors: list[DetectorData], duration: float,
                  sampling_frequency: float, minimum_frequency: float = 20.0):
         self._lib = _capi.load()
+        self._staged_lock = threading.Lock()
         self.model = model
         self.model_id = {"sinegaussian": _capi.MODEL_SINEGAUSSIAN, "taylorf2": _capi.MODEL_TAYLORF2}[model]
         self.n_detectors = len(detectors)
@@ -200,6 +202,38 @@ class Analysis:
         _capi.check(self._lib.gwl_eval_host(self._h, _capi.dptr(block), B, PRECISIONS[precision], _capi.dptr(out)),
                     "gwl_eval_host")
         return out
+
+    def log_likelihood_ratio_staged(self, params: dict, precision: str = "fp64") -> np.ndarray:
+        """Like log_likelihood_ratio_host for a dict of equal-length arrays, with the
+        parameter block written straight into the library's pinned staging
+        buffer (gwl_host_buffers / gwl_eval_host_staged): no block allocation
+        and no host copies inside the library."""
+        n = 1
+        for v in params.values():
+            sh = np.shape(v)
+            if len(sh):
+                n = max(n, sh[0])
+        with self._staged_lock:  # the staging buffer is shared by the calls on this analysis
+            return self._staged(params, n, precision)
+
+    def _staged(self, params: dict, n: int, precision: str) -> np.ndarray:
+        pp = ctypes.POINTER(ctypes.c_double)()
+        po = ctypes.POINTER(ctypes.c_double)()
+        _capi.check(self._lib.gwl_host_buffers(self._h, int(n), ctypes.byref(pp), ctypes.byref(po)), "gwl_host_buffers")
+        key = (ctypes.addressof(pp.contents), ctypes.addressof(po.contents), n)
+        if getattr(self, "_staged_key", None) != key:
+            self._staged_block = np.ctypeslib.as_array(pp, shape=(_capi.NPARAM * n,)).reshape(_capi.NPARAM, n)
+            self._staged_out = np.ctypeslib.as_array(po, shape=(n,))
+            self._staged_key = key
+        block = self._staged_block
+        for key_, slot in _capi.SLOT.items():
+            v = params.get(key_)
+            if v is None:
+                block[slot] = 0.0
+            else:
+                block[slot] = v
+        _capi.check(self._lib.gwl_eval_host_staged(self._h, int(n), PRECISIONS[precision]), "gwl_eval_host_staged")
+        return self._staged_out.copy()
 
     def log_likelihood_ratio_device(self, block_ptr: int, B: int, out_ptr: int, precision: str = "fp64",
                                     stream: int = 0):

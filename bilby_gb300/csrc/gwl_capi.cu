@@ -128,7 +128,7 @@ struct gwl_analysis {
   double* d_tm = nullptr;
   size_t tm_bytes = 0;
   double* h_params = nullptr;  // pinned staging for gwl_eval_host
-  double* h_out = nullptr;
+  double* h_out = nullptr;      // [ws_B + 1]: the results, then the device status word
   int* d_status = nullptr;
   cudaStream_t stream = nullptr;
   SideStream side;  // the accurate kernel beside the fast one
@@ -379,7 +379,7 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
     if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_tm), tm, false))) return rc;
   }
   GWL_CUDA(cudaMallocHost(&a->h_params, sizeof(double) * GWL_NPARAM * B));
-  GWL_CUDA(cudaMallocHost(&a->h_out, sizeof(double) * B));
+  GWL_CUDA(cudaMallocHost(&a->h_out, sizeof(double) * (B + 1)));
   a->ws_B = B;
   a->part_bytes = part;
   a->tm_bytes = tm;
@@ -1259,6 +1259,28 @@ int gwl_inner_products_device(gwl_analysis* a, const double* params, int64_t B, 
   return rc;
 }
 
+namespace {
+// One evaluation of the B points in the pinned staging buffer h_params into
+// h_out (the caller holds the analysis lock): upload, launch sequence,
+// download of the results and the device status word, one synchronisation.
+int eval_staged(gwl_analysis* a, int64_t B, int32_t precision) {
+  GWL_CUDA(cudaMemcpyAsync(a->d_params, a->h_params, sizeof(double) * GWL_NPARAM * B, cudaMemcpyHostToDevice,
+                           a->stream));
+  int rc = run_eval(a, a->d_params, B, precision, a->d_out, nullptr, nullptr, a->stream);
+  if (rc) return rc;
+  GWL_CUDA(cudaMemcpyAsync(a->h_out, a->d_out, sizeof(double) * B, cudaMemcpyDeviceToHost, a->stream));
+  int* h_status = reinterpret_cast<int*>(a->h_out + B);
+  GWL_CUDA(cudaMemcpyAsync(h_status, a->d_status, sizeof(int), cudaMemcpyDeviceToHost, a->stream));
+  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  if (*h_status != kDevStatusOk) {
+    cudaMemset(a->d_status, 0, sizeof(int));
+    set_error("a bounded device wait gave up (bulk copy did not complete)");
+    return GWL_ERR_TIMEOUT;
+  }
+  return GWL_OK;
+}
+}  // namespace
+
 int gwl_eval_host(gwl_analysis* a, const double* params, int64_t B, int32_t precision, double* out) {
   if (!a || (B > 0 && (!params || !out))) {
     set_error("null argument");
@@ -1271,21 +1293,40 @@ int gwl_eval_host(gwl_analysis* a, const double* params, int64_t B, int32_t prec
   if (rc) return rc;
   // stage through pinned buffers so that both copies are true async DMA
   std::memcpy(a->h_params, params, sizeof(double) * GWL_NPARAM * B);
-  GWL_CUDA(cudaMemcpyAsync(a->d_params, a->h_params, sizeof(double) * GWL_NPARAM * B, cudaMemcpyHostToDevice,
-                           a->stream));
-  rc = run_eval(a, a->d_params, B, precision, a->d_out, nullptr, nullptr, a->stream);
-  if (rc) return rc;
-  GWL_CUDA(cudaMemcpyAsync(a->h_out, a->d_out, sizeof(double) * B, cudaMemcpyDeviceToHost, a->stream));
-  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  if ((rc = eval_staged(a, B, precision))) return rc;
   std::memcpy(out, a->h_out, sizeof(double) * B);
-  int status = 0;
-  GWL_CUDA(cudaMemcpy(&status, a->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (status != kDevStatusOk) {
-    cudaMemset(a->d_status, 0, sizeof(int));
-    set_error("a bounded device wait gave up (bulk copy did not complete)");
-    return GWL_ERR_TIMEOUT;
-  }
   return GWL_OK;
+}
+
+int gwl_host_buffers(gwl_analysis* a, int64_t B, double** params, double** out) {
+  if (!a || B <= 0 || !params || !out) {
+    set_error("null argument or empty batch");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  LaunchArgs L = make_args(a, B, GWL_PRECISION_FP64);
+  int rc = ensure_workspace(a, B, L);
+  if (rc) return rc;
+  *params = a->h_params;
+  *out = a->h_out;
+  return GWL_OK;
+}
+
+int gwl_eval_host_staged(gwl_analysis* a, int64_t B, int32_t precision) {
+  if (!a || B < 0) {
+    set_error("null argument or negative batch size");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (B == 0) return GWL_OK;
+  std::lock_guard<std::mutex> g(a->mu);
+  if (B > a->ws_B || !a->h_params) {
+    set_error("gwl_eval_host_staged: call gwl_host_buffers for this batch size first");
+    return GWL_ERR_ARGUMENT;
+  }
+  LaunchArgs L = make_args(a, B, precision);
+  int rc = ensure_workspace(a, B, L);  // the time-marginalisation work space may still be missing
+  if (rc) return rc;
+  return eval_staged(a, B, precision);
 }
 
 int gwl_source_polarizations(int32_t model, const double* frequency, int64_t n, const double* params,

@@ -398,8 +398,7 @@ class GravitationalWaveTransient(_Base):
             self.analysis.log_likelihood_ratio_device(block.data_ptr(), n, res.data_ptr(), precision, stream)
             return res
         arrays = {k: np.asarray(v, dtype=np.float64) for k, v in parameters.items()}
-        block = params_block(self._prepare(arrays))
-        return self.analysis.log_likelihood_ratio_host(block, precision)
+        return self.analysis.log_likelihood_ratio_staged(self._prepare(arrays), precision)
 
     def log_likelihood_ratio_from_unit_cube(self, unit, device_priors, precision=None, out=None):
         """lnL ratios of a batch given as unit-cube samples: ``unit`` is a CUDA

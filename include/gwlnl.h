@@ -212,6 +212,15 @@ int gwl_batcher_eval(gwl_batcher *b, const gwl_batch_item *items, int32_t n, int
 /* Reads and clears the batcher's device status word (non-zero: a bounded wait gave up). */
 int gwl_batcher_status(gwl_batcher *b, int *device_status);
 
+/* Zero-copy host staging: gwl_host_buffers returns the analysis's pinned
+ * parameter block [GWL_NPARAM][B] and result buffer [B] (valid until a
+ * larger batch reallocates them); the caller fills the block and calls
+ * gwl_eval_host_staged, which runs gwl_eval_host without the two host
+ * copies and leaves the lnL ratios in the result buffer.  Same results as
+ * gwl_eval_host (no counterpart in the reference). */
+int gwl_host_buffers(gwl_analysis *a, int64_t B, double **params, double **out);
+int gwl_eval_host_staged(gwl_analysis *a, int64_t B, int32_t precision);
+
 /* log_likelihood_ratio for B points without allocating device memory, for
  * callers that cannot let a library call cudaMalloc (an application that
  * reserves the GPU's memory for its own pool, or a latency-critical loop
