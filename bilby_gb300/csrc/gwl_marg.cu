@@ -395,8 +395,18 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         hh_part += norm * a.inv_psd[d][L] * (A * A * (g1 + g2) * (g1 + g2) + Cx * Cx * (g1 - g2) * (g1 - g2));
       }
     }
+    if (MIXED && threadIdx.x == 0) {
+      // this point's candidate window of FFT indices (checked exactly in C):
+      // the last FFT stages compute only the outputs inside it
+      const double jit = r.jitter;
+      const double jl = floor((a.t_min - a.start_time0 - jit) * a.tm_inv_step) - 3.0;
+      const double jh = ceil((a.t_max - a.start_time0 - jit) * a.tm_inv_step) + 2.0;
+      s_jr[0] = (long long)fmax(0.0, jl);
+      s_jr[1] = (long long)fmin((double)(L - 1), jh);
+    }
     __syncthreads();
     // ---- B: in-place FFT, radix-4 passes (two radix-2 stages each) -------
+    const int64_t n_win = MIXED ? (int64_t)(s_jr[1] - s_jr[0] + 1) : 0;
     int stage = 1;
     if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
       stage = 5;  // stages 1-4 ran with the integrand
@@ -461,7 +471,12 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     for (; stage < log2L; stage += 2) {
       const int64_t h = (int64_t)1 << (stage - 1);  // half-length of the first of the two stages
       const int64_t s1 = L / (2 * h), s2 = L / (4 * h);  // twiddle strides of the two stages
-      for (int64_t bf = threadIdx.x; bf < L / 4; bf += blockDim.x) {
+      // mixed, the last two stages (h = L / 4): output j comes from the
+      // butterfly at j mod h alone, so only the window's butterflies run
+      const bool prune = MIXED && stage + 1 == log2L && n_win > 0 && n_win <= h;
+      const int64_t n_bf = prune ? n_win : L / 4;
+      for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
+        const int64_t bf = prune ? ((s_jr[0] + t) & (h - 1)) : t;
         const int64_t pos = bf & (h - 1);
         const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
         const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
@@ -485,7 +500,10 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     }
     if (stage == log2L) {  // a last radix-2 stage (half-length L / 2, twiddle exp(-2 pi i q / L))
       const int64_t h = L / 2;
-      for (int64_t q = threadIdx.x; q < h; q += blockDim.x) {
+      const bool prune = MIXED && n_win > 0 && n_win <= h;  // only the window's butterflies
+      const int64_t n_bf = prune ? n_win : h;
+      for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
+        const int64_t q = prune ? ((s_jr[0] + t) & (h - 1)) : t;
         const C w = tw(q);
         const C x0 = buf[P(q)], x1 = buf[P(q + h)];
         const R tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
@@ -527,11 +545,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         s_scal[2] = sr;
         s_scal[3] = a.tm_step;
         s_scal[4] = a.tm_prob;
-        // candidate window from the real-valued bounds, checked exactly below
-        const double jl = floor((a.t_min - a.start_time0 - jit) * a.tm_inv_step) - 3.0;
-        const double jh = ceil((a.t_max - a.start_time0 - jit) * a.tm_inv_step) + 2.0;
-        s_jr[0] = (long long)fmax(0.0, jl);
-        s_jr[1] = (long long)fmin((double)(L - 1), jh);
+        // the candidate window (s_jr) was set before the FFT
       } else if (a.dist_marg) {
         s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)hh_ref);
       }
