@@ -186,3 +186,16 @@ def test_mixed_at_the_injection(fixture, request):
     assert ref[0] > 20.0, ref[0]  # a loud signal
     assert np.all(np.abs(exact[::4] - ref) <= FP64_RTOL * scale)
     assert np.max(np.abs(got - exact)) <= MIXED_ATOL, np.abs(got - exact)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_staged_host_evaluation_matches(tf2_small, precision):
+    """log_likelihood_ratio_staged (parameters written into the pinned staging
+    buffer, gwl_eval_host_staged) gives the results of gwl_eval_host bit for
+    bit, for a batch, a smaller batch after it, and a larger one."""
+    w, dets, an = tf2_small
+    for n in (300, 17, 700):
+        p = draw_points(w, n, np.random.default_rng(60 + n))
+        ref = an.log_likelihood_ratio_host(params_block(p), precision)
+        got = an.log_likelihood_ratio_staged(p, precision)
+        assert np.array_equal(ref, got)
