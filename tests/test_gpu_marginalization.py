@@ -139,3 +139,51 @@ def test_phase_marginalization_vs_brute_force(gpu, tmp_path):
         brute = np.log(np.mean(np.exp(lnl - lnl.max()))) + lnl.max()
         q["phase"] = 0.0
         assert abs(marg.log_likelihood_ratio(q) - brute) < 1e-6 * max(1.0, abs(brute))
+
+
+@pytest.mark.parametrize("combo", ["t", "tp", "tpd"])
+def test_mixed_time_marginalized_matches_float64_fft16384(gpu, tmp_path, combo):
+    """The mixed time-marginalised kernel at FFT length 16384 (8 s at 4096 Hz:
+    an even number of stages, a radix-4 last pass pruned to the prior window)
+    against the float64 kernel on 96 prior draws: |dlnL| <= 1e-3."""
+    from bilby_gb300.workloads import draw_points
+    w = WORKLOADS["tf2_marg_8s"]
+    like, priors = make_likelihood(w, combo, "mixed", tmp_path / "table.npz")
+    p = draw_points(w, 96, np.random.default_rng(71))
+    p["geocent_time"] = np.full(96, float(priors["geocent_time"]))
+    if "p" in combo:
+        p["phase"] = np.zeros(96)
+    if "d" in combo:
+        p["luminosity_distance"] = np.full(96, float(priors["luminosity_distance"]))
+    mixed = like.log_likelihood_ratio_batch(p, precision="mixed")
+    fp64 = like.log_likelihood_ratio_batch(p, precision="fp64")
+    assert np.all(np.abs(mixed - fp64) <= 1e-3), np.abs(mixed - fp64).max()
+
+
+def test_mixed_time_marginalized_sine_gaussian(gpu, tmp_path):
+    """Time marginalisation of the sine-Gaussian in mixed precision (the
+    full-band integrand, the padded buffer, radix-16 passes and the pruned last
+    pass) against float64 on 64 draws (4 s at 2048 Hz, FFT length 4096):
+    |dlnL| <= 1e-3 + 2e-8 |lnL| (the sine-Gaussian mixed tolerance)."""
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.source import sinegaussian
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    from bilby_gb300.workloads import draw_points
+    w = WORKLOADS["sg_4s"]
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=sinegaussian)
+    ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+    tc = w.injection["geocent_time"]
+    priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1)}
+    like = GravitationalWaveTransient(ifos, wfg, priors=priors, time_marginalization=True, precision="mixed")
+    p = draw_points(w, 64, np.random.default_rng(73))
+    p["geocent_time"] = np.full(64, float(priors["geocent_time"]))
+    mixed = like.log_likelihood_ratio_batch(p, precision="mixed")
+    fp64 = like.log_likelihood_ratio_batch(p, precision="fp64")
+    assert np.all(np.abs(mixed - fp64) <= 1e-3 + 2e-8 * np.abs(fp64)), np.abs(mixed - fp64).max()
