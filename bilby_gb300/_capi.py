@@ -74,6 +74,8 @@ SIGNATURES = {
                                                ctypes.c_void_p]),
     "gwl_inner_products_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "gwl_time_series_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p]),
     "gwl_source_polarizations": (ctypes.c_int, [ctypes.c_int32, c_double_p, ctypes.c_int64, c_double_p,
                                                 ctypes.c_double, c_double_p, c_double_p]),
     "gwl_detector_response": (ctypes.c_int, [ctypes.POINTER(GwlDetector), c_double_p, ctypes.c_int64, c_double_p,

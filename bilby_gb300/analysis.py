@@ -248,6 +248,43 @@ class Analysis:
             self._h, ctypes.c_void_p(block_ptr), int(B), PRECISIONS[precision], ctypes.c_void_p(dh_ptr),
             ctypes.c_void_p(hh_ptr), ctypes.c_void_p(stream)), "gwl_inner_products_device")
 
+    def time_series_device(self, block_ptr: int, B: int, series_ptr: int, hh_ptr: int, stream: int = 0):
+        """The float64 <d|h>(t) transform of every point ([B, 2 (n_bins - 1)]
+        doubles) and <h|h> ([B]), device pointers, asynchronous on ``stream``."""
+        _capi.check(self._lib.gwl_time_series_device(self._h, ctypes.c_void_p(block_ptr), int(B),
+                                                     ctypes.c_void_p(series_ptr), ctypes.c_void_p(hh_ptr),
+                                                     ctypes.c_void_p(stream)), "gwl_time_series_device")
+
+    def inner_products_host(self, block: np.ndarray, precision: str = "fp64") -> tuple[np.ndarray, np.ndarray]:
+        """Host parameter block [NPARAM, B] -> (complex <d|h> [B], <h|h> [B]),
+        evaluated by the fused kernels (synchronous)."""
+        import torch
+        block = np.ascontiguousarray(block, dtype=np.float64)
+        B = block.shape[1]
+        dev = torch.from_numpy(block).cuda()
+        dh = torch.empty((B, 2), dtype=torch.float64, device=dev.device)
+        hh = torch.empty(B, dtype=torch.float64, device=dev.device)
+        stream = torch.cuda.current_stream(dev.device)
+        self.inner_products_device(dev.data_ptr(), B, dh.data_ptr(), hh.data_ptr(), precision, stream.cuda_stream)
+        stream.synchronize()
+        dh = dh.cpu().numpy()
+        return dh[:, 0] + 1j * dh[:, 1], hh.cpu().numpy()
+
+    def time_series_host(self, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """Host parameter block [NPARAM, B] -> (complex <d|h>(t) [B, n_bins - 1],
+        <h|h> [B]) from the float64 time-marginalisation kernel (synchronous)."""
+        import torch
+        block = np.ascontiguousarray(block, dtype=np.float64)
+        B, L = block.shape[1], self.n_bins - 1
+        dev = torch.from_numpy(block).cuda()
+        series = torch.empty((B, L, 2), dtype=torch.float64, device=dev.device)
+        hh = torch.empty(B, dtype=torch.float64, device=dev.device)
+        stream = torch.cuda.current_stream(dev.device)
+        self.time_series_device(dev.data_ptr(), B, series.data_ptr(), hh.data_ptr(), stream.cuda_stream)
+        stream.synchronize()
+        s = series.cpu().numpy()
+        return s[..., 0] + 1j * s[..., 1], hh.cpu().numpy()
+
     def set_profiling(self, enable: bool):
         _capi.check(self._lib.gwl_set_profiling(self._h, int(enable)), "gwl_set_profiling")
 

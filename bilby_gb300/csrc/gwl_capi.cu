@@ -387,7 +387,7 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
 }
 
 int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, double* d_out, double* d_dh,
-             double* d_hh, cudaStream_t s) {
+             double* d_hh, cudaStream_t s, double* d_series = nullptr) {
   if (precision != GWL_PRECISION_FP64 && precision != GWL_PRECISION_MIXED) {
     set_error("precision must be GWL_PRECISION_FP64 or GWL_PRECISION_MIXED");
     return GWL_ERR_ARGUMENT;
@@ -403,6 +403,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.dh_out = d_dh;
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
+  L.tm_series = d_series;
   if (a->relbin || a->multiband || a->roq) {
     // relative binning / multi-banding / ROQ: per-point set-up, then one warp
     // per point over the bin edges, banded frequencies or nodes (no marking
@@ -1257,6 +1258,30 @@ int gwl_inner_products_device(gwl_analysis* a, const double* params, int64_t B, 
   const int rc = run_eval(a, params, B, precision, nullptr, d_inner_h, h_inner_h, static_cast<cudaStream_t>(stream));
   a->time_marg = saved;
   return rc;
+}
+
+int gwl_time_series_device(gwl_analysis* a, const double* params, int64_t B, double* series, double* h_inner_h,
+                           void* stream) {
+  if (!a || (B > 0 && (!params || !series || !h_inner_h))) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->time_marg) {
+    set_error("gwl_time_series_device needs time marginalisation enabled");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (a->relbin || a->multiband || a->roq) {
+    set_error("gwl_time_series_device serves the full frequency grid only");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (B <= 0) return GWL_OK;
+  LaunchArgs L = make_args(a, B, GWL_PRECISION_FP64);
+  int rc = ensure_workspace(a, B, L);
+  if (rc) return rc;
+  // the marginalised lnL goes to the work space's result slots
+  return run_eval(a, params, B, GWL_PRECISION_FP64, a->d_out, nullptr, h_inner_h, static_cast<cudaStream_t>(stream),
+                  series);
 }
 
 namespace {

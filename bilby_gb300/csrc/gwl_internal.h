@@ -128,6 +128,7 @@ struct LaunchArgs {
   double bbox[4];
   double ref_dist;
   double* tm_work;                      // time-marginalisation work space
+  double* tm_series;                    // optional [B][2 n_fft] FFT of the integrand (float64 kernel)
   // relative binning: the model at the bin edges, its ratio to the fiducial
   // response, and the per-bin summary data of each detector
   int relbin;

@@ -520,6 +520,16 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     // ---- C: prior window, marginalised lnL per time sample, logsumexp ----
     double hh = 0.0;
     if (!(MIXED && a.model == GWL_MODEL_TAYLORF2)) hh = block_sum(hh_part, red);
+    if constexpr (!MIXED) {
+      if (a.tm_series) {
+        // the whole transform in natural order, d_inner_h_array of
+        // base.py:325-330, and <h|h> (block_sum ends with a barrier, so the
+        // last FFT stage's writes are visible)
+        double2* dst = reinterpret_cast<double2*>(a.tm_series) + (size_t)i * L;
+        for (int64_t k = threadIdx.x; k < L; k += blockDim.x) dst[k] = buf[k];
+        if (a.hh_out && threadIdx.x == 0) a.hh_out[i] = hh;
+      }
+    }
     const double jit = r.jitter;
     // per-point scalars, computed once (float64 issues slowly) and shared
     if (MIXED && a.model == GWL_MODEL_TAYLORF2 && threadIdx.x < D) {

@@ -197,6 +197,26 @@ class Interferometer:
 
     minimum_frequency = property(lambda self: self.strain_data.minimum_frequency)
     maximum_frequency = property(lambda self: self.strain_data.maximum_frequency)
+    frequency_domain_strain = property(lambda self: self.strain_data.frequency_domain_strain)
+
+    # noise-weighted inner products over the masked band (interferometer.py:607-679,
+    # gw/utils.py:118-190): host utilities on arrays the caller already holds
+    def _weighted(self, aa, bb):
+        m = self.frequency_mask
+        return 4 / self.duration * np.sum(np.conj(aa[m]) * bb[m] / self.power_spectral_density_array[m])
+
+    def inner_product(self, signal):
+        return self._weighted(signal, self.frequency_domain_strain)
+
+    def optimal_snr_squared(self, signal):
+        return self._weighted(signal, signal).real
+
+    def template_template_inner_product(self, signal_1, signal_2):
+        return self._weighted(signal_1, signal_2)
+
+    def matched_filter_snr(self, signal):
+        return self.inner_product(signal) / self.optimal_snr_squared(signal) ** 0.5
+
     frequency_array = property(lambda self: self.strain_data.frequency_array)
     frequency_mask = property(lambda self: self.strain_data.frequency_mask)
     sampling_frequency = property(lambda self: self.strain_data.sampling_frequency)

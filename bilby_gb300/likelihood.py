@@ -144,6 +144,7 @@ class GravitationalWaveTransient(_Base):
             priors["luminosity_distance"] = float(self._ref_dist)
             self._marginalized_parameters.append("luminosity_distance")
         self._analysis = None
+        self._detector_analyses = {}
         self._build_analysis()
 
     # ------------------------------------------------------------------
@@ -286,21 +287,23 @@ class GravitationalWaveTransient(_Base):
             self._distance_array, self.distance_prior_array, float(self._ref_dist), self.phase_marginalization)
         self.cache_lookup_table()
 
-    def _build_analysis(self):
-        ifos = self.interferometers
+    @staticmethod
+    def _detector_data(ifo) -> DetectorData:
+        geom = ifo.geometry
+        return DetectorData(ifo.name, np.asarray(geom.vertex, dtype=np.float64),
+                            np.asarray(geom.detector_tensor, dtype=np.float64), float(ifo.strain_data.start_time),
+                            np.asarray(ifo.strain_data.frequency_domain_strain, dtype=np.complex128),
+                            np.asarray(ifo.power_spectral_density_array, dtype=np.float64),
+                            np.asarray(ifo.strain_data.frequency_mask, dtype=bool))
+
+    def _new_analysis(self, ifos) -> Analysis:
         freq = np.asarray(ifos[0].strain_data.frequency_array, dtype=np.float64)
-        dets = []
-        for ifo in ifos:
-            geom = ifo.geometry
-            dets.append(DetectorData(ifo.name, np.asarray(geom.vertex, dtype=np.float64),
-                                     np.asarray(geom.detector_tensor, dtype=np.float64),
-                                     float(ifo.strain_data.start_time),
-                                     np.asarray(ifo.strain_data.frequency_domain_strain, dtype=np.complex128),
-                                     np.asarray(ifo.power_spectral_density_array, dtype=np.float64),
-                                     np.asarray(ifo.strain_data.frequency_mask, dtype=bool)))
         fmin = self.waveform_generator.waveform_arguments.get("minimum_frequency", 20.0)
-        an = Analysis(self._model, freq, dets, float(ifos[0].strain_data.duration),
-                      float(ifos[0].strain_data.sampling_frequency), fmin)
+        return Analysis(self._model, freq, [self._detector_data(ifo) for ifo in ifos],
+                        float(ifos[0].strain_data.duration), float(ifos[0].strain_data.sampling_frequency), fmin)
+
+    def _build_analysis(self):
+        an = self._new_analysis(self.interferometers)
         if self.time_marginalization:
             tp = self.priors["geocent_time"]
             an.set_time_marginalization(True, self.jitter_time, tp.minimum, tp.maximum)
@@ -317,6 +320,7 @@ class GravitationalWaveTransient(_Base):
     def __getstate__(self):
         state = self.__dict__.copy()
         state["_analysis"] = None
+        state["_detector_analyses"] = {}
         return state
 
     def __setstate__(self, state):
@@ -428,6 +432,263 @@ class GravitationalWaveTransient(_Base):
         res = self.analysis.autotune(block.data_ptr(), block.shape[1], torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         return res
+
+    # ------------------------------------------------------------------
+    # per-detector quantities and posterior reconstruction
+    # (base.py:108-148, 260-354, 448-770)
+    # ------------------------------------------------------------------
+    class _CalculatedSNRs:
+        """The inner products of one detector, or their sum over detectors
+        (``+`` / ``+=``): base.py:108-148."""
+        __slots__ = ("d_inner_h", "optimal_snr_squared", "complex_matched_filter_snr", "d_inner_h_array",
+                     "optimal_snr_squared_array")
+
+        def __init__(self, d_inner_h=0j, optimal_snr_squared=0, complex_matched_filter_snr=0j, d_inner_h_array=None,
+                     optimal_snr_squared_array=None):
+            self.d_inner_h = d_inner_h
+            self.optimal_snr_squared = optimal_snr_squared
+            self.complex_matched_filter_snr = complex_matched_filter_snr
+            self.d_inner_h_array = d_inner_h_array
+            self.optimal_snr_squared_array = optimal_snr_squared_array
+
+        def __add__(self, other):
+            new = copy.deepcopy(self)
+            new += other
+            return new
+
+        def __iadd__(self, other):
+            # None is the identity of the array slots
+            for key in self.__slots__:
+                mine, theirs = getattr(self, key), getattr(other, key)
+                if mine is None:
+                    setattr(self, key, theirs)
+                elif theirs is not None:
+                    setattr(self, key, mine + theirs)
+            return self
+
+        def __repr__(self):
+            return (f"_CalculatedSNRs(d_inner_h={self.d_inner_h}, optimal_snr_squared={self.optimal_snr_squared}, "
+                    f"complex_matched_filter_snr={self.complex_matched_filter_snr})")
+
+        @property
+        def snrs_as_sample(self) -> dict:
+            return {"matched_filter_snr": self.complex_matched_filter_snr,
+                    "optimal_snr": self.optimal_snr_squared.real ** 0.5}
+
+    def _detector_analysis(self, interferometer) -> Analysis:
+        """A device-resident analysis of one detector of this likelihood (built
+        on first use), with time marginalisation configured so that the
+        float64 transform <d|h>(t) is available."""
+        name = interferometer.name
+        an = self._detector_analyses.get(name)
+        if an is None:
+            matches = [ifo for ifo in self.interferometers if ifo.name == name]
+            if not matches:
+                raise ValueError(f"interferometer {name} is not part of this likelihood")
+            an = self._new_analysis(matches[:1])
+            if self.time_marginalization:
+                tp = self.priors["geocent_time"]
+                an.set_time_marginalization(True, False, tp.minimum, tp.maximum)
+            self._detector_analyses[name] = an
+        return an
+
+    def _snr_block(self, parameters) -> np.ndarray:
+        """The parameter block of ``parameters`` as given: sky position, psi and
+        geocent_time (already jittered by the caller, as in base.py:427-428)
+        are used as they are; the source parameters pass through the waveform
+        generator's conversion."""
+        converted, _ = self.waveform_generator.parameter_conversion(dict(parameters))
+        converted["time_jitter"] = 0.0
+        return params_block(converted, 1)
+
+    def calculate_snrs(self, waveform_polarizations, interferometer, *, return_array=True, parameters):
+        """The inner products of ``interferometer`` at ``parameters``
+        (base.py:260-354): <d|h>, <h|h>, the complex matched-filter SNR and,
+        with time marginalisation and ``return_array``, the transform
+        d_inner_h_array[j] = 4/T FFT(h conj(d) / S)[j] over the FFT length
+        n_frequencies - 1.  All are evaluated in float64 by the fused GPU
+        kernels, which generate the source model of this likelihood's waveform
+        generator at ``parameters``; ``waveform_polarizations`` (that model at
+        the same parameters, in the reference's call) is accepted for the
+        reference's signature and not read."""
+        an = self._detector_analysis(interferometer)
+        block = self._snr_block(parameters)
+        dh, hh = an.inner_products_host(block, "fp64")
+        d_inner_h, optimal_snr_squared = complex(dh[0]), float(hh[0])
+        d_inner_h_array = None
+        if return_array and self.time_marginalization:
+            series, _ = an.time_series_host(block)
+            d_inner_h_array = series[0]
+        return self._CalculatedSNRs(d_inner_h=d_inner_h, optimal_snr_squared=optimal_snr_squared,
+                                    complex_matched_filter_snr=d_inner_h / optimal_snr_squared ** 0.5,
+                                    d_inner_h_array=d_inner_h_array)
+
+    def _setup_rho(self, d_inner_h, optimal_snr_squared, parameters):
+        """base.py:879-885."""
+        scale = parameters["luminosity_distance"] / self._ref_dist
+        return d_inner_h * scale, np.real(optimal_snr_squared) * scale ** 2
+
+    def distance_marginalized_likelihood(self, d_inner_h, h_inner_h, *, parameters):
+        """base.py:775-784: the lookup table's bicubic spline (the kernels' own
+        float64 evaluator, run on the host), -inf outside its box."""
+        dh_ref, hh_ref = self._setup_rho(d_inner_h, h_inner_h, parameters)
+        dh_ref = np.abs(dh_ref) if self.phase_marginalization else np.real(dh_ref)
+        tx, ty, c = self._spline_tck
+        x = np.atleast_1d(np.asarray(dh_ref, dtype=np.float64))
+        y = np.broadcast_to(np.asarray(hh_ref, dtype=np.float64), x.shape)
+        out = _capi.host_bicubic(x, y, tx, ty, c, self._spline_bbox)
+        return float(out[0]) if np.ndim(dh_ref) == 0 else out
+
+    def phase_marginalized_likelihood(self, d_inner_h, h_inner_h):
+        """base.py:786-792: ln I0(|<d|h>|) - <h|h> / 2."""
+        x = np.atleast_1d(np.abs(np.asarray(d_inner_h))).astype(np.float64)
+        out = _capi.host_ln_i0(x) - np.real(h_inner_h) / 2
+        return float(out[0]) if np.ndim(d_inner_h) == 0 else out
+
+    def time_marginalized_likelihood(self, d_inner_h_tc_array, h_inner_h, *, parameters):
+        """base.py:794-820: logsumexp over the time samples inside the
+        geocent_time prior, weighted by prior(t) * delta_tc."""
+        from scipy.special import logsumexp
+        times = self._times
+        if self.jitter_time:
+            times = self._times + parameters["time_jitter"]
+        tp = self.priors["geocent_time"]
+        keep = (times >= tp.minimum) & (times <= tp.maximum)
+        times = times[keep]
+        series = np.asarray(d_inner_h_tc_array)[keep]
+        weights = tp.prob(times) * self._delta_tc
+        if self.distance_marginalization:
+            lnl_t = self.distance_marginalized_likelihood(series, h_inner_h, parameters=parameters)
+        elif self.phase_marginalization:
+            lnl_t = self.phase_marginalized_likelihood(series, h_inner_h)
+        else:
+            lnl_t = series.real - np.real(h_inner_h) / 2
+        return logsumexp(lnl_t, b=weights)
+
+    def compute_log_likelihood_from_snrs(self, total_snrs, parameters):
+        """base.py:448-477 on the host, from inner products already computed
+        (by ``calculate_snrs``)."""
+        if self.time_marginalization:
+            return self.time_marginalized_likelihood(total_snrs.d_inner_h_array, total_snrs.optimal_snr_squared,
+                                                     parameters=parameters)
+        if self.distance_marginalization:
+            return self.distance_marginalized_likelihood(total_snrs.d_inner_h, total_snrs.optimal_snr_squared,
+                                                         parameters=parameters)
+        if self.phase_marginalization:
+            return self.phase_marginalized_likelihood(total_snrs.d_inner_h, total_snrs.optimal_snr_squared)
+        return np.real(total_snrs.d_inner_h) - total_snrs.optimal_snr_squared / 2
+
+    def compute_per_detector_log_likelihood(self, parameters):
+        """base.py:479-499: adds ``<ifo>_log_likelihood`` to ``parameters`` (in
+        place) for every detector and returns a copy."""
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        if self.time_marginalization and self.jitter_time:
+            parameters["geocent_time"] += parameters["time_jitter"]
+        for ifo in self.interferometers:
+            snrs = self.calculate_snrs(None, ifo, parameters=parameters)
+            parameters[f"{ifo.name}_log_likelihood"] = self.compute_log_likelihood_from_snrs(snrs, parameters)
+        if self.time_marginalization and self.jitter_time:
+            parameters["geocent_time"] -= parameters["time_jitter"]
+        return parameters.copy()
+
+    def _calculate_inner_products(self, signal_polarizations, parameters):
+        """base.py:707-716: <d|h> and <h|h> summed over detectors."""
+        total = self._CalculatedSNRs()
+        for ifo in self.interferometers:
+            total += self.calculate_snrs(signal_polarizations, ifo, return_array=False, parameters=parameters)
+        return total.d_inner_h, total.optimal_snr_squared
+
+    def generate_posterior_sample_from_marginalized_likelihood(self, parameters):
+        """base.py:502-541: draw the marginalised parameters (time, then
+        distance, then phase) from their conditional posteriors at
+        ``parameters``, with the package's shared random generator."""
+        if len(self._marginalized_parameters) == 0:
+            return parameters
+        if self.time_marginalization:
+            parameters["geocent_time"] = self.generate_time_sample_from_marginalized_likelihood(
+                parameters=parameters)
+        if self.distance_marginalization:
+            parameters["luminosity_distance"] = self.generate_distance_sample_from_marginalized_likelihood(
+                parameters=parameters)
+        if self.phase_marginalization:
+            parameters["phase"] = self.generate_phase_sample_from_marginalized_likelihood(parameters=parameters)
+        return parameters.copy()
+
+    def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        """base.py:577-653: the time posterior on a 16384 Hz grid.  The
+        detector responses come from the GPU (the source and response
+        kernels); the zero-padded transform and the draw are host work, as in
+        the reference."""
+        from .prior import Interped
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        if self.jitter_time:
+            parameters["geocent_time"] += parameters["time_jitter"]
+        if signal_polarizations is None:
+            signal_polarizations = self.waveform_generator.frequency_domain_strain(parameters)
+        fs_up = 16384
+        wfg = self.waveform_generator
+        n_up = int(wfg.duration * fs_up)
+        t0 = parameters["geocent_time"] - wfg.start_time  # core/utils/series.py:91-112
+        times = np.linspace(t0, wfg.duration + t0 - 1 / fs_up, num=n_up)
+        times = times % wfg.duration + wfg.start_time
+        tp = self.priors["geocent_time"]
+        in_prior = (times >= tp.minimum) & (times < tp.maximum)
+        times = times[in_prior]
+        d_inner_h = np.zeros(len(times), dtype=complex)
+        psd = np.ones(n_up)
+        signal_long = np.zeros(n_up, dtype=complex)
+        data = np.zeros(n_up, dtype=complex)
+        for ifo in self.interferometers:
+            n_ifo = len(ifo.frequency_domain_strain)
+            mask = ifo.frequency_mask
+            signal_long[:n_ifo] = ifo.get_detector_response(signal_polarizations, parameters)
+            data[:n_ifo] = np.conj(ifo.frequency_domain_strain)
+            psd[:n_ifo][mask] = ifo.power_spectral_density_array[mask]
+            d_inner_h += np.fft.fft(signal_long * data / psd)[in_prior]
+        _, h_inner_h = self._calculate_inner_products(signal_polarizations, parameters)
+        h_inner_h = np.array([h_inner_h])
+        if self.distance_marginalization:
+            lnl_t = self.distance_marginalized_likelihood(d_inner_h, h_inner_h, parameters=parameters)
+        elif self.phase_marginalization:
+            lnl_t = self.phase_marginalized_likelihood(d_inner_h, h_inner_h)
+        else:
+            lnl_t = d_inner_h.real - h_inner_h.real / 2
+        post = np.exp(lnl_t - np.max(lnl_t)) * tp.prob(times)
+        keep = post > np.max(post) / 1000
+        if np.sum(keep) < 3:
+            keep[1:-1] = keep[1:-1] | keep[2:] | keep[:-2]
+        return Interped(times[keep], post[keep]).sample()
+
+    def generate_distance_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        """base.py:655-705: the distance posterior on the lookup table's
+        distance grid."""
+        from .prior import Interped
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        d_inner_h, h_inner_h = self._calculate_inner_products(signal_polarizations, parameters)
+        ratio = parameters["luminosity_distance"] / self._distance_array
+        dh = d_inner_h * ratio
+        hh = h_inner_h * ratio ** 2
+        if self.phase_marginalization:
+            lnl_d = self.phase_marginalized_likelihood(dh, hh)
+        else:
+            lnl_d = dh.real - hh.real / 2
+        post = np.exp(lnl_d - np.max(lnl_d)) * self.distance_prior_array
+        new_distance = Interped(self._distance_array, post).sample()
+        if signal_polarizations is not None:  # base.py:1061-1063: rescaled in place
+            for mode in signal_polarizations:
+                signal_polarizations[mode] *= self._ref_dist / new_distance
+        return new_distance
+
+    def generate_phase_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        """base.py:734-770: the phase posterior on 101 phases in [0, 2 pi],
+        for a signal whose phase enters as exp(-2 i phase)."""
+        from .prior import Interped
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        d_inner_h, h_inner_h = self._calculate_inner_products(signal_polarizations, parameters)
+        phases = np.linspace(0, 2 * np.pi, 101)
+        log_post = (d_inner_h * np.exp(-2j * phases) - h_inner_h / 2).real
+        post = np.exp(log_post - np.max(log_post))
+        return Interped(phases, post).sample()
 
     # ------------------------------------------------------------------
     def __repr__(self):

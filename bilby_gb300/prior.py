@@ -110,3 +110,49 @@ class Gaussian(Prior):
 
     def prob(self, val):
         return np.exp(-(self.mu - val) ** 2 / (2 * self.sigma ** 2)) / (2 * np.pi) ** 0.5 / self.sigma
+
+
+class Interped(Prior):
+    """A density tabulated at points ``xx`` (bilby/core/prior/interpolated.py:10-160):
+    linear interpolation of ``yy`` onto an evenly spaced grid of the same
+    length between ``minimum`` and ``maximum`` (the extent of ``xx`` unless
+    narrowed), normalised by the trapezoid rule; ``rescale`` is the linear
+    interpolation of the inverse of the cumulative trapezoid, whose last value
+    is set to exactly one."""
+
+    def __init__(self, xx, yy, minimum=np.nan, maximum=np.nan, **kwargs):
+        from scipy.interpolate import interp1d
+        xx = np.asarray(xx, dtype=np.float64)
+        yy = np.asarray(yy, dtype=np.float64)
+        self.min_limit, self.max_limit = float(np.min(xx)), float(np.max(xx))
+        minimum = float(np.nanmax(np.array((self.min_limit, minimum))))
+        maximum = float(np.nanmin(np.array((self.max_limit, maximum))))
+        super().__init__(minimum, maximum, **kwargs)
+        full = interp1d(x=xx, y=yy, bounds_error=False, fill_value=0)
+        self.xx = np.linspace(minimum, maximum, len(xx))
+        self.yy = full(self.xx)
+        self._tabulate()
+
+    def _tabulate(self):
+        from scipy.integrate import cumulative_trapezoid, trapezoid
+        from scipy.interpolate import interp1d
+        self.yy = self.yy / trapezoid(self.yy, self.xx)
+        self.YY = cumulative_trapezoid(self.yy, self.xx, initial=0)
+        self.YY[-1] = 1
+        self._pdf = interp1d(x=self.xx, y=self.yy, bounds_error=False, fill_value=0)
+        self._inverse_cdf = interp1d(x=self.YY, y=self.xx, bounds_error=True)
+
+    def prob(self, val):
+        return self._pdf(val)[()]
+
+    def rescale(self, val):
+        return self._inverse_cdf(val)[()]
+
+    def sample(self, size=None, *, random_state=None):
+        """One uniform draw per sample from the shared generator (or
+        ``random_state``), rescaled (bilby/core/prior/base.py:143-165)."""
+        from .random import resolve
+        rng = resolve(random_state)
+        if isinstance(size, (int, np.integer)):
+            size = (size,)
+        return self.rescale(rng.uniform(low=0, high=1, size=size))

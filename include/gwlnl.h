@@ -152,6 +152,16 @@ int gwl_eval_host(gwl_analysis *a, const double *params, int64_t B, int32_t prec
 int gwl_inner_products_device(gwl_analysis *a, const double *params, int64_t B, int32_t precision,
                               double *d_inner_h, double *h_inner_h, void *stream);
 
+/* The time series of <d|h> that time marginalisation sums over, for B points
+ * (device pointers, float64): series[b] is the length-L transform
+ * 4/T FFT(h conj(d) / S)[j], j < L = n_frequencies - 1, summed over
+ * detectors, interleaved complex ([B][2L] doubles), i.e. the
+ * d_inner_h_array of base.py:325-330; h_inner_h[b] = <h|h>.  Needs time
+ * marginalisation enabled and the full frequency grid (no relative binning,
+ * multi-banding or ROQ).  Asynchronous on `stream`. */
+int gwl_time_series_device(gwl_analysis *a, const double *params, int64_t B, double *series, double *h_inner_h,
+                           void *stream);
+
 /* Source polarisations {plus, cross} of one parameter point on a frequency
  * grid (host in, host out, float64): source.py:1153-1209 for the
  * sine-Gaussian; the TaylorF2 model for GWL_MODEL_TAYLORF2.  `params` is one

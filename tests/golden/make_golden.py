@@ -38,6 +38,13 @@ Outputs
 ``tests/golden/sky_frames.npz``
     The reference's ``get_sky_frame_parameters`` (base.py:1091-1137) for
     detector-pair frames and detector time references on random points.
+``tests/golden/tf2_marg_8s_2k_snrs.npz``
+    The reference's ``calculate_snrs`` per detector (<d|h>, <h|h>, matched-
+    filter SNR; with time marginalisation the d_inner_h_array inside the
+    prior window, its sum and power), ``compute_per_detector_log_likelihood``
+    without and with marginalisation, and the draws of
+    ``generate_posterior_sample_from_marginalized_likelihood`` with the
+    shared generator seeded per point.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -392,6 +399,89 @@ def run_frames(bilby, n=16):
     print("sky frames", len(FRAME_CASES), "cases")
 
 
+RECON_COMBOS = ["t", "d", "p", "tpd"]
+RECON_SEED = 4321
+
+
+def run_snrs(bilby, name="tf2_marg_8s_2k", n_points=3):
+    """The per-detector inner products (base.py:260-354), per-detector
+    likelihoods (base.py:479-499) and posterior reconstruction draws
+    (base.py:502-770) of the reference, on points of the marginalised
+    workload.  The time series d_inner_h_array is stored inside the
+    geocent_time prior window only, with its full-length sum and power."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 7)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    # plain likelihood: calculate_snrs and per-detector lnL
+    ifos, wfg = build_reference(bilby, w, taylorf2_aligned)
+    like = bilby.gw.likelihood.GravitationalWaveTransient(interferometers=ifos, waveform_generator=wfg)
+    names = [ifo.name for ifo in ifos]
+    dh = np.zeros((n_points, len(ifos)), complex)
+    hh = np.zeros((n_points, len(ifos)))
+    mf = np.zeros((n_points, len(ifos)), complex)
+    per_det = np.zeros((n_points, len(ifos)))
+    for i in range(n_points):
+        q = point(params, i)
+        q.pop("time_jitter")
+        pols = wfg.frequency_domain_strain(dict(q))
+        for k, ifo in enumerate(ifos):
+            s = like.calculate_snrs(pols, ifo, parameters=dict(q))
+            dh[i, k], hh[i, k], mf[i, k] = s.d_inner_h, s.optimal_snr_squared, s.complex_matched_filter_snr
+        res = like.compute_per_detector_log_likelihood(dict(q))
+        per_det[i] = [res[f"{n}_log_likelihood"] for n in names]
+    out.update(snr_dh=dh, snr_hh=hh, snr_mf=mf, per_det_lnl=per_det)
+    # marginalised likelihoods: per-detector lnL, the time series, reconstruction
+    for combo in RECON_COMBOS:
+        ifos, wfg = build_reference(bilby, w, taylorf2_aligned)
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, t, p, d)
+        like = bilby.gw.likelihood.GravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors,
+            time_marginalization=t, phase_marginalization=p, distance_marginalization=d)
+        per_det = np.zeros((n_points, len(ifos)))
+        draws = np.zeros((n_points, 3))
+        for i in range(n_points):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+            else:
+                q.pop("time_jitter")
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            res = like.compute_per_detector_log_likelihood(dict(q))
+            per_det[i] = [res[f"{n}_log_likelihood"] for n in names]
+            if combo == "t":
+                qq = dict(q)
+                qq["geocent_time"] += qq["time_jitter"]
+                pols = wfg.frequency_domain_strain(dict(qq))
+                win = None
+                for k, ifo in enumerate(ifos):
+                    s = like.calculate_snrs(pols, ifo, parameters=dict(qq))
+                    arr = s.d_inner_h_array
+                    times = like._times + qq["time_jitter"]
+                    tp = like.priors["geocent_time"]
+                    idx = np.nonzero((times >= tp.minimum) & (times <= tp.maximum))[0]
+                    if win is None:
+                        win = np.zeros((len(ifos), len(idx)), complex)
+                        out[f"series_idx_{i}"] = idx
+                    win[k] = arr[idx]
+                    out.setdefault("series_sum", np.zeros((n_points, len(ifos)), complex))[i, k] = arr.sum()
+                    out.setdefault("series_power", np.zeros((n_points, len(ifos))))[i, k] = np.sum(np.abs(arr) ** 2)
+                out[f"series_{i}"] = win
+            bilby.core.utils.random.seed(RECON_SEED + i)
+            sample = like.generate_posterior_sample_from_marginalized_likelihood(dict(q))
+            draws[i] = [sample["geocent_time"], sample["luminosity_distance"], sample["phase"]]
+        out["per_det_lnl_" + combo] = per_det
+        out["recon_" + combo] = draws
+        print(f"{name}[{combo}]: per-detector lnL and reconstruction draws done")
+    out["detectors"] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, f"{name}_snrs.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -416,8 +506,18 @@ def main():
     ap.add_argument("--frames-only", action="store_true")
     ap.add_argument("--priors-only", action="store_true")
     ap.add_argument("--roq-only", action="store_true")
+    ap.add_argument("--snrs-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.snrs_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_snrs(bilby)
+            finally:
+                os.chdir(cwd)
+        return
     if args.roq_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -466,6 +566,7 @@ def main():
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)
                 run_roq(bilby)
+                run_snrs(bilby)
             finally:
                 os.chdir(cwd)
 
