@@ -133,6 +133,15 @@ class Analysis:
             _capi.dptr(sm)), "gwl_set_relative_binning")
         self.relative_binning = True
 
+    def set_relative_binning_time_weights(self, weights):
+        """``weights`` [n_det, n_bins] complex: 4/T h0_d conj(d) / S on the full
+        grid, for relative binning with time marginalisation."""
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.complex128).view(np.float64))
+        if w.size != 2 * self.n_detectors * self.n_bins:
+            raise ValueError("time weights must have shape (n_detectors, n_bins)")
+        _capi.check(self._lib.gwl_set_relative_binning_time_weights(self._h, _capi.dptr(w)),
+                    "gwl_set_relative_binning_time_weights")
+
     def set_multiband(self, enable: bool, frequencies=None, linear=None, quadratic=None, band_start=None,
                       band_df=None):
         """Multi-banding: ``frequencies`` [K] banded frequencies, ``linear``

@@ -89,6 +89,10 @@ struct gwl_analysis {
   double* rb_freq = nullptr;
   double2* rb_h0inv[kMaxDet] = {};
   double* rb_sum[kMaxDet] = {};
+  std::vector<int64_t> h_rb_index;  // host copy of the edges
+  int rb_tm = 0;                    // time-marginalisation weights set for these bins
+  double2* rb_g[kMaxDet] = {};
+  int32_t* rb_bin = nullptr;
   // multi-banding
   int multiband = 0;
   int64_t mb_points = 0;
@@ -322,9 +326,11 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.rb_edges = a->rb_edges;
   L.rb_index = a->rb_index;
   L.rb_freq = a->rb_freq;
+  L.rb_bin = a->rb_bin;
   for (int d = 0; d < a->n_det; ++d) {
     L.rb_h0inv[d] = a->rb_h0inv[d];
     L.rb_sum[d] = a->rb_sum[d];
+    L.rb_g[d] = a->rb_g[d];
   }
   L.multiband = a->multiband;
   L.mb_points = a->mb_points;
@@ -404,6 +410,24 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
   L.tm_series = d_series;
+  if (a->relbin && a->time_marg && d_out) {
+    // relative binning with time marginalisation: the float64 time-marginalised
+    // kernel over the piecewise-linear full-grid waveform
+    if (!a->rb_tm) {
+      set_error("relative binning with time marginalisation needs gwl_set_relative_binning_time_weights");
+      return GWL_ERR_ARGUMENT;
+    }
+    L.precision = GWL_PRECISION_FP64;
+    L.rf_tol = 0.0;
+    GWL_CUDA(launch_prologue(L, s));
+    if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+    GWL_CUDA(launch_time_marginalized(L, s));
+    if (a->profiling) {
+      GWL_CUDA(cudaEventRecord(a->ev_end, s));
+      a->ev_pending = 1;
+    }
+    return GWL_OK;
+  }
   if (a->relbin || a->multiband || a->roq) {
     // relative binning / multi-banding / ROQ: per-point set-up, then one warp
     // per point over the bin edges, banded frequencies or nodes (no marking
@@ -984,8 +1008,8 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
-    if (a->relbin || a->multiband || a->roq) {
-      set_error("time marginalisation is not available with relative binning, multi-banding or ROQ");
+    if (a->multiband || a->roq) {
+      set_error("time marginalisation is not available with multi-banding or ROQ");
       return GWL_ERR_UNSUPPORTED;
     }
   }
@@ -1049,8 +1073,8 @@ int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const
     a->relbin = 0;
     return GWL_OK;
   }
-  if (a->time_marg || a->multiband || a->roq) {
-    set_error("relative binning excludes time marginalisation, multi-banding and ROQ");
+  if (a->multiband || a->roq) {
+    set_error("relative binning excludes multi-banding and ROQ");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_edges < 2 || !edge_index || !h0_inverse || !summary) {
@@ -1079,7 +1103,38 @@ int gwl_set_relative_binning(gwl_analysis* a, int enable, int32_t n_edges, const
     if ((rc = upload(a, &a->rb_sum[d], sm))) return rc;
   }
   a->rb_edges = n_edges;
+  a->h_rb_index = idx;
+  a->rb_tm = 0;  // new bins need new time-marginalisation weights
   a->relbin = 1;
+  return GWL_OK;
+}
+
+int gwl_set_relative_binning_time_weights(gwl_analysis* a, const double* weights) {
+  if (!a || !weights) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->relbin) {
+    set_error("set the relative-binning bins first (gwl_set_relative_binning)");
+    return GWL_ERR_ARGUMENT;
+  }
+  const std::vector<int64_t>& idx = a->h_rb_index;
+  const int64_t k0 = idx.front(), k1 = idx.back();
+  // bin b holds the grid indices [idx[b], idx[b + 1]); the last bin also idx.back()
+  std::vector<int32_t> bin((size_t)(k1 - k0 + 1));
+  for (size_t b = 0; b + 1 < idx.size(); ++b)
+    for (int64_t k = idx[b]; k < idx[b + 1]; ++k) bin[(size_t)(k - k0)] = (int32_t)b;
+  bin.back() = (int32_t)(idx.size() - 2);
+  int rc;
+  if ((rc = upload(a, &a->rb_bin, bin))) return rc;
+  for (int d = 0; d < a->n_det; ++d) {
+    std::vector<double2> w((size_t)a->n_bins);
+    for (int64_t k = 0; k < a->n_bins; ++k)
+      w[(size_t)k] = make_double2(weights[((size_t)d * a->n_bins + k) * 2], weights[((size_t)d * a->n_bins + k) * 2 + 1]);
+    if ((rc = upload(a, &a->rb_g[d], w))) return rc;
+  }
+  a->rb_tm = 1;
   return GWL_OK;
 }
 
@@ -1271,8 +1326,8 @@ int gwl_time_series_device(gwl_analysis* a, const double* params, int64_t B, dou
     set_error("gwl_time_series_device needs time marginalisation enabled");
     return GWL_ERR_ARGUMENT;
   }
-  if (a->relbin || a->multiband || a->roq) {
-    set_error("gwl_time_series_device serves the full frequency grid only");
+  if (a->multiband || a->roq) {
+    set_error("gwl_time_series_device serves the full frequency grid and relative binning only");
     return GWL_ERR_ARGUMENT;
   }
   if (B <= 0) return GWL_OK;

@@ -137,6 +137,11 @@ struct LaunchArgs {
   const double* rb_freq;                // [rb_edges] edge frequencies
   const double2* rb_h0inv[kMaxDet];     // [rb_edges] 1 / h0_d(f_e)
   const double* rb_sum[kMaxDet];        // [rb_edges - 1][6]: a0 re, a0 im, a1 re, a1 im, b0, b1
+  // relative binning with time marginalisation: the full-grid weights
+  // 4/T h0_d(f) conj(d(f)) / S(f) and the bin of each grid index in
+  // [rb_index[0], rb_index[rb_edges - 1]]
+  const double2* rb_g[kMaxDet];         // [n_bins]
+  const int32_t* rb_bin;                // [rb_index[last] - rb_index[0] + 1]
   // multi-banding: the model at the banded frequencies, weighted by the
   // per-detector linear (complex) and quadratic (real) coefficients
   int multiband;

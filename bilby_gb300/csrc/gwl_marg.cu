@@ -334,6 +334,67 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
           hh_part += norm * a.v_scale[d] * (A * A * hh1[d] + Cx * Cx * hh2[d]);
         }
       }
+    } else if (a.relbin) {
+      // relative binning (relative.py:365-396, 398-420): the ratios
+      // h_d(f_e) / h0_d(f_e) at the bin edges in shared memory, <h|h> from the
+      // summary data, and the integrand from the full-grid waveform
+      // h0_d(f) (r0_b + r1_b (f - f_b)) of each bin b
+      double2* s_rat = reinterpret_cast<double2*>(smem);  // [D][nE]
+      const int nE = a.rb_edges, nB = nE - 1;
+      const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+      const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+      const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+      for (int e = threadIdx.x; e < nE; e += blockDim.x) {
+        const double f = a.rb_freq[e];
+        double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+        const bool on = r.valid && (tf2 ? tf2_pols_tab(a, r, a.rb_index[e], f, u, lnu, pu5, hp, hx)
+                                        : plain_pols(a, r, f, hp, hx));
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double2 q = make_double2(0.0, 0.0);
+          if (on) {
+            // interferometer.py:341-362 at explicit frequencies (no mask)
+            const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+            double sn, cs;
+            sincos(2.0 * kPi * r.dt[d] * f, &sn, &cs);
+            const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+            const double2 g = a.rb_h0inv[d][e];
+            q = make_double2(hre * g.x - him * g.y, hre * g.y + him * g.x);
+          }
+          s_rat[d * nE + e] = q;
+        }
+      }
+      __syncthreads();
+      for (int b = threadIdx.x; b < nB; b += blockDim.x) {
+        const double width = a.rb_freq[b + 1] - a.rb_freq[b];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double2 q0 = s_rat[d * nE + b], q1 = s_rat[d * nE + b + 1];
+          const double r0r = (q1.x + q0.x) / 2, r0i = (q1.y + q0.y) / 2;
+          const double r1r = (q1.x - q0.x) / width, r1i = (q1.y - q0.y) / width;
+          const double* sd = a.rb_sum[d] + (size_t)b * 6;
+          hh_part += sd[4] * (r0r * r0r + r0i * r0i) + 2.0 * sd[5] * (r0r * r1r + r0i * r1i);
+        }
+      }
+      const int64_t k0 = a.rb_index[0], k1 = a.rb_index[nE - 1];
+      for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
+        double zr = 0.0, zi = 0.0;
+        if (r.valid && k >= k0 && k <= k1) {
+          const int b = a.rb_bin[k - k0];
+          const double fb0 = a.rb_freq[b], fb1 = a.rb_freq[b + 1];
+          const double x = a.freq[k] - (fb1 + fb0) / 2, width = fb1 - fb0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const double2 q0 = s_rat[d * nE + b], q1 = s_rat[d * nE + b + 1];
+            const double rr = (q1.x + q0.x) / 2 + (q1.x - q0.x) / width * x;
+            const double ri = (q1.y + q0.y) / 2 + (q1.y - q0.y) / width * x;
+            const double2 g = a.rb_g[d][k];  // 4/T h0 conj(d) / S
+            zr += g.x * rr - g.y * ri;
+            zi += g.x * ri + g.y * rr;
+          }
+        }
+        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(zr, zi);
+      }
     } else {
       // e^{i w f_k} for this thread's bins k = tid, tid + T, ... by rotation
       double zc[D], zs[D], rc[D], rs[D];
@@ -374,7 +435,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       hh_part *= norm;
     }
     // The last bin (index L) only enters <h|h>; the FFT uses bins 0..L-1.
-    if (!MIXED && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
+    if (!MIXED && !a.relbin && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
       double2 hp, hx;
       const double f = a.freq[L];
       if (plain_pols(a, r, f, hp, hx)) {
@@ -745,8 +806,15 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
     const unsigned grid = (unsigned)a.B;
     k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d32, log2L);
   } else {
+    // relative binning: the edge ratios in shared memory
+    const size_t smem = a.relbin ? (size_t)a.rb_edges * D * sizeof(double2) : 0;
+    if (smem > 48 * 1024) {
+      cudaError_t e =
+          cudaFuncSetAttribute(k_time_marg<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
     const unsigned grid = (unsigned)std::min<int64_t>(a.B, tm_grid_fp64());
-    k_time_marg<D, false><<<grid, kTmThreads, 0, s>>>(a, g_twiddle.d64, log2L);
+    k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d64, log2L);
   }
   return cudaGetLastError();
 }
@@ -754,6 +822,8 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
   const int log2L = log2_exact(a.n_fft);
   if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
+  if (a.precision != GWL_PRECISION_MIXED && a.relbin && (size_t)a.rb_edges * a.n_det * sizeof(double2) > 200 * 1024)
+    return cudaErrorInvalidValue;  // the host checks the edge count first
   if (a.precision == GWL_PRECISION_MIXED &&
       ((size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) + (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0) >
            200 * 1024 ||

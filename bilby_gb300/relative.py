@@ -10,8 +10,11 @@ runs on the GPU: one warp per parameter point evaluates the model at the bin
 edges, forms the ratio to the fiducial response and sums the summary data
 (``k_relbin``, behind ``gwl_set_relative_binning`` in include/gwlnl.h).
 
-Time marginalisation, which the reference supports by rebuilding the full
-waveform for an FFT, has no GPU kernel here and raises NotImplementedError.
+With time marginalisation (relative.py:380-420) the float64
+time-marginalised kernel rebuilds the piecewise-linear full-grid waveform
+from the edge ratios, transforms it against the data and marginalises over
+time with <h|h> from the summary data
+(``gwl_set_relative_binning_time_weights``).
 """
 from __future__ import annotations
 
@@ -36,10 +39,10 @@ class RelativeBinningGravitationalWaveTransient(GravitationalWaveTransient):
                  time_marginalization=False, phase_marginalization=False, priors=None,
                  distance_marginalization_lookup_table=None, jitter_time=True, reference_frame="sky",
                  time_reference="geocenter", chi=1, epsilon=0.5, precision="fp64"):
-        if time_marginalization:
-            raise NotImplementedError("time marginalisation with relative binning has no GPU kernel")
         self._rb = None
+        self._rb_time_weights = None
         super().__init__(interferometers, waveform_generator, distance_marginalization=distance_marginalization,
+                         time_marginalization=time_marginalization,
                          phase_marginalization=phase_marginalization, priors=priors,
                          distance_marginalization_lookup_table=distance_marginalization_lookup_table,
                          jitter_time=jitter_time, reference_frame=reference_frame, time_reference=time_reference,
@@ -49,6 +52,8 @@ class RelativeBinningGravitationalWaveTransient(GravitationalWaveTransient):
             fiducial_parameters = priors.sample()
         self.fiducial_parameters = dict(fiducial_parameters)
         self._unset_fiducial()
+        if self.time_marginalization:  # relative.py:139-140
+            self.fiducial_parameters["geocent_time"] = self._start_time
         if self.distance_marginalization:
             self.fiducial_parameters["luminosity_distance"] = self._ref_dist
         if self.phase_marginalization:
@@ -190,12 +195,39 @@ class RelativeBinningGravitationalWaveTransient(GravitationalWaveTransient):
         sm = np.stack([np.stack([a0.real, a0.imag, a1.real, a1.imag, b0.real, b1.real], axis=-1)
                        for a0, a1, b0, b1 in (self.summary_data[ifo.name] for ifo in self.interferometers)])
         self._rb = (np.asarray(self.bin_inds, dtype=np.int64), inv, sm)
-        self.analysis.set_relative_binning(True, *self._rb)
+        self._rb_time_weights = self._time_weights() if self.time_marginalization else None
+        self._set_bins(self.analysis)
+
+    def _time_weights(self):
+        """4/T h0_d conj(d) / S on the full grid, zero outside the mask and
+        outside the first and last bin edges (relative.py:380-420 before the
+        per-point ratio)."""
+        out = []
+        k0, k1 = int(self.bin_inds[0]), int(self.bin_inds[-1])
+        for ifo in self.interferometers:
+            mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool).copy()
+            mask[:k0] = False
+            mask[k1 + 1:] = False
+            w = np.zeros(len(mask), dtype=np.complex128)
+            h0 = np.asarray(self.per_detector_fiducial_waveforms[ifo.name])
+            d = np.asarray(ifo.strain_data.frequency_domain_strain)
+            psd = np.asarray(ifo.power_spectral_density_array)
+            w[mask] = 4 / ifo.strain_data.duration * h0[mask] * np.conj(d[mask]) / psd[mask]
+            out.append(w)
+        return np.stack(out)
+
+    def _set_bins(self, an):
+        an.set_relative_binning(True, *self._rb)
+        if self._rb_time_weights is not None:
+            an.set_relative_binning_time_weights(self._rb_time_weights)
 
     def _build_analysis(self):
         super()._build_analysis()
         if getattr(self, "_rb", None) is not None:
-            self._analysis.set_relative_binning(True, *self._rb)
+            self._set_bins(self._analysis)
+
+    def _detector_analysis(self, interferometer):
+        raise NotImplementedError("per-detector quantities of the relative-binning likelihood are not built")
 
     # ------------------------------------------------------------------
     # fiducial optimisation (relative.py:256-317)

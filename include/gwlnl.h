@@ -263,9 +263,19 @@ int gwl_profile_last_kernel_ms(gwl_analysis *a, float *ms);
  * h0_inverse ([n_det][n_edges][2]: 1 / h0_d(f_e), re/im) and sums the per-bin
  * summary data ([n_det][n_edges - 1][6]: a0 re, a0 im, a1 re, a1 im, b0, b1)
  * in float64 for either precision.  Phase and distance marginalisation
- * apply; time marginalisation is refused (GWL_ERR_UNSUPPORTED). */
+ * apply; time marginalisation needs gwl_set_relative_binning_time_weights
+ * as well (after each call of this function). */
 int gwl_set_relative_binning(gwl_analysis *a, int enable, int32_t n_edges, const int64_t *edge_index,
                              const double *h0_inverse, const double *summary);
+
+/* Relative binning with time marginalisation (relative.py:380-420): the
+ * full-grid weights weights[d][k] = 4/T h0_d(f_k) conj(d_d(f_k)) / S_d(f_k)
+ * ([n_det][n_bins][2], re/im; zero outside the frequency mask and outside
+ * the first and last bin edges).  Each evaluation then rebuilds the
+ * piecewise-linear waveform h0_d(f) (r0_b + r1_b (f - f_b)) on the grid,
+ * transforms it against the data (float64, FFT length n_bins - 1) and
+ * marginalises over time with <h|h> from the summary data. */
+int gwl_set_relative_binning_time_weights(gwl_analysis *a, const double *weights);
 
 /* Multi-banding (replaces MBGravitationalWaveTransient.calculate_snrs with
  * linear interpolation of <h|h>, bilby/gw/likelihood/multiband.py:741-819;

@@ -48,7 +48,8 @@ Outputs
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
-    without marginalisation, with phase and with distance marginalisation.
+    without marginalisation, with phase, with distance, with time, and with
+    time, phase and distance marginalisation.
 """
 from __future__ import annotations
 
@@ -176,6 +177,7 @@ def run_marginalised(bilby, name, n_points):
 
 
 RELBIN_COMBOS = ["none", "p", "d"]
+RELBIN_TIME_COMBOS = ["t", "tpd"]
 
 
 def run_relbin(bilby, name, n_fixed, n_random):
@@ -185,22 +187,32 @@ def run_relbin(bilby, name, n_fixed, n_random):
     pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
     params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
     n = n_fixed + n_random
+    # drawn after the points, so that the points do not depend on it
+    jitter = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
     out = {"p_" + k: v for k, v in params.items()}
-    for combo in RELBIN_COMBOS:
+    out["time_jitter"] = jitter
+    for combo in RELBIN_COMBOS + RELBIN_TIME_COMBOS:
         ifos, _ = build_reference(bilby, w, taylorf2_aligned)
         wfg = bilby.gw.waveform_generator.WaveformGenerator(
             duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
             frequency_domain_source_model=taylorf2_aligned_relative_binning,
             waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
-        p, d = "p" in combo, "d" in combo
-        priors = make_priors(bilby, w, False, p, d)
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, t, p, d)
+        # with time marginalisation and jitter the reference's constructor
+        # evaluates the fiducial point, which then needs a time_jitter entry
+        fiducial = dict(w.injection, time_jitter=0.0) if t else dict(w.injection)
         like = bilby.gw.likelihood.RelativeBinningGravitationalWaveTransient(
-            interferometers=ifos, waveform_generator=wfg, fiducial_parameters=dict(w.injection),
-            priors=priors if (p or d) else None, phase_marginalization=p, distance_marginalization=d)
+            interferometers=ifos, waveform_generator=wfg, fiducial_parameters=fiducial,
+            priors=priors if (t or p or d) else None, time_marginalization=t, phase_marginalization=p,
+            distance_marginalization=d)
         t0 = time.perf_counter()
         vals = []
         for i in range(n):
             q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+                q["time_jitter"] = float(jitter[i])
             if p:
                 q["phase"] = 0.0
             if d:

@@ -2,9 +2,9 @@
 RelativeBinningGravitationalWaveTransient (tests/golden/tf2_128s_relbin.npz,
 written by the reference with the oracle's TaylorF2 as its source model):
 the same bins and summary data, and lnL ratios without marginalisation, with
-phase and with distance marginalisation.  Also: the relative-binning lnL
-agrees with the full likelihood near the fiducial point, batch equals single,
-and time marginalisation is refused.
+phase, with distance, with time, and with time, phase and distance
+marginalisation.  Also: the relative-binning lnL agrees with the full
+likelihood near the fiducial point, and batch equals single.
 
 Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
 table, as for the full likelihood)."""
@@ -17,7 +17,7 @@ from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, point
 pytestmark = pytest.mark.gpu
 
 
-def make(combo, tmp_path, time_marginalization=False):
+def make(combo, tmp_path):
     from bilby_gb300 import random as grandom
     from bilby_gb300.detector import InterferometerList
     from bilby_gb300.prior import PowerLaw, Uniform
@@ -33,6 +33,9 @@ def make(combo, tmp_path, time_marginalization=False):
                             waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
     ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
     priors = {}
+    if "t" in combo:
+        tc = w.injection["geocent_time"]
+        priors["geocent_time"] = Uniform(tc - 0.1, tc + 0.1)
     if "p" in combo:
         priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
     if "d" in combo:
@@ -42,7 +45,7 @@ def make(combo, tmp_path, time_marginalization=False):
         ifos, wfg, fiducial_parameters=dict(w.injection), priors=priors or None,
         phase_marginalization="p" in combo, distance_marginalization="d" in combo,
         distance_marginalization_lookup_table=str(tmp_path / "table.npz"),
-        time_marginalization=time_marginalization)
+        time_marginalization="t" in combo)
     return w, ifos, wfg, like, priors
 
 
@@ -62,7 +65,7 @@ def test_bins_and_summary_match_the_reference(plain):
         assert np.max(np.abs(ours - ref)) <= 1e-11 * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("combo", ["none", "p", "d"])
+@pytest.mark.parametrize("combo", ["none", "p", "d", "t", "tpd"])
 def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     w, ifos, wfg, like, priors = make(combo, tmp_path)
     z = golden("tf2_128s_relbin")
@@ -70,6 +73,9 @@ def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     pts = []
     for i in range(len(params["mass_1"])):
         q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = float(z["time_jitter"][i])
         if "p" in combo:
             q["phase"] = 0.0
         if "d" in combo:
@@ -113,7 +119,3 @@ def test_close_to_the_full_likelihood_near_the_fiducial(plain):
     assert e[1e-5] < 0.05, e
     assert e[1e-5] < e[1e-4] / 5, e
 
-
-def test_time_marginalisation_is_refused(gpu, tmp_path):
-    with pytest.raises(NotImplementedError):
-        make("t", tmp_path, time_marginalization=True)
