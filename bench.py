@@ -277,10 +277,42 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
         e1.record(stream)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
-    return {"workload": name, "bins": int(like.number_of_bins), "batch": batch,
-            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
-            "precision": "fp64", "setup_s": setup_s,
-            "launch": "prologue + one warp per point over the bin edges"}
+    res = {"workload": name, "bins": int(like.number_of_bins), "batch": batch,
+           "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+           "precision": "fp64", "setup_s": setup_s,
+           "launch": "prologue + one warp per point over the bin edges"}
+    # with time marginalisation (relative.py:380-420): the float64 FFT of
+    # length n_bins - 1 over the rebuilt piecewise-linear waveform, per point
+    from bilby_gb300.prior import Uniform
+    tc = w.injection["geocent_time"]
+    priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1)}
+    like_t = RelativeBinningGravitationalWaveTransient(base.interferometers, base.waveform_generator,
+                                                       fiducial_parameters=dict(w.injection), priors=priors,
+                                                       time_marginalization=True)
+    an_t = like_t.analysis
+    bt = 2048
+    p = draw_points(w, bt, rng)
+    p["geocent_time"] = np.full(bt, float(priors["geocent_time"]))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, bt)
+    block = torch.from_numpy(params_block(p)).cuda()
+    out_t = torch.empty(bt, dtype=torch.float64, device="cuda")
+    for s in range(warmup):
+        an_t.log_likelihood_ratio_device(block.data_ptr(), bt, out_t.data_ptr(), "fp64", stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms_t = []
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        an_t.log_likelihood_ratio_device(block.data_ptr(), bt, out_t.data_ptr(), "fp64", stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms_t.append(e0.elapsed_time(e1))
+    res["time_marginalized"] = {"batch": bt, "fft_length": int(an_t.n_bins - 1),
+                                "value": bt * steps / (sum(ms_t) / 1e3), "unit": "evals/s",
+                                "ms_per_launch": float(np.mean(ms_t)), "precision": "fp64",
+                                "finite": bool(torch.isfinite(out_t).all().item())}
+    return res
 
 
 def bench_multiband(name, steps, warmup, batch=16384, seed=37):

@@ -142,6 +142,20 @@ class Analysis:
         _capi.check(self._lib.gwl_set_relative_binning_time_weights(self._h, _capi.dptr(w)),
                     "gwl_set_relative_binning_time_weights")
 
+    def set_multiband_time_marginalization(self, n_fft: int, index_start, source, delta_tc: float,
+                                           antenna_time: float):
+        """Multi-banding with time marginalisation: for each full-resolution
+        index k < n_fft, ``source[index_start[k]:index_start[k + 1]]`` are the
+        banded points scattered there (a negative code -j - 1: point j, in
+        <h|h> only)."""
+        ptr = np.ascontiguousarray(index_start, dtype=np.int32)
+        src = np.ascontiguousarray(source, dtype=np.int32)
+        if len(ptr) != n_fft + 1:
+            raise ValueError("index_start must have n_fft + 1 entries")
+        _capi.check(self._lib.gwl_set_multiband_time_marginalization(
+            self._h, int(n_fft), ptr.ctypes.data_as(ctypes.c_void_p), src.ctypes.data_as(ctypes.c_void_p),
+            float(delta_tc), float(antenna_time)), "gwl_set_multiband_time_marginalization")
+
     def set_multiband(self, enable: bool, frequencies=None, linear=None, quadratic=None, band_start=None,
                       band_df=None):
         """Multi-banding: ``frequencies`` [K] banded frequencies, ``linear``

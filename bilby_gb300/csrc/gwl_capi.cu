@@ -107,6 +107,11 @@ struct gwl_analysis {
   float2* mb_lw[kMaxDet] = {};
   double mb_lw_scale[kMaxDet] = {};
   double* mb_qprefix[kMaxDet] = {};
+  int mb_tm = 0;  // multi-banding time-marginalisation tables set for these bands
+  int64_t mb_tm_n = 0;
+  double mb_tm_delta_tc = 0.0, mb_tm_antenna_time = 0.0;
+  int32_t* mb_tm_ptr = nullptr;
+  int32_t* mb_tm_src = nullptr;
   // reduced-order quadrature
   int roq = 0;
   int roq_nl = 0, roq_nq = 0;
@@ -308,6 +313,19 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.delta_tc = 2.0 / a->fs;
   L.start_time0 = a->start0;
   L.n_fft = a->n_bins - 1;
+  L.tm_first = 1;
+  if (a->multiband && a->mb_tm) {
+    // multiband.py:714-726: FFT length Nbs[-1] / 2, times start + j delta_tc,
+    // antenna patterns at the prior's mid time
+    L.n_fft = a->mb_tm_n;
+    L.delta_tc = a->mb_tm_delta_tc;
+    L.tm_first = 0;
+    L.antenna_fixed = 1;
+    L.antenna_time = a->mb_tm_antenna_time;
+    L.mb_tm = 1;
+    L.mb_tm_ptr = a->mb_tm_ptr;
+    L.mb_tm_src = a->mb_tm_src;
+  }
   L.tx = a->tx;
   L.ty = a->ty;
   L.tc = a->tc;
@@ -410,11 +428,15 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
   L.tm_series = d_series;
-  if (a->relbin && a->time_marg && d_out) {
-    // relative binning with time marginalisation: the float64 time-marginalised
-    // kernel over the piecewise-linear full-grid waveform
-    if (!a->rb_tm) {
+  if ((a->relbin || a->multiband) && a->time_marg && d_out) {
+    // relative binning / multi-banding with time marginalisation: the float64
+    // time-marginalised kernel over the rebuilt full-resolution integrand
+    if (a->relbin && !a->rb_tm) {
       set_error("relative binning with time marginalisation needs gwl_set_relative_binning_time_weights");
+      return GWL_ERR_ARGUMENT;
+    }
+    if (a->multiband && !a->mb_tm) {
+      set_error("multi-banding with time marginalisation needs gwl_set_multiband_time_marginalization");
       return GWL_ERR_ARGUMENT;
     }
     L.precision = GWL_PRECISION_FP64;
@@ -1008,8 +1030,8 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
-    if (a->multiband || a->roq) {
-      set_error("time marginalisation is not available with multi-banding or ROQ");
+    if (a->roq) {
+      set_error("time marginalisation is not available with ROQ");
       return GWL_ERR_UNSUPPORTED;
     }
   }
@@ -1150,8 +1172,8 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
     a->multiband = 0;
     return GWL_OK;
   }
-  if (a->time_marg || a->relbin || a->roq) {
-    set_error("multi-banding excludes time marginalisation, relative binning and ROQ");
+  if (a->relbin || a->roq) {
+    set_error("multi-banding excludes relative binning and ROQ");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_points < 1 || !frequencies || !linear || !quadratic || n_bands < 1 || !band_start || !band_df) {
@@ -1230,7 +1252,57 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   if ((rc = upload(a, &a->mb_band_df, bd))) return rc;
   a->mb_bands = n_bands;
   a->mb_points = n_points;
+  a->mb_tm = 0;  // new bands need new time-marginalisation tables
   a->multiband = 1;
+  return GWL_OK;
+}
+
+int gwl_set_multiband_time_marginalization(gwl_analysis* a, int64_t n_fft, const int32_t* index_start,
+                                           const int32_t* source, double delta_tc, double antenna_time) {
+  if (!a || !index_start || !source) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->multiband) {
+    set_error("set the bands first (gwl_set_multiband)");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (n_fft < 2 || (n_fft & (n_fft - 1)) != 0 || n_fft > ((int64_t)1 << 26)) {
+    set_error("the multi-banding FFT length must be a power of two");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (!(delta_tc > 0) || !std::isfinite(antenna_time)) {
+    set_error("delta_tc must be positive and the antenna time finite");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<int32_t> ptr(index_start, index_start + n_fft + 1);
+  if (ptr[0] != 0 || ptr[(size_t)n_fft] != (int32_t)a->mb_points) {
+    set_error("index_start must run from 0 to the number of banded points");
+    return GWL_ERR_ARGUMENT;
+  }
+  for (int64_t k = 0; k < n_fft; ++k)
+    if (ptr[(size_t)k + 1] < ptr[(size_t)k]) {
+      set_error("index_start must be non-decreasing");
+      return GWL_ERR_ARGUMENT;
+    }
+  std::vector<int32_t> src(source, source + a->mb_points);
+  std::vector<char> seen((size_t)a->mb_points, 0);
+  for (int32_t c : src) {
+    const int64_t j = c >= 0 ? c : -(int64_t)c - 1;
+    if (j >= a->mb_points || seen[(size_t)j]) {
+      set_error("source must list every banded point exactly once");
+      return GWL_ERR_ARGUMENT;
+    }
+    seen[(size_t)j] = 1;
+  }
+  int rc;
+  if ((rc = upload(a, &a->mb_tm_ptr, ptr))) return rc;
+  if ((rc = upload(a, &a->mb_tm_src, src))) return rc;
+  a->mb_tm_n = n_fft;
+  a->mb_tm_delta_tc = delta_tc;
+  a->mb_tm_antenna_time = antenna_time;
+  a->mb_tm = 1;
   return GWL_OK;
 }
 

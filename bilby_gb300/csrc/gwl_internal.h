@@ -129,6 +129,9 @@ struct LaunchArgs {
   double ref_dist;
   double* tm_work;                      // time-marginalisation work space
   double* tm_series;                    // optional [B][2 n_fft] FFT of the integrand (float64 kernel)
+  int tm_first;                         // time of FFT index j: start + (j + tm_first) * duration / n_fft
+  int antenna_fixed;                    // antenna patterns at antenna_time instead of geocent_time
+  double antenna_time;
   // relative binning: the model at the bin edges, its ratio to the fiducial
   // response, and the per-bin summary data of each detector
   int relbin;
@@ -160,6 +163,13 @@ struct LaunchArgs {
   const float2* mb_lw[kMaxDet];         // [mb_points]
   double mb_lw_scale[kMaxDet];
   const double* mb_qprefix[kMaxDet];    // [mb_points + 1]
+  // multi-banding with time marginalisation: for each full-resolution index
+  // k < n_fft the banded points scattered there, mb_tm_src[mb_tm_ptr[k] ..
+  // mb_tm_ptr[k + 1]); a code c >= 0 is banded point c, c < 0 is banded point
+  // -c - 1 counted in <h|h> only (replaced at its index within its band)
+  int mb_tm;
+  const int32_t* mb_tm_ptr;             // [n_fft + 1]
+  const int32_t* mb_tm_src;             // [mb_points]
   // reduced-order quadrature: the model at the linear and quadratic nodes,
   // time-dependent linear weights on the grid (t_start + k) dt, k < n_time
   int roq;

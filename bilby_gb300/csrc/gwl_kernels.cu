@@ -49,9 +49,17 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
   const double gmst = pymod(gmst_radians(tgeo), kTwoPi);
   bool ok = isfinite(ra) && isfinite(dec) && isfinite(psi) && isfinite(tgeo);
   const SkyTrig sky = sky_trig(ra, dec, psi, gmst);
+  // an interferometer reference time (multiband.py:724-725, interferometer.py:333-336)
+  // fixes the time of the antenna patterns; the delay stays at geocent_time
+  const SkyTrig sky_ant =
+      a.antenna_fixed ? sky_trig(ra, dec, psi, pymod(gmst_radians(a.antenna_time), kTwoPi)) : sky;
   for (int d = 0; d < a.n_det; ++d) {
     double fp, fx, delay;
     antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky, &fp, &fx, &delay);
+    if (a.antenna_fixed) {
+      double unused;
+      antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky_ant, &fp, &fx, &unused);
+    }
     r.fp[d] = fp;
     r.fx[d] = fx;
     // interferometer.py:355-358: subtract the two GPS times first, then add the delay.

@@ -72,12 +72,11 @@ __device__ __forceinline__ bool plain_pols(const LaunchArgs& a, const PointRec& 
   return true;
 }
 
-// The same TaylorF2 polarisations from the per-bin power table f^(1/3),
-// ln(f) / 3, f^(-5/3), f^(-7/6); u = (pi M)^(1/3), pu5 = 3 / (128 eta u^5).
-__device__ __forceinline__ bool tf2_pols_tab(const LaunchArgs& a, const PointRec& r, int64_t k, double f, double u,
-                                             double lnu, double pu5, double2& hp, double2& hx) {
+// The same TaylorF2 polarisations from a power-table entry t = {f^(1/3),
+// ln(f) / 3, f^(-5/3), f^(-7/6)}; u = (pi M)^(1/3), pu5 = 3 / (128 eta u^5).
+__device__ __forceinline__ bool tf2_pols_t(const LaunchArgs& a, const PointRec& r, const double4& t, double f,
+                                           double u, double lnu, double pu5, double2& hp, double2& hx) {
   if (f < a.fmin || f >= r.f_isco) return false;
-  const double4 t = a.ftab[k];
   const double v = u * t.x, lnv = lnu + t.y;
   double s = r.a[7];
 #pragma unroll
@@ -92,6 +91,13 @@ __device__ __forceinline__ bool tf2_pols_tab(const LaunchArgs& a, const PointRec
   hp = make_double2(pf * ere, pf * eim);
   hx = make_double2(ci * eim, -ci * ere);
   return true;
+}
+
+// ... at grid bin k of the per-bin power table
+__device__ __forceinline__ bool tf2_pols_tab(const LaunchArgs& a, const PointRec& r, int64_t k, double f, double u,
+                                             double lnu, double pu5, double2& hp, double2& hx) {
+  if (f < a.fmin || f >= r.f_isco) return false;
+  return tf2_pols_t(a, r, a.ftab[k], f, u, lnu, pu5, hp, hx);
 }
 
 // (c + i s) *= (rc + i rs)
@@ -395,6 +401,41 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         }
         buf[bit_reverse((uint32_t)k, log2L)] = make_double2(zr, zi);
       }
+    } else if (a.mb_tm) {
+      // multi-banding (multiband.py:714-726, 792-800): the banded strain
+      // times the linear coefficients, scattered to the full-resolution
+      // indices int(f_j T) in band order, then the FFT; <h|h> from the
+      // quadratic coefficients over every banded point
+      const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+      const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+      const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+      for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
+        double zr = 0.0, zi = 0.0;
+        const int32_t c1 = a.mb_tm_ptr[k + 1];
+        for (int32_t c = a.mb_tm_ptr[k]; r.valid && c < c1; ++c) {
+          const int32_t code = a.mb_tm_src[c];
+          const int64_t j = code >= 0 ? (int64_t)code : -(int64_t)code - 1;
+          const double f = a.mb_freq[j];
+          double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+          if (!(tf2 ? tf2_pols_t(a, r, a.mb_pow[j], f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx)))
+            continue;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            // interferometer.py:341-362 at explicit frequencies (no mask)
+            const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+            double sn, cs;
+            sincos(2.0 * kPi * r.dt[d] * f, &sn, &cs);
+            const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+            hh_part += (hre * hre + him * him) * a.mb_quad[d][j];
+            if (code >= 0) {
+              const double2 w = a.mb_lin[d][j];
+              zr += hre * w.x - him * w.y;
+              zi += hre * w.y + him * w.x;
+            }
+          }
+        }
+        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(zr, zi);
+      }
     } else {
       // e^{i w f_k} for this thread's bins k = tid, tid + T, ... by rotation
       double zc[D], zs[D], rc[D], rs[D];
@@ -435,7 +476,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       hh_part *= norm;
     }
     // The last bin (index L) only enters <h|h>; the FFT uses bins 0..L-1.
-    if (!MIXED && !a.relbin && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
+    if (!MIXED && !a.relbin && !a.mb_tm && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
       double2 hp, hx;
       const double f = a.freq[L];
       if (plain_pols(a, r, f, hp, hx)) {
@@ -641,7 +682,9 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
     double m = -INFINITY, acc = 0.0;
     for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
-      const double lin = (j + 1 == L) ? a.duration : (double)(j + 1) * step;
+      // base.py:1027-1035 (linspace(0, T, L + 1)[1:], the last sample exactly T), or
+      // multiband.py:714-717 (arange(L) * delta_tc)
+      const double lin = a.tm_first ? ((j + 1 == L) ? a.duration : (double)(j + 1) * step) : (double)j * step;
       const double t = (a.start_time0 + lin) + jit;
       if (!(t >= a.t_min && t <= a.t_max)) continue;
       const C x = buf[P(j)];

@@ -11,9 +11,14 @@ warp per parameter point evaluates the model at the banded frequencies and
 contracts it with the coefficients (``k_multiband``, behind
 ``gwl_set_multiband`` in include/gwlnl.h).
 
-Not built: the IFFT-FFT evaluation of <h|h> (``linear_interpolation=False``)
-and time marginalisation, which raise NotImplementedError; weights files
-need h5py, as in the reference.
+With time marginalisation (multiband.py:714-726, 792-800) the float64
+time-marginalised kernel scatters the banded strain times the linear
+coefficients to the full-resolution grid, transforms it and marginalises
+over time (``gwl_set_multiband_time_marginalization``).
+
+Not built: the IFFT-FFT evaluation of <h|h> (``linear_interpolation=False``),
+which raises NotImplementedError; weights files need h5py, as in the
+reference.
 """
 from __future__ import annotations
 
@@ -53,13 +58,13 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
                  distance_marginalization=False, phase_marginalization=False, priors=None,
                  time_marginalization=False, jitter_time=True, distance_marginalization_lookup_table=None,
                  reference_frame="sky", time_reference="geocenter", precision="fp64"):
-        if time_marginalization:
-            raise NotImplementedError("time marginalisation with multi-banding has no GPU kernel")
         if not linear_interpolation:
             raise NotImplementedError("the IFFT-FFT evaluation of <h|h> has no GPU kernel; "
                                       "use linear_interpolation=True")
         self._mb = None
+        self._mb_tm = None
         super().__init__(interferometers, waveform_generator, priors=priors,
+                         time_marginalization=time_marginalization,
                          distance_marginalization=distance_marginalization,
                          phase_marginalization=phase_marginalization,
                          distance_marginalization_lookup_table=distance_marginalization_lookup_table,
@@ -82,6 +87,8 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
                 with h5py.File(weights, "r") as f:
                     weights = recursively_load_dict_contents_from_group(f, "/")
             self.setup_multibanding_from_weights(weights)
+        if self.time_marginalization:
+            self._setup_time_marginalization_multiband()
         self._upload()
 
     # ------------------------------------------------------------------
@@ -421,6 +428,41 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
             else:
                 setattr(self, key, value)
 
+    def _setup_time_marginalization_multiband(self):
+        """multiband.py:714-726: an FFT of length Nbs[-1] / 2 on the time
+        grid start + j T / N, the banded points' full-resolution indices, and
+        the antenna patterns fixed at the middle of the geocent_time prior
+        (set on the interferometers, as the reference does)."""
+        n = int(self.Nbs[-1]) // 2
+        self._delta_tc = self.durations[0] / n
+        self._times = self._ifo_start_time + np.arange(n) * self._delta_tc
+        self.time_prior_array = self.priors["geocent_time"].prob(self._times) * self._delta_tc
+        self._full_to_multiband = [int(f * self.durations[0]) for f in self.banded_frequency_points]
+        tp = self.priors["geocent_time"]
+        self._beam_pattern_reference_time = (tp.minimum + tp.maximum) / 2
+        for ifo in self.interferometers:
+            ifo.reference_time = self._beam_pattern_reference_time
+        full = np.asarray(self._full_to_multiband, dtype=np.int64)
+        if full.size and (full.min() < 0 or full.max() >= n):
+            raise ValueError("a banded frequency maps outside the time-marginalisation FFT")
+        # per band, a later point at the same index replaces an earlier one
+        # (numpy's buffered indexed +=); across bands the values add
+        code = np.arange(len(full), dtype=np.int64)
+        for s0, e0 in np.asarray(self.start_end_idxs):
+            seg = full[s0:e0 + 1]
+            _, last = np.unique(seg[::-1], return_index=True)
+            keep = np.zeros(len(seg), dtype=bool)
+            keep[len(seg) - 1 - last] = True
+            code[s0:e0 + 1][~keep] = -code[s0:e0 + 1][~keep] - 1
+        order = np.argsort(full, kind="stable")
+        ptr = np.zeros(n + 1, dtype=np.int64)
+        ptr[1:] = np.cumsum(np.bincount(full, minlength=n))
+        self._mb_tm = (n, ptr.astype(np.int32), code[order].astype(np.int32), float(self._delta_tc),
+                       float(self._beam_pattern_reference_time))
+
+    def _detector_analysis(self, interferometer):
+        raise NotImplementedError("per-detector quantities of the multi-banded likelihood are not built")
+
     def _upload(self):
         names = [ifo.name for ifo in self.interferometers]
         lin = np.stack([np.asarray(self.linear_coeffs[n]) for n in names])
@@ -428,9 +470,14 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
         band_start = np.append(np.asarray(self.start_end_idxs)[:, 0], np.asarray(self.start_end_idxs)[-1, 1] + 1)
         self._mb = (np.asarray(self.banded_frequency_points, dtype=np.float64), lin, quad, band_start,
                     1.0 / np.asarray(self.durations, dtype=np.float64))
-        self.analysis.set_multiband(True, *self._mb)
+        self._set_bands(self.analysis)
+
+    def _set_bands(self, an):
+        an.set_multiband(True, *self._mb)
+        if self._mb_tm is not None:
+            an.set_multiband_time_marginalization(*self._mb_tm)
 
     def _build_analysis(self):
         super()._build_analysis()
         if getattr(self, "_mb", None) is not None:
-            self._analysis.set_multiband(True, *self._mb)
+            self._set_bands(self._analysis)

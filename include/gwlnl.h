@@ -287,10 +287,25 @@ int gwl_set_relative_binning_time_weights(gwl_analysis *a, const double *weights
  * coefficients, in float64 for either precision.  The banded frequencies
  * come in n_bands runs: band b holds indices [band_start[b], band_start[b+1])
  * uniformly spaced by band_df[b] (1 / T^(b)).  Phase and distance
- * marginalisation apply; time marginalisation is refused. */
+ * marginalisation apply; time marginalisation needs
+ * gwl_set_multiband_time_marginalization as well (after each call of this
+ * function). */
 int gwl_set_multiband(gwl_analysis *a, int enable, int64_t n_points, const double *frequencies,
                       const double *linear, const double *quadratic, int32_t n_bands, const int64_t *band_start,
                       const double *band_df);
+
+/* Multi-banding with time marginalisation (multiband.py:714-726, 792-800):
+ * the banded strain times the linear coefficients is scattered to the
+ * full-resolution indices k < n_fft (a power of two, Nbs[-1] / 2) and
+ * transformed (float64); time sample j is start + j delta_tc (+ jitter).
+ * index_start [n_fft + 1] and source [n_points] list, for each k, the banded
+ * points scattered there in band order: a code c >= 0 is banded point c; a
+ * code c < 0 is banded point -c - 1, which a later point of its band replaced
+ * at that index (it enters <h|h> only).  antenna_time fixes the time of the
+ * antenna patterns (the reference sets the interferometers' reference_time
+ * to the middle of the geocent_time prior); the delays stay at geocent_time. */
+int gwl_set_multiband_time_marginalization(gwl_analysis *a, int64_t n_fft, const int32_t *index_start,
+                                           const int32_t *source, double delta_tc, double antenna_time);
 
 /* Reduced-order quadrature (replaces ROQGravitationalWaveTransient.
  * calculate_snrs for one linear and one quadratic basis without time

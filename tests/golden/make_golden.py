@@ -24,7 +24,8 @@ Outputs
     The reference's ``MBGravitationalWaveTransient`` on tf2_128s (reference
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
     frequencies, linear and quadratic coefficients and lnL ratios without
-    marginalisation, with phase and with distance marginalisation.
+    marginalisation, with phase, with distance, with time, and with time,
+    phase and distance marginalisation.
 ``tests/golden/tf2_marg_8s_2k_roq.npz``
     The reference's ``ROQGravitationalWaveTransient`` on tf2_marg_8s_2k with the
     seeded synthetic basis of ``oracle/roq_basis.py``: its time grid, the rows
@@ -242,22 +243,29 @@ def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
     pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
     params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
     n = n_fixed + n_random
+    # drawn after the points, so that the points do not depend on it
+    jitter = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
     out = {"p_" + k: v for k, v in params.items()}
-    for combo in RELBIN_COMBOS:
+    out["time_jitter"] = jitter
+    for combo in RELBIN_COMBOS + RELBIN_TIME_COMBOS:
         ifos, _ = build_reference(bilby, w, taylorf2_aligned)
         wfg = bilby.gw.waveform_generator.WaveformGenerator(
             duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
             frequency_domain_source_model=taylorf2_aligned_frequency_sequence,
             waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
-        p, d = "p" in combo, "d" in combo
-        priors = make_priors(bilby, w, False, p, d)
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, t, p, d)
         like = bilby.gw.likelihood.MBGravitationalWaveTransient(
             interferometers=ifos, waveform_generator=wfg, reference_chirp_mass=reference_chirp_mass,
-            priors=priors if (p or d) else None, phase_marginalization=p, distance_marginalization=d)
+            priors=priors if (t or p or d) else None, time_marginalization=t, phase_marginalization=p,
+            distance_marginalization=d)
         t0 = time.perf_counter()
         vals = []
         for i in range(n):
             q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+                q["time_jitter"] = float(jitter[i])
             if p:
                 q["phase"] = 0.0
             if d:
@@ -551,7 +559,6 @@ def main():
             os.chdir(tmp)
             try:
                 run_multiband(bilby, "tf2_128s", 8, 8)
-                run_roq(bilby)
             finally:
                 os.chdir(cwd)
         return

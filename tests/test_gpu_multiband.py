@@ -1,8 +1,8 @@
 """Multi-banding on the GPU against the reference's own MBGravitationalWaveTransient
 (tests/golden/tf2_128s_multiband.npz, written by the reference with the
 oracle's TaylorF2 as its source model): lnL ratios without marginalisation,
-with phase and with distance marginalisation; batch equals single; the
-unsupported options are refused.
+with phase, with distance, with time, and with time, phase and distance
+marginalisation; batch equals single; the unsupported options are refused.
 
 Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
 table, as for the full likelihood)."""
@@ -31,26 +31,34 @@ def make(combo, tmp_path, **kw):
                             waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
     ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
     priors = {}
+    if "t" in combo:
+        tc = w.injection["geocent_time"]
+        priors["geocent_time"] = Uniform(tc - 0.1, tc + 0.1)
     if "p" in combo:
         priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
     if "d" in combo:
         priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
                                                  DISTANCE_PRIOR["maximum"])
     like = MBGravitationalWaveTransient(ifos, wfg, reference_chirp_mass=0.87, priors=priors or None,
+                                        time_marginalization="t" in combo,
                                         phase_marginalization="p" in combo, distance_marginalization="d" in combo,
                                         distance_marginalization_lookup_table=str(tmp_path / "table.npz"), **kw)
     return like, priors
 
 
-@pytest.mark.parametrize("combo", ["none", "p", "d"])
+@pytest.mark.parametrize("combo", ["none", "p", "d", "t", "tpd"])
 def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     like, priors = make(combo, tmp_path)
     z = golden("tf2_128s_multiband")
-    assert len(like.banded_frequency_points) == len(z["mb_banded_frequency_points"])
+    if "t" not in combo:  # the time prior moves the bands (time_offset, multiband.py:197-225)
+        assert len(like.banded_frequency_points) == len(z["mb_banded_frequency_points"])
     params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
     pts = []
     for i in range(len(params["mass_1"])):
         q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = float(z["time_jitter"][i])
         if "p" in combo:
             q["phase"] = 0.0
         if "d" in combo:
