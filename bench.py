@@ -246,6 +246,40 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
             "fraction_of_points_with_abs_dlnl_le_1e-3": frac_ok}
 
 
+def time_launches(an, block, n, steps, warmup, precision="fp64"):
+    """Mean CUDA-event milliseconds of one evaluation launch of ``n`` points
+    (the device block ``block``), L2 flushed before every timed launch."""
+    import torch
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for s in range(warmup):
+        an.log_likelihood_ratio_device(block.data_ptr(), n, out.data_ptr(), precision, stream.cuda_stream)
+    torch.cuda.synchronize()
+    ms = []
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        an.log_likelihood_ratio_device(block.data_ptr(), n, out.data_ptr(), precision, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms)), bool(torch.isfinite(out).all().item())
+
+
+def time_marginalized_block(w, n, rng):
+    """``n`` prior draws of workload ``w`` with geocent_time at the segment
+    start (the marginalised likelihood's fixed value) and a time jitter."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    p = draw_points(w, n, rng)
+    p["geocent_time"] = np.full(n, float(w.start_time))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, n)
+    return torch.from_numpy(params_block(p)).cuda()
+
+
 def bench_relbin(name, steps, warmup, batch=65536, seed=31):
     """Relative binning (bilby/gw/likelihood/relative.py) on the GPU: fiducial
     = the injection, default chi = 1 and epsilon = 0.5; float64 throughout."""
@@ -289,29 +323,12 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
     like_t = RelativeBinningGravitationalWaveTransient(base.interferometers, base.waveform_generator,
                                                        fiducial_parameters=dict(w.injection), priors=priors,
                                                        time_marginalization=True)
-    an_t = like_t.analysis
     bt = 2048
-    p = draw_points(w, bt, rng)
-    p["geocent_time"] = np.full(bt, float(priors["geocent_time"]))
-    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, bt)
-    block = torch.from_numpy(params_block(p)).cuda()
-    out_t = torch.empty(bt, dtype=torch.float64, device="cuda")
-    for s in range(warmup):
-        an_t.log_likelihood_ratio_device(block.data_ptr(), bt, out_t.data_ptr(), "fp64", stream.cuda_stream)
-    torch.cuda.synchronize()
-    ms_t = []
-    for s in range(steps):
-        flush.fill_(float(s))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        an_t.log_likelihood_ratio_device(block.data_ptr(), bt, out_t.data_ptr(), "fp64", stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms_t.append(e0.elapsed_time(e1))
-    res["time_marginalized"] = {"batch": bt, "fft_length": int(an_t.n_bins - 1),
-                                "value": bt * steps / (sum(ms_t) / 1e3), "unit": "evals/s",
-                                "ms_per_launch": float(np.mean(ms_t)), "precision": "fp64",
-                                "finite": bool(torch.isfinite(out_t).all().item())}
+    ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
+    res["time_marginalized"] = {"batch": bt, "fft_length": int(like_t.analysis.n_bins - 1),
+                                "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
+                                "precision": "fp64", "finite": finite,
+                                "reference_cpu_ms_per_eval": 42.0}
     return res
 
 
@@ -358,12 +375,27 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     an.log_likelihood_ratio_device(blocks[0].data_ptr(), batch, o64.data_ptr(), "fp64", stream.cuda_stream)
     an.log_likelihood_ratio_device(blocks[0].data_ptr(), batch, omx.data_ptr(), "mixed", stream.cuda_stream)
     torch.cuda.synchronize()
+    # with time marginalisation (multiband.py:714-726, 792-800): the float64
+    # FFT of length Nbs[-1] / 2 over the scattered banded strain, per point
+    from bilby_gb300.prior import Uniform
+    tc = w.injection["geocent_time"]
+    like_t = MBGravitationalWaveTransient(base.interferometers, base.waveform_generator, reference_chirp_mass=0.87,
+                                          priors={"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
+                                          time_marginalization=True)
+    bt = 2048
+    ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
+    for ifo in base.interferometers:  # the MB time set-up fixes the antenna time on the interferometers
+        ifo.reference_time = None
     return {"workload": name, "bands": int(like.number_of_bands),
             "banded_frequencies": int(len(like.banded_frequency_points)), "batch": batch,
             "value": res["fp64"]["value"], "unit": "evals/s", "ms_per_launch": res["fp64"]["ms_per_launch"],
             "precision": "fp64", "mixed": res["mixed"], "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
             "max_abs_dlnl_mixed_vs_fp64": float((omx - o64).abs().max().item()), "setup_s": setup_s,
-            "launch": "prologue + one warp per point over the banded frequencies"}
+            "launch": "prologue + one warp per point over the banded frequencies",
+            "time_marginalized": {"batch": bt, "fft_length": int(like_t._mb_tm[0]),
+                                  "banded_frequencies": int(len(like_t.banded_frequency_points)),
+                                  "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
+                                  "precision": "fp64", "finite": finite, "reference_cpu_ms_per_eval": 63.0}}
 
 
 def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, seed=41):

@@ -87,6 +87,8 @@ SIGNATURES = {
                                      ctypes.c_int32, c_double_p, ctypes.c_int32, c_double_p, c_double_p, c_double_p]),
     "gwl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "gwl_profile_last_kernel_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "gwl_set_roq_time_marginalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_double_p,
+                                                       ctypes.c_double, ctypes.c_double]),
     "gwl_set_multiband_time_marginalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
     "gwl_set_relative_binning_time_weights": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),

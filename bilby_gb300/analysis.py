@@ -142,6 +142,14 @@ class Analysis:
         _capi.check(self._lib.gwl_set_relative_binning_time_weights(self._h, _capi.dptr(w)),
                     "gwl_set_relative_binning_time_weights")
 
+    def set_roq_time_marginalization(self, times, delta_tc: float, antenna_time: float):
+        """ROQ with time marginalisation: the marginalisation grid ``times``
+        (absolute, increasing), its spacing and the antenna time."""
+        t = np.ascontiguousarray(times, dtype=np.float64)
+        _capi.check(self._lib.gwl_set_roq_time_marginalization(self._h, len(t), _capi.dptr(t), float(delta_tc),
+                                                               float(antenna_time)),
+                    "gwl_set_roq_time_marginalization")
+
     def set_multiband_time_marginalization(self, n_fft: int, index_start, source, delta_tc: float,
                                            antenna_time: float):
         """Multi-banding with time marginalisation: for each full-resolution

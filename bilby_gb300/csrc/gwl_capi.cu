@@ -112,6 +112,10 @@ struct gwl_analysis {
   double mb_tm_delta_tc = 0.0, mb_tm_antenna_time = 0.0;
   int32_t* mb_tm_ptr = nullptr;
   int32_t* mb_tm_src = nullptr;
+  int roq_tm = 0;  // ROQ time-marginalisation grid set for these weights
+  int64_t roq_tm_n = 0, roq_tm_chunk = 0, roq_tm_rows = 0;
+  double roq_tm_delta_tc = 0.0, roq_tm_antenna_time = 0.0;
+  double* roq_tm_times = nullptr;
   // reduced-order quadrature
   int roq = 0;
   int roq_nl = 0, roq_nq = 0;
@@ -381,6 +385,18 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.roq_wl[d] = a->roq_wl[d];
     L.roq_wq[d] = a->roq_wq[d];
   }
+  if (a->roq && a->roq_tm) {
+    // roq.py:320-331: the marginalisation's own time grid, antenna patterns
+    // and delays at the prior's mid time
+    L.roq_tm = 1;
+    L.roq_tm_n = a->roq_tm_n;
+    L.roq_tm_chunk = a->roq_tm_chunk;
+    L.roq_tm_rows = a->roq_tm_rows;
+    L.roq_tm_times = a->roq_tm_times;
+    L.delta_tc = a->roq_tm_delta_tc;
+    L.antenna_fixed = 1;
+    L.antenna_time = a->roq_tm_antenna_time;
+  }
   return L;
 }
 
@@ -388,7 +404,7 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
   const size_t part = (size_t)std::max(a->n_chunks_plain, a->n_chunks_mixed) * B * a->n_det * kPartStride *
                       sizeof(double);
   size_t tm = 0;
-  if (a->time_marg) tm = time_marg_work_bytes(L);
+  if (a->time_marg && !a->roq) tm = time_marg_work_bytes(L);  // ROQ marginalises without an FFT
   if (B <= a->ws_B && part <= a->part_bytes && tm <= a->tm_bytes) return GWL_OK;
   GWL_CUDA(cudaStreamSynchronize(a->stream));
   free_workspace(a);
@@ -428,6 +444,22 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
   L.tm_series = d_series;
+  if (a->roq && a->time_marg && d_out) {
+    if (!a->roq_tm) {
+      set_error("ROQ with time marginalisation needs gwl_set_roq_time_marginalization");
+      return GWL_ERR_ARGUMENT;
+    }
+    L.precision = GWL_PRECISION_FP64;
+    L.rf_tol = 0.0;
+    GWL_CUDA(launch_prologue(L, s));
+    if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+    GWL_CUDA(launch_roq_time_marginalized(L, s));
+    if (a->profiling) {
+      GWL_CUDA(cudaEventRecord(a->ev_end, s));
+      a->ev_pending = 1;
+    }
+    return GWL_OK;
+  }
   if ((a->relbin || a->multiband) && a->time_marg && d_out) {
     // relative binning / multi-banding with time marginalisation: the float64
     // time-marginalised kernel over the rebuilt full-resolution integrand
@@ -1030,10 +1062,6 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time marginalisation needs an even FFT length (n_bins - 1)");
       return GWL_ERR_UNSUPPORTED;
     }
-    if (a->roq) {
-      set_error("time marginalisation is not available with ROQ");
-      return GWL_ERR_UNSUPPORTED;
-    }
   }
   a->time_marg = enable ? 1 : 0;
   a->jitter = jitter ? 1 : 0;
@@ -1330,8 +1358,8 @@ int gwl_set_roq(gwl_analysis* a, int enable, int32_t n_linear, const double* nod
     a->roq = 0;
     return GWL_OK;
   }
-  if (a->time_marg || a->relbin || a->multiband) {
-    set_error("ROQ excludes time marginalisation, relative binning and multi-banding");
+  if (a->relbin || a->multiband) {
+    set_error("ROQ excludes relative binning and multi-banding");
     return GWL_ERR_UNSUPPORTED;
   }
   if (n_linear < 1 || n_quadratic < 1 || n_time < 5 || !(time_step > 0) || time_start_index < 0 || !nodes_linear ||
@@ -1360,7 +1388,59 @@ int gwl_set_roq(gwl_analysis* a, int enable, int32_t n_linear, const double* nod
   a->roq_n_time = n_time;
   a->roq_time_start = time_start_index;
   a->roq_dt = time_step;
+  a->roq_tm = 0;  // new weights need a new time-marginalisation grid
   a->roq = 1;
+  return GWL_OK;
+}
+
+int gwl_set_roq_time_marginalization(gwl_analysis* a, int64_t n_times, const double* times, double delta_tc,
+                                     double antenna_time) {
+  if (!a || !times) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!a->roq) {
+    set_error("set the ROQ weights first (gwl_set_roq)");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (n_times < 1 || !(delta_tc > 0) || !std::isfinite(antenna_time)) {
+    set_error("ROQ time marginalisation needs at least one time, a positive delta_tc and a finite antenna time");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<double> t(times, times + n_times);
+  for (int64_t j = 1; j < n_times; ++j)
+    if (!(t[(size_t)j] > t[(size_t)j - 1])) {
+      set_error("ROQ marginalisation times must increase");
+      return GWL_ERR_ARGUMENT;
+    }
+  // rows one chunk of samples reads per detector: the span of its detector
+  // times on the weight grid plus the five-sample stencil (the jitter shifts
+  // both ends alike); chunks of 1024 samples, halved until they fit
+  const double t0 = (double)a->roq_time_start * a->roq_dt;
+  const double space = (double)(a->roq_time_start + 1) * a->roq_dt - t0;
+  int64_t chunk = 1024, rows = 0;
+  for (;; chunk /= 2) {
+    double span = 0.0;
+    for (int64_t j0 = 0; j0 < n_times; j0 += chunk)
+      span = std::max(span, t[(size_t)std::min(n_times, j0 + chunk) - 1] - t[(size_t)j0]);
+    rows = (int64_t)std::ceil(span / space) + 8;
+    const size_t smem = (size_t)a->n_det * ((size_t)a->roq_nl + (size_t)rows) * sizeof(double2);
+    if (smem <= 200 * 1024) break;
+    if (chunk == 1) {
+      set_error("ROQ time marginalisation: " + std::to_string(a->roq_nl) +
+                " linear nodes per detector exceed the shared memory of one CTA");
+      return GWL_ERR_UNSUPPORTED;
+    }
+  }
+  int rc;
+  if ((rc = upload(a, &a->roq_tm_times, t))) return rc;
+  a->roq_tm_n = n_times;
+  a->roq_tm_chunk = chunk;
+  a->roq_tm_rows = rows;
+  a->roq_tm_delta_tc = delta_tc;
+  a->roq_tm_antenna_time = antenna_time;
+  a->roq_tm = 1;
   return GWL_OK;
 }
 
@@ -1380,6 +1460,10 @@ int gwl_inner_products_device(gwl_analysis* a, const double* params, int64_t B, 
     return GWL_ERR_ARGUMENT;
   }
   std::lock_guard<std::mutex> g(a->mu);
+  if (a->roq && a->roq_tm) {
+    set_error("per-point inner products are not available for ROQ with time marginalisation");
+    return GWL_ERR_UNSUPPORTED;
+  }
   const int saved = a->time_marg;
   a->time_marg = 0;
   const int rc = run_eval(a, params, B, precision, nullptr, d_inner_h, h_inner_h, static_cast<cudaStream_t>(stream));

@@ -182,6 +182,13 @@ struct LaunchArgs {
   const double4* roq_pq;                // [roq_nq] and of the quadratic nodes
   const double2* roq_wl[kMaxDet];       // [roq_n_time][roq_nl]
   const double* roq_wq[kMaxDet];        // [roq_nq]
+  // ROQ with time marginalisation (roq.py:320-331, 535-541, 604-651): the
+  // regular time grid of the marginalisation and the most weight rows one
+  // point reads per detector; the prologue then stores in dt[d] the detector's
+  // delay at antenna_time alone
+  int roq_tm;
+  int64_t roq_tm_n, roq_tm_chunk, roq_tm_rows;  // samples, samples per chunk, rows per chunk (at most)
+  const double* roq_tm_times;           // [roq_tm_n]
 };
 
 // A batch over several analyses evaluated by one persistent launch: per item
@@ -238,6 +245,7 @@ cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_roq_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 // Ordering of a mixed TaylorF2 launch: the band-end keys, doubled when points
 // can be marked for the accurate kernel (rf_tol > 0; their keys take the upper

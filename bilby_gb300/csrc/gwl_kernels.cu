@@ -56,15 +56,14 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
   for (int d = 0; d < a.n_det; ++d) {
     double fp, fx, delay;
     antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky, &fp, &fx, &delay);
-    if (a.antenna_fixed) {
-      double unused;
-      antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky_ant, &fp, &fx, &unused);
-    }
+    double delay_ref = delay;
+    if (a.antenna_fixed) antenna_and_delay(a.det[d].tensor, a.det[d].vertex, sky_ant, &fp, &fx, &delay_ref);
     r.fp[d] = fp;
     r.fx[d] = fx;
     // interferometer.py:355-358: subtract the two GPS times first, then add the delay.
     const double dt_geocent = tgeo - a.det[d].start_time;
-    r.dt[d] = dt_geocent + delay;
+    // ROQ with time marginalisation: the delay at the antenna time alone (roq.py:529-541)
+    r.dt[d] = a.roq_tm ? delay_ref : dt_geocent + delay;
     // frac(dt * df) in cycles per bin as 0.64 fixed point, so that the phase
     // 2 pi f_k dt = 2 pi k (dt df) reduces exactly modulo one cycle.
     const double x = r.dt[d] * a.step;

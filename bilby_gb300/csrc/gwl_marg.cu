@@ -785,6 +785,180 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   }
 }
 
+// ---------------------------------------------------------------------------
+// ROQ with time marginalisation (roq.py:320-331, 467-541, 604-651, with
+// base.py:794-820): one CTA per point.
+//   1. conj(h_d) at the linear nodes into shared memory (antenna patterns at
+//      the prior's mid time, no time shift), <h|h> from the quadratic nodes;
+//   then per chunk of roq_tm_chunk time samples:
+//   2. D_d[k] = sum_q W_d[k][q] conj(h_d(F_q)) for the weight rows k the
+//      chunk's samples read (one warp per row, fixed-order reduction);
+//   3. for each time sample t_j of the marginalisation grid inside the prior,
+//      <d|h>(t_j) = sum_d of the five-sample interpolation of D_d at the
+//      detector time (t_j - start) + delay_d + jitter (LIGO-T2100224), the
+//      marginalised lnL and a logsumexp weighted by prior(t_j) delta_tc.
+// float64 throughout.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[2 * kTmThreads];
+  __shared__ long long s_rows[2 * kMaxDet];
+  const int nl = a.roq_nl, nq = a.roq_nq;
+  const int64_t n = a.roq_tm_n, max_rows = a.roq_tm_rows;
+  double2* s_h = reinterpret_cast<double2*>(smem);  // [D][nl]
+  double2* s_D = s_h + (size_t)D * nl;              // [D][max_rows], the current chunk's rows
+  // roq.py:624-625: the weight grid's first time and spacing
+  const double t0 = (double)a.roq_time_start * a.roq_dt;
+  const double space = (double)(a.roq_time_start + 1) * a.roq_dt - t0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+    const PointRec& r = a.rec[i];
+    const double jit = r.jitter;
+    const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+    const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+    const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+    double hh_part = 0.0;
+    for (int q = threadIdx.x; q < nl; q += blockDim.x) {
+      double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+      const double f = a.roq_fl[q];
+      const bool on = r.valid && (tf2 ? tf2_pols_t(a, r, a.roq_pl[q], f, u, lnu, pu5, hp, hx)
+                                      : plain_pols(a, r, f, hp, hx));
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double hr = on ? hp.x * r.fp[d] + hx.x * r.fx[d] : 0.0;
+        const double hi = on ? hp.y * r.fp[d] + hx.y * r.fx[d] : 0.0;
+        s_h[(size_t)d * nl + q] = make_double2(hr, -hi);
+      }
+    }
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+      const double f = a.roq_fq[q];
+      if (!(r.valid && (tf2 ? tf2_pols_t(a, r, a.roq_pq[q], f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx))))
+        continue;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double hr = hp.x * r.fp[d] + hx.x * r.fx[d], hi = hp.y * r.fp[d] + hx.y * r.fx[d];
+        hh_part += (hr * hr + hi * hi) * a.roq_wq[d][q];
+      }
+    }
+    const double hh = block_sum(hh_part, red);  // ends with a barrier: s_h is complete
+    const double sr = r.dist / a.ref_dist, hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
+    const double prob = 1.0 / (a.t_max - a.t_min);
+    double m = -INFINITY, acc = 0.0;
+    // the time samples in chunks, each with the weight rows its detector times read
+    for (int64_t j0 = 0; j0 < n; j0 += a.roq_tm_chunk) {
+      const int64_t j1 = (j0 + a.roq_tm_chunk < n ? j0 + a.roq_tm_chunk : n) - 1;
+      if (threadIdx.x < D) {
+        // the detector time grows with j: the rows of the chunk's first and last sample
+        const int d = threadIdx.x;
+        const double x0 = ((a.roq_tm_times[j0] - a.det[d].start_time) + r.dt[d]) + jit;
+        const double x1 = ((a.roq_tm_times[j1] - a.det[d].start_time) + r.dt[d]) + jit;
+        long long lo = (long long)floor((x0 - t0) / space) - 2, hi = (long long)floor((x1 - t0) / space) + 2;
+        lo = lo < 0 ? 0 : lo;
+        hi = hi > a.roq_n_time - 1 ? a.roq_n_time - 1 : hi;
+        if (hi - lo + 1 > max_rows) hi = lo + max_rows - 1;
+        s_rows[2 * d] = lo;
+        s_rows[2 * d + 1] = hi >= lo ? hi - lo + 1 : 0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const long long lo = s_rows[2 * d], nr = s_rows[2 * d + 1];
+        for (long long k = warp; k < nr; k += n_warps) {
+          const double2* w = a.roq_wl[d] + (size_t)(lo + k) * nl;
+          const double2* h = s_h + (size_t)d * nl;
+          double ar = 0.0, ai = 0.0;
+          for (int q = lane; q < nl; q += 32) {
+            const double2 wv = w[q], hv = h[q];
+            ar += wv.x * hv.x - wv.y * hv.y;
+            ai += wv.x * hv.y + wv.y * hv.x;
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            ar += __shfl_xor_sync(0xffffffffu, ar, o);
+            ai += __shfl_xor_sync(0xffffffffu, ai, o);
+          }
+          if (lane == 0) s_D[(size_t)d * max_rows + k] = make_double2(ar, ai);
+        }
+      }
+      __syncthreads();
+      for (int64_t j = j0 + threadIdx.x; j <= j1; j += blockDim.x) {
+        const double tj = a.roq_tm_times[j];
+        const double t = tj + jit;
+        if (!(t >= a.t_min && t <= a.t_max)) continue;
+        double xr = 0.0, xi = 0.0;
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double x = ((tj - a.det[d].start_time) + r.dt[d]) + jit;
+          const double tpr = (x - t0) / space;
+          const double fc = floor(tpr);
+          const long long k = (long long)fc - s_rows[2 * d] - 2;
+          if (k < 0 || k + 4 >= s_rows[2 * d + 1]) {
+            ok = false;  // outside the weight grid
+            continue;
+          }
+          const double2* Dd = s_D + (size_t)d * max_rows + k;
+          const double2 m2 = Dd[0], m1 = Dd[1], c0 = Dd[2], p1 = Dd[3], p2 = Dd[4];
+          const double b = tpr - fc, a1 = 1.0 - b;
+          const double c = (a1 * a1 * a1 - a1) / 6.0, dd = (b * b * b - b) / 6.0;
+          const double r1r = (-m2.x + 8.0 * m1.x - 14.0 * c0.x + 8.0 * p1.x - p2.x) / 4.0;
+          const double r1i = (-m2.y + 8.0 * m1.y - 14.0 * c0.y + 8.0 * p1.y - p2.y) / 4.0;
+          const double r2r = c0.x - 2.0 * p1.x + p2.x, r2i = c0.y - 2.0 * p1.y + p2.y;
+          xr += a1 * c0.x + b * p1.x + c * r1r + dd * r2r;
+          xi += a1 * c0.y + b * p1.y + c * r1i + dd * r2i;
+        }
+        double l;
+        if (!ok) {
+          l = -INFINITY;
+        } else if (a.dist_marg) {
+          const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
+          l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
+        } else if (a.phase_marg) {
+          l = ln_i0(sqrt(xr * xr + xi * xi)) - hh / 2;
+        } else {
+          l = xr - hh / 2;
+        }
+        if (l > m) {
+          acc = isfinite(m) ? acc * exp(m - l) + 1.0 : 1.0;
+          m = l;
+        } else if (isfinite(l)) {
+          acc += exp(l - m);
+        }
+      }
+      __syncthreads();  // s_rows and s_D are rewritten by the next chunk
+    }
+    // combine the (m, acc) pairs in a fixed tree order
+    double* redm = red;
+    double* reds = red + kTmThreads;
+    redm[threadIdx.x] = m;
+    reds[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kTmThreads / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        const double m1 = redm[threadIdx.x], m2 = redm[threadIdx.x + w];
+        const double s1 = reds[threadIdx.x], s2 = reds[threadIdx.x + w];
+        const double mm = fmax(m1, m2);
+        double ss = 0.0;
+        if (isfinite(mm)) ss = (isfinite(m1) ? s1 * exp(m1 - mm) : 0.0) + (isfinite(m2) ? s2 * exp(m2 - mm) : 0.0);
+        redm[threadIdx.x] = mm;
+        reds[threadIdx.x] = ss;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double amax = redm[0], total = reds[0] * prob * a.delta_tc;
+      double lnl;
+      if (!r.valid) lnl = -1.7976931348623157e308;
+      else if (!isfinite(amax)) lnl = amax;
+      else lnl = amax + log(total);
+      a.out[i] = lnl;
+    }
+    __syncthreads();
+  }
+}
+
 namespace {
 
 struct TwiddleCache {
@@ -860,6 +1034,34 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
     k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d64, log2L);
   }
   return cudaGetLastError();
+}
+
+size_t roq_time_marg_smem(const LaunchArgs& a) {
+  return (size_t)a.n_det * ((size_t)a.roq_nl + (size_t)a.roq_tm_rows) * sizeof(double2);
+}
+
+template <int D>
+static cudaError_t launch_roq_tm_d(const LaunchArgs& a, cudaStream_t s) {
+  const size_t smem = roq_time_marg_smem(a);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_roq_time_marg<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned grid = (unsigned)std::min<int64_t>(a.B, 4 * (int64_t)tm_grid_fp64());
+  k_roq_time_marg<D><<<grid, kTmThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roq_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
+  // checked on the host first
+  if (roq_time_marg_smem(a) > 200 * 1024 || a.roq_tm_n < 1 || a.roq_tm_chunk < 1 || a.roq_tm_rows < 5)
+    return cudaErrorInvalidValue;
+  switch (a.n_det) {
+    case 1: return launch_roq_tm_d<1>(a, s);
+    case 2: return launch_roq_tm_d<2>(a, s);
+    case 3: return launch_roq_tm_d<3>(a, s);
+    default: return launch_roq_tm_d<4>(a, s);
+  }
 }
 
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {

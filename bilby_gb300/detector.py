@@ -194,6 +194,7 @@ class Interferometer:
         self.power_spectral_density = power_spectral_density
         self.strain_data = InterferometerStrainData(minimum_frequency, maximum_frequency)
         self.calibration_model = calibration_model
+        self.meta_data = dict()
 
     minimum_frequency = property(lambda self: self.strain_data.minimum_frequency)
     maximum_frequency = property(lambda self: self.strain_data.maximum_frequency)
@@ -252,6 +253,10 @@ class Interferometer:
             injection_polarizations = waveform_generator.frequency_domain_strain(parameters)
         signal = self.get_detector_response(injection_polarizations, parameters)
         self.strain_data.frequency_domain_strain = self.strain_data.frequency_domain_strain + signal
+        # interferometer.py:512-516 (read by the ROQ time resolution)
+        self.meta_data["optimal_SNR"] = self.optimal_snr_squared(signal).real ** 0.5
+        self.meta_data["matched_filter_SNR"] = self.matched_filter_snr(signal)
+        self.meta_data["parameters"] = parameters
         return injection_polarizations
 
 
@@ -301,5 +306,5 @@ class InterferometerList(list):
 
     @property
     def meta_data(self):
-        return {ifo.name: dict(minimum_frequency=ifo.minimum_frequency, maximum_frequency=ifo.maximum_frequency)
-                for ifo in self}
+        return {ifo.name: dict(ifo.meta_data, minimum_frequency=ifo.minimum_frequency,
+                               maximum_frequency=ifo.maximum_frequency) for ifo in self}

@@ -10,9 +10,13 @@ evaluates the model at the frequency nodes, contracts it with the weights of
 the five time samples around each detector's arrival time and interpolates
 (``k_roq``, behind ``gwl_set_roq`` in include/gwlnl.h).
 
-Not built: several bases selected by prior ranges, multi-banded ROQ weights
-and time marginalisation (NotImplementedError); hdf5 files need h5py, as in
-the reference.
+With time marginalisation (roq.py:320-331, 535-541, 604-651) one CTA per
+point contracts the weight rows its detector times read, interpolates <d|h>
+at every sample of the marginalisation grid and marginalises
+(``k_roq_time_marg``, behind ``gwl_set_roq_time_marginalization``).
+
+Not built: several bases selected by prior ranges and multi-banded ROQ
+weights (NotImplementedError); hdf5 files need h5py, as in the reference.
 """
 from __future__ import annotations
 
@@ -40,10 +44,11 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
                  distance_marginalization=False, phase_marginalization=False, time_marginalization=False,
                  jitter_time=True, delta_tc=None, distance_marginalization_lookup_table=None, reference_frame="sky",
                  time_reference="geocenter", parameter_conversion=None, precision="fp64"):
-        if time_marginalization:
-            raise NotImplementedError("time marginalisation with ROQ has no GPU kernel")
         self._roq = None
+        self._roq_tm = None
+        self._delta_tc_request = delta_tc
         super().__init__(interferometers, waveform_generator, priors=priors,
+                         time_marginalization=time_marginalization,
                          distance_marginalization=distance_marginalization,
                          phase_marginalization=phase_marginalization,
                          distance_marginalization_lookup_table=distance_marginalization_lookup_table,
@@ -205,6 +210,27 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
             inv_psd = 1 / np.asarray(ifo.power_spectral_density_array)[mask][ifo_idxs]
             self.weights[ifo.name + "_quadratic"] = [4. / duration * quad[:, roq_idxs] @ inv_psd]
 
+    def _setup_time_marginalization(self):
+        """roq.py:320-331: delta_tc from the constructor or the ROQ time
+        resolution, shrunk so that it divides the geocent_time prior; the
+        samples sit at the middles of the intervals; the antenna patterns and
+        delays are taken at the prior's mid time."""
+        tp = self.priors["geocent_time"]
+        if type(tp).__name__ != "Uniform":
+            raise NotImplementedError("time marginalisation on the GPU needs a Uniform geocent_time prior")
+        delta_tc = self._delta_tc_request
+        if delta_tc is None:
+            delta_tc = self._get_time_resolution()
+        tcmin, tcmax = tp.minimum, tp.maximum
+        n = int(np.ceil((tcmax - tcmin) / delta_tc))
+        self._delta_tc = (tcmax - tcmin) / n
+        self._times = tcmin + self._delta_tc / 2. + np.arange(n) * self._delta_tc
+        self._beam_pattern_reference_time = (tcmin + tcmax) / 2.
+        self.time_prior_array = tp.prob(self._times) * self._delta_tc
+
+    def _detector_analysis(self, interferometer):
+        raise NotImplementedError("per-detector quantities of the ROQ likelihood are not built")
+
     def _upload(self):
         ts = np.asarray(self.weights["time_samples"], dtype=np.float64)
         dt = float(ts[1] - ts[0])
@@ -217,9 +243,17 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         wq = np.stack([np.asarray(self.weights[n + "_quadratic"][0]).real for n in names])
         self._roq = (np.asarray(self.weights["frequency_nodes_linear"][0], dtype=np.float64),
                      np.asarray(self.weights["frequency_nodes_quadratic"][0], dtype=np.float64), start, dt, wl, wq)
-        self.analysis.set_roq(True, *self._roq)
+        if self.time_marginalization:
+            self._roq_tm = (np.asarray(self._times, dtype=np.float64), float(self._delta_tc),
+                            float(self._beam_pattern_reference_time))
+        self._set_weights_on(self.analysis)
+
+    def _set_weights_on(self, an):
+        an.set_roq(True, *self._roq)
+        if self._roq_tm is not None:
+            an.set_roq_time_marginalization(*self._roq_tm)
 
     def _build_analysis(self):
         super()._build_analysis()
         if getattr(self, "_roq", None) is not None:
-            self._analysis.set_roq(True, *self._roq)
+            self._set_weights_on(self._analysis)

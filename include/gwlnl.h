@@ -320,10 +320,24 @@ int gwl_set_multiband_time_marginalization(gwl_analysis *a, int64_t n_fft, const
  * arrival time (LIGO-T2100224); <h|h> = sum_j |h(G_j)|^2 w_j
  * (quadratic_weights [n_det][n_quadratic]).  float64 for either precision;
  * an arrival time within two samples of the grid's ends gives lnL = -inf, as
- * in the reference. */
+ * in the reference.  Time marginalisation needs
+ * gwl_set_roq_time_marginalization as well. */
 int gwl_set_roq(gwl_analysis *a, int enable, int32_t n_linear, const double *nodes_linear, int32_t n_quadratic,
                 const double *nodes_quadratic, int64_t n_time, int64_t time_start_index, double time_step,
                 const double *linear_weights, const double *quadratic_weights);
+
+/* ROQ with time marginalisation (roq.py:320-331, 535-541, 604-651): the
+ * marginalisation grid times[n_times] (absolute GPS, increasing; the
+ * reference's tc_min + delta_tc / 2 + j delta_tc), the weight delta_tc of
+ * each sample, and antenna_time, the time of the antenna patterns and of the
+ * detector delays (the middle of the geocent_time prior).  Each evaluation
+ * then contracts the linear weights of every row its detector times read
+ * with conj(h) at the linear nodes, interpolates <d|h> at each time sample
+ * from five rows (LIGO-T2100224), sums over detectors and marginalises
+ * (float64), in chunks of time samples whose rows fit in shared memory.
+ * Refused when the linear nodes alone do not fit.  gwl_set_roq resets it. */
+int gwl_set_roq_time_marginalization(gwl_analysis *a, int64_t n_times, const double *times, double delta_tc,
+                                     double antenna_time);
 
 /* On-device prior rescaling and parameter conversion for the batch path
  * (replaces, for the supported priors, PriorDict.rescale, bilby/core/prior/

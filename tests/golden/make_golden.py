@@ -30,8 +30,9 @@ Outputs
     The reference's ``ROQGravitationalWaveTransient`` on tf2_marg_8s_2k with the
     seeded synthetic basis of ``oracle/roq_basis.py``: its time grid, the rows
     of the linear weights the stored points read, the quadratic weights, the
-    frequency nodes, and lnL ratios without marginalisation, with phase and
-    with distance marginalisation.
+    frequency nodes, and lnL ratios without marginalisation, with phase, with
+    distance, with time, and with time, phase and distance marginalisation
+    (with the time grid's spacing and length).
 ``tests/golden/priors.npz``
     The reference's ``PriorDict.rescale`` of fixed unit-cube samples for the
     GW prior kinds the device rescaler supports, followed by
@@ -296,8 +297,11 @@ def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
     params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
     params.pop("time_jitter", None)
     n = n_fixed + n_random
+    # drawn after the points, so that the points do not depend on it
+    jitter = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
     out = {"p_" + k: v for k, v in params.items()}
-    for combo in RELBIN_COMBOS:
+    out["time_jitter"] = jitter
+    for combo in RELBIN_COMBOS + RELBIN_TIME_COMBOS:
         ifos, _ = build_reference(bilby, w, taylorf2_aligned)
         fm = ifos[0].frequency_array[ifos[0].frequency_mask]
         nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
@@ -306,15 +310,21 @@ def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
             frequency_domain_source_model=taylorf2_aligned_roq,
             waveform_arguments=dict(minimum_frequency=w.minimum_frequency, frequency_nodes_linear=nl,
                                     frequency_nodes_quadratic=nq))
-        p, d = "p" in combo, "d" in combo
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
         priors = make_priors(bilby, w, True, p, d)
         like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
             interferometers=ifos, waveform_generator=wfg, priors=priors, linear_matrix=bl.T,
-            quadratic_matrix=bq.T, phase_marginalization=p, distance_marginalization=d)
+            quadratic_matrix=bq.T, time_marginalization=t, phase_marginalization=p, distance_marginalization=d)
+        if t:
+            out["roq_tm_delta_tc_" + combo] = float(like._delta_tc)
+            out["roq_tm_n_times_" + combo] = len(like._times)
         t0 = time.perf_counter()
         vals = []
         for i in range(n):
             q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+                q["time_jitter"] = float(jitter[i])
             if p:
                 q["phase"] = 0.0
             if d:

@@ -1,9 +1,11 @@
 """ROQ on the GPU against the reference's own ROQGravitationalWaveTransient
 (tests/golden/tf2_marg_8s_2k_roq.npz: the reference's weights for a seeded
 synthetic basis, stored for the time samples the points read, and its lnL
-ratios without marginalisation, with phase and with distance
-marginalisation).  The rows of the linear weights that were not stored are
-NaN, so reading any other time sample would show.
+ratios without marginalisation, with phase, with distance, with time, and
+with time, phase and distance marginalisation).  The rows of the linear
+weights that were not stored are NaN, so reading any other time sample would
+show.  With time marginalisation every row of the prior window is read, so
+those likelihoods compute their weights from the same seeded basis.
 
 Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
 table, as for the full likelihood)."""
@@ -57,19 +59,34 @@ def make(combo, tmp_path, **kw):
         priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
                                                  DISTANCE_PRIOR["maximum"])
     z = golden("tf2_marg_8s_2k_roq")
-    like = ROQGravitationalWaveTransient(ifos, wfg, priors, weights=golden_weights(z, [i.name for i in ifos]),
+    if "t" in combo:
+        from oracle import roq_basis
+        fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+        nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
+        wfg.waveform_arguments.update(frequency_nodes_linear=nl, frequency_nodes_quadratic=nq)
+        source = dict(linear_matrix=bl.T, quadratic_matrix=bq.T)
+    else:
+        source = dict(weights=golden_weights(z, [i.name for i in ifos]))
+    like = ROQGravitationalWaveTransient(ifos, wfg, priors, time_marginalization="t" in combo,
                                          phase_marginalization="p" in combo, distance_marginalization="d" in combo,
-                                         distance_marginalization_lookup_table=str(tmp_path / "table.npz"), **kw)
+                                         distance_marginalization_lookup_table=str(tmp_path / "table.npz"),
+                                         **source, **kw)
     return like, priors, z
 
 
-@pytest.mark.parametrize("combo", ["none", "p", "d"])
+@pytest.mark.parametrize("combo", ["none", "p", "d", "t", "tpd"])
 def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     like, priors, z = make(combo, tmp_path)
+    if "t" in combo:  # the same marginalisation grid (roq.py:320-331)
+        assert like._delta_tc == pytest.approx(float(z["roq_tm_delta_tc_" + combo]), rel=1e-12)
+        assert len(like._times) == int(z["roq_tm_n_times_" + combo])
     params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
     pts = []
     for i in range(len(params["mass_1"])):
         q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = float(z["time_jitter"][i])
         if "p" in combo:
             q["phase"] = 0.0
         if "d" in combo:
@@ -82,7 +99,3 @@ def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     rtol = 1e-8 if "d" in combo else 1e-9
     assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
 
-
-def test_time_marginalisation_is_refused(gpu, tmp_path):
-    with pytest.raises(NotImplementedError):
-        make("none", tmp_path, time_marginalization=True)
