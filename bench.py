@@ -448,11 +448,22 @@ def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, s
         e1.record(stream)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
-    return {"workload": name, "linear_nodes": n_linear, "quadratic_nodes": n_quadratic,
-            "time_samples": int(len(like.weights["time_samples"])), "batch": batch,
-            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
-            "precision": "fp64", "setup_s": setup_s, "basis": "seeded random basis of the stated size",
-            "launch": "prologue + one warp per point over the nodes"}
+    res = {"workload": name, "linear_nodes": n_linear, "quadratic_nodes": n_quadratic,
+           "time_samples": int(len(like.weights["time_samples"])), "batch": batch,
+           "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+           "precision": "fp64", "setup_s": setup_s, "basis": "seeded random basis of the stated size",
+           "launch": "prologue + one warp per point over the nodes"}
+    # with time marginalisation (roq.py:320-331, 604-651): every weight row of
+    # the prior window contracted per point, five-sample interpolation per time
+    like_t = ROQGravitationalWaveTransient(ifos, wfg, {"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
+                                           linear_matrix=lin, quadratic_matrix=quad, time_marginalization=True)
+    bt = 1024
+    ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
+    res["time_marginalized"] = {"batch": bt, "marginalization_samples": int(len(like_t._times)),
+                                "weight_rows": int(len(like_t.weights["time_samples"])),
+                                "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
+                                "precision": "fp64", "finite": finite}
+    return res
 
 
 def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):

@@ -1025,7 +1025,7 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
   } else {
     // relative binning: the edge ratios in shared memory
     const size_t smem = a.relbin ? (size_t)a.rb_edges * D * sizeof(double2) : 0;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {  // static and dynamic together may pass 48 KB
       cudaError_t e =
           cudaFuncSetAttribute(k_time_marg<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -1042,11 +1042,10 @@ size_t roq_time_marg_smem(const LaunchArgs& a) {
 
 template <int D>
 static cudaError_t launch_roq_tm_d(const LaunchArgs& a, cudaStream_t s) {
+  // the opt-in covers the dynamic part; static and dynamic together may pass 48 KB
   const size_t smem = roq_time_marg_smem(a);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_roq_time_marg<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  cudaError_t e = cudaFuncSetAttribute(k_roq_time_marg<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)std::min<int64_t>(a.B, 4 * (int64_t)tm_grid_fp64());
   k_roq_time_marg<D><<<grid, kTmThreads, smem, s>>>(a);
   return cudaGetLastError();

@@ -99,3 +99,28 @@ def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     rtol = 1e-8 if "d" in combo else 1e-9
     assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
 
+
+
+def test_time_marginalized_with_many_nodes(gpu, tmp_path):
+    """300 linear nodes: the nodes and each chunk's weight rows take more than
+    48 KB of shared memory together with the kernel's static arrays."""
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.roq import ROQGravitationalWaveTransient
+    from oracle import roq_basis
+    like, priors, z = make("t", tmp_path)
+    ifos, wfg = like.interferometers, like.waveform_generator
+    fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    nl, bl, nq, bq = roq_basis.build(fm, n_linear=300, n_quadratic=60, n_train=400,
+                                     minimum_frequency=w.minimum_frequency)
+    wfg.waveform_arguments.update(frequency_nodes_linear=nl, frequency_nodes_quadratic=nq)
+    tc = w.injection["geocent_time"]
+    big = ROQGravitationalWaveTransient(ifos, wfg, {"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
+                                        linear_matrix=bl.T, quadratic_matrix=bq.T, time_marginalization=True)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    params["geocent_time"] = np.full(len(params["mass_1"]), float(w.start_time))
+    params["time_jitter"] = z["time_jitter"]
+    batch = big.log_likelihood_ratio_batch(params)
+    single = np.array([big.log_likelihood_ratio(point(params, i)) for i in range(len(batch))])
+    assert np.all(np.isfinite(batch))
+    assert np.array_equal(single, batch)
