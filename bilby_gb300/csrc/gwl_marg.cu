@@ -527,36 +527,44 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       __syncthreads();
       stage = 2;
     }
-    if constexpr (MIXED) {
-      // radix-16 passes (four radix-2 stages in registers): fewer shared-memory
-      // round trips and barriers; the stage-j twiddles of a group depend only
+    {
+      // radix-16 passes (mixed; radix-8 in float64, within the register
+      // budget): RB radix-2 stages in registers, fewer round trips through the
+      // buffer and fewer barriers; the stage-j twiddles of a group depend only
       // on (k mod 2^j)
-      for (; stage + 3 <= log2L; stage += 4) {
+      constexpr int RB = MIXED ? 4 : 3, RN = 1 << RB;
+      for (; stage + RB - 1 <= log2L; stage += RB) {
         const int64_t h0 = (int64_t)1 << (stage - 1);
-        for (int64_t gi = threadIdx.x; gi < L / 16; gi += blockDim.x) {
+        for (int64_t gi = threadIdx.x; gi < L / RN; gi += blockDim.x) {
           const int64_t pos = gi & (h0 - 1);
-          const int64_t b0 = ((gi >> (stage - 1)) << (stage + 3)) + pos;
-          C x[16];
+          const int64_t b0 = ((gi >> (stage - 1)) << (stage - 1 + RB)) + pos;
+          C x[RN];
 #pragma unroll
-          for (int k = 0; k < 16; ++k) x[k] = buf[P(b0 + k * h0)];
+          for (int k = 0; k < RN; ++k) x[k] = buf[P(b0 + k * h0)];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
+          for (int j = 0; j < RB; ++j) {
             // exp(-2 pi i (pos + m h0) L / (2 h0 2^j) / L) = tw(pos stride) * exp(-2 pi i m / 2^(j+1))
             const int64_t stride = L / (2 * (h0 << j));
-            const C w0 = tw(pos * stride);
-            C w[8];
-            w[0] = w0;
+            C w[MIXED ? 8 : 1];
+            if constexpr (MIXED) {
+              const C w0 = tw(pos * stride);
+              w[0] = w0;
 #pragma unroll
-            for (int m = 1; m < (1 << j); ++m) {
-              const float2 u = s_w16[m << (3 - j)];
-              w[m].x = w0.x * u.x - w0.y * u.y;
-              w[m].y = w0.x * u.y + w0.y * u.x;
+              for (int m = 1; m < (1 << j); ++m) {
+                const float2 u = s_w16[m << (3 - j)];
+                w[m].x = w0.x * u.x - w0.y * u.y;
+                w[m].y = w0.x * u.y + w0.y * u.x;
+              }
             }
 #pragma unroll
-            for (int k = 0; k < 16; ++k) {
+            for (int k = 0; k < RN; ++k) {
               if (k & (1 << j)) continue;
               const int k2 = k | (1 << j);
-              const C ww = w[k & ((1 << j) - 1)];
+              // float64: each twiddle from the table (few registers),
+              // exp(-2 pi i (pos + m h0) stride / L) for m = k mod 2^j
+              C ww;
+              if constexpr (MIXED) ww = w[k & ((1 << j) - 1)];
+              else ww = tw((pos + (int64_t)(k & ((1 << j) - 1)) * h0) * stride);
               const R tr = ww.x * x[k2].x - ww.y * x[k2].y, ti = ww.x * x[k2].y + ww.y * x[k2].x;
               x[k2].x = x[k].x - tr;
               x[k2].y = x[k].y - ti;
@@ -565,7 +573,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             }
           }
 #pragma unroll
-          for (int k = 0; k < 16; ++k) buf[P(b0 + k * h0)] = x[k];
+          for (int k = 0; k < RN; ++k) buf[P(b0 + k * h0)] = x[k];
         }
         __syncthreads();
       }
