@@ -163,6 +163,7 @@ class Analysis:
         _capi.check(self._lib.gwl_set_multiband_time_marginalization(
             self._h, int(n_fft), ptr.ctypes.data_as(ctypes.c_void_p), src.ctypes.data_as(ctypes.c_void_p),
             float(delta_tc), float(antenna_time)), "gwl_set_multiband_time_marginalization")
+        self.time_fft_length = int(n_fft)
 
     def set_multiband(self, enable: bool, frequencies=None, linear=None, quadratic=None, band_start=None,
                       band_df=None):
@@ -306,7 +307,7 @@ class Analysis:
         <h|h> [B]) from the float64 time-marginalisation kernel (synchronous)."""
         import torch
         block = np.ascontiguousarray(block, dtype=np.float64)
-        B, L = block.shape[1], self.n_bins - 1
+        B, L = block.shape[1], getattr(self, "time_fft_length", self.n_bins - 1)
         dev = torch.from_numpy(block).cuda()
         series = torch.empty((B, L, 2), dtype=torch.float64, device=dev.device)
         hh = torch.empty(B, dtype=torch.float64, device=dev.device)

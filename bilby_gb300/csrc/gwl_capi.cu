@@ -1482,8 +1482,8 @@ int gwl_time_series_device(gwl_analysis* a, const double* params, int64_t B, dou
     set_error("gwl_time_series_device needs time marginalisation enabled");
     return GWL_ERR_ARGUMENT;
   }
-  if (a->multiband || a->roq) {
-    set_error("gwl_time_series_device serves the full frequency grid and relative binning only");
+  if (a->roq) {
+    set_error("gwl_time_series_device serves the full grid, relative binning and multi-banding");
     return GWL_ERR_ARGUMENT;
   }
   if (B <= 0) return GWL_OK;

@@ -461,7 +461,29 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
                        float(self._beam_pattern_reference_time))
 
     def _detector_analysis(self, interferometer):
-        raise NotImplementedError("per-detector quantities of the multi-banded likelihood are not built")
+        """A one-detector analysis with this detector's coefficients (and the
+        time-marginalisation tables): calculate_snrs then gives the
+        multi-banded inner products of multiband.py:728-807."""
+        name = interferometer.name
+        an = self._detector_analyses.get(name)
+        if an is None:
+            names = [ifo.name for ifo in self.interferometers]
+            if name not in names:
+                raise ValueError(f"interferometer {name} is not part of this likelihood")
+            k = names.index(name)
+            an = self._new_analysis([self.interferometers[k]])
+            if self.time_marginalization:
+                tp = self.priors["geocent_time"]
+                an.set_time_marginalization(True, False, tp.minimum, tp.maximum)
+            freqs, lin, quad, band_start, band_df = self._mb
+            an.set_multiband(True, freqs, lin[k:k + 1], quad[k:k + 1], band_start, band_df)
+            if self._mb_tm is not None:
+                an.set_multiband_time_marginalization(*self._mb_tm)
+            self._detector_analyses[name] = an
+        return an
+
+    def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        raise NotImplementedError("the time posterior of the multi-banded likelihood is not built")
 
     def _upload(self):
         names = [ifo.name for ifo in self.interferometers]

@@ -227,7 +227,29 @@ class RelativeBinningGravitationalWaveTransient(GravitationalWaveTransient):
             self._set_bins(self._analysis)
 
     def _detector_analysis(self, interferometer):
-        raise NotImplementedError("per-detector quantities of the relative-binning likelihood are not built")
+        """A one-detector analysis with this detector's bins, 1 / h0 at the
+        edges, summary data (and time weights): calculate_snrs then gives the
+        relative-binning inner products of relative.py:398-420."""
+        name = interferometer.name
+        an = self._detector_analyses.get(name)
+        if an is None:
+            names = [ifo.name for ifo in self.interferometers]
+            if name not in names:
+                raise ValueError(f"interferometer {name} is not part of this likelihood")
+            k = names.index(name)
+            an = self._new_analysis([self.interferometers[k]])
+            if self.time_marginalization:
+                tp = self.priors["geocent_time"]
+                an.set_time_marginalization(True, False, tp.minimum, tp.maximum)
+            idx, inv, sm = self._rb
+            an.set_relative_binning(True, idx, inv[k:k + 1], sm[k:k + 1])
+            if self._rb_time_weights is not None:
+                an.set_relative_binning_time_weights(self._rb_time_weights[k:k + 1])
+            self._detector_analyses[name] = an
+        return an
+
+    def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        raise NotImplementedError("the time posterior of the relative-binning likelihood is not built")
 
     # ------------------------------------------------------------------
     # fiducial optimisation (relative.py:256-317)

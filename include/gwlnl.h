@@ -157,8 +157,11 @@ int gwl_inner_products_device(gwl_analysis *a, const double *params, int64_t B, 
  * 4/T FFT(h conj(d) / S)[j], j < L = n_frequencies - 1, summed over
  * detectors, interleaved complex ([B][2L] doubles), i.e. the
  * d_inner_h_array of base.py:325-330; h_inner_h[b] = <h|h>.  Needs time
- * marginalisation enabled and the full frequency grid (no relative binning,
- * multi-banding or ROQ).  Asynchronous on `stream`. */
+ * marginalisation enabled.  With relative binning the transform is of the
+ * rebuilt piecewise-linear waveform (relative.py:410-418), with multi-banding
+ * of the scattered banded strain times the linear coefficients, length
+ * Nbs[-1] / 2 (multiband.py:792-800); ROQ is refused.  Asynchronous on
+ * `stream`. */
 int gwl_time_series_device(gwl_analysis *a, const double *params, int64_t B, double *series, double *h_inner_h,
                            void *stream);
 

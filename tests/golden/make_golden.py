@@ -47,6 +47,10 @@ Outputs
     without and with marginalisation, and the draws of
     ``generate_posterior_sample_from_marginalized_likelihood`` with the
     shared generator seeded per point.
+``tests/golden/tf2_128s_fast_snrs.npz``
+    ``calculate_snrs`` and ``compute_per_detector_log_likelihood`` of the
+    reference's relative-binning and multi-banded likelihoods, without and
+    with time marginalisation.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -512,6 +516,75 @@ def run_snrs(bilby, name="tf2_marg_8s_2k", n_points=3):
     np.savez_compressed(os.path.join(HERE, f"{name}_snrs.npz"), **out)
 
 
+def run_fast_snrs(bilby, name="tf2_128s", n_points=2):
+    """calculate_snrs and compute_per_detector_log_likelihood of the
+    reference's relative-binning and multi-banded likelihoods, without and
+    with time marginalisation (the d_inner_h_array inside the prior window,
+    its sum and power)."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 11)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    for kind in ("relbin", "multiband"):
+        for combo in ("none", "t"):
+            ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+            t = combo == "t"
+            priors = make_priors(bilby, w, t, False, False)
+            if kind == "relbin":
+                wfg = bilby.gw.waveform_generator.WaveformGenerator(
+                    duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                    frequency_domain_source_model=taylorf2_aligned_relative_binning,
+                    waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+                fiducial = dict(w.injection, time_jitter=0.0) if t else dict(w.injection)
+                like = bilby.gw.likelihood.RelativeBinningGravitationalWaveTransient(
+                    interferometers=ifos, waveform_generator=wfg, fiducial_parameters=fiducial,
+                    priors=priors if t else None, time_marginalization=t)
+            else:
+                wfg = bilby.gw.waveform_generator.WaveformGenerator(
+                    duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                    frequency_domain_source_model=taylorf2_aligned_frequency_sequence,
+                    waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+                like = bilby.gw.likelihood.MBGravitationalWaveTransient(
+                    interferometers=ifos, waveform_generator=wfg, reference_chirp_mass=0.87,
+                    priors=priors if t else None, time_marginalization=t)
+            key = f"{kind}_{combo}"
+            dh = np.zeros((n_points, len(ifos)), complex)
+            hh = np.zeros((n_points, len(ifos)))
+            per_det = np.zeros((n_points, len(ifos)))
+            for i in range(n_points):
+                q = point(params, i)
+                if t:
+                    q["geocent_time"] = float(priors["geocent_time"]) + q["time_jitter"]
+                else:
+                    q.pop("time_jitter")
+                pols = wfg.frequency_domain_strain(dict(q))
+                for k, ifo in enumerate(ifos):
+                    snr = like.calculate_snrs(pols, ifo, parameters=dict(q))
+                    dh[i, k], hh[i, k] = snr.d_inner_h, snr.optimal_snr_squared
+                    if t:
+                        arr = np.asarray(snr.d_inner_h_array)
+                        times = like._times + q["time_jitter"]
+                        tp = like.priors["geocent_time"]
+                        idx = np.nonzero((times >= tp.minimum) & (times <= tp.maximum))[0]
+                        out[f"{key}_series_idx_{i}_{k}"] = idx
+                        out[f"{key}_series_{i}_{k}"] = arr[idx]
+                        out[f"{key}_series_len"] = len(arr)
+                        out.setdefault(f"{key}_series_sum", np.zeros((n_points, len(ifos)), complex))[i, k] = arr.sum()
+                        out.setdefault(f"{key}_series_power", np.zeros((n_points, len(ifos))))[i, k] = \
+                            np.sum(np.abs(arr) ** 2)
+                qq = dict(q)
+                if t:
+                    qq["geocent_time"] -= qq["time_jitter"]
+                res = like.compute_per_detector_log_likelihood(qq)
+                per_det[i] = [res[f"{ifo.name}_log_likelihood"] for ifo in ifos]
+            out[f"{key}_dh"] = dh
+            out[f"{key}_hh"] = hh
+            out[f"{key}_per_det_lnl"] = per_det
+            print(f"{name} {key}: per-detector SNRs done")
+    np.savez_compressed(os.path.join(HERE, f"{name}_fast_snrs.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -545,6 +618,7 @@ def main():
             os.chdir(tmp)
             try:
                 run_snrs(bilby)
+                run_fast_snrs(bilby)
             finally:
                 os.chdir(cwd)
         return
@@ -596,6 +670,7 @@ def main():
                 run_multiband(bilby, "tf2_128s", 8, 8)
                 run_roq(bilby)
                 run_snrs(bilby)
+                run_fast_snrs(bilby)
             finally:
                 os.chdir(cwd)
 

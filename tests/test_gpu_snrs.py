@@ -130,3 +130,69 @@ def test_unmarginalized_reconstruction_returns_parameters(gpu, tmp_path):
     like, priors = make_likelihood(w, "", "fp64", tmp_path / "table.npz")
     q = points(z, priors, "")[0]
     assert like.generate_posterior_sample_from_marginalized_likelihood(q) is q
+
+
+def fast_likelihood(kind, combo, tmp_path):
+    """The package's relative-binning or multi-banded likelihood on tf2_128s
+    (fiducial = the injection; reference chirp mass 0.87), as the golden
+    generator builds the reference's."""
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.relative import RelativeBinningGravitationalWaveTransient
+    from bilby_gb300.source import taylorf2_aligned_frequency_sequence, taylorf2_aligned_relative_binning
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    w = WORKLOADS["tf2_128s"]
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    model = taylorf2_aligned_relative_binning if kind == "relbin" else taylorf2_aligned_frequency_sequence
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=model,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+    tc = w.injection["geocent_time"]
+    t = combo == "t"
+    priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1)} if t else None
+    if kind == "relbin":
+        like = RelativeBinningGravitationalWaveTransient(ifos, wfg, fiducial_parameters=dict(w.injection),
+                                                         priors=priors, time_marginalization=t)
+    else:
+        like = MBGravitationalWaveTransient(ifos, wfg, reference_chirp_mass=0.87, priors=priors,
+                                            time_marginalization=t)
+    return like, priors
+
+
+@pytest.mark.parametrize("kind", ["relbin", "multiband"])
+@pytest.mark.parametrize("combo", ["none", "t"])
+def test_fast_likelihood_snrs_match_reference(gpu, tmp_path, kind, combo):
+    z = golden("tf2_128s_fast_snrs")
+    like, priors = fast_likelihood(kind, combo, tmp_path)
+    key = f"{kind}_{combo}"
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    names = [ifo.name for ifo in like.interferometers]
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if combo == "t":
+            q["geocent_time"] = float(priors["geocent_time"]) + q["time_jitter"]
+        else:
+            q.pop("time_jitter")
+        for k, ifo in enumerate(like.interferometers):
+            s = like.calculate_snrs(None, ifo, parameters=dict(q))
+            dh, hh = z[f"{key}_dh"][i, k], z[f"{key}_hh"][i, k]
+            scale = max(1.0, abs(dh), hh)
+            assert abs(s.d_inner_h - dh) <= 1e-9 * scale, (key, i, k)
+            assert abs(s.optimal_snr_squared - hh) <= 1e-9 * scale, (key, i, k)
+            if combo == "t":
+                arr = s.d_inner_h_array
+                assert len(arr) == int(z[f"{key}_series_len"])
+                win = z[f"{key}_series_{i}_{k}"]
+                assert np.max(np.abs(arr[z[f"{key}_series_idx_{i}_{k}"]] - win)) <= 1e-9 * max(1.0, np.max(np.abs(win)))
+                assert np.sum(np.abs(arr) ** 2) == pytest.approx(z[f"{key}_series_power"][i, k], rel=1e-9)
+        qq = dict(q)
+        if combo == "t":
+            qq["geocent_time"] -= qq["time_jitter"]
+        res = like.compute_per_detector_log_likelihood(qq)
+        got = [res[f"{n}_log_likelihood"] for n in names]
+        assert close(got, z[f"{key}_per_det_lnl"][i]), (key, i, got)
