@@ -483,7 +483,26 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
         return an
 
     def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
-        raise NotImplementedError("the time posterior of the multi-banded likelihood is not built")
+        """multiband.py:822-855: a draw from the time posterior on the
+        marginalisation grid, from the GPU's <d|h>(t) summed over detectors,
+        with numpy's global generator as the reference uses."""
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        total = self._CalculatedSNRs()
+        for ifo in self.interferometers:
+            total += self.calculate_snrs(signal_polarizations, ifo, parameters=parameters)
+        d_inner_h, h_inner_h = total.d_inner_h_array, total.optimal_snr_squared
+        if self.distance_marginalization:
+            lnl_t = self.distance_marginalized_likelihood(d_inner_h, h_inner_h, parameters=parameters)
+        elif self.phase_marginalization:
+            lnl_t = self.phase_marginalized_likelihood(d_inner_h, h_inner_h)
+        else:
+            lnl_t = d_inner_h.real - h_inner_h / 2
+        times = self._times
+        if self.jitter_time:
+            times = times + parameters["time_jitter"]
+        post = np.exp(lnl_t - np.max(lnl_t)) * self.priors["geocent_time"].prob(times)
+        post /= np.sum(post)
+        return np.random.choice(times, p=post)
 
     def _upload(self):
         names = [ifo.name for ifo in self.interferometers]

@@ -576,8 +576,12 @@ def run_fast_snrs(bilby, name="tf2_128s", n_points=2):
                 qq = dict(q)
                 if t:
                     qq["geocent_time"] -= qq["time_jitter"]
-                res = like.compute_per_detector_log_likelihood(qq)
+                res = like.compute_per_detector_log_likelihood(dict(qq))
                 per_det[i] = [res[f"{ifo.name}_log_likelihood"] for ifo in ifos]
+                if t and kind == "multiband":  # multiband.py:822-855 draws with numpy's global generator
+                    np.random.seed(RECON_SEED + i)
+                    out.setdefault(f"{key}_time_draw", np.zeros(n_points))[i] = \
+                        like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
             out[f"{key}_dh"] = dh
             out[f"{key}_hh"] = hh
             out[f"{key}_per_det_lnl"] = per_det

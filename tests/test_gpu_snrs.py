@@ -193,6 +193,11 @@ def test_fast_likelihood_snrs_match_reference(gpu, tmp_path, kind, combo):
         qq = dict(q)
         if combo == "t":
             qq["geocent_time"] -= qq["time_jitter"]
-        res = like.compute_per_detector_log_likelihood(qq)
+        res = like.compute_per_detector_log_likelihood(dict(qq))
         got = [res[f"{n}_log_likelihood"] for n in names]
         assert close(got, z[f"{key}_per_det_lnl"][i]), (key, i, got)
+        if kind == "multiband" and combo == "t":
+            # multiband.py:822-855: a grid time drawn with numpy's global generator
+            np.random.seed(RECON_SEED + i)
+            draw = like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
+            assert draw == z[f"{key}_time_draw"][i], (i, draw)
