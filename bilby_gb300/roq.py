@@ -229,7 +229,23 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         self.time_prior_array = tp.prob(self._times) * self._delta_tc
 
     def _detector_analysis(self, interferometer):
-        raise NotImplementedError("per-detector quantities of the ROQ likelihood are not built")
+        """A one-detector analysis with this detector's weights: calculate_snrs
+        then gives the ROQ inner products of roq.py:467-541 (without time
+        marginalisation; with it, not built)."""
+        if self.time_marginalization:
+            raise NotImplementedError("per-detector quantities of the time-marginalised ROQ likelihood are not built")
+        name = interferometer.name
+        an = self._detector_analyses.get(name)
+        if an is None:
+            names = [ifo.name for ifo in self.interferometers]
+            if name not in names:
+                raise ValueError(f"interferometer {name} is not part of this likelihood")
+            k = names.index(name)
+            an = self._new_analysis([self.interferometers[k]])
+            fl, fq, start, dt, wl, wq = self._roq
+            an.set_roq(True, fl, fq, start, dt, wl[k:k + 1], wq[k:k + 1])
+            self._detector_analyses[name] = an
+        return an
 
     def _upload(self):
         ts = np.asarray(self.weights["time_samples"], dtype=np.float64)

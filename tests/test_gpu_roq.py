@@ -124,3 +124,25 @@ def test_time_marginalized_with_many_nodes(gpu, tmp_path):
     single = np.array([big.log_likelihood_ratio(point(params, i)) for i in range(len(batch))])
     assert np.all(np.isfinite(batch))
     assert np.array_equal(single, batch)
+
+
+@pytest.mark.parametrize("combo", ["none", "pd"])
+def test_per_detector_snrs_sum_to_the_likelihood(gpu, tmp_path, combo):
+    """calculate_snrs per detector (one-detector analyses with that
+    detector's weights) summed and passed to compute_log_likelihood_from_snrs
+    equals the likelihood of the whole network."""
+    like, priors, z = make(combo, tmp_path)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    for i in range(4):
+        q = point(params, i)
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        total = like._CalculatedSNRs()
+        for ifo in like.interferometers:
+            total += like.calculate_snrs(None, ifo, parameters=dict(q))
+        lnl = like.compute_log_likelihood_from_snrs(total, dict(q))
+        ref = like.log_likelihood_ratio(dict(q))
+        rtol = 1e-8 if "d" in combo else 1e-9
+        assert abs(lnl - ref) <= rtol * max(1.0, abs(ref)), (i, lnl, ref)
