@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <map>
+#include <mutex>
 
 #include "gwl_device.cuh"
 #include "gwl_internal.h"
@@ -969,18 +971,25 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
 
 namespace {
 
-struct TwiddleCache {
-  int64_t L = 0;
+// exp(-2 pi i t / L), t < L / 2, in float64 and float32, one table per FFT
+// length, kept for the life of the process: analyses of different lengths
+// may launch at the same time from different host threads, so a table is
+// never replaced or freed while a kernel may read it.
+struct TwiddleTables {
   double2* d64 = nullptr;
   float2* d32 = nullptr;
 };
-TwiddleCache g_twiddle;
+std::mutex g_twiddle_mu;
+std::map<int64_t, TwiddleTables> g_twiddles;
 
-cudaError_t ensure_twiddles(int64_t L) {
-  if (g_twiddle.L == L) return cudaSuccess;
-  cudaFree(g_twiddle.d64);
-  cudaFree(g_twiddle.d32);
-  g_twiddle = TwiddleCache();
+cudaError_t twiddles_for(int64_t L, TwiddleTables* out) {
+  std::lock_guard<std::mutex> g(g_twiddle_mu);
+  auto it = g_twiddles.find(L);
+  if (it != g_twiddles.end()) {
+    *out = it->second;
+    return cudaSuccess;
+  }
+  TwiddleTables t;
   const int64_t H = L / 2;
   double2* h64 = new double2[H];
   float2* h32 = new float2[H];
@@ -990,14 +999,20 @@ cudaError_t ensure_twiddles(int64_t L) {
     h64[t] = make_double2(std::cos(ang), std::sin(ang));
     h32[t] = make_float2((float)h64[t].x, (float)h64[t].y);
   }
-  cudaError_t e = cudaMalloc(&g_twiddle.d64, H * sizeof(double2));
-  if (e == cudaSuccess) e = cudaMalloc(&g_twiddle.d32, H * sizeof(float2));
-  if (e == cudaSuccess) e = cudaMemcpy(g_twiddle.d64, h64, H * sizeof(double2), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(g_twiddle.d32, h32, H * sizeof(float2), cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMalloc(&t.d64, H * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc(&t.d32, H * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(t.d64, h64, H * sizeof(double2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(t.d32, h32, H * sizeof(float2), cudaMemcpyHostToDevice);
   delete[] h64;
   delete[] h32;
-  if (e == cudaSuccess) g_twiddle.L = L;
-  return e;
+  if (e != cudaSuccess) {
+    cudaFree(t.d64);
+    cudaFree(t.d32);
+    return e;
+  }
+  g_twiddles[L] = t;
+  *out = t;
+  return cudaSuccess;
 }
 
 int log2_exact(int64_t L) {
@@ -1021,7 +1036,7 @@ size_t time_marg_work_bytes(const LaunchArgs& a) {
 }
 
 template <int D>
-static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
+static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L, const TwiddleTables& tw) {
   if (a.precision == GWL_PRECISION_MIXED) {
     // the FFT buffer, then the distance spline's knots
     const size_t smem = (size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) +
@@ -1029,7 +1044,7 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
     cudaError_t e = cudaFuncSetAttribute(k_time_marg<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)a.B;
-    k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d32, log2L);
+    k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, tw.d32, log2L);
   } else {
     // relative binning: the edge ratios in shared memory
     const size_t smem = a.relbin ? (size_t)a.rb_edges * D * sizeof(double2) : 0;
@@ -1039,7 +1054,7 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L) {
       if (e != cudaSuccess) return e;
     }
     const unsigned grid = (unsigned)std::min<int64_t>(a.B, tm_grid_fp64());
-    k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, g_twiddle.d64, log2L);
+    k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, tw.d64, log2L);
   }
   return cudaGetLastError();
 }
@@ -1081,13 +1096,14 @@ cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
            200 * 1024 ||
                                              a.n_fft / 2 > (int64_t)kTmTwiddleRows * kTmTwiddleRows))
     return cudaErrorInvalidValue;
-  cudaError_t e = ensure_twiddles(a.n_fft);
+  TwiddleTables tw;
+  cudaError_t e = twiddles_for(a.n_fft, &tw);
   if (e != cudaSuccess) return e;
   switch (a.n_det) {
-    case 1: return launch_tm_d<1>(a, s, log2L);
-    case 2: return launch_tm_d<2>(a, s, log2L);
-    case 3: return launch_tm_d<3>(a, s, log2L);
-    default: return launch_tm_d<4>(a, s, log2L);
+    case 1: return launch_tm_d<1>(a, s, log2L, tw);
+    case 2: return launch_tm_d<2>(a, s, log2L, tw);
+    case 3: return launch_tm_d<3>(a, s, log2L, tw);
+    default: return launch_tm_d<4>(a, s, log2L, tw);
   }
 }
 

@@ -187,3 +187,39 @@ def test_mixed_time_marginalized_sine_gaussian(gpu, tmp_path):
     mixed = like.log_likelihood_ratio_batch(p, precision="mixed")
     fp64 = like.log_likelihood_ratio_batch(p, precision="fp64")
     assert np.all(np.abs(mixed - fp64) <= 1e-3 + 2e-8 * np.abs(fp64)), np.abs(mixed - fp64).max()
+
+
+def test_concurrent_analyses_of_different_fft_lengths(gpu, tmp_path):
+    """Two time-marginalised analyses of different FFT lengths (8192 and 4096)
+    evaluated at the same time from two host threads give the values they give
+    one after the other: each length keeps its own twiddle tables."""
+    import threading
+    from dataclasses import replace
+    w8 = WORKLOADS["tf2_marg_8s_2k"]
+    w4 = replace(w8, duration=4.0, start_time=w8.injection["geocent_time"] - 3.0)
+    likes = []
+    for w, sub in ((w8, "a"), (w4, "b")):
+        (tmp_path / sub).mkdir()
+        like, priors = make_likelihood(w, "tpd", "mixed", tmp_path / sub / "table.npz")
+        z = golden(w8.name)
+        params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+        params["geocent_time"] = np.full(len(params["mass_1"]), float(priors["geocent_time"]))
+        params["phase"] = np.zeros(len(params["mass_1"]))
+        params["luminosity_distance"] = np.full(len(params["mass_1"]), float(priors["luminosity_distance"]))
+        likes.append((like, params))
+    for precision in ("fp64", "mixed"):
+        alone = [like.log_likelihood_ratio_batch(p, precision=precision) for like, p in likes]
+        results = [[], []]
+
+        def work(k):
+            like, p = likes[k]
+            for _ in range(20):
+                results[k].append(like.log_likelihood_ratio_batch(p, precision=precision))
+
+        threads = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        for k in range(2):
+            assert all(np.array_equal(r, alone[k]) for r in results[k]), (precision, k)
