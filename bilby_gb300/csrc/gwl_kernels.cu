@@ -1637,17 +1637,17 @@ static int sm_count_k() {
 }
 
 // shared-memory limits and occupancies of the mixed TaylorF2 kernels, once
+// per process (a function-local static: initialised once even when several
+// host threads make their first launches at the same time)
 static cudaError_t configure_mixed() {
-  static bool configured = false;
-  if (!configured) {
+  static const cudaError_t status = [] {
     cudaError_t e;
     if ((e = set_mixed_smem<1>()) != cudaSuccess) return e;
     if ((e = set_mixed_smem<2>()) != cudaSuccess) return e;
     if ((e = set_mixed_smem<3>()) != cudaSuccess) return e;
-    if ((e = set_mixed_smem<4>()) != cudaSuccess) return e;
-    configured = true;
-  }
-  return cudaSuccess;
+    return set_mixed_smem<4>();
+  }();
+  return status;
 }
 
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
