@@ -638,15 +638,16 @@ class GravitationalWaveTransient(_Base):
         psd = np.ones(n_up)
         signal_long = np.zeros(n_up, dtype=complex)
         data = np.zeros(n_up, dtype=complex)
+        h_inner_h = np.zeros(1)
         for ifo in self.interferometers:
             n_ifo = len(ifo.frequency_domain_strain)
             mask = ifo.frequency_mask
-            signal_long[:n_ifo] = ifo.get_detector_response(signal_polarizations, parameters)
+            signal = self._compute_full_waveform(signal_polarizations, ifo, parameters)
+            signal_long[:n_ifo] = signal
             data[:n_ifo] = np.conj(ifo.frequency_domain_strain)
             psd[:n_ifo][mask] = ifo.power_spectral_density_array[mask]
             d_inner_h += np.fft.fft(signal_long * data / psd)[in_prior]
-        _, h_inner_h = self._calculate_inner_products(signal_polarizations, parameters)
-        h_inner_h = np.array([h_inner_h])
+            h_inner_h += ifo.optimal_snr_squared(signal=signal).real
         if self.distance_marginalization:
             lnl_t = self.distance_marginalized_likelihood(d_inner_h, h_inner_h, parameters=parameters)
         elif self.phase_marginalization:
@@ -658,6 +659,11 @@ class GravitationalWaveTransient(_Base):
         if np.sum(keep) < 3:
             keep[1:-1] = keep[1:-1] | keep[2:] | keep[:-2]
         return Interped(times[keep], post[keep]).sample()
+
+    def _compute_full_waveform(self, signal_polarizations, interferometer, parameters):
+        """base.py:718-732: the detector response on the full grid (the GPU's
+        response kernel for this package's interferometers)."""
+        return interferometer.get_detector_response(signal_polarizations, parameters)
 
     def generate_distance_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
         """base.py:655-705: the distance posterior on the lookup table's

@@ -248,8 +248,29 @@ class RelativeBinningGravitationalWaveTransient(GravitationalWaveTransient):
             self._detector_analyses[name] = an
         return an
 
-    def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
-        raise NotImplementedError("the time posterior of the relative-binning likelihood is not built")
+    def _compute_full_waveform(self, signal_polarizations, interferometer, parameters):
+        """relative.py:365-396: the fiducial response times the piecewise-linear
+        ratio r0_b + r1_b (f - f_b) on the grid between the first and last
+        edges.  The model and its response at the edges come from the float64
+        GPU kernels (explicit frequencies, no mask)."""
+        name = interferometer.name
+        block = self._snr_block(parameters)[:, 0]
+        fmin = self.waveform_generator.waveform_arguments.get("minimum_frequency", 20.0)
+        edges = np.asarray(self.bin_freqs, dtype=np.float64)
+        plus, cross = _capi.source_polarizations(self.analysis.model_id, edges, block, fmin)
+        geom = interferometer.geometry
+        strain = _capi.detector_response(name, geom.vertex, geom.detector_tensor,
+                                         interferometer.strain_data.start_time, np.ones(len(edges), dtype=bool),
+                                         edges, plus, cross, block)
+        ratio = strain / self.per_detector_fiducial_waveform_points[name]
+        r0 = (ratio[1:] + ratio[:-1]) / 2
+        r1 = (ratio[1:] - ratio[:-1]) / self.bin_widths
+        idxs = slice(int(self.bin_inds[0]), int(self.bin_inds[-1]) + 1)
+        f = np.asarray(interferometer.frequency_array)
+        full = np.zeros(len(f), dtype=complex)
+        full[idxs] = (np.repeat(r0, self.bin_sizes)
+                      + np.repeat(r1, self.bin_sizes) * (f[idxs] - np.repeat(self.bin_centers, self.bin_sizes)))
+        return self.per_detector_fiducial_waveforms[name] * full
 
     # ------------------------------------------------------------------
     # fiducial optimisation (relative.py:256-317)

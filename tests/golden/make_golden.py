@@ -582,6 +582,10 @@ def run_fast_snrs(bilby, name="tf2_128s", n_points=2):
                     np.random.seed(RECON_SEED + i)
                     out.setdefault(f"{key}_time_draw", np.zeros(n_points))[i] = \
                         like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
+                if t and kind == "relbin":  # base.py:577-653 with the piecewise waveform, bilby's generator
+                    bilby.core.utils.random.seed(RECON_SEED + i)
+                    out.setdefault(f"{key}_time_draw", np.zeros(n_points))[i] = \
+                        like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
             out[f"{key}_dh"] = dh
             out[f"{key}_hh"] = hh
             out[f"{key}_per_det_lnl"] = per_det

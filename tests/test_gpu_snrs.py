@@ -201,3 +201,9 @@ def test_fast_likelihood_snrs_match_reference(gpu, tmp_path, kind, combo):
             np.random.seed(RECON_SEED + i)
             draw = like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
             assert draw == z[f"{key}_time_draw"][i], (i, draw)
+        if kind == "relbin" and combo == "t":
+            # base.py:577-653 over the piecewise waveform of relative.py:380-396
+            from bilby_gb300 import random as grandom
+            grandom.seed(RECON_SEED + i)
+            draw = like.generate_time_sample_from_marginalized_likelihood(parameters=dict(qq))
+            assert abs(draw - z[f"{key}_time_draw"][i]) <= 1e-7, (i, draw)
