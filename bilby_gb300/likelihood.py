@@ -514,14 +514,16 @@ class GravitationalWaveTransient(_Base):
         an = self._detector_analysis(interferometer)
         block = self._snr_block(parameters)
         dh, hh = an.inner_products_host(block, "fp64")
-        d_inner_h, optimal_snr_squared = complex(dh[0]), float(hh[0])
+        # numpy scalars: <h|h> = 0 gives an infinite or NaN matched-filter SNR, as in the reference
+        d_inner_h, optimal_snr_squared = np.complex128(dh[0]), np.float64(hh[0])
         d_inner_h_array = None
         if return_array and self.time_marginalization:
             series, _ = an.time_series_host(block)
             d_inner_h_array = series[0]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            mf = d_inner_h / optimal_snr_squared ** 0.5
         return self._CalculatedSNRs(d_inner_h=d_inner_h, optimal_snr_squared=optimal_snr_squared,
-                                    complex_matched_filter_snr=d_inner_h / optimal_snr_squared ** 0.5,
-                                    d_inner_h_array=d_inner_h_array)
+                                    complex_matched_filter_snr=mf, d_inner_h_array=d_inner_h_array)
 
     def _setup_rho(self, d_inner_h, optimal_snr_squared, parameters):
         """base.py:879-885."""
