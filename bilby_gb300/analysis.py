@@ -149,6 +149,7 @@ class Analysis:
         _capi.check(self._lib.gwl_set_roq_time_marginalization(self._h, len(t), _capi.dptr(t), float(delta_tc),
                                                                float(antenna_time)),
                     "gwl_set_roq_time_marginalization")
+        self.time_fft_length = len(t)  # the length of its <d|h>(t) series
 
     def set_multiband_time_marginalization(self, n_fft: int, index_start, source, delta_tc: float,
                                            antenna_time: float):

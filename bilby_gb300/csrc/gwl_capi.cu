@@ -1460,10 +1460,6 @@ int gwl_inner_products_device(gwl_analysis* a, const double* params, int64_t B, 
     return GWL_ERR_ARGUMENT;
   }
   std::lock_guard<std::mutex> g(a->mu);
-  if (a->roq && a->roq_tm) {
-    set_error("per-point inner products are not available for ROQ with time marginalisation");
-    return GWL_ERR_UNSUPPORTED;
-  }
   const int saved = a->time_marg;
   a->time_marg = 0;
   const int rc = run_eval(a, params, B, precision, nullptr, d_inner_h, h_inner_h, static_cast<cudaStream_t>(stream));
@@ -1482,8 +1478,8 @@ int gwl_time_series_device(gwl_analysis* a, const double* params, int64_t B, dou
     set_error("gwl_time_series_device needs time marginalisation enabled");
     return GWL_ERR_ARGUMENT;
   }
-  if (a->roq) {
-    set_error("gwl_time_series_device serves the full grid, relative binning and multi-banding");
+  if (a->roq && !a->roq_tm) {
+    set_error("gwl_time_series_device needs the ROQ time-marginalisation grid (gwl_set_roq_time_marginalization)");
     return GWL_ERR_ARGUMENT;
   }
   if (B <= 0) return GWL_OK;

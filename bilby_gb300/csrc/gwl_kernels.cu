@@ -1292,7 +1292,7 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_roq(LaunchArgs a) {
   const PointRec& r = a.rec[i];
   double dr = 0.0, di = 0.0, hh = 0.0;
   if (r.valid) {
-    double fp[D], fx[D], ar[D][5], ai[D][5];
+    double fp[D], fx[D], ar[D][5], ai[D][5], tifo[D];
     int64_t row[D][5];
     bool inb[D];
     const double t0 = (double)a.roq_time_start * a.roq_dt;
@@ -1301,8 +1301,13 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_roq(LaunchArgs a) {
     for (int d = 0; d < D; ++d) {
       fp[d] = r.fp[d];
       fx[d] = r.fx[d];
+      // the detector's arrival time after the segment start: with time
+      // marginalisation dt holds the delay at the antenna time alone and the
+      // jitter enters only the time series (roq.py:529-541: geocent_time as
+      // given, minus the start, plus that delay)
+      tifo[d] = a.roq_tm ? (par(a, GWL_P_GEOCENT_TIME, i) - a.det[d].start_time) + r.dt[d] : r.dt[d];
       // roq.py:552-575: the five samples around the arrival time
-      const int64_t c = (int64_t)floor((r.dt[d] - t0) / step);
+      const int64_t c = (int64_t)floor((tifo[d] - t0) / step);
       inb[d] = c - 2 >= 0 && c + 2 < a.roq_n_time;
 #pragma unroll
       for (int m = 0; m < 5; ++m) {
@@ -1353,7 +1358,7 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_roq(LaunchArgs a) {
       const double ts0 = (double)(a.roq_time_start + row[d][0]) * a.roq_dt;
       const double ts1 = (double)(a.roq_time_start + row[d][1]) * a.roq_dt;
       const double ts3 = (double)(a.roq_time_start + row[d][3]) * a.roq_dt;
-      const double aa = (ts3 - r.dt[d]) / fmax(ts1 - ts0, 1e-12);
+      const double aa = (ts3 - tifo[d]) / fmax(ts1 - ts0, 1e-12);
       const double bb = 1.0 - aa;
       const double cc = (aa * aa * aa - aa) / 6.0, dd = (bb * bb * bb - bb) / 6.0;
       const double r1r = (-ar[d][0] + 8.0 * ar[d][1] - 14.0 * ar[d][2] + 8.0 * ar[d][3] - ar[d][4]) / 4.0;

@@ -853,6 +853,7 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
       }
     }
     const double hh = block_sum(hh_part, red);  // ends with a barrier: s_h is complete
+    if (a.tm_series && a.hh_out && threadIdx.x == 0) a.hh_out[i] = hh;
     const double sr = r.dist / a.ref_dist, hh_ref = hh * r.dist * r.dist / (a.ref_dist * a.ref_dist);
     const double prob = 1.0 / (a.t_max - a.t_min);
     double m = -INFINITY, acc = 0.0;
@@ -896,7 +897,8 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
       for (int64_t j = j0 + threadIdx.x; j <= j1; j += blockDim.x) {
         const double tj = a.roq_tm_times[j];
         const double t = tj + jit;
-        if (!(t >= a.t_min && t <= a.t_max)) continue;
+        const bool in_prior = t >= a.t_min && t <= a.t_max;
+        if (!in_prior && !a.tm_series) continue;
         double xr = 0.0, xi = 0.0;
         bool ok = true;
 #pragma unroll
@@ -918,6 +920,12 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
           const double r2r = c0.x - 2.0 * p1.x + p2.x, r2i = c0.y - 2.0 * p1.y + p2.y;
           xr += a1 * c0.x + b * p1.x + c * r1r + dd * r2r;
           xi += a1 * c0.y + b * p1.y + c * r1i + dd * r2i;
+        }
+        if (a.tm_series) {
+          // d_inner_h_array of roq.py:535-541 at every sample (NaN outside the weight grid)
+          reinterpret_cast<double2*>(a.tm_series)[(size_t)i * n + j] =
+              ok ? make_double2(xr, xi) : make_double2(NAN, NAN);
+          if (!in_prior) continue;
         }
         double l;
         if (!ok) {

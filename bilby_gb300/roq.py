@@ -229,11 +229,10 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         self.time_prior_array = tp.prob(self._times) * self._delta_tc
 
     def _detector_analysis(self, interferometer):
-        """A one-detector analysis with this detector's weights: calculate_snrs
-        then gives the ROQ inner products of roq.py:467-541 (without time
-        marginalisation; with it, not built)."""
-        if self.time_marginalization:
-            raise NotImplementedError("per-detector quantities of the time-marginalised ROQ likelihood are not built")
+        """A one-detector analysis with this detector's weights (and the
+        marginalisation grid): calculate_snrs then gives the ROQ inner
+        products of roq.py:467-541, with the five-sample <d|h>(t) series under
+        time marginalisation."""
         name = interferometer.name
         an = self._detector_analyses.get(name)
         if an is None:
@@ -242,10 +241,46 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
                 raise ValueError(f"interferometer {name} is not part of this likelihood")
             k = names.index(name)
             an = self._new_analysis([self.interferometers[k]])
+            if self.time_marginalization:
+                tp = self.priors["geocent_time"]
+                an.set_time_marginalization(True, self.jitter_time, tp.minimum, tp.maximum)
             fl, fq, start, dt, wl, wq = self._roq
             an.set_roq(True, fl, fq, start, dt, wl[k:k + 1], wq[k:k + 1])
+            if self._roq_tm is not None:
+                an.set_roq_time_marginalization(*self._roq_tm)
             self._detector_analyses[name] = an
         return an
+
+    def _snr_block(self, parameters):
+        """As the base class's, but the time jitter is kept: the ROQ time
+        series adds it to the detector times itself (roq.py:535-539)."""
+        from .analysis import params_block
+        converted, _ = self.waveform_generator.parameter_conversion(dict(parameters))
+        converted["time_jitter"] = parameters.get("time_jitter", 0.0) if self.time_marginalization else 0.0
+        return params_block(converted, 1)
+
+    def generate_time_sample_from_marginalized_likelihood(self, signal_polarizations=None, *, parameters):
+        """roq.py:1238-1271: a draw from the time posterior on the
+        marginalisation grid, from the GPU's <d|h>(t) summed over detectors,
+        with the package's shared generator."""
+        from .random import Generator
+        parameters.update(self.get_sky_frame_parameters(parameters))
+        total = self._CalculatedSNRs()
+        for ifo in self.interferometers:
+            total += self.calculate_snrs(signal_polarizations, ifo, parameters=parameters)
+        d_inner_h, h_inner_h = total.d_inner_h_array, total.optimal_snr_squared
+        if self.distance_marginalization:
+            lnl_t = self.distance_marginalized_likelihood(d_inner_h, h_inner_h, parameters=parameters)
+        elif self.phase_marginalization:
+            lnl_t = self.phase_marginalized_likelihood(d_inner_h, h_inner_h)
+        else:
+            lnl_t = d_inner_h.real - h_inner_h / 2
+        times = self._times
+        if self.jitter_time:
+            times = times + parameters["time_jitter"]
+        post = np.exp(np.asarray(lnl_t - np.max(lnl_t))) * np.asarray(self.priors["geocent_time"].prob(times))
+        post /= np.sum(post)
+        return Generator.rng.choice(times, p=post)
 
     def _upload(self):
         ts = np.asarray(self.weights["time_samples"], dtype=np.float64)

@@ -160,8 +160,9 @@ int gwl_inner_products_device(gwl_analysis *a, const double *params, int64_t B, 
  * marginalisation enabled.  With relative binning the transform is of the
  * rebuilt piecewise-linear waveform (relative.py:410-418), with multi-banding
  * of the scattered banded strain times the linear coefficients, length
- * Nbs[-1] / 2 (multiband.py:792-800); ROQ is refused.  Asynchronous on
- * `stream`. */
+ * Nbs[-1] / 2 (multiband.py:792-800); with ROQ the five-sample
+ * interpolation at each sample of the marginalisation grid, length n_times
+ * (roq.py:535-541, 604-651).  Asynchronous on `stream`. */
 int gwl_time_series_device(gwl_analysis *a, const double *params, int64_t B, double *series, double *h_inner_h,
                            void *stream);
 

@@ -51,6 +51,9 @@ Outputs
     ``calculate_snrs`` and ``compute_per_detector_log_likelihood`` of the
     reference's relative-binning and multi-banded likelihoods, without and
     with time marginalisation.
+``tests/golden/tf2_marg_8s_2k_roq_snrs.npz``
+    The same for the reference's ROQ likelihood (seeded synthetic basis),
+    with the time draw under time marginalisation.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -593,6 +596,65 @@ def run_fast_snrs(bilby, name="tf2_128s", n_points=2):
     np.savez_compressed(os.path.join(HERE, f"{name}_fast_snrs.npz"), **out)
 
 
+def run_roq_snrs(bilby, name="tf2_marg_8s_2k", n_points=2):
+    """calculate_snrs, compute_per_detector_log_likelihood and (with time
+    marginalisation) the time draw of the reference's ROQ likelihood with the
+    seeded synthetic basis of oracle/roq_basis.py; the d_inner_h_array is
+    stored for its first 400 samples, with its sum and power."""
+    from oracle import roq_basis
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 13)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in ("none", "t"):
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+        nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_roq,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency, frequency_nodes_linear=nl,
+                                    frequency_nodes_quadratic=nq))
+        t = combo == "t"
+        priors = make_priors(bilby, w, True, False, False)
+        like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, linear_matrix=bl.T,
+            quadratic_matrix=bq.T, time_marginalization=t)
+        key = f"roq_{combo}"
+        dh = np.zeros((n_points, len(ifos)), complex)
+        hh = np.zeros((n_points, len(ifos)))
+        per_det = np.zeros((n_points, len(ifos)))
+        for i in range(n_points):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+            else:
+                q.pop("time_jitter")
+            pols = wfg.frequency_domain_strain(dict(q))
+            for k, ifo in enumerate(ifos):
+                snr = like.calculate_snrs(pols, ifo, parameters=dict(q))
+                dh[i, k], hh[i, k] = snr.d_inner_h, snr.optimal_snr_squared
+                if t:
+                    arr = np.asarray(snr.d_inner_h_array)
+                    out[f"{key}_series_{i}_{k}"] = arr[:400]
+                    out[f"{key}_series_len"] = len(arr)
+                    out.setdefault(f"{key}_series_sum", np.zeros((n_points, len(ifos)), complex))[i, k] = arr.sum()
+                    out.setdefault(f"{key}_series_power", np.zeros((n_points, len(ifos))))[i, k] = \
+                        np.sum(np.abs(arr) ** 2)
+            res = like.compute_per_detector_log_likelihood(dict(q))
+            per_det[i] = [res[f"{ifo.name}_log_likelihood"] for ifo in ifos]
+            if t:  # roq.py:1238-1271 draws with bilby's generator
+                bilby.core.utils.random.seed(RECON_SEED + i)
+                out.setdefault(f"{key}_time_draw", np.zeros(n_points))[i] = \
+                    like.generate_time_sample_from_marginalized_likelihood(parameters=dict(q))
+        out[f"{key}_dh"] = dh
+        out[f"{key}_hh"] = hh
+        out[f"{key}_per_det_lnl"] = per_det
+        print(f"{name} {key}: per-detector SNRs done")
+    np.savez_compressed(os.path.join(HERE, f"{name}_roq_snrs.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -627,6 +689,7 @@ def main():
             try:
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
+                run_roq_snrs(bilby)
             finally:
                 os.chdir(cwd)
         return
@@ -679,6 +742,7 @@ def main():
                 run_roq(bilby)
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
+                run_roq_snrs(bilby)
             finally:
                 os.chdir(cwd)
 
