@@ -49,6 +49,30 @@ def _power_of_two_at_least(x):
     return 2 ** math.ceil(np.log2(x))
 
 
+def scatter_lists(full_index, start_end_idxs, n):
+    """For each full-resolution index k < n, the banded points scattered
+    there by multiband.py:794-798 (``full_d_h[idx[band]] += values[band]``,
+    band by band), as (index_start [n + 1], source): source codes j >= 0
+    contribute; within one band a later point at the same index replaces an
+    earlier one (numpy's buffered indexed +=), and the replaced point j is
+    listed as -j - 1 (it still enters <h|h>).  Across bands the values add, in
+    band order."""
+    full = np.asarray(full_index, dtype=np.int64)
+    if full.size and (full.min() < 0 or full.max() >= n):
+        raise ValueError("a banded frequency maps outside the time-marginalisation FFT")
+    code = np.arange(len(full), dtype=np.int64)
+    for s0, e0 in np.asarray(start_end_idxs):
+        seg = full[s0:e0 + 1]
+        _, last = np.unique(seg[::-1], return_index=True)
+        keep = np.zeros(len(seg), dtype=bool)
+        keep[len(seg) - 1 - last] = True
+        code[s0:e0 + 1][~keep] = -code[s0:e0 + 1][~keep] - 1
+    order = np.argsort(full, kind="stable")
+    ptr = np.zeros(n + 1, dtype=np.int64)
+    ptr[1:] = np.cumsum(np.bincount(full, minlength=n))
+    return ptr.astype(np.int32), code[order].astype(np.int32)
+
+
 class MBGravitationalWaveTransient(GravitationalWaveTransient):
     """Multi-banded likelihood on the GPU (bilby/gw/likelihood/multiband.py:99-130)."""
 
@@ -442,23 +466,8 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
         self._beam_pattern_reference_time = (tp.minimum + tp.maximum) / 2
         for ifo in self.interferometers:
             ifo.reference_time = self._beam_pattern_reference_time
-        full = np.asarray(self._full_to_multiband, dtype=np.int64)
-        if full.size and (full.min() < 0 or full.max() >= n):
-            raise ValueError("a banded frequency maps outside the time-marginalisation FFT")
-        # per band, a later point at the same index replaces an earlier one
-        # (numpy's buffered indexed +=); across bands the values add
-        code = np.arange(len(full), dtype=np.int64)
-        for s0, e0 in np.asarray(self.start_end_idxs):
-            seg = full[s0:e0 + 1]
-            _, last = np.unique(seg[::-1], return_index=True)
-            keep = np.zeros(len(seg), dtype=bool)
-            keep[len(seg) - 1 - last] = True
-            code[s0:e0 + 1][~keep] = -code[s0:e0 + 1][~keep] - 1
-        order = np.argsort(full, kind="stable")
-        ptr = np.zeros(n + 1, dtype=np.int64)
-        ptr[1:] = np.cumsum(np.bincount(full, minlength=n))
-        self._mb_tm = (n, ptr.astype(np.int32), code[order].astype(np.int32), float(self._delta_tc),
-                       float(self._beam_pattern_reference_time))
+        ptr, src = scatter_lists(self._full_to_multiband, self.start_end_idxs, n)
+        self._mb_tm = (n, ptr, src, float(self._delta_tc), float(self._beam_pattern_reference_time))
 
     def _detector_analysis(self, interferometer):
         """A one-detector analysis with this detector's coefficients (and the

@@ -92,3 +92,28 @@ def test_host_setup_reproduces_the_reference(mb):
         assert np.max(np.abs(lin - ref)) <= 1e-12 * np.max(np.abs(ref))
         quad, ref = like.quadratic_coeffs[d.name], weights[f"quadratic_coeffs_{q}"]
         assert np.max(np.abs(quad - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_scatter_lists_reproduce_numpy_indexed_add():
+    """The scatter lists of the time-marginalised multi-banding give, for
+    random values, what multiband.py:794-798's band-by-band indexed += gives,
+    duplicates within and across bands included."""
+    from bilby_gb300.multiband import scatter_lists
+    rng = np.random.default_rng(4)
+    n = 64
+    full = np.concatenate([rng.integers(0, 20, 30), rng.integers(10, 40, 25), rng.integers(30, 64, 40)])
+    bands = np.array([[0, 29], [30, 54], [55, 94]])
+    values = rng.standard_normal(len(full)) + 1j * rng.standard_normal(len(full))
+    ref = np.zeros(n, dtype=complex)
+    for s0, e0 in bands:
+        ref[full[s0:e0 + 1]] += values[s0:e0 + 1]
+    ptr, src = scatter_lists(full, bands, n)
+    got = np.zeros(n, dtype=complex)
+    for k in range(n):
+        for c in src[ptr[k]:ptr[k + 1]]:
+            if c >= 0:
+                got[k] += values[c]
+    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=1e-14)
+    # every banded point listed exactly once (replaced ones as -j - 1)
+    decoded = np.where(src >= 0, src, -src - 1)
+    assert np.array_equal(np.sort(decoded), np.arange(len(full)))
