@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving run")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the serving run")
     ap.add_argument("--n-analyses", type=int, default=64)
+    ap.add_argument("--serve-streams", type=int, default=3, help="serving steps in flight")
+    ap.add_argument("--serve-max-points", type=int, default=1 << 15, help="points per serving step at most")
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
     ap.add_argument("--no-multiband", action="store_true", help="skip the multi-banding workload")
@@ -525,14 +527,14 @@ def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
             "setup_s_incl_distance_table": setup_s}
 
 
-def bench_serving(likes, ws, seconds, capacity, n_clients=200, seed=23):
+def bench_serving(likes, ws, seconds, capacity, n_clients=200, seed=23, n_streams=3, max_points=1 << 15):
     """200 clients with Poisson arrivals (rate for ~80% load), batches
     log-uniform in [64, 8192] points from the analyses above."""
     from bilby_gb300.analysis import params_block
     from bilby_gb300.serving import LikelihoodServer
     from bilby_gb300.workloads import draw_points
     rng = np.random.default_rng(seed)
-    srv = LikelihoodServer(hbm_budget_bytes=160e9, max_points_per_step=1 << 16, n_streams=2)
+    srv = LikelihoodServer(hbm_budget_bytes=160e9, max_points_per_step=max_points, n_streams=n_streams)
     for q, lk in enumerate(likes):
         srv.add_analysis(q, lk)
     mean_b = (8192 - 64) / math.log(128)
@@ -763,7 +765,8 @@ def run_ours(args, rank, world, local):
         ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
         uneven = bench_uneven(ulikes, uws, max(3, args.steps // 2), args.warmup)
         if not args.no_serving:
-            served = bench_serving(ulikes, uws, args.serve_seconds, uneven["value"])
+            served = bench_serving(ulikes, uws, args.serve_seconds, uneven["value"], n_streams=args.serve_streams,
+                                   max_points=args.serve_max_points)
         if args.no_uneven:
             uneven = None
 

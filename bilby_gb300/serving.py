@@ -155,7 +155,7 @@ class GpuBackend:
 
 
 class LikelihoodServer:
-    def __init__(self, hbm_budget_bytes: float = 160e9, max_points_per_step: int = 1 << 16, n_streams: int = 2,
+    def __init__(self, hbm_budget_bytes: float = 160e9, max_points_per_step: int = 1 << 15, n_streams: int = 3,
                  backend=None, precision: str = "mixed", use_graphs: bool = False, poll_s: float = 5e-5):
         self.budget = float(hbm_budget_bytes)
         self.max_points = int(max_points_per_step)
