@@ -564,7 +564,8 @@ def bench_serving(likes, ws, seconds, capacity, n_clients=200, seed=23, n_stream
     srv.stop()
     out = srv.stats.summary()
     out.update({"clients": n_clients, "arrival_rate_per_s": rate, "target_load": 0.8,
-                "batch": "log-uniform [64, 8192]", "streams": 2, "hbm_budget_gb": 160})
+                "batch": "log-uniform [64, 8192]", "streams": n_streams, "max_points_per_step": max_points,
+                "hbm_budget_gb": 160})
     return out
 
 
