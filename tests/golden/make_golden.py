@@ -54,6 +54,9 @@ Outputs
 ``tests/golden/tf2_marg_8s_2k_roq_snrs.npz``
     The same for the reference's ROQ likelihood (seeded synthetic basis),
     with the time draw under time marginalisation.
+``tests/golden/sg_4s_marg.npz``
+    The reference's time- and time+phase-marginalised likelihood for the
+    sine-Gaussian workload.
 ``tests/golden/tf2_128s_relbin.npz``
     The reference's ``RelativeBinningGravitationalWaveTransient`` on tf2_128s
     (fiducial = the injection): its bin edges, summary data and lnL ratios
@@ -655,6 +658,33 @@ def run_roq_snrs(bilby, name="tf2_marg_8s_2k", n_points=2):
     np.savez_compressed(os.path.join(HERE, f"{name}_roq_snrs.npz"), **out)
 
 
+def run_sg_marginalised(bilby, name="sg_4s", n_points=16):
+    """The reference's time- and time+phase-marginalised likelihood for the
+    sine-Gaussian burst (no distance parameter, so no distance
+    marginalisation)."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 17)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in ("t", "tp"):
+        ifos, wfg = build_reference(bilby, w, bilby.gw.source.sinegaussian)
+        priors = make_priors(bilby, w, True, "p" in combo, False)
+        like = bilby.gw.likelihood.GravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, time_marginalization=True,
+            phase_marginalization="p" in combo)
+        vals = []
+        for i in range(n_points):
+            q = point(params, i)
+            q["geocent_time"] = float(priors["geocent_time"])
+            if "p" in combo:
+                q["phase"] = 0.0
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name}[{combo}] done")
+    np.savez_compressed(os.path.join(HERE, f"{name}_marg.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -690,6 +720,7 @@ def main():
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
                 run_roq_snrs(bilby)
+                run_sg_marginalised(bilby)
             finally:
                 os.chdir(cwd)
         return
@@ -743,6 +774,7 @@ def main():
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
                 run_roq_snrs(bilby)
+                run_sg_marginalised(bilby)
             finally:
                 os.chdir(cwd)
 

@@ -223,3 +223,43 @@ def test_concurrent_analyses_of_different_fft_lengths(gpu, tmp_path):
             t.join()
         for k in range(2):
             assert all(np.array_equal(r, alone[k]) for r in results[k]), (precision, k)
+
+
+@pytest.mark.parametrize("combo", ["t", "tp"])
+def test_sine_gaussian_marginalized_vs_reference_golden(gpu, tmp_path, combo):
+    """The sine-Gaussian burst with time (and phase) marginalisation against
+    the reference's values (tests/golden/sg_4s_marg.npz).  float64: 1e-8
+    relative; mixed: 1e-3 + 2e-8 |lnL| (float32 terms of templates far louder
+    than the data, as in the plain sine-Gaussian tests)."""
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.source import sinegaussian
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    w = WORKLOADS["sg_4s"]
+    z = golden("sg_4s_marg")
+    for precision in ("fp64", "mixed"):
+        grandom.seed(w.seed)
+        ifos = InterferometerList(list(w.detectors))
+        ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+        wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency,
+                                start_time=w.start_time, frequency_domain_source_model=sinegaussian)
+        ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
+        tc = w.injection["geocent_time"]
+        priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1)}
+        if "p" in combo:
+            priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
+        like = GravitationalWaveTransient(ifos, wfg, priors=priors, time_marginalization=True,
+                                          phase_marginalization="p" in combo, precision=precision)
+        params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+        n = len(params["hrss"])
+        params["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+        if "p" in combo:
+            params["phase"] = np.zeros(n)
+        got = like.log_likelihood_ratio_batch(params)
+        ref = z["lnl_" + combo]
+        if precision == "fp64":
+            assert np.all(np.abs(got - ref) <= 1e-8 * np.maximum(1.0, np.abs(ref))), got - ref
+        else:
+            assert np.all(np.abs(got - ref) <= 1e-3 + 2e-8 * np.abs(ref)), got - ref
