@@ -263,3 +263,39 @@ def test_sine_gaussian_marginalized_vs_reference_golden(gpu, tmp_path, combo):
             assert np.all(np.abs(got - ref) <= 1e-8 * np.maximum(1.0, np.abs(ref))), got - ref
         else:
             assert np.all(np.abs(got - ref) <= 1e-3 + 2e-8 * np.abs(ref)), got - ref
+
+
+@pytest.mark.parametrize("combo", ["t", "d"])
+def test_time_and_distance_marginalization_vs_brute_force(gpu, tmp_path, combo):
+    """The pattern of the reference's marginalization_test.py:383-430: the
+    marginalised lnL equals the log of the prior-weighted sum of the plain
+    likelihood over a grid of the marginalised parameter (time: the
+    marginalisation's own time samples; distance: the lookup table's
+    distance grid), to the reference's delta of 0.5 (the plain likelihood on
+    the time grid also moves the antenna patterns with the time)."""
+    from scipy.special import logsumexp
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    plain, _ = make_likelihood(w, "", "fp64", tmp_path / "t0.npz")
+    marg, priors = make_likelihood(w, combo, "fp64", tmp_path / "t1.npz")
+    z = golden(w.name)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    params.pop("time_jitter")
+    params = {k: np.r_[v[:4], w.injection[k]] for k, v in params.items()}
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if combo == "t":
+            tp = marg.priors["geocent_time"]
+            times = marg._times[(marg._times >= tp.minimum) & (marg._times <= tp.maximum)]
+            grid = {k: np.full(len(times), v) for k, v in q.items()}
+            grid["geocent_time"] = times
+            brute = logsumexp(plain.log_likelihood_ratio_batch(grid), b=tp.prob(times) * marg._delta_tc)
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = 0.0
+        else:
+            dist = marg._distance_array
+            grid = {k: np.full(len(dist), v) for k, v in q.items()}
+            grid["luminosity_distance"] = dist
+            brute = logsumexp(plain.log_likelihood_ratio_batch(grid), b=marg.distance_prior_array * marg._delta_distance)
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        got = marg.log_likelihood_ratio(q)
+        assert abs(got - brute) < 0.5, (combo, i, got, brute)
