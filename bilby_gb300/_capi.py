@@ -72,6 +72,10 @@ SIGNATURES = {
     "gwl_eval_host": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int64, ctypes.c_int32, c_double_p]),
     "gwl_eval_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                                ctypes.c_void_p]),
+    "gwl_noalloc_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gwl_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.POINTER(ctypes.c_int)]),
+    "gwl_inject_device_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "gwl_inner_products_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "gwl_time_series_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

@@ -1883,6 +1883,42 @@ int gwl_batcher_last_refined(gwl_batcher* b, void* stream, int64_t* count) {
   return GWL_OK;
 }
 
+int gwl_selftest_bounded_wait(uint32_t poll_limit, void* stream, int* device_status, int* arrived) {
+  if (!device_status || !arrived || poll_limit == 0) {
+    set_error("null argument or zero poll limit");
+    return GWL_ERR_ARGUMENT;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* d = nullptr;
+  GWL_CUDA(cudaMalloc(&d, 2 * sizeof(int)));
+  cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(int), s);
+  if (e == cudaSuccess) e = launch_wait_selftest(poll_limit, d, d + 1, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(device_status, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(arrived, d + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error(std::string("gwl_selftest_bounded_wait: ") + cudaGetErrorString(e));
+    return GWL_ERR_CUDA;
+  }
+  if (*device_status == kDevStatusTimeout) {
+    set_error("a bounded device wait gave up (bulk copy did not complete)");
+    return GWL_ERR_TIMEOUT;
+  }
+  return GWL_OK;
+}
+
+int gwl_inject_device_status(gwl_analysis* a, int value) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  GWL_CUDA(cudaMemcpyAsync(a->d_status, &value, sizeof(int), cudaMemcpyHostToDevice, a->stream));
+  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  return GWL_OK;
+}
+
 int gwl_batcher_status(gwl_batcher* b, int* device_status) {
   if (!b || !device_status) {
     set_error("null argument");

@@ -262,6 +262,7 @@ cudaError_t launch_detector_response(const DetGeom& g, const double* freq, int64
 cudaError_t launch_distance_table(const double* dh_axis, int n_dh, const double* hh_axis, int n_hh,
                                   const double* scaling, const double* scaling2, const double* weight, int n,
                                   double* lni0_work, int phase, double log_norm, double* table);
+cudaError_t launch_wait_selftest(uint32_t limit, int* status, int* arrived, cudaStream_t s);
 
 void set_error(const std::string& msg);
 int noalloc_launch_args(gwl_analysis* a, int64_t B, LaunchArgs* L, size_t* rec_bytes, size_t* part_bytes);

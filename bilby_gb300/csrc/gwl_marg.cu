@@ -22,6 +22,7 @@
 #include <mutex>
 
 #include "gwl_device.cuh"
+#include "gwl_device_cache.h"
 #include "gwl_internal.h"
 #include "gwl_math.cuh"
 
@@ -979,48 +980,45 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
 
 namespace {
 
-// exp(-2 pi i t / L), t < L / 2, in float64 and float32, one table per FFT
-// length, kept for the life of the process: analyses of different lengths
-// may launch at the same time from different host threads, so a table is
-// never replaced or freed while a kernel may read it.
+// exp(-2 pi i t / L), t < L / 2, in float64 and float32, one table per
+// (device, FFT length), kept for the life of the process: analyses of
+// different lengths may launch at the same time from different host threads,
+// so a table is never replaced or freed while a kernel may read it, and the
+// tables of one device are never handed to a launch on another.
 struct TwiddleTables {
   double2* d64 = nullptr;
   float2* d32 = nullptr;
 };
-std::mutex g_twiddle_mu;
-std::map<int64_t, TwiddleTables> g_twiddles;
+PerDeviceCache<TwiddleTables> g_twiddles;
 
 cudaError_t twiddles_for(int64_t L, TwiddleTables* out) {
-  std::lock_guard<std::mutex> g(g_twiddle_mu);
-  auto it = g_twiddles.find(L);
-  if (it != g_twiddles.end()) {
-    *out = it->second;
-    return cudaSuccess;
-  }
-  TwiddleTables t;
-  const int64_t H = L / 2;
-  double2* h64 = new double2[H];
-  float2* h32 = new float2[H];
-  for (int64_t t = 0; t < H; ++t) {
-    // exp(-2 pi i t / L), argument reduced to an exact rational of pi
-    const double ang = -2.0 * 3.141592653589793 * (double)t / (double)L;
-    h64[t] = make_double2(std::cos(ang), std::sin(ang));
-    h32[t] = make_float2((float)h64[t].x, (float)h64[t].y);
-  }
-  cudaError_t e = cudaMalloc(&t.d64, H * sizeof(double2));
-  if (e == cudaSuccess) e = cudaMalloc(&t.d32, H * sizeof(float2));
-  if (e == cudaSuccess) e = cudaMemcpy(t.d64, h64, H * sizeof(double2), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(t.d32, h32, H * sizeof(float2), cudaMemcpyHostToDevice);
-  delete[] h64;
-  delete[] h32;
-  if (e != cudaSuccess) {
-    cudaFree(t.d64);
-    cudaFree(t.d32);
-    return e;
-  }
-  g_twiddles[L] = t;
-  *out = t;
-  return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const int rc = g_twiddles.get(dev, L, out, [L](TwiddleTables* t) -> int {
+    const int64_t H = L / 2;
+    double2* h64 = new double2[H];
+    float2* h32 = new float2[H];
+    for (int64_t q = 0; q < H; ++q) {
+      // exp(-2 pi i q / L), argument reduced to an exact rational of pi
+      const double ang = -2.0 * 3.141592653589793 * (double)q / (double)L;
+      h64[q] = make_double2(std::cos(ang), std::sin(ang));
+      h32[q] = make_float2((float)h64[q].x, (float)h64[q].y);
+    }
+    cudaError_t err = cudaMalloc(&t->d64, H * sizeof(double2));
+    if (err == cudaSuccess) err = cudaMalloc(&t->d32, H * sizeof(float2));
+    if (err == cudaSuccess) err = cudaMemcpy(t->d64, h64, H * sizeof(double2), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(t->d32, h32, H * sizeof(float2), cudaMemcpyHostToDevice);
+    delete[] h64;
+    delete[] h32;
+    if (err != cudaSuccess) {
+      cudaFree(t->d64);
+      cudaFree(t->d32);
+      return (int)err;
+    }
+    return 0;
+  });
+  return static_cast<cudaError_t>(rc);
 }
 
 int log2_exact(int64_t L) {

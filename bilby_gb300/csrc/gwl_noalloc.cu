@@ -19,6 +19,8 @@
 // before any stream capture.  All calls share the buffer, which keeps the
 // contents of the last call: calls whose launches overlap on the GPU (two
 // streams, two threads) race on it and must be serialised by the caller.
+// The kernels' status word (a bounded wait that gave up, an ordering key out
+// of range) lives in the buffer too; gwl_noalloc_status reads and clears it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -119,4 +121,43 @@ extern "C" int gwl_eval_device_noalloc(gwl_analysis* a, const double* params, in
     return GWL_ERR_CUDA;
   }
   return GWL_OK;
+}
+
+extern "C" int gwl_noalloc_status(void* stream, int* device_status) {
+  if (!device_status) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  *device_status = kDevStatusOk;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    set_error(std::string("gwl_noalloc_status: no usable current device: ") + cudaGetErrorString(e));
+    return GWL_ERR_CUDA;
+  }
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    base = g_scratch_ptr[dev];
+  }
+  if (!base) return GWL_OK;  // no call on this device yet
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int word = 0;
+  if ((e = cudaMemcpyAsync(&word, base, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    set_error(std::string("gwl_noalloc_status: ") + cudaGetErrorString(e));
+    return GWL_ERR_CUDA;
+  }
+  *device_status = word;
+  if (word == kDevStatusOk) return GWL_OK;
+  if ((e = cudaMemsetAsync(base, 0, sizeof(int), s)) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    set_error(std::string("gwl_noalloc_status: ") + cudaGetErrorString(e));
+    return GWL_ERR_CUDA;
+  }
+  if (word == kDevStatusTimeout) {
+    set_error("gwl_eval_device_noalloc: a bounded device wait gave up (bulk copy did not complete)");
+    return GWL_ERR_TIMEOUT;
+  }
+  set_error("gwl_eval_device_noalloc: a point's ordering key was out of range");
+  return GWL_ERR_ARGUMENT;
 }

@@ -153,4 +153,23 @@ cudaError_t launch_distance_table(const double* dh_axis, int n_dh, const double*
   return cudaDeviceSynchronize();
 }
 
+// Self-test of the bounded bulk-copy wait used by the likelihood kernels: one
+// thread arms an mbarrier for 16 bytes of transaction and issues no copy, so
+// the phase can never complete; mbar_wait_bounded gives up after `limit`
+// polls and records kDevStatusTimeout.  Nothing is in flight when the CTA
+// returns.  `arrived` receives 1 if the wait (impossibly) completed.
+__global__ void k_wait_selftest(uint32_t limit, int* status, int* arrived) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  mbar_fence_init();
+  mbar_expect_tx(&bar, 16);
+  *arrived = mbar_wait_bounded(&bar, 0, status, limit) ? 1 : 0;
+}
+
+cudaError_t launch_wait_selftest(uint32_t limit, int* status, int* arrived, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(limit, status, arrived);
+  return cudaGetLastError();
+}
+
 }  // namespace gwl

@@ -54,6 +54,15 @@ def _is_fixed(prior):
 
 N_DISTANCE_GRID = 10000  # base.py:210-212
 
+# parameters the fused kernels read for each source model: the source model's
+# own arguments (bilby/gw/source.py:1153 for the sine-Gaussian) and the
+# projection's sky position, polarisation angle and time (interferometer.py:303-368)
+_PROJECTION = ("ra", "dec", "psi", "geocent_time")
+REQUIRED_PARAMETERS = {
+    "sinegaussian": ("hrss", "Q", "frequency") + _PROJECTION,
+    "taylorf2": ("mass_1", "mass_2", "chi_1", "chi_2", "luminosity_distance", "theta_jn", "phase") + _PROJECTION,
+}
+
 
 def d_inner_h_ref_axis(n, phase_marginalization):
     """base.py:904-914."""
@@ -362,12 +371,28 @@ class GravitationalWaveTransient(_Base):
         return dict(ra=ra, dec=dec, geocent_time=geocent_time)
 
     def _prepare(self, parameters: dict) -> dict:
+        """Sky frame, the waveform generator's parameter conversion and the
+        time jitter (base.py:419-446, waveform_generator.py:260-269); raises
+        ``KeyError`` when a parameter the source model or the projection needs
+        is still missing after conversion, as the reference's source call does."""
         p = dict(parameters)
         p.update(self.get_sky_frame_parameters(p))
         converted, _ = self.waveform_generator.parameter_conversion(dict(p))
         if self.time_marginalization and self.jitter_time:
             converted["time_jitter"] = p.get("time_jitter", 0.0)
+        missing = [k for k in REQUIRED_PARAMETERS[self._model] if converted.get(k) is None]
+        if missing:
+            raise KeyError(f"parameters missing after conversion: {missing}")
         return converted
+
+    def parameters_block(self, parameters) -> np.ndarray:
+        """The [NPARAM, B] float64 block the kernels read, from a sampler's
+        parameter dictionary (scalars or equal-length arrays), after the same
+        preparation as ``log_likelihood_ratio``.  The caller's dictionary is
+        not modified."""
+        arrays = {k: (np.asarray(v, dtype=np.float64) if not isinstance(v, str) else v)
+                  for k, v in copy.deepcopy(dict(parameters)).items()}
+        return params_block(self._prepare(arrays))
 
     def log_likelihood_ratio(self, parameters):
         """base.py:419-446 for one point: a batch of size one on the GPU."""

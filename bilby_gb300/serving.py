@@ -163,6 +163,7 @@ class LikelihoodServer:
         self.backend = backend if backend is not None else GpuBackend(n_streams, precision, use_graphs)
         self.poll_s = poll_s
         self.analyses: dict = {}
+        self.likelihoods: dict = {}
         self.resident = 0
         self.pending: deque = deque()
         self.inflight: list = []
@@ -175,7 +176,9 @@ class LikelihoodServer:
     # -- analyses ----------------------------------------------------------
     def add_analysis(self, key, analysis):
         """Register a device-resident analysis (an ``Analysis`` or a likelihood
-        holding one); refused with AdmissionError beyond the HBM budget."""
+        holding one); refused with AdmissionError beyond the HBM budget.  A
+        likelihood also serves sampler parameter dictionaries
+        (``submit_parameters``) and its noise log-likelihood."""
         an = getattr(analysis, "analysis", analysis)
         size = self.backend.resident_bytes(an)
         with self.cv:
@@ -185,12 +188,31 @@ class LikelihoodServer:
                 raise AdmissionError(f"analysis {key!r} ({size / 1e9:.3f} GB) does not fit in the "
                                      f"{self.budget / 1e9:.1f} GB budget ({self.resident / 1e9:.3f} GB resident)")
             self.analyses[key] = an
+            self.likelihoods[key] = analysis if hasattr(analysis, "parameters_block") else None
             self.resident += size
 
     def remove_analysis(self, key):
         with self.cv:
             an = self.analyses.pop(key)
+            self.likelihoods.pop(key, None)
             self.resident -= self.backend.resident_bytes(an)
+
+    def _likelihood(self, key):
+        if key not in self.analyses:
+            raise KeyError(f"unknown analysis {key!r}")
+        like = self.likelihoods.get(key)
+        if like is None:
+            raise TypeError(f"analysis {key!r} was registered without a likelihood: send packed parameter blocks")
+        return like
+
+    def noise_log_likelihood(self, key) -> float:
+        """The noise log-likelihood of a registered analysis (base.py:413-417)."""
+        like = self.likelihoods.get(key)
+        if like is not None:
+            return float(like.noise_log_likelihood())
+        if key not in self.analyses:
+            raise KeyError(f"unknown analysis {key!r}")
+        return float(self.analyses[key].noise_log_likelihood())
 
     # -- requests ----------------------------------------------------------
     def submit(self, key, block, client=None) -> cf.Future:
@@ -215,6 +237,22 @@ class LikelihoodServer:
             self.pending.append(req)
             self.cv.notify()
         return fut
+
+    def submit_parameters(self, key, parameters, client=None) -> cf.Future:
+        """Queue a sampler's parameter dictionary (scalars or equal-length
+        arrays) for a registered likelihood.  The likelihood's own preparation
+        runs first (sky frame, parameter conversion, time jitter), so the
+        result equals its ``log_likelihood_ratio`` / ``log_likelihood_ratio_batch``;
+        a dictionary that lacks a needed parameter fails with ``KeyError``."""
+        try:
+            block = self._likelihood(key).parameters_block(parameters)
+        except Exception as e:
+            fut: cf.Future = cf.Future()
+            fut.set_exception(e)
+            with self.cv:
+                self.stats.failed += 1
+            return fut
+        return self.submit(key, block, client)
 
     def cancel_client(self, client):
         """Drop the queued requests of a client that went away (their futures are cancelled)."""
@@ -333,8 +371,14 @@ class LikelihoodServer:
 # ---------------------------------------------------------------------------
 def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
     """Accept client processes on ``address`` (a Unix socket path or
-    (host, port)); each connection sends ``("eval", key, block)`` messages and
-    receives ``("ok", results)`` or ``("error", message)``.  Returns the
+    (host, port)).  Each connection sends one of
+
+    * ``("eval", key, block)``: a packed [NPARAM, B] block;
+    * ``("eval_parameters", key, parameters)``: a sampler's dictionary,
+      prepared by the registered likelihood (``submit_parameters``);
+    * ``("noise", key, None)``: the analysis's noise log-likelihood;
+
+    and receives ``("ok", results)`` or ``("error", message)``.  Returns the
     listener (close it to stop accepting)."""
     from multiprocessing.connection import Listener
     listener = Listener(address, authkey=authkey)
@@ -344,10 +388,19 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
         try:
             while True:
                 msg = conn.recv()
-                if not isinstance(msg, tuple) or len(msg) != 3 or msg[0] != "eval":
+                if not isinstance(msg, tuple) or len(msg) != 3 or msg[0] not in ("eval", "eval_parameters", "noise"):
                     conn.send(("error", "malformed message"))
                     continue
-                fut = server.submit(msg[1], msg[2], client=token)
+                if msg[0] == "noise":
+                    try:
+                        conn.send(("ok", server.noise_log_likelihood(msg[1])))
+                    except Exception as e:
+                        conn.send(("error", f"{type(e).__name__}: {e}"))
+                    continue
+                if msg[0] == "eval":
+                    fut = server.submit(msg[1], msg[2], client=token)
+                else:
+                    fut = server.submit_parameters(msg[1], msg[2], client=token)
                 try:
                     conn.send(("ok", fut.result()))
                 except Exception as e:
@@ -370,13 +423,20 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
 
 
 class ServedLikelihood:
-    """A sampler-side likelihood that sends each call to the serving process:
-    ``log_likelihood_ratio(parameters)`` evaluates one point,
-    ``log_likelihood_ratio_batch(params)`` a batch (dict of arrays)."""
+    """A sampler-side likelihood that sends each call to the serving process.
 
-    def __init__(self, address, key, noise_log_likelihood: float = 0.0, authkey: bytes = b"gwlnl"):
+    ``log_likelihood_ratio(parameters)`` evaluates one point and
+    ``log_likelihood_ratio_batch(parameters)`` a batch (a dict of equal-length
+    arrays).  The server prepares the dictionary with the registered
+    likelihood (sky frame, parameter conversion, time jitter), so any
+    parameter set the direct ``GravitationalWaveTransient`` accepts (e.g.
+    ``chirp_mass`` / ``mass_ratio``) gives the same result here, and a set
+    that lacks a needed parameter raises.  ``noise_log_likelihood()`` is the
+    server's value for the analysis, fetched once."""
+
+    def __init__(self, address, key, authkey: bytes = b"gwlnl"):
         self.address, self.key, self.authkey = address, key, authkey
-        self._noise = noise_log_likelihood
+        self._noise = None
         self._conn = None
 
     def _connection(self):
@@ -390,20 +450,27 @@ class ServedLikelihood:
         st["_conn"] = None
         return st
 
-    def log_likelihood_ratio_batch(self, params) -> np.ndarray:
-        from .analysis import params_block
+    def _call(self, kind, payload):
         conn = self._connection()
-        conn.send(("eval", self.key, params_block(params)))
-        status, payload = conn.recv()
+        conn.send((kind, self.key, payload))
+        status, result = conn.recv()
         if status != "ok":
-            raise RuntimeError(payload)
-        return payload
+            if result.startswith("KeyError"):
+                raise KeyError(result)
+            raise RuntimeError(result)
+        return result
+
+    def log_likelihood_ratio_batch(self, parameters) -> np.ndarray:
+        return self._call("eval_parameters", {k: (v if isinstance(v, str) else np.asarray(v, dtype=np.float64))
+                                              for k, v in dict(parameters).items()})
 
     def log_likelihood_ratio(self, parameters) -> float:
         return float(self.log_likelihood_ratio_batch(parameters)[0])
 
     def noise_log_likelihood(self) -> float:
+        if self._noise is None:
+            self._noise = float(self._call("noise", None))
         return self._noise
 
     def log_likelihood(self, parameters) -> float:
-        return self.log_likelihood_ratio(parameters) + self._noise
+        return self.log_likelihood_ratio(parameters) + self.noise_log_likelihood()

@@ -242,13 +242,21 @@ int gwl_eval_host_staged(gwl_analysis *a, int64_t B, int32_t precision);
  * counterpart in the reference.  Mixed-precision TaylorF2 analyses without
  * time marginalisation only (GWL_ERR_UNSUPPORTED otherwise).  params / out
  * are device pointers as for gwl_eval_device; asynchronous on `stream`; the
- * device status word is not read back.  The work space is a static 32 MiB
+ * device status word is not read back (gwl_noalloc_status does).  The work space is a static 32 MiB
  * device buffer shared by all calls: B is limited to what fits (about 1,800
  * points for 128 s at 4096 Hz with 3 detectors, about 40,000 for 8 s at
  * 2048 Hz with 2 detectors); larger B returns GWL_ERR_ARGUMENT.  The first
  * call on a device looks up the buffer's address -- make it before any
  * stream capture.  Calls that overlap on the GPU race on the buffer. */
 int gwl_eval_device_noalloc(gwl_analysis *a, const double *params, int64_t B, double *out, void *stream);
+
+/* The status word of gwl_eval_device_noalloc's kernels on the current
+ * device: waits for `stream`, writes the word to *device_status (0 = ok,
+ * 1 = a bounded bulk-copy wait gave up, 2 = a point's ordering key out of
+ * range) and clears it.  Returns GWL_OK for 0, GWL_ERR_TIMEOUT for 1 and
+ * GWL_ERR_ARGUMENT for 2.  It allocates nothing.  No counterpart in the
+ * reference. */
+int gwl_noalloc_status(void *stream, int *device_status);
 
 /* Measurement hooks: with profiling enabled, each evaluation records CUDA
  * events on its stream around its dominant kernel (the fused likelihood or
@@ -418,6 +426,17 @@ int gwl_set_refinement(gwl_analysis *a, double tolerance);
 int gwl_get_refinement(gwl_analysis *a, double *tolerance);
 int gwl_last_refined(gwl_analysis *a, void *stream, int64_t *count);
 int gwl_batcher_last_refined(gwl_batcher *b, void *stream, int64_t *count);
+
+/* Diagnostics of the failure path (no counterpart in the reference).
+ * gwl_selftest_bounded_wait runs one CTA that arms a bulk-copy barrier for
+ * 16 bytes and issues no copy, so the kernels' bounded wait must give up
+ * after `poll_limit` polls: it returns GWL_ERR_TIMEOUT with *device_status = 1
+ * and *arrived = 0, nothing left in flight.  gwl_inject_device_status writes
+ * `value` into an analysis's device status word, as a kernel whose wait gave
+ * up would, so that the next host evaluation reports it (GWL_ERR_TIMEOUT)
+ * and clears it. */
+int gwl_selftest_bounded_wait(uint32_t poll_limit, void *stream, int *device_status, int *arrived);
+int gwl_inject_device_status(gwl_analysis *a, int value);
 
 /* Description of the last error on this thread ("" if none). */
 const char *gwl_last_error(void);

@@ -4,9 +4,10 @@ third-party modules it imports but that this container does not ship.
 TEST INFRASTRUCTURE ONLY.  This module is used to generate the golden
 fixtures under ``tests/golden/`` and by CPU tests that cross-check the numpy
 restatement in :mod:`oracle.restate` against the reference itself.  It needs
-the reference source tree (``GWL_REFERENCE_ROOT``, default
-``/root/reference``); it is never imported by the library, by ``bench.py`` or
-by any GPU test.
+the reference source tree: the directory named by ``GWL_REFERENCE_ROOT``, or
+else a checkout named ``reference`` beside this repository (``../reference``
+from the repository root).  It is never imported by the library, by
+``bench.py`` or by any GPU test.
 
 Stand-ins provided (only what the likelihood hot path touches):
 
@@ -33,7 +34,8 @@ from unittest.mock import MagicMock
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("GWL_REFERENCE_ROOT", "/root/reference")
+_REPO_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFERENCE_ROOT = os.environ.get("GWL_REFERENCE_ROOT") or os.path.normpath(os.path.join(_REPO_ROOT, "..", "reference"))
 
 _INSTALLED = False
 

@@ -20,6 +20,11 @@ Outputs
     Prior draws and the reference's ``log_likelihood_ratio`` for each draw,
     the reference's ``noise_log_likelihood``, and a checksum of the strain it
     generated, so a test can check that the oracle regenerates the same data.
+``tests/golden/tf2_marg_8s_2k.npz``, ``tests/golden/tf2_marg_8s.npz``
+    Prior draws of the marginalised TaylorF2 workloads at 8 s and 2048 Hz
+    (FFT length 8192) and 4096 Hz (FFT length 16384) and the reference's
+    ``log_likelihood_ratio`` under each of the seven combinations of time,
+    phase and distance marginalisation.
 ``tests/golden/tf2_128s_multiband.npz``
     The reference's ``MBGravitationalWaveTransient`` on tf2_128s (reference
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
@@ -710,8 +715,19 @@ def main():
     ap.add_argument("--priors-only", action="store_true")
     ap.add_argument("--roq-only", action="store_true")
     ap.add_argument("--snrs-only", action="store_true")
+    ap.add_argument("--marg-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.marg_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_marginalised(bilby, "tf2_marg_8s_2k", 8)
+                run_marginalised(bilby, "tf2_marg_8s", 16)
+            finally:
+                os.chdir(cwd)
+        return
     if args.snrs_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -768,6 +784,7 @@ def main():
             os.chdir(tmp)  # the reference caches its distance table in the working directory
             try:
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
+                run_marginalised(bilby, "tf2_marg_8s", 16)
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)
                 run_roq(bilby)

@@ -74,3 +74,44 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     monkeypatch.setattr(_build, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _capi.load()
+
+
+CACHE_PROBE = r"""
+#include <cstdio>
+#include "gwl_device_cache.h"
+int main() {
+  gwl::PerDeviceCache<long> cache;
+  int made = 0;
+  long v = 0;
+  auto make = [&](long* out) { *out = 1000 + (++made); return 0; };
+  // the same FFT length on two devices gives two entries
+  if (cache.get(0, 16384, &v, make) || v != 1001) return 1;
+  if (cache.get(1, 16384, &v, make) || v != 1002) return 2;
+  if (cache.get(0, 16384, &v, make) || v != 1001) return 3;   // found, not remade
+  if (cache.get(1, 16384, &v, make) || v != 1002) return 4;
+  if (cache.get(0, 8192, &v, make) || v != 1003) return 5;
+  // a failed make keeps nothing and is retried on the next lookup
+  if (cache.get(2, 16384, &v, [](long*) { return 7; }) != 7) return 6;
+  if (cache.get(2, 16384, &v, make) || v != 1004) return 7;
+  if (made != 4 || cache.size() != 4) return 8;
+  std::puts("ok");
+  return 0;
+}
+"""
+
+
+def test_twiddle_tables_are_keyed_by_device_and_length(tmp_path):
+    """The process-wide cache of the FFT twiddle tables keys on (device,
+    length): the host logic, compiled with g++ against the library's header."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "probe.cpp"
+    src.write_text(CACHE_PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "bilby_gb300", "csrc"), str(src), "-o",
+                    str(exe), "-pthread"], check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert res.returncode == 0 and res.stdout.strip() == "ok", (res.returncode, res.stdout)

@@ -1,6 +1,8 @@
 """Marginalised likelihoods on the GPU against the reference's own values
-(tests/golden/tf2_marg_8s_2k.npz, generated by the reference with the oracle's
-TaylorF2 as its source model) and against brute-force integrals of the
+(tests/golden/tf2_marg_8s_2k.npz at 8 s and 2048 Hz, FFT length 8192, and
+tests/golden/tf2_marg_8s.npz at 8 s and 4096 Hz, FFT length 16384; generated
+by the reference with the oracle's TaylorF2 as its source model) and against
+brute-force integrals of the
 non-marginalised likelihood (the pattern of the reference's
 test/gw/likelihood/marginalization_test.py:383-430).
 
@@ -65,10 +67,11 @@ def golden_points(w, priors, combo):
     return pts, z["lnl_" + combo]
 
 
+@pytest.mark.parametrize("workload", ["tf2_marg_8s_2k", "tf2_marg_8s"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("combo", COMBOS)
-def test_marginalized_vs_reference_golden(gpu, tmp_path, combo, precision):
-    w = WORKLOADS["tf2_marg_8s_2k"]
+def test_marginalized_vs_reference_golden(gpu, tmp_path, combo, precision, workload):
+    w = WORKLOADS[workload]
     like, priors = make_likelihood(w, combo, precision, tmp_path / "table.npz")
     pts, ref = golden_points(w, priors, combo)
     single = np.array([like.log_likelihood_ratio(q) for q in pts])

@@ -51,9 +51,11 @@ def test_oracle_matches_reference_log_likelihood_ratio(name):
         assert abs(got - z["lnl"][i]) <= 1e-12 * scale
 
 
-def test_oracle_time_and_phase_marginalization_matches_reference():
-    """The reference's time / phase / time+phase marginalised values."""
-    w = WORKLOADS["tf2_marg_8s_2k"]
+@pytest.mark.parametrize("name", ["tf2_marg_8s_2k", "tf2_marg_8s"])
+def test_oracle_time_and_phase_marginalization_matches_reference(name):
+    """The reference's time / phase / time+phase marginalised values at FFT
+    lengths 8192 and 16384."""
+    w = WORKLOADS[name]
     z = golden(w.name)
     dets = OD.build_workload(w)
     assert np.allclose(OD.strain_checksum(dets), z["checksum"], rtol=1e-13, atol=0)

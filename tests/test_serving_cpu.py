@@ -145,12 +145,14 @@ def test_client_that_goes_away_is_dropped():
 
 
 def _client_proc(address, key, seed, conn):
-    like = ServedLikelihood(address, key)
+    from multiprocessing.connection import Client
+    c = Client(address, authkey=b"gwlnl")
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(5):
-        p = {k: rng.normal(size=3) for k in _capi.PARAM_SLOTS}
-        out.append((p, like.log_likelihood_ratio_batch(p)))
+        b = rng.normal(size=(_capi.NPARAM, 3))
+        c.send(("eval", key, b))
+        out.append((b, c.recv()[1]))
     conn.send(out)
 
 
@@ -178,11 +180,92 @@ def test_ipc_front_end_with_client_processes():
         p.start()
         pipes.append(r)
         procs.append(p)
-    from bilby_gb300.analysis import params_block
     for r, p in zip(pipes, procs):
-        for params, got in r.recv():
-            assert np.array_equal(got, 3.0 * params_block(params).sum(axis=0))
+        for b, got in r.recv():
+            assert np.array_equal(got, 3.0 * b.sum(axis=0))
         p.join(30)
         assert p.exitcode == 0
+    listener.close()
+    srv.stop()
+
+
+class _HostOnlyLikelihood:
+    """A real likelihood's parameter preparation with a fake device analysis."""
+
+    def __init__(self, like, analysis, noise):
+        self.like, self.analysis, self._noise = like, analysis, noise
+
+    def parameters_block(self, parameters):
+        return self.like.parameters_block(parameters)
+
+    def noise_log_likelihood(self):
+        return self._noise
+
+
+def _tf2_likelihood(monkeypatch):
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.likelihood import GravitationalWaveTransient
+    from bilby_gb300.source import taylorf2_aligned
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    monkeypatch.setattr(GravitationalWaveTransient, "_build_analysis", lambda self: None)
+    grandom.seed(3)
+    ifos = InterferometerList(["H1", "L1"])
+    ifos.set_strain_data_from_power_spectral_densities(2048.0, 4.0, 1126259640.0)
+    wfg = WaveformGenerator(duration=4.0, sampling_frequency=2048.0, start_time=1126259640.0,
+                            frequency_domain_source_model=taylorf2_aligned,
+                            waveform_arguments=dict(minimum_frequency=20.0))
+    return GravitationalWaveTransient(ifos, wfg)
+
+
+SAMPLER_POINT = dict(chirp_mass=22.0, mass_ratio=0.7, chi_1=0.01, chi_2=-0.02, luminosity_distance=400.0,
+                     theta_jn=0.3, phase=1.0, ra=1.0, dec=0.2, psi=0.5, geocent_time=1126259642.0)
+
+
+def _sampler_client(address, key, conn):
+    like = ServedLikelihood(address, key)
+    batch = {k: np.full(4, v) for k, v in SAMPLER_POINT.items()}
+    batch["chirp_mass"] = np.array([15.0, 20.0, 25.0, 30.0])
+    res = {"single": like.log_likelihood_ratio(dict(SAMPLER_POINT)), "batch": like.log_likelihood_ratio_batch(batch),
+           "noise": like.noise_log_likelihood(), "log_likelihood": like.log_likelihood(dict(SAMPLER_POINT))}
+    missing = dict(SAMPLER_POINT)
+    missing.pop("psi")
+    try:
+        like.log_likelihood_ratio(missing)
+        res["missing"] = None
+    except KeyError as e:
+        res["missing"] = str(e)
+    conn.send((batch, res))
+
+
+def test_served_client_prepares_sampler_parameters_like_the_likelihood(monkeypatch):
+    """A sampler dict in chirp mass / mass ratio through the IPC client gives
+    the block the direct likelihood builds (sky frame, conversion, jitter run
+    server-side), the server's noise lnL, and KeyError for a missing psi."""
+    like = _tf2_likelihood(monkeypatch)
+    direct = like.parameters_block(dict(SAMPLER_POINT))
+    assert direct[_capi.SLOT["mass_1"], 0] > direct[_capi.SLOT["mass_2"], 0] > 0
+    with pytest.raises(KeyError):
+        like.parameters_block({k: v for k, v in SAMPLER_POINT.items() if k != "psi"})
+    srv = LikelihoodServer(hbm_budget_bytes=1e9, backend=FakeBackend(delay=0.002)).start()
+    an = FakeAnalysis(10, 3.0)
+    srv.add_analysis("tf2", _HostOnlyLikelihood(like, an, -123.5))
+    srv.add_analysis("bare", an)
+    with pytest.raises(TypeError):
+        srv.submit_parameters("bare", dict(SAMPLER_POINT)).result(5)
+    path = os.path.join(tempfile.mkdtemp(), "gwl.sock")
+    listener = serve_ipc(srv, path)
+    ctx = mp.get_context("spawn")
+    r, w = ctx.Pipe(duplex=False)
+    proc = ctx.Process(target=_sampler_client, args=(path, "tf2", w))
+    proc.start()
+    batch, res = r.recv()
+    proc.join(60)
+    assert proc.exitcode == 0
+    assert res["single"] == 3.0 * direct.sum(axis=0)[0]
+    assert np.array_equal(res["batch"], 3.0 * like.parameters_block(batch).sum(axis=0))
+    assert res["noise"] == -123.5
+    assert res["log_likelihood"] == res["single"] - 123.5
+    assert res["missing"] is not None and "psi" in res["missing"]
     listener.close()
     srv.stop()
