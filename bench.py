@@ -1,32 +1,46 @@
 """Benchmark of the GW-transient likelihood hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-One step = one launch sequence of the fused likelihood over one batch of
-parameter points (default workload ``tf2_128s``: 3.5PN aligned-spin TaylorF2,
-H1/L1/V1, 128 s at 4096 Hz = 262145 bins, 4096 points per launch) with the
-data, PSD and tables resident in HBM.  ``value`` is the mixed-precision
-throughput in likelihood evaluations per second, timed with CUDA events on the
-launching stream; the L2 is flushed (256 MiB write) before every timed
-launch.  ``e2e`` is the same metric through the public API
-(``GravitationalWaveTransient.log_likelihood_ratio_batch`` with host numpy
-arrays: parameter conversion, host->device copy, launch, device->host copy).
-The plain float64 kernel (the drop-in) is timed on the same workload for the
-ratio, and |dlnL| of the mixed results against it is reported.
+The metric is the served mixed-precision likelihood against the plain float64
+kernel on the mixed-duration TaylorF2 workload: 64 analyses (durations 4-128
+s, 2048 or 4096 Hz, 2-3 detectors, 256-4096 points each, 75,945 points in
+all), served to 200 sampler clients.
+
+* ``value``: one step is one batched launch sequence over all 64 analyses
+  (one persistent kernel per detector count, replayed from a CUDA graph) with
+  the parameter blocks resident in HBM; mixed precision with its error
+  control; CUDA events on the launching stream; inputs larger than L2 and the
+  L2 flushed (256 MiB write) before every timed step.
+* ``e2e``: the served path end to end: 200 clients in 8 spawned processes send
+  sampler parameter dictionaries (chirp mass / mass ratio) through the IPC
+  client ``ServedLikelihood``; the server converts them, copies them to the
+  device, runs continuously batched steps and copies the results back.
+  ``e2e.value`` is the saturated throughput (every client back to back);
+  ``p50_ms`` / ``p99_ms`` are the clients' latencies at 80% of it (Poisson
+  arrivals).
+* ``fp64``: the plain float64 kernel (the drop-in) over the whole uneven
+  batch; ``served_over_fp64`` = e2e / fp64.
+* Sub-objects: the single-analysis TaylorF2 launch (128 s at 4096 Hz,
+  4096 points: the kernel the roofline is measured on), the sine-Gaussian
+  configuration, the time+phase+distance marginalised configuration, the fast
+  likelihoods, the single-point drop-in call, and CPU baselines measured in
+  this run on the host cores (the oracle's numpy restatement of bilby's path).
 
 ``--impl reference`` times the reference algorithm on the host cores (the
-oracle's numpy restatement of bilby's path, one process per core) on a
-bounded sample of the same workload.
+oracle, one process per core) over the same 64-analysis mix.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import multiprocessing as mp
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -37,6 +51,29 @@ sys.path.insert(0, ROOT)
 
 METRIC = "lnL evals/s, served mixed-precision vs plain FP64 @|ΔlnL|≤1e-3; p50/p99 ms"
 FLUSH_BYTES = 256 << 20
+WORKLOAD = "uneven64_served"
+
+# Issue slots (thread instructions) per (point, in-band bin) of the mixed
+# TaylorF2 inner loop, frozen from ncu's executed-instruction count of
+# k_mixed_tf2 at tf2_128s, B = 4096 (H1/L1/V1): 1008 M warp instructions x
+# 31.7 active lanes / (4096 points x 259,585 in-band bins) = 30.1.  Per
+# detector the loop spends 7 slots (weight angle add, int-to-float
+# conversion, two multiplies, the hardware cosine, the shared-memory load,
+# one FMA), so D detectors take 9 + 7 D.
+ISSUE_PER_POINT_BIN = {1: 16.0, 2: 23.0, 3: 30.0}
+# files that define k_mixed_tf2: the DRAM traffic of a committed ncu capture
+# is used only while their hash matches the one recorded with it
+KERNEL_SOURCES = ["bilby_gb300/csrc/gwl_kernels.cu", "bilby_gb300/csrc/gwl_phase.cuh",
+                  "bilby_gb300/csrc/gwl_device.cuh", "bilby_gb300/csrc/gwl_math.cuh",
+                  "bilby_gb300/csrc/gwl_internal.h"]
+
+
+def kernel_source_hash() -> str:
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
 
 
 def parse():
@@ -45,21 +82,27 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tf2_128s")
-    ap.add_argument("--batch", type=int, default=0, help="points per launch (default: the workload's)")
-    ap.add_argument("--fp64-batch", type=int, default=512, help="points per launch of the float64 comparison")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
-    ap.add_argument("--no-uneven", action="store_true", help="skip the 64-analysis uneven batch")
-    ap.add_argument("--no-serving", action="store_true", help="skip the serving run")
-    ap.add_argument("--serve-seconds", type=float, default=8.0, help="duration of the serving run")
     ap.add_argument("--n-analyses", type=int, default=64)
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the float64 uneven batch")
+    ap.add_argument("--single-workload", default="tf2_128s", help="the single-analysis (roofline) workload")
+    ap.add_argument("--batch", type=int, default=0, help="points per single-analysis launch (default: the workload's)")
+    ap.add_argument("--fp64-batch", type=int, default=512, help="points per float64 single-analysis launch")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=6.0, help="pool time per CPU baseline sample")
+    ap.add_argument("--cpu-latency-draws", type=int, default=200, help="single-process draws per CPU latency")
+    ap.add_argument("--no-serving", action="store_true", help="skip both serving runs")
+    ap.add_argument("--no-ipc", action="store_true", help="skip the IPC serving run")
+    ap.add_argument("--serve-seconds", type=float, default=6.0, help="duration of each serving run")
+    ap.add_argument("--ipc-procs", type=int, default=8, help="client processes of the IPC serving run")
     ap.add_argument("--serve-streams", type=int, default=3, help="serving steps in flight")
     ap.add_argument("--serve-max-points", type=int, default=1 << 15, help="points per serving step at most")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-analysis launch")
+    ap.add_argument("--no-sg", action="store_true", help="skip the sine-Gaussian workload")
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
     ap.add_argument("--no-multiband", action="store_true", help="skip the multi-banding workload")
     ap.add_argument("--no-roq", action="store_true", help="skip the ROQ workload")
+    ap.add_argument("--no-drop-in", action="store_true", help="skip the single-point call latency")
     return ap.parse_args()
 
 
@@ -138,42 +181,18 @@ def build_likelihood(w, precision="mixed"):
     return GravitationalWaveTransient(ifos, wfg, precision=precision)
 
 
-def algorithmic_counts(w, B, n_groups=None):
-    """Per-launch algorithmic work of the mixed kernel.
-
-    bytes: compulsory traffic of one launch -- the per-bin weight tables read
-    once (TaylorF2: polar weights, 8 B per bin and detector; sine-Gaussian:
-    float32 frequency, weights and 1/S), the parameter block in and the
-    partial sums out (TaylorF2 real-part kernel: 8 B per point, detector and
-    chunk group).
-    ops: issue slots per (point, bin) of the inner loop.  TaylorF2: six
-    wrapping 64-bit adds stepping the phase recurrence (12), per detector a
-    32-bit add of the weight's angle, the int-to-float conversion, two
-    multiplies, the SFU cosine, the shared-memory load and one FMA (7), and two
-    32-bit adds per further detector for its time shift relative to the first.
-    Sine-Gaussian: the two float-float Gaussians and per detector the shift,
-    sincospi and six accumulations.
-    """
-    n_in = w.n_bins - int(math.ceil(w.minimum_frequency * w.duration))
-    D = len(w.detectors)
-    if w.model == "taylorf2":
-        table = n_in * 8 * D
-        ops_per_pb = 12 + 7 * D + 2 * (D - 1)
-        groups = n_groups or int(math.ceil(math.ceil(n_in / 512) / 4))
-        partial = groups * B * D * 8
-    else:
-        table = n_in * (4 + 12 * D)
-        ops_per_pb = 60 + 30 * D
-        partial = int(math.ceil(n_in / 512)) * B * D * 6 * 8
-    bytes_launch = table + 15 * 8 * B + partial
-    return bytes_launch, ops_per_pb * n_in * B
+def uneven_launches_per_step(ws) -> int:
+    """Kernels one batched step launches: prologue, ordering scan and scatter,
+    per detector count the fast kernel and the accurate kernel of the error
+    control, the split-K reduction and the finalize."""
+    classes = {len(w.detectors) for w in ws}
+    return 3 + 2 * len(classes) + 2
 
 
-# ---------------------------------------------------------------------------
-# uneven batching (many analyses in one launch) and serving
-# ---------------------------------------------------------------------------
-def bench_uneven(likes, ws, steps, warmup, seed=17):
-    """One batched launch over all analyses per step (CUDA graph replay); L2 flushed before each."""
+def bench_uneven(likes, ws, steps, warmup, fp64_steps, seed=17):
+    """Value of the line: one batched launch over all analyses per step
+    (CUDA graph replay), then the plain float64 kernel over the same whole
+    batch, and |dlnL| between the two for every point."""
     import torch
     from bilby_gb300.analysis import params_block
     from bilby_gb300.batching import Batcher
@@ -187,65 +206,320 @@ def bench_uneven(likes, ws, steps, warmup, seed=17):
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     tuned = [lk.analysis.autotune(b.data_ptr(), b.shape[1], stream.cuda_stream)[0] for lk, b in zip(likes, blocks)]
     torch.cuda.synchronize()
-    for _ in range(warmup):
-        bat.eval_device(items, "mixed", stream.cuda_stream)
-    torch.cuda.synchronize()
-    ms = []
-    for s in range(steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(s))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        bat.eval_device(items, "mixed", stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    bat.check()
+
+    def run(precision, n_steps, n_warm):
+        for _ in range(n_warm):
+            bat.eval_device(items, precision, stream.cuda_stream)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_steps)]
+        for s in range(n_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(s))
+            ev[s][0].record(stream)
+            bat.eval_device(items, precision, stream.cuda_stream)
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+        bat.check()
+        return [a.elapsed_time(b) for a, b in ev]
+
+    ms = run("mixed", steps, warmup)
     refined = bat.last_refined(stream.cuda_stream)
+    mixed = torch.cat([o.clone() for o in outs])
+    ms64 = run("fp64", fp64_steps, 1)
+    fp64 = torch.cat(outs)
     pts = sum(w.batch for w in ws)
     pbd = sum(w.batch * (w.n_bins - int(w.minimum_frequency * w.duration)) * len(w.detectors) for w in ws)
     value = pts * steps / (sum(ms) / 1e3)
-    # the plain float64 kernel on the same analyses (the first fp64_points points
-    # of each): one launch sequence per analysis, L2 flushed before each step
-    fp64_points = 64
-    sub_blocks = [b[:, :fp64_points].contiguous() for b in blocks]
-    sub = [(lk.analysis, b, b.shape[1], torch.empty(b.shape[1], dtype=torch.float64, device="cuda"))
-           for lk, b in zip(likes, sub_blocks)]
-    sub_items = [(an, b.data_ptr(), n, o.data_ptr()) for an, b, n, o in sub]
-    bat.eval_device(sub_items, "fp64", stream.cuda_stream)
-    torch.cuda.synchronize()
-    ms64 = []
-    for s in range(2):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(s))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        bat.eval_device(sub_items, "fp64", stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms64.append(e0.elapsed_time(e1))
-    pts64 = sum(n for _, _, n, _ in sub)
-    value64 = pts64 * len(ms64) / (sum(ms64) / 1e3)
-    errs = torch.cat([(o64 - o[:n]).abs() for (_, _, n, o64), o in zip(sub, outs)]).cpu().numpy()
-    lnls = torch.cat([o64 for (_, _, _, o64) in sub]).cpu().numpy()
+    value64 = pts * fp64_steps / (sum(ms64) / 1e3)
+    errs = (mixed - fp64).abs().cpu().numpy()
+    lnls = fp64.cpu().numpy()
     j = int(np.argmax(errs))
-    dl, lnl_at = float(errs[j]), float(lnls[j])
-    quiet = np.abs(lnls) < 1e4
-    dl_quiet = float(errs[quiet].max()) if quiet.any() else 0.0
-    dl_1e3 = float(errs[np.abs(lnls) < 1e3].max()) if (np.abs(lnls) < 1e3).any() else 0.0
-    frac_ok = float(np.mean(errs <= 1e-3))
     bat.close()
-    return {"analyses": len(ws), "points_per_launch": pts, "value": value,
-            "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+    return {"analyses": len(ws), "points_per_step": pts, "value": value, "unit": "evals/s",
+            "ms_per_step": float(np.mean(ms)), "ms_steps": ms,
             "point_bin_detector_per_s": pbd * steps / (sum(ms) / 1e3),
-            "launch": "one persistent kernel per kernel class (detectors x partial kind), CUDA-graph replay",
-            "refined_points_per_launch": refined,
+            "launch": "one persistent kernel per detector count, CUDA-graph replay",
+            "launches_per_step": uneven_launches_per_step(ws),
+            "refined_points_per_step": refined,
             "autotuned_chunks_per_group": {str(c): tuned.count(c) for c in sorted(set(tuned))},
-            "fp64": {"value": value64, "unit": "evals/s", "points_per_step": pts64,
-                     "sample": f"the first {fp64_points} points of every analysis, one launch sequence per analysis"},
-            "mixed_over_fp64": value / value64, "max_abs_dlnl_mixed_vs_fp64": dl, "lnl_at_max_dlnl": lnl_at,
-            "max_abs_dlnl_where_abs_lnl_below_1e4": dl_quiet, "max_abs_dlnl_where_abs_lnl_below_1e3": dl_1e3,
-            "fraction_of_points_with_abs_dlnl_le_1e-3": frac_ok}
+            "fp64": {"value": value64, "unit": "evals/s", "points_per_step": pts, "steps": fp64_steps,
+                     "ms_per_step": float(np.mean(ms64)), "sample": "the whole uneven batch, one batched launch"},
+            "mixed_over_fp64": value / value64,
+            "max_abs_dlnl_mixed_vs_fp64": float(errs[j]), "lnl_at_max_dlnl": float(lnls[j]),
+            "fraction_of_points_with_abs_dlnl_le_1e-3": float(np.mean(errs <= 1e-3)),
+            "points_compared": int(len(errs))}
+
+
+# ---------------------------------------------------------------------------
+# serving: in-process submissions and IPC clients in other processes
+# ---------------------------------------------------------------------------
+def make_server(likes, n_streams, max_points):
+    from bilby_gb300.serving import LikelihoodServer
+    srv = LikelihoodServer(hbm_budget_bytes=160e9, max_points_per_step=max_points, n_streams=n_streams)
+    for q, lk in enumerate(likes):
+        srv.add_analysis(q, lk)
+    return srv.start()
+
+
+def bench_serving(srv, ws, seconds, capacity, n_clients=200, seed=23):
+    """200 clients with Poisson arrivals (rate for ~80% load), batches
+    log-uniform in [64, 8192] points, submitted in-process as packed blocks."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    rng = np.random.default_rng(seed)
+    mean_b = (8192 - 64) / math.log(128)
+    rate = 0.8 * capacity / mean_b
+    pool = [params_block(draw_points(w, 8192, rng)) for w in ws]
+    for q in range(len(ws)):
+        srv.submit(q, pool[q][:, :64]).result(120)
+    srv.stats = type(srv.stats)()
+    futs = []
+    t0 = time.perf_counter()
+    t_next = t0
+    while t_next - t0 < seconds:
+        t_next += rng.exponential(1.0 / rate)
+        now = time.perf_counter()
+        if t_next > now:
+            time.sleep(t_next - now)
+        q = int(rng.integers(0, len(ws)))
+        b = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
+        off = int(rng.integers(0, 8192 - b + 1))
+        futs.append(srv.submit(q, pool[q][:, off:off + b], client=int(rng.integers(0, n_clients))))
+    for f in futs:
+        f.result(300)
+    out = srv.stats.summary()
+    out.update({"clients": n_clients, "arrival_rate_per_s": rate, "target_load": 0.8,
+                "batch": "log-uniform [64, 8192]", "submission": "in-process, packed parameter blocks"})
+    return out
+
+
+def _sampler_pool(w, n, rng):
+    """Prior draws of an analysis as a sampler sends them: chirp mass and
+    mass ratio instead of component masses."""
+    from bilby_gb300.workloads import draw_points
+    p = draw_points(w, n, rng)
+    m1, m2 = p.pop("mass_1"), p.pop("mass_2")
+    p["chirp_mass"] = (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2
+    p["mass_ratio"] = m2 / m1
+    return p
+
+
+def _ipc_client_proc(address, ws, clients, rate_per_client, t_start, seconds, closed_loop, seed, conn):
+    """Sampler clients of one process, one thread and one connection each,
+    each bound to one analysis; per request: (scheduled arrival, completion,
+    points)."""
+    from bilby_gb300.serving import ServedLikelihood
+    rng0 = np.random.default_rng(seed)
+    pools = {}
+    for c in clients:
+        q = c % len(ws)
+        if q not in pools:
+            pools[q] = _sampler_pool(ws[q], 8192, rng0)
+    records = []
+    lock = threading.Lock()
+
+    def client(c):
+        q = c % len(ws)
+        like = ServedLikelihood(address, q)
+        rng = np.random.default_rng(seed * 1000 + c)
+        pool = pools[q]
+        like.log_likelihood_ratio_batch({k: v[:8] for k, v in pool.items()})  # connect
+        t_arr = t_start
+        mine = []
+        while True:
+            if closed_loop:
+                t_arr = max(time.perf_counter(), t_start)
+            else:
+                t_arr += rng.exponential(1.0 / rate_per_client)
+            if t_arr - t_start >= seconds:
+                break
+            now = time.perf_counter()
+            if t_arr > now:
+                time.sleep(t_arr - now)
+            b = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
+            off = int(rng.integers(0, 8192 - b + 1))
+            res = like.log_likelihood_ratio_batch({k: v[off:off + b] for k, v in pool.items()})
+            t_done = time.perf_counter()
+            ok = bool(np.all(np.isfinite(res))) and len(res) == b
+            mine.append((t_arr, t_done, b, ok))
+        with lock:
+            records.extend(mine)
+
+    threads = [threading.Thread(target=client, args=(c,)) for c in clients]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    conn.send(records)
+    conn.close()
+
+
+def bench_serving_ipc(srv, ws, seconds, procs=8, n_clients=200, seed=29):
+    """The served path end to end: client processes send sampler dictionaries
+    through ServedLikelihood over a Unix socket.  Phase 1: every client back to
+    back (saturated throughput); phase 2: Poisson arrivals at 80% of it
+    (latency)."""
+    from bilby_gb300.serving import serve_ipc
+    address = os.path.join(tempfile.mkdtemp(), "gwl.sock")
+    listener = serve_ipc(srv, address)
+    ctx = mp.get_context("spawn")
+    groups = [list(range(p, n_clients, procs)) for p in range(procs)]
+
+    def phase(closed_loop, rate_per_client, dur):
+        srv.stats = type(srv.stats)()
+        t_start = time.perf_counter() + 6.0   # time for the client processes to start and connect
+        pipes, ps = [], []
+        for p, cl in enumerate(groups):
+            r, w_ = ctx.Pipe(duplex=False)
+            pr = ctx.Process(target=_ipc_client_proc,
+                             args=(address, ws, cl, rate_per_client, t_start, dur, closed_loop, seed + p, w_))
+            pr.start()
+            pipes.append(r)
+            ps.append(pr)
+        recs = []
+        for r in pipes:
+            recs.extend(r.recv())
+        for pr in ps:
+            pr.join(60)
+        lat = np.array([d - a for a, d, _, _ in recs]) * 1e3
+        pts = sum(b for _, _, b, _ in recs)
+        span = max(d for _, d, _, _ in recs) - t_start
+        return {"requests": len(recs), "points": int(pts), "evals_per_s": pts / span,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "all_finite": all(ok for *_, ok in recs), "server": srv.stats.summary()}
+
+    sat = phase(True, 0.0, seconds)
+    mean_b = (8192 - 64) / math.log(128)
+    rate = 0.8 * sat["evals_per_s"] / mean_b
+    loaded = phase(False, rate / n_clients, seconds)
+    threading.Thread(target=listener.close, daemon=True).start()
+    return {"clients": n_clients, "client_processes": procs, "batch": "log-uniform [64, 8192]",
+            "request": "sampler dict (chirp_mass, mass_ratio, spins, distance, angles, time) through "
+                       "ServedLikelihood; converted in the server by the analysis's likelihood",
+            "saturated": sat, "at_80pct": dict(loaded, arrival_rate_per_s=rate, target_load=0.8)}
+
+
+def bench_single(args, like, w, B, steps, warmup, sptr):
+    """The single-analysis launch (the roofline's kernel): mixed precision at
+    B points, the plain float64 kernel at a smaller batch, |dlnL| between
+    them, and the public batch API with host arrays."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    an = like.analysis
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(w.draw_seed + 7919)
+    host_params = [draw_points(w, B, rng) for _ in range(4)]
+    blocks = [torch.from_numpy(params_block(p)).cuda() for p in host_params]
+    out = torch.empty(B, dtype=torch.float64, device="cuda")
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    tuned_cpg, _ = an.autotune(blocks[0].data_ptr(), B, sptr)
+    an.set_profiling(True)
+
+    def timed(precision, bl, n_steps, warm):
+        for s in range(warm):
+            an.log_likelihood_ratio_device(bl[s % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(), precision,
+                                           sptr)
+        torch.cuda.synchronize()
+        an.last_kernel_ms()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_steps)]
+        kms = []
+        for s in range(n_steps):
+            flush.fill_(float(s))
+            ev[s][0].record(stream)
+            an.log_likelihood_ratio_device(bl[(warm + s) % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(),
+                                           precision, sptr)
+            ev[s][1].record(stream)
+            kms.append(an.last_kernel_ms())
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in ev], kms
+
+    ms, kms = timed("mixed", blocks, steps, warmup)
+    refined = an.last_refined(sptr)
+    Bf = min(args.fp64_batch, B)
+    fblocks = [b[:, :Bf].contiguous() for b in blocks[:3]]
+    fms, _ = timed("fp64", fblocks, 3, 1)
+    an.set_profiling(False)
+    res64 = torch.empty(Bf, dtype=torch.float64, device="cuda")
+    resmx = torch.empty(Bf, dtype=torch.float64, device="cuda")
+    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, res64.data_ptr(), "fp64", sptr)
+    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, resmx.data_ptr(), "mixed", sptr)
+    torch.cuda.synchronize()
+    e2e = []
+    for s in range(warmup + steps):
+        p = host_params[s % len(host_params)]
+        t0 = time.perf_counter()
+        res = like.log_likelihood_ratio_batch(p)
+        if s >= warmup:
+            e2e.append(time.perf_counter() - t0)
+        assert res.shape == (B,)
+    value = B * steps / (sum(ms) / 1e3)
+    fp64_value = Bf * 3 / (sum(fms) / 1e3)
+    return {"workload": w.name, "model": w.model, "detectors": list(w.detectors), "n_bins": w.n_bins, "batch": B,
+            "value": value, "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
+            "kernel_ms": float(np.mean(kms)), "autotuned_chunks_per_group": tuned_cpg,
+            "refined_points_per_launch": refined,
+            "fp64": {"value": fp64_value, "unit": "evals/s", "batch": Bf},
+            "mixed_over_fp64": value / fp64_value,
+            "max_abs_dlnl_mixed_vs_fp64": float((res64 - resmx).abs().max().item()),
+            "e2e": {"value": B * steps / sum(e2e), "unit": "evals/s", "h2d_bytes_per_step": 8 * 15 * B,
+                    "d2h_bytes_per_step": 8 * B,
+                    "call": "GravitationalWaveTransient.log_likelihood_ratio_batch(dict of host numpy arrays)"}}
+
+
+def bench_sine_gaussian(steps, warmup, batch=10000, seed=43):
+    """The sine-Gaussian configuration: H1+L1, 4 s at 2048 Hz, 10^4 prior
+    draws per launch; mixed and float64 kernels and |dlnL| between them."""
+    import torch
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import WORKLOADS, draw_points
+    w = WORKLOADS["sg_4s"]
+    like = build_likelihood(w, precision="mixed")
+    an = like.analysis
+    rng = np.random.default_rng(seed)
+    half = batch // 2
+    pf = draw_points(w, half, rng, fixed_extrinsic=True)
+    pr = draw_points(w, batch - half, rng, fixed_extrinsic=False)
+    block = torch.from_numpy(params_block({k: np.concatenate([pf[k], pr[k]]) for k in pf})).cuda()
+    res = {}
+    outs = {}
+    for precision in ("mixed", "fp64"):
+        ms, finite = time_launches(an, block, batch, steps, warmup, precision)
+        res[precision] = {"value": batch / (ms / 1e3), "unit": "evals/s", "ms_per_launch": ms}
+        o = torch.empty(batch, dtype=torch.float64, device="cuda")
+        an.log_likelihood_ratio_device(block.data_ptr(), batch, o.data_ptr(), precision,
+                                       torch.cuda.current_stream().cuda_stream)
+        outs[precision] = o
+    torch.cuda.synchronize()
+    err = (outs["mixed"] - outs["fp64"]).abs()
+    return {"workload": w.name, "batch": batch, "draws": "half at the injection's sky position and time, half "
+            "with sky, psi and time drawn", "mixed": res["mixed"], "fp64": res["fp64"],
+            "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+            "max_abs_dlnl_mixed_vs_fp64": float(err.max().item()),
+            "refined_points_per_launch": an.last_refined(torch.cuda.current_stream().cuda_stream)}
+
+
+def bench_drop_in(like, w, n_calls=200, seed=47):
+    """log_likelihood_ratio(dict): one point per call, the call samplers make
+    unchanged; p50 / p99 milliseconds per call for each precision."""
+    from bilby_gb300.workloads import draw_points, point
+    p = draw_points(w, n_calls + 10, np.random.default_rng(seed))
+    out = {}
+    for precision in ("fp64", "mixed"):
+        like.precision = precision
+        lat = []
+        for i in range(n_calls + 10):
+            t0 = time.perf_counter()
+            v = like.log_likelihood_ratio(point(p, i))
+            if i >= 10:
+                lat.append(time.perf_counter() - t0)
+            assert np.isfinite(v)
+        lat = np.array(lat) * 1e3
+        out[precision] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                          "calls": n_calls}
+    like.precision = "mixed"
+    return {"workload": w.name, "call": "GravitationalWaveTransient.log_likelihood_ratio(dict of floats)",
+            **out}
 
 
 def time_launches(an, block, n, steps, warmup, precision="fp64"):
@@ -329,8 +603,7 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
     ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
     res["time_marginalized"] = {"batch": bt, "fft_length": int(like_t.analysis.n_bins - 1),
                                 "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
-                                "precision": "fp64", "finite": finite,
-                                "reference_cpu_ms_per_eval": 42.0}
+                                "precision": "fp64", "finite": finite}
     return res
 
 
@@ -397,7 +670,7 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
             "time_marginalized": {"batch": bt, "fft_length": int(like_t._mb_tm[0]),
                                   "banded_frequencies": int(len(like_t.banded_frequency_points)),
                                   "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
-                                  "precision": "fp64", "finite": finite, "reference_cpu_ms_per_eval": 63.0}}
+                                  "precision": "fp64", "finite": finite}}
 
 
 def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, seed=41):
@@ -527,330 +800,391 @@ def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
             "setup_s_incl_distance_table": setup_s}
 
 
-def bench_serving(likes, ws, seconds, capacity, n_clients=200, seed=23, n_streams=3, max_points=1 << 15):
-    """200 clients with Poisson arrivals (rate for ~80% load), batches
-    log-uniform in [64, 8192] points from the analyses above."""
-    from bilby_gb300.analysis import params_block
-    from bilby_gb300.serving import LikelihoodServer
-    from bilby_gb300.workloads import draw_points
-    rng = np.random.default_rng(seed)
-    srv = LikelihoodServer(hbm_budget_bytes=160e9, max_points_per_step=max_points, n_streams=n_streams)
-    for q, lk in enumerate(likes):
-        srv.add_analysis(q, lk)
-    mean_b = (8192 - 64) / math.log(128)
-    rate = 0.8 * capacity / mean_b                # requests per second, all clients together
-    pool = []
-    for q in range(len(ws)):                      # pre-drawn parameter blocks per analysis
-        pool.append(params_block(draw_points(ws[q], 8192, rng)))
-    srv.start()
-    # warm-up: compile paths and allocate work space
-    for q in range(len(ws)):
-        srv.submit(q, pool[q][:, :64]).result(120)
-    srv.stats = type(srv.stats)()
-    futs = []
-    t0 = time.perf_counter()
-    t_next = t0
-    while t_next - t0 < seconds:
-        t_next += rng.exponential(1.0 / rate)
-        now = time.perf_counter()
-        if t_next > now:
-            time.sleep(t_next - now)
-        q = int(rng.integers(0, len(ws)))
-        b = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
-        off = int(rng.integers(0, 8192 - b + 1))
-        futs.append(srv.submit(q, pool[q][:, off:off + b], client=int(rng.integers(0, n_clients))))
-    for f in futs:
-        f.result(300)
-    srv.stop()
-    out = srv.stats.summary()
-    out.update({"clients": n_clients, "arrival_rate_per_s": rate, "target_load": 0.8,
-                "batch": "log-uniform [64, 8192]", "streams": n_streams, "max_points_per_step": max_points,
-                "hbm_budget_gb": 160})
-    return out
-
-
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle's numpy restatement of the reference path
+# CPU baselines: the oracle's numpy restatement of the reference path on the
+# host cores (one spawned process per core, OMP_NUM_THREADS=1)
 # ---------------------------------------------------------------------------
-_CPU = {}
+_CPU: dict = {}
 
 
-def _cpu_init(name):
-    from bilby_gb300.workloads import WORKLOADS
+def _cpu_init(kind):
+    """Worker state for one CPU configuration (built once per process)."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS
     from oracle import data as OD
+    from oracle import restate as R
+    name = {"sg": "sg_4s", "tf2": "tf2_128s", "marg": "tf2_marg_8s", "relbin": "tf2_128s"}[kind]
     w = WORKLOADS[name]
-    _CPU["w"] = w
-    _CPU["dets"] = OD.build_workload(w)
-    _CPU["src"] = OD.source_for(w.model, w.minimum_frequency)
+    _CPU.update(kind=kind, w=w, dets=OD.build_workload(w), src=OD.source_for(w.model, w.minimum_frequency))
+    if kind == "marg":
+        tc = w.injection["geocent_time"]
+        lo, hi = tc - 0.1, tc + 0.1
+        m = R.Marginalization(time=True, phase=True, distance=True)
+        R.setup_time_marginalization(m, w.start_time, w.duration, w.sampling_frequency, lo, hi)
+        dist = np.linspace(DISTANCE_PRIOR["minimum"], DISTANCE_PRIOR["maximum"], 10000)
+        prior = dist ** 2 / np.sum(dist ** 2 * (dist[1] - dist[0]))
+        ref = float(np.interp(0.5, np.cumsum(prior) / np.sum(prior), dist))
+        # a table of the reference's shape (400 x 800): the spline's per-sample
+        # cost does not depend on its values; its one-off build is not timed
+        R.setup_distance_marginalization(m, dist, prior, ref, table=np.zeros((400, 800)))
+        _CPU.update(marg=m, prior=lambda t: ((t >= lo) & (t <= hi)) / (hi - lo))
+    if kind == "relbin":
+        from oracle import relbin as RB
+        _CPU["relbin"] = RB.setup(_CPU["dets"], _CPU["src"], dict(w.injection))
 
 
 def _cpu_eval(p):
     from oracle import restate as R
+    k = _CPU["kind"]
+    if k == "marg":
+        return R.log_likelihood_ratio(_CPU["dets"], _CPU["src"], p, _CPU["marg"], _CPU["prior"])
+    if k == "relbin":
+        from oracle import relbin as RB
+        return RB.log_likelihood_ratio(_CPU["dets"], _CPU["src"], _CPU["relbin"], p)
     return R.log_likelihood_ratio(_CPU["dets"], _CPU["src"], p)
 
 
 def _cpu_eval_timed(p):
-    """Seconds one evaluation takes inside its worker process."""
     t0 = time.perf_counter()
     _cpu_eval(p)
     return time.perf_counter() - t0
 
 
-class CpuBaseline:
-    """The oracle (numpy restatement of bilby's log_likelihood_ratio) on all
-    host cores: one spawned process per core, OMP_NUM_THREADS=1."""
+def _cpu_points(kind, n, seed=123):
+    from bilby_gb300.workloads import WORKLOADS, draw_points, point
+    name = {"sg": "sg_4s", "tf2": "tf2_128s", "marg": "tf2_marg_8s", "relbin": "tf2_128s"}[kind]
+    w = WORKLOADS[name]
+    p = draw_points(w, n, np.random.default_rng(seed))
+    pts = [point(p, i) for i in range(n)]
+    for q in pts:
+        if kind == "marg":
+            q["geocent_time"], q["phase"] = float(w.start_time), 0.0
+            q["luminosity_distance"] = 1000.0
+        else:
+            q.pop("time_jitter", None)
+    return pts
 
-    def __init__(self, name):
-        from bilby_gb300.workloads import WORKLOADS, draw_points, point
-        self.name = name
-        self.w = WORKLOADS[name]
-        self.cores = len(os.sched_getaffinity(0))
-        os.environ["OMP_NUM_THREADS"] = "1"
-        _cpu_init(name)
-        self.params = draw_points(self.w, 4096, np.random.default_rng(123))
-        self.point = point
-        t0 = time.perf_counter()
-        _cpu_eval(point(self.params, 0))
-        self.per_eval = time.perf_counter() - t0
-        self.pool = mp.get_context("spawn").Pool(self.cores, initializer=_cpu_init, initargs=(name,))
-        self.pool.map(_cpu_eval, [point(self.params, i) for i in range(self.cores)])
-        self.offset = 0
 
-    def sample(self, target_seconds):
-        n = max(self.cores, int(target_seconds * self.cores / max(self.per_eval, 1e-6)))
-        n = min(n, 4096)
-        pts = [self.point(self.params, (self.offset + i) % 4096) for i in range(n)]
-        self.offset += n
+def cpu_config(kind, pool_seconds, latency_draws):
+    """(i) one process, ``latency_draws`` draws after 10 warm-up calls: p50 /
+    p99 milliseconds; (ii) a pool of one process per core for about
+    ``pool_seconds``: evaluations per second."""
+    cores = len(os.sched_getaffinity(0))
+    ctx = mp.get_context("spawn")
+    pts = _cpu_points(kind, max(latency_draws + 10, 4 * cores))
+    with ctx.Pool(1, initializer=_cpu_init, initargs=(kind,)) as one:
+        lat = np.array(one.map(_cpu_eval_timed, pts[:latency_draws + 10], chunksize=latency_draws + 10))[10:] * 1e3
+    per = float(np.median(lat)) / 1e3
+    n = int(min(20000, max(4 * cores, pool_seconds * cores / max(per, 1e-6))))
+    pool_pts = [pts[i % len(pts)] for i in range(n)]
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(kind,)) as pool:
+        pool.map(_cpu_eval, pool_pts[:cores], chunksize=1)
         t0 = time.perf_counter()
-        lat = np.array(self.pool.map(_cpu_eval_timed, pts, chunksize=max(1, n // (4 * self.cores))))
+        pool.map(_cpu_eval, pool_pts, chunksize=max(1, n // (8 * cores)))
         dt = time.perf_counter() - t0
-        return {"value": n / dt, "unit": "evals/s", "cores": self.cores, "kind": "port",
-                "latency_ms_p50": float(np.percentile(lat, 50) * 1e3),
-                "latency_ms_p99": float(np.percentile(lat, 99) * 1e3),
-                "latency_note": "one evaluation inside its worker, all workers busy",
-                "sample": f"{n} prior draws of {self.name} through the oracle (numpy restatement of bilby's "
-                          f"log_likelihood_ratio), {self.cores} processes, OMP_NUM_THREADS=1, {dt:.1f} s"}
+    what = {"sg": "sg_4s, plain", "tf2": "tf2_128s, plain", "marg": "tf2_marg_8s, time+phase+distance",
+            "relbin": "tf2_128s, relative binning (fiducial = injection), plain"}[kind]
+    return {"value": n / dt, "unit": "evals/s", "cores": cores, "kind": "port",
+            "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+            "sample": f"{what}: {latency_draws} draws in one process for the latency; {n} draws over {cores} "
+                      f"processes in {dt:.1f} s for the throughput; oracle (numpy restatement of bilby's "
+                      f"log_likelihood_ratio), OMP_NUM_THREADS=1"}
+
+
+def _mix_worker(n_analyses, mine, conn):
+    """Owns the oracle analyses ``mine`` of the 64-analysis mix; per command
+    evaluates one draw of each and sends back the seconds of each evaluation."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    from bilby_gb300.workloads import draw_points, point, uneven_analyses
+    from oracle import data as OD
+    from oracle import restate as R
+    ws = uneven_analyses(n_analyses)
+    own = {}
+    for q in mine:
+        w = ws[q]
+        own[q] = (OD.build_workload(w), OD.source_for(w.model, w.minimum_frequency),
+                  draw_points(w, 64, np.random.default_rng(500 + q)))
+    conn.send("ready")
+    it = 0
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        times = []
+        for q in mine:
+            dets, src, p = own[q]
+            t0 = time.perf_counter()
+            R.log_likelihood_ratio(dets, src, point(p, it % 64))
+            times.append((q, time.perf_counter() - t0))
+        it += 1
+        conn.send(times)
+    conn.close()
+
+
+class CpuMix:
+    """The 64-analysis mix on the host cores: analyses spread over one
+    process per core by their cost (bins x detectors, longest first onto the
+    least-loaded process); one step evaluates one draw of every analysis
+    (the uniform mix the served requests draw from), all processes at once."""
+
+    def __init__(self, n_analyses=64):
+        from bilby_gb300.workloads import uneven_analyses
+        self.cores = len(os.sched_getaffinity(0))
+        ws = uneven_analyses(n_analyses)
+        cost = [w.n_bins * len(w.detectors) for w in ws]
+        n_proc = min(self.cores, n_analyses)
+        loads, owned = [0] * n_proc, [[] for _ in range(n_proc)]
+        for q in sorted(range(n_analyses), key=lambda q: -cost[q]):
+            j = int(np.argmin(loads))
+            owned[j].append(q)
+            loads[j] += cost[q]
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for mine in owned:
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_mix_worker, args=(n_analyses, mine, b))
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        for c in self.conns:
+            assert c.recv() == "ready"
+        self.n = n_analyses
+
+    def step(self):
+        t0 = time.perf_counter()
+        for c in self.conns:
+            c.send(1)
+        times = []
+        for c in self.conns:
+            times.extend(c.recv())
+        return time.perf_counter() - t0, times
 
     def close(self):
-        self.pool.close()
-        self.pool.join()
+        for c in self.conns:
+            c.send(None)
+        for p in self.procs:
+            p.join(30)
 
-
-def cpu_baseline(name, target_seconds):
-    cb = CpuBaseline(name)
-    try:
-        return cb.sample(target_seconds)
-    finally:
-        cb.close()
+    def run(self, steps, warmup):
+        for _ in range(warmup):
+            self.step()
+        walls, evals = [], []
+        for _ in range(steps):
+            wall, t = self.step()
+            walls.append(wall)
+            evals.extend(s for _, s in t)
+        lat = np.array(evals) * 1e3
+        return {"value": self.n * steps / sum(walls), "unit": "evals/s", "cores": len(self.procs), "kind": "port",
+                "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+                "sample": f"{steps} steps of one draw of each of the {self.n} analyses of the mix, {len(self.procs)} "
+                          f"processes (analyses assigned by bins x detectors), oracle (numpy restatement of bilby's "
+                          f"log_likelihood_ratio), OMP_NUM_THREADS=1, {sum(walls):.1f} s"}
 
 
 # ---------------------------------------------------------------------------
+def mix_config(n):
+    from bilby_gb300.workloads import uneven_analyses
+    ws = uneven_analyses(n)
+    return {"workload": WORKLOAD, "analyses": n, "points_per_step": sum(w.batch for w in ws),
+            "durations_s": [4, 8, 16, 32, 64, 128], "sampling_frequencies": [2048, 4096],
+            "detectors": "2 or 3 of H1, L1, V1", "model": "taylorf2 (3.5PN aligned spin)",
+            "clients": 200, "batch_per_request": "log-uniform [64, 8192]"}
+
+
 def run_reference(args, rank, world):
-    from bilby_gb300.workloads import WORKLOADS
     if rank != 0:
         return
-    w = WORKLOADS[args.workload]
-    cb = CpuBaseline(args.workload)
-    values = []
-    for s in range(args.warmup + args.steps):
-        r = cb.sample(max(2.0, 90.0 / max(1, args.warmup + args.steps)))
-        if s >= args.warmup:
-            values.append(r["value"])
-    cb.close()
-    v = float(np.median(values))
-    line = {"metric": METRIC, "value": v, "unit": "evals/s", "impl": "reference", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "batch": w.batch, "detectors": list(w.detectors),
-                       "n_bins": w.n_bins, "model": w.model},
-            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"]},
-            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    mix = CpuMix(args.n_analyses)
+    try:
+        steps = max(args.steps, 10)
+        r = mix.run(steps, max(1, args.warmup))
+    finally:
+        mix.close()
+    line = {"metric": METRIC, "value": r["value"], "unit": "evals/s", "impl": "reference", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.n_analyses / r["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection per analysis)",
+            "config": dict(mix_config(args.n_analyses), parallelism=f"host cores x{r['cores']}"),
+            "p50_ms": r["latency_ms_p50"], "p99_ms": r["latency_ms_p99"],
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": r["value"], "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 def run_ours(args, rank, world, local):
     import torch
     from bilby_gb300 import _build, _capi
-    from bilby_gb300.analysis import params_block
-    from bilby_gb300.workloads import WORKLOADS, draw_points
+    from bilby_gb300.workloads import WORKLOADS, uneven_analyses
 
-    w = WORKLOADS[args.workload]
-    B = args.batch or w.batch
     torch.cuda.set_device(local)
     _build.build()
     from bilby_gb300.replicas import ReplicaGroup
     dist = ReplicaGroup(world, backend="nccl")
-    cpu = None
+    cpu = {}
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.workload, args.cpu_seconds)   # spawned before any CUDA work of this process
-    like = build_likelihood(w, precision="mixed")
-    an = like.analysis
+        # spawned before any CUDA work of this process
+        mix = CpuMix(args.n_analyses)
+        try:
+            cpu["mix"] = mix.run(10, 2)
+        finally:
+            mix.close()
+        for kind in ("sg", "tf2", "marg", "relbin"):
+            cpu[kind] = cpu_config(kind, args.cpu_seconds, args.cpu_latency_draws)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
-    n_blocks = args.warmup + args.steps
-    rng = np.random.default_rng(w.draw_seed + 7919 * rank)
-    host_params = [draw_points(w, B, rng) for _ in range(n_blocks)]
-    blocks = [torch.from_numpy(params_block(p)).cuda() for p in host_params]
-    out = torch.empty(B, dtype=torch.float64, device="cuda")
-    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    # launch shape for this workload (outside the timed region)
-    tuned_cpg, _ = an.autotune(blocks[0].data_ptr(), B, sptr)
-    an.set_profiling(True)
 
-    def timed(precision, bl, n_steps, warm):
-        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
-        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
-        kms = []
-        for s in range(warm):
-            an.log_likelihood_ratio_device(bl[s % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(), precision, sptr)
-        torch.cuda.synchronize()
-        an.last_kernel_ms()
-        dist.barrier()
-        torch.cuda.synchronize()
-        for s in range(n_steps):
-            flush.fill_(float(s))
-            ev0[s].record(stream)
-            an.log_likelihood_ratio_device(bl[(warm + s) % len(bl)].data_ptr(), bl[0].shape[1], out.data_ptr(),
-                                           precision, sptr)
-            ev1[s].record(stream)
-            kms.append(an.last_kernel_ms())
-        torch.cuda.synchronize()
-        dist.barrier()
-        ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-        return ms, kms
-
-    # -- headline: mixed precision, resident inputs ----------------------------
-    # clocks sampled every 10 ms from the warm-up through the timed steps
+    # -- the line's value: the 64-analysis batched step, device resident -------
+    uws = uneven_analyses(args.n_analyses)
+    ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.05)
-    ms, kms = timed("mixed", blocks, args.steps, args.warmup)
+    dist.barrier()
+    uneven = bench_uneven(ulikes, uws, args.steps, args.warmup, args.fp64_steps)
+    dist.barrier()
     clk = clocks.stop()
-    refined = an.last_refined(sptr)  # points of the last timed batch whose sums were recomputed
-    total_ms = dist.max(float(np.sum(ms)))
-    value = world * B * args.steps / (total_ms / 1e3)
+    total_ms = dist.max(float(np.sum(uneven["ms_steps"])))
+    value = world * uneven["points_per_step"] * args.steps / (total_ms / 1e3)
 
-    # -- plain float64 kernel on the same workload (smaller batch) and |dlnL| --
-    Bf = min(args.fp64_batch, B)
-    fblocks = [b[:, :Bf].contiguous() for b in blocks[:3]]
-    fms, _ = timed("fp64", fblocks, 3, 1)
-    fp64_value = Bf * 3 / (float(np.sum(fms)) / 1e3)
-    res64 = torch.empty(Bf, dtype=torch.float64, device="cuda")
-    resmx = torch.empty(Bf, dtype=torch.float64, device="cuda")
-    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, res64.data_ptr(), "fp64", sptr)
-    an.log_likelihood_ratio_device(fblocks[0].data_ptr(), Bf, resmx.data_ptr(), "mixed", sptr)
-    torch.cuda.synchronize()
-    an.last_kernel_ms()
-    dlnl = float((res64 - resmx).abs().max().item())
+    # -- served: in-process and through IPC client processes -------------------
+    served = ipc = None
+    if world == 1 and not args.no_serving:
+        srv = make_server(ulikes, args.serve_streams, args.serve_max_points)
+        served = bench_serving(srv, uws, args.serve_seconds, uneven["value"])
+        if not args.no_ipc:
+            ipc = bench_serving_ipc(srv, uws, args.serve_seconds, procs=args.ipc_procs)
+        srv.stop()
 
-    # -- end to end through the public API with host buffers --------------------
-    e2e_times = []
-    for s in range(args.warmup + args.steps):
-        p = host_params[s % n_blocks]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = like.log_likelihood_ratio_batch(p)
-        t1 = time.perf_counter()
-        if s >= args.warmup:
-            e2e_times.append(t1 - t0)
-        assert res.shape == (B,)
-    e2e_total = dist.max(float(np.sum(e2e_times)))
-    e2e_value = world * B * args.steps / e2e_total
+    # -- the single-analysis launch: the roofline's kernel ----------------------
+    single = drop_in = None
+    w = WORKLOADS[args.single_workload]
+    if not args.no_single:
+        like = build_likelihood(w, precision="mixed")
+        single = bench_single(args, like, w, args.batch or w.batch, args.steps, args.warmup, sptr)
+        if not args.no_drop_in:
+            drop_in = bench_drop_in(like, w)
+        like.analysis.close()
+    sg = bench_sine_gaussian(max(3, args.steps // 2), args.warmup) if world == 1 and not args.no_sg else None
+    relbin = bench_relbin("tf2_128s", max(3, args.steps // 2), args.warmup) \
+        if world == 1 and not args.no_relbin else None
+    multiband = bench_multiband("tf2_128s", max(3, args.steps // 4), args.warmup) \
+        if world == 1 and not args.no_multiband else None
+    roq = bench_roq("tf2_marg_8s_2k", max(3, args.steps // 2), args.warmup) if world == 1 and not args.no_roq else None
+    marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup) \
+        if world == 1 and not args.no_marg else None
 
-    # -- many analyses in one launch, then the serving loop ---------------------
-    uneven = served = None
-    if world == 1 and (not args.no_uneven or not args.no_serving):
-        from bilby_gb300.workloads import uneven_analyses
-        uws = uneven_analyses(args.n_analyses)
-        ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
-        uneven = bench_uneven(ulikes, uws, max(3, args.steps // 2), args.warmup)
-        if not args.no_serving:
-            served = bench_serving(ulikes, uws, args.serve_seconds, uneven["value"], n_streams=args.serve_streams,
-                                   max_points=args.serve_max_points)
-        if args.no_uneven:
-            uneven = None
-
-    relbin = None
-    if world == 1 and not args.no_relbin:
-        relbin = bench_relbin("tf2_128s", max(3, args.steps // 2), args.warmup)
-
-    multiband = None
-    if world == 1 and not args.no_multiband:
-        multiband = bench_multiband("tf2_128s", max(3, args.steps // 4), args.warmup)
-
-    roq = None
-    if world == 1 and not args.no_roq:
-        roq = bench_roq("tf2_marg_8s_2k", max(3, args.steps // 2), args.warmup)
-
-    marg = None
-    if world == 1 and not args.no_marg:
-        marg = bench_marginalized("tf2_marg_8s", max(3, args.steps // 4), args.warmup)
-
-    # -- roofline of the dominant kernel ---------------------------------------
+    # -- roofline of the mixed TaylorF2 inner loop -----------------------------
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    n_groups = int(math.ceil(math.ceil((w.n_bins - int(math.ceil(w.minimum_frequency * w.duration))) / 512)
-                             / tuned_cpg))
-    bytes_launch, ops_launch = algorithmic_counts(w, B, n_groups)
-    kernel_ms = float(np.mean(kms))
-    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    props = torch.cuda.get_device_properties(local)
-    issue_peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12  # Tops/s, FP32 lanes at the sampled clock
-    an.set_profiling(False)
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"{w.name}_mixed_traffic.json")
-    if os.path.exists(tpath):
-        t = json.load(open(tpath))
-        # DRAM bytes of one launch from an ncu capture of this workload and batch
-        traffic = t.get("traffic_bytes_per_launch") if t.get("batch") == B else None
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "MEASURED_PEAKS.json (of measured)"
+    if hbm_peak is None:
+        hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s (of fallback)"
+    roofline = roofline_hbm = None
+    if single is not None:
+        D = len(w.detectors)
+        n_in = w.n_bins - int(math.ceil(w.minimum_frequency * w.duration))
+        B = single["batch"]
+        kernel_ms = single["kernel_ms"]
+        sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        props = torch.cuda.get_device_properties(local)
+        lanes = props.multi_processor_count * 128
+        issue_peak = lanes * sm_mhz * 1e6 / 1e12
+        achieved = ISSUE_PER_POINT_BIN[D] * n_in * B / (kernel_ms / 1e3) / 1e12
+        n_groups = int(math.ceil(math.ceil(n_in / 512) / single["autotuned_chunks_per_group"]))
+        bytes_launch = n_in * 8 * D + 15 * 8 * B + n_groups * B * D * 8
+        traffic, traffic_note = None, "no ncu capture recorded for this kernel source"
+        tpath = os.path.join(ROOT, "profiles", f"{w.name}_mixed_traffic.json")
+        if os.path.exists(tpath):
+            t = json.load(open(tpath))
+            if t.get("batch") != B:
+                traffic_note = f"ncu capture at batch {t.get('batch')}, not {B}"
+            elif t.get("kernel_source_sha16") != kernel_source_hash():
+                traffic_note = "ncu capture of another kernel source (hash mismatch): not used"
+            else:
+                traffic = t["traffic_bytes_per_launch"]
+                traffic_note = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, " + tpath[len(ROOT) + 1:]
+        roofline = {"bound": "issue", "achieved": achieved, "peak": issue_peak, "unit": "Tinst/s",
+                    "frac": achieved / issue_peak, "traffic": traffic, "kernel": "k_mixed_tf2",
+                    "workload": f"{w.name}, B = {B}", "kernel_ms": kernel_ms,
+                    "work": f"{ISSUE_PER_POINT_BIN[D]} thread instructions per (point, in-band bin), frozen from "
+                            f"ncu's executed-instruction count; {n_in} in-band bins",
+                    "peak_source": f"{props.multi_processor_count} SMs x 128 lanes x sampled SM clock {sm_mhz} MHz",
+                    "traffic_note": traffic_note,
+                    "note": "the served step runs the same inner loop (k_multi_tf2); tables are reused from shared "
+                            "memory by every point of a CTA, so DRAM is not the bound"}
+        roofline_hbm = {"bound": "hbm", "achieved": bytes_launch / (kernel_ms / 1e3) / 1e9, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": bytes_launch / (kernel_ms / 1e3) / 1e9 / hbm_peak,
+                        "traffic": traffic, "peak_source": peak_src,
+                        "work": "compulsory bytes: polar weight tables (8 B per bin and detector), the parameter "
+                                "block and the partial sums"}
 
     if rank == 0:
+        e2e_v = ipc["saturated"]["evals_per_s"] if ipc else None
         line = {
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (exact 0.64 fixed-point phase recurrence, float-float anchors)",
-            "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection)",
-            "config": {"workload": w.name, "model": w.model, "detectors": list(w.detectors), "n_bins": w.n_bins,
-                       "duration_s": w.duration, "sampling_frequency": w.sampling_frequency, "batch": B,
-                       "parallelism": f"replicas x{world}", "l2": "flushed before every timed launch (256 MiB write)",
-                       "autotuned_chunks_per_group": tuned_cpg},
-            "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
-            "fp64": {"value": fp64_value, "unit": "evals/s", "batch": Bf},
-            "mixed_over_fp64": value / world / fp64_value,
-            "max_abs_dlnl_mixed_vs_fp64": dlnl,
-            "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": 8 * _capi.NPARAM * B,
-                    "d2h_bytes_per_step": 8 * B},
-            "gpu_launches": (7 if w.model == "taylorf2" else 4) * args.steps * world,
-            "refined_points_per_launch": refined,
-            "roofline": {"bound": "hbm", "achieved": bytes_launch / (kernel_ms / 1e3) / 1e9, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": bytes_launch / (kernel_ms / 1e3) / 1e9 / hbm_peak,
-                         "traffic": traffic, "kernel": f"k_mixed_{'tf2' if w.model == 'taylorf2' else 'sg'}",
-                         "kernel_ms": kernel_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                         "traffic_source": "profiles/tf2_128s_mixed_traffic.json (ncu dram__bytes_read+write)",
-                         "note": "tables are L2/shared-memory resident and reused by every point of the launch; "
-                                 "the kernel is bound by INT/FP32/SFU issue, see compute"},
-            "compute": {"bound": "fp32_issue", "achieved": ops_launch / (kernel_ms / 1e3) / 1e12,
-                        "peak": issue_peak, "unit": "Tops/s",
-                        "frac": ops_launch / (kernel_ms / 1e3) / 1e12 / issue_peak,
-                        "peak_source": "152 SMs x 128 FP32 lanes x sampled SM clock"},
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (exact 0.64 fixed-point phase recurrence, float-float anchors, error control to 1e-3)",
+            "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection per analysis)",
+            "config": dict(mix_config(args.n_analyses), parallelism=f"replicas x{world}",
+                           l2="inputs larger than L2 and flushed before every timed step (256 MiB write)"),
+            "fp64": uneven["fp64"],
+            "mixed_over_fp64": uneven["mixed_over_fp64"],
+            "served_over_fp64": (e2e_v / uneven["fp64"]["value"]) if e2e_v else None,
+            "max_abs_dlnl_mixed_vs_fp64": uneven["max_abs_dlnl_mixed_vs_fp64"],
+            "fraction_of_points_with_abs_dlnl_le_1e-3": uneven["fraction_of_points_with_abs_dlnl_le_1e-3"],
+            "gpu_launches": uneven["launches_per_step"] * args.steps * world,
+            "p50_ms": ipc["at_80pct"]["p50_ms"] if ipc else None,
+            "p99_ms": ipc["at_80pct"]["p99_ms"] if ipc else None,
             "clocks": clk,
+            "uneven": uneven,
         }
-        if marg is not None:
+        if ipc:
+            srv_stats = ipc["saturated"]["server"]
+            pts_step = srv_stats.get("mean_points_per_step") or 0.0
+            line["e2e"] = {"value": e2e_v, "unit": "evals/s",
+                           "h2d_bytes_per_step": int(8 * _capi.NPARAM * pts_step), "d2h_bytes_per_step": int(8 * pts_step),
+                           "path": "sampler dicts from 200 clients in 8 processes -> ServedLikelihood (IPC) -> "
+                                   "server conversion -> pinned staging -> H2D -> batched step -> D2H -> client"}
+        if roofline:
+            line["roofline"] = roofline
+            line["roofline_hbm"] = roofline_hbm
+        if cpu:
+            line["cpu_baseline"] = cpu["mix"]
+            line["cpu_baselines"] = {"sg_4s": cpu["sg"], "tf2_128s": cpu["tf2"], "tf2_marg_8s_tpd": cpu["marg"],
+                                     "tf2_128s_relative_binning": cpu["relbin"]}
+            line["gpu_over_cpu"] = {
+                "mixed_mix_value": value / cpu["mix"]["value"],
+                "fp64_mix_precision_matched": uneven["fp64"]["value"] / cpu["mix"]["value"],
+                "served_e2e": (e2e_v / cpu["mix"]["value"]) if e2e_v else None}
+        if served:
+            line["served"] = {"in_process": served, "ipc": ipc}
+        if single:
+            line["single_analysis"] = single
+            if cpu:
+                single["fp64_over_cpu"] = single["fp64"]["value"] / cpu["tf2"]["value"]
+                single["mixed_over_cpu"] = single["value"] / cpu["tf2"]["value"]
+        if drop_in:
+            line["drop_in_call"] = drop_in
+        if sg:
+            line["sine_gaussian"] = sg
+            if cpu:
+                sg["fp64_over_cpu"] = sg["fp64"]["value"] / cpu["sg"]["value"]
+                sg["mixed_over_cpu"] = sg["mixed"]["value"] / cpu["sg"]["value"]
+        if marg:
             line["marginalized"] = marg
-        if relbin is not None:
+            if cpu:
+                marg["fp64_over_cpu"] = marg["fp64"]["value"] / cpu["marg"]["value"]
+                marg["mixed_over_cpu"] = marg["mixed"]["value"] / cpu["marg"]["value"]
+        if relbin:
             line["relative_binning"] = relbin
-        if multiband is not None:
+            if cpu:
+                relbin["fp64_over_cpu"] = relbin["value"] / cpu["relbin"]["value"]
+        if multiband:
             line["multiband"] = multiband
-        if roq is not None:
+        if roq:
             line["roq"] = roq
-        if uneven is not None:
-            line["uneven"] = uneven
-        if served is not None:
-            line["served"] = served
-        if cpu is not None:
-            line["cpu_baseline"] = cpu
         print(json.dumps(line))
     dist.close()
 
