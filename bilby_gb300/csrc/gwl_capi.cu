@@ -64,6 +64,7 @@ struct gwl_analysis {
   float2* w[kMaxDet] = {};
   uint2* wp[kMaxDet] = {};  // TaylorF2: the same weights in polar form {float |w|, arg(w) as 0.32 fixed cycles}
   float* v[kMaxDet] = {};
+  float* v_lo[kMaxDet] = {};  // sine-Gaussian: low words of the scaled inverse PSD
   double* hh_prefix[kMaxDet] = {};
   double* rf_p2[kMaxDet] = {};  // TaylorF2: prefix sums of |w|^2 and of |w| over signal-dominated bins
   double* rf_p1[kMaxDet] = {};
@@ -292,6 +293,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.w[d] = a->w[d];
     L.wp[d] = a->wp[d];
     L.v[d] = a->v[d];
+    L.v_lo[d] = a->v_lo[d];
     L.hh_prefix[d] = a->hh_prefix[d];
     L.rf_p2[d] = a->rf_p2[d];
     L.rf_p1[d] = a->rf_p1[d];
@@ -299,7 +301,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.v_scale[d] = a->v_scale[d];
   }
   // the list and its count are set by the entry point that launches k_refine
-  L.rf_tol = (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) ? a->refine_tol : 0.0;
+  L.rf_tol = precision == GWL_PRECISION_MIXED ? a->refine_tol : 0.0;
   L.cos_tab = a->cos_tab;
   L.freq = a->freq;
   L.freq_f = a->freq_f;
@@ -516,6 +518,13 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     ordering_with_marks(L);
     a->last_rf_count = L.rf_count;
     GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * (2 * L.order_keys + 1), s));
+  } else if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN && !(a->time_marg && d_out) &&
+             L.rf_tol > 0) {
+    // sine-Gaussian: the finalize marks the points whose error bound exceeds
+    // the tolerance and counts them here; k_sg_refine recomputes them
+    L.rf_count = a->d_order_hist;
+    a->last_rf_count = L.rf_count;
+    GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
   } else {
     L.rf_tol = 0.0;
   }
@@ -523,6 +532,14 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   if (ordered) GWL_CUDA(launch_order(L, s));
   if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
   if (a->time_marg && d_out) {
+    if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN) {
+      // the mixed sine-Gaussian pass first: its float-float <h|h> partial sums
+      // are what the time-marginalised kernel reads
+      LaunchArgs P = L;
+      P.rf_tol = 0.0;
+      P.rf_count = nullptr;
+      GWL_CUDA(launch_mixed(P, s));
+    }
     GWL_CUDA(launch_time_marginalized(L, s));
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
@@ -530,7 +547,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     }
     return GWL_OK;
   }
-  const bool acc = precision == GWL_PRECISION_MIXED && L.rf_tol > 0;
+  const bool acc = precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2 && L.rf_tol > 0;
   if (acc) {
     // the marked points in the accurate kernel on the side stream, beside the fast kernel
     GWL_CUDA(side_fork(a->side, s));
@@ -547,6 +564,8 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   }
   if (acc) GWL_CUDA(side_join(a->side, s));
   GWL_CUDA(launch_finalize(L, s));
+  if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN && L.rf_tol > 0)
+    GWL_CUDA(launch_sg_refine(L, s));
   return GWL_OK;
 }
 
@@ -829,7 +848,11 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
         if ((rc = upload(a, &a->wp[d], wpol))) goto fail;
       }
       if (a->model == GWL_MODEL_SINEGAUSSIAN) {
+        // float-float inverse PSD for the float-float <h|h> of the mixed kernel
+        std::vector<float> vl(P, 0.f);
+        for (int64_t k = 0; k < N; ++k) vl[k] = (float)(ip[k] / a->v_scale[d] - (double)vf[k]);
         if ((rc = upload(a, &a->v[d], vf))) goto fail;
+        if ((rc = upload(a, &a->v_lo[d], vl))) goto fail;
       } else {
         // <h|h> prefix sums of f^(-7/3) / S over the analysis grid
         std::vector<double> pre(N + 1, 0.0);

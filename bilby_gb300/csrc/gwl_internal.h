@@ -84,6 +84,7 @@ struct LaunchArgs {
   const float2* w[kMaxDet];             // [n_pad] mixed data weights (scaled)
   const uint2* wp[kMaxDet];             // [n_pad] TaylorF2: polar weights {float |w| bits, arg(w) 0.32 cycles}
   const float* v[kMaxDet];              // [n_pad] mixed inverse PSD (scaled)
+  const float* v_lo[kMaxDet];           // [n_pad] sine-Gaussian: low words of the scaled inverse PSD (v + v_lo)
   const double* hh_prefix[kMaxDet];     // [n_bins + 1] TaylorF2 <h|h> prefix sums
   double w_scale[kMaxDet], v_scale[kMaxDet];
   const float2* basis;                  // [n_pad][kNumBasis] float-float phase basis
@@ -240,6 +241,7 @@ cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_mixed_acc(const LaunchArgs& a, cudaStream_t s);
 
 cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_sg_refine(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_order(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_relbin(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);

@@ -865,14 +865,40 @@ __global__ void __launch_bounds__(kAccThreads) k_mixed_tf2_acc(LaunchArgs a) {
     acc_unit<D, CPLX>(a, a.order[u / a.n_groups], u % a.n_groups, tab);
 }
 
-// Sine-Gaussian, mixed precision.  Shared memory per chunk: float32
-// frequencies, each detector's weights d / S and 1 / S (scaled).
+// Sine-Gaussian, mixed precision (bilby/gw/source.py:1197-1207 projected as
+// in interferometer.py:341-362, summed as in gw/utils.py:118-138).
+//
+// Per detector d the projection is conj(h_d) = M_d (a_d hp + i c_d hx) e^{+i theta}
+// with hp = g1 + g2, hx = g1 - g2, g1,2 = exp(-pi^2 tau^2 (f -+ f0)^2),
+// M_d = |(Fp P, Fx X)| and (a_d, c_d) = (Fp P, Fx X) / M_d.  Four partial sums:
+//   0, 1: Re, Im of sum (a hp + i c hx) e^{i theta} w      (float32, Kahan)
+//   2:    sum (a^2 hp^2 + c^2 hx^2) v                      (float-float)
+//   3:    sum (|a hp| + |c hx|)^2 |w|^2                    (float32: error norm)
+// <h|h> is float-float throughout: the Gaussians come from the float-float
+// multiplicative recurrence g(k + s) = g(k) r(k), r(k + s) = r(k) c with
+// c = exp(-2 A df^2) (A = pi^2 tau^2, s = +-1), walked away from the peak so
+// that g only shrinks, restarted from float64 values every kSgSegment bins
+// (the recurrence's relative error grows as n^2 2^-47, about 2e-10 at 256);
+// v = v_hi + v_lo is the float-float inverse PSD.  <d|h> sums float32 terms
+// whose rounding errors are independent from bin to bin; the finalize bounds
+// them by sum 3 and sends points over the tolerance to k_sg_refine.
+constexpr int kSgSegment = 256;
+
+__device__ __forceinline__ void ff_mul_to(float& h, float& l, float bh, float bl) {
+  const float p = __fmul_rn(h, bh);
+  float e = __fmaf_rn(h, bh, -p);
+  e = __fmaf_rn(h, bl, e);
+  e = __fmaf_rn(l, bh, e);
+  h = __fadd_rn(p, e);
+  l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
 template <int D>
 __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
   constexpr int CH = kChunkMixed;
-  __shared__ __align__(16) float s_f[CH];
   __shared__ __align__(16) float2 s_w[D][CH];
-  __shared__ __align__(16) float s_v[D][CH];
+  __shared__ __align__(16) float s_vh[D][CH];
+  __shared__ __align__(16) float s_vl[D][CH];
   __shared__ uint64_t bar;
   const int64_t k0 = a.k_base + (int64_t)blockIdx.y * CH;
   const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
@@ -883,75 +909,191 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, CH * 4 + D * CH * 12);
-    bulk_g2s(s_f, a.freq_f + k0, CH * 4, &bar);
+    mbar_expect_tx(&bar, D * CH * 16);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       bulk_g2s(s_w[d], a.w[d] + k0, CH * 8, &bar);
-      bulk_g2s(s_v[d], a.v[d] + k0, CH * 4, &bar);
+      bulk_g2s(s_vh[d], a.v[d] + k0, CH * 4, &bar);
+      bulk_g2s(s_vl[d], a.v_lo[d] + k0, CH * 4, &bar);
     }
   }
   const bool arrived = mbar_wait_bounded(&bar, 0, a.status, kWaitLimit);
-  double t[D][6];
+  double t[D][4];
 #pragma unroll
   for (int d = 0; d < D; ++d)
 #pragma unroll
-    for (int q = 0; q < 6; ++q) t[d][q] = 0.0;
+    for (int q = 0; q < 4; ++q) t[d][q] = 0.0;
   if (have && arrived && a.rec[i].valid) {
     const PointRec& r = a.rec[i];
-    const float f0h = __double2float_rn(r.sg_f0);
-    const float f0l = __double2float_rn(r.sg_f0 - (double)f0h);
-    const float gah = __double2float_rn(r.sg_a);
-    const float gal = __double2float_rn(r.sg_a - (double)gah);
+    float ad[D], cd[D], a2h[D], a2l[D], c2h[D], c2l[D];
     uint32_t xl[D], xh[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
+      const double A = r.fp[d] * r.amp, C = r.fx[d] * r.amp2, M = hypot(A, C);
+      const double an = M > 0 ? A / M : 0.0, cn = M > 0 ? C / M : 0.0;
+      ad[d] = (float)an;
+      cd[d] = (float)cn;
+      const ff q = ff_from_double(an * an), u = ff_from_double(cn * cn);
+      a2h[d] = q.hi;
+      a2l[d] = q.lo;
+      c2h[d] = u.hi;
+      c2l[d] = u.lo;
       xl[d] = r.xfix[d][0];
       xh[d] = r.xfix[d][1];
     }
-    for (int jf = 0; jf < CH; jf += kFlush) {
-      float acc[D][6], cmp[D][6];
+    const double f0 = r.sg_f0, A = r.sg_a, df = a.step;
+    const ff cc = ff_from_double(exp(-2.0 * A * df * df));
+    // bins [0, ja) lie below the peak (walked downwards), [ja, CH) above it
+    const double jp = floor((f0 - a.freq[k0]) / df);
+    const int ja = (int)fmin(fmax(jp + 1.0, 0.0), (double)CH);
+    for (int run = 0; run < 2; ++run) {
+      const int dir = run == 0 ? 1 : -1;
+      int j = run == 0 ? ja : ja - 1;
+      int left = run == 0 ? CH - ja : ja;
+      while (left > 0) {
+        const int n = min(left, kSgSegment);
+        // float64 start of the recurrence at bin j
+        const double f = a.freq[k0 + j], x = f - f0, y = f + f0, st = dir * df;
+        ff g1 = ff_from_double(exp(-A * x * x)), r1 = ff_from_double(exp(-A * (2.0 * x * st + df * df)));
+        ff g2 = ff_from_double(exp(-A * y * y)), r2 = ff_from_double(exp(-A * (2.0 * y * st + df * df)));
+        if (g1.hi == 0.f) r1.hi = r1.lo = 0.f;  // underflowed: stays zero (never inf * 0)
+        if (g2.hi == 0.f) r2.hi = r2.lo = 0.f;
+        float sr[D], cr[D], si[D], ci[D], hh[D], hl[D], e2[D];
 #pragma unroll
-      for (int d = 0; d < D; ++d)
+        for (int d = 0; d < D; ++d) sr[d] = cr[d] = si[d] = ci[d] = hh[d] = hl[d] = e2[d] = 0.f;
+        for (int q = 0; q < n; ++q, j += dir) {
+          float hph = g1.hi, hpl = g1.lo, hxh = g1.hi, hxl = g1.lo;
+          ff_add(hph, hpl, g2.hi, g2.lo);
+          ff_add(hxh, hxl, -g2.hi, -g2.lo);
+          // squares as unnormalised float-float pairs
+          const float p2 = __fmul_rn(hph, hph), p2e = __fmaf_rn(2.f * hph, hpl, __fmaf_rn(hph, hph, -p2));
+          const float x2 = __fmul_rn(hxh, hxh), x2e = __fmaf_rn(2.f * hxh, hxl, __fmaf_rn(hxh, hxh, -x2));
+          const uint32_t k = (uint32_t)(k0 + j);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc[d][q] = cmp[d][q] = 0.f;
-      for (int j = jf; j < jf + kFlush; ++j) {
-        const float f = s_f[j];
-        const float g1 = gauss_ff(f, f0h, f0l, gah, gal, -1.0f);
-        const float g2 = gauss_ff(f, f0h, f0l, gah, gal, 1.0f);
-        const float hp = g1 + g2, hx = g1 - g2;
-        const float hp2 = hp * hp, hx2 = hx * hx;
-        const uint32_t k = (uint32_t)(k0 + j);
+          for (int d = 0; d < D; ++d) {
+            // The phase is linear in k: use the accurate sincospi on the exact
+            // fraction so that no approximation error repeats coherently.
+            const float ph = fixed_phase_cycles(k, xl[d], xh[d]);
+            float sn, cs;
+            sincospif(2.0f * ph, &sn, &cs);
+            const float2 w = s_w[d][j];
+            const float ere = w.x * cs - w.y * sn, eim = w.x * sn + w.y * cs;
+            const float u = ad[d] * hph, z = cd[d] * hxh;
+            kahan_add(sr[d], cr[d], u * ere - z * eim);
+            kahan_add(si[d], ci[d], u * eim + z * ere);
+            // (a^2 hp^2 + c^2 hx^2) v in float-float
+            const float q1 = __fmul_rn(a2h[d], p2);
+            float q1e = __fmaf_rn(a2h[d], p2, -q1);
+            q1e = __fmaf_rn(a2h[d], p2e, __fmaf_rn(a2l[d], p2, q1e));
+            const float q2 = __fmul_rn(c2h[d], x2);
+            float q2e = __fmaf_rn(c2h[d], x2, -q2);
+            q2e = __fmaf_rn(c2h[d], x2e, __fmaf_rn(c2l[d], x2, q2e));
+            const float sh = __fadd_rn(q1, q2), sb = __fsub_rn(sh, q1);
+            const float se = __fadd_rn(__fadd_rn(__fsub_rn(q1, __fsub_rn(sh, sb)), __fsub_rn(q2, sb)),
+                                       __fadd_rn(q1e, q2e));
+            ff_mac(hh[d], hl[d], sh, se, s_vh[d][j], s_vl[d][j]);
+            const float m = fabsf(u) + fabsf(z);
+            e2[d] = __fmaf_rn(m * m, __fmaf_rn(w.x, w.x, w.y * w.y), e2[d]);
+          }
+          ff_mul_to(g1.hi, g1.lo, r1.hi, r1.lo);
+          ff_mul_to(r1.hi, r1.lo, cc.hi, cc.lo);
+          ff_mul_to(g2.hi, g2.lo, r2.hi, r2.lo);
+          ff_mul_to(r2.hi, r2.lo, cc.hi, cc.lo);
+        }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          // The sine-Gaussian's phase is linear in k, so the error of the
-          // hardware sin/cos approximation would repeat coherently from bin
-          // to bin: use the accurate sincospi on the exact fraction.
-          const float ph = fixed_phase_cycles(k, xl[d], xh[d]);
-          float sn, cs;
-          sincospif(2.0f * ph, &sn, &cs);
-          const float2 w = s_w[d][j];
-          const float ere = w.x * cs - w.y * sn, eim = w.x * sn + w.y * cs;
-          const float vv = s_v[d][j];
-          kahan_add(acc[d][0], cmp[d][0], hp * ere);
-          kahan_add(acc[d][1], cmp[d][1], hp * eim);
-          kahan_add(acc[d][2], cmp[d][2], hx * ere);
-          kahan_add(acc[d][3], cmp[d][3], hx * eim);
-          kahan_add(acc[d][4], cmp[d][4], hp2 * vv);
-          kahan_add(acc[d][5], cmp[d][5], hx2 * vv);
+          t[d][0] += (double)sr[d] - (double)cr[d];
+          t[d][1] += (double)si[d] - (double)ci[d];
+          t[d][2] += (double)hh[d] + (double)hl[d];
+          t[d][3] += (double)e2[d];
         }
+        left -= n;
       }
-#pragma unroll
-      for (int d = 0; d < D; ++d)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) t[d][q] += (double)acc[d][q] - (double)cmp[d][q];
     }
   }
   if (have) {
 #pragma unroll
     for (int d = 0; d < D; ++d)
 #pragma unroll
-      for (int q = 0; q < 6; ++q) a.part[(((int64_t)blockIdx.y * D + d) * kPartStride + q) * a.B + i] = t[d][q];
+      for (int q = 0; q < 4; ++q) a.part[(((int64_t)blockIdx.y * D + d) * kPartStride + q) * a.B + i] = t[d][q];
+  }
+}
+
+// Sine-Gaussian points whose mixed-precision error bound exceeds the
+// tolerance: float64 totals over the in-band bins (the plain kernel's
+// arithmetic), one CTA per point, fixed-order reduction, then the point's
+// lnL replaces the mixed one.
+constexpr int kSgRefineThreads = 256;
+__device__ void finish_point(const LaunchArgs& a, const PointRec& r, int64_t i, double dr, double di, double hh);
+
+template <int D>
+__global__ void __launch_bounds__(kSgRefineThreads) k_sg_refine(LaunchArgs a) {
+  __shared__ double s_red[kSgRefineThreads / 32][3 * D];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t n = a.k_hi - a.k_lo, per = (n + kSgRefineThreads - 1) / kSgRefineThreads;
+  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+    const PointRec& r = a.rec[i];
+    if (!r.refine) continue;  // the same i for the whole block
+    const double f0 = r.sg_f0, amp = r.a[0], dplus = r.a[1], dcross = r.a[2], tau2 = r.a[3];
+    const double pi2 = 9.869604401089358;
+    double acc[3 * D];
+#pragma unroll
+    for (int q = 0; q < 3 * D; ++q) acc[q] = 0.0;
+    const int64_t kb = a.k_lo + threadIdx.x * per, ke = min(kb + per, a.k_hi);
+    if (kb < ke) {
+      double zc[D], zs[D], rc[D], rs[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double w2 = 2.0 * kPi * r.dt[d];
+        sincos(w2 * a.freq[kb], &zs[d], &zc[d]);
+        sincos(w2 * a.step, &rs[d], &rc[d]);
+      }
+      for (int64_t k = kb; k < ke; ++k) {
+        const double f = a.freq[k];
+        const double fm = f - f0, fpl = f + f0;
+        const double neg = exp(-(fm * fm) * pi2 * tau2);
+        const double pos = exp(-(fpl * fpl) * pi2 * tau2);
+        const double hp = amp * (neg + pos) / dplus;
+        const double hx_im = -(amp * (neg - pos) / dcross);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double is = a.inv_psd[d][k];
+          if (is != 0.0) {
+            const double sre = hp * r.fp[d], sim = hx_im * r.fx[d];
+            const double hre = sre * zc[d] + sim * zs[d], him = sim * zc[d] - sre * zs[d];
+            const double2 dd = reinterpret_cast<const double2*>(a.strain[d])[k];
+            acc[3 * d] += (hre * dd.x + him * dd.y) * is;
+            acc[3 * d + 1] += (hre * dd.y - him * dd.x) * is;
+            acc[3 * d + 2] += (hre * hre + him * him) * is;
+          }
+          rotate(zc[d], zs[d], rc[d], rs[d]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3 * D; ++q)
+      for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 3 * D; ++q) s_red[warp][q] = acc[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double norm = 4.0 / a.duration;
+      double dr = 0.0, di = 0.0, hh = 0.0;
+      for (int d = 0; d < D; ++d) {
+        double x = 0.0, y = 0.0, z = 0.0;
+        for (int w = 0; w < kSgRefineThreads / 32; ++w) {
+          x += s_red[w][3 * d];
+          y += s_red[w][3 * d + 1];
+          z += s_red[w][3 * d + 2];
+        }
+        dr += norm * x;
+        di += norm * y;
+        hh += norm * z;
+      }
+      finish_point(a, r, i, dr, di, hh);
+    }
+    __syncthreads();
   }
 }
 
@@ -984,8 +1126,18 @@ __device__ __forceinline__ void sum_groups(const LaunchArgs& a, int64_t i, int d
     for (int t = 0; t < NQ; ++t) p[t] += q[c * gs + (int64_t)t * a.B];
 }
 
+// Error bound of the mixed sine-Gaussian lnL (k_mixed_sg): its <d|h> terms
+// carry independent float32 rounding errors of relative size below about
+// 2.5e-7 (weights, the phase fraction, the Gaussian's high word, products), so
+// their sum errs by kSgRandomErr (a 4-sigma margin) times the Euclidean norm of
+// the terms; the float32 antenna factors add a coherent kSgCoherentErr |<d|h>|
+// and the float-float <h|h> (recurrence, inverse PSD) kSgHhErr <h|h>.
+constexpr double kSgRandomErr = 1e-6;
+constexpr double kSgCoherentErr = 1e-7;
+constexpr double kSgHhErr = 2e-9;
+
 __device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const PointRec& r, double* dh_re,
-                                double* dh_im, double* hh) {
+                                double* dh_im, double* hh, double* err = nullptr) {
   const double norm = 4.0 / a.duration;
   double sdr = 0.0, sdi = 0.0, shh = 0.0;
   for (int d = 0; d < a.n_det; ++d) {
@@ -993,7 +1145,7 @@ __device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const
     if (a.precision == GWL_PRECISION_FP64) {
       if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<3>(a, i, d, G, p);
       else sum_groups<2>(a, i, d, G, p);
-    } else if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<6>(a, i, d, G, p);
+    } else if (a.model == GWL_MODEL_SINEGAUSSIAN) sum_groups<4>(a, i, d, G, p);
     else if (a.cplx) sum_groups<2>(a, i, d, G, p);
     else sum_groups<1>(a, i, d, G, p);
     double dr, di, h;
@@ -1010,12 +1162,12 @@ __device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const
       const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
       h = norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
     } else if (a.model == GWL_MODEL_SINEGAUSSIAN) {
-      // conj(h) = (Fp P hp + i Fx X hx) e^{+i theta}; sums S1 = sum hp e w, S2 = sum hx e w
-      const double P = r.amp, X = r.amp2, ws = a.w_scale[d], vs = a.v_scale[d];
-      const double A = r.fp[d] * P, C = r.fx[d] * X;
-      dr = norm * ws * (A * p[0] - C * p[3]);
-      di = norm * ws * (A * p[1] + C * p[2]);
-      h = norm * vs * (A * A * p[4] + C * C * p[5]);
+      // conj(h) = M (a hp + i c hx) e^{+i theta}, M = |(Fp P, Fx X)| (see k_mixed_sg)
+      const double M = hypot(r.fp[d] * r.amp, r.fx[d] * r.amp2), ws = a.w_scale[d], vs = a.v_scale[d];
+      dr = norm * ws * M * p[0];
+      di = norm * ws * M * p[1];
+      h = norm * vs * M * M * p[2];
+      if (err) *err += kSgRandomErr * norm * ws * M * sqrt(fmax(p[3], 0.0));
     } else {
       // conj(h_det) = A0 f^(-7/6) conj(Q) e^{+i Phi},  Q = Fp (1 + c^2)/2 - i Fx c
       const double ci = r.cos_i;
@@ -1056,7 +1208,7 @@ __device__ double distance_marginalized(const LaunchArgs& a, double dh_re, doubl
 // the six sums of the sine-Gaussian mixed kernel, re/im for TaylorF2 mixed.
 __device__ __host__ __forceinline__ int part_components(const LaunchArgs& a) {
   if (a.precision == GWL_PRECISION_FP64) return a.model == GWL_MODEL_SINEGAUSSIAN ? 3 : 2;
-  return a.model == GWL_MODEL_SINEGAUSSIAN ? 6 : (a.cplx ? 2 : 1);
+  return a.model == GWL_MODEL_SINEGAUSSIAN ? 4 : (a.cplx ? 2 : 1);
 }
 
 // One (point, detector, component) chain: the partial sums of all groups
@@ -1111,9 +1263,20 @@ __device__ void finish_point(const LaunchArgs& a, const PointRec& r, int64_t i, 
 // G: the groups still to be summed (1 after k_reduce_parts)
 __device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int64_t G) {
   const PointRec& r = a.rec[i];
-  double dr, di, hh;
-  detector_totals(a, i, G, r, &dr, &di, &hh);
+  double dr, di, hh, err = 0.0;
+  const bool sg_bound = a.model == GWL_MODEL_SINEGAUSSIAN && a.precision == GWL_PRECISION_MIXED && a.rf_tol > 0 &&
+                        a.rf_count && r.valid;
+  detector_totals(a, i, G, r, &dr, &di, &hh, sg_bound ? &err : nullptr);
   finish_point(a, r, i, dr, di, hh);
+  if (sg_bound) {
+    err += kSgCoherentErr * (fabs(dr) + fabs(di)) + kSgHhErr * hh;
+    // the bound holds for Re <d|h> - <h|h> / 2 and, as ln I0 has slope at
+    // most one, for the phase-marginalised ln I0(|<d|h>|) - <h|h> / 2
+    if (!(err <= a.rf_tol)) {
+      a.rec[i].refine = 1;
+      atomicAdd(a.rf_count, 1);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1700,6 +1863,13 @@ cudaError_t launch_finalize(const LaunchArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const int threads = kPointThreads;
   k_finalize<<<(unsigned)((a.B + threads - 1) / threads), threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_refine(const LaunchArgs& a, cudaStream_t s) {
+  if (a.model != GWL_MODEL_SINEGAUSSIAN || !(a.rf_tol > 0) || !a.rf_count || a.B <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)min(a.B, (int64_t)4 * sm_count_k());
+  GWL_DISPATCH_D(k_sg_refine, grid, kSgRefineThreads, 0, s, a);
   return cudaGetLastError();
 }
 

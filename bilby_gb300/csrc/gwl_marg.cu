@@ -225,8 +225,6 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
       const float f0h = (float)r.sg_f0, f0l = (float)(r.sg_f0 - (double)f0h);
       const float gah = (float)r.sg_a, gal = (float)(r.sg_a - (double)gah);
-      float hh1[D], hh2[D];
-      for (int d = 0; d < D; ++d) hh1[d] = hh2[d] = 0.f;
       if (a.model == GWL_MODEL_TAYLORF2) {
         // The integrand fused with the first four FFT stages.  After them the
         // positions 16 b .. 16 b + 15 hold the 16-point DFT of the bins
@@ -329,18 +327,21 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
               const float ar = cre[d] * hp, ai = -cim[d] * hx;
               zr += ar * er + ai * ei;
               zi += ai * er - ar * ei;
-              const float vv = a.v[d][k];
-              hh1[d] = __fmaf_rn(hp * hp, vv, hh1[d]);
-              hh2[d] = __fmaf_rn(hx * hx, vv, hh2[d]);
             }
           }
         }
         buf[P(bit_reverse((uint32_t)k, log2L))] = make_float2(zr, zi);
       }
-      if (a.model == GWL_MODEL_SINEGAUSSIAN) {
+      if (a.model == GWL_MODEL_SINEGAUSSIAN && threadIdx.x == 0 && r.valid) {
+        // the float-float <h|h> of the k_mixed_sg pass launched before this
+        // kernel (partial sum 2 of every chunk group, in group order)
+        const int64_t gs = (int64_t)a.n_det * kPartStride * a.B;
         for (int d = 0; d < D; ++d) {
           const double A = r.fp[d] * r.amp, Cx = r.fx[d] * r.amp2;
-          hh_part += norm * a.v_scale[d] * (A * A * hh1[d] + Cx * Cx * hh2[d]);
+          const double* q = a.part + ((int64_t)d * kPartStride + 2) * a.B + i;
+          double p2 = 0.0;
+          for (int64_t g = 0; g < a.n_chunks; ++g) p2 += q[g * gs];
+          hh_part += norm * a.v_scale[d] * (A * A + Cx * Cx) * p2;
         }
       }
     } else if (a.relbin) {
@@ -488,16 +489,6 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
           const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
           hh_part += norm * (sre * sre + sim * sim) * is;
         }
-      }
-    }
-    if (MIXED && a.model == GWL_MODEL_SINEGAUSSIAN && threadIdx.x == 0 && r.valid && L >= a.k_lo && L < a.k_hi) {
-      const double f = a.freq[L];
-      const double pi2 = 9.869604401089358;
-      const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
-      const double g1 = exp(-(fm * fm) * pi2 * r.a[3]), g2 = exp(-(fpl * fpl) * pi2 * r.a[3]);
-      for (int d = 0; d < D; ++d) {
-        const double A = r.fp[d] * r.amp, Cx = r.fx[d] * r.amp2;
-        hh_part += norm * a.inv_psd[d][L] * (A * A * (g1 + g2) * (g1 + g2) + Cx * Cx * (g1 - g2) * (g1 - g2));
       }
     }
     if (MIXED && threadIdx.x == 0) {

@@ -77,6 +77,62 @@ def optimal_snr_squared_ref_axis(n):
     return np.logspace(-5, 10, n)
 
 
+class ParameterPreparer:
+    """The preparation of a sampler's parameter dictionary that precedes the
+    likelihood kernels (base.py:419-446): the sky frame
+    (``get_sky_frame_parameters``, base.py:1091-1137), the waveform
+    generator's ``parameter_conversion`` (waveform_generator.py:260-269) and
+    the time jitter of time marginalisation (base.py:427-428).  Raises
+    ``KeyError`` when a parameter the source model or the projection needs is
+    missing after conversion, as the reference's source-model call does."""
+
+    def __init__(self, model, parameter_conversion, frame=None, time_reference="geocent", reference_vertex=None,
+                 jitter=False):
+        self.model = model
+        self.parameter_conversion = parameter_conversion
+        self.frame = frame
+        self.time_reference = time_reference
+        self.reference_vertex = reference_vertex
+        self.jitter = jitter
+
+    def sky_frame(self, parameters):
+        time = parameters.get(f"{self.time_reference}_time", None)
+        if self.frame is not None:
+            try:
+                ra, dec = self.frame.zenith_azimuth_to_ra_dec(parameters["zenith"], parameters["azimuth"], time)
+            except KeyError:
+                if "ra" in parameters and "dec" in parameters:
+                    ra, dec = parameters["ra"], parameters["dec"]
+                else:
+                    raise
+        else:
+            ra, dec = parameters["ra"], parameters["dec"]
+        if "geocent" not in self.time_reference and f"{self.time_reference}_time" in parameters:
+            from .frames import time_delay_from_geocenter
+            geocent_time = time - time_delay_from_geocenter(self.reference_vertex, ra, dec, time)
+        else:
+            geocent_time = parameters["geocent_time"]
+        return dict(ra=ra, dec=dec, geocent_time=geocent_time)
+
+    def prepare(self, parameters: dict) -> dict:
+        p = dict(parameters)
+        p.update(self.sky_frame(p))
+        converted, _ = self.parameter_conversion(dict(p))
+        if self.jitter:
+            converted["time_jitter"] = p.get("time_jitter", 0.0)
+        missing = [k for k in REQUIRED_PARAMETERS[self.model] if converted.get(k) is None]
+        if missing:
+            raise KeyError(f"parameters missing after conversion: {missing}")
+        return converted
+
+    def block(self, parameters) -> np.ndarray:
+        """The [NPARAM, B] float64 block of a dictionary of scalars or
+        equal-length arrays; the caller's dictionary is not modified."""
+        arrays = {k: (np.asarray(v, dtype=np.float64) if not isinstance(v, str) else v)
+                  for k, v in copy.deepcopy(dict(parameters)).items()}
+        return params_block(self.prepare(arrays))
+
+
 class GravitationalWaveTransient(_Base):
     """GPU drop-in for bilby's GravitationalWaveTransient (sine-Gaussian and
     aligned-spin TaylorF2 source models, identity calibration)."""
@@ -350,49 +406,28 @@ class GravitationalWaveTransient(_Base):
             self._noise_log_likelihood_value = self.analysis.noise_log_likelihood()
         return self._noise_log_likelihood_value
 
+    @property
+    def preparer(self) -> "ParameterPreparer":
+        """What ``log_likelihood_ratio`` does to a parameter dictionary before
+        the kernels read it, as a small picklable object (the serving client
+        runs it in the sampler's process)."""
+        vertex = None if self.reference_ifo is None else np.asarray(self.reference_ifo.geometry.vertex, dtype=np.float64)
+        return ParameterPreparer(self._model, self.waveform_generator.parameter_conversion, self._frame,
+                                 self.time_reference, vertex, self.time_marginalization and self.jitter_time)
+
     def get_sky_frame_parameters(self, parameters):
         """base.py:1091-1137, vectorised."""
-        time = parameters.get(f"{self.time_reference}_time", None)
-        if self._frame is not None:
-            try:
-                ra, dec = self._frame.zenith_azimuth_to_ra_dec(parameters["zenith"], parameters["azimuth"], time)
-            except KeyError:
-                if "ra" in parameters and "dec" in parameters:
-                    ra, dec = parameters["ra"], parameters["dec"]
-                else:
-                    raise
-        else:
-            ra, dec = parameters["ra"], parameters["dec"]
-        if "geocent" not in self.time_reference and f"{self.time_reference}_time" in parameters:
-            from .frames import time_delay_from_geocenter
-            geocent_time = time - time_delay_from_geocenter(self.reference_ifo.geometry.vertex, ra, dec, time)
-        else:
-            geocent_time = parameters["geocent_time"]
-        return dict(ra=ra, dec=dec, geocent_time=geocent_time)
+        return self.preparer.sky_frame(parameters)
 
     def _prepare(self, parameters: dict) -> dict:
-        """Sky frame, the waveform generator's parameter conversion and the
-        time jitter (base.py:419-446, waveform_generator.py:260-269); raises
-        ``KeyError`` when a parameter the source model or the projection needs
-        is still missing after conversion, as the reference's source call does."""
-        p = dict(parameters)
-        p.update(self.get_sky_frame_parameters(p))
-        converted, _ = self.waveform_generator.parameter_conversion(dict(p))
-        if self.time_marginalization and self.jitter_time:
-            converted["time_jitter"] = p.get("time_jitter", 0.0)
-        missing = [k for k in REQUIRED_PARAMETERS[self._model] if converted.get(k) is None]
-        if missing:
-            raise KeyError(f"parameters missing after conversion: {missing}")
-        return converted
+        return self.preparer.prepare(parameters)
 
     def parameters_block(self, parameters) -> np.ndarray:
         """The [NPARAM, B] float64 block the kernels read, from a sampler's
         parameter dictionary (scalars or equal-length arrays), after the same
         preparation as ``log_likelihood_ratio``.  The caller's dictionary is
         not modified."""
-        arrays = {k: (np.asarray(v, dtype=np.float64) if not isinstance(v, str) else v)
-                  for k, v in copy.deepcopy(dict(parameters)).items()}
-        return params_block(self._prepare(arrays))
+        return self.preparer.block(parameters)
 
     def log_likelihood_ratio(self, parameters):
         """base.py:419-446 for one point: a batch of size one on the GPU."""

@@ -205,6 +205,11 @@ class LikelihoodServer:
             raise TypeError(f"analysis {key!r} was registered without a likelihood: send packed parameter blocks")
         return like
 
+    def preparer(self, key):
+        """The registered likelihood's parameter preparation (a picklable
+        ``ParameterPreparer``), for clients that convert in their own process."""
+        return self._likelihood(key).preparer
+
     def noise_log_likelihood(self, key) -> float:
         """The noise log-likelihood of a registered analysis (base.py:413-417)."""
         like = self.likelihoods.get(key)
@@ -377,6 +382,8 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
     * ``("eval_parameters", key, parameters)``: a sampler's dictionary,
       prepared by the registered likelihood (``submit_parameters``);
     * ``("noise", key, None)``: the analysis's noise log-likelihood;
+    * ``("spec", key, None)``: the registered likelihood's parameter
+      preparation (``ParameterPreparer``), so that the client converts;
 
     and receives ``("ok", results)`` or ``("error", message)``.  Returns the
     listener (close it to stop accepting)."""
@@ -388,12 +395,14 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
         try:
             while True:
                 msg = conn.recv()
-                if not isinstance(msg, tuple) or len(msg) != 3 or msg[0] not in ("eval", "eval_parameters", "noise"):
+                if not isinstance(msg, tuple) or len(msg) != 3 or \
+                        msg[0] not in ("eval", "eval_parameters", "noise", "spec"):
                     conn.send(("error", "malformed message"))
                     continue
-                if msg[0] == "noise":
+                if msg[0] in ("noise", "spec"):
                     try:
-                        conn.send(("ok", server.noise_log_likelihood(msg[1])))
+                        what = server.noise_log_likelihood if msg[0] == "noise" else server.preparer
+                        conn.send(("ok", what(msg[1])))
                     except Exception as e:
                         conn.send(("error", f"{type(e).__name__}: {e}"))
                     continue
@@ -427,16 +436,21 @@ class ServedLikelihood:
 
     ``log_likelihood_ratio(parameters)`` evaluates one point and
     ``log_likelihood_ratio_batch(parameters)`` a batch (a dict of equal-length
-    arrays).  The server prepares the dictionary with the registered
-    likelihood (sky frame, parameter conversion, time jitter), so any
-    parameter set the direct ``GravitationalWaveTransient`` accepts (e.g.
-    ``chirp_mass`` / ``mass_ratio``) gives the same result here, and a set
-    that lacks a needed parameter raises.  ``noise_log_likelihood()`` is the
+    arrays).  The dictionary is prepared exactly as the registered likelihood
+    prepares it (sky frame, parameter conversion, time jitter): by default in
+    this process, with the likelihood's ``ParameterPreparer`` fetched from the
+    server on first use, so that only the packed float64 block travels; with
+    ``convert_on_client=False`` the server converts.  Either way any parameter
+    set the direct ``GravitationalWaveTransient`` accepts (e.g. ``chirp_mass``
+    / ``mass_ratio``) gives the same result here, and a set that lacks a
+    needed parameter raises ``KeyError``.  ``noise_log_likelihood()`` is the
     server's value for the analysis, fetched once."""
 
-    def __init__(self, address, key, authkey: bytes = b"gwlnl"):
+    def __init__(self, address, key, authkey: bytes = b"gwlnl", convert_on_client: bool = True):
         self.address, self.key, self.authkey = address, key, authkey
+        self.convert_on_client = convert_on_client
         self._noise = None
+        self._preparer = None
         self._conn = None
 
     def _connection(self):
@@ -460,7 +474,15 @@ class ServedLikelihood:
             raise RuntimeError(result)
         return result
 
+    @property
+    def preparer(self):
+        if self._preparer is None:
+            self._preparer = self._call("spec", None)
+        return self._preparer
+
     def log_likelihood_ratio_batch(self, parameters) -> np.ndarray:
+        if self.convert_on_client:
+            return self._call("eval", self.preparer.block(parameters))
         return self._call("eval_parameters", {k: (v if isinstance(v, str) else np.asarray(v, dtype=np.float64))
                                               for k, v in dict(parameters).items()})
 

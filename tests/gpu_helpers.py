@@ -30,10 +30,38 @@ def oracle_plain(dets, w: Workload, params: dict, idx) -> tuple[np.ndarray, np.n
     return np.array(lnl), np.array(scale)
 
 
+_POOL: dict = {}
+
+
+def _pool_init(w):
+    import os
+    os.environ["OMP_NUM_THREADS"] = "1"
+    _POOL["dets"] = OD.build_workload(w)
+    _POOL["src"] = OD.source_for(w.model, w.minimum_frequency)
+
+
+def _pool_eval(p):
+    dh, hh = R.plain_terms(_POOL["dets"], _POOL["src"], p)
+    return float(np.real(dh) - hh / 2), R.parity_scale(dh, hh)
+
+
+def oracle_plain_pool(w: Workload, params: dict, idx) -> tuple[np.ndarray, np.ndarray]:
+    """``oracle_plain`` over the host cores: a pool of processes started with
+    ``spawn`` (safe after CUDA is initialised), each building the workload's
+    oracle data once."""
+    import multiprocessing as mp
+    import os
+    pts = [point(params, i) for i in idx]
+    n = max(1, min(len(os.sched_getaffinity(0)), 32, len(pts)))
+    with mp.get_context("spawn").Pool(n, initializer=_pool_init, initargs=(w,)) as pool:
+        res = pool.map(_pool_eval, pts, chunksize=max(1, len(pts) // (4 * n)))
+    return np.array([r[0] for r in res]), np.array([r[1] for r in res])
+
+
 def small_workload(base: str, **changes) -> Workload:
     from dataclasses import replace
     return replace(WORKLOADS[base], **changes)
 
 
-__all__ = ["device_analysis", "oracle_plain", "params_block", "draw_points", "point", "small_workload",
+__all__ = ["device_analysis", "oracle_plain", "oracle_plain_pool", "params_block", "draw_points", "point", "small_workload",
            "FP64_RTOL", "MIXED_ATOL", "WORKLOADS"]

@@ -11,16 +11,14 @@ CASES = [("H1L1", "geocent"), ("H1L1", "H1"), ("sky", "L1"), ("L1V1", "V1")]
 
 
 def frame_object(frame, tref):
+    """The likelihood's parameter preparation for a sky frame and time reference."""
     from bilby_gb300.detector import get_empty_interferometer
     from bilby_gb300.frames import ReferenceFrame
-    from bilby_gb300.likelihood import GravitationalWaveTransient
-    like = object.__new__(GravitationalWaveTransient)
-    like._frame = None if frame == "sky" else ReferenceFrame(frame)
+    from bilby_gb300.likelihood import ParameterPreparer
+    f = None if frame == "sky" else ReferenceFrame(frame)
     if "geocent" in tref:
-        like.time_reference, like.reference_ifo = "geocent", None
-    else:
-        like.time_reference, like.reference_ifo = tref, get_empty_interferometer(tref)
-    return like
+        return ParameterPreparer("taylorf2", None, f, "geocent", None)
+    return ParameterPreparer("taylorf2", None, f, tref, get_empty_interferometer(tref).geometry.vertex)
 
 
 @pytest.mark.parametrize("q", range(len(CASES)))
@@ -31,7 +29,7 @@ def test_sky_frame_parameters_match_the_reference(q):
     key = "geocent_time" if "geocent" in tref else f"{tref}_time"
     p = dict(zenith=z["p_zenith"], azimuth=z["p_azimuth"], ra=z["p_ra"], dec=z["p_dec"])
     p[key] = z["p_t"]
-    got = like.get_sky_frame_parameters(p)
+    got = like.sky_frame(p)
     ref = z[f"frame_{q}"]
     assert np.allclose(np.asarray(got["ra"]), ref[:, 0], rtol=0, atol=1e-12)
     assert np.allclose(np.asarray(got["dec"]), ref[:, 1], rtol=0, atol=1e-12)

@@ -39,11 +39,13 @@ def test_alone_and_in_the_mix(gpu):
     assert s["steps"] < 62  # requests were batched together
 
 
-def test_served_client_equals_direct_likelihood_for_sampler_dicts(gpu, tmp_path):
+@pytest.mark.parametrize("convert_on_client", [True, False])
+def test_served_client_equals_direct_likelihood_for_sampler_dicts(gpu, tmp_path, convert_on_client):
     """A sampler dictionary in chirp mass / mass ratio, sent by the IPC client
-    (one point and a batch), gives bit for bit what the direct likelihood's
-    log_likelihood_ratio / log_likelihood_ratio_batch give, and the client's
-    noise lnL is the likelihood's."""
+    (one point and a batch; converted in the client or in the server), gives
+    bit for bit what the direct likelihood's log_likelihood_ratio /
+    log_likelihood_ratio_batch give, and the client's noise lnL is the
+    likelihood's."""
     import threading
     from bilby_gb300.serving import LikelihoodServer, ServedLikelihood, serve_ipc
     w = [w for w in uneven_analyses(24, seed=11) if w.duration <= 16][0]
@@ -51,7 +53,7 @@ def test_served_client_equals_direct_likelihood_for_sampler_dicts(gpu, tmp_path)
     srv = LikelihoodServer(hbm_budget_bytes=20e9, max_points_per_step=20000).start()
     srv.add_analysis("a", like)
     listener = serve_ipc(srv, str(tmp_path / "gwl.sock"))
-    client = ServedLikelihood(str(tmp_path / "gwl.sock"), "a")
+    client = ServedLikelihood(str(tmp_path / "gwl.sock"), "a", convert_on_client=convert_on_client)
     p = draw_points(w, 64, np.random.default_rng(5))
     mc = (p["mass_1"] * p["mass_2"]) ** 0.6 / (p["mass_1"] + p["mass_2"]) ** 0.2
     sampler = {k: v for k, v in p.items() if k not in ("mass_1", "mass_2")}

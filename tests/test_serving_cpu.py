@@ -198,6 +198,10 @@ class _HostOnlyLikelihood:
     def parameters_block(self, parameters):
         return self.like.parameters_block(parameters)
 
+    @property
+    def preparer(self):
+        return self.like.preparer
+
     def noise_log_likelihood(self):
         return self._noise
 
@@ -222,8 +226,8 @@ SAMPLER_POINT = dict(chirp_mass=22.0, mass_ratio=0.7, chi_1=0.01, chi_2=-0.02, l
                      theta_jn=0.3, phase=1.0, ra=1.0, dec=0.2, psi=0.5, geocent_time=1126259642.0)
 
 
-def _sampler_client(address, key, conn):
-    like = ServedLikelihood(address, key)
+def _sampler_client(address, key, convert_on_client, conn):
+    like = ServedLikelihood(address, key, convert_on_client=convert_on_client)
     batch = {k: np.full(4, v) for k, v in SAMPLER_POINT.items()}
     batch["chirp_mass"] = np.array([15.0, 20.0, 25.0, 30.0])
     res = {"single": like.log_likelihood_ratio(dict(SAMPLER_POINT)), "batch": like.log_likelihood_ratio_batch(batch),
@@ -238,10 +242,12 @@ def _sampler_client(address, key, conn):
     conn.send((batch, res))
 
 
-def test_served_client_prepares_sampler_parameters_like_the_likelihood(monkeypatch):
+@pytest.mark.parametrize("convert_on_client", [True, False])
+def test_served_client_prepares_sampler_parameters_like_the_likelihood(monkeypatch, convert_on_client):
     """A sampler dict in chirp mass / mass ratio through the IPC client gives
     the block the direct likelihood builds (sky frame, conversion, jitter run
-    server-side), the server's noise lnL, and KeyError for a missing psi."""
+    in the client with the likelihood's preparer, or in the server), the
+    server's noise lnL, and KeyError for a missing psi."""
     like = _tf2_likelihood(monkeypatch)
     direct = like.parameters_block(dict(SAMPLER_POINT))
     assert direct[_capi.SLOT["mass_1"], 0] > direct[_capi.SLOT["mass_2"], 0] > 0
@@ -257,7 +263,7 @@ def test_served_client_prepares_sampler_parameters_like_the_likelihood(monkeypat
     listener = serve_ipc(srv, path)
     ctx = mp.get_context("spawn")
     r, w = ctx.Pipe(duplex=False)
-    proc = ctx.Process(target=_sampler_client, args=(path, "tf2", w))
+    proc = ctx.Process(target=_sampler_client, args=(path, "tf2", convert_on_client, w))
     proc.start()
     batch, res = r.recv()
     proc.join(60)
