@@ -7,6 +7,14 @@ from __future__ import annotations
 import numpy as np
 
 
+def _xp(x):
+    """numpy, or torch for a torch tensor (CUDA batches convert on the device)."""
+    if hasattr(x, "is_cuda"):
+        import torch
+        return torch
+    return np
+
+
 def _component_masses(p):
     """generate_component_masses (conversion.py:1826-1990), detector frame."""
     out = dict(p)
@@ -57,16 +65,17 @@ def convert_to_lal_binary_black_hole_parameters(parameters):
         key = f"chi_{idx}"
         if key in original and f"a_{idx}" not in original:
             converted[f"a_{idx}"] = abs(converted[key])
-            converted[f"cos_tilt_{idx}"] = np.sign(converted[key])
+            converted[f"cos_tilt_{idx}"] = _xp(converted[key]).sign(converted[key])
     for key in ("phi_jl", "phi_12"):
         converted.setdefault(key, 0.0)
     for angle in ("tilt_1", "tilt_2", "theta_jn"):
         if f"cos_{angle}" in converted:
             with np.errstate(invalid="ignore"):
-                converted[angle] = np.arccos(converted[f"cos_{angle}"])
+                converted[angle] = _xp(converted[f"cos_{angle}"]).arccos(converted[f"cos_{angle}"])
     if "delta_phase" in converted:
         with np.errstate(invalid="ignore"):
-            converted["phase"] = np.mod(converted["delta_phase"] - np.sign(np.cos(converted["theta_jn"]))
-                                        * converted["psi"], 2 * np.pi)
+            xp = _xp(converted["delta_phase"])
+            converted["phase"] = xp.remainder(converted["delta_phase"] - xp.sign(xp.cos(converted["theta_jn"]))
+                                              * converted["psi"], 2 * np.pi)
     added = [k for k in converted if k not in original]
     return converted, added

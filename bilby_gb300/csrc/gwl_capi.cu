@@ -106,6 +106,7 @@ struct gwl_analysis {
   double* mb_band_df = nullptr;
   float2* mb_basis = nullptr;
   float2* mb_lw[kMaxDet] = {};
+  double* mb_l2prefix[kMaxDet] = {};
   double mb_lw_scale[kMaxDet] = {};
   double* mb_qprefix[kMaxDet] = {};
   int mb_tm = 0;  // multi-banding time-marginalisation tables set for these bands
@@ -370,6 +371,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.mb_basis = a->mb_basis;
   for (int d = 0; d < a->n_det; ++d) {
     L.mb_lw[d] = a->mb_lw[d];
+    L.mb_l2prefix[d] = a->mb_l2prefix[d];
     L.mb_lw_scale[d] = a->mb_lw_scale[d];
     L.mb_qprefix[d] = a->mb_qprefix[d];
   }
@@ -495,7 +497,21 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       GWL_CUDA(launch_relbin(L, s));
     } else if (a->multiband) {
       if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2) {
+        // points whose error bound exceeds the tolerance are marked by the
+        // mixed kernel and recomputed by the float64 one
+        L.rf_tol = a->refine_tol;
+        if (L.rf_tol > 0) {
+          L.rf_count = a->d_order_hist;
+          a->last_rf_count = L.rf_count;
+          GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
+        }
         GWL_CUDA(launch_multiband_mixed(L, s));
+        if (L.rf_tol > 0) {
+          LaunchArgs R = L;
+          R.precision = GWL_PRECISION_FP64;
+          R.mb_refine_only = 1;
+          GWL_CUDA(launch_multiband(R, s));
+        }
       } else {
         GWL_CUDA(launch_multiband(L, s));
       }
@@ -518,18 +534,21 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     ordering_with_marks(L);
     a->last_rf_count = L.rf_count;
     GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * (2 * L.order_keys + 1), s));
-  } else if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN && !(a->time_marg && d_out) &&
-             L.rf_tol > 0) {
-    // sine-Gaussian: the finalize marks the points whose error bound exceeds
-    // the tolerance and counts them here; k_sg_refine recomputes them
-    L.rf_count = a->d_order_hist;
+  } else if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN && !(a->time_marg && d_out)) {
+    // sine-Gaussian: points ordered by centre frequency; the finalize marks
+    // the points whose error bound exceeds the tolerance and counts them
+    // after the histogram; k_sg_refine recomputes them
+    L.order = a->d_order;
+    L.order_hist = a->d_order_hist;
+    ordering_by_peak(L);
+    if (!(L.rf_tol > 0)) L.rf_count = nullptr;
     a->last_rf_count = L.rf_count;
-    GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
+    GWL_CUDA(cudaMemsetAsync(L.order_hist, 0, sizeof(int32_t) * (2 * L.order_keys + 1), s));
   } else {
     L.rf_tol = 0.0;
   }
   GWL_CUDA(launch_prologue(L, s));
-  if (ordered) GWL_CUDA(launch_order(L, s));
+  if (ordered || L.order) GWL_CUDA(launch_order(L, s));
   if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
   if (a->time_marg && d_out) {
     if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN) {
@@ -1292,10 +1311,16 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
     }
     a->mb_lw_scale[d] = lmax > 0 ? lmax : 1.0;
     std::vector<float2> lw(n_points);
-    for (int64_t k = 0; k < n_points; ++k)
+    std::vector<double> l2(n_points + 1, 0.0);
+    KahanSum acc2;
+    for (int64_t k = 0; k < n_points; ++k) {
       lw[k] = make_float2((float)(lr[k] / a->mb_lw_scale[d]), (float)(li[k] / a->mb_lw_scale[d]));
+      acc2.add((double)lw[k].x * lw[k].x + (double)lw[k].y * lw[k].y);
+      l2[k + 1] = acc2.value();
+    }
     if ((rc = upload(a, &a->mb_lw[d], lw))) return rc;
     if ((rc = upload(a, &a->mb_qprefix[d], qp))) return rc;
+    if ((rc = upload(a, &a->mb_l2prefix[d], l2))) return rc;
   }
   std::vector<int64_t> bs(band_start, band_start + n_bands + 1);
   std::vector<double> bd(band_df, band_df + n_bands);

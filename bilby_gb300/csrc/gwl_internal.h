@@ -164,6 +164,8 @@ struct LaunchArgs {
   const float2* mb_lw[kMaxDet];         // [mb_points]
   double mb_lw_scale[kMaxDet];
   const double* mb_qprefix[kMaxDet];    // [mb_points + 1]
+  const double* mb_l2prefix[kMaxDet];   // [mb_points + 1] prefix sums of |mb_lw|^2 (error bound of the mixed kernel)
+  int mb_refine_only;                   // float64 multi-banding kernel: only the points marked by the mixed one
   // multi-banding with time marginalisation: for each full-resolution index
   // k < n_fft the banded points scattered there, mb_tm_src[mb_tm_ptr[k] ..
   // mb_tm_ptr[k + 1]); a code c >= 0 is banded point c, c < 0 is banded point
@@ -254,6 +256,7 @@ void order_layout(int64_t n_chunks, int* keys, int* shift);
 // half); the marked count follows the 2 * order_keys histogram words (zeroed
 // with them: 2 * order_keys + 1 words in all).  order_hist, if set, must hold them.
 void ordering_with_marks(LaunchArgs& L);
+void ordering_by_peak(LaunchArgs& L);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 size_t time_marg_work_bytes(const LaunchArgs& a);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,

@@ -29,6 +29,14 @@ __device__ __forceinline__ double par(const LaunchArgs& a, int slot, int64_t i) 
 // that (buckets in descending order) they fill the first slots
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int order_key(const LaunchArgs& a, const PointRec& r) {
+  if (a.model == GWL_MODEL_SINEGAUSSIAN) {
+    // sine-Gaussian: the bin of the centre frequency, so that the points of a
+    // warp walk their Gaussians (k_mixed_sg) over runs of nearly equal length
+    if (!r.valid) return 0;
+    const double kp = floor((r.sg_f0 - a.freq[a.k_base]) / a.step);
+    const double n = (double)(a.n_chunks * a.chunk);
+    return (int)((int64_t)fmin(fmax(kp, 0.0), n) >> a.order_shift);
+  }
   if (!r.valid || r.k_end <= r.k_start) return 0;
   int64_t c = (r.k_end - a.k_base + a.chunk - 1) / a.chunk;
   c = c < 0 ? 0 : (c > a.n_chunks ? a.n_chunks : c);
@@ -873,16 +881,22 @@ __global__ void __launch_bounds__(kAccThreads) k_mixed_tf2_acc(LaunchArgs a) {
 // M_d = |(Fp P, Fx X)| and (a_d, c_d) = (Fp P, Fx X) / M_d.  Four partial sums:
 //   0, 1: Re, Im of sum (a hp + i c hx) e^{i theta} w      (float32, Kahan)
 //   2:    sum (a^2 hp^2 + c^2 hx^2) v                      (float-float)
-//   3:    sum (|a hp| + |c hx|)^2 |w|^2                    (float32: error norm)
+//   3:    sum (a^2 hp^2 + c^2 hx^2) |w|^2                  (float32: error norm)
+// The 0.32 fixed-point phase of bin k is exact; its float32 rounding is undone
+// to first order (see the loop), so the phase contributes no error.
+// Points are taken in the order of their centre frequencies (order_key), so
+// that the threads of a warp walk runs of nearly equal lengths.
 // <h|h> is float-float throughout: the Gaussians come from the float-float
 // multiplicative recurrence g(k + s) = g(k) r(k), r(k + s) = r(k) c with
 // c = exp(-2 A df^2) (A = pi^2 tau^2, s = +-1), walked away from the peak so
-// that g only shrinks, restarted from float64 values every kSgSegment bins
-// (the recurrence's relative error grows as n^2 2^-47, about 2e-10 at 256);
+// that g only shrinks, started from float64 values at the first bin of each
+// walk (each float-float product errs by about 2^-48, so after n steps the
+// error of g is a sum of n random-walk errors of r: 3.6e-15 n^1.5 / sqrt(3),
+// 2.4e-11 at n = 512, with a worst case of n^2 2^-48 / 2 = 4.7e-10);
 // v = v_hi + v_lo is the float-float inverse PSD.  <d|h> sums float32 terms
 // whose rounding errors are independent from bin to bin; the finalize bounds
 // them by sum 3 and sends points over the tolerance to k_sg_refine.
-constexpr int kSgSegment = 256;
+constexpr int kSgSegment = kChunkMixed;
 
 __device__ __forceinline__ void ff_mul_to(float& h, float& l, float bh, float bl) {
   const float p = __fmul_rn(h, bh);
@@ -901,8 +915,9 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
   __shared__ __align__(16) float s_vl[D][CH];
   __shared__ uint64_t bar;
   const int64_t k0 = a.k_base + (int64_t)blockIdx.y * CH;
-  const int64_t i = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
-  const bool have = i < a.B;
+  const int64_t slot = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
+  const bool have = slot < a.B;
+  const int64_t i = have && a.order ? (int64_t)a.order[slot] : slot;  // points ordered by centre frequency
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     mbar_fence_init();
@@ -971,11 +986,19 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
           const uint32_t k = (uint32_t)(k0 + j);
 #pragma unroll
           for (int d = 0; d < D; ++d) {
-            // The phase is linear in k: use the accurate sincospi on the exact
-            // fraction so that no approximation error repeats coherently.
-            const float ph = fixed_phase_cycles(k, xl[d], xh[d]);
+            // The phase is linear in k: the accurate sincospi of the 0.32
+            // fixed-point fraction rounded to float32, corrected to first
+            // order by the exact integer residual of that rounding, so that
+            // no approximation error repeats coherently and the phase error
+            // is below 1e-14 rad.
+            const int top = (int)(k * xh[d] + __umulhi(k, xl[d]));
+            const float fc = __int2float_rn(top);
+            const float eps = __int2float_rn((int)((long long)top - __float2ll_rz(fc))) * 1.4629180792671596e-09f;
             float sn, cs;
-            sincospif(2.0f * ph, &sn, &cs);
+            sincospif(fc * 4.656612873077393e-10f, &sn, &cs);  // 2 pi top 2^-32 rad
+            const float c1 = __fmaf_rn(-eps, sn, cs);
+            sn = __fmaf_rn(eps, cs, sn);
+            cs = c1;
             const float2 w = s_w[d][j];
             const float ere = w.x * cs - w.y * sn, eim = w.x * sn + w.y * cs;
             const float u = ad[d] * hph, z = cd[d] * hxh;
@@ -992,8 +1015,8 @@ __global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
             const float se = __fadd_rn(__fadd_rn(__fsub_rn(q1, __fsub_rn(sh, sb)), __fsub_rn(q2, sb)),
                                        __fadd_rn(q1e, q2e));
             ff_mac(hh[d], hl[d], sh, se, s_vh[d][j], s_vl[d][j]);
-            const float m = fabsf(u) + fabsf(z);
-            e2[d] = __fmaf_rn(m * m, __fmaf_rn(w.x, w.x, w.y * w.y), e2[d]);
+            // |term|^2 = (u^2 + z^2) |w|^2 (the rotation keeps the modulus)
+            e2[d] = __fmaf_rn(__fmaf_rn(u, u, z * z), __fmaf_rn(w.x, w.x, w.y * w.y), e2[d]);
           }
           ff_mul_to(g1.hi, g1.lo, r1.hi, r1.lo);
           ff_mul_to(r1.hi, r1.lo, cc.hi, cc.lo);
@@ -1126,15 +1149,17 @@ __device__ __forceinline__ void sum_groups(const LaunchArgs& a, int64_t i, int d
     for (int t = 0; t < NQ; ++t) p[t] += q[c * gs + (int64_t)t * a.B];
 }
 
-// Error bound of the mixed sine-Gaussian lnL (k_mixed_sg): its <d|h> terms
-// carry independent float32 rounding errors of relative size below about
-// 2.5e-7 (weights, the phase fraction, the Gaussian's high word, products), so
-// their sum errs by kSgRandomErr (a 4-sigma margin) times the Euclidean norm of
-// the terms; the float32 antenna factors add a coherent kSgCoherentErr |<d|h>|
-// and the float-float <h|h> (recurrence, inverse PSD) kSgHhErr <h|h>.
-constexpr double kSgRandomErr = 1e-6;
+// Error bound of the mixed sine-Gaussian lnL (k_mixed_sg).  Each <d|h> term
+// carries six rounding errors of at most 2^-24 relative (the two weight
+// components, the Gaussian's high word, sincospi's result, the product and
+// the FMA), independent from bin to bin: an rms of about 8.5e-8 per term, so
+// the sum errs by less than kSgRandomErr (4 sigma) times the Euclidean norm of
+// the terms.  The float32 antenna factors add a coherent kSgCoherentErr
+// |<d|h>|; the float-float <h|h> errs by less than kSgHhErr relative (the
+// recurrence's worst case over a 512-bin walk is 4.7e-10).
+constexpr double kSgRandomErr = 3.5e-7;
 constexpr double kSgCoherentErr = 1e-7;
-constexpr double kSgHhErr = 2e-9;
+constexpr double kSgHhErr = 5e-10;
 
 __device__ void detector_totals(const LaunchArgs& a, int64_t i, int64_t G, const PointRec& r, double* dh_re,
                                 double* dh_im, double* hh, double* err = nullptr) {
@@ -1546,6 +1571,7 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband(LaunchArgs a) {
   const int64_t i = (int64_t)blockIdx.x * kRelbinWarps + (threadIdx.x >> 5);
   if (i >= a.B) return;  // uniform over the warp
   const PointRec& r = a.rec[i];
+  if (a.mb_refine_only && !r.refine) return;  // uniform over the warp
   double sr = 0.0, si = 0.0, hh = 0.0;
   if (r.valid) {
     double fp[D], fx[D], w2[D];
@@ -1608,6 +1634,8 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband(LaunchArgs a) {
 // 8-term float32 partials folded into float-float, then float64 over the
 // warp.  <h|h> needs no per-frequency work: A^2 |Q_d|^2 times the prefix sum
 // of f^(-7/3) quad over the point's band.
+constexpr double kMbRandomErr = 1e-6;
+
 template <int D>
 __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArgs a) {
   const int lane = threadIdx.x & 31;
@@ -1679,9 +1707,11 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArg
         for (int d = 0; d < D; ++d) {
           const uint64_t full = base + Y[d] + idx * X[d];
           const uint32_t top = (uint32_t)((full + 0x80000000ull) >> 32);
-          const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
+          // sincospi of the exact fraction (cycles in [-1/2, 1/2)): rounding
+          // errors independent from term to term, bounded in the epilogue
+          const float ph = __fmul_rn(__int2float_rn((int)top), 4.656612873077393e-10f);  // 2 * 2^-32
           float sn, cs;
-          __sincosf(ph, &sn, &cs);
+          sincospif(ph, &sn, &cs);
           const float2 L = __ldg(a.mb_lw[d] + k);
           // h_d L with h_d proportional to exp(-i phase)
           pre[d] = __fmaf_rn(cs, L.x, __fmaf_rn(sn, L.y, pre[d]));
@@ -1714,12 +1744,22 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArg
     if (lane == 0) {
       // sum_d A Q_d P_d scale_d, Q_d = Fp (1 + c^2) / 2 - i Fx c
       const double ci = r.cos_i, pfac = (1.0 + ci * ci) / 2.0;
+      double err = 0.0;
       for (int d = 0; d < D; ++d) {
         const double qr = r.fp[d] * pfac, qi = -r.fx[d] * ci;
         const double pr = P_re[d] * a.mb_lw_scale[d], pm = P_im[d] * a.mb_lw_scale[d];
         sr += r.amp * (qr * pr - qi * pm);
         si += r.amp * (qr * pm + qi * pr);
         hh += r.amp * r.amp * (qr * qr + qi * qi) * (a.mb_qprefix[d][kb1] - a.mb_qprefix[d][kb0]);
+        // float32 terms with independent relative errors below about 2.5e-7
+        // (the phase fraction, sincospi, the weight, two FMAs): kMbRandomErr
+        // (a 4-sigma margin) times their Euclidean norm
+        err += kMbRandomErr * r.amp * hypot(qr, qi) * a.mb_lw_scale[d] *
+               sqrt(fmax(a.mb_l2prefix[d][kb1] - a.mb_l2prefix[d][kb0], 0.0));
+      }
+      if (a.rf_tol > 0 && a.rf_count && !(err <= a.rf_tol)) {
+        a.rec[i].refine = 1;
+        atomicAdd(a.rf_count, 1);
       }
     }
   }
@@ -1902,6 +1942,15 @@ void order_layout(int64_t n_chunks, int* keys, int* shift) {
   while ((n_chunks >> sh) + 1 > kOrderMaxKeys) ++sh;
   *shift = sh;
   *keys = (int)(n_chunks >> sh) + 1;
+}
+
+void ordering_by_peak(LaunchArgs& L) {
+  int keys = 0, shift = 0;
+  order_layout(L.n_chunks * L.chunk, &keys, &shift);
+  L.order_shift = shift;
+  L.order_half = 0;
+  L.order_keys = keys;
+  L.rf_count = L.order_hist ? L.order_hist + 2 * L.order_keys : nullptr;
 }
 
 void ordering_with_marks(LaunchArgs& L) {

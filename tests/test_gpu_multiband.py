@@ -125,3 +125,27 @@ def test_mixed_precision_loud_points_run(gpu, tmp_path):
     block = params_block(like._prepare(p))
     mixed = like.analysis.log_likelihood_ratio_host(block, "mixed")
     assert np.all(np.isfinite(mixed))
+
+
+def test_mixed_holds_1e3_and_refines_loud_templates(gpu, tmp_path):
+    """The mixed-precision multi-banded kernel against the float64 one on
+    prior draws and on templates 100 to 10^4 times louder (distances down to
+    0.02 Mpc, <h|h> up to ~1e11): the error bound sends the loud ones to the
+    float64 kernel and every result stays within 1e-3; of the prior draws
+    (20-200 Mpc) at most 1% need recomputation."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    like, _ = make("none", tmp_path)
+    an = like.analysis
+    w = WORKLOADS["tf2_128s"]
+    p = draw_points(w, 2000, np.random.default_rng(8))
+    mixed = an.log_likelihood_ratio_host(params_block(p), "mixed")
+    assert an.last_refined() <= 20
+    fp64 = an.log_likelihood_ratio_host(params_block(p), "fp64")
+    assert np.max(np.abs(mixed - fp64)) <= 1e-3, np.max(np.abs(mixed - fp64))
+    loud = draw_points(w, 300, np.random.default_rng(9))
+    loud["luminosity_distance"] = 10 ** np.random.default_rng(10).uniform(np.log10(0.02), np.log10(2.0), 300)
+    mixed = an.log_likelihood_ratio_host(params_block(loud), "mixed")
+    assert an.last_refined() > 0
+    fp64 = an.log_likelihood_ratio_host(params_block(loud), "fp64")
+    assert np.max(np.abs(mixed - fp64)) <= 1e-3, np.max(np.abs(mixed - fp64))
