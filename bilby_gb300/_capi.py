@@ -63,6 +63,8 @@ SIGNATURES = {
     "gwl_noise_log_likelihood": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "gwl_set_time_marginalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                     ctypes.c_double]),
+    "gwl_set_time_prior": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int64, ctypes.c_double,
+                                          ctypes.c_double]),
     "gwl_set_phase_marginalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "gwl_set_distance_marginalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_int32,
                                                         c_double_p, ctypes.c_int32, c_double_p, c_double_p,

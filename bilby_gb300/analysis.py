@@ -93,6 +93,16 @@ class Analysis:
                                                            float(t_max)), "gwl_set_time_marginalization")
         self.time_marginalization = bool(enable)
 
+    def set_time_prior(self, density=None, t0: float = 0.0, h: float = 1.0):
+        """A geocent_time prior other than Uniform (``gwl_set_time_prior``):
+        its density on the nodes t0 + g h; None returns to Uniform."""
+        if density is None:
+            _capi.check(self._lib.gwl_set_time_prior(self._h, None, 0, 0.0, 1.0), "gwl_set_time_prior")
+            return
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        _capi.check(self._lib.gwl_set_time_prior(self._h, _capi.dptr(d), len(d), float(t0), float(h)),
+                    "gwl_set_time_prior")
+
     def set_phase_marginalization(self, enable: bool):
         _capi.check(self._lib.gwl_set_phase_marginalization(self._h, int(enable)), "gwl_set_phase_marginalization")
         self.phase_marginalization = bool(enable)

@@ -74,6 +74,10 @@ struct gwl_analysis {
   // marginalisation
   int time_marg = 0, jitter = 0, phase_marg = 0, dist_marg = 0;
   double t_min = 0, t_max = 0;
+  double* tm_prior = nullptr;  // time prior density on a uniform grid (nullptr: Uniform)
+  float* tm_prior_f = nullptr;
+  int64_t tm_prior_n = 0;
+  double tm_prior_t0 = 0, tm_prior_inv_h = 0;
   double* tx = nullptr;
   double* ty = nullptr;
   double* tc = nullptr;
@@ -346,6 +350,11 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.tm_step = a->duration / (double)(a->n_bins - 1);  // linspace(0, T, L + 1) spacing, L = n_bins - 1
   L.tm_inv_step = (double)(a->n_bins - 1) / a->duration;
   L.tm_prob = a->t_max > a->t_min ? 1.0 / (a->t_max - a->t_min) : 0.0;
+  L.tm_prior = a->tm_prior;
+  L.tm_prior_f = a->tm_prior_f;
+  L.tm_prior_n = a->tm_prior_n;
+  L.tm_prior_t0 = a->tm_prior_t0;
+  L.tm_prior_inv_h = a->tm_prior_inv_h;
   L.inv_ref_dist = a->ref_dist > 0 ? 1.0 / a->ref_dist : 0.0;
   L.relbin = a->relbin;
   L.rb_edges = a->rb_edges;
@@ -1109,6 +1118,43 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
   a->jitter = jitter ? 1 : 0;
   a->t_min = t_min;
   a->t_max = t_max;
+  return GWL_OK;
+}
+
+int gwl_set_time_prior(gwl_analysis* a, const double* density, int64_t n, double t0, double h) {
+  if (!a || (n > 0 && !density)) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (n == 0) {  // back to the Uniform prior of the time-marginalisation window
+    a->tm_prior = nullptr;
+    a->tm_prior_f = nullptr;
+    a->tm_prior_n = 0;
+    return GWL_OK;
+  }
+  int e2 = 0;
+  if (n < 4 || !(h > 0) || std::frexp(h, &e2) != 0.5 || !std::isfinite(t0) || std::fmod(t0, h) != 0.0) {
+    set_error("time prior table: need n >= 4 nodes, h a power of two and t0 a multiple of h");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::vector<double> p(density, density + n);
+  std::vector<float> pf(n);
+  for (int64_t k = 0; k < n; ++k) {
+    if (!(p[k] >= 0.0) || !std::isfinite(p[k])) {
+      set_error("time prior table: densities must be finite and non-negative");
+      return GWL_ERR_ARGUMENT;
+    }
+    pf[k] = (float)p[k];
+  }
+  // earlier tables stay allocated (in the analysis's table list) until the
+  // analysis is destroyed: a launch in flight may still read them
+  int rc;
+  if ((rc = upload(a, &a->tm_prior, p))) return rc;
+  if ((rc = upload(a, &a->tm_prior_f, pf))) return rc;
+  a->tm_prior_n = n;
+  a->tm_prior_t0 = t0;
+  a->tm_prior_inv_h = 1.0 / h;
   return GWL_OK;
 }
 

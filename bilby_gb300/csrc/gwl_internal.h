@@ -163,6 +163,13 @@ struct LaunchArgs {
   const float2* mb_basis;               // [mb_points][kNumBasis]
   const float2* mb_lw[kMaxDet];         // [mb_points]
   double mb_lw_scale[kMaxDet];
+  // time marginalisation with a prior other than Uniform: its density on the
+  // nodes t0 + g h (g < tm_prior_n, h a power of two), read by 4-node Lagrange
+  // interpolation; tm_prior == nullptr means the Uniform density tm_prob
+  const double* tm_prior;
+  const float* tm_prior_f;
+  int64_t tm_prior_n;
+  double tm_prior_t0, tm_prior_inv_h;
   const double* mb_qprefix[kMaxDet];    // [mb_points + 1]
   const double* mb_l2prefix[kMaxDet];   // [mb_points + 1] prefix sums of |mb_lw|^2 (error bound of the mixed kernel)
   int mb_refine_only;                   // float64 multi-banding kernel: only the points marked by the mixed one

@@ -29,7 +29,34 @@
 namespace gwl {
 
 constexpr int kTmThreads = 512;
-constexpr int kTmTwiddleRows = 128;  // two-level twiddle tables: L / 2 <= 128 * 128
+constexpr int kTmTwiddleRows = 128;
+
+// The density of a geocent_time prior other than Uniform at GPS time t
+// (LaunchArgs::tm_prior): Lagrange interpolation through the four table nodes
+// around t, shifted inwards at the ends of the table (the nodes lie inside the
+// prior's support, so a time between a support edge and the first node is
+// extrapolated by less than one node spacing); zero beyond.  t - t0 is exact
+// (t0 and the nodes are multiples of a power-of-two step), so a sample on a
+// node reads that node's density exactly.
+__device__ __forceinline__ double tm_prior_density(const LaunchArgs& a, double t) {
+  const double x = (t - a.tm_prior_t0) * a.tm_prior_inv_h;
+  if (!(x >= -1.0 && x <= (double)a.tm_prior_n)) return 0.0;
+  const int64_t g = max((int64_t)0, min((int64_t)floor(x) - 1, a.tm_prior_n - 4));
+  const double u = x - (double)g, u1 = u - 1.0, u2 = u - 2.0, u3 = u - 3.0;
+  const double* p = a.tm_prior + g;
+  const double v = (p[3] * u * u1 * u2 - p[0] * u1 * u2 * u3) / 6.0 + (p[1] * u * u2 * u3 - p[2] * u * u1 * u3) / 2.0;
+  return fmax(v, 0.0);
+}
+
+__device__ __forceinline__ float tm_prior_density_f(const LaunchArgs& a, double t) {
+  const double x = (t - a.tm_prior_t0) * a.tm_prior_inv_h;
+  if (!(x >= -1.0 && x <= (double)a.tm_prior_n)) return 0.f;
+  const int64_t g = max((int64_t)0, min((int64_t)floor(x) - 1, a.tm_prior_n - 4));
+  const float u = (float)(x - (double)g), u1 = u - 1.f, u2 = u - 2.f, u3 = u - 3.f;
+  const float* p = a.tm_prior_f + g;
+  const float v = (p[3] * u * u1 * u2 - p[0] * u1 * u2 * u3) * (1.f / 6.f) + (p[1] * u * u2 * u3 - p[2] * u * u1 * u3) * 0.5f;
+  return fmaxf(v, 0.f);
+}  // two-level twiddle tables: L / 2 <= 128 * 128
 
 template <bool MIXED>
 struct TmTypes;
@@ -689,6 +716,19 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       const double lin = a.tm_first ? ((j + 1 == L) ? a.duration : (double)(j + 1) * step) : (double)j * step;
       const double t = (a.start_time0 + lin) + jit;
       if (!(t >= a.t_min && t <= a.t_max)) continue;
+      // base.py:807: prior(t_j) delta_tc; a Uniform prior's constant is applied once, below
+      double lw = 0.0;
+      if (a.tm_prior) {
+        if constexpr (MIXED) {
+          const float pw = tm_prior_density_f(a, t);
+          if (!(pw > 0.f)) continue;
+          lw = (double)__logf(pw);
+        } else {
+          const double pw = tm_prior_density(a, t);
+          if (!(pw > 0.0)) continue;
+          lw = log(pw);
+        }
+      }
       const C x = buf[P(j)];
       double l;
       if constexpr (MIXED) {
@@ -703,6 +743,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         } else {
           l = (double)xr - hh / 2;
         }
+        l += lw;
         if (l > m) {
           acc = isfinite(m) ? acc * (double)__expf((float)(m - l)) + 1.0 : 1.0;
           m = l;
@@ -719,6 +760,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         } else {
           l = xr - hh / 2;
         }
+        l += lw;
         if (l > m) {
           acc = isfinite(m) ? acc * exp(m - l) + 1.0 : 1.0;
           m = l;
@@ -775,7 +817,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
     }
     if (threadIdx.x == 0) {
-      const double amax = redm[0], total = reds[0] * prob * a.delta_tc;
+      const double amax = redm[0], total = reds[0] * (a.tm_prior ? 1.0 : prob) * a.delta_tc;
       double lnl;
       if (!r.valid) lnl = -1.7976931348623157e308;
       else if (!isfinite(amax)) lnl = amax;
@@ -920,7 +962,8 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
           if (!in_prior) continue;
         }
         double l;
-        if (!ok) {
+        const double pw = a.tm_prior ? tm_prior_density(a, t) : 1.0;  // base.py:807, prior(t_j)
+        if (!ok || !(pw > 0.0)) {
           l = -INFINITY;
         } else if (a.dist_marg) {
           const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
@@ -930,6 +973,7 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
         } else {
           l = xr - hh / 2;
         }
+        if (a.tm_prior && isfinite(l)) l += log(pw);
         if (l > m) {
           acc = isfinite(m) ? acc * exp(m - l) + 1.0 : 1.0;
           m = l;
@@ -958,7 +1002,7 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
       __syncthreads();
     }
     if (threadIdx.x == 0) {
-      const double amax = redm[0], total = reds[0] * prob * a.delta_tc;
+      const double amax = redm[0], total = reds[0] * (a.tm_prior ? 1.0 : prob) * a.delta_tc;
       double lnl;
       if (!r.valid) lnl = -1.7976931348623157e308;
       else if (!isfinite(amax)) lnl = amax;

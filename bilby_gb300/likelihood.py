@@ -64,6 +64,29 @@ REQUIRED_PARAMETERS = {
 }
 
 
+def time_prior_table(prior, t_lo, t_hi, delta_tc):
+    """The density of a geocent_time prior for the time-marginalised kernels:
+    ``(density, t0, h)`` on the nodes t0 + g h, g < len(density), that lie in
+    [max(prior.minimum, t_lo), min(prior.maximum, t_hi)].  h is the power of
+    two at most delta_tc / 8 and t0 a multiple of it, so every node time is
+    exact in float64 and the kernels' 4-node interpolation reads a time on a
+    node exactly; Lagrange interpolation at spacing delta_tc / 8 leaves a
+    relative error of order (h / width)^4 for a prior of that width.  Returns
+    None for a Uniform prior (a constant weight)."""
+    if type(prior).__name__ == "Uniform":
+        return None
+    lo = max(float(prior.minimum), float(t_lo))
+    hi = min(float(prior.maximum), float(t_hi))
+    h = 2.0 ** np.floor(np.log2(delta_tc / 8))
+    t0 = np.ceil(lo / h) * h
+    n = int(np.floor((hi - t0) / h)) + 1
+    if n < 4:
+        raise ValueError("the geocent_time prior's support is narrower than four table nodes")
+    grid = t0 + h * np.arange(n)
+    density = np.asarray(prior.prob(grid), dtype=np.float64)
+    return np.nan_to_num(density, nan=0.0, posinf=0.0, neginf=0.0), float(t0), float(h)
+
+
 def d_inner_h_ref_axis(n, phase_marginalization):
     """base.py:904-914."""
     if phase_marginalization:
@@ -266,15 +289,16 @@ class GravitationalWaveTransient(_Base):
             return Uniform(-self._delta_tc / 2, self._delta_tc / 2, boundary="periodic", name="time_jitter")
 
     def _setup_time_marginalization(self):
-        """base.py:1027-1035; the GPU path needs a Uniform geocent_time prior."""
+        """base.py:1027-1035, with the prior's density tabulated for the kernels
+        when the geocent_time prior is not Uniform (``time_prior_table``)."""
         fs = self.waveform_generator.sampling_frequency
         self._delta_tc = 2 / fs
         duration = self.interferometers[0].duration
         self._times = self._start_time + np.linspace(0, duration, int(duration / 2 * fs + 1))[1:]
         tp = self.priors["geocent_time"]
-        if type(tp).__name__ != "Uniform":
-            raise NotImplementedError("time marginalisation on the GPU needs a Uniform geocent_time prior")
         self.time_prior_array = tp.prob(self._times) * self._delta_tc
+        self._time_prior_table = time_prior_table(tp, self._start_time - self._delta_tc,
+                                                  self._start_time + duration + self._delta_tc, self._delta_tc)
 
     def _setup_distance_marginalization(self, lookup_table=None):
         """base.py:916-992: load a matching cached table or build it (on the GPU)."""
@@ -369,15 +393,22 @@ class GravitationalWaveTransient(_Base):
 
     def _build_analysis(self):
         an = self._new_analysis(self.interferometers)
+        self._configure_analysis(an)
+        self._analysis = an
+
+    def _configure_analysis(self, an):
+        """The marginalisation settings of this likelihood on a device analysis."""
         if self.time_marginalization:
             tp = self.priors["geocent_time"]
             an.set_time_marginalization(True, self.jitter_time, tp.minimum, tp.maximum)
+            table = getattr(self, "_time_prior_table", None)
+            if table is not None:
+                an.set_time_prior(*table)
         if self.phase_marginalization:
             an.set_phase_marginalization(True)
         if self.distance_marginalization:
             tx, ty, c = self._spline_tck
             an.set_distance_marginalization(True, tx, ty, c, self._spline_bbox, self._ref_dist)
-        self._analysis = an
 
     # ------------------------------------------------------------------
     # pickling: the device handle is rebuilt in the receiving process
@@ -442,7 +473,10 @@ class GravitationalWaveTransient(_Base):
         """Evaluate a batch.  ``parameters`` maps names to equal-length numpy
         arrays (result: numpy float64) or to CUDA tensors (result: a CUDA
         float64 tensor, computed asynchronously on torch's current stream)."""
-        precision = precision or self.precision
+        return self._batch_on(self.analysis, parameters, precision or self.precision, out)
+
+    def _batch_on(self, analysis, parameters, precision, out=None):
+        """``log_likelihood_ratio_batch`` on a given device analysis."""
         first = next(iter(parameters.values()))
         if hasattr(first, "is_cuda") and first.is_cuda:
             import torch
@@ -459,10 +493,10 @@ class GravitationalWaveTransient(_Base):
                     block[slot] = v.to(torch.float64) if hasattr(v, "to") else float(v)
             res = out if out is not None else torch.empty(n, dtype=torch.float64, device=first.device)
             stream = torch.cuda.current_stream(first.device).cuda_stream
-            self.analysis.log_likelihood_ratio_device(block.data_ptr(), n, res.data_ptr(), precision, stream)
+            analysis.log_likelihood_ratio_device(block.data_ptr(), n, res.data_ptr(), precision, stream)
             return res
         arrays = {k: np.asarray(v, dtype=np.float64) for k, v in parameters.items()}
-        return self.analysis.log_likelihood_ratio_staged(self._prepare(arrays), precision)
+        return analysis.log_likelihood_ratio_staged(self._prepare(arrays), precision)
 
     def log_likelihood_ratio_from_unit_cube(self, unit, device_priors, precision=None, out=None):
         """lnL ratios of a batch given as unit-cube samples: ``unit`` is a CUDA

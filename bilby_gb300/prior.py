@@ -112,6 +112,30 @@ class Gaussian(Prior):
         return np.exp(-(self.mu - val) ** 2 / (2 * self.sigma ** 2)) / (2 * np.pi) ** 0.5 / self.sigma
 
 
+class TruncatedGaussian(Prior):
+    """A Gaussian of mean mu and width sigma restricted to [minimum, maximum]
+    (analytical.py:583-640)."""
+
+    def __init__(self, mu, sigma, minimum, maximum, **kwargs):
+        super().__init__(minimum, maximum, **kwargs)
+        self.mu, self.sigma = mu, sigma
+
+    @property
+    def normalisation(self):
+        from scipy.special import erf
+        return (erf((self.maximum - self.mu) / 2 ** 0.5 / self.sigma)
+                - erf((self.minimum - self.mu) / 2 ** 0.5 / self.sigma)) / 2
+
+    def rescale(self, val):
+        from scipy.special import erf, erfinv
+        return erfinv(2 * val * self.normalisation + erf((self.minimum - self.mu) / 2 ** 0.5 / self.sigma)) \
+            * 2 ** 0.5 * self.sigma + self.mu
+
+    def prob(self, val):
+        return np.exp(-(self.mu - val) ** 2 / (2 * self.sigma ** 2)) / (2 * np.pi) ** 0.5 / self.sigma \
+            / self.normalisation * self.is_in_prior_range(val)
+
+
 class Interped(Prior):
     """A density tabulated at points ``xx`` (bilby/core/prior/interpolated.py:10-160):
     linear interpolation of ``yy`` onto an evenly spaced grid of the same

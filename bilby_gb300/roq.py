@@ -1,7 +1,7 @@
 """Drop-in GPU ``ROQGravitationalWaveTransient`` (reduced-order quadrature).
 
 Same constructor as ``bilby.gw.likelihood.ROQGravitationalWaveTransient``
-(bilby/gw/likelihood/roq.py:14-215) for one linear and one quadratic basis.
+(bilby/gw/likelihood/roq.py:14-215).
 The weights -- time-dependent linear weights by inverse FFTs of d/S times each
 basis element, quadratic weights from 1/S (roq.py:736-1007) -- are computed
 once on the host in float64, or taken from a weights dictionary; every
@@ -15,8 +15,16 @@ point contracts the weight rows its detector times read, interpolates <d|h>
 at every sample of the marginalisation grid and marginalises
 (``k_roq_time_marg``, behind ``gwl_set_roq_time_marginalization``).
 
-Not built: several bases selected by prior ranges and multi-banded ROQ
-weights (NotImplementedError); hdf5 files need h5py, as in the reference.
+Several linear and quadratic bases (roq.py:193-460): a weights dictionary
+(or .npz file) with one weight array per basis, the frequency nodes of each
+and their prior ranges; each point takes the first basis of each kind whose
+prior ranges hold its parameters, as the reference's _update_basis does.
+Every pair of bases a batch uses gets its own device-resident analysis (the
+same data, that pair's nodes and weights); a batch is grouped by pair,
+evaluated pair by pair and put back in order.
+
+Not built: multi-banded ROQ weights (NotImplementedError); hdf5 files need
+h5py, as in the reference.
 """
 from __future__ import annotations
 
@@ -76,20 +84,164 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
                     self.perform_roq_params_check(ifo)
             self.weights = dict()
             self._set_weights(linear, quadratic)
+        name0 = self.interferometers[0].name
+        self.number_of_bases_linear = len(self.weights[f"{name0}_linear"])
+        self.number_of_bases_quadratic = len(self.weights[f"{name0}_quadratic"])
+        self._cache = dict(parameters=None, basis_number_linear=0, basis_number_quadratic=0)
         for basis_type in ("linear", "quadratic"):
-            if len(self.weights[f"{self.interferometers[0].name}_{basis_type}"]) != 1:
-                raise NotImplementedError("several ROQ bases (selected by prior ranges) have no GPU kernel")
-            key = f"frequency_nodes_{basis_type}"
-            args = self.waveform_generator.waveform_arguments
-            if key not in self.weights and key not in args:
-                raise AttributeError(f"{key} should be contained in weights or waveform arguments.")
-            if key not in args:
-                args[key] = self.weights[key][0]
-            elif key not in self.weights:
-                self.weights[key] = [args[key]]
-        self.number_of_bases_linear = 1
-        self.number_of_bases_quadratic = 1
+            if getattr(self, f"number_of_bases_{basis_type}") > 1:
+                self._verify_numbers_of_prior_ranges_and_frequency_nodes(basis_type)
+            else:
+                self._check_frequency_nodes_exist_for_single_basis(basis_type)
+            self._verify_prior_ranges(basis_type)
+        self._basis_analyses = {}
         self._upload()
+
+    # ------------------------------------------------------------------
+    # several bases (roq.py:193-460)
+    # ------------------------------------------------------------------
+    @property
+    def multiple_bases(self) -> bool:
+        return self.number_of_bases_linear > 1 or self.number_of_bases_quadratic > 1
+
+    def _verify_numbers_of_prior_ranges_and_frequency_nodes(self, basis_type):
+        """roq.py:216-247."""
+        n = getattr(self, f"number_of_bases_{basis_type}")
+        key = f"prior_range_{basis_type}"
+        if key not in self.weights:
+            raise AttributeError(f'For the use of multiple {basis_type} ROQ bases, weights should contain "{key}".')
+        for param_name, ranges in self.weights[key].items():
+            if len(ranges) != n:
+                raise ValueError(f'The number of prior ranges for "{param_name}" does not match the number of '
+                                 f'{basis_type} bases')
+        key = f"frequency_nodes_{basis_type}"
+        if key not in self.weights:
+            raise AttributeError(f'For the use of multiple {basis_type} ROQ bases, weights should contain "{key}".')
+        if len(self.weights[key]) != n:
+            raise ValueError(f"The number of arrays of frequency nodes does not match the number of {basis_type} bases")
+
+    def _verify_prior_ranges(self, basis_type):
+        """roq.py:249-276: the prior must lie inside the union of the ranges."""
+        key = f"prior_range_{basis_type}"
+        if key not in self.weights or self.priors is None:
+            return
+        for param_name, ranges in self.weights[key].items():
+            if param_name not in self.priors:
+                continue
+            ranges = np.asarray(ranges, dtype=np.float64)
+            prior = self.priors[param_name]
+            if prior.minimum < np.min(ranges[:, 0]):
+                raise BilbyROQParamsRangeError(f"Prior minimum of {param_name} {prior.minimum} less than ROQ basis "
+                                               f"bound {np.min(ranges[:, 0])}")
+            if prior.maximum > np.max(ranges[:, 1]):
+                raise BilbyROQParamsRangeError(f"Prior maximum of {param_name} {prior.maximum} greater than ROQ "
+                                               f"basis bound {np.max(ranges[:, 1])}")
+
+    def _check_frequency_nodes_exist_for_single_basis(self, basis_type):
+        """roq.py:278-296."""
+        key = f"frequency_nodes_{basis_type}"
+        args = self.waveform_generator.waveform_arguments
+        if key not in self.weights and key not in args:
+            raise AttributeError(f"{key} should be contained in weights or waveform arguments.")
+        if key not in args:
+            args[key] = self.weights[key][0]
+        elif key not in self.weights:
+            self.weights[key] = [args[key]]
+
+    def basis_numbers(self, parameters):
+        """The (linear, quadratic) basis of each point, vectorised
+        (roq.py:398-431): after the ROQ's own parameter_conversion, the first
+        basis whose prior range holds every ranged parameter the point has;
+        IndexError when none does, as in the reference."""
+        p = dict(parameters)
+        if self.parameter_conversion is not None:
+            p = self.parameter_conversion(p)
+        sizes = [np.size(v) for v in p.values() if not isinstance(v, str)]
+        n_points = max(sizes) if sizes else 1
+        out = []
+        for basis_type in ("linear", "quadratic"):
+            n = getattr(self, f"number_of_bases_{basis_type}")
+            if n == 1:
+                out.append(np.zeros(n_points, dtype=np.int64))
+                continue
+            ok = np.ones((n, n_points), dtype=bool)
+            for name, ranges in self.weights[f"prior_range_{basis_type}"].items():
+                if name not in p:
+                    continue
+                r = np.asarray(ranges, dtype=np.float64)
+                v = np.broadcast_to(np.asarray(p[name], dtype=np.float64), (n_points,))
+                ok &= (r[:, :1] <= v) & (r[:, 1:2] >= v)
+            if not ok.any(axis=0).all():
+                raise IndexError(f"a point lies in no {basis_type} ROQ basis' prior range")
+            out.append(np.argmax(ok, axis=0).astype(np.int64))
+        return out[0], out[1]
+
+    def _update_basis(self, parameters):
+        """roq.py:398-431 for one point: the cache the per-detector methods read."""
+        il, iq = self.basis_numbers(parameters)
+        self._cache.update(parameters=dict(parameters), basis_number_linear=int(il[0]),
+                           basis_number_quadratic=int(iq[0]))
+
+    @property
+    def basis_number_linear(self):
+        return self._cache["basis_number_linear"] if self.number_of_bases_linear > 1 else 0
+
+    @property
+    def basis_number_quadratic(self):
+        return self._cache["basis_number_quadratic"] if self.number_of_bases_quadratic > 1 else 0
+
+    def _analysis_for(self, il, iq):
+        """The device analysis of the pair (linear basis il, quadratic basis iq)."""
+        if (il, iq) == (0, 0):
+            return self.analysis
+        an = self._basis_analyses.get((il, iq))
+        if an is None:
+            an = self._new_analysis(self.interferometers)
+            self._configure_analysis(an)
+            an.set_roq(True, *self._roq_for(il, iq))
+            if self._roq_tm is not None:
+                an.set_roq_time_marginalization(*self._roq_tm)
+            self._basis_analyses[(il, iq)] = an
+        return an
+
+    def log_likelihood_ratio(self, parameters):
+        """roq.py:461-463: select the bases, then the likelihood."""
+        if not self.multiple_bases:
+            return super().log_likelihood_ratio(parameters)
+        import copy
+        from .analysis import params_block
+        self._update_basis(parameters)
+        an = self._analysis_for(self._cache["basis_number_linear"], self._cache["basis_number_quadratic"])
+        block = params_block(self._prepare(copy.deepcopy(parameters)), 1)
+        return float(an.log_likelihood_ratio_host(block, self.precision)[0])
+
+    def log_likelihood_ratio_batch(self, parameters, precision=None, out=None):
+        """A batch grouped by basis pair (numpy arrays or CUDA tensors)."""
+        if not self.multiple_bases:
+            return super().log_likelihood_ratio_batch(parameters, precision, out)
+        precision = precision or self.precision
+        first = next(iter(parameters.values()))
+        cuda = hasattr(first, "is_cuda") and first.is_cuda
+        host = {k: (v.detach().cpu().numpy() if cuda else np.asarray(v, dtype=np.float64))
+                for k, v in parameters.items()}
+        n = len(np.atleast_1d(host[next(iter(host))]))
+        il, iq = self.basis_numbers(host)
+        if cuda:
+            import torch
+            res = out if out is not None else torch.empty(n, dtype=torch.float64, device=first.device)
+        else:
+            res = np.empty(n)
+        for pair in sorted(set(zip(il.tolist(), iq.tolist()))):
+            idx = np.nonzero((il == pair[0]) & (iq == pair[1]))[0]
+            if cuda:
+                import torch
+                ti = torch.from_numpy(idx).to(first.device)
+                sub = {k: (v[ti] if v.ndim and v.shape[0] == n else v) for k, v in parameters.items()}
+                res[ti] = self._batch_on(self._analysis_for(*pair), sub, precision)
+            else:
+                sub = {k: (v[idx] if np.ndim(v) and len(v) == n else v) for k, v in host.items()}
+                res[idx] = self._batch_on(self._analysis_for(*pair), sub, precision)
+        return res
 
     # ------------------------------------------------------------------
     # basis and weights (host, float64)
@@ -216,8 +368,8 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         samples sit at the middles of the intervals; the antenna patterns and
         delays are taken at the prior's mid time."""
         tp = self.priors["geocent_time"]
-        if type(tp).__name__ != "Uniform":
-            raise NotImplementedError("time marginalisation on the GPU needs a Uniform geocent_time prior")
+        if not (np.isfinite(tp.minimum) and np.isfinite(tp.maximum)):
+            raise ValueError("ROQ time marginalisation needs a geocent_time prior with finite bounds")
         delta_tc = self._delta_tc_request
         if delta_tc is None:
             delta_tc = self._get_time_resolution()
@@ -227,6 +379,8 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         self._times = tcmin + self._delta_tc / 2. + np.arange(n) * self._delta_tc
         self._beam_pattern_reference_time = (tcmin + tcmax) / 2.
         self.time_prior_array = tp.prob(self._times) * self._delta_tc
+        from .likelihood import time_prior_table
+        self._time_prior_table = time_prior_table(tp, tcmin, tcmax, self._delta_tc)
 
     def _detector_analysis(self, interferometer):
         """A one-detector analysis with this detector's weights (and the
@@ -234,7 +388,8 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         products of roq.py:467-541, with the five-sample <d|h>(t) series under
         time marginalisation."""
         name = interferometer.name
-        an = self._detector_analyses.get(name)
+        pair = (self.basis_number_linear, self.basis_number_quadratic)  # the reference's cached bases
+        an = self._detector_analyses.get((name, pair))
         if an is None:
             names = [ifo.name for ifo in self.interferometers]
             if name not in names:
@@ -244,11 +399,11 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
             if self.time_marginalization:
                 tp = self.priors["geocent_time"]
                 an.set_time_marginalization(True, self.jitter_time, tp.minimum, tp.maximum)
-            fl, fq, start, dt, wl, wq = self._roq
+            fl, fq, start, dt, wl, wq = self._roq_for(*pair)
             an.set_roq(True, fl, fq, start, dt, wl[k:k + 1], wq[k:k + 1])
             if self._roq_tm is not None:
                 an.set_roq_time_marginalization(*self._roq_tm)
-            self._detector_analyses[name] = an
+            self._detector_analyses[(name, pair)] = an
         return an
 
     def _snr_block(self, parameters):
@@ -289,15 +444,26 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         # the device rebuilds time sample k as (start + k) * dt, the grid of roq.py:765
         if not np.array_equal(ts, np.arange(start, start + len(ts)) * dt):
             raise ValueError("ROQ time samples must be the grid (start + k) * dt")
-        names = [ifo.name for ifo in self.interferometers]
-        wl = np.stack([np.asarray(self.weights[n + "_linear"][0]) for n in names])
-        wq = np.stack([np.asarray(self.weights[n + "_quadratic"][0]).real for n in names])
-        self._roq = (np.asarray(self.weights["frequency_nodes_linear"][0], dtype=np.float64),
-                     np.asarray(self.weights["frequency_nodes_quadratic"][0], dtype=np.float64), start, dt, wl, wq)
+        self._roq_grid = (start, dt)
+        self._roq = self._roq_for(0, 0)
         if self.time_marginalization:
             self._roq_tm = (np.asarray(self._times, dtype=np.float64), float(self._delta_tc),
                             float(self._beam_pattern_reference_time))
         self._set_weights_on(self.analysis)
+
+    def __getstate__(self):
+        state = super().__getstate__()
+        state["_basis_analyses"] = {}
+        return state
+
+    def _roq_for(self, il, iq):
+        """gwl_set_roq arguments of the pair (linear basis il, quadratic basis iq)."""
+        start, dt = self._roq_grid
+        names = [ifo.name for ifo in self.interferometers]
+        wl = np.stack([np.asarray(self.weights[n + "_linear"][il]) for n in names])
+        wq = np.stack([np.asarray(self.weights[n + "_quadratic"][iq]).real for n in names])
+        return (np.asarray(self.weights["frequency_nodes_linear"][il], dtype=np.float64),
+                np.asarray(self.weights["frequency_nodes_quadratic"][iq], dtype=np.float64), start, dt, wl, wq)
 
     def _set_weights_on(self, an):
         an.set_roq(True, *self._roq)

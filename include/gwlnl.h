@@ -120,6 +120,15 @@ int gwl_noise_log_likelihood(gwl_analysis *a, double *out);
  * grid to have an even number of FFT points (n_bins - 1). */
 int gwl_set_time_marginalization(gwl_analysis *a, int enable, int jitter, double t_min, double t_max);
 
+/* A geocent_time prior other than Uniform for time marginalisation: the
+ * reference weights each time sample t_j (jittered) by
+ * priors['geocent_time'].prob(t_j) * delta_tc (bilby/gw/likelihood/base.py:
+ * 794-820).  `density` holds that density on the n nodes t0 + g h, with h a
+ * power of two (seconds) and t0 a multiple of h, so that every node time is
+ * exact in float64; the kernels interpolate it with four nodes (one-sided at
+ * the ends).  n = 0 returns to the Uniform prior of [t_min, t_max]. */
+int gwl_set_time_prior(gwl_analysis *a, const double *density, int64_t n, double t0, double h);
+
 /* Phase marginalisation (base.py:202-205, 786-792): ln I0(|<d|h>|) - <h|h>/2. */
 int gwl_set_phase_marginalization(gwl_analysis *a, int enable);
 

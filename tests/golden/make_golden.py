@@ -25,6 +25,9 @@ Outputs
     (FFT length 8192) and 4096 Hz (FFT length 16384) and the reference's
     ``log_likelihood_ratio`` under each of the seven combinations of time,
     phase and distance marginalisation.
+``tests/golden/tf2_marg_8s_2k_time_prior.npz``
+    The reference's time-marginalised lnL under a TruncatedGaussian
+    geocent_time prior (time, time+phase, time+distance, all three).
 ``tests/golden/tf2_128s_multiband.npz``
     The reference's ``MBGravitationalWaveTransient`` on tf2_128s (reference
     chirp mass 0.87, linear-interpolation <h|h>): its bands, banded
@@ -38,6 +41,12 @@ Outputs
     frequency nodes, and lnL ratios without marginalisation, with phase, with
     distance, with time, and with time, phase and distance marginalisation
     (with the time grid's spacing and length).
+``tests/golden/tf2_marg_8s_2k_roq_multibasis.npz``
+    The reference's ROQ likelihood with two linear and two quadratic seeded
+    synthetic bases selected per point by chirp-mass ranges (a weights
+    dictionary merged from single-basis weights): the sampler-style draws,
+    the basis pair the reference selected for each, and its lnL ratios
+    without and with time marginalisation.
 ``tests/golden/priors.npz``
     The reference's ``PriorDict.rescale`` of fixed unit-cube samples for the
     GW prior kinds the device rescaler supports, followed by
@@ -371,6 +380,94 @@ def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
     np.savez_compressed(os.path.join(HERE, f"{name}_roq.npz"), **out)
 
 
+# two seeded synthetic bases over overlapping chirp-mass ranges; the
+# quadratic ranges differ from the linear ones, so that points take every
+# (linear, quadratic) pair of bases
+ROQ_BASES = [dict(seed=2024, mass_range=(10.0, 25.0)), dict(seed=2031, mass_range=(20.0, 40.0))]
+ROQ_PRIOR_RANGE_LINEAR = np.array([[8.0, 21.0], [19.0, 35.0]])
+ROQ_PRIOR_RANGE_QUADRATIC = np.array([[8.0, 25.0], [23.0, 35.0]])
+
+
+def merge_roq_weights(single, prior_range_linear, prior_range_quadratic):
+    """One weights dictionary with several bases (roq.py:193-260) from the
+    weights of single-basis likelihoods on the same data: the per-detector
+    weight lists and the frequency-node lists concatenated, the time samples
+    shared, and the chirp-mass prior range of each basis."""
+    out = {"time_samples": np.asarray(single[0]["time_samples"])}
+    for key in single[0]:
+        if key.endswith("_linear") or key.endswith("_quadratic"):
+            out[key] = [np.asarray(w[key][0]) for w in single]
+    out["prior_range_linear"] = {"chirp_mass": np.asarray(prior_range_linear)}
+    out["prior_range_quadratic"] = {"chirp_mass": np.asarray(prior_range_quadratic)}
+    return out
+
+
+def roq_multibasis_points(w, n, seed):
+    """Sampler-style draws for the two-basis ROQ: chirp mass U[9, 34], mass
+    ratio U[0.4, 1], the workload's other parameters."""
+    rng = np.random.default_rng(seed)
+    p = draw_points(w, n, rng, fixed_extrinsic=False)
+    p.pop("mass_1")
+    p.pop("mass_2")
+    p["chirp_mass"] = rng.uniform(9.0, 34.0, n)
+    p["mass_ratio"] = rng.uniform(0.4, 1.0, n)
+    p["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
+    return p
+
+
+def run_roq_multibasis(bilby, name="tf2_marg_8s_2k", n_points=24):
+    """The reference's ROQGravitationalWaveTransient with two linear and two
+    quadratic bases selected per point by chirp-mass ranges (roq.py:193-460),
+    given as a weights dictionary, without and with time marginalisation:
+    the basis numbers it selected and its lnL ratios."""
+    from oracle import roq_basis
+    w = WORKLOADS[name]
+    params = roq_multibasis_points(w, n_points, w.draw_seed + 23)
+    out = {"p_" + k: v for k, v in params.items()}
+    for combo in ("none", "t"):
+        t = combo == "t"
+        single = []
+        for b in ROQ_BASES:
+            ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+            fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+            nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency, seed=b["seed"],
+                                            mass_range=b["mass_range"])
+            wfg = bilby.gw.waveform_generator.WaveformGenerator(
+                duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                frequency_domain_source_model=taylorf2_aligned_roq,
+                waveform_arguments=dict(minimum_frequency=w.minimum_frequency, frequency_nodes_linear=nl,
+                                        frequency_nodes_quadratic=nq))
+            one = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+                interferometers=ifos, waveform_generator=wfg, priors=make_priors(bilby, w, True),
+                linear_matrix=bl.T, quadratic_matrix=bq.T)
+            single.append(dict(one.weights, frequency_nodes_linear=[nl], frequency_nodes_quadratic=[nq]))
+        weights = merge_roq_weights(single, ROQ_PRIOR_RANGE_LINEAR, ROQ_PRIOR_RANGE_QUADRATIC)
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_roq,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+        priors = make_priors(bilby, w, True)
+        priors["chirp_mass"] = bilby.core.prior.Uniform(9.0, 34.0, name="chirp_mass")
+        like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, weights=weights, time_marginalization=t)
+        vals, bl_, bq_ = [], [], []
+        for i in range(n_points):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+            else:
+                q.pop("time_jitter")
+            vals.append(like.log_likelihood_ratio(q))
+            bl_.append(like.basis_number_linear)
+            bq_.append(like.basis_number_quadratic)
+        out["lnl_" + combo] = np.array(vals)
+        out["basis_linear_" + combo] = np.array(bl_)
+        out["basis_quadratic_" + combo] = np.array(bq_)
+        print(f"{name} roq two bases [{combo}]: basis pairs {sorted(set(zip(bl_, bq_)))}")
+    np.savez_compressed(os.path.join(HERE, f"{name}_roq_multibasis.npz"), **out)
+
+
 def run_priors(bilby, n=256):
     from bilby.core.prior import (Cosine, Gaussian, LogUniform, PowerLaw, PriorDict, Sine, TruncatedGaussian,
                                   Uniform)
@@ -690,6 +787,42 @@ def run_sg_marginalised(bilby, name="sg_4s", n_points=16):
     np.savez_compressed(os.path.join(HERE, f"{name}_marg.npz"), **out)
 
 
+TIME_PRIOR = dict(mu_offset=0.02, sigma=0.04)   # TruncatedGaussian on geocent_time, within t_inj +- 0.1 s
+
+
+def run_time_prior(bilby, name="tf2_marg_8s_2k", n_points=8):
+    """The reference's time-marginalised likelihood under a geocent_time prior
+    other than Uniform: TruncatedGaussian(mu = t_inj + 0.02, sigma = 0.04,
+    t_inj -+ 0.1), with time, time+phase, time+distance and all three."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 19)
+    params = draw_points(w, n_points, rng, fixed_extrinsic=False)
+    params["time_jitter"] = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n_points)
+    out = {"p_" + k: v for k, v in params.items()}
+    tc = w.injection["geocent_time"]
+    for combo in ("t", "tp", "td", "tpd"):
+        ifos, wfg = build_reference(bilby, w, taylorf2_aligned)
+        priors = make_priors(bilby, w, True, "p" in combo, "d" in combo)
+        priors["geocent_time"] = bilby.core.prior.TruncatedGaussian(
+            mu=tc + TIME_PRIOR["mu_offset"], sigma=TIME_PRIOR["sigma"], minimum=tc - 0.1, maximum=tc + 0.1,
+            name="geocent_time")
+        like = bilby.gw.likelihood.GravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, time_marginalization=True,
+            phase_marginalization="p" in combo, distance_marginalization="d" in combo)
+        vals = []
+        for i in range(n_points):
+            q = point(params, i)
+            q["geocent_time"] = float(priors["geocent_time"])
+            if "p" in combo:
+                q["phase"] = 0.0
+            if "d" in combo:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} time prior [{combo}] done")
+    np.savez_compressed(os.path.join(HERE, f"{name}_time_prior.npz"), **out)
+
+
 def known_answer(bilby):
     """test/gw/likelihood_test.py:143-201 (noise lnL only; the lnL value
     there needs IMRPhenomPv2 from lalsimulation)."""
@@ -716,8 +849,22 @@ def main():
     ap.add_argument("--roq-only", action="store_true")
     ap.add_argument("--snrs-only", action="store_true")
     ap.add_argument("--marg-only", action="store_true")
+    ap.add_argument("--time-prior-only", action="store_true")
+    ap.add_argument("--roq-multibasis-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.roq_multibasis_only or args.time_prior_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                if args.time_prior_only:
+                    run_time_prior(bilby)
+                if args.roq_multibasis_only:
+                    run_roq_multibasis(bilby)
+            finally:
+                os.chdir(cwd)
+        return
     if args.marg_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -785,9 +932,11 @@ def main():
             try:
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
                 run_marginalised(bilby, "tf2_marg_8s", 16)
+                run_time_prior(bilby)
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)
                 run_roq(bilby)
+                run_roq_multibasis(bilby)
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
                 run_roq_snrs(bilby)

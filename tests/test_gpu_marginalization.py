@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 COMBOS = ["t", "p", "d", "tp", "td", "pd", "tpd"]
 
 
-def make_likelihood(w, combo, precision, table_path):
+def make_likelihood(w, combo, precision, table_path, time_prior=None):
     from bilby_gb300 import random as grandom
     from bilby_gb300.detector import InterferometerList
     from bilby_gb300.likelihood import GravitationalWaveTransient
@@ -36,14 +36,14 @@ def make_likelihood(w, combo, precision, table_path):
     ifos.inject_signal(waveform_generator=wfg, parameters=dict(w.injection))
     tc = w.injection["geocent_time"]
     priors = {}
-    if "t" in combo:
-        priors["geocent_time"] = Uniform(tc - 0.1, tc + 0.1)
+    if "t" in combo or time_prior is not None:
+        priors["geocent_time"] = time_prior if time_prior is not None else Uniform(tc - 0.1, tc + 0.1)
     if "p" in combo:
         priors["phase"] = Uniform(0, 2 * np.pi, boundary="periodic")
     if "d" in combo:
         priors["luminosity_distance"] = PowerLaw(DISTANCE_PRIOR["alpha"], DISTANCE_PRIOR["minimum"],
                                                  DISTANCE_PRIOR["maximum"])
-    like = GravitationalWaveTransient(ifos, wfg, priors=priors, time_marginalization="t" in combo,
+    like = GravitationalWaveTransient(ifos, wfg, priors=priors, time_marginalization="t" in combo or time_prior is not None,
                                       phase_marginalization="p" in combo, distance_marginalization="d" in combo,
                                       distance_marginalization_lookup_table=str(table_path), precision=precision)
     return like, priors
@@ -301,3 +301,31 @@ def test_time_and_distance_marginalization_vs_brute_force(gpu, tmp_path, combo):
             q["luminosity_distance"] = float(priors["luminosity_distance"])
         got = marg.log_likelihood_ratio(q)
         assert abs(got - brute) < 0.5, (combo, i, got, brute)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("combo", ["t", "tp", "td", "tpd"])
+def test_time_prior_other_than_uniform_vs_reference(gpu, tmp_path, combo, precision):
+    """Time marginalisation under a TruncatedGaussian geocent_time prior (each
+    jittered time sample weighted by prior(t) delta_tc, base.py:794-820)
+    against the reference's values (tests/golden/tf2_marg_8s_2k_time_prior.npz):
+    float64 |dlnL| <= 1e-8 max(1, |lnL|), mixed |dlnL| <= 1e-3."""
+    from bilby_gb300.prior import TruncatedGaussian
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    z = golden("tf2_marg_8s_2k_time_prior")
+    tc = w.injection["geocent_time"]
+    like, priors = make_likelihood(w, combo.replace("t", ""), precision, tmp_path / "table.npz",
+                                   time_prior=TruncatedGaussian(tc + 0.02, 0.04, tc - 0.1, tc + 0.1))
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    n = len(params["mass_1"])
+    params["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+    if "p" in combo:
+        params["phase"] = np.zeros(n)
+    if "d" in combo:
+        params["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+    got = like.log_likelihood_ratio_batch(params)
+    ref = z["lnl_" + combo]
+    if precision == "fp64":
+        assert np.all(np.abs(got - ref) <= 1e-8 * np.maximum(1.0, np.abs(ref))), got - ref
+    else:
+        assert np.max(np.abs(got - ref)) <= 1e-3, got - ref

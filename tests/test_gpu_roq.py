@@ -191,3 +191,88 @@ def test_per_detector_snrs_match_reference(gpu, tmp_path, combo):
             grandom.seed(4321 + i)
             draw = like.generate_time_sample_from_marginalized_likelihood(parameters=dict(q))
             assert draw == z[f"{key}_time_draw"][i], (i, draw)
+
+
+ROQ_BASES = [dict(seed=2024, mass_range=(10.0, 25.0)), dict(seed=2031, mass_range=(20.0, 40.0))]
+PRIOR_RANGE_LINEAR = np.array([[8.0, 21.0], [19.0, 35.0]])
+PRIOR_RANGE_QUADRATIC = np.array([[8.0, 25.0], [23.0, 35.0]])
+
+
+def two_basis_likelihood(time_marginalization):
+    """The two-basis ROQ likelihood of tests/golden/tf2_marg_8s_2k_roq_multibasis.npz:
+    each basis' weights computed by this package from its seeded synthetic
+    basis, merged into one weights dictionary with the chirp-mass ranges."""
+    from bilby_gb300 import random as grandom
+    from bilby_gb300.detector import InterferometerList
+    from bilby_gb300.prior import Uniform
+    from bilby_gb300.roq import ROQGravitationalWaveTransient
+    from bilby_gb300.source import taylorf2_aligned, taylorf2_aligned_roq
+    from bilby_gb300.waveform_generator import WaveformGenerator
+    from oracle import roq_basis
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    grandom.seed(w.seed)
+    ifos = InterferometerList(list(w.detectors))
+    ifos.set_strain_data_from_power_spectral_densities(w.sampling_frequency, w.duration, w.start_time)
+    inj = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    ifos.inject_signal(waveform_generator=inj, parameters=dict(w.injection))
+    tc = w.injection["geocent_time"]
+    fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+    single = []
+    for b in ROQ_BASES:
+        nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency, seed=b["seed"],
+                                        mass_range=b["mass_range"])
+        wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                                frequency_domain_source_model=taylorf2_aligned_roq,
+                                waveform_arguments=dict(minimum_frequency=w.minimum_frequency,
+                                                        frequency_nodes_linear=nl, frequency_nodes_quadratic=nq))
+        one = ROQGravitationalWaveTransient(ifos, wfg, {"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
+                                            linear_matrix=bl.T, quadratic_matrix=bq.T)
+        single.append(one.weights)
+        one.analysis.close()
+    weights = {"time_samples": np.asarray(single[0]["time_samples"]),
+               "prior_range_linear": {"chirp_mass": PRIOR_RANGE_LINEAR},
+               "prior_range_quadratic": {"chirp_mass": PRIOR_RANGE_QUADRATIC}}
+    for key in single[0]:
+        if key.endswith("_linear") or key.endswith("_quadratic"):
+            weights[key] = [np.asarray(s[key][0]) for s in single]
+    wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+                            frequency_domain_source_model=taylorf2_aligned_roq,
+                            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+    priors = {"geocent_time": Uniform(tc - 0.1, tc + 0.1), "chirp_mass": Uniform(9.0, 34.0)}
+    like = ROQGravitationalWaveTransient(ifos, wfg, priors, weights=weights,
+                                         time_marginalization=time_marginalization)
+    return like, priors
+
+
+@pytest.mark.parametrize("combo", ["none", "t"])
+def test_two_bases_selected_by_chirp_mass_match_the_reference(gpu, combo):
+    """Several ROQ bases (roq.py:193-460): per point the same (linear,
+    quadratic) basis pair as the reference, and its lnL ratio to
+    1e-9 * max(1, |lnL|); the grouped batch equals the single calls."""
+    z = golden("tf2_marg_8s_2k_roq_multibasis")
+    like, priors = two_basis_likelihood(combo == "t")
+    assert like.number_of_bases_linear == 2 and like.number_of_bases_quadratic == 2
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    n = len(params["chirp_mass"])
+    if combo == "t":
+        params["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+    else:
+        params.pop("time_jitter")
+    single, bl, bq = [], [], []
+    for i in range(n):
+        single.append(like.log_likelihood_ratio(point(params, i)))
+        bl.append(like.basis_number_linear)
+        bq.append(like.basis_number_quadratic)
+    assert np.array_equal(bl, z["basis_linear_" + combo]) and np.array_equal(bq, z["basis_quadratic_" + combo])
+    single = np.array(single)
+    ref = z["lnl_" + combo]
+    assert np.all(np.abs(single - ref) <= 1e-9 * np.maximum(1.0, np.abs(ref))), single - ref
+    assert np.array_equal(like.log_likelihood_ratio_batch(params), single)
+    # CUDA tensors convert chirp mass / mass ratio with torch's device arithmetic,
+    # which differs from numpy's in the last bits of the masses
+    import torch
+    dev = {k: torch.from_numpy(np.asarray(v, dtype=np.float64)).cuda() for k, v in params.items()}
+    got = like.log_likelihood_ratio_batch(dev).cpu().numpy()
+    assert np.all(np.abs(got - single) <= 1e-9 * np.maximum(1.0, np.abs(single))), got - single

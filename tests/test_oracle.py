@@ -89,3 +89,54 @@ def test_oracle_geometry_is_bilbys():
         ifo = get_empty_interferometer(name)
         assert np.allclose(ifo.geometry.vertex, v, rtol=1e-15, atol=0)
         assert np.allclose(ifo.geometry.detector_tensor, t, rtol=1e-14, atol=1e-16)
+
+
+def test_oracle_time_prior_other_than_uniform_matches_reference():
+    """The reference's time-marginalised values under a TruncatedGaussian
+    geocent_time prior (tests/golden/tf2_marg_8s_2k_time_prior.npz)."""
+    from bilby_gb300.prior import TruncatedGaussian
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    z = golden("tf2_marg_8s_2k_time_prior")
+    dets = OD.build_workload(w)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    src = OD.source_for(w.model, w.minimum_frequency)
+    tc = w.injection["geocent_time"]
+    prior = TruncatedGaussian(tc + 0.02, 0.04, tc - 0.1, tc + 0.1)
+    for combo in ("t", "tp"):
+        m = R.Marginalization(time=True, phase="p" in combo)
+        R.setup_time_marginalization(m, w.start_time, w.duration, w.sampling_frequency, tc - 0.1, tc + 0.1)
+        for i in range(len(params["mass_1"])):
+            q = point(params, i)
+            q["geocent_time"] = w.start_time
+            if m.phase:
+                q["phase"] = 0.0
+            got = R.log_likelihood_ratio(dets, src, q, m, prior.prob)
+            ref = z["lnl_" + combo][i]
+            assert abs(got - ref) <= 1e-10 * max(1.0, abs(ref)), (combo, i, got, ref)
+
+
+def test_time_prior_table_interpolates_the_density():
+    """The kernels' 4-node Lagrange interpolation (restated here in numpy) of
+    the table from time_prior_table reproduces the prior's density at any
+    time of the window to 1e-10 relative, reads nodes exactly, and the node
+    times are exact multiples of a power-of-two step."""
+    from bilby_gb300.likelihood import time_prior_table
+    from bilby_gb300.prior import Gaussian, TruncatedGaussian, Uniform
+    tc, dtc = 1126259646.0, 2.0 / 4096
+    assert time_prior_table(Uniform(tc - 0.1, tc + 0.1), tc - 4, tc + 4, dtc) is None
+    for prior in (TruncatedGaussian(tc + 0.02, 0.04, tc - 0.1, tc + 0.1), Gaussian(tc, 0.5)):
+        dens, t0, h = time_prior_table(prior, tc - 6, tc + 2, dtc)
+        assert np.log2(h) == np.floor(np.log2(h)) and h <= dtc / 8 and t0 % h == 0.0
+        n = len(dens)
+        lo = max(prior.minimum, tc - 6)
+        hi = min(prior.maximum, tc + 2)
+        t = np.concatenate([np.random.default_rng(0).uniform(lo, hi, 2000), [lo, hi, t0 + 7 * h]])
+        x = (t - t0) / h
+        g = np.clip(np.floor(x).astype(np.int64) - 1, 0, n - 4)
+        u = x - g
+        p = [dens[g + q] for q in range(4)]
+        v = (p[3] * u * (u - 1) * (u - 2) - p[0] * (u - 1) * (u - 2) * (u - 3)) / 6 \
+            + (p[1] * u * (u - 2) * (u - 3) - p[2] * u * (u - 1) * (u - 3)) / 2
+        ref = prior.prob(t)
+        assert np.max(np.abs(v - ref) / ref) < 1e-10
+        assert v[-1] == dens[7]

@@ -69,3 +69,50 @@ def test_weights_match_the_reference():
         assert np.max(np.abs(lin - ref)) <= 1e-10 * np.max(np.abs(ref))
         quad = like.weights[ifo.name + "_quadratic"][0]
         assert np.max(np.abs(quad - z[f"roq_quadratic_{q}"])) <= 1e-12 * np.max(np.abs(quad))
+
+
+def _reference_update_basis(weights, n_bases, basis_type, parameters):
+    """roq.py:398-431 restated for one point: the first basis whose range
+    holds every ranged parameter the point has."""
+    if n_bases == 1:
+        return 0
+    ok = np.ones(n_bases, dtype=bool)
+    for name, ranges in weights[f"prior_range_{basis_type}"].items():
+        if name not in parameters:
+            continue
+        ok *= (ranges[:, 0] <= parameters[name]) * (ranges[:, 1] >= parameters[name])
+    return np.arange(n_bases)[ok][0]
+
+
+def test_basis_selection_matches_the_reference_rule():
+    """Vectorised basis selection of the multi-basis ROQ likelihood against
+    the reference's per-point rule, with a second ranged parameter that some
+    points lack, and IndexError for a point outside every range."""
+    import pytest
+    from bilby_gb300.roq import ROQGravitationalWaveTransient
+    like = object.__new__(ROQGravitationalWaveTransient)
+    like.parameter_conversion = None
+    like.number_of_bases_linear, like.number_of_bases_quadratic = 3, 2
+    like.weights = {
+        "prior_range_linear": {"chirp_mass": np.array([[5.0, 12.0], [10.0, 20.0], [18.0, 40.0]]),
+                               "mass_ratio": np.array([[0.1, 1.0], [0.5, 1.0], [0.1, 1.0]])},
+        "prior_range_quadratic": {"chirp_mass": np.array([[5.0, 15.0], [14.0, 40.0]])}}
+    rng = np.random.default_rng(3)
+    p = {"chirp_mass": rng.uniform(5.0, 40.0, 600), "mass_ratio": rng.uniform(0.1, 1.0, 600)}
+    ref, keep = [], []
+    for i in range(600):
+        q = {k: v[i] for k, v in p.items()}
+        try:
+            ref.append((_reference_update_basis(like.weights, 3, "linear", q),
+                        _reference_update_basis(like.weights, 2, "quadratic", q)))
+            keep.append(i)
+        except IndexError:  # in no linear basis' range (chirp mass 12-18, mass ratio below 0.5)
+            pass
+    assert 300 < len(keep) < 600
+    il, iq = like.basis_numbers({k: v[keep] for k, v in p.items()})
+    assert list(zip(il.tolist(), iq.tolist())) == [(int(a), int(b)) for a, b in ref]
+    assert {int(a) for a, _ in ref} == {0, 1, 2}
+    il, _ = like.basis_numbers({"chirp_mass": np.array([11.0, 19.0])})   # no mass_ratio: not ranged
+    assert list(il) == [0, 1]
+    with pytest.raises(IndexError):
+        like.basis_numbers({"chirp_mass": np.array([50.0])})
