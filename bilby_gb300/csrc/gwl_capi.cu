@@ -1109,8 +1109,10 @@ int gwl_set_time_marginalization(gwl_analysis* a, int enable, int jitter, double
       set_error("time prior must have t_max > t_min");
       return GWL_ERR_ARGUMENT;
     }
-    if ((a->n_bins - 1) % 2 != 0) {
-      set_error("time marginalisation needs an even FFT length (n_bins - 1)");
+    int m_odd = 0, log2n = 0;
+    if (!fft_length_supported(a->n_bins - 1, &m_odd, &log2n)) {
+      set_error("time marginalisation needs an FFT length n_bins - 1 = m 2^p with m odd, m <= " +
+                std::to_string(kTmMaxOddFactor) + " and p >= 4");
       return GWL_ERR_UNSUPPORTED;
     }
   }

@@ -265,6 +265,10 @@ void order_layout(int64_t n_chunks, int* keys, int* shift);
 void ordering_with_marks(LaunchArgs& L);
 void ordering_by_peak(LaunchArgs& L);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
+// FFT lengths the time-marginalised kernels take: L = m 2^p with m odd,
+// m <= kTmMaxOddFactor and p >= 4 (m and p returned)
+constexpr int kTmMaxOddFactor = 127;
+bool fft_length_supported(int64_t L, int* m_odd, int* log2N);
 size_t time_marg_work_bytes(const LaunchArgs& a);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,
                                         double fmin, double* plus, double* cross, cudaStream_t s);

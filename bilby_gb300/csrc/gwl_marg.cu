@@ -8,7 +8,12 @@
 //      (mixed precision, float32) or into this CTA's slot of an L2-resident
 //      work buffer (float64; 16 B * L does not fit in shared memory);
 //   B. an in-place radix-2 decimation-in-time FFT of length L (numpy's sign
-//      convention, exp(-2 pi i m k / L));
+//      convention, exp(-2 pi i m k / L)).  For L = m 2^p with m odd and
+//      greater than one, the integrand's residue class r = k mod m goes to
+//      block r of the buffer (bit-reversed there), the radix-2 stages run as m
+//      independent transforms Y_r of length N = 2^p, and the output is
+//      X[j] = sum_r exp(-2 pi i r j / L) Y_r[j mod N], formed only where it is
+//      read (the prior window's samples; every j for the float64 series);
 //   C. the time samples inside the geocent_time prior, paired with FFT index
 //      j exactly as the reference pairs them (times[j] = start + (j+1) 2/fs
 //      + jitter), the per-sample marginalised log-likelihood, and a
@@ -164,7 +169,7 @@ __device__ double block_sum(double v, double* red) {
 
 template <int D, bool MIXED>
 __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const typename TmTypes<MIXED>::C* twiddle,
-                                                          int log2L) {
+                                                          int log2N, int m_odd) {
   using C = typename TmTypes<MIXED>::C;
   using R = typename TmTypes<MIXED>::R;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -177,8 +182,13 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   // shared-memory tables (q = 128 q1 + q2), instead of loads from global memory
   __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
   __shared__ float2 s_w16[16];
-  const int64_t L = a.n_fft;
+  const int64_t L = a.n_fft, N2 = (int64_t)1 << log2N;  // L = m_odd N2
   const double norm = 4.0 / a.duration;
+  // buffer position of integrand bin k: block k mod m_odd, bit-reversed within it
+  const auto brpos = [&](int64_t k) -> int64_t {
+    if (m_odd == 1) return (int64_t)bit_reverse((uint32_t)k, log2N);
+    return (k % m_odd) * N2 + (int64_t)bit_reverse((uint32_t)(k / m_odd), log2N);
+  };
   if constexpr (MIXED) {
     const int64_t half = L / 2;
     for (int q = threadIdx.x; q < kTmTwiddleRows; q += blockDim.x) {
@@ -216,6 +226,28 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   // mixed: one padding slot after every 16 elements of the shared-memory
   // buffer, so that the strided accesses of the FFT passes spread over the banks
   const auto P = [](int64_t q) -> int64_t { return MIXED ? q + (q >> 4) : q; };
+  // output j of the length-L transform from the m_odd blocks' transforms
+  const auto out_at = [&](const C* b, int64_t j) -> C {
+    const int64_t jn = j & (N2 - 1);
+    if (m_odd == 1) return b[P(jn)];
+    C x;
+    x.x = 0;
+    x.y = 0;
+    int64_t q = 0;  // r j mod L
+    for (int r = 0; r < m_odd; ++r) {
+      C w = q < L / 2 ? tw(q) : tw(q - L / 2);
+      if (q >= L / 2) {
+        w.x = -w.x;
+        w.y = -w.y;
+      }
+      const C y = b[P(r * N2 + jn)];
+      x.x += w.x * y.x - w.y * y.y;
+      x.y += w.x * y.y + w.y * y.x;
+      q += j;
+      if (q >= L) q -= L;
+    }
+    return x;
+  };
   for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
     C* buf = MIXED ? reinterpret_cast<C*>(smem) : reinterpret_cast<C*>(a.tm_work) + (size_t)blockIdx.x * L;
     const PointRec& r = a.rec[i];
@@ -260,12 +292,14 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         // bins in it: a thread takes blocks b, evaluates their in-band bins,
         // and writes the 16 outputs (zeros when none); consecutive threads
         // write consecutive blocks.
-        const int64_t R = L >> 4;
-        const int lr = log2L - 4;
+        const int64_t R = L >> 4, R2 = N2 >> 4;
+        const int lr = log2N - 4;
         const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
         const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
         for (int64_t bb = threadIdx.x; bb < R; bb += blockDim.x) {
-          const int64_t q = (int64_t)bit_reverse((uint32_t)bb, lr);
+          // block bb / R2 of the m_odd transforms: bins q + j L / 16 with
+          // q = (bb / R2) + m_odd bitrev(bb mod R2)
+          const int64_t q = bb / R2 + m_odd * (int64_t)bit_reverse((uint32_t)(bb % R2), lr);
           float yr[16], yi[16];
 #pragma unroll
           for (int v = 0; v < 16; ++v) yr[v] = yi[v] = 0.f;
@@ -357,7 +391,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             }
           }
         }
-        buf[P(bit_reverse((uint32_t)k, log2L))] = make_float2(zr, zi);
+        buf[P(brpos(k))] = make_float2(zr, zi);
       }
       if (a.model == GWL_MODEL_SINEGAUSSIAN && threadIdx.x == 0 && r.valid) {
         // the float-float <h|h> of the k_mixed_sg pass launched before this
@@ -430,7 +464,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             zi += g.x * ri + g.y * rr;
           }
         }
-        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(zr, zi);
+        buf[brpos(k)] = make_double2(zr, zi);
       }
     } else if (a.mb_tm) {
       // multi-banding (multiband.py:714-726, 792-800): the banded strain
@@ -465,7 +499,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             }
           }
         }
-        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(zr, zi);
+        buf[brpos(k)] = make_double2(zr, zi);
       }
     } else {
       // e^{i w f_k} for this thread's bins k = tid, tid + T, ... by rotation
@@ -500,7 +534,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
             }
           }
         }
-        buf[bit_reverse((uint32_t)k, log2L)] = make_double2(norm * zr, norm * zi);
+        buf[brpos(k)] = make_double2(norm * zr, norm * zi);
 #pragma unroll
         for (int d = 0; d < D; ++d) tm_rotate(zc[d], zs[d], rc[d], rs[d]);
       }
@@ -533,7 +567,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     int stage = 1;
     if (MIXED && a.model == GWL_MODEL_TAYLORF2) {
       stage = 5;  // stages 1-4 ran with the integrand
-    } else if (log2L & 1) {  // one radix-2 stage first when log2 L is odd
+    } else if (log2N & 1) {  // one radix-2 stage first when log2 N is odd
       for (int64_t bf = threadIdx.x; bf < L / 2; bf += blockDim.x) {
         const int64_t i0 = 2 * bf, i1 = i0 + 1;
         const C x0 = buf[P(i0)], x1 = buf[P(i1)];
@@ -554,7 +588,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       // buffer and fewer barriers; the stage-j twiddles of a group depend only
       // on (k mod 2^j)
       constexpr int RB = MIXED ? 4 : 3, RN = 1 << RB;
-      for (; stage + RB - 1 <= log2L; stage += RB) {
+      for (; stage + RB - 1 <= log2N; stage += RB) {
         const int64_t h0 = (int64_t)1 << (stage - 1);
         for (int64_t gi = threadIdx.x; gi < L / RN; gi += blockDim.x) {
           const int64_t pos = gi & (h0 - 1);
@@ -599,15 +633,15 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         __syncthreads();
       }
     }
-    for (; stage < log2L; stage += 2) {
+    for (; stage < log2N; stage += 2) {
       const int64_t h = (int64_t)1 << (stage - 1);  // half-length of the first of the two stages
       const int64_t s1 = L / (2 * h), s2 = L / (4 * h);  // twiddle strides of the two stages
-      // mixed, the last two stages (h = L / 4): output j comes from the
-      // butterfly at j mod h alone, so only the window's butterflies run
-      const bool prune = MIXED && stage + 1 == log2L && n_win > 0 && n_win <= h;
-      const int64_t n_bf = prune ? n_win : L / 4;
+      // mixed, the last two stages (h = N / 4): output j of each block comes
+      // from the block's butterfly at j mod h alone, so only the window's run
+      const bool prune = MIXED && stage + 1 == log2N && n_win > 0 && n_win <= h;
+      const int64_t n_bf = prune ? n_win * m_odd : L / 4;
       for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
-        const int64_t bf = prune ? ((s_jr[0] + t) & (h - 1)) : t;
+        const int64_t bf = prune ? ((t / n_win) * h + ((s_jr[0] + t % n_win) & (h - 1))) : t;
         const int64_t pos = bf & (h - 1);
         const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
         const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
@@ -629,13 +663,14 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
       __syncthreads();
     }
-    if (stage == log2L) {  // a last radix-2 stage (half-length L / 2, twiddle exp(-2 pi i q / L))
-      const int64_t h = L / 2;
+    if (stage == log2N) {  // a last radix-2 stage (half-length N / 2, twiddle exp(-2 pi i l / N))
+      const int64_t h = N2 / 2;
       const bool prune = MIXED && n_win > 0 && n_win <= h;  // only the window's butterflies
-      const int64_t n_bf = prune ? n_win : h;
+      const int64_t n_bf = prune ? n_win * m_odd : L / 2;
       for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
-        const int64_t q = prune ? ((s_jr[0] + t) & (h - 1)) : t;
-        const C w = tw(q);
+        const int64_t l = prune ? ((s_jr[0] + t % n_win) & (h - 1)) : t % h;
+        const int64_t q = (prune ? t / n_win : t / h) * N2 + l;
+        const C w = tw(l * m_odd);
         const C x0 = buf[P(q)], x1 = buf[P(q + h)];
         const R tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
         C y0, y1;
@@ -657,7 +692,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         // base.py:325-330, and <h|h> (block_sum ends with a barrier, so the
         // last FFT stage's writes are visible)
         double2* dst = reinterpret_cast<double2*>(a.tm_series) + (size_t)i * L;
-        for (int64_t k = threadIdx.x; k < L; k += blockDim.x) dst[k] = buf[k];
+        for (int64_t k = threadIdx.x; k < L; k += blockDim.x) dst[k] = out_at(buf, k);
         if (a.hh_out && threadIdx.x == 0) a.hh_out[i] = hh;
       }
     }
@@ -729,7 +764,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
           lw = log(pw);
         }
       }
-      const C x = buf[P(j)];
+      const C x = out_at(buf, j);
       double l;
       if constexpr (MIXED) {
         // float32 per-sample work; the large terms combine in float64
@@ -1056,11 +1091,6 @@ cudaError_t twiddles_for(int64_t L, TwiddleTables* out) {
   return static_cast<cudaError_t>(rc);
 }
 
-int log2_exact(int64_t L) {
-  int s = 0;
-  while (((int64_t)1 << s) < L) ++s;
-  return ((int64_t)1 << s) == L ? s : -1;
-}
 
 int tm_grid_fp64() {
   int dev = 0, sms = 0;
@@ -1071,13 +1101,27 @@ int tm_grid_fp64() {
 
 }  // namespace
 
+bool fft_length_supported(int64_t L, int* m_odd, int* log2N) {
+  if (L < 16) return false;
+  int64_t m = L;
+  int p = 0;
+  while ((m & 1) == 0) {
+    m >>= 1;
+    ++p;
+  }
+  if (p < 4 || m > kTmMaxOddFactor) return false;
+  *m_odd = (int)m;
+  *log2N = p;
+  return true;
+}
+
 size_t time_marg_work_bytes(const LaunchArgs& a) {
   // float64 integrand / FFT slots, one per resident CTA
   return (size_t)tm_grid_fp64() * (size_t)a.n_fft * sizeof(double2);
 }
 
 template <int D>
-static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L, const TwiddleTables& tw) {
+static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2N, int m_odd, const TwiddleTables& tw) {
   if (a.precision == GWL_PRECISION_MIXED) {
     // the FFT buffer, then the distance spline's knots
     const size_t smem = (size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) +
@@ -1085,7 +1129,7 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L, c
     cudaError_t e = cudaFuncSetAttribute(k_time_marg<D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)a.B;
-    k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, tw.d32, log2L);
+    k_time_marg<D, true><<<grid, kTmThreads, smem, s>>>(a, tw.d32, log2N, m_odd);
   } else {
     // relative binning: the edge ratios in shared memory
     const size_t smem = a.relbin ? (size_t)a.rb_edges * D * sizeof(double2) : 0;
@@ -1095,7 +1139,7 @@ static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2L, c
       if (e != cudaSuccess) return e;
     }
     const unsigned grid = (unsigned)std::min<int64_t>(a.B, tm_grid_fp64());
-    k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, tw.d64, log2L);
+    k_time_marg<D, false><<<grid, kTmThreads, smem, s>>>(a, tw.d64, log2N, m_odd);
   }
   return cudaGetLastError();
 }
@@ -1128,8 +1172,8 @@ cudaError_t launch_roq_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
-  const int log2L = log2_exact(a.n_fft);
-  if (log2L < 1) return cudaErrorInvalidValue;  // the host rejects non-power-of-two lengths first
+  int m_odd = 0, log2N = 0;
+  if (!fft_length_supported(a.n_fft, &m_odd, &log2N)) return cudaErrorInvalidValue;  // checked on the host first
   if (a.precision != GWL_PRECISION_MIXED && a.relbin && (size_t)a.rb_edges * a.n_det * sizeof(double2) > 200 * 1024)
     return cudaErrorInvalidValue;  // the host checks the edge count first
   if (a.precision == GWL_PRECISION_MIXED &&
@@ -1141,10 +1185,10 @@ cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s) {
   cudaError_t e = twiddles_for(a.n_fft, &tw);
   if (e != cudaSuccess) return e;
   switch (a.n_det) {
-    case 1: return launch_tm_d<1>(a, s, log2L, tw);
-    case 2: return launch_tm_d<2>(a, s, log2L, tw);
-    case 3: return launch_tm_d<3>(a, s, log2L, tw);
-    default: return launch_tm_d<4>(a, s, log2L, tw);
+    case 1: return launch_tm_d<1>(a, s, log2N, m_odd, tw);
+    case 2: return launch_tm_d<2>(a, s, log2N, m_odd, tw);
+    case 3: return launch_tm_d<3>(a, s, log2N, m_odd, tw);
+    default: return launch_tm_d<4>(a, s, log2N, m_odd, tw);
   }
 }
 

@@ -12,6 +12,8 @@ shapes and prior ranges of the configurations the benchmark is quoted on:
 ``tf2_marg_8s`` TaylorF2 m1, m2 U[10, 40] Msun, H1+L1, 8 s at 4096 Hz (16385 bins,
                FFT length 16384), time + phase + distance marginalisation; 8192 points.
 ``tf2_marg_8s_2k`` the same at 2048 Hz (8193 bins, FFT length 8192).
+``tf2_marg_6s_2k`` the same for a 6 s segment at 2048 Hz (6145 bins, FFT length
+               6144 = 3 x 2048, not a power of two).
 
 Prior draws for the extrinsic parameters: ra U[0, 2 pi), dec = arcsin U[-1, 1],
 psi U[0, pi), geocent_time U[t_inj - 0.1, t_inj + 0.1]; theta_jn = arccos U[-1, 1],
@@ -68,6 +70,11 @@ WORKLOADS = {
         "tf2_marg_8s_2k", "taylorf2", ("H1", "L1"), 2048.0, 8.0, seed=4, draw_seed=4, batch=8192,
         injection=dict(mass_1=30.0, mass_2=25.0, chi_1=0.02, chi_2=-0.01, luminosity_distance=800.0,
                        theta_jn=0.4, phase=1.3, geocent_time=START_TIME + 6.0, **_SKY),
+        time_marginalization=True, phase_marginalization=True, distance_marginalization=True),
+    "tf2_marg_6s_2k": Workload(
+        "tf2_marg_6s_2k", "taylorf2", ("H1", "L1"), 2048.0, 6.0, seed=4, draw_seed=6, batch=8192,
+        injection=dict(mass_1=30.0, mass_2=25.0, chi_1=0.02, chi_2=-0.01, luminosity_distance=800.0,
+                       theta_jn=0.4, phase=1.3, geocent_time=START_TIME + 4.0, **_SKY),
         time_marginalization=True, phase_marginalization=True, distance_marginalization=True),
 }
 

@@ -25,6 +25,9 @@ Outputs
     (FFT length 8192) and 4096 Hz (FFT length 16384) and the reference's
     ``log_likelihood_ratio`` under each of the seven combinations of time,
     phase and distance marginalisation.
+``tests/golden/tf2_marg_6s_2k.npz``
+    The same seven combinations on a 6 s segment at 2048 Hz, whose FFT length
+    (6144 = 3 x 2048) is not a power of two.
 ``tests/golden/tf2_marg_8s_2k_time_prior.npz``
     The reference's time-marginalised lnL under a TruncatedGaussian
     geocent_time prior (time, time+phase, time+distance, all three).
@@ -860,6 +863,7 @@ def main():
             try:
                 if args.time_prior_only:
                     run_time_prior(bilby)
+                    run_marginalised(bilby, "tf2_marg_6s_2k", 8)
                 if args.roq_multibasis_only:
                     run_roq_multibasis(bilby)
             finally:
@@ -932,6 +936,7 @@ def main():
             try:
                 run_marginalised(bilby, "tf2_marg_8s_2k", 8)
                 run_marginalised(bilby, "tf2_marg_8s", 16)
+                run_marginalised(bilby, "tf2_marg_6s_2k", 8)
                 run_time_prior(bilby)
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)

@@ -67,7 +67,7 @@ def golden_points(w, priors, combo):
     return pts, z["lnl_" + combo]
 
 
-@pytest.mark.parametrize("workload", ["tf2_marg_8s_2k", "tf2_marg_8s"])
+@pytest.mark.parametrize("workload", ["tf2_marg_8s_2k", "tf2_marg_8s", "tf2_marg_6s_2k"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("combo", COMBOS)
 def test_marginalized_vs_reference_golden(gpu, tmp_path, combo, precision, workload):
@@ -329,3 +329,32 @@ def test_time_prior_other_than_uniform_vs_reference(gpu, tmp_path, combo, precis
         assert np.all(np.abs(got - ref) <= 1e-8 * np.maximum(1.0, np.abs(ref))), got - ref
     else:
         assert np.max(np.abs(got - ref)) <= 1e-3, got - ref
+
+
+def test_time_series_at_a_length_that_is_not_a_power_of_two(gpu):
+    """The float64 transform d_inner_h_array of base.py:325-330 at FFT length
+    6144 = 3 x 2048 (6 s at 2048 Hz: three radix-2 transforms of 2048 combined
+    by a radix-3 step) against numpy's FFT in the oracle, summed over
+    detectors, for points on and off the injection."""
+    from oracle import data as OD
+    from oracle import restate as R
+    from tests.gpu_helpers import device_analysis, draw_points, params_block
+    w = WORKLOADS["tf2_marg_6s_2k"]
+    dets = OD.build_workload(w)
+    an = device_analysis(dets, "taylorf2", w)
+    tc = w.injection["geocent_time"]
+    an.set_time_marginalization(True, False, tc - 0.1, tc + 0.1)
+    p = draw_points(w, 6, np.random.default_rng(12))
+    for k in ("mass_1", "mass_2", "chi_1", "chi_2", "luminosity_distance", "theta_jn", "phase", "ra", "dec", "psi",
+              "geocent_time"):
+        p[k][0] = w.injection[k]
+    p["time_jitter"] = np.zeros(6)
+    series, hh = an.time_series_host(params_block(p))
+    assert series.shape == (6, 6144)
+    src = OD.source_for(w.model, w.minimum_frequency)
+    for i in range(6):
+        q = point(p, i)
+        pols = src(dets[0].frequency, **q)
+        ref = sum(R.snrs(d, pols, q, True)[2] for d in dets)
+        assert np.max(np.abs(series[i] - ref)) <= 1e-9 * np.max(np.abs(ref)), i
+    an.close()

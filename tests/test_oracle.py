@@ -51,7 +51,7 @@ def test_oracle_matches_reference_log_likelihood_ratio(name):
         assert abs(got - z["lnl"][i]) <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["tf2_marg_8s_2k", "tf2_marg_8s"])
+@pytest.mark.parametrize("name", ["tf2_marg_8s_2k", "tf2_marg_8s", "tf2_marg_6s_2k"])
 def test_oracle_time_and_phase_marginalization_matches_reference(name):
     """The reference's time / phase / time+phase marginalised values at FFT
     lengths 8192 and 16384."""
