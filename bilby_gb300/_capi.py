@@ -113,6 +113,7 @@ SIGNATURES = {
     "gwl_priors_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "gwl_priors_rescale": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "gwl_priors_set_frame": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "gwl_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                     ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)]),
     "gwl_get_chunks_per_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),

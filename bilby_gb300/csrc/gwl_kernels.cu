@@ -907,15 +907,19 @@ __device__ __forceinline__ void ff_mul_to(float& h, float& l, float bh, float bl
   l = __fsub_rn(e, __fsub_rn(h, p));
 }
 
+// 64 points per CTA: twice the CTAs of the other mixed kernels, so that a
+// batch of ten thousand points fills every SM with several CTAs
+constexpr int kSgPointsPerCta = 64;
+
 template <int D>
-__global__ void __launch_bounds__(kPointsPerCta) k_mixed_sg(LaunchArgs a) {
+__global__ void __launch_bounds__(kSgPointsPerCta) k_mixed_sg(LaunchArgs a) {
   constexpr int CH = kChunkMixed;
   __shared__ __align__(16) float2 s_w[D][CH];
   __shared__ __align__(16) float s_vh[D][CH];
   __shared__ __align__(16) float s_vl[D][CH];
   __shared__ uint64_t bar;
   const int64_t k0 = a.k_base + (int64_t)blockIdx.y * CH;
-  const int64_t slot = (int64_t)blockIdx.x * kPointsPerCta + threadIdx.x;
+  const int64_t slot = (int64_t)blockIdx.x * kSgPointsPerCta + threadIdx.x;
   const bool have = slot < a.B;
   const int64_t i = have && a.order ? (int64_t)a.order[slot] : slot;  // points ordered by centre frequency
   if (threadIdx.x == 0) {
@@ -1860,8 +1864,8 @@ static cudaError_t configure_mixed() {
 
 cudaError_t launch_mixed(const LaunchArgs& a, cudaStream_t s) {
   if (a.model == GWL_MODEL_SINEGAUSSIAN) {
-    dim3 grid((unsigned)((a.B + kPointsPerCta - 1) / kPointsPerCta), (unsigned)a.n_chunks);
-    GWL_DISPATCH_D(k_mixed_sg, grid, kPointsPerCta, 0, s, a);
+    dim3 grid((unsigned)((a.B + kSgPointsPerCta - 1) / kSgPointsPerCta), (unsigned)a.n_chunks);
+    GWL_DISPATCH_D(k_mixed_sg, grid, kSgPointsPerCta, 0, s, a);
   } else {
     const cudaError_t ce = configure_mixed();
     if (ce != cudaSuccess) return ce;

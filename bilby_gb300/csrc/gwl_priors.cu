@@ -17,13 +17,24 @@
 #include <string>
 #include <vector>
 
+#include "gwl_device.cuh"
 #include "gwl_internal.h"
 #include "gwl_math.cuh"
+
+namespace gwl {
+// detector-frame conversion of a prior program (gwl_priors_set_frame)
+struct PriorFrame {
+  int has_rotation = 0, has_vertex = 0;
+  double rotation[9] = {};
+  double vertex[3] = {};
+};
+}  // namespace gwl
 
 struct gwl_priors {
   int n = 0;
   gwl::PriorEntry* d_entries = nullptr;
   std::vector<double*> tables;
+  gwl::PriorFrame frame;
   std::mutex mu;
 };
 
@@ -83,11 +94,13 @@ __device__ __forceinline__ double prior_value(const PriorEntry& e, double u) {
   }
 }
 
-__global__ void k_priors(const PriorEntry* entries, int n, const double* unit, int64_t B, double* params) {
+__global__ void k_priors(const PriorEntry* entries, int n, const double* unit, int64_t B, double* params,
+                         PriorFrame frame) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
-  double mc = NAN, q = NAN, mt = NAN, cti = NAN;
-  bool has_mc = false, has_q = false, has_mt = false, has_cti = false;
+  double mc = NAN, q = NAN, mt = NAN, cti = NAN, zen = NAN, azi = NAN, tdet = NAN;
+  bool has_mc = false, has_q = false, has_mt = false, has_cti = false, has_zen = false, has_azi = false,
+       has_tdet = false;
   for (int k = 0; k < n; ++k) {
     const PriorEntry& e = entries[k];
     const double u = e.column >= 0 ? unit[(int64_t)e.column * B + i] : 0.0;
@@ -97,6 +110,9 @@ __global__ void k_priors(const PriorEntry* entries, int n, const double* unit, i
       case GWL_T_MASS_RATIO: q = v; has_q = true; break;
       case GWL_T_TOTAL_MASS: mt = v; has_mt = true; break;
       case GWL_T_COS_THETA_JN: cti = v; has_cti = true; break;
+      case GWL_T_ZENITH: zen = v; has_zen = true; break;
+      case GWL_T_AZIMUTH: azi = v; has_azi = true; break;
+      case GWL_T_DETECTOR_TIME: tdet = v; has_tdet = true; break;
       default:
         if (e.target >= 0 && e.target < GWL_NPARAM) params[(int64_t)e.target * B + i] = v;
     }
@@ -109,6 +125,31 @@ __global__ void k_priors(const PriorEntry* entries, int n, const double* unit, i
     params[(int64_t)GWL_P_MASS_2 * B + i] = m1 * q;
   }
   if (has_cti) params[(int64_t)GWL_P_THETA_JN * B + i] = acos(cti);
+  // base.py:1091-1137: the sampled time is the reference detector's when it
+  // is sampled, else geocent_time
+  const double t = has_tdet ? tdet : params[(int64_t)GWL_P_GEOCENT_TIME * B + i];
+  if (frame.has_rotation && has_zen && has_azi) {
+    // zenith / azimuth in the detector-pair frame to ra / dec (gw/utils.py:232-256)
+    const double wx = sin(zen) * cos(azi), wy = sin(zen) * sin(azi), wz = cos(zen);
+    const double* R = frame.rotation;
+    const double ox = R[0] * wx + R[1] * wy + R[2] * wz;
+    const double oy = R[3] * wx + R[4] * wy + R[5] * wz;
+    const double oz = R[6] * wx + R[7] * wy + R[8] * wz;
+    const double theta = acos(oz);
+    const double phi = pymod(atan2(oy, ox), kTwoPi);
+    params[(int64_t)GWL_P_RA * B + i] = pymod(phi + gmst_radians(t), kTwoPi);
+    params[(int64_t)GWL_P_DEC * B + i] = kPi / 2 - theta;
+  }
+  if (frame.has_vertex && has_tdet) {
+    // geometry.py:319-343: geocent_time = t - time_delay_from_geocenter(vertex, ra, dec, t)
+    const double ra = params[(int64_t)GWL_P_RA * B + i], dec = params[(int64_t)GWL_P_DEC * B + i];
+    const double gmst = pymod(gmst_radians(t), kTwoPi);
+    const double ph = ra - gmst, th = kPi / 2 - dec;
+    const double ox = sin(th) * cos(ph), oy = sin(th) * sin(ph), oz = cos(th);
+    const double delay = ((0.0 - frame.vertex[0]) * ox + (0.0 - frame.vertex[1]) * oy + (0.0 - frame.vertex[2]) * oz) /
+                         kSpeedOfLight;
+    params[(int64_t)GWL_P_GEOCENT_TIME * B + i] = t - delay;
+  }
 }
 
 }  // namespace gwl
@@ -135,7 +176,7 @@ int gwl_priors_create(const gwl_prior* entries, int32_t n, gwl_priors** out) {
     for (int q = 0; q < 4; ++q) d.p[q] = e.p[q];
     const bool table = e.kind == GWL_PRIOR_TABLE_LINEAR || e.kind == GWL_PRIOR_TABLE_BSPLINE;
     if (e.kind < GWL_PRIOR_DELTA || e.kind > GWL_PRIOR_TABLE_BSPLINE ||
-        (e.target < 0 || (e.target >= GWL_NPARAM && (e.target < GWL_T_CHIRP_MASS || e.target > GWL_T_COS_THETA_JN)))) {
+        (e.target < 0 || (e.target >= GWL_NPARAM && (e.target < GWL_T_CHIRP_MASS || e.target > GWL_T_DETECTOR_TIME)))) {
       set_error("gwl_priors_create: unknown prior kind or target in entry " + std::to_string(k));
       gwl_priors_destroy(p);
       return GWL_ERR_ARGUMENT;
@@ -198,12 +239,25 @@ int gwl_priors_rescale(gwl_priors* p, const double* unit, int64_t B, double* par
   std::lock_guard<std::mutex> g(p->mu);
   const int threads = 128;
   gwl::k_priors<<<(unsigned)((B + threads - 1) / threads), threads, 0, static_cast<cudaStream_t>(stream)>>>(
-      p->d_entries, p->n, unit, B, params);
+      p->d_entries, p->n, unit, B, params, p->frame);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("gwl_priors_rescale: ") + cudaGetErrorString(e));
     return GWL_ERR_CUDA;
   }
+  return GWL_OK;
+}
+
+int gwl_priors_set_frame(gwl_priors* p, const double* rotation, const double* vertex) {
+  if (!p) {
+    set_error("gwl_priors_set_frame: null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(p->mu);
+  p->frame.has_rotation = rotation ? 1 : 0;
+  p->frame.has_vertex = vertex ? 1 : 0;
+  for (int k = 0; k < 9; ++k) p->frame.rotation[k] = rotation ? rotation[k] : 0.0;
+  for (int k = 0; k < 3; ++k) p->frame.vertex[k] = vertex ? vertex[k] : 0.0;
   return GWL_OK;
 }
 

@@ -503,11 +503,16 @@ class GravitationalWaveTransient(_Base):
         float64 tensor [len(device_priors.keys), B]; the priors' inverse CDFs and
         the mass / inclination conversions run on the device
         (``bilby_gb300.priors_device.DevicePriors``), then the likelihood, all
-        on torch's current stream with no host work per point.  Needs the sky
-        frame and geocentre time (no detector-frame sampling)."""
+        on torch's current stream with no host work per point.  With a
+        detector-pair reference frame or a detector time reference the priors'
+        zenith / azimuth and ``<detector>_time`` columns become ra / dec and
+        geocent_time on the device, as get_sky_frame_parameters does
+        (base.py:1091-1137)."""
         import torch
-        if self._frame is not None or self.time_reference != "geocent":
-            raise NotImplementedError("unit-cube batches need reference_frame='sky' and geocentre time")
+        rotation = None if self._frame is None else np.asarray(self._frame.rotation, dtype=np.float64)
+        vertex = None if self.reference_ifo is None else np.asarray(self.reference_ifo.geometry.vertex,
+                                                                    dtype=np.float64)
+        device_priors.set_frame(rotation, vertex)
         block = device_priors.rescale(unit)
         n = block.shape[1]
         res = out if out is not None else torch.empty(n, dtype=torch.float64, device=block.device)

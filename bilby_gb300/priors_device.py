@@ -5,7 +5,9 @@ this package's mirrors) into a ``gwl_priors`` program: each sampled key reads
 one column of a unit-cube tensor and applies its inverse CDF; fixed priors
 become constants; chirp mass / total mass with mass ratio become the
 component masses, and cos_theta_jn becomes theta_jn
-(bilby/core/prior/dict.py PriorDict.rescale, bilby/gw/conversion.py:182-283).
+(bilby/core/prior/dict.py PriorDict.rescale, bilby/gw/conversion.py:182-283),
+and with a frame set (``set_frame``) zenith / azimuth and a detector's arrival
+time become ra / dec and geocent_time (bilby/gw/likelihood/base.py:1091-1137).
 ``rescale(unit)`` then maps a [len(keys), B] CUDA float64 tensor to the
 [NPARAM, B] parameter block in one launch, so a sampler's unit-cube batch
 goes to the likelihood without host work per point
@@ -21,7 +23,9 @@ from . import _capi
 
 PRIOR_DELTA, PRIOR_UNIFORM, PRIOR_POWERLAW, PRIOR_SINE, PRIOR_COSINE = 0, 1, 2, 3, 4
 PRIOR_GAUSSIAN, PRIOR_TRUNCATED_GAUSSIAN, PRIOR_TABLE_LINEAR, PRIOR_TABLE_BSPLINE = 5, 6, 7, 8
-TARGETS_EXTRA = {"chirp_mass": 100, "mass_ratio": 101, "total_mass": 102, "cos_theta_jn": 103}
+TARGETS_EXTRA = {"chirp_mass": 100, "mass_ratio": 101, "total_mass": 102, "cos_theta_jn": 103, "zenith": 104,
+                 "azimuth": 105}
+TARGET_DETECTOR_TIME = 106  # "<detector>_time": the arrival time at the likelihood's reference detector
 
 
 class GwlPrior(ctypes.Structure):
@@ -82,6 +86,8 @@ def compile_program(priors, keys):
             target = _capi.SLOT[key]
         elif key in TARGETS_EXTRA:
             target = TARGETS_EXTRA[key]
+        elif key.endswith("_time"):
+            target = TARGET_DETECTOR_TIME
         else:
             raise NotImplementedError(f"no device conversion for parameter {key}")
         if key in keys:
@@ -142,6 +148,16 @@ class DevicePriors:
                                                  ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
                     "gwl_priors_rescale")
         return out
+
+    def set_frame(self, rotation=None, vertex=None):
+        """Detector-frame conversion (``gwl_priors_set_frame``): the 3x3 rotation
+        of the detector-pair frame and the reference detector's vertex; None
+        clears either."""
+        r = None if rotation is None else np.ascontiguousarray(rotation, dtype=np.float64).reshape(9)
+        v = None if vertex is None else np.ascontiguousarray(vertex, dtype=np.float64).reshape(3)
+        self._frame_keep = (r, v)
+        _capi.check(self._lib.gwl_priors_set_frame(self._h, None if r is None else _capi.dptr(r),
+                                                   None if v is None else _capi.dptr(v)), "gwl_priors_set_frame")
 
     def close(self):
         h = getattr(self, "_h", None)

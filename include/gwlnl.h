@@ -386,7 +386,10 @@ enum {
   GWL_T_CHIRP_MASS = 100,
   GWL_T_MASS_RATIO = 101,
   GWL_T_TOTAL_MASS = 102,
-  GWL_T_COS_THETA_JN = 103
+  GWL_T_COS_THETA_JN = 103,
+  GWL_T_ZENITH = 104,        /* detector-pair frame (gwl_priors_set_frame) */
+  GWL_T_AZIMUTH = 105,
+  GWL_T_DETECTOR_TIME = 106  /* arrival time at the reference detector (gwl_priors_set_frame) */
 };
 typedef struct gwl_prior {
   int32_t kind;          /* GWL_PRIOR_* */
@@ -403,6 +406,16 @@ int gwl_priors_destroy(gwl_priors *p);
 /* unit: device [n_columns][B]; params: device [GWL_NPARAM][B] (slots without
  * an entry are left as they are) */
 int gwl_priors_rescale(gwl_priors *p, const double *unit, int64_t B, double *params, void *stream);
+
+/* Detector-frame sampling for the batch path (get_sky_frame_parameters,
+ * bilby/gw/likelihood/base.py:1091-1137): with `rotation` (the 3x3 row-major
+ * rotation of the detector-pair frame, bilby/gw/geometry.py rotation_matrix_
+ * from_delta) the GWL_T_ZENITH / GWL_T_AZIMUTH values become ra / dec at
+ * the sampled time (the reference detector's arrival time when one is
+ * sampled, else geocent_time); with `vertex` (the reference detector's
+ * vertex, m) the GWL_T_DETECTOR_TIME value becomes geocent_time =
+ * t - time_delay_from_geocenter(vertex, ra, dec, t).  NULL clears either. */
+int gwl_priors_set_frame(gwl_priors *p, const double *rotation, const double *vertex);
 
 /* Autotuner (no counterpart in the reference, which has no launch shapes):
  * times the mixed-precision TaylorF2 launch sequence on the caller's B device
