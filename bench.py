@@ -600,10 +600,23 @@ def bench_relbin(name, steps, warmup, batch=65536, seed=31):
                                                        fiducial_parameters=dict(w.injection), priors=priors,
                                                        time_marginalization=True)
     bt = 2048
-    ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
-    res["time_marginalized"] = {"batch": bt, "fft_length": int(like_t.analysis.n_bins - 1),
-                                "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
-                                "precision": "fp64", "finite": finite}
+    block = time_marginalized_block(w, bt, rng)
+    tm = {"batch": bt, "fft_length": int(like_t.analysis.n_bins - 1),
+          "launch": "prologue + windowed four-step transform, one CTA per point (float32 with refinement "
+                    "of the marked points in float64, or float64)"}
+    outs = {}
+    for precision in ("fp64", "mixed"):
+        ms_t, finite = time_launches(like_t.analysis, block, bt, steps, warmup, precision=precision)
+        o = torch.empty(bt, dtype=torch.float64, device="cuda")
+        like_t.analysis.log_likelihood_ratio_device(block.data_ptr(), bt, o.data_ptr(), precision, stream.cuda_stream)
+        torch.cuda.synchronize()
+        outs[precision] = o
+        tm[precision] = {"value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t, "finite": finite}
+        if precision == "mixed":
+            tm[precision]["refined_points_per_launch"] = int(like_t.analysis.last_refined())
+    tm["mixed_over_fp64"] = tm["mixed"]["value"] / tm["fp64"]["value"]
+    tm["max_abs_dlnl_mixed_vs_fp64"] = float((outs["mixed"] - outs["fp64"]).abs().max().item())
+    res["time_marginalized"] = tm
     return res
 
 

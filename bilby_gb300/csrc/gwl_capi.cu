@@ -98,6 +98,8 @@ struct gwl_analysis {
   int rb_tm = 0;                    // time-marginalisation weights set for these bins
   double2* rb_g[kMaxDet] = {};
   int32_t* rb_bin = nullptr;
+  float2* rb_gf[kMaxDet] = {};  // mixed-precision copies over the bins' span
+  RbBinF* rb_bx = nullptr;
   // multi-banding
   int multiband = 0;
   int64_t mb_points = 0;
@@ -361,10 +363,12 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.rb_index = a->rb_index;
   L.rb_freq = a->rb_freq;
   L.rb_bin = a->rb_bin;
+  L.rb_bx = a->rb_bx;
   for (int d = 0; d < a->n_det; ++d) {
     L.rb_h0inv[d] = a->rb_h0inv[d];
     L.rb_sum[d] = a->rb_sum[d];
     L.rb_g[d] = a->rb_g[d];
+    L.rb_gf[d] = a->rb_gf[d];
   }
   L.multiband = a->multiband;
   L.mb_points = a->mb_points;
@@ -417,7 +421,13 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
   const size_t part = (size_t)std::max(a->n_chunks_plain, a->n_chunks_mixed) * B * a->n_det * kPartStride *
                       sizeof(double);
   size_t tm = 0;
-  if (a->time_marg && !a->roq) tm = time_marg_work_bytes(L);  // ROQ marginalises without an FFT
+  if (a->time_marg && !a->roq) {  // ROQ marginalises without an FFT
+    // the float64 kernel over the whole FFT keeps one transform per resident
+    // CTA in global memory; the windowed kernels need none
+    LaunchArgs F = L;
+    F.precision = GWL_PRECISION_FP64;
+    if (!time_marg_window_fits(F)) tm = time_marg_work_bytes(L);
+  }
   if (B <= a->ws_B && part <= a->part_bytes && tm <= a->tm_bytes) return GWL_OK;
   GWL_CUDA(cudaStreamSynchronize(a->stream));
   free_workspace(a);
@@ -447,6 +457,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   }
   if (B <= 0) return GWL_OK;
   LaunchArgs L = make_args(a, B, precision);
+  L.tm_series = d_series;
   int rc = ensure_workspace(a, B, L);
   if (rc) return rc;
   L.params = d_params;
@@ -484,11 +495,39 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       set_error("multi-banding with time marginalisation needs gwl_set_multiband_time_marginalization");
       return GWL_ERR_ARGUMENT;
     }
-    L.precision = GWL_PRECISION_FP64;
+    // the windowed four-step transform where its shared memory fits (mixed
+    // precision for relative binning, with the float64 kernel recomputing the
+    // points over the tolerance), else the float64 kernel over the whole FFT
     L.rf_tol = 0.0;
+    L.precision = (precision == GWL_PRECISION_MIXED && a->relbin) ? GWL_PRECISION_MIXED : GWL_PRECISION_FP64;
+    bool window = time_marg_window_fits(L);
+    if (!window && L.precision == GWL_PRECISION_MIXED) {
+      L.precision = GWL_PRECISION_FP64;
+      window = time_marg_window_fits(L);
+    }
+    const bool mixed = window && L.precision == GWL_PRECISION_MIXED && a->refine_tol > 0;
     GWL_CUDA(launch_prologue(L, s));
+    if (mixed) {
+      // marks of the windowed mixed kernel (after the prologue, which would
+      // otherwise apply the full-grid kernels' bound)
+      L.rf_tol = a->refine_tol;
+      L.rf_count = a->d_order_hist;
+      a->last_rf_count = L.rf_count;
+      GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
+    }
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
-    GWL_CUDA(launch_time_marginalized(L, s));
+    if (window) {
+      GWL_CUDA(launch_time_marg_window(L, s));
+      if (mixed) {
+        LaunchArgs R = L;
+        R.precision = GWL_PRECISION_FP64;
+        R.rf_tol = 0.0;
+        R.tw_refine_only = 1;
+        GWL_CUDA(launch_time_marg_window(R, s));
+      }
+    } else {
+      GWL_CUDA(launch_time_marginalized(L, s));
+    }
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
       a->ev_pending = 1;
@@ -1268,11 +1307,23 @@ int gwl_set_relative_binning_time_weights(gwl_analysis* a, const double* weights
   bin.back() = (int32_t)(idx.size() - 2);
   int rc;
   if ((rc = upload(a, &a->rb_bin, bin))) return rc;
+  // mixed precision: f_k - (f_b + f_b+1) / 2 of each grid index, in float32
+  std::vector<RbBinF> bx(bin.size());
+  for (size_t q = 0; q < bin.size(); ++q) {
+    const int32_t b = bin[q];
+    const double fc = (a->h_freq[idx[(size_t)b]] + a->h_freq[idx[(size_t)b + 1]]) / 2;
+    bx[q] = RbBinF{b, (float)(a->h_freq[(size_t)k0 + q] - fc)};
+  }
+  if ((rc = upload(a, &a->rb_bx, bx))) return rc;
   for (int d = 0; d < a->n_det; ++d) {
     std::vector<double2> w((size_t)a->n_bins);
     for (int64_t k = 0; k < a->n_bins; ++k)
       w[(size_t)k] = make_double2(weights[((size_t)d * a->n_bins + k) * 2], weights[((size_t)d * a->n_bins + k) * 2 + 1]);
+    std::vector<float2> wf(bin.size());
+    for (size_t q = 0; q < wf.size(); ++q)
+      wf[q] = make_float2((float)w[(size_t)k0 + q].x, (float)w[(size_t)k0 + q].y);
     if ((rc = upload(a, &a->rb_g[d], w))) return rc;
+    if ((rc = upload(a, &a->rb_gf[d], wf))) return rc;
   }
   a->rb_tm = 1;
   return GWL_OK;

@@ -59,6 +59,13 @@ struct PointRec {
   int32_t refine;                    // TaylorF2 mixed: error bound above the tolerance (LaunchArgs::rf_tol)
 };
 
+// Relative binning, per grid index: its bin and the offset of its frequency
+// from the bin's centre.
+struct RbBinF {
+  int32_t bin;
+  float x;
+};
+
 struct DetGeom {
   double vertex[3];
   double tensor[9];
@@ -146,6 +153,11 @@ struct LaunchArgs {
   // [rb_index[0], rb_index[rb_edges - 1]]
   const double2* rb_g[kMaxDet];         // [n_bins]
   const int32_t* rb_bin;                // [rb_index[last] - rb_index[0] + 1]
+  // ... and for the mixed-precision kernel over the same span: the weights in
+  // float32 and, per grid index, its bin with f - (f_b + f_b+1) / 2
+  const float2* rb_gf[kMaxDet];         // [rb_index[last] - rb_index[0] + 1]
+  const RbBinF* rb_bx;                  // [rb_index[last] - rb_index[0] + 1]
+  int tw_refine_only;                   // float64 windowed time marginalisation: only the marked points
   // multi-banding: the model at the banded frequencies, weighted by the
   // per-detector linear (complex) and quadratic (real) coefficients
   int multiband;
@@ -265,6 +277,11 @@ void order_layout(int64_t n_chunks, int* keys, int* shift);
 void ordering_with_marks(LaunchArgs& L);
 void ordering_by_peak(LaunchArgs& L);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
+// Relative binning / multi-banding with time marginalisation by the windowed
+// four-step transform (gwl_marg_window.cu): whether this launch's shared
+// memory fits, and the launch (mixed precision: relative binning only).
+bool time_marg_window_fits(const LaunchArgs& a);
+cudaError_t launch_time_marg_window(const LaunchArgs& a, cudaStream_t s);
 // FFT lengths the time-marginalised kernels take: L = m 2^p with m odd,
 // m <= kTmMaxOddFactor and p >= 4 (m and p returned)
 constexpr int kTmMaxOddFactor = 127;

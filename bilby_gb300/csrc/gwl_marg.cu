@@ -29,118 +29,13 @@
 #include "gwl_device.cuh"
 #include "gwl_device_cache.h"
 #include "gwl_internal.h"
+#include "gwl_marg_common.cuh"
 #include "gwl_math.cuh"
 
 namespace gwl {
 
 constexpr int kTmThreads = 512;
 constexpr int kTmTwiddleRows = 128;
-
-// The density of a geocent_time prior other than Uniform at GPS time t
-// (LaunchArgs::tm_prior): Lagrange interpolation through the four table nodes
-// around t, shifted inwards at the ends of the table (the nodes lie inside the
-// prior's support, so a time between a support edge and the first node is
-// extrapolated by less than one node spacing); zero beyond.  t - t0 is exact
-// (t0 and the nodes are multiples of a power-of-two step), so a sample on a
-// node reads that node's density exactly.
-__device__ __forceinline__ double tm_prior_density(const LaunchArgs& a, double t) {
-  const double x = (t - a.tm_prior_t0) * a.tm_prior_inv_h;
-  if (!(x >= -1.0 && x <= (double)a.tm_prior_n)) return 0.0;
-  const int64_t g = max((int64_t)0, min((int64_t)floor(x) - 1, a.tm_prior_n - 4));
-  const double u = x - (double)g, u1 = u - 1.0, u2 = u - 2.0, u3 = u - 3.0;
-  const double* p = a.tm_prior + g;
-  const double v = (p[3] * u * u1 * u2 - p[0] * u1 * u2 * u3) / 6.0 + (p[1] * u * u2 * u3 - p[2] * u * u1 * u3) / 2.0;
-  return fmax(v, 0.0);
-}
-
-__device__ __forceinline__ float tm_prior_density_f(const LaunchArgs& a, double t) {
-  const double x = (t - a.tm_prior_t0) * a.tm_prior_inv_h;
-  if (!(x >= -1.0 && x <= (double)a.tm_prior_n)) return 0.f;
-  const int64_t g = max((int64_t)0, min((int64_t)floor(x) - 1, a.tm_prior_n - 4));
-  const float u = (float)(x - (double)g), u1 = u - 1.f, u2 = u - 2.f, u3 = u - 3.f;
-  const float* p = a.tm_prior_f + g;
-  const float v = (p[3] * u * u1 * u2 - p[0] * u1 * u2 * u3) * (1.f / 6.f) + (p[1] * u * u2 * u3 - p[2] * u * u1 * u3) * 0.5f;
-  return fmaxf(v, 0.f);
-}  // two-level twiddle tables: L / 2 <= 128 * 128
-
-template <bool MIXED>
-struct TmTypes;
-template <>
-struct TmTypes<true> {
-  using C = float2;
-  using R = float;
-};
-template <>
-struct TmTypes<false> {
-  using C = double2;
-  using R = double;
-};
-
-__device__ __forceinline__ uint32_t bit_reverse(uint32_t k, int log2n) { return __brev(k) >> (32 - log2n); }
-
-// float64 source polarisations of the plain kernels at one frequency.
-__device__ __forceinline__ bool plain_pols(const LaunchArgs& a, const PointRec& r, double f, double2& hp, double2& hx) {
-  if (a.model == GWL_MODEL_SINEGAUSSIAN) {
-    const double pi2 = 9.869604401089358;
-    const double fm = f - r.sg_f0, fpl = f + r.sg_f0;
-    const double neg = exp(-(fm * fm) * pi2 * r.a[3]);
-    const double pos = exp(-(fpl * fpl) * pi2 * r.a[3]);
-    hp = make_double2(r.a[0] * (neg + pos) / r.a[1], 0.0);
-    hx = make_double2(0.0, -(r.a[0] * (neg - pos) / r.a[2]));
-    return true;
-  }
-  if (f < a.fmin || f >= r.f_isco) return false;
-  const double v = cbrt(kPi * r.m_sec * f), lnv = log(v);
-  double s = 0.0, vk = 1.0;
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    s = s + (r.a[q] + r.l[q] * lnv) * vk;
-    vk = vk * v;
-  }
-  const double psi = (-2.0 * r.phase - kPi / 4) + 3.0 / (128.0 * r.eta) * s / (v * v * v * v * v);
-  const double amp = r.amp * pow(f, -7.0 / 6.0);
-  double sp, cp;
-  sincos(psi, &sp, &cp);
-  const double ere = amp * cp, eim = -amp * sp, ci = r.cos_i, pf = (1.0 + ci * ci) / 2.0;
-  hp = make_double2(pf * ere, pf * eim);
-  hx = make_double2(ci * eim, -ci * ere);
-  return true;
-}
-
-// The same TaylorF2 polarisations from a power-table entry t = {f^(1/3),
-// ln(f) / 3, f^(-5/3), f^(-7/6)}; u = (pi M)^(1/3), pu5 = 3 / (128 eta u^5).
-__device__ __forceinline__ bool tf2_pols_t(const LaunchArgs& a, const PointRec& r, const double4& t, double f,
-                                           double u, double lnu, double pu5, double2& hp, double2& hx) {
-  if (f < a.fmin || f >= r.f_isco) return false;
-  const double v = u * t.x, lnv = lnu + t.y;
-  double s = r.a[7];
-#pragma unroll
-  for (int q = 6; q >= 0; --q) s = s * v + r.a[q];
-  const double v5 = v * v * v * v * v;
-  s = s + lnv * (r.l[5] + r.l[6] * v) * v5;
-  const double psi = (-2.0 * r.phase - kPi / 4) + pu5 * s * t.z;
-  const double amp = r.amp * t.w;
-  double sp, cp;
-  sincos(psi, &sp, &cp);
-  const double ere = amp * cp, eim = -amp * sp, ci = r.cos_i, pf = (1.0 + ci * ci) / 2.0;
-  hp = make_double2(pf * ere, pf * eim);
-  hx = make_double2(ci * eim, -ci * ere);
-  return true;
-}
-
-// ... at grid bin k of the per-bin power table
-__device__ __forceinline__ bool tf2_pols_tab(const LaunchArgs& a, const PointRec& r, int64_t k, double f, double u,
-                                             double lnu, double pu5, double2& hp, double2& hx) {
-  if (f < a.fmin || f >= r.f_isco) return false;
-  return tf2_pols_t(a, r, a.ftab[k], f, u, lnu, pu5, hp, hx);
-}
-
-// (c + i s) *= (rc + i rs)
-__device__ __forceinline__ void tm_rotate(double& c, double& s, double rc, double rs) {
-  const double t = c * rc - s * rs;
-  s = c * rs + s * rc;
-  c = t;
-}
 
 // Block-wide reductions over kTmThreads threads in a fixed tree order.
 __device__ double block_max(double v, double* red) {
@@ -411,42 +306,10 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       // summary data, and the integrand from the full-grid waveform
       // h0_d(f) (r0_b + r1_b (f - f_b)) of each bin b
       double2* s_rat = reinterpret_cast<double2*>(smem);  // [D][nE]
-      const int nE = a.rb_edges, nB = nE - 1;
-      const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
-      const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
-      const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
-      for (int e = threadIdx.x; e < nE; e += blockDim.x) {
-        const double f = a.rb_freq[e];
-        double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
-        const bool on = r.valid && (tf2 ? tf2_pols_tab(a, r, a.rb_index[e], f, u, lnu, pu5, hp, hx)
-                                        : plain_pols(a, r, f, hp, hx));
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          double2 q = make_double2(0.0, 0.0);
-          if (on) {
-            // interferometer.py:341-362 at explicit frequencies (no mask)
-            const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
-            double sn, cs;
-            sincos(2.0 * kPi * r.dt[d] * f, &sn, &cs);
-            const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
-            const double2 g = a.rb_h0inv[d][e];
-            q = make_double2(hre * g.x - him * g.y, hre * g.y + him * g.x);
-          }
-          s_rat[d * nE + e] = q;
-        }
-      }
+      const int nE = a.rb_edges;
+      relbin_edge_ratios<D>(a, r, s_rat);
       __syncthreads();
-      for (int b = threadIdx.x; b < nB; b += blockDim.x) {
-        const double width = a.rb_freq[b + 1] - a.rb_freq[b];
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          const double2 q0 = s_rat[d * nE + b], q1 = s_rat[d * nE + b + 1];
-          const double r0r = (q1.x + q0.x) / 2, r0i = (q1.y + q0.y) / 2;
-          const double r1r = (q1.x - q0.x) / width, r1i = (q1.y - q0.y) / width;
-          const double* sd = a.rb_sum[d] + (size_t)b * 6;
-          hh_part += sd[4] * (r0r * r0r + r0i * r0i) + 2.0 * sd[5] * (r0r * r1r + r0i * r1i);
-        }
-      }
+      hh_part = relbin_hh_part<D>(a, s_rat);
       const int64_t k0 = a.rb_index[0], k1 = a.rb_index[nE - 1];
       for (int64_t k = threadIdx.x; k < L; k += blockDim.x) {
         double zr = 0.0, zi = 0.0;
@@ -746,63 +609,14 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
     double m = -INFINITY, acc = 0.0;
     for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
-      // base.py:1027-1035 (linspace(0, T, L + 1)[1:], the last sample exactly T), or
-      // multiband.py:714-717 (arange(L) * delta_tc)
-      const double lin = a.tm_first ? ((j + 1 == L) ? a.duration : (double)(j + 1) * step) : (double)j * step;
-      const double t = (a.start_time0 + lin) + jit;
-      if (!(t >= a.t_min && t <= a.t_max)) continue;
-      // base.py:807: prior(t_j) delta_tc; a Uniform prior's constant is applied once, below
-      double lw = 0.0;
-      if (a.tm_prior) {
-        if constexpr (MIXED) {
-          const float pw = tm_prior_density_f(a, t);
-          if (!(pw > 0.f)) continue;
-          lw = (double)__logf(pw);
-        } else {
-          const double pw = tm_prior_density(a, t);
-          if (!(pw > 0.0)) continue;
-          lw = log(pw);
-        }
-      }
+      const double t = tm_sample_time(a, j, L, step, jit);
+      double lw;
+      if (!tm_log_weight<MIXED>(a, t, lw)) continue;
       const C x = out_at(buf, j);
       double l;
-      if constexpr (MIXED) {
-        // float32 per-sample work; the large terms combine in float64
-        const float xr = x.x, xi = x.y;
-        if (a.dist_marg) {
-          const float dx = a.phase_marg ? sqrtf(xr * xr + xi * xi) * (float)sr : xr * (float)sr;
-          l = (double)bicubic_eval_row_f(s_tx, a.nx, a.ny, a.tc_f, a.bbox, dx, s_row);
-        } else if (a.phase_marg) {
-          const float ax = sqrtf(xr * xr + xi * xi);
-          l = ((double)ax + (double)ln_i0_minus_x(ax)) - hh / 2;
-        } else {
-          l = (double)xr - hh / 2;
-        }
-        l += lw;
-        if (l > m) {
-          acc = isfinite(m) ? acc * (double)__expf((float)(m - l)) + 1.0 : 1.0;
-          m = l;
-        } else if (isfinite(l)) {
-          acc += (double)__expf((float)(l - m));
-        }
-      } else {
-        const double xr = x.x, xi = x.y;
-        if (a.dist_marg) {
-          const double dx = a.phase_marg ? sqrt(xr * xr + xi * xi) * sr : xr * sr;
-          l = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx, hh_ref);
-        } else if (a.phase_marg) {
-          l = ln_i0(sqrt(xr * xr + xi * xi)) - hh / 2;
-        } else {
-          l = xr - hh / 2;
-        }
-        l += lw;
-        if (l > m) {
-          acc = isfinite(m) ? acc * exp(m - l) + 1.0 : 1.0;
-          m = l;
-        } else if (isfinite(l)) {
-          acc += exp(l - m);
-        }
-      }
+      if constexpr (MIXED) l = tm_lnl_mixed(a, x.x, x.y, hh, sr, s_tx, s_row);
+      else l = tm_lnl_fp64(a, x.x, x.y, hh, hh_ref, sr);
+      tm_lse_push<MIXED>(l + lw, m, acc);
     }
     // combine (m, acc) pairs over the block in a fixed order
     double* redm = red;
@@ -1048,18 +862,14 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
   }
 }
 
-namespace {
-
 // exp(-2 pi i t / L), t < L / 2, in float64 and float32, one table per
 // (device, FFT length), kept for the life of the process: analyses of
 // different lengths may launch at the same time from different host threads,
 // so a table is never replaced or freed while a kernel may read it, and the
 // tables of one device are never handed to a launch on another.
-struct TwiddleTables {
-  double2* d64 = nullptr;
-  float2* d32 = nullptr;
-};
+namespace {
 PerDeviceCache<TwiddleTables> g_twiddles;
+}  // namespace
 
 cudaError_t twiddles_for(int64_t L, TwiddleTables* out) {
   int dev = 0;
@@ -1091,6 +901,7 @@ cudaError_t twiddles_for(int64_t L, TwiddleTables* out) {
   return static_cast<cudaError_t>(rc);
 }
 
+namespace {
 
 int tm_grid_fp64() {
   int dev = 0, sms = 0;

@@ -237,7 +237,8 @@ int gwl_batcher_status(gwl_batcher *b, int *device_status);
 
 /* Zero-copy host staging: gwl_host_buffers returns the analysis's pinned
  * parameter block [GWL_NPARAM][B] and result buffer [B] (valid until a
- * larger batch reallocates them); the caller fills the block and calls
+ * larger batch, or a first gwl_time_series_device call on a relative-binning
+ * or multi-banding analysis, reallocates them); the caller fills the block and calls
  * gwl_eval_host_staged, which runs gwl_eval_host without the two host
  * copies and leaves the lnL ratios in the result buffer.  Same results as
  * gwl_eval_host (no counterpart in the reference). */

@@ -7,7 +7,9 @@ marginalisation.  Also: the relative-binning lnL agrees with the full
 likelihood near the fiducial point, and batch equals single.
 
 Tolerances: float64 |dlnL| <= 1e-9 * max(1, |lnL|) (1e-8 with the distance
-table, as for the full likelihood)."""
+table, as for the full likelihood); the mixed-precision time-marginalised
+kernel (windowed four-step transform in float32, with error control) |dlnL| <=
+1e-3 against the reference and against the float64 kernel."""
 import numpy as np
 import pytest
 
@@ -17,7 +19,7 @@ from bilby_gb300.workloads import DISTANCE_PRIOR, WORKLOADS, point
 pytestmark = pytest.mark.gpu
 
 
-def make(combo, tmp_path):
+def make(combo, tmp_path, precision="fp64"):
     from bilby_gb300 import random as grandom
     from bilby_gb300.detector import InterferometerList
     from bilby_gb300.prior import PowerLaw, Uniform
@@ -45,7 +47,7 @@ def make(combo, tmp_path):
         ifos, wfg, fiducial_parameters=dict(w.injection), priors=priors or None,
         phase_marginalization="p" in combo, distance_marginalization="d" in combo,
         distance_marginalization_lookup_table=str(tmp_path / "table.npz"),
-        time_marginalization="t" in combo)
+        time_marginalization="t" in combo, precision=precision)
     return w, ifos, wfg, like, priors
 
 
@@ -119,3 +121,46 @@ def test_close_to_the_full_likelihood_near_the_fiducial(plain):
     assert e[1e-5] < 0.05, e
     assert e[1e-5] < e[1e-4] / 5, e
 
+
+@pytest.mark.parametrize("combo", ["t", "tpd"])
+def test_mixed_time_marginalized_matches_the_reference(gpu, tmp_path, combo):
+    w, ifos, wfg, like, priors = make(combo, tmp_path, precision="mixed")
+    z = golden("tf2_128s_relbin")
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    n = len(params["mass_1"])
+    batch = {k: np.asarray(v, dtype=float).copy() for k, v in params.items()}
+    batch["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+    batch["time_jitter"] = np.asarray(z["time_jitter"], dtype=float)
+    if "p" in combo:
+        batch["phase"] = np.zeros(n)
+    if "d" in combo:
+        batch["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+    ref = z["lnl_" + combo]
+    got = like.log_likelihood_ratio_batch(batch)
+    assert np.all(np.abs(got - ref) <= 1e-3), got - ref
+
+
+def test_mixed_time_marginalized_prior_draws_within_1e3_of_fp64(gpu, tmp_path):
+    """2048 prior draws (sky, masses, spins, distance, inclination) with time,
+    phase and distance marginalisation: the mixed kernel (with its refinement)
+    against the float64 windowed kernel; the error bound marks few points."""
+    from bilby_gb300.workloads import draw_points
+    w, ifos, wfg, like, priors = make("tpd", tmp_path, precision="mixed")
+    _, _, _, like64, _ = make("tpd", tmp_path, precision="fp64")
+    rng = np.random.default_rng(17)
+    p = draw_points(w, 2048, rng)
+    p["geocent_time"] = np.full(2048, float(priors["geocent_time"]))
+    p["phase"] = np.zeros(2048)
+    p["luminosity_distance"] = np.full(2048, float(priors["luminosity_distance"]))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, 2048)
+    mx = like.log_likelihood_ratio_batch(p)
+    refined = like.analysis.last_refined()
+    f64 = like64.log_likelihood_ratio_batch(p)
+    assert np.all(np.isfinite(mx))
+    assert np.max(np.abs(mx - f64)) <= 1e-3, np.max(np.abs(mx - f64))
+    assert refined <= 2048 // 10, refined
+    # with the error control off, every point comes from the float32 kernel
+    like.analysis.refinement_tolerance = 0.0
+    raw = like.log_likelihood_ratio_batch(p)
+    assert like.analysis.last_refined() == 0
+    assert np.max(np.abs(raw - f64)) <= 1e-3, np.max(np.abs(raw - f64))
