@@ -148,6 +148,8 @@ struct gwl_analysis {
   int* last_rf_count = nullptr;     // marked points of the last mixed TaylorF2 evaluation (device)
   double* d_tm = nullptr;
   size_t tm_bytes = 0;
+  double* d_twpart = nullptr;  // windowed float64 recomputation: shares, then the per-point unit counters
+  size_t twpart_bytes = 0;
   double* h_params = nullptr;  // pinned staging for gwl_eval_host
   double* h_out = nullptr;      // [ws_B + 1]: the results, then the device status word
   int* d_status = nullptr;
@@ -196,6 +198,9 @@ void free_workspace(gwl_analysis* a) {
   cudaFree(a->d_order);
   cudaFree(a->d_order_hist);
   cudaFree(a->d_tm);
+  cudaFree(a->d_twpart);
+  a->d_twpart = nullptr;
+  a->twpart_bytes = 0;
   cudaFreeHost(a->h_params);
   cudaFreeHost(a->h_out);
   a->h_params = a->h_out = nullptr;
@@ -427,6 +432,9 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
     LaunchArgs F = L;
     F.precision = GWL_PRECISION_FP64;
     if (!time_marg_window_fits(F)) tm = time_marg_work_bytes(L);
+    // the mixed windowed multi-banding kernel: one slot of banded values per CTA
+    if (a->multiband && a->mb_tm && a->model == GWL_MODEL_TAYLORF2)
+      tm = std::max(tm, (size_t)time_marg_window_slots() * (size_t)a->mb_points * sizeof(float2));
   }
   if (B <= a->ws_B && part <= a->part_bytes && tm <= a->tm_bytes) return GWL_OK;
   GWL_CUDA(cudaStreamSynchronize(a->stream));
@@ -468,6 +476,11 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   L.hh_out = d_hh;
   L.tm_work = a->d_tm;
   L.tm_series = d_series;
+  if (a->multiband && a->mb_points > 0) {
+    L.tw_scratch = reinterpret_cast<float2*>(a->d_tm);
+    L.tw_scratch_slots = std::min<int64_t>(time_marg_window_slots(),
+                                           (int64_t)(a->tm_bytes / ((size_t)a->mb_points * sizeof(float2))));
+  }
   if (a->roq && a->time_marg && d_out) {
     if (!a->roq_tm) {
       set_error("ROQ with time marginalisation needs gwl_set_roq_time_marginalization");
@@ -496,22 +509,37 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       return GWL_ERR_ARGUMENT;
     }
     // the windowed four-step transform where its shared memory fits (mixed
-    // precision for relative binning, with the float64 kernel recomputing the
-    // points over the tolerance), else the float64 kernel over the whole FFT
+    // precision for relative binning and TaylorF2 multi-banding, with the
+    // float64 kernel recomputing the points over the tolerance), else the
+    // float64 kernel over the whole FFT
     L.rf_tol = 0.0;
-    L.precision = (precision == GWL_PRECISION_MIXED && a->relbin) ? GWL_PRECISION_MIXED : GWL_PRECISION_FP64;
-    bool window = time_marg_window_fits(L);
+    L.precision = (precision == GWL_PRECISION_MIXED && (a->relbin || a->model == GWL_MODEL_TAYLORF2))
+                      ? GWL_PRECISION_MIXED
+                      : GWL_PRECISION_FP64;
+    bool window = time_marg_window_fits(L) && (L.precision != GWL_PRECISION_MIXED || time_marg_window_mixed_ready(L));
     if (!window && L.precision == GWL_PRECISION_MIXED) {
       L.precision = GWL_PRECISION_FP64;
       window = time_marg_window_fits(L);
     }
     const bool mixed = window && L.precision == GWL_PRECISION_MIXED && a->refine_tol > 0;
+    constexpr int64_t kShareUnits = 4096;  // float64 recomputation units in flight at most
+    const size_t share = mixed ? time_marg_window_share_bytes(L) : 0;
+    const size_t share_total = share * kShareUnits + sizeof(int) * kShareUnits;
+    if (mixed && share_total > a->twpart_bytes) {
+      GWL_CUDA(cudaStreamSynchronize(s));
+      cudaFree(a->d_twpart);
+      a->d_twpart = nullptr;
+      a->twpart_bytes = 0;
+      if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_twpart), share_total, false))) return rc;
+      a->twpart_bytes = share_total;
+    }
     GWL_CUDA(launch_prologue(L, s));
     if (mixed) {
       // marks of the windowed mixed kernel (after the prologue, which would
-      // otherwise apply the full-grid kernels' bound)
+      // otherwise apply the full-grid kernels' bound), listed in d_order
       L.rf_tol = a->refine_tol;
       L.rf_count = a->d_order_hist;
+      L.rf_list = a->d_order;
       a->last_rf_count = L.rf_count;
       GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
     }
@@ -523,6 +551,10 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
         R.precision = GWL_PRECISION_FP64;
         R.rf_tol = 0.0;
         R.tw_refine_only = 1;
+        R.tw_part = a->d_twpart;
+        R.tw_part_units = kShareUnits;
+        R.tw_done = reinterpret_cast<int*>(reinterpret_cast<char*>(a->d_twpart) + share * kShareUnits);
+        GWL_CUDA(cudaMemsetAsync(R.tw_done, 0, sizeof(int) * kShareUnits, s));
         GWL_CUDA(launch_time_marg_window(R, s));
       }
     } else {

@@ -158,6 +158,12 @@ struct LaunchArgs {
   const float2* rb_gf[kMaxDet];         // [rb_index[last] - rb_index[0] + 1]
   const RbBinF* rb_bx;                  // [rb_index[last] - rb_index[0] + 1]
   int tw_refine_only;                   // float64 windowed time marginalisation: only the marked points
+  float2* tw_scratch;                   // mixed windowed multi-banding: [tw_scratch_slots][mb_points] banded values
+  int64_t tw_scratch_slots;
+  int32_t* rf_list;                     // windowed mixed kernel: the marked points, [*rf_count]
+  double* tw_part;                      // float64 recomputation: [tw_part_units][n_win_max + 1] complex shares
+  int* tw_done;                         // ... finished units per marked point, [tw_part_units], zeroed before
+  int64_t tw_part_units;
   // multi-banding: the model at the banded frequencies, weighted by the
   // per-detector linear (complex) and quadratic (real) coefficients
   int multiband;
@@ -281,6 +287,10 @@ cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 // four-step transform (gwl_marg_window.cu): whether this launch's shared
 // memory fits, and the launch (mixed precision: relative binning only).
 bool time_marg_window_fits(const LaunchArgs& a);
+bool time_marg_window_mixed_ready(const LaunchArgs& a);  // the mixed kernel's tables and work space are there
+int64_t time_marg_window_slots();                        // work-space slots of the mixed multi-banding kernel
+// bytes per unit of the float64 recomputation's shares (0: the window does not fit)
+size_t time_marg_window_share_bytes(const LaunchArgs& a);
 cudaError_t launch_time_marg_window(const LaunchArgs& a, cudaStream_t s);
 // FFT lengths the time-marginalised kernels take: L = m 2^p with m odd,
 // m <= kTmMaxOddFactor and p >= 4 (m and p returned)

@@ -19,8 +19,10 @@
 // butterflies and n_win N1 window terms, against L/2 log2(L) butterflies for
 // the whole transform.
 //
-// Mixed precision (relative binning): float32 integrand, transform and window
-// sums, with the per-bin ratio coefficients r0, r1 and <h|h> in float64.  The
+// Mixed precision: float32 integrand, transform and compensated window sums;
+// relative binning keeps the per-bin ratio coefficients and <h|h> in float64,
+// multi-banding (TaylorF2) forms its banded values with the exact fixed-point
+// phase of the non-marginalised mixed kernel.  The
 // error bound of a point is s (kWinErrNorm ||z||_2 + kWinErrPeak max_j |X_j|),
 // s the largest sensitivity dl_j / d|X_j| over the window; points over the
 // tolerance are marked and recomputed by the float64 kernel.
@@ -34,6 +36,7 @@
 #include "gwl_internal.h"
 #include "gwl_marg_common.cuh"
 #include "gwl_math.cuh"
+#include "gwl_phase.cuh"
 
 namespace gwl {
 
@@ -51,6 +54,10 @@ constexpr int kWinOutRows = 1024;   // mixed output twiddles: q = 1024 q1 + q2
 // between 5 and 120 Mpc with |X| up to 1.9e4).
 constexpr double kWinErrNorm = 6e-7;
 constexpr double kWinErrPeak = 2e-7;
+// ... plus, for multi-banding, the independent relative errors (below about
+// 2.5e-7) of the banded terms (phase fraction, sincospi, weight, products):
+// four standard deviations of their sum over the window's samples
+constexpr double kWinErrTerm = 1e-6;
 
 namespace {
 
@@ -137,7 +144,8 @@ __device__ __forceinline__ void win_pass(C* cols, int cs, int log2n2, int stage,
   }
 }
 
-template <int D, bool MIXED>
+// MB: multi-banding (else relative binning)
+template <int D, bool MIXED, bool MB>
 __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     k_tm_window(LaunchArgs a, WinLayout lay, const typename TmTypes<MIXED>::C* twiddle) {
   using C = typename TmTypes<MIXED>::C;
@@ -149,6 +157,8 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
   __shared__ double s_red[2 * kWinWarps];
   __shared__ double s_scal[4];
   __shared__ long long s_jr[2];
+  __shared__ long long s_kb[2];
+  __shared__ int s_last;
   __shared__ SplineRowF s_row;
   const int L = (int)a.n_fft, N1 = (int)lay.n1;  // L < 2^30 (checked on the host)
   const int log2n2 = lay.log2n2;
@@ -208,12 +218,29 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
 
   const double norm = 4.0 / a.duration;
   const int nE = a.rb_edges, nB = nE - 1;
-  const int k0 = a.relbin ? (int)a.rb_index[0] : 0, k1 = a.relbin ? (int)a.rb_index[nE - 1] : -1;
-  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+  const int k0 = MB ? 0 : (int)a.rb_index[0], k1 = MB ? -1 : (int)a.rb_index[nE - 1];
+  // Work units.  Evaluation: one per point.  Float64 recomputation of the
+  // points the mixed kernel marked (rf_list[0 .. *rf_count)): P units per
+  // point, unit c taking the column groups c, c + P, ...; each writes its
+  // window sums and <h|h> share to tw_part, and the last of the point's units
+  // to finish adds the P shares in a fixed order and completes the point.
+  int P = 1;
+  int64_t n_units = a.B;
+  if (a.tw_refine_only) {
+    const int64_t cnt = *a.rf_count;
+    const int64_t groups = (N1 + G - 1) / G;
+    // at least four column groups per unit (each unit repeats the per-point set-up)
+    if (cnt > 0) P = (int)std::max<int64_t>(1, std::min<int64_t>(groups / 4, (int64_t)gridDim.x / cnt));
+    if (cnt * P > a.tw_part_units) P = (int)std::max<int64_t>(1, a.tw_part_units / std::max<int64_t>(cnt, 1));
+    n_units = cnt * P;
+  }
+  for (int64_t unit = blockIdx.x; unit < n_units; unit += gridDim.x) {
+    const int64_t slot = unit / P;
+    const int part_c = (int)(unit - slot * P);
+    const int64_t i = a.tw_refine_only ? (int64_t)a.rf_list[slot] : unit;
     const PointRec& r = a.rec[i];
-    if (a.tw_refine_only && !r.refine) continue;  // the same i for the whole CTA
     if (!r.valid) {
-      if (threadIdx.x == 0) a.out[i] = -1.7976931348623157e308;  // nan_to_num(-inf)
+      if (threadIdx.x == 0 && part_c == 0) a.out[i] = -1.7976931348623157e308;  // nan_to_num(-inf)
       continue;
     }
     const double jit = r.jitter;
@@ -233,12 +260,13 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     }
     // ---- per-point set-up ----------------------------------------------
     double hh_part = 0.0;
+    float z2 = 0.f;  // mixed: sum of |z_k|^2 (error bound)
     double2* rat = reinterpret_cast<double2*>(smem + lay.off_rat);  // relative binning: [D][nE]
     float4* coef = reinterpret_cast<float4*>(smem + lay.off_coef);  // mixed: [D][nB] {r0, r1}, then [D][nB] lo(r0)
-    if (a.relbin) {
+    if constexpr (!MB) {
       relbin_edge_ratios<D>(a, r, rat);
       __syncthreads();
-      hh_part = relbin_hh_part<D>(a, rat);
+      if (part_c == 0) hh_part = relbin_hh_part<D>(a, rat);
       if constexpr (MIXED) {
         // relative.py:374-377: r0 = (q_b+1 + q_b) / 2, r1 = (q_b+1 - q_b) / width;
         // r0 as float-float (its rounding would be the same for every grid
@@ -255,9 +283,99 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         }
       }
     }
+    // mixed multi-banding: z_m = sum_d A Q_d exp(-i phase_d(f_m)) L_d(f_m) at
+    // every banded frequency m into this CTA's slot of the work space
+    // (L2-resident), as k_multiband_mixed forms its terms: the TaylorF2 phase
+    // from the float-float basis, detector d's time shift exact in 0.64 fixed
+    // point per band, sincospi of the exact fraction; <h|h> from the prefix
+    // sums of the quadratic coefficients over the point's band.
+    float2* zb = nullptr;
+    if constexpr (MIXED && MB) {
+      {
+        zb = a.tw_scratch + (size_t)blockIdx.x * (size_t)a.mb_points;
+        uint64_t* s_y = reinterpret_cast<uint64_t*>(smem + lay.off_rat);  // [bands][D]: frac(f_b0 dt_d)
+        uint64_t* s_x = s_y + a.mb_bands * D;                              // [bands][D]: frac(df_b dt_d)
+        float2* s_g = reinterpret_cast<float2*>(s_x + a.mb_bands * D);     // [D]: A Q_d scale_d
+        for (int t = threadIdx.x; t < a.mb_bands * D; t += blockDim.x) {
+          const int b = t / D, d = t - b * D;
+          const double y = a.mb_freq[a.mb_band_start[b]] * r.dt[d], x = a.mb_band_df[b] * r.dt[d];
+          double fy = ldexp(y - floor(y), 64), fx = ldexp(x - floor(x), 64);
+          if (!(fy < 18446744073709551616.0)) fy = 0.0;
+          if (!(fx < 18446744073709551616.0)) fx = 0.0;
+          s_y[t] = (uint64_t)fy;
+          s_x[t] = (uint64_t)fx;
+        }
+        if (threadIdx.x == 32) {
+          // the point's band among the banded frequencies: fmin <= f < f_isco
+          int64_t lo = 0, hi = a.mb_points;
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) / 2;
+            if (a.mb_freq[mid] >= a.fmin) hi = mid; else lo = mid + 1;
+          }
+          const int64_t kb0 = lo;
+          hi = a.mb_points;
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) / 2;
+            if (a.mb_freq[mid] >= r.f_isco) hi = mid; else lo = mid + 1;
+          }
+          const int64_t kb1 = lo;
+          s_kb[0] = kb0;
+          s_kb[1] = kb1;
+          const double ci = r.cos_i, pfac = (1.0 + ci * ci) / 2.0;
+          for (int d = 0; d < D; ++d) {
+            const double qr = r.fp[d] * pfac, qi = -r.fx[d] * ci;
+            s_g[d] = make_float2((float)(r.amp * qr * a.mb_lw_scale[d]), (float)(r.amp * qi * a.mb_lw_scale[d]));
+            hh_part += r.amp * r.amp * (qr * qr + qi * qi) * (a.mb_qprefix[d][kb1] - a.mb_qprefix[d][kb0]);
+          }
+        }
+        float ch[kNumBasis + 1], cl[kNumBasis + 1];
+#pragma unroll
+        for (int b = 0; b <= kNumBasis; ++b) {
+          ch[b] = r.c_hi[b];
+          cl[b] = r.c_lo[b];
+        }
+        __syncthreads();
+        const int64_t kb0 = s_kb[0], kb1 = s_kb[1];
+        for (int b = 0; b < a.mb_bands; ++b) {
+          const int64_t bs = a.mb_band_start[b], be = a.mb_band_start[b + 1];
+          for (int64_t m = bs + threadIdx.x; m < be; m += blockDim.x) {
+            float2 z = make_float2(0.f, 0.f);
+            if (m >= kb0 && m < kb1) {
+              const float4* bp = reinterpret_cast<const float4*>(a.mb_basis + m * kNumBasis);
+              float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+              for (int q = 0; q < kNumBasis / 2; ++q) {
+                const float4 v = __ldg(bp + q);
+                ff_mac(s_hi, s_lo, ch[2 * q], cl[2 * q], v.x, v.y);
+                ff_mac(s_hi, s_lo, ch[2 * q + 1], cl[2 * q + 1], v.z, v.w);
+              }
+              const uint64_t base = to_fixed(s_hi, s_lo), idx = (uint64_t)(m - bs);
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                const uint64_t full = base + s_y[b * D + d] + idx * s_x[b * D + d];
+                const uint32_t top = (uint32_t)((full + 0x80000000ull) >> 32);
+                const float ph = __fmul_rn(__int2float_rn((int)top), 4.656612873077393e-10f);  // 2 * 2^-32
+                float sn, cs;
+                sincospif(ph, &sn, &cs);
+                const float2 Lw = __ldg(a.mb_lw[d] + m);
+                // exp(-i 2 pi frac) L, then times A Q_d scale_d
+                const float tr = cs * Lw.x + sn * Lw.y, ti = cs * Lw.y - sn * Lw.x;
+                const float2 g = s_g[d];
+                z.x += g.x * tr - g.y * ti;
+                z.y += g.x * ti + g.y * tr;
+              }
+              z2 += z.x * z.x + z.y * z.y;
+            }
+            zb[m] = z;
+          }
+        }
+        __syncthreads();
+      }
+    }
     const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
-    const double u = (a.mb_tm && tf2) ? cbrt(kPi * r.m_sec) : 0.0, lnu = (a.mb_tm && tf2) ? log(u) : 0.0;
-    const double pu5 = (a.mb_tm && tf2) ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+    const double u = (MB && !MIXED && tf2) ? cbrt(kPi * r.m_sec) : 0.0;
+    const double lnu = (MB && !MIXED && tf2) ? log(u) : 0.0;
+    const double pu5 = (MB && !MIXED && tf2) ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
     for (int t = threadIdx.x; t < lay.n_win_max; t += blockDim.x) {
       C z;
       z.x = 0;
@@ -270,12 +388,11 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     const int j_lo = (int)s_jr[0];
     const int n_win = (int)(s_jr[1] - s_jr[0] + 1);
     // integrand z_k (k < L): 4/T sum_d h_d,k conj(d_k) / S_k
-    float z2 = 0.f;  // mixed: sum of |z_k|^2 (error bound)
     const auto integrand = [&](int k) -> C {
       C z;
       z.x = 0;
       z.y = 0;
-      if (a.relbin) {
+      if constexpr (!MB) {
         if constexpr (MIXED) {
           // float32: ratio r0 + r1 (f - f_b) times the weight 4/T h0 conj(d) / S;
           // no branch around the loads (a clamped index and a zero factor
@@ -315,7 +432,19 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         }
         return z;
       }
-      if constexpr (!MIXED) {
+      if constexpr (MIXED) {
+        // multi-banding: the banded values at the full-resolution indices
+        // int(f_m T) (multiband.py:714-726)
+        const int32_t c1 = a.mb_tm_ptr[k + 1];
+        for (int32_t c = a.mb_tm_ptr[k]; c < c1; ++c) {
+          const int32_t code = a.mb_tm_src[c];
+          if (code >= 0) {
+            const float2 v = zb[code];
+            z.x += v.x;
+            z.y += v.y;
+          }
+        }
+      } else {
         // multi-banding: the banded strain times the linear coefficients at the
         // full-resolution indices int(f_j T); <h|h> from the quadratic ones
         const int32_t c1 = a.mb_tm_ptr[k + 1];
@@ -345,7 +474,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     };
 
     // ---- columns: integrand, transform, window sums ------------------------
-    for (int n1_0 = 0; n1_0 < N1; n1_0 += G) {
+    for (int n1_0 = part_c * G; n1_0 < N1; n1_0 += P * G) {
       // A block b of RN0 positions of column g holds, after the first RB0
       // stages, the RN0-point DFT of the column's elements q + m N2 / RN0
       // (m < RN0), q = bitrev(b) over log2(N2) - RB0 bits.
@@ -407,7 +536,9 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
       // compensation in acc_lo.
       for (int t = threadIdx.x; t < n_win; t += blockDim.x) {
         const int j = j_lo + t, jm = j & (N2 - 1);
-        int qq = qst[t];
+        // n1 j mod L: carried from the previous group, or (a unit of a split
+        // recomputation, whose groups are P apart) formed afresh
+        int qq = P > 1 ? (int)(((int64_t)n1_0 * j) % L) : qst[t];
         C s = acc[t], e;
         if constexpr (MIXED) e = acc_lo[t];
 #pragma unroll
@@ -461,6 +592,35 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
       }
     }
     __syncthreads();
+    if (P > 1) {
+      // this unit's share to the point's slot; the last unit adds them up
+      double2* share = reinterpret_cast<double2*>(a.tw_part) + (size_t)unit * (lay.n_win_max + 1);
+      for (int t = threadIdx.x; t < n_win; t += blockDim.x) share[t] = make_double2(acc[t].x, acc[t].y);
+      if (threadIdx.x == 0) share[lay.n_win_max] = make_double2(s_scal[1], 0.0);
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) s_last = atomicAdd(a.tw_done + slot, 1) == P - 1;
+      __syncthreads();
+      if (!s_last) continue;  // uniform over the CTA
+      __threadfence();
+      const double2* shares = reinterpret_cast<const double2*>(a.tw_part) + (size_t)slot * P * (lay.n_win_max + 1);
+      for (int t = threadIdx.x; t < n_win; t += blockDim.x) {
+        double xr = 0.0, xi = 0.0;
+        for (int c = 0; c < P; ++c) {
+          const double2 v = __ldcg(shares + (size_t)c * (lay.n_win_max + 1) + t);
+          xr += v.x;
+          xi += v.y;
+        }
+        acc[t].x = (R)xr;
+        acc[t].y = (R)xi;
+      }
+      if (threadIdx.x == 0) {
+        double h = 0.0;
+        for (int c = 0; c < P; ++c) h += __ldcg(shares + (size_t)c * (lay.n_win_max + 1) + lay.n_win_max).x;
+        s_scal[1] = h;
+      }
+      __syncthreads();
+    }
     const double step = s_scal[0], hh_all = s_scal[1], sr = s_scal[2], znorm = s_scal[3];
     const double hh_ref = hh_all * sr * sr;
     double m = -INFINITY, lse = 0.0;
@@ -530,9 +690,10 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
           const double dn = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, fmax(dx - del, 0.0), hh_ref);
           sens = fmin(1.25 * sr * fabs(up - dn) / (dx + del - fmax(dx - del, 0.0)) + 1e-6, 1e6);
         }
-        if (!(sens * (kWinErrNorm * znorm + kWinErrPeak * xpk) <= a.rf_tol)) {
+        const double err = (kWinErrNorm + (MB ? kWinErrTerm : 0.0)) * znorm + kWinErrPeak * xpk;
+        if (!(sens * err <= a.rf_tol)) {
           a.rec[i].refine = 1;
-          atomicAdd(a.rf_count, 1);
+          a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
         }
       }
     }
@@ -568,7 +729,9 @@ bool win_layout(const LaunchArgs& a, WinLayout* lay) {
   lay->off_q = (int)off;
   off = up16(off + (size_t)lay->n_win_max * sizeof(int));
   lay->off_rat = (int)off;
-  off = up16(off + (a.relbin ? (size_t)a.n_det * a.rb_edges * sizeof(double2) : 0));
+  size_t rat = a.relbin ? (size_t)a.n_det * a.rb_edges * sizeof(double2) : 0;
+  if (MIXED && a.mb_tm) rat = (size_t)a.mb_bands * a.n_det * 2 * sizeof(uint64_t) + (size_t)a.n_det * sizeof(float2);
+  off = up16(off + rat);
   lay->off_coef = (int)off;
   off = up16(off + ((MIXED && a.relbin) ? (size_t)a.n_det * (a.rb_edges - 1) * (sizeof(float4) + sizeof(float2)) : 0));
   lay->off_knots = (int)off;
@@ -577,18 +740,21 @@ bool win_layout(const LaunchArgs& a, WinLayout* lay) {
   return off <= (size_t)200 * 1024;
 }
 
-template <int D, bool MIXED>
+template <int D, bool MIXED, bool MB>
 cudaError_t launch_win_d(const LaunchArgs& a, const WinLayout& lay, const TwiddleTables& tw, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_tm_window<D, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_tm_window<D, MIXED, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned grid = (unsigned)std::min<int64_t>(a.B, 8 * (int64_t)std::max(sms, 1));
+  // the recomputation's unit count is known on the device only
+  int64_t grid = a.tw_refine_only ? 8 * (int64_t)std::max(sms, 1) : std::min<int64_t>(a.B, 8 * (int64_t)std::max(sms, 1));
+  if (MIXED && a.mb_tm) grid = std::min<int64_t>(grid, a.tw_scratch_slots);  // one work-space slot per CTA
   const typename TmTypes<MIXED>::C* twp;
   if constexpr (MIXED) twp = tw.d32;
   else twp = tw.d64;
-  k_tm_window<D, MIXED><<<grid, kWinThreads, lay.bytes, s>>>(a, lay, twp);
+  k_tm_window<D, MIXED, MB><<<(unsigned)grid, kWinThreads, lay.bytes, s>>>(a, lay, twp);
   return cudaGetLastError();
 }
 
@@ -599,15 +765,43 @@ cudaError_t launch_win(const LaunchArgs& a, cudaStream_t s) {
   TwiddleTables tw;
   cudaError_t e = twiddles_for(a.n_fft, &tw);
   if (e != cudaSuccess) return e;
+  if (a.mb_tm) {
+    switch (a.n_det) {
+      case 1: return launch_win_d<1, MIXED, true>(a, lay, tw, s);
+      case 2: return launch_win_d<2, MIXED, true>(a, lay, tw, s);
+      case 3: return launch_win_d<3, MIXED, true>(a, lay, tw, s);
+      default: return launch_win_d<4, MIXED, true>(a, lay, tw, s);
+    }
+  }
   switch (a.n_det) {
-    case 1: return launch_win_d<1, MIXED>(a, lay, tw, s);
-    case 2: return launch_win_d<2, MIXED>(a, lay, tw, s);
-    case 3: return launch_win_d<3, MIXED>(a, lay, tw, s);
-    default: return launch_win_d<4, MIXED>(a, lay, tw, s);
+    case 1: return launch_win_d<1, MIXED, false>(a, lay, tw, s);
+    case 2: return launch_win_d<2, MIXED, false>(a, lay, tw, s);
+    case 3: return launch_win_d<3, MIXED, false>(a, lay, tw, s);
+    default: return launch_win_d<4, MIXED, false>(a, lay, tw, s);
   }
 }
 
 }  // namespace
+
+bool time_marg_window_mixed_ready(const LaunchArgs& a) {
+  if (a.relbin) return a.rb_bx != nullptr;
+  return a.mb_tm && a.model == GWL_MODEL_TAYLORF2 && a.mb_basis && a.tw_scratch && a.tw_scratch_slots > 0;
+}
+
+int64_t time_marg_window_slots() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return 2 * (int64_t)std::max(sms, 1);  // the mixed kernel's resident CTAs
+}
+
+size_t time_marg_window_share_bytes(const LaunchArgs& a) {
+  LaunchArgs F = a;
+  F.precision = GWL_PRECISION_FP64;
+  WinLayout lay;
+  if (!win_layout<false>(F, &lay)) return 0;
+  return (size_t)(lay.n_win_max + 1) * sizeof(double2);
+}
 
 bool time_marg_window_fits(const LaunchArgs& a) {
   if (!(a.relbin || a.mb_tm) || a.tm_series) return false;
@@ -617,7 +811,7 @@ bool time_marg_window_fits(const LaunchArgs& a) {
 
 cudaError_t launch_time_marg_window(const LaunchArgs& a, cudaStream_t s) {
   if (a.precision == GWL_PRECISION_MIXED) {
-    if (!a.relbin || !a.rb_bx) return cudaErrorInvalidValue;  // mixed: relative binning only
+    if (!time_marg_window_mixed_ready(a)) return cudaErrorInvalidValue;  // checked on the host first
     return launch_win<true>(a, s);
   }
   return launch_win<false>(a, s);

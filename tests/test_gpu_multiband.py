@@ -149,3 +149,66 @@ def test_mixed_holds_1e3_and_refines_loud_templates(gpu, tmp_path):
     assert an.last_refined() > 0
     fp64 = an.log_likelihood_ratio_host(params_block(loud), "fp64")
     assert np.max(np.abs(mixed - fp64)) <= 1e-3, np.max(np.abs(mixed - fp64))
+
+
+@pytest.mark.parametrize("combo", ["t", "tpd"])
+def test_mixed_time_marginalized_matches_the_reference_and_float64(gpu, tmp_path, combo):
+    """Time marginalisation in mixed precision (banded values with the exact
+    fixed-point phase, windowed four-step transform in float32 with
+    compensated window sums, float64 recomputation of the marked points):
+    |dlnL| <= 1e-3 against the reference on the golden points, and against
+    the float64 kernel on 1024 prior draws and on 1024 loud templates
+    (5-120 Mpc at the injection's masses and sky position)."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    w = WORKLOADS["tf2_128s"]
+    like, priors = make(combo, tmp_path, precision="mixed")
+    z = golden("tf2_128s_multiband")
+    params = {k[2:]: np.asarray(z[k], dtype=float) for k in z.files if k.startswith("p_")}
+    rng = np.random.default_rng(47)
+
+    def fix(p, jitter):
+        p = dict(p)
+        n = len(p["mass_1"])
+        p["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+        p["time_jitter"] = jitter if jitter is not None else rng.uniform(-1 / w.sampling_frequency,
+                                                                         1 / w.sampling_frequency, n)
+        if "p" in combo:
+            p["phase"] = np.zeros(n)
+        if "d" in combo:
+            p["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+        return p
+
+    golden_pts = fix(params, np.asarray(z["time_jitter"], dtype=float))
+    got = like.log_likelihood_ratio_batch(golden_pts)
+    ref = z["lnl_" + combo]
+    assert np.all(np.abs(got - ref) <= 1e-3), got - ref
+    loud = {k: np.full(1024, float(v)) for k, v in w.injection.items()}
+    loud["luminosity_distance"] = rng.uniform(5.0, 120.0, 1024)
+    loud["theta_jn"] = rng.uniform(0.0, np.pi, 1024)
+    for p in (fix(draw_points(w, 1024, rng), None), fix(loud, None)):
+        block = params_block(like._prepare(p))
+        mixed = like.analysis.log_likelihood_ratio_host(block, "mixed")
+        fp64 = like.analysis.log_likelihood_ratio_host(block, "fp64")
+        err = np.abs(mixed - fp64)
+        assert np.all(np.isfinite(mixed))
+        assert np.all(err <= 1e-3), (err.max(), fp64[np.argmax(err)])
+
+
+def test_split_recomputation_equals_float64(gpu, tmp_path):
+    """Every point marked (tolerance 1e-12) and recomputed by the split
+    float64 recomputation: equal to the float64 kernel's results to rounding."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    w = WORKLOADS["tf2_128s"]
+    like, priors = make("t", tmp_path, precision="mixed")
+    rng = np.random.default_rng(29)
+    p = draw_points(w, 8, rng)
+    p["geocent_time"] = np.full(8, float(priors["geocent_time"]))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, 8)
+    block = params_block(like._prepare(p))
+    like.analysis.refinement_tolerance = 1e-12
+    mixed = like.analysis.log_likelihood_ratio_host(block, "mixed")
+    assert like.analysis.last_refined() == 8
+    fp64 = like.analysis.log_likelihood_ratio_host(block, "fp64")
+    assert np.all(np.abs(mixed - fp64) <= 1e-10 * np.maximum(1.0, np.abs(fp64))), mixed - fp64

@@ -164,3 +164,26 @@ def test_mixed_time_marginalized_prior_draws_within_1e3_of_fp64(gpu, tmp_path):
     raw = like.log_likelihood_ratio_batch(p)
     assert like.analysis.last_refined() == 0
     assert np.max(np.abs(raw - f64)) <= 1e-3, np.max(np.abs(raw - f64))
+
+
+def test_split_recomputation_equals_float64(gpu, tmp_path):
+    """With the tolerance at 1e-12 every point is marked and recomputed in
+    float64 by the split recomputation (several CTAs per point, shares added
+    in a fixed order): the results equal the float64 kernel's to rounding, and
+    repeat bit for bit."""
+    from bilby_gb300.workloads import draw_points
+    w, ifos, wfg, like, priors = make("tpd", tmp_path, precision="mixed")
+    _, _, _, like64, _ = make("tpd", tmp_path, precision="fp64")
+    rng = np.random.default_rng(23)
+    p = draw_points(w, 8, rng)
+    p["geocent_time"] = np.full(8, float(priors["geocent_time"]))
+    p["phase"] = np.zeros(8)
+    p["luminosity_distance"] = np.full(8, float(priors["luminosity_distance"]))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, 8)
+    like.analysis.refinement_tolerance = 1e-12
+    a = like.log_likelihood_ratio_batch(p)
+    assert like.analysis.last_refined() == 8
+    b = like.log_likelihood_ratio_batch(p)
+    f64 = like64.log_likelihood_ratio_batch(p)
+    assert np.array_equal(a, b)
+    assert np.all(np.abs(a - f64) <= 1e-10 * np.maximum(1.0, np.abs(f64))), a - f64
