@@ -815,6 +815,8 @@ def bench_marginalized(name, steps, warmup, fp64_batch=256, seed=29):
             ms.append(e0.elapsed_time(e1))
         res[precision] = {"value": B * n / (sum(ms) / 1e3), "unit": "evals/s", "batch": B,
                           "ms_per_launch": float(np.mean(ms))}
+        if precision == "mixed":
+            res[precision]["refined_points_per_launch"] = int(an.last_refined())
     m = torch.empty(fp64_batch, dtype=torch.float64, device="cuda")
     f = torch.empty(fp64_batch, dtype=torch.float64, device="cuda")
     bl = block[:, :fp64_batch].contiguous()

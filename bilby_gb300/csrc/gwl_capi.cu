@@ -457,6 +457,62 @@ int ensure_workspace(gwl_analysis* a, int64_t B, const LaunchArgs& L) {
   return GWL_OK;
 }
 
+// The windowed time-marginalisation kernels' float64 recomputation: shares
+// of at most kShareUnits units (window sums and <h|h>), then one finished-unit
+// counter per unit; grown on demand.
+constexpr int64_t kShareUnits = 4096;
+
+int ensure_window_shares(gwl_analysis* a, const LaunchArgs& L, cudaStream_t s, size_t* share) {
+  *share = time_marg_window_share_bytes(L);
+  const size_t total = *share * kShareUnits + sizeof(int) * kShareUnits;
+  if (total <= a->twpart_bytes) return GWL_OK;
+  GWL_CUDA(cudaStreamSynchronize(s));
+  cudaFree(a->d_twpart);
+  a->d_twpart = nullptr;
+  a->twpart_bytes = 0;
+  int rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_twpart), total, false);
+  if (rc) return rc;
+  a->twpart_bytes = total;
+  return GWL_OK;
+}
+
+// Marks of a mixed time-marginalised kernel (after the prologue, which would
+// otherwise apply the full-grid kernels' bound): listed in d_order, counted
+// in d_order_hist.
+int set_window_marks(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
+  L.rf_tol = a->refine_tol;
+  L.rf_count = a->d_order_hist;
+  L.rf_list = a->d_order;
+  a->last_rf_count = L.rf_count;
+  GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
+  return GWL_OK;
+}
+
+// The float64 recomputation of the listed points by the windowed kernel,
+// split over several CTAs per point.
+int launch_window_refine(gwl_analysis* a, const LaunchArgs& L, cudaStream_t s, size_t share) {
+  LaunchArgs R = L;
+  R.precision = GWL_PRECISION_FP64;
+  R.rf_tol = 0.0;
+  R.tw_refine_only = 1;
+  R.tw_part = a->d_twpart;
+  R.tw_part_units = kShareUnits;
+  R.tw_done = reinterpret_cast<int*>(reinterpret_cast<char*>(a->d_twpart) + share * kShareUnits);
+  GWL_CUDA(cudaMemsetAsync(R.tw_done, 0, sizeof(int) * kShareUnits, s));
+  GWL_CUDA(launch_time_marg_window(R, s));
+  return GWL_OK;
+}
+
+// The windowed kernel after the prologue: mixed precision with its marks and
+// their recomputation, or float64 alone.
+int launch_window_marg(gwl_analysis* a, LaunchArgs& L, cudaStream_t s, bool mixed, size_t share) {
+  int rc;
+  if (mixed && (rc = set_window_marks(a, L, s))) return rc;
+  GWL_CUDA(launch_time_marg_window(L, s));
+  if (mixed && (rc = launch_window_refine(a, L, s, share))) return rc;
+  return GWL_OK;
+}
+
 int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, double* d_out, double* d_dh,
              double* d_hh, cudaStream_t s, double* d_series = nullptr) {
   if (precision != GWL_PRECISION_FP64 && precision != GWL_PRECISION_MIXED) {
@@ -522,41 +578,13 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       window = time_marg_window_fits(L);
     }
     const bool mixed = window && L.precision == GWL_PRECISION_MIXED && a->refine_tol > 0;
-    constexpr int64_t kShareUnits = 4096;  // float64 recomputation units in flight at most
-    const size_t share = mixed ? time_marg_window_share_bytes(L) : 0;
-    const size_t share_total = share * kShareUnits + sizeof(int) * kShareUnits;
-    if (mixed && share_total > a->twpart_bytes) {
-      GWL_CUDA(cudaStreamSynchronize(s));
-      cudaFree(a->d_twpart);
-      a->d_twpart = nullptr;
-      a->twpart_bytes = 0;
-      if ((rc = dev_alloc(a, reinterpret_cast<char**>(&a->d_twpart), share_total, false))) return rc;
-      a->twpart_bytes = share_total;
-    }
+    size_t share = 0;
+    a->last_rf_count = nullptr;  // no marks unless the mixed kernel sets them
+    if (mixed && (rc = ensure_window_shares(a, L, s, &share))) return rc;
     GWL_CUDA(launch_prologue(L, s));
-    if (mixed) {
-      // marks of the windowed mixed kernel (after the prologue, which would
-      // otherwise apply the full-grid kernels' bound), listed in d_order
-      L.rf_tol = a->refine_tol;
-      L.rf_count = a->d_order_hist;
-      L.rf_list = a->d_order;
-      a->last_rf_count = L.rf_count;
-      GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
-    }
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
     if (window) {
-      GWL_CUDA(launch_time_marg_window(L, s));
-      if (mixed) {
-        LaunchArgs R = L;
-        R.precision = GWL_PRECISION_FP64;
-        R.rf_tol = 0.0;
-        R.tw_refine_only = 1;
-        R.tw_part = a->d_twpart;
-        R.tw_part_units = kShareUnits;
-        R.tw_done = reinterpret_cast<int*>(reinterpret_cast<char*>(a->d_twpart) + share * kShareUnits);
-        GWL_CUDA(cudaMemsetAsync(R.tw_done, 0, sizeof(int) * kShareUnits, s));
-        GWL_CUDA(launch_time_marg_window(R, s));
-      }
+      if ((rc = launch_window_marg(a, L, s, mixed, share))) return rc;
     } else {
       GWL_CUDA(launch_time_marginalized(L, s));
     }
@@ -631,6 +659,16 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
   if (ordered || L.order) GWL_CUDA(launch_order(L, s));
   if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
   if (a->time_marg && d_out) {
+    // mixed TaylorF2: the whole-FFT kernel marks the points over its error
+    // bound; the windowed float64 kernel recomputes them, split over CTAs
+    const bool marks = precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2 && a->refine_tol > 0 &&
+                       time_marg_window_refine_fits(L);
+    size_t share = 0;
+    a->last_rf_count = nullptr;  // no marks unless set below
+    if (marks) {
+      if ((rc = ensure_window_shares(a, L, s, &share))) return rc;
+      set_window_marks(a, L, s);
+    }
     if (precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_SINEGAUSSIAN) {
       // the mixed sine-Gaussian pass first: its float-float <h|h> partial sums
       // are what the time-marginalised kernel reads
@@ -640,6 +678,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       GWL_CUDA(launch_mixed(P, s));
     }
     GWL_CUDA(launch_time_marginalized(L, s));
+    if (marks && (rc = launch_window_refine(a, L, s, share))) return rc;
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
       a->ev_pending = 1;

@@ -288,6 +288,7 @@ cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
 // memory fits, and the launch (mixed precision: relative binning only).
 bool time_marg_window_fits(const LaunchArgs& a);
 bool time_marg_window_mixed_ready(const LaunchArgs& a);  // the mixed kernel's tables and work space are there
+bool time_marg_window_refine_fits(const LaunchArgs& a);  // the float64 recomputation of marked points fits
 int64_t time_marg_window_slots();                        // work-space slots of the mixed multi-banding kernel
 // bytes per unit of the float64 recomputation's shares (0: the window does not fit)
 size_t time_marg_window_share_bytes(const LaunchArgs& a);

@@ -36,6 +36,14 @@ namespace gwl {
 
 constexpr int kTmThreads = 512;
 constexpr int kTmTwiddleRows = 128;
+// Error model of the mixed TaylorF2 kernel (|dlnL| <= s |dX| over the prior
+// window, s from tm_sensitivity): __sincosf's and the weights' independent
+// per-bin errors and the float32 transform's rounding as ||z||_2 where the
+// outputs are noise, the transform's coherent rounding as |X| at a peak.
+// Measured on tf2_marg_8s (8192 prior draws and loud templates at 20-800 Mpc
+// with |X| up to 3e4): |dX| <= 2e-6 ||z||_2 + 1.3e-7 |X|max.
+constexpr double kTmErrNorm = 2e-6;
+constexpr double kTmErrPeak = 2.5e-7;
 
 // Block-wide reductions over kTmThreads threads in a fixed tree order.
 __device__ double block_max(double v, double* red) {
@@ -148,6 +156,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     const PointRec& r = a.rec[i];
     // ---- A: integrand --------------------------------------------------
     double hh_part = 0.0;
+    float z2 = 0.f;  // mixed TaylorF2: sum of |z_k|^2 over this thread's bins (error bound)
     if constexpr (MIXED) {
       // per-point float32 coefficients, computed once (float64 issues slowly) and shared
       if (threadIdx.x == 0) {
@@ -225,6 +234,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
               zr += gre[d] * er + gim[d] * ei;
               zi += gim[d] * er - gre[d] * ei;
             }
+            z2 += zr * zr + zi * zi;
             // Y[v] += z exp(-2 pi i j v / 16)
 #pragma unroll
             for (int v = 0; v < 16; ++v) {
@@ -608,14 +618,19 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     const int64_t j_lo = s_jr[0], j_hi = s_jr[1];
     // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
     double m = -INFINITY, acc = 0.0;
+    float xmax = 0.f;  // mixed: the largest |X| over this thread's samples (error bound)
     for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
       const double t = tm_sample_time(a, j, L, step, jit);
       double lw;
       if (!tm_log_weight<MIXED>(a, t, lw)) continue;
       const C x = out_at(buf, j);
       double l;
-      if constexpr (MIXED) l = tm_lnl_mixed(a, x.x, x.y, hh, sr, s_tx, s_row);
-      else l = tm_lnl_fp64(a, x.x, x.y, hh, hh_ref, sr);
+      if constexpr (MIXED) {
+        l = tm_lnl_mixed(a, x.x, x.y, hh, sr, s_tx, s_row);
+        xmax = fmaxf(xmax, sqrtf(x.x * x.x + x.y * x.y));
+      } else {
+        l = tm_lnl_fp64(a, x.x, x.y, hh, hh_ref, sr);
+      }
       tm_lse_push<MIXED>(l + lw, m, acc);
     }
     // combine (m, acc) pairs over the block in a fixed order
@@ -626,11 +641,19 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       // near the maximum serves), then sum acc_t exp(m_t - M) in float32; both
       // by xor-shuffles within warps and a fixed-order sum of the 16 warps
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      float mf = (float)m;
+      float mf = (float)m, zz = z2, xm = xmax;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
+      for (int o = 16; o > 0; o >>= 1) {
+        mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
+        zz += __shfl_xor_sync(0xffffffffu, zz, o);
+        xm = fmaxf(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+      }
       float* redf = reinterpret_cast<float*>(reds);
-      if (lane == 0) redf[warp] = mf;
+      if (lane == 0) {
+        redf[warp] = mf;
+        redf[kTmThreads / 32 + warp] = zz;       // error bound: sum of |z|^2 ...
+        redf[2 * (kTmThreads / 32) + warp] = xm;  // ... and the largest |X|
+      }
       __syncthreads();
       float M = redf[0];
       for (int w = 1; w < kTmThreads / 32; ++w) M = fmaxf(M, redf[w]);
@@ -642,9 +665,15 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       if (lane == 0) redf[warp] = sm;
       __syncthreads();
       if (threadIdx.x == 0) {
-        float total = 0.f;
-        for (int w = 0; w < kTmThreads / 32; ++w) total += redf[w];
+        float total = 0.f, zs = 0.f, xp = 0.f;
+        for (int w = 0; w < kTmThreads / 32; ++w) {
+          total += redf[w];
+          zs += redf[kTmThreads / 32 + w];
+          xp = fmaxf(xp, redf[2 * (kTmThreads / 32) + w]);
+        }
         redm[0] = isfinite(M) ? (double)M : -INFINITY;
+        redm[1] = sqrt((double)zs);
+        redm[2] = (double)xp;
         reds[0] = (double)total;
       }
       __syncthreads();
@@ -673,6 +702,15 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       // mixed: the logarithm of the O(1..1e3) sum in float32 (error ~1e-7)
       else lnl = amax + (MIXED ? (double)logf((float)total) : log(total));
       a.out[i] = lnl;
+      if (MIXED && a.model == GWL_MODEL_TAYLORF2 && a.rf_tol > 0 && a.rf_count && a.rf_list && r.valid) {
+        // |dlnL| <= s (kTmErrNorm ||z||_2 + kTmErrPeak max|X|): points over the
+        // tolerance are listed for the float64 recomputation
+        const double err = tm_sensitivity(a, redm[2], sr, s_tx, s_row) * (kTmErrNorm * redm[1] + kTmErrPeak * redm[2]);
+        if (!(err <= a.rf_tol)) {
+          a.rec[i].refine = 1;
+          a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
+        }
+      }
     }
     __syncthreads();
   }

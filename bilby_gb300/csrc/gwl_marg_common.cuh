@@ -241,6 +241,24 @@ __device__ __forceinline__ void tm_lse_push(double l, double& m, double& acc) {
   }
 }
 
+// The largest sensitivity dl_j / d|X_j| of the per-sample lnL over a window
+// whose largest |<d|h>(t_j)| is xpk: 1 for the real part and for ln I0
+// (I1 / I0 < 1); with the distance table sr E[d_ref / d], which grows with |X|
+// (the table is convex in its first argument), so its value at xpk.  It comes
+// from a central difference of the float32 spline row of the point's <h|h>
+// (knots in shared memory; the float64 table's dependent loads would stall the
+// CTA), with a margin for the difference's rounding.  |dlnL| is at most this
+// times the largest error of X over the window.
+__device__ inline double tm_sensitivity(const LaunchArgs& a, double xpk, double sr, const float* s_tx,
+                                        const SplineRowF& row) {
+  if (!a.dist_marg) return 1.0;
+  const float dx = (float)(xpk * sr), del = fmaxf(1e-3f * dx, 1e-2f), lo = fmaxf(dx - del, 0.f);
+  const float up = bicubic_eval_row_f(s_tx, a.nx, a.ny, a.tc_f, a.bbox, dx + del, row);
+  const float dn = bicubic_eval_row_f(s_tx, a.nx, a.ny, a.tc_f, a.bbox, lo, row);
+  const double d = fabs((double)up - (double)dn) / ((double)(dx + del) - (double)lo);
+  return fmin(sr * (1.25 * d + 5e-3), 1e6);  // an undefined difference gives 1e6
+}
+
 // exp(-2 pi i t / L) for t < L / 2 in float64 and float32, one pair of tables
 // per (device, FFT length), kept for the life of the process (gwl_marg.cu).
 struct TwiddleTables {

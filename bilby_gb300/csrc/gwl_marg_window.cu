@@ -42,7 +42,6 @@ namespace gwl {
 
 constexpr int kWinThreads = 512;
 constexpr int kWinWarps = kWinThreads / 32;
-constexpr int kWinMaxLog2Col = 11;  // column transforms of up to 2048 points
 constexpr int kWinOutRows = 1024;   // mixed output twiddles: q = 1024 q1 + q2
 // Error model of the mixed kernel (|dlnL| <= s |dX| at the window's
 // samples): the float32 transform's rounding grows as ||z||_2 where the
@@ -71,9 +70,16 @@ struct WinLayout {
   int bytes;
 };
 
-template <bool MIXED>
+// Columns per pass (the full-grid TaylorF2 source: one, its band being a few
+// hundred bins of short transforms) and the column length's limit.
+template <bool MIXED, int SRC>
 __host__ __device__ constexpr int win_columns() {
-  return MIXED ? 4 : 2;
+  return SRC == 2 ? 1 : (MIXED ? 4 : 2);
+}
+
+template <bool MIXED, int SRC>
+__host__ __device__ constexpr int win_max_log2_col() {
+  return 11;
 }
 
 // radix-2 stages evaluated with the integrand, in registers
@@ -144,13 +150,16 @@ __device__ __forceinline__ void win_pass(C* cols, int cs, int log2n2, int stage,
   }
 }
 
-// MB: multi-banding (else relative binning)
-template <int D, bool MIXED, bool MB>
+// The integrand's source: relative binning, multi-banding, or the TaylorF2
+// model on the full frequency grid.
+constexpr int kSrcRelbin = 0, kSrcMultiband = 1, kSrcTf2 = 2;
+
+template <int D, bool MIXED, int SRC>
 __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     k_tm_window(LaunchArgs a, WinLayout lay, const typename TmTypes<MIXED>::C* twiddle) {
   using C = typename TmTypes<MIXED>::C;
   using R = typename TmTypes<MIXED>::R;
-  constexpr int G = win_columns<MIXED>();
+  constexpr int G = win_columns<MIXED, SRC>();
   constexpr int RB0 = win_first_stages<MIXED>(), RN0 = 1 << RB0;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ C s_w16[16];
@@ -160,6 +169,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
   __shared__ long long s_kb[2];
   __shared__ int s_last;
   __shared__ SplineRowF s_row;
+  __shared__ int s_tband[2];  // full-grid TaylorF2: the point's band
   const int L = (int)a.n_fft, N1 = (int)lay.n1;  // L < 2^30 (checked on the host)
   const int log2n2 = lay.log2n2;
   const int N2 = 1 << log2n2, n2q = N2 >> RB0, cs = win_stride(N2);
@@ -173,6 +183,23 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
   float2* otw_lo = reinterpret_cast<float2*>(smem + lay.off_otw_lo);
   float* s_tx = reinterpret_cast<float*>(smem + lay.off_knots);
   float* s_ty = s_tx + a.nx;
+
+  // Work units.  Evaluation: one per point.  Float64 recomputation of the
+  // points the mixed kernel marked (rf_list[0 .. *rf_count)): P units per
+  // point, unit c taking the column groups c, c + P, ...; each writes its
+  // window sums and <h|h> share to tw_part, and the last of the point's units
+  // to finish adds the P shares in a fixed order and completes the point.
+  int P = 1;
+  int64_t n_units = a.B;
+  if (a.tw_refine_only) {
+    const int64_t cnt = *a.rf_count;
+    const int64_t groups = (N1 + G - 1) / G;
+    // at least four column groups per unit (each unit repeats the per-point set-up)
+    if (cnt > 0) P = (int)std::max<int64_t>(1, std::min<int64_t>(groups / 4, (int64_t)gridDim.x / cnt));
+    if (cnt * P > a.tw_part_units) P = (int)std::max<int64_t>(1, a.tw_part_units / std::max<int64_t>(cnt, 1));
+    n_units = cnt * P;
+  }
+  if ((int64_t)blockIdx.x >= n_units) return;  // no work for this CTA (uniform)
 
   // ---- tables, once per CTA ----------------------------------------------
   for (int e = threadIdx.x; e < N2 - 1; e += blockDim.x) {
@@ -218,22 +245,8 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
 
   const double norm = 4.0 / a.duration;
   const int nE = a.rb_edges, nB = nE - 1;
-  const int k0 = MB ? 0 : (int)a.rb_index[0], k1 = MB ? -1 : (int)a.rb_index[nE - 1];
-  // Work units.  Evaluation: one per point.  Float64 recomputation of the
-  // points the mixed kernel marked (rf_list[0 .. *rf_count)): P units per
-  // point, unit c taking the column groups c, c + P, ...; each writes its
-  // window sums and <h|h> share to tw_part, and the last of the point's units
-  // to finish adds the P shares in a fixed order and completes the point.
-  int P = 1;
-  int64_t n_units = a.B;
-  if (a.tw_refine_only) {
-    const int64_t cnt = *a.rf_count;
-    const int64_t groups = (N1 + G - 1) / G;
-    // at least four column groups per unit (each unit repeats the per-point set-up)
-    if (cnt > 0) P = (int)std::max<int64_t>(1, std::min<int64_t>(groups / 4, (int64_t)gridDim.x / cnt));
-    if (cnt * P > a.tw_part_units) P = (int)std::max<int64_t>(1, a.tw_part_units / std::max<int64_t>(cnt, 1));
-    n_units = cnt * P;
-  }
+  constexpr bool MB = SRC == kSrcMultiband;
+  const int k0 = SRC == kSrcRelbin ? (int)a.rb_index[0] : 0, k1 = SRC == kSrcRelbin ? (int)a.rb_index[nE - 1] : -1;
   for (int64_t unit = blockIdx.x; unit < n_units; unit += gridDim.x) {
     const int64_t slot = unit / P;
     const int part_c = (int)(unit - slot * P);
@@ -263,7 +276,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
     float z2 = 0.f;  // mixed: sum of |z_k|^2 (error bound)
     double2* rat = reinterpret_cast<double2*>(smem + lay.off_rat);  // relative binning: [D][nE]
     float4* coef = reinterpret_cast<float4*>(smem + lay.off_coef);  // mixed: [D][nB] {r0, r1}, then [D][nB] lo(r0)
-    if constexpr (!MB) {
+    if constexpr (SRC == kSrcRelbin) {
       relbin_edge_ratios<D>(a, r, rat);
       __syncthreads();
       if (part_c == 0) hh_part = relbin_hh_part<D>(a, rat);
@@ -372,10 +385,29 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         __syncthreads();
       }
     }
+    if constexpr (SRC == kSrcTf2) {
+      if (threadIdx.x == 32) {
+        s_tband[0] = (int)max(r.k_start, a.k_lo);
+        s_tband[1] = (int)min(min(r.k_end, a.k_hi), (int64_t)L);
+        if (!MIXED && part_c == 0 && L >= a.k_lo && L < a.k_hi) {
+          // the last bin (index L) enters <h|h> only; the transform uses bins 0 .. L - 1
+          double2 hp, hx;
+          const double f = a.freq[L];
+          if (plain_pols(a, r, f, hp, hx)) {
+            for (int d = 0; d < D; ++d) {
+              const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+              hh_part += norm * (sre * sre + sim * sim) * a.inv_psd[d][L];
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
     const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
-    const double u = (MB && !MIXED && tf2) ? cbrt(kPi * r.m_sec) : 0.0;
-    const double lnu = (MB && !MIXED && tf2) ? log(u) : 0.0;
-    const double pu5 = (MB && !MIXED && tf2) ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+    const bool pw = SRC != kSrcRelbin && !MIXED && tf2;  // float64 model from the power tables
+    const double u = pw ? cbrt(kPi * r.m_sec) : 0.0;
+    const double lnu = pw ? log(u) : 0.0;
+    const double pu5 = pw ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
     for (int t = threadIdx.x; t < lay.n_win_max; t += blockDim.x) {
       C z;
       z.x = 0;
@@ -392,7 +424,36 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
       C z;
       z.x = 0;
       z.y = 0;
-      if constexpr (!MB) {
+      if constexpr (SRC == kSrcTf2) {
+        if (k < s_tband[0] || k >= s_tband[1]) return z;
+        if constexpr (!MIXED) {
+          // float64 (base.py:325-330): the model from the per-bin power
+          // table, the detector response with its time shift, h conj(d) / S
+          // (the recomputation of the points the mixed whole-FFT kernel marks)
+          const double f = a.freq[k];
+          double2 hp, hx;
+          if (tf2_pols_tab(a, r, k, f, u, lnu, pu5, hp, hx)) {
+            double zr = 0.0, zi = 0.0, hs = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              const double is = a.inv_psd[d][k];
+              if (is == 0.0) continue;
+              const double sre = hp.x * r.fp[d] + hx.x * r.fx[d], sim = hp.y * r.fp[d] + hx.y * r.fx[d];
+              double sn, cs;
+              sincos(2.0 * kPi * r.dt[d] * f, &sn, &cs);
+              const double hre = sre * cs + sim * sn, him = sim * cs - sre * sn;
+              const double2 dd = reinterpret_cast<const double2*>(a.strain[d])[k];
+              zr += (hre * dd.x + him * dd.y) * is;
+              zi += (him * dd.x - hre * dd.y) * is;
+              hs += (hre * hre + him * him) * is;
+            }
+            z.x = norm * zr;
+            z.y = norm * zi;
+            hh_part += norm * hs;
+          }
+        }
+        return z;
+      } else if constexpr (!MB) {
         if constexpr (MIXED) {
           // float32: ratio r0 + r1 (f - f_b) times the weight 4/T h0 conj(d) / S;
           // no branch around the loads (a clamped index and a zero factor
@@ -482,6 +543,22 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         const int g = bb % G, b = bb / G, n1 = n1_0 + g;
         const int q = log2n2 > RB0 ? (int)bit_reverse((uint32_t)b, log2n2 - RB0) : 0;
         C x[RN0];
+        if constexpr (SRC == kSrcTf2) {
+          // the band is a few hundred of the column's bins: a block with none
+          // of its RN0 elements (N1 N2 / RN0 apart) in it writes zeros
+          const int64_t kmin = (int64_t)n1 + (int64_t)N1 * q, stride = (int64_t)N1 * n2q;
+          const int64_t lo = (int64_t)s_tband[0] - kmin, hi = (int64_t)s_tband[1] - kmin;
+          const int64_t m_lo = lo <= 0 ? 0 : (lo + stride - 1) / stride, m_hi = hi <= 0 ? -1 : (hi - 1) / stride;
+          if (n1 >= N1 || m_lo > min(m_hi, (int64_t)RN0 - 1)) {
+            C* col = cols + g * cs;
+            C zero;
+            zero.x = 0;
+            zero.y = 0;
+#pragma unroll
+            for (int m = 0; m < RN0; ++m) col[win_pad(b * RN0 + m)] = zero;
+            continue;
+          }
+        }
 #pragma unroll
         for (int m = 0; m < RN0; ++m) {
           // register slot m holds element bitrev(m) (decimation in time)
@@ -679,18 +756,9 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
       else lnl = M + log(total);
       a.out[i] = lnl;
       if (MIXED && a.rf_tol > 0 && a.rf_count) {
-        // |dlnL| <= max_j |dl_j| <= s |dX|max, s the largest dl/d|X| over the
-        // window: 1 for the real part and for ln I0 (I1 / I0 < 1); with the
-        // distance table sr E[d_ref / d], which grows with |X| (the table is
-        // convex in its first argument), so its value at the largest |X|
-        double sens = 1.0;
-        if (a.dist_marg) {
-          const double dx = xpk * sr, del = fmax(1e-3 * dx, 1e-3);
-          const double up = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, dx + del, hh_ref);
-          const double dn = bicubic_eval(a.tx, a.nx, a.ty, a.ny, a.tc, a.bbox, fmax(dx - del, 0.0), hh_ref);
-          sens = fmin(1.25 * sr * fabs(up - dn) / (dx + del - fmax(dx - del, 0.0)) + 1e-6, 1e6);
-        }
-        const double err = (kWinErrNorm + (MB ? kWinErrTerm : 0.0)) * znorm + kWinErrPeak * xpk;
+        // |dlnL| <= max_j |dl_j| <= s |dX|max
+        const double sens = tm_sensitivity(a, xpk, sr, s_tx, s_row);
+        const double err = (kWinErrNorm + (SRC != kSrcRelbin ? kWinErrTerm : 0.0)) * znorm + kWinErrPeak * xpk;
         if (!(sens * err <= a.rf_tol)) {
           a.rec[i].refine = 1;
           a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
@@ -702,12 +770,12 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
 }
 
 // Shared-memory layout for n_det detectors; false when it does not fit.
-template <bool MIXED>
+template <bool MIXED, int SRC>
 bool win_layout(const LaunchArgs& a, WinLayout* lay) {
   using C = typename TmTypes<MIXED>::C;
   int m_odd = 0, log2N = 0;
   if (!fft_length_supported(a.n_fft, &m_odd, &log2N) || a.n_fft >= ((int64_t)1 << 30)) return false;
-  const int log2n2 = std::min(log2N, kWinMaxLog2Col);
+  const int log2n2 = std::min(log2N, win_max_log2_col<MIXED, SRC>());
   const int64_t n2 = (int64_t)1 << log2n2;
   lay->log2n2 = log2n2;
   lay->n1 = a.n_fft >> log2n2;
@@ -717,7 +785,7 @@ bool win_layout(const LaunchArgs& a, WinLayout* lay) {
   lay->n_win_max = (int)std::ceil(width) + 10;
   lay->n_otw_hi = (int)((a.n_fft / 2 + kWinOutRows - 1) / kWinOutRows);
   const auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
-  size_t off = up16((size_t)win_columns<MIXED>() * (size_t)win_stride((int)n2) * sizeof(C));
+  size_t off = up16((size_t)win_columns<MIXED, SRC>() * (size_t)win_stride((int)n2) * sizeof(C));
   lay->off_ctw = (int)off;
   off = up16(off + (size_t)(n2 - 1) * sizeof(C));
   lay->off_otw_hi = (int)off;
@@ -740,10 +808,10 @@ bool win_layout(const LaunchArgs& a, WinLayout* lay) {
   return off <= (size_t)200 * 1024;
 }
 
-template <int D, bool MIXED, bool MB>
+template <int D, bool MIXED, int SRC>
 cudaError_t launch_win_d(const LaunchArgs& a, const WinLayout& lay, const TwiddleTables& tw, cudaStream_t s) {
   cudaError_t e =
-      cudaFuncSetAttribute(k_tm_window<D, MIXED, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes);
+      cudaFuncSetAttribute(k_tm_window<D, MIXED, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -754,30 +822,49 @@ cudaError_t launch_win_d(const LaunchArgs& a, const WinLayout& lay, const Twiddl
   const typename TmTypes<MIXED>::C* twp;
   if constexpr (MIXED) twp = tw.d32;
   else twp = tw.d64;
-  k_tm_window<D, MIXED, MB><<<(unsigned)grid, kWinThreads, lay.bytes, s>>>(a, lay, twp);
+  k_tm_window<D, MIXED, SRC><<<(unsigned)grid, kWinThreads, lay.bytes, s>>>(a, lay, twp);
   return cudaGetLastError();
+}
+
+template <bool MIXED, int SRC>
+cudaError_t launch_win_src(const LaunchArgs& a, const WinLayout& lay, const TwiddleTables& tw, cudaStream_t s) {
+  switch (a.n_det) {
+    case 1: return launch_win_d<1, MIXED, SRC>(a, lay, tw, s);
+    case 2: return launch_win_d<2, MIXED, SRC>(a, lay, tw, s);
+    case 3: return launch_win_d<3, MIXED, SRC>(a, lay, tw, s);
+    default: return launch_win_d<4, MIXED, SRC>(a, lay, tw, s);
+  }
+}
+
+template <bool MIXED, int SRC>
+cudaError_t launch_win_layout(const LaunchArgs& a, cudaStream_t s) {
+  WinLayout lay;
+  if (!win_layout<MIXED, SRC>(a, &lay)) return cudaErrorInvalidValue;  // checked on the host first
+  TwiddleTables tw;
+  cudaError_t e = twiddles_for(a.n_fft, &tw);
+  if (e != cudaSuccess) return e;
+  return launch_win_src<MIXED, SRC>(a, lay, tw, s);
+}
+
+int win_source(const LaunchArgs& a) { return a.relbin ? kSrcRelbin : (a.mb_tm ? kSrcMultiband : kSrcTf2); }
+
+template <bool MIXED>
+bool win_layout_any(const LaunchArgs& a, WinLayout* lay) {
+  switch (win_source(a)) {
+    case kSrcRelbin: return win_layout<MIXED, kSrcRelbin>(a, lay);
+    case kSrcMultiband: return win_layout<MIXED, kSrcMultiband>(a, lay);
+    default: return !MIXED && win_layout<false, kSrcTf2>(a, lay);
+  }
 }
 
 template <bool MIXED>
 cudaError_t launch_win(const LaunchArgs& a, cudaStream_t s) {
-  WinLayout lay;
-  if (!win_layout<MIXED>(a, &lay)) return cudaErrorInvalidValue;  // checked on the host first
-  TwiddleTables tw;
-  cudaError_t e = twiddles_for(a.n_fft, &tw);
-  if (e != cudaSuccess) return e;
-  if (a.mb_tm) {
-    switch (a.n_det) {
-      case 1: return launch_win_d<1, MIXED, true>(a, lay, tw, s);
-      case 2: return launch_win_d<2, MIXED, true>(a, lay, tw, s);
-      case 3: return launch_win_d<3, MIXED, true>(a, lay, tw, s);
-      default: return launch_win_d<4, MIXED, true>(a, lay, tw, s);
-    }
-  }
-  switch (a.n_det) {
-    case 1: return launch_win_d<1, MIXED, false>(a, lay, tw, s);
-    case 2: return launch_win_d<2, MIXED, false>(a, lay, tw, s);
-    case 3: return launch_win_d<3, MIXED, false>(a, lay, tw, s);
-    default: return launch_win_d<4, MIXED, false>(a, lay, tw, s);
+  switch (win_source(a)) {
+    case kSrcRelbin: return launch_win_layout<MIXED, kSrcRelbin>(a, s);
+    case kSrcMultiband: return launch_win_layout<MIXED, kSrcMultiband>(a, s);
+    default:
+      if constexpr (MIXED) return cudaErrorInvalidValue;  // float64 only
+      else return launch_win_layout<false, kSrcTf2>(a, s);
   }
 }
 
@@ -799,14 +886,24 @@ size_t time_marg_window_share_bytes(const LaunchArgs& a) {
   LaunchArgs F = a;
   F.precision = GWL_PRECISION_FP64;
   WinLayout lay;
-  if (!win_layout<false>(F, &lay)) return 0;
+  if (!win_layout_any<false>(F, &lay)) return 0;
   return (size_t)(lay.n_win_max + 1) * sizeof(double2);
 }
 
+bool time_marg_window_refine_fits(const LaunchArgs& a) {
+  if (a.tm_series || a.roq) return false;
+  LaunchArgs F = a;
+  F.precision = GWL_PRECISION_FP64;
+  WinLayout lay;
+  return win_layout_any<false>(F, &lay);
+}
+
 bool time_marg_window_fits(const LaunchArgs& a) {
+  // relative binning and multi-banding, either precision (the full-grid
+  // TaylorF2 source serves only the recomputation of marked points)
   if (!(a.relbin || a.mb_tm) || a.tm_series) return false;
   WinLayout lay;
-  return a.precision == GWL_PRECISION_MIXED ? win_layout<true>(a, &lay) : win_layout<false>(a, &lay);
+  return a.precision == GWL_PRECISION_MIXED ? win_layout_any<true>(a, &lay) : win_layout_any<false>(a, &lay);
 }
 
 cudaError_t launch_time_marg_window(const LaunchArgs& a, cudaStream_t s) {

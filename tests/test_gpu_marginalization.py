@@ -163,6 +163,38 @@ def test_mixed_time_marginalized_matches_float64_fft16384(gpu, tmp_path, combo):
     assert np.all(np.abs(mixed - fp64) <= 1e-3), np.abs(mixed - fp64).max()
 
 
+@pytest.mark.parametrize("combo", ["t", "tpd"])
+def test_mixed_time_marginalized_error_control_on_loud_templates(gpu, tmp_path, combo):
+    """Loud templates (the injection's masses and sky position at 20-800 Mpc,
+    |<d|h>| up to 3e4), where the float32 transform alone errs by up to 6e-3:
+    the mixed kernel marks the points over its error bound, the windowed
+    float64 kernel recomputes them (split over CTAs), and every result is
+    within 1e-3 of the float64 kernel's; with the control off the marks
+    vanish."""
+    w = WORKLOADS["tf2_marg_8s"]
+    like, priors = make_likelihood(w, combo, "mixed", tmp_path / "table.npz")
+    rng = np.random.default_rng(73)
+    n = 1024
+    p = {k: np.full(n, float(v)) for k, v in w.injection.items()}
+    p["luminosity_distance"] = rng.uniform(20.0, 800.0, n)
+    p["theta_jn"] = rng.uniform(0.0, np.pi, n)
+    p["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+    p["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, n)
+    if "p" in combo:
+        p["phase"] = np.zeros(n)
+    if "d" in combo:
+        p["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+    mixed = like.log_likelihood_ratio_batch(p, precision="mixed")
+    refined = like.analysis.last_refined()
+    fp64 = like.log_likelihood_ratio_batch(p, precision="fp64")
+    assert np.all(np.abs(mixed - fp64) <= 1e-3), np.abs(mixed - fp64).max()
+    if combo == "t":
+        assert refined > 0
+    like.analysis.refinement_tolerance = 0.0
+    like.log_likelihood_ratio_batch(p, precision="mixed")
+    assert like.analysis.last_refined() == 0
+
+
 def test_mixed_time_marginalized_sine_gaussian(gpu, tmp_path):
     """Time marginalisation of the sine-Gaussian in mixed precision (the
     full-band integrand, the padded buffer, radix-16 passes and the pruned last
