@@ -63,6 +63,7 @@ struct gwl_analysis {
   double* inv_psd[kMaxDet] = {};
   float2* w[kMaxDet] = {};
   uint2* wp[kMaxDet] = {};  // TaylorF2: the same weights in polar form {float |w|, arg(w) as 0.32 fixed cycles}
+  uint4* wq[kMaxDet] = {};  // TaylorF2 fast kernel: bin pairs {|w|, |w|, angle or angle increment} (LaunchArgs::wq)
   float* v[kMaxDet] = {};
   float* v_lo[kMaxDet] = {};  // sine-Gaussian: low words of the scaled inverse PSD
   double* hh_prefix[kMaxDet] = {};
@@ -304,6 +305,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
     L.inv_psd[d] = a->inv_psd[d];
     L.w[d] = a->w[d];
     L.wp[d] = a->wp[d];
+    L.wq[d] = a->wq[d];
     L.v[d] = a->v[d];
     L.v_lo[d] = a->v_lo[d];
     L.hh_prefix[d] = a->hh_prefix[d];
@@ -984,6 +986,17 @@ int gwl_analysis_create(const gwl_analysis_desc* desc, gwl_analysis** out) {
           wpol[k] = make_uint2(mb, th);
         }
         if ((rc = upload(a, &a->wp[d], wpol))) goto fail;
+        // the fast kernel's pairs: magnitudes side by side, then the angle at
+        // the first bin of each 8-bin block and the increment over the
+        // previous bin elsewhere (P is a multiple of 16)
+        std::vector<uint4> wpair(P / 2);
+        for (int64_t q = 0; q < P / 2; ++q) {
+          const int64_t k = 2 * q;
+          const uint32_t tau0 = (k % 8 == 0) ? wpol[k].y : wpol[k].y - wpol[k - 1].y;
+          const uint32_t tau1 = wpol[k + 1].y - wpol[k].y;
+          wpair[q] = make_uint4(wpol[k].x, wpol[k + 1].x, tau0, tau1);
+        }
+        if ((rc = upload(a, &a->wq[d], wpair))) goto fail;
       }
       if (a->model == GWL_MODEL_SINEGAUSSIAN) {
         // float-float inverse PSD for the float-float <h|h> of the mixed kernel

@@ -90,6 +90,9 @@ struct LaunchArgs {
   const double* inv_psd[kMaxDet];       // [n_pad] mask / S
   const float2* w[kMaxDet];             // [n_pad] mixed data weights (scaled)
   const uint2* wp[kMaxDet];             // [n_pad] TaylorF2: polar weights {float |w| bits, arg(w) 0.32 cycles}
+  const uint4* wq[kMaxDet];             // [n_pad / 2] TaylorF2 fast kernel: per bin pair {|w| even, |w| odd,
+                                        // tau even, tau odd}, tau = arg(w) at bins k % 8 == 0, else
+                                        // arg(w_k) - arg(w_{k-1}) (0.32 cycles, wrapping)
   const float* v[kMaxDet];              // [n_pad] mixed inverse PSD (scaled)
   const float* v_lo[kMaxDet];           // [n_pad] sine-Gaussian: low words of the scaled inverse PSD (v + v_lo)
   const double* hh_prefix[kMaxDet];     // [n_bins + 1] TaylorF2 <h|h> prefix sums

@@ -438,50 +438,38 @@ __device__ __forceinline__ float fixed_phase_cycles(uint32_t k, uint32_t xlo, ui
 }
 
 constexpr int kFlush = 64;  // bins summed in float32 before folding into float64 (sine-Gaussian)
-constexpr int kFold = 8;    // bins summed in float32 before folding into float-float (TaylorF2)
+constexpr int kFold = 8;    // bins summed in float32 before folding into float-float (direct TaylorF2 chunks)
 
 // TaylorF2, mixed precision.
 //
 // Phase: about anchor bins k_a (every J bins, J from the Taylor-remainder
-// bound below) the phase in cycles Phi(k_a + j) = sum_n A_n j^n is a degree-6
-// polynomial whose coefficients A_n = sum_b c_b T_n,b(k_a) come from the
-// per-analysis Taylor tables of the basis functions (orders 0..3 in
-// float-float).  Its forward differences are converted to 0.64 fixed point
-// (cycles modulo one) and the phase is stepped bin by bin with wrapping
-// 64-bit integer adds, which are exact: no rounding error accumulates along
-// the interval.  The detector time shift k * frac(dt df) is another exact
-// 0.64 fixed-point sequence.  Only the final sin/cos and the complex
-// multiply-accumulate with the weights w = f^(-7/6) d / S are float32.
+// bound below) the phase in cycles Phi(k_a + j) = sum_n A_n j^n is a
+// polynomial of degree 4 to 6 whose coefficients A_n = sum_b c_b T_n,b(k_a)
+// come from the per-analysis Taylor tables of the basis functions (orders
+// 0..3 in float-float).  It is split into a quadratic part Q(j) = A_0 + A_1 j
+// + A_2 j^2 plus detector 0's time shift, kept exactly in 0.64 fixed point
+// (cycles modulo one), and the rest C(j) = sum_{n >= 3} A_n j^n, a small
+// fraction of a cycle over the interval, evaluated in float32.  Q is stepped
+// once per 8-bin block with wrapping 64-bit integer adds, which are exact:
+// its value and first difference at the block start, step-8 forward
+// differences.  Inside a block the phase of bin i is the 32-bit top word
+// top(i) = top(Q) + i top(dQ) (truncation error below 8 units of 2^-32
+// cycle) plus the float32 remainder C(i, 2) 2 A_2 + C(j) (radians).  The
+// detector time shifts relative to detector 0 are exact 0.64 sequences
+// stepped per block, and their 32-bit slope per bin is added inside it.
+// The weight table of this kernel holds per bin pair {|w| even, |w| odd,
+// tau even, tau odd}, tau the weight angle arg(w) at a block's first bin and
+// the angle increment arg(w_k) - arg(w_{k-1}) elsewhere, so that each bin's
+// 32-bit angle is one three-input add of the previous bin's.  Two bins run
+// as one packed float pair (f32x2 multiply-adds); only the hardware cosine
+// and the packed multiply-accumulate with the weights w = f^(-7/6) d / S are
+// float32.  The even and odd bins' float32 partial sums (8 terms each) are
+// folded every 16 bins into float-float accumulators.
 //
 // Work split (split-K): CTA (tile, g) holds 128 points and walks chunks
 // g, g + G, ... of 512 bins; each chunk's weights come in by 1-D bulk async
 // copies into a double-buffered shared-memory stage.  One partial sum per
 // (g, detector, point) is written, point fastest.
-
-// One bin of the anchored phase recurrence: detector d's phase (top 32 bits
-// of the 0.64 fixed-point cycle count) is base + lh[d] (lh[0] = 0); with the
-// polar weight w = |w| e^{i theta} (theta in 0.32 fixed cycles) the terms are
-// Re w e^{i phase} = |w| cos(phase + theta) and Im = |w| sin(phase + theta).
-// w points at the bin's weight of detector 0; detector d's weight is
-// kChunkMixed entries further per detector.
-template <int D, bool CPLX>
-__device__ __forceinline__ void tf2_bin(uint32_t base, const uint32_t* lh, const uint2* w, float* are, float* aim) {
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const uint2 wv = w[d * kChunkMixed];
-    const uint32_t top = (d == 0 ? base : base + lh[d]) + wv.y;
-    const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);  // 2 pi 2^-32
-    const float mag = __uint_as_float(wv.x);
-    if (CPLX) {
-      float sn, cs;
-      __sincosf(ph, &sn, &cs);
-      are[d] = __fmaf_rn(mag, cs, are[d]);
-      aim[d] = __fmaf_rn(mag, sn, aim[d]);
-    } else {
-      are[d] = __fmaf_rn(mag, __cosf(ph), are[d]);
-    }
-  }
-}
 
 // Accurate variant, for the points the prologue marks (LaunchArgs::rf_tol).
 // The hardware cosine's error is a smooth function of the angle, so it adds up
@@ -518,32 +506,63 @@ __device__ __forceinline__ void acc_ff(float& hi, float& lo, float m, float c_hi
   lo = __fmaf_rn(m, c_lo, lo);
 }
 
-// A whole 8-bin block of the anchored recurrence.  DEG is the degree of the
-// phase polynomial about the anchor: with DEG < 6 the higher differences are
-// zero, so the adds skipped here would only add zero.
-template <int D, bool CPLX, int DEG>
-__device__ __forceinline__ void tf2_block8(uint64_t& D0, uint64_t& D1, uint64_t& D2, uint64_t& D3, uint64_t& D4,
-                                           uint64_t& D5, uint64_t D6, uint32_t* lh, const uint32_t* r32,
-                                           const uint2* w, float* are, float* aim) {
+// One 8-bin block of the anchored walk, two bins per packed pair.  top[d]:
+// detector d's 32-bit phase at the block start without the weight angle (on
+// return: at the block's last bin, with it); sl[d]: its slope per bin.  wq:
+// detector 0's four bin pairs of the block in the stage (detector d is
+// kChunkMixed / 2 pairs further per detector).  jj: (j, j + 1) of the first
+// pair relative to the anchor (advanced by 8).  A3..A6: the cubic and higher
+// Taylor coefficients in radians (both lanes equal; A5 = A6 = 0 below degree
+// 5), q1..q3: the local quadratic remainder C(i, 2) 2 A_2 of pairs 1..3.
+// MASK: bins outside [lo, hi) contribute nothing (band edges).
+template <int D, bool CPLX, bool HI, bool MASK>
+__device__ __forceinline__ void tf2_block(uint32_t* top, const uint32_t* sl, const uint4* wq, float2& jj,
+                                          float2 A3, float2 A4, float2 A5, float2 A6, float2 q1, float2 q2,
+                                          float2 q3, int lo, int hi, float2* acc, float2* acci) {
+  const float2 cc = make_float2(1.4629180792671596e-09f, 1.4629180792671596e-09f);  // 2 pi 2^-32
+  const float2 two = make_float2(2.f, 2.f);
 #pragma unroll
-  for (int j = 0; j < kFold; ++j) {
-    tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + j, are, aim);
+  for (int p = 0; p < 4; ++p) {
+    float2 t = HI ? fma2(fma2(A6, jj, A5), jj, A4) : A4;
+    t = fma2(t, jj, A3);
+    float2 rq = mul2(mul2(t, mul2(jj, jj)), jj);
+    if (p == 1) rq = add2(rq, q1);
+    if (p == 2) rq = add2(rq, q2);
+    if (p == 3) rq = add2(rq, q3);
+    jj = add2(jj, two);
 #pragma unroll
-    for (int d = 1; d < D; ++d) lh[d] += r32[d];
-    D0 += D1; D1 += D2; D2 += D3; D3 += D4;
-    if (DEG >= 5) D4 += D5;
-    if (DEG >= 6) D5 += D6;
+    for (int d = 0; d < D; ++d) {
+      const uint4 q = wq[d * (kChunkMixed / 2) + p];
+      const uint32_t ta = p == 0 ? top[d] + q.z : top[d] + sl[d] + q.z;
+      const uint32_t tb = ta + sl[d] + q.w;
+      top[d] = tb;
+      const float2 ph = fma2(make_float2(__int2float_rn((int)ta), __int2float_rn((int)tb)), cc, rq);
+      float2 mag = make_float2(__uint_as_float(q.x), __uint_as_float(q.y));
+      if (MASK) {
+        mag.x = (2 * p >= lo && 2 * p < hi) ? mag.x : 0.f;
+        mag.y = (2 * p + 1 >= lo && 2 * p + 1 < hi) ? mag.y : 0.f;
+      }
+      if (CPLX) {
+        float s0, c0, s1, c1;
+        __sincosf(ph.x, &s0, &c0);
+        __sincosf(ph.y, &s1, &c1);
+        acc[d] = fma2(mag, make_float2(c0, c1), acc[d]);
+        acci[d] = fma2(mag, make_float2(s0, s1), acci[d]);
+      } else {
+        acc[d] = fma2(mag, make_float2(__cosf(ph.x), __cosf(ph.y)), acc[d]);
+      }
+    }
   }
 }
 
 // A chunk where no anchor interval meets the Taylor bound: the phase of every
 // bin in float-float from the per-bin basis table (sum_b c_b phi_b(f_k)),
-// the time shift exact in 0.64 fixed point.
+// the time shift exact in 0.64 fixed point; the weights from the plain polar
+// table in global memory.
 template <int D, bool CPLX>
-__device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const uint2* w, int64_t k0, int64_t ks, int jlast,
+__device__ __forceinline__ void direct_chunk(const LaunchArgs& a, int64_t k0, int64_t ks, int jlast,
                                              const float* ch, const float* cl, const uint64_t* X, const uint64_t* Q,
                                              float* ahi, float* alo, float* bhi, float* blo) {
-  constexpr int CH = kChunkMixed;
   for (int jb = 0; jb < jlast; jb += kFold) {
     float are[D], aim[D];
 #pragma unroll
@@ -563,7 +582,7 @@ __device__ __forceinline__ void direct_chunk(const LaunchArgs& a, const uint2* w
       const uint32_t bu = (uint32_t)((to_fixed(s_hi, s_lo) + 0x80000000ull) >> 32);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        const uint2 wv = w[d * CH + j];
+        const uint2 wv = __ldg(a.wp[d] + k);
         const uint32_t top = bu + (uint32_t)(((uint64_t)k * X[d] + Q[d]) >> 32) + wv.y;
         const float ph = __fmul_rn(__int2float_rn((int)top), 1.4629180792671596e-09f);
         float sn, cs;
@@ -610,25 +629,17 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
   const int64_t c_end = min(a.n_chunks, (kmax - a.k_base + CH - 1) / CH);
   const int64_t nit = c_end > g ? (c_end - g + G - 1) / G : 0;
 
-  float ch[kNumBasis + 1], cl[kNumBasis + 1];
-  uint64_t X[D];
+  // the point's record: basis coefficients, time shifts and offsets are read
+  // from it where they are needed (anchor set-ups), not held in registers
+  const PointRec* rp = have ? a.rec + i : a.rec;
   float c0 = 0.f;
   // constant phase offset of detector d (real-part kernel), read when needed
   const auto qoff = [&](int d) -> uint64_t {
     if (CPLX) return 0;
-    return ((uint64_t)a.rec[i].qfix[d][1] << 32) | a.rec[i].qfix[d][0];
+    return ((uint64_t)rp->qfix[d][1] << 32) | rp->qfix[d][0];
   };
-  if (have && valid) {
-    const PointRec& r = a.rec[i];
-#pragma unroll
-    for (int b = 0; b <= kNumBasis; ++b) {
-      ch[b] = r.c_hi[b];
-      cl[b] = r.c_lo[b];
-    }
-#pragma unroll
-    for (int d = 0; d < D; ++d) X[d] = ((uint64_t)r.xfix[d][1] << 32) | r.xfix[d][0];
-    c0 = fabsf(r.c_hi[0]);
-  }
+  const auto xfix = [&](int d) -> uint64_t { return ((uint64_t)rp->xfix[d][1] << 32) | rp->xfix[d][0]; };
+  if (have && valid) c0 = fabsf(rp->c_hi[0]);
   double tre[D], tim[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) tre[d] = tim[d] = 0.0;
@@ -641,7 +652,7 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&bar[s0], stage_bytes);
 #pragma unroll
-    for (int d = 0; d < D; ++d) bulk_g2s(s_w + s0 * D * CH + d * CH, a.wp[d] + k0, CH * 8, &bar[s0]);
+    for (int d = 0; d < D; ++d) bulk_g2s(s_w + s0 * D * CH + d * CH, a.wq[d] + k0 / 2, CH * 8, &bar[s0]);
   }
   int64_t done = 0;
   for (int64_t it = 0; it < nit; ++it) {
@@ -655,7 +666,7 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
       uint2* dst = s_w + (s ^ 1) * D * CH;
       mbar_expect_tx(&bar[s ^ 1], stage_bytes);
 #pragma unroll
-      for (int d = 0; d < D; ++d) bulk_g2s(dst + d * CH, a.wp[d] + k1, CH * 8, &bar[s ^ 1]);
+      for (int d = 0; d < D; ++d) bulk_g2s(dst + d * CH, a.wq[d] + k1 / 2, CH * 8, &bar[s ^ 1]);
     }
     const bool arrived = mbar_wait_bounded(&bar[s], (uint32_t)((itg >> 1) & 1), a.status, kWaitLimit);
     done = it + 1;
@@ -667,82 +678,126 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
       // point never depends on the other points of the batch
       const int J = anchor_interval(c0 * __powf((float)k0 * (float)a.step, -5.0f / 3.0f),
                                     (float)max(k0, (int64_t)8));
-      uint64_t D0 = 0, D1 = 0, D2 = 0, D3 = 0, D4 = 0, D5 = 0, D6 = 0;
       const int jlast = (int)min((int64_t)CH, ke - k0);
-      // 8-bin float32 partial sums folded into float-float accumulators
+      // float32 partial sums folded into float-float accumulators
       float ahi[D], alo[D], bhi[D], blo[D];
 #pragma unroll
       for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
       if (J == 0) {
-        uint64_t Q[D];
+        float ch[kNumBasis + 1], cl[kNumBasis + 1];
 #pragma unroll
-        for (int d = 0; d < D; ++d) Q[d] = qoff(d);
-        direct_chunk<D, CPLX>(a, w, k0, ks, jlast, ch, cl, X, Q, ahi, alo, bhi, blo);
+        for (int b = 0; b <= kNumBasis; ++b) {
+          ch[b] = rp->c_hi[b];
+          cl[b] = rp->c_lo[b];
+        }
+        uint64_t X[D], Q[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          X[d] = xfix(d);
+          Q[d] = qoff(d);
+        }
+        direct_chunk<D, CPLX>(a, k0, ks, jlast, ch, cl, X, Q, ahi, alo, bhi, blo);
       } else {
-        // detector 0's time shift rides in the phase recurrence (a linear
-        // term: D0 += k X0, D1 += X0); detector d > 0 adds its shift relative
-        // to detector 0, R_d = X_d - X_0, whose top 32 bits are taken exactly
-        // at the start of every 8-bin block and stepped in 32 bits inside it
-        // (error at most 4.5 * 2^-32 cycle)
-        const uint64_t X0 = X[0];
-        uint64_t R[D], L64[D];
+        // detector 0's time shift and constant offset ride in the exact
+        // quadratic part (a linear term: Q(j) += (k + j) X0 + q0); detector
+        // d > 0 adds its shift relative to detector 0, R_d = X_d - X_0, as an
+        // exact 0.64 sequence L_d stepped per block, whose top word (rounded)
+        // starts the block and whose rounded top word r32 is its slope per bin
+        // (error at most 4.5 * 2^-32 cycle).  The +2^31 offsets make the top
+        // words of E0, F0 and L_d rounded rather than truncated.
+        uint64_t R8[D], L64[D];
         uint32_t r32[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          R[d] = X[d] - X0;
-          r32[d] = (uint32_t)((R[d] + 0x80000000ull) >> 32);
+          const uint64_t Rd = xfix(d) - xfix(0);
+          r32[d] = (uint32_t)((Rd + 0x80000000ull) >> 32);
+          R8[d] = Rd * 8ull;
           L64[d] = 0;
         }
-        int deg = 6;
-        for (int jb = 0; jb < jlast; jb += kFold) {
+        // E0, E1, E2: Q at the block start and its step-8 differences; F0, F1:
+        // dQ = Q(j + 1) - Q(j) at the block start and its step-8 difference
+        uint64_t E0 = 0, E1 = 0, E2 = 0, F0 = 0, F1 = 0;
+        const float2 zero2 = make_float2(0.f, 0.f);
+        float2 A3 = zero2, A4 = zero2, A5 = zero2, A6 = zero2, q1 = zero2, q2 = zero2, q3 = zero2, jj = zero2;
+        bool hi_deg = false;
+        float2 acc[D], acci[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) acc[d] = acci[d] = zero2;
+        const uint4* w4 = reinterpret_cast<const uint4*>(w);
+        for (int jb = 0; jb < jlast; jb += 8) {
           const int64_t k = k0 + jb;
           if ((jb & (J - 1)) == 0) {
-            deg = anchor_degree(c0 * __powf((float)k * (float)a.step, -5.0f / 3.0f), (float)J / (float)k);
-            // Taylor coefficients of the phase about k (cycles per bin), truncated at degree deg
-            uint64_t Dn[kAnchorOrders];
-            anchor_differences(a.anchors, k, ch, cl, deg, Dn);
-            const uint64_t q0 = qoff(0);
-            D0 = Dn[0] + (uint64_t)k * X0 + q0;
-            D1 = Dn[1] + X0;
-            D2 = Dn[2];
-            D3 = Dn[3];
-            D4 = Dn[4];
-            D5 = Dn[5];
-            D6 = Dn[6];
+            const int deg = anchor_degree(c0 * __powf((float)k * (float)a.step, -5.0f / 3.0f), (float)J / (float)k);
+            AnchorTaylor t;
+            anchor_taylor(a.anchors, k, rp->c_hi, rp->c_lo, t);
+            const uint64_t q0 = qoff(0), X0 = xfix(0);
+            // Q(j) = A0 + A1 j + A2 j^2: Delta_8 Q(0) = 8 A1 + 64 A2, Delta_8^2 Q = 128 A2,
+            // dQ(0) = A1 + A2, Delta_8 dQ = 16 A2 (scalings by powers of two are exact)
+            float eh = 8.f * t.h[1], el = 8.f * t.l[1];
+            ff_add(eh, el, 64.f * t.h[2], 64.f * t.l[2]);
+            float fh = t.h[1], fl = t.l[1];
+            ff_add(fh, fl, t.h[2], t.l[2]);
+            E0 = to_fixed(t.h[0], t.l[0]) + (uint64_t)k * X0 + q0 + 0x80000000ull;
+            E1 = to_fixed(eh, el) + 8ull * X0;
+            E2 = to_fixed(128.f * t.h[2], 128.f * t.l[2]);
+            F0 = to_fixed(fh, fl) + X0 + 0x80000000ull;
+            F1 = to_fixed(16.f * t.h[2], 16.f * t.l[2]);
 #pragma unroll
-            for (int d = 1; d < D; ++d) L64[d] = (uint64_t)k * R[d] + (qoff(d) - q0);
+            for (int d = 1; d < D; ++d) L64[d] = (uint64_t)k * (xfix(d) - X0) + (qoff(d) - q0) + 0x80000000ull;
+            // C(j) = j^3 (A3 + j (A4 + j (A5 + j A6))) in radians, truncated at degree deg
+            const float tp = 6.283185307179586f;
+            const float a3 = __fmul_rn(__fadd_rn(t.h[3], t.l[3]), tp), a4 = __fmul_rn(t.f[0], tp);
+            const float a5 = deg >= 5 ? __fmul_rn(t.f[1], tp) : 0.f, a6 = deg >= 6 ? __fmul_rn(t.f[2], tp) : 0.f;
+            A3 = make_float2(a3, a3);
+            A4 = make_float2(a4, a4);
+            A5 = make_float2(a5, a5);
+            A6 = make_float2(a6, a6);
+            hi_deg = deg > 4;
+            // local quadratic remainder Q(jb + i) - Q(jb) - i dQ(jb) = C(i, 2) 2 A2, radians
+            const float a2 = __fmul_rn(2.f * t.h[2], tp);
+            q1 = make_float2(a2, 3.f * a2);
+            q2 = make_float2(6.f * a2, 10.f * a2);
+            q3 = make_float2(15.f * a2, 21.f * a2);
+            jj = make_float2(0.f, 1.f);
           }
-          uint32_t lh[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) lh[d] = (uint32_t)(L64[d] >> 32);
-          float are[D], aim[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) are[d] = aim[d] = 0.f;
-          if (jb + kFold <= jlast && k >= ks) {
-            // a whole block inside the band
-            if (deg == 4) {
-              tf2_block8<D, CPLX, 4>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
-            } else if (deg == 5) {
-              tf2_block8<D, CPLX, 5>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
-            } else {
-              tf2_block8<D, CPLX, 6>(D0, D1, D2, D3, D4, D5, D6, lh, r32, w + jb, are, aim);
-            }
-          } else {
-            const int je = min(jb + kFold, jlast);
-            for (int j = jb; j < je; ++j) {
-              if (k0 + j >= ks) tf2_bin<D, CPLX>((uint32_t)(D0 >> 32), lh, w + j, are, aim);
-#pragma unroll
-              for (int d = 1; d < D; ++d) lh[d] += r32[d];
-              D0 += D1; D1 += D2; D2 += D3; D3 += D4; D4 += D5; D5 += D6;
-            }
-          }
-#pragma unroll
-          for (int d = 1; d < D; ++d) L64[d] += R[d] * (uint64_t)kFold;
+          uint32_t top[D], sl[D];
+          const uint32_t e0 = (uint32_t)(E0 >> 32), f0 = (uint32_t)(F0 >> 32);
 #pragma unroll
           for (int d = 0; d < D; ++d) {
-            two_sum_acc(ahi[d], alo[d], are[d]);
-            if (CPLX) two_sum_acc(bhi[d], blo[d], aim[d]);
+            top[d] = d == 0 ? e0 : e0 + (uint32_t)(L64[d] >> 32);
+            sl[d] = d == 0 ? f0 : f0 + r32[d];
           }
+          const uint4* wq = w4 + (jb >> 1);
+          if (jb + 8 <= jlast && k >= ks) {
+            // a whole block inside the band
+            if (hi_deg) {
+              tf2_block<D, CPLX, true, false>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, 0, 8, acc, acci);
+            } else {
+              tf2_block<D, CPLX, false, false>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, 0, 8, acc, acci);
+            }
+          } else {
+            const int lo = (int)max((int64_t)0, ks - k), hi = min(8, jlast - jb);
+            tf2_block<D, CPLX, true, true>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, lo, hi, acc, acci);
+          }
+          E0 += E1;
+          E1 += E2;
+          F0 += F1;
+#pragma unroll
+          for (int d = 1; d < D; ++d) L64[d] += R8[d];
+          if (jb & 8) {
+            // every 16 bins: the even and odd partial sums into float-float
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              two_sum_acc(ahi[d], alo[d], __fadd_rn(acc[d].x, acc[d].y));
+              if (CPLX) two_sum_acc(bhi[d], blo[d], __fadd_rn(acci[d].x, acci[d].y));
+              acc[d] = acci[d] = zero2;
+            }
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          two_sum_acc(ahi[d], alo[d], __fadd_rn(acc[d].x, acc[d].y));
+          if (CPLX) two_sum_acc(bhi[d], blo[d], __fadd_rn(acci[d].x, acci[d].y));
         }
       }
 #pragma unroll

@@ -1,7 +1,7 @@
-// Anchored TaylorF2 phase recurrence shared by the bin-walking kernels: the
-// Taylor coefficients of the phase about an anchor bin from the per-analysis
-// tables of the basis functions, their forward differences in 0.64 fixed
-// point, and the choice of anchor interval and polynomial degree.
+// Anchored TaylorF2 phase shared by the bin-walking kernels: the Taylor
+// coefficients of the phase about an anchor bin from the per-analysis tables
+// of the basis functions, the choice of anchor interval and polynomial
+// degree, and packed float-pair arithmetic.
 #pragma once
 
 #include <cstdint>
@@ -81,15 +81,19 @@ __device__ __forceinline__ int anchor_degree(float n_cycles, float x) {
   return 6;
 }
 
-// Forward differences D[0..6] (0.64 fixed point, cycles) of the phase
-// polynomial about anchor bin k, truncated at degree deg: the float-float
-// dot products A_n = sum_b c_b T_n,b(k) (orders 0..3 float-float, 4..6
-// float32) and Delta_m = m! sum_n S(n, m) A_n (Stirling numbers).  ch / cl:
-// the point's basis coefficients (index kNumBasis: the constant).
-__device__ __forceinline__ void anchor_differences(const float* anchors, int64_t k, const float* ch, const float* cl,
-                                                   int deg, uint64_t* D) {
+// Taylor coefficients A_n of the phase polynomial about anchor bin k, in
+// cycles: Phi(k + j) = sum_n A_n j^n.  A_n = sum_b c_b T_n,b(k) from the
+// per-analysis Taylor tables of the basis functions, orders 0..3 as
+// float-float dot products and 4..6 in float32.  ch / cl: the point's basis
+// coefficients (index kNumBasis: the constant).
+struct AnchorTaylor {
+  float h[kAnchorFF], l[kAnchorFF];   // orders 0..3, float-float
+  float f[kAnchorOrders - kAnchorFF]; // orders 4..6
+};
+
+__device__ __forceinline__ void anchor_taylor(const float* anchors, int64_t k, const float* ch, const float* cl,
+                                              AnchorTaylor& t) {
   const float* an = anchors + (k / kAnchorStep) * kAnchorFloats;
-  float Ah[kAnchorFF], Al[kAnchorFF], Af[kAnchorOrders - kAnchorFF];
 #pragma unroll
   for (int n = 0; n < kAnchorFF; ++n) {
     float sh = n == 0 ? ch[kNumBasis] : 0.f, sl = n == 0 ? cl[kNumBasis] : 0.f;
@@ -97,37 +101,51 @@ __device__ __forceinline__ void anchor_differences(const float* anchors, int64_t
     for (int b = 0; b < kNumBasis; ++b)
       ff_mac(sh, sl, ch[b], cl[b], __ldg(an + n * kNumBasis + b),
              __ldg(an + kAnchorOrders * kNumBasis + n * kNumBasis + b));
-    Ah[n] = sh;
-    Al[n] = sl;
+    t.h[n] = sh;
+    t.l[n] = sl;
   }
 #pragma unroll
   for (int n = kAnchorFF; n < kAnchorOrders; ++n) {
     float sf = 0.f;
 #pragma unroll
     for (int b = 0; b < kNumBasis; ++b) sf = __fmaf_rn(ch[b], __ldg(an + n * kNumBasis + b), sf);
-    Af[n - kAnchorFF] = sf;
+    t.f[n - kAnchorFF] = sf;
   }
-  const float A4 = Af[0], A5 = deg >= 5 ? Af[1] : 0.f, A6 = deg >= 6 ? Af[2] : 0.f;
-  float d1h = Ah[1], d1l = Al[1];
-  ff_add(d1h, d1l, Ah[2], Al[2]);
-  ff_add(d1h, d1l, Ah[3], Al[3]);
-  ff_add(d1h, d1l, __fadd_rn(__fadd_rn(A4, A5), A6), 0.f);
-  float d2h = Ah[2], d2l = Al[2];
-  ff_scale(d2h, d2l, 2.f);
-  float t3h = Ah[3], t3l = Al[3];
-  ff_scale(t3h, t3l, 6.f);
-  ff_add(d2h, d2l, t3h, t3l);
-  ff_add(d2h, d2l, lin3(14.f, A4, 30.f, A5, 62.f, A6), 0.f);
-  float d3h = Ah[3], d3l = Al[3];
-  ff_scale(d3h, d3l, 6.f);
-  ff_add(d3h, d3l, lin3(36.f, A4, 150.f, A5, 540.f, A6), 0.f);
-  D[0] = to_fixed(Ah[0], Al[0]);
-  D[1] = to_fixed(d1h, d1l);
-  D[2] = to_fixed(d2h, d2l);
-  D[3] = to_fixed(d3h, d3l);
-  D[4] = to_fixed(lin3(24.f, A4, 240.f, A5, 1560.f, A6), 0.f);
-  D[5] = to_fixed(__fmaf_rn(1800.f, A6, __fmul_rn(120.f, A5)), 0.f);
-  D[6] = to_fixed(__fmul_rn(720.f, A6), 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Packed float pairs: the sm_100-family f32x2 instructions do two IEEE
+// round-to-nearest float32 operations in one issue slot.  Lane x and lane y
+// are independent; the pair lives in one 64-bit register pair.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
 }
 
 }  // namespace gwl
