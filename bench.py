@@ -97,6 +97,8 @@ def parse():
     ap.add_argument("--serve-streams", type=int, default=3, help="serving steps in flight")
     ap.add_argument("--serve-max-points", type=int, default=1 << 15, help="points per serving step at most")
     ap.add_argument("--no-single", action="store_true", help="skip the single-analysis launch")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="profiling runs: skip the 64-analysis step and the served runs (the line's value is null)")
     ap.add_argument("--no-sg", action="store_true", help="skip the sine-Gaussian workload")
     ap.add_argument("--no-marg", action="store_true", help="skip the marginalised workload")
     ap.add_argument("--no-relbin", action="store_true", help="skip the relative-binning workload")
@@ -700,12 +702,46 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
             "time_marginalized": tm}
 
 
+def eim_basis(f, n_linear, n_quadratic, n_train, seed, fmin, mass_range=(10.0, 40.0)):
+    """A seeded ROQ basis of the stated size on frequencies ``f``: reduced
+    bases (SVD) of normalised TaylorF2 training waveforms (and of their
+    squared moduli) with greedy empirical-interpolation nodes, the standard
+    construction (Field et al., arXiv:1308.3565).  Returns (linear nodes,
+    linear basis N x n, quadratic nodes, quadratic basis N x m)."""
+    from bilby_gb300.source import taylorf2_aligned
+    rng = np.random.default_rng(seed)
+    lin, quad = [], []
+    for _ in range(n_train):
+        m1, m2 = np.sort(rng.uniform(*mass_range, 2))[::-1]
+        h = taylorf2_aligned(f, m1, m2, rng.uniform(-0.05, 0.05), rng.uniform(-0.05, 0.05), 100.0, 0.0, 0.0,
+                             minimum_frequency=fmin)["plus"]
+        lin.append(h / np.linalg.norm(h))
+        q = np.abs(h) ** 2
+        quad.append(q / np.linalg.norm(q))
+
+    def eim(basis):
+        nodes = [int(np.argmax(np.abs(basis[:, 0])))]
+        for j in range(1, basis.shape[1]):
+            coef = np.linalg.solve(basis[nodes, :j], basis[nodes, j])
+            nodes.append(int(np.argmax(np.abs(basis[:, j] - basis[:, :j] @ coef))))
+        return np.array(nodes), np.linalg.solve(basis[nodes, :].T, basis.T).T
+
+    ul = np.linalg.svd(np.array(lin).T, full_matrices=False)[0][:, :n_linear]
+    uq = np.linalg.svd(np.array(quad).T, full_matrices=False)[0][:, :n_quadratic]
+    nl, bl = eim(ul)
+    nq, bq = eim(uq)
+    order_l, order_q = np.argsort(nl), np.argsort(nq)
+    return f[nl][order_l], bl[:, order_l], f[nq][order_q], bq[:, order_q].real
+
+
 def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, seed=41):
     """Reduced-order quadrature on the GPU (bilby/gw/likelihood/roq.py, one
     basis).  ROQ bases are data files the container does not have, so a
-    seeded random basis of the stated size stands in: the cost of an
-    evaluation depends on the numbers of nodes and time samples, not on the
-    basis values.  float64 throughout."""
+    seeded empirical-interpolation basis of TaylorF2 waveforms of the stated
+    size stands in (eim_basis).  The float64 cost depends on the numbers of
+    nodes and time samples only; the mixed-precision error bound, and so the
+    share of points recomputed in float64, on the sizes of the weight-node
+    products, which a basis of real waveforms gives."""
     import torch
     from bilby_gb300.analysis import params_block
     from bilby_gb300.prior import Uniform
@@ -718,10 +754,7 @@ def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, s
     ifos = base.interferometers
     rng = np.random.default_rng(seed)
     fm = np.asarray(ifos[0].strain_data.frequency_array)[np.asarray(ifos[0].strain_data.frequency_mask)]
-    lin = rng.standard_normal((len(fm), n_linear)) + 1j * rng.standard_normal((len(fm), n_linear))
-    quad = rng.standard_normal((len(fm), n_quadratic))
-    nl = np.sort(rng.choice(fm, n_linear, replace=False))
-    nq = np.sort(rng.choice(fm, n_quadratic, replace=False))
+    nl, lin, nq, quad = eim_basis(fm, n_linear, n_quadratic, 2 * n_linear + 100, seed, w.minimum_frequency)
     wfg = WaveformGenerator(duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
                             frequency_domain_source_model=taylorf2_aligned_roq,
                             waveform_arguments=dict(minimum_frequency=w.minimum_frequency,
@@ -753,18 +786,37 @@ def bench_roq(name, steps, warmup, batch=65536, n_linear=400, n_quadratic=100, s
     res = {"workload": name, "linear_nodes": n_linear, "quadratic_nodes": n_quadratic,
            "time_samples": int(len(like.weights["time_samples"])), "batch": batch,
            "value": batch * steps / (sum(ms) / 1e3), "unit": "evals/s", "ms_per_launch": float(np.mean(ms)),
-           "precision": "fp64", "setup_s": setup_s, "basis": "seeded random basis of the stated size",
+           "precision": "fp64", "setup_s": setup_s,
+           "basis": "seeded empirical-interpolation basis of TaylorF2 waveforms of the stated size",
            "launch": "prologue + one warp per point over the nodes"}
     # with time marginalisation (roq.py:320-331, 604-651): every weight row of
     # the prior window contracted per point, five-sample interpolation per time
     like_t = ROQGravitationalWaveTransient(ifos, wfg, {"geocent_time": Uniform(tc - 0.1, tc + 0.1)},
                                            linear_matrix=lin, quadratic_matrix=quad, time_marginalization=True)
-    bt = 1024
-    ms_t, finite = time_launches(like_t.analysis, time_marginalized_block(w, bt, rng), bt, steps, warmup)
-    res["time_marginalized"] = {"batch": bt, "marginalization_samples": int(len(like_t._times)),
-                                "weight_rows": int(len(like_t.weights["time_samples"])),
-                                "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
-                                "precision": "fp64", "finite": finite}
+    bt, bm = 1024, 8192
+    blk_t = time_marginalized_block(w, bt, rng)   # parameter blocks are [slot][point]: one per batch size
+    blk_m = time_marginalized_block(w, bm, rng)
+    an_t = like_t.analysis
+    ms_t, finite = time_launches(an_t, blk_t, bt, steps, warmup)
+    ms_m, finite_m = time_launches(an_t, blk_m, bm, steps, warmup, "mixed")
+    refined = an_t.last_refined()
+    o64 = torch.empty(bt, dtype=torch.float64, device="cuda")
+    omx = torch.empty(bt, dtype=torch.float64, device="cuda")
+    an_t.log_likelihood_ratio_device(blk_t.data_ptr(), bt, o64.data_ptr(), "fp64", stream.cuda_stream)
+    an_t.log_likelihood_ratio_device(blk_t.data_ptr(), bt, omx.data_ptr(), "mixed", stream.cuda_stream)
+    torch.cuda.synchronize()
+    res["time_marginalized"] = {
+        "marginalization_samples": int(len(like_t._times)), "weight_rows": int(len(like_t.weights["time_samples"])),
+        "launch": "prologue + per point the model at the nodes, one complex float32 GEMM per detector over every "
+                  "weight row (cuBLAS, pedantic float32), per point the interpolation and marginalisation in "
+                  "float32 with the error bound, float64 recomputation of the marked points",
+        "fp64": {"batch": bt, "value": bt / (ms_t / 1e3), "unit": "evals/s", "ms_per_launch": ms_t,
+                 "finite": finite},
+        "mixed": {"batch": bm, "value": bm / (ms_m / 1e3), "unit": "evals/s", "ms_per_launch": ms_m,
+                  "finite": finite_m, "refined_points_per_launch": refined},
+        "mixed_over_fp64": (bm / ms_m) / (bt / ms_t),
+        "max_abs_dlnl_mixed_vs_fp64": float((omx - o64).abs().max().item()),
+        "points_compared": bt}
     return res
 
 
@@ -1063,21 +1115,23 @@ def run_ours(args, rank, world, local):
     sptr = stream.cuda_stream
 
     # -- the line's value: the 64-analysis batched step, device resident -------
-    uws = uneven_analyses(args.n_analyses)
-    ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
+    uneven = value = total_ms = None
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.05)
-    dist.barrier()
-    uneven = bench_uneven(ulikes, uws, args.steps, args.warmup, args.fp64_steps)
-    dist.barrier()
+    if not args.no_uneven:
+        uws = uneven_analyses(args.n_analyses)
+        ulikes = [build_likelihood(uw, precision="mixed") for uw in uws]
+        dist.barrier()
+        uneven = bench_uneven(ulikes, uws, args.steps, args.warmup, args.fp64_steps)
+        dist.barrier()
+        total_ms = dist.max(float(np.sum(uneven["ms_steps"])))
+        value = world * uneven["points_per_step"] * args.steps / (total_ms / 1e3)
     clk = clocks.stop()
-    total_ms = dist.max(float(np.sum(uneven["ms_steps"])))
-    value = world * uneven["points_per_step"] * args.steps / (total_ms / 1e3)
 
     # -- served: in-process and through IPC client processes -------------------
     served = ipc = None
-    if world == 1 and not args.no_serving:
+    if world == 1 and not args.no_serving and uneven is not None:
         srv = make_server(ulikes, args.serve_streams, args.serve_max_points)
         served = bench_serving(srv, uws, args.serve_seconds, uneven["value"])
         if not args.no_ipc:
@@ -1150,20 +1204,23 @@ def run_ours(args, rank, world, local):
 
     if rank == 0:
         e2e_v = ipc["saturated"]["evals_per_s"] if ipc else None
+        ue = uneven or {"fp64": {"value": None}, "mixed_over_fp64": None, "max_abs_dlnl_mixed_vs_fp64": None,
+                        "fraction_of_points_with_abs_dlnl_le_1e-3": None, "launches_per_step": 0}
         line = {
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps if total_ms else None,
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (exact 0.64 fixed-point phase recurrence, float-float anchors, error control to 1e-3)",
             "data": "synthetic (seeded noise from the bundled aLIGO O4 / AdV PSDs, one injection per analysis)",
             "config": dict(mix_config(args.n_analyses), parallelism=f"replicas x{world}",
                            l2="inputs larger than L2 and flushed before every timed step (256 MiB write)"),
-            "fp64": uneven["fp64"],
-            "mixed_over_fp64": uneven["mixed_over_fp64"],
-            "served_over_fp64": (e2e_v / uneven["fp64"]["value"]) if e2e_v else None,
-            "max_abs_dlnl_mixed_vs_fp64": uneven["max_abs_dlnl_mixed_vs_fp64"],
-            "fraction_of_points_with_abs_dlnl_le_1e-3": uneven["fraction_of_points_with_abs_dlnl_le_1e-3"],
-            "gpu_launches": uneven["launches_per_step"] * args.steps * world,
+            "fp64": ue["fp64"],
+            "mixed_over_fp64": ue["mixed_over_fp64"],
+            "served_over_fp64": (e2e_v / ue["fp64"]["value"]) if e2e_v else None,
+            "max_abs_dlnl_mixed_vs_fp64": ue["max_abs_dlnl_mixed_vs_fp64"],
+            "fraction_of_points_with_abs_dlnl_le_1e-3": ue["fraction_of_points_with_abs_dlnl_le_1e-3"],
+            "gpu_launches": ue["launches_per_step"] * args.steps * world,
             "p50_ms": ipc["at_80pct"]["p50_ms"] if ipc else None,
             "p99_ms": ipc["at_80pct"]["p99_ms"] if ipc else None,
             "clocks": clk,
@@ -1184,8 +1241,8 @@ def run_ours(args, rank, world, local):
             line["cpu_baselines"] = {"sg_4s": cpu["sg"], "tf2_128s": cpu["tf2"], "tf2_marg_8s_tpd": cpu["marg"],
                                      "tf2_128s_relative_binning": cpu["relbin"]}
             line["gpu_over_cpu"] = {
-                "mixed_mix_value": value / cpu["mix"]["value"],
-                "fp64_mix_precision_matched": uneven["fp64"]["value"] / cpu["mix"]["value"],
+                "mixed_mix_value": value / cpu["mix"]["value"] if value else None,
+                "fp64_mix_precision_matched": ue["fp64"]["value"] / cpu["mix"]["value"] if uneven else None,
                 "served_e2e": (e2e_v / cpu["mix"]["value"]) if e2e_v else None}
         if served:
             line["served"] = {"in_process": served, "ipc": ipc}

@@ -55,7 +55,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     extra = list(extra or [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcudart", "-lcublas"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -1,5 +1,6 @@
 // Host runtime behind include/gwlnl.h: builds the device-resident tables of an
 // analysis, owns its work space and sequences the kernels of one evaluation.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -136,6 +137,16 @@ struct gwl_analysis {
   double4* roq_pq = nullptr;
   double2* roq_wl[kMaxDet] = {};
   double* roq_wq[kMaxDet] = {};
+  float2* roq_wl32[kMaxDet] = {};  // float32 copy of roq_wl, nodes zero-padded to roq_nl_pad (mixed time marginalisation)
+  float roq_wnorm[kMaxDet][kRoqSplits] = {};  // per node group: largest row norm of roq_wl
+  int roq_nl_pad = 0, roq_ks = 0;
+  int2* roq_tm_g = nullptr;        // per marginalisation sample: its weight-grid index, floor and fraction
+  // mixed ROQ time marginalisation: cuBLAS handle and one chunk's buffers
+  cublasHandle_t blas = nullptr;
+  float2* d_roq_h32 = nullptr;
+  float2* d_roq_d32 = nullptr;
+  double* d_roq_hh = nullptr;
+  int64_t roq_ws_points = 0;
   // work space
   int chunks_per_group = kChunksPerGroup;  // split-K depth of the TaylorF2 mixed kernel (gwl_autotune)
   int64_t ws_B = 0;
@@ -211,6 +222,12 @@ void free_workspace(gwl_analysis* a) {
   a->last_rf_count = nullptr;
   a->ws_B = 0;
   a->part_bytes = a->tm_bytes = 0;
+  cudaFree(a->d_roq_h32);
+  cudaFree(a->d_roq_d32);
+  cudaFree(a->d_roq_hh);
+  a->d_roq_h32 = a->d_roq_d32 = nullptr;
+  a->d_roq_hh = nullptr;
+  a->roq_ws_points = 0;
 }
 
 float2 split_ff(double x) {
@@ -408,7 +425,12 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   for (int d = 0; d < a->n_det; ++d) {
     L.roq_wl[d] = a->roq_wl[d];
     L.roq_wq[d] = a->roq_wq[d];
+    L.roq_wl32[d] = a->roq_wl32[d];
+    for (int sp = 0; sp < kRoqSplits; ++sp) L.roq_wnorm[d][sp] = a->roq_wnorm[d][sp];
   }
+  L.roq_nl_pad = a->roq_nl_pad;
+  L.roq_ks = a->roq_ks;
+  L.roq_tm_g = a->roq_tm_g;
   if (a->roq && a->roq_tm) {
     // roq.py:320-331: the marginalisation's own time grid, antenna patterns
     // and delays at the prior's mid time
@@ -515,6 +537,83 @@ int launch_window_marg(gwl_analysis* a, LaunchArgs& L, cudaStream_t s, bool mixe
   return GWL_OK;
 }
 
+// ROQ with time marginalisation in mixed precision, chunk by chunk: the node
+// values, one complex float32 GEMM per detector (D_d = W_d^T conj(h_d) over
+// every weight row), the interpolation and marginalisation with the error
+// bound, then the float64 kernel on the listed points.
+int run_roq_tm_mixed(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
+  const int64_t B = L.B, chunk = std::min<int64_t>(B, kRoqMixedChunk);
+  const int64_t np = a->roq_nl_pad, ks = a->roq_ks, nt = a->roq_n_time, D = a->n_det;
+  if (np > INT32_MAX || nt * chunk > INT32_MAX) {
+    set_error("ROQ time marginalisation: too many nodes or weight rows for a matrix product");
+    return GWL_ERR_UNSUPPORTED;
+  }
+  int rc;
+  if (a->roq_ws_points < chunk) {
+    cudaFree(a->d_roq_h32);
+    cudaFree(a->d_roq_d32);
+    cudaFree(a->d_roq_hh);
+    a->d_roq_h32 = a->d_roq_d32 = nullptr;
+    a->d_roq_hh = nullptr;
+    a->roq_ws_points = 0;
+    if ((rc = dev_alloc(a, &a->d_roq_h32, (size_t)(D * chunk * np), false))) return rc;
+    if ((rc = dev_alloc(a, &a->d_roq_d32, (size_t)(D * kRoqSplits * chunk * nt), false))) return rc;
+    if ((rc = dev_alloc(a, &a->d_roq_hh, (size_t)chunk, false))) return rc;
+    a->roq_ws_points = chunk;
+  }
+  if (!a->blas) {
+    if (cublasCreate(&a->blas) != CUBLAS_STATUS_SUCCESS) {
+      a->blas = nullptr;
+      set_error("cublasCreate failed");
+      return GWL_ERR_CUDA;
+    }
+    // float32 arithmetic throughout: no reduced-precision tensor-core path
+    cublasSetMathMode(a->blas, CUBLAS_PEDANTIC_MATH);
+  }
+  if (cublasSetStream(a->blas, s) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasSetStream failed");
+    return GWL_ERR_CUDA;
+  }
+  const bool marks = a->refine_tol > 0;
+  L.rf_tol = a->refine_tol;
+  L.rf_count = marks ? a->d_order_hist : nullptr;
+  L.rf_list = marks ? a->d_order : nullptr;
+  if (marks) GWL_CUDA(cudaMemsetAsync(L.rf_count, 0, sizeof(int32_t), s));
+  L.roq_h32 = a->d_roq_h32;
+  L.roq_d32 = a->d_roq_d32;
+  L.roq_hh = a->d_roq_hh;
+  const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+  for (int64_t c0 = 0; c0 < B; c0 += chunk) {
+    const int64_t cn = std::min(chunk, B - c0);
+    L.roq_c0 = c0;
+    L.roq_cn = cn;
+    GWL_CUDA(launch_roq_nodes32(L, s));
+    for (int64_t d = 0; d < D; ++d) {
+      // column-major, one batch entry per node group s: W_d,s^T (nt x ks, the
+      // row-major [nt][np] table from column s ks), H_d,s (ks x cn), D_d,s (nt x cn)
+      const cublasStatus_t st = cublasCgemmStridedBatched(
+          a->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)nt, (int)cn, (int)ks, &one,
+          reinterpret_cast<const cuComplex*>(a->roq_wl32[d]), (int)np, (long long)ks,
+          reinterpret_cast<const cuComplex*>(a->d_roq_h32 + (size_t)(d * cn * np)), (int)np, (long long)ks, &zero,
+          reinterpret_cast<cuComplex*>(a->d_roq_d32 + (size_t)(d * kRoqSplits * cn * nt)), (int)nt,
+          (long long)(cn * nt), kRoqSplits);
+      if (st != CUBLAS_STATUS_SUCCESS) {
+        set_error("cublasCgemmStridedBatched failed with status " + std::to_string((int)st));
+        return GWL_ERR_CUDA;
+      }
+    }
+    GWL_CUDA(launch_roq_tm_mixed(L, s));
+  }
+  if (marks) {
+    LaunchArgs R = L;
+    R.rf_tol = 0.0;
+    R.rf_list_only = 1;
+    GWL_CUDA(launch_roq_time_marginalized(R, s));
+    a->last_rf_count = L.rf_count;
+  }
+  return GWL_OK;
+}
+
 int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, double* d_out, double* d_dh,
              double* d_hh, cudaStream_t s, double* d_series = nullptr) {
   if (precision != GWL_PRECISION_FP64 && precision != GWL_PRECISION_MIXED) {
@@ -544,11 +643,20 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       set_error("ROQ with time marginalisation needs gwl_set_roq_time_marginalization");
       return GWL_ERR_ARGUMENT;
     }
+    // mixed precision: float32 matrix products and marginalisation, the
+    // points over the error bound recomputed in float64; float64 alone when
+    // the time series is requested
+    const bool mixed = precision == GWL_PRECISION_MIXED && !d_series && roq_tm_mixed_fits(L);
     L.precision = GWL_PRECISION_FP64;
     L.rf_tol = 0.0;
+    a->last_rf_count = nullptr;
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
-    GWL_CUDA(launch_roq_time_marginalized(L, s));
+    if (mixed) {
+      if ((rc = run_roq_tm_mixed(a, L, s))) return rc;
+    } else {
+      GWL_CUDA(launch_roq_time_marginalized(L, s));
+    }
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));
       a->ev_pending = 1;
@@ -1051,6 +1159,7 @@ int gwl_analysis_destroy(gwl_analysis* a) {
     std::lock_guard<std::mutex> g(a->mu);
     cudaStreamSynchronize(a->stream);
     free_workspace(a);
+    if (a->blas) cublasDestroy(a->blas);
     for (void* p : a->tables) cudaFree(p);
     a->tables.clear();
     if (a->ev_begin) cudaEventDestroy(a->ev_begin);
@@ -1613,6 +1722,24 @@ int gwl_set_roq(gwl_analysis* a, int enable, int32_t n_linear, const double* nod
                            quadratic_weights + (size_t)(d + 1) * n_quadratic);
     if ((rc = upload(a, &a->roq_wl[d], wl))) return rc;
     if ((rc = upload(a, &a->roq_wq[d], wq))) return rc;
+    // float32 copy with the nodes zero-padded to kRoqSplits groups of ks, and
+    // per group the largest row norm, for the mixed time marginalisation
+    const int ks = (n_linear + kRoqSplits - 1) / kRoqSplits, np = ks * kRoqSplits;
+    std::vector<float2> w32((size_t)n_time * np, make_float2(0.f, 0.f));
+    double wmax[kRoqSplits] = {};
+    for (int64_t k = 0; k < n_time; ++k) {
+      double n2[kRoqSplits] = {};
+      for (int q = 0; q < n_linear; ++q) {
+        const double2 v = wl[(size_t)k * n_linear + q];
+        w32[(size_t)k * np + q] = make_float2((float)v.x, (float)v.y);
+        n2[q / ks] += v.x * v.x + v.y * v.y;
+      }
+      for (int sp = 0; sp < kRoqSplits; ++sp) wmax[sp] = std::max(wmax[sp], std::sqrt(n2[sp]));
+    }
+    if ((rc = upload(a, &a->roq_wl32[d], w32))) return rc;
+    for (int sp = 0; sp < kRoqSplits; ++sp) a->roq_wnorm[d][sp] = (float)wmax[sp];
+    a->roq_ks = ks;
+    a->roq_nl_pad = np;
   }
   a->roq_nl = n_linear;
   a->roq_nq = n_quadratic;
@@ -1666,6 +1793,19 @@ int gwl_set_roq_time_marginalization(gwl_analysis* a, int64_t n_times, const dou
   }
   int rc;
   if ((rc = upload(a, &a->roq_tm_times, t))) return rc;
+  // the mixed kernel's weight-grid index of each sample, (t_j - start_0 - t0) / dt
+  // in float64 split into its floor and a float32 fraction (per point and
+  // detector it adds ((start_0 - start_d) + delay_d + jitter) / dt, split alike)
+  std::vector<int2> gidx((size_t)n_times);
+  for (int64_t j = 0; j < n_times; ++j) {
+    const double x = ((t[(size_t)j] - a->geom[0].start_time) - t0) / space;
+    const double fx = std::floor(x);
+    const float fr = (float)(x - fx);
+    int bits;
+    std::memcpy(&bits, &fr, 4);
+    gidx[(size_t)j] = make_int2((int)fx, bits);
+  }
+  if ((rc = upload(a, &a->roq_tm_g, gidx))) return rc;
   a->roq_tm_n = n_times;
   a->roq_tm_chunk = chunk;
   a->roq_tm_rows = rows;

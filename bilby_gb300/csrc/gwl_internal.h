@@ -40,6 +40,7 @@ constexpr double kRefineL1 = 1e-7;
 constexpr double kRefineLoudPower = 10.0;
 constexpr double kRefineDefaultTol = 5e-4;
 constexpr int kCosTable = 1024;        // angles of the float-float cos / sin table of the accurate kernel
+constexpr int kRoqSplits = 8;          // node groups of the mixed ROQ time-marginalised matrix products
 
 // Per-point quantities computed once per evaluation by the float64 prologue.
 struct PointRec {
@@ -220,6 +221,21 @@ struct LaunchArgs {
   int roq_tm;
   int64_t roq_tm_n, roq_tm_chunk, roq_tm_rows;  // samples, samples per chunk, rows per chunk (at most)
   const double* roq_tm_times;           // [roq_tm_n]
+  // ... in mixed precision, over one chunk of points [roq_c0, roq_c0 + roq_cn):
+  // conj(h_d) at the linear nodes in float32, complex float32 matrix
+  // products per detector over every weight row, the nodes split into
+  // kRoqSplits groups of roq_ks (roq_d32[d][s] = roq_wl32 h over group s),
+  // then per point the groups' sums in float-float and the per-sample
+  // interpolation and marginalisation in float32
+  const float2* roq_wl32[kMaxDet];      // [roq_n_time][roq_nl_pad] float32 copy of roq_wl, zero-padded
+  float roq_wnorm[kMaxDet][kRoqSplits]; // per node group: largest Euclidean norm of a row of roq_wl
+  int roq_nl_pad, roq_ks;               // kRoqSplits * roq_ks nodes (padded), roq_ks per group
+  const int2* roq_tm_g;                 // [roq_tm_n] (t_j - start_0 - t_grid0) / dt: {floor, float fraction bits}
+  float2* roq_h32;                      // [n_det][roq_cn][roq_nl_pad]
+  float2* roq_d32;                      // [n_det][kRoqSplits][roq_cn][roq_n_time]
+  double* roq_hh;                       // [roq_cn] <h|h>
+  int64_t roq_c0, roq_cn;
+  int rf_list_only;                     // float64 ROQ time marginalisation of the listed points alone
 };
 
 // A batch over several analyses evaluated by one persistent launch: per item
@@ -278,6 +294,13 @@ cudaError_t launch_multiband(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_multiband_mixed(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_roq(const LaunchArgs& a, cudaStream_t s);
 cudaError_t launch_roq_time_marginalized(const LaunchArgs& a, cudaStream_t s);
+// Mixed ROQ time marginalisation of one chunk: the node values before the
+// matrix products, the interpolation and marginalisation after them.
+constexpr int64_t kRoqMixedChunk = 1024;  // points per chunk
+// whether the mixed kernel's shared memory (rows of every detector, spline knots) fits
+bool roq_tm_mixed_fits(const LaunchArgs& a);
+cudaError_t launch_roq_nodes32(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_roq_tm_mixed(const LaunchArgs& a, cudaStream_t s);
 void order_layout(int64_t n_chunks, int* keys, int* shift);
 // Ordering of a mixed TaylorF2 launch: the band-end keys, doubled when points
 // can be marked for the accurate kernel (rf_tol > 0; their keys take the upper

@@ -511,24 +511,27 @@ __device__ __forceinline__ void acc_ff(float& hi, float& lo, float m, float c_hi
 // return: at the block's last bin, with it); sl[d]: its slope per bin.  wq:
 // detector 0's four bin pairs of the block in the stage (detector d is
 // kChunkMixed / 2 pairs further per detector).  jj: (j, j + 1) of the first
-// pair relative to the anchor (advanced by 8).  A3..A6: the cubic and higher
-// Taylor coefficients in radians (both lanes equal; A5 = A6 = 0 below degree
-// 5), q1..q3: the local quadratic remainder C(i, 2) 2 A_2 of pairs 1..3.
+// pair relative to the anchor (advanced by 8).  A3, A4: the cubic and quartic
+// Taylor coefficients in radians (both lanes equal), a5, a6 the quintic and
+// sextic ones (zero below degree 5; HI blocks only), a2: the second
+// difference of the quadratic part, whose local remainder is C(i, 2) a2.
 // MASK: bins outside [lo, hi) contribute nothing (band edges).
 template <int D, bool CPLX, bool HI, bool MASK>
 __device__ __forceinline__ void tf2_block(uint32_t* top, const uint32_t* sl, const uint4* wq, float2& jj,
-                                          float2 A3, float2 A4, float2 A5, float2 A6, float2 q1, float2 q2,
-                                          float2 q3, int lo, int hi, float2* acc, float2* acci) {
+                                          float2 A3, float2 A4, float a5, float a6, float a2, int lo, int hi,
+                                          float2* acc, float2* acci) {
   const float2 cc = make_float2(1.4629180792671596e-09f, 1.4629180792671596e-09f);  // 2 pi 2^-32
   const float2 two = make_float2(2.f, 2.f);
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
-    float2 t = HI ? fma2(fma2(A6, jj, A5), jj, A4) : A4;
+    float2 t = HI ? fma2(fma2(make_float2(a6, a6), jj, make_float2(a5, a5)), jj, A4) : A4;
     t = fma2(t, jj, A3);
     float2 rq = mul2(mul2(t, mul2(jj, jj)), jj);
-    if (p == 1) rq = add2(rq, q1);
-    if (p == 2) rq = add2(rq, q2);
-    if (p == 3) rq = add2(rq, q3);
+    // + C(i, 2) a2 for bins i = 2p, 2p + 1 (binomials 0 1 3 6 10 15 21 28 ...)
+    if (p > 0) {
+      rq.x = __fmaf_rn(a2, (float)((2 * p) * (2 * p - 1) / 2), rq.x);
+      rq.y = __fmaf_rn(a2, (float)((2 * p + 1) * (2 * p) / 2), rq.y);
+    }
     jj = add2(jj, two);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -640,9 +643,11 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
   };
   const auto xfix = [&](int d) -> uint64_t { return ((uint64_t)rp->xfix[d][1] << 32) | rp->xfix[d][0]; };
   if (have && valid) c0 = fabsf(rp->c_hi[0]);
-  double tre[D], tim[D];
+  // float32 partial sums folded into float-float accumulators, over every
+  // chunk of the unit (real part; imaginary part for the complex kernel)
+  float ahi[D], alo[D], bhi[D], blo[D];
 #pragma unroll
-  for (int d = 0; d < D; ++d) tre[d] = tim[d] = 0.0;
+  for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
 
   const uint32_t stage_bytes = D * CH * 8;
   const int64_t it0 = it_global;
@@ -679,10 +684,6 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
       const int J = anchor_interval(c0 * __powf((float)k0 * (float)a.step, -5.0f / 3.0f),
                                     (float)max(k0, (int64_t)8));
       const int jlast = (int)min((int64_t)CH, ke - k0);
-      // float32 partial sums folded into float-float accumulators
-      float ahi[D], alo[D], bhi[D], blo[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) ahi[d] = alo[d] = bhi[d] = blo[d] = 0.f;
       if (J == 0) {
         float ch[kNumBasis + 1], cl[kNumBasis + 1];
 #pragma unroll
@@ -718,7 +719,8 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
         // dQ = Q(j + 1) - Q(j) at the block start and its step-8 difference
         uint64_t E0 = 0, E1 = 0, E2 = 0, F0 = 0, F1 = 0;
         const float2 zero2 = make_float2(0.f, 0.f);
-        float2 A3 = zero2, A4 = zero2, A5 = zero2, A6 = zero2, q1 = zero2, q2 = zero2, q3 = zero2, jj = zero2;
+        float2 A3 = zero2, A4 = zero2, jj = zero2;
+        float a5 = 0.f, a6 = 0.f, a2 = 0.f;
         bool hi_deg = false;
         float2 acc[D], acci[D];
 #pragma unroll
@@ -747,17 +749,14 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
             // C(j) = j^3 (A3 + j (A4 + j (A5 + j A6))) in radians, truncated at degree deg
             const float tp = 6.283185307179586f;
             const float a3 = __fmul_rn(__fadd_rn(t.h[3], t.l[3]), tp), a4 = __fmul_rn(t.f[0], tp);
-            const float a5 = deg >= 5 ? __fmul_rn(t.f[1], tp) : 0.f, a6 = deg >= 6 ? __fmul_rn(t.f[2], tp) : 0.f;
+            a5 = deg >= 5 ? __fmul_rn(t.f[1], tp) : 0.f;
+            a6 = deg >= 6 ? __fmul_rn(t.f[2], tp) : 0.f;
             A3 = make_float2(a3, a3);
             A4 = make_float2(a4, a4);
-            A5 = make_float2(a5, a5);
-            A6 = make_float2(a6, a6);
             hi_deg = deg > 4;
-            // local quadratic remainder Q(jb + i) - Q(jb) - i dQ(jb) = C(i, 2) 2 A2, radians
-            const float a2 = __fmul_rn(2.f * t.h[2], tp);
-            q1 = make_float2(a2, 3.f * a2);
-            q2 = make_float2(6.f * a2, 10.f * a2);
-            q3 = make_float2(15.f * a2, 21.f * a2);
+            // second difference of Q in radians: the local quadratic remainder
+            // Q(jb + i) - Q(jb) - i dQ(jb) = C(i, 2) 2 A2
+            a2 = __fmul_rn(2.f * t.h[2], tp);
             jj = make_float2(0.f, 1.f);
           }
           uint32_t top[D], sl[D];
@@ -771,13 +770,13 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
           if (jb + 8 <= jlast && k >= ks) {
             // a whole block inside the band
             if (hi_deg) {
-              tf2_block<D, CPLX, true, false>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, 0, 8, acc, acci);
+              tf2_block<D, CPLX, true, false>(top, sl, wq, jj, A3, A4, a5, a6, a2, 0, 8, acc, acci);
             } else {
-              tf2_block<D, CPLX, false, false>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, 0, 8, acc, acci);
+              tf2_block<D, CPLX, false, false>(top, sl, wq, jj, A3, A4, a5, a6, a2, 0, 8, acc, acci);
             }
           } else {
             const int lo = (int)max((int64_t)0, ks - k), hi = min(8, jlast - jb);
-            tf2_block<D, CPLX, true, true>(top, sl, wq, jj, A3, A4, A5, A6, q1, q2, q3, lo, hi, acc, acci);
+            tf2_block<D, CPLX, true, true>(top, sl, wq, jj, A3, A4, a5, a6, a2, lo, hi, acc, acci);
           }
           E0 += E1;
           E1 += E2;
@@ -800,11 +799,6 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
           if (CPLX) two_sum_acc(bhi[d], blo[d], __fadd_rn(acci[d].x, acci[d].y));
         }
       }
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        tre[d] += (double)ahi[d] + (double)alo[d];
-        if (CPLX) tim[d] += (double)bhi[d] + (double)blo[d];
-      }
     }
     __syncthreads();
   }
@@ -812,8 +806,8 @@ __device__ __noinline__ void tf2_unit(const LaunchArgs& a, int64_t tile, int64_t
   if (have) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      a.part[((g * D + d) * kPartStride + 0) * a.B + i] = tre[d];
-      if (CPLX) a.part[((g * D + d) * kPartStride + 1) * a.B + i] = tim[d];
+      a.part[((g * D + d) * kPartStride + 0) * a.B + i] = (double)ahi[d] + (double)alo[d];
+      if (CPLX) a.part[((g * D + d) * kPartStride + 1) * a.B + i] = (double)bhi[d] + (double)blo[d];
     }
   }
 }

@@ -31,6 +31,7 @@
 #include "gwl_internal.h"
 #include "gwl_marg_common.cuh"
 #include "gwl_math.cuh"
+#include "gwl_phase.cuh"
 
 namespace gwl {
 
@@ -743,7 +744,10 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
   const double t0 = (double)a.roq_time_start * a.roq_dt;
   const double space = (double)(a.roq_time_start + 1) * a.roq_dt - t0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
-  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+  // every point, or (the recomputation of a mixed launch) the listed ones
+  const int64_t n_items = a.rf_list_only ? (int64_t)*a.rf_count : a.B;
+  for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int64_t i = a.rf_list_only ? (int64_t)a.rf_list[it] : it;
     const PointRec& r = a.rec[i];
     const double jit = r.jitter;
     const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
@@ -897,6 +901,331 @@ __global__ void __launch_bounds__(kTmThreads) k_roq_time_marg(LaunchArgs a) {
       a.out[i] = lnl;
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ROQ with time marginalisation, mixed precision.  Step 2 of the float64
+// kernel, D_d[k] = sum_q W_d[k][q] conj(h_d(F_q)), is a matrix product over
+// the batch: (weight rows x linear nodes) x (linear nodes x points) per
+// detector.  It runs as complex float32 GEMMs over every row of the weight
+// grid (cuBLAS, pedantic float32 math: no reduced-precision tensor path),
+// one per group of kRoqSplits consecutive node groups (a strided batch), so
+// that each float32 sum has a few tens of terms; around them
+//   k_roq_nodes32: conj(h_d) at the linear nodes from the float64 model,
+//     stored as float32 pairs (zero in the padding), with <h|h> (float64,
+//     quadratic nodes);
+//   k_roq_tm_mixed: per point, the groups' partial rows summed in
+//     float-float (TwoSum) into shared memory over the rows the point reads,
+//     the five-sample interpolation at each marginalisation sample's detector
+//     time, the per-sample marginalised lnL and the logsumexp in float32 (the
+//     large terms in float64).  The detector time's index on the weight grid
+//     is the float64 value of the float64 kernel split into integer and
+//     fraction parts on the host (per sample) and once per point (per
+//     detector), so that no float64 arithmetic runs per sample.
+// Error bound of a point (|dlnL| <= s |dX|, s = tm_sensitivity): the float32
+// rounding of each group's products and sums, below kRoqErrNorm times
+// C_d = (sum_s (max_k ||W_dk,s||_2 ||h_d,s||_2)^2)^(1/2) per detector (the
+// groups' errors are independent; a K-term float32 dot product errs by about
+// u ||w|| ||h|| / sqrt(2) when summed in order), and the rounding of the
+// summed rows and the interpolation, below kRoqErrPeak max_j |X_j|.  On the
+// 400-node synthetic basis of the benchmark, summed in order in float32, the
+// error is at most 0.83 u C_d; kRoqErrNorm = 6 u covers that with the
+// interpolation's weights (their absolute sum is below 1.8) and a margin of 4.
+// Points over the tolerance are listed for the float64 kernel.
+// ---------------------------------------------------------------------------
+constexpr double kRoqErrNorm = 6.0 * 5.9604644775390625e-08;
+constexpr double kRoqErrPeak = 1e-6;
+constexpr int kRoqNodeThreads = 128;
+constexpr int kRoqMixThreads = 256;
+
+template <int D>
+__global__ void __launch_bounds__(kRoqNodeThreads) k_roq_nodes32(LaunchArgs a) {
+  __shared__ double red[kRoqNodeThreads / 32];
+  const int64_t p = blockIdx.x, i = a.roq_c0 + p, cn = a.roq_cn;
+  const int nl = a.roq_nl, nq = a.roq_nq, np = a.roq_nl_pad;
+  const PointRec& r = a.rec[i];
+  const bool tf2 = a.model == GWL_MODEL_TAYLORF2;
+  const double u = tf2 ? cbrt(kPi * r.m_sec) : 0.0, lnu = tf2 ? log(u) : 0.0;
+  const double pu5 = tf2 ? 3.0 / (128.0 * r.eta) / (u * u * u * u * u) : 0.0;
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+    const bool on = q < nl && r.valid &&
+                    (tf2 ? tf2_pols_t(a, r, a.roq_pl[q], a.roq_fl[q], u, lnu, pu5, hp, hx)
+                         : plain_pols(a, r, a.roq_fl[q], hp, hx));
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double hr = on ? hp.x * r.fp[d] + hx.x * r.fx[d] : 0.0;
+      const double hi = on ? hp.y * r.fp[d] + hx.y * r.fx[d] : 0.0;
+      a.roq_h32[((size_t)d * cn + p) * np + q] = make_float2((float)hr, (float)-hi);
+    }
+  }
+  double hh_part = 0.0;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
+    const double f = a.roq_fq[q];
+    if (!(r.valid && (tf2 ? tf2_pols_t(a, r, a.roq_pq[q], f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx))))
+      continue;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double hr = hp.x * r.fp[d] + hx.x * r.fx[d], hi = hp.y * r.fp[d] + hx.y * r.fx[d];
+      hh_part += (hr * hr + hi * hi) * a.roq_wq[d][q];
+    }
+  }
+  // a fixed-order sum: xor-shuffles within the warps, then the warps in order
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) hh_part += __shfl_xor_sync(0xffffffffu, hh_part, o);
+  if (lane == 0) red[warp] = hh_part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kRoqNodeThreads / 32; ++w) t += red[w];
+    a.roq_hh[p] = t;
+  }
+}
+
+// rows of detector d the samples [j0, j1) read: grid indices from
+// floor(g_j) + b_d - 2 to floor(g_j) + b_d + 1 + 2, clamped to the grid
+__device__ __forceinline__ void roq_row_range(const LaunchArgs& a, int64_t j0, int64_t j1, int bi, int64_t* lo,
+                                              int64_t* n) {
+  const int64_t nt = a.roq_n_time;
+  if (j1 <= j0) {
+    *lo = 0;
+    *n = 0;
+    return;
+  }
+  int64_t k0 = (int64_t)a.roq_tm_g[j0].x + bi - 2, k1 = (int64_t)a.roq_tm_g[j1 - 1].x + bi + 3;
+  k0 = k0 < 0 ? 0 : k0;
+  k1 = k1 > nt - 1 ? nt - 1 : k1;
+  *lo = k0;
+  *n = k1 >= k0 ? k1 - k0 + 1 : 0;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kRoqMixThreads) k_roq_tm_mixed(LaunchArgs a) {
+  // dynamic shared memory: the distance spline's knots tx [nx], ty [ny], then
+  // per detector the summed rows the point reads (float32 pairs, nt at most)
+  extern __shared__ __align__(16) float s_dyn[];
+  __shared__ SplineRowF s_row;
+  __shared__ float redf[3 * (kRoqMixThreads / 32)];
+  __shared__ float s_hn[kMaxDet * kRoqSplits];
+  __shared__ double s_scal[2];
+  __shared__ int s_bi[kMaxDet];
+  __shared__ float s_bf[kMaxDet];
+  __shared__ long long s_j[2], s_klo[kMaxDet], s_kn[kMaxDet];
+  const int64_t p = blockIdx.x, i = a.roq_c0 + p, cn = a.roq_cn, nt = a.roq_n_time;
+  const PointRec& r = a.rec[i];
+  float* s_tx = s_dyn;
+  float* s_ty = s_dyn + a.nx;
+  const int kn0 = a.dist_marg ? ((a.nx + a.ny + 3) & ~3) : 0;
+  float2* s_rows = reinterpret_cast<float2*>(s_dyn + kn0);  // [D][nt]
+  if (a.dist_marg) {
+    for (int q = threadIdx.x; q < a.nx; q += blockDim.x) s_tx[q] = a.tx_f[q];
+    for (int q = threadIdx.x; q < a.ny; q += blockDim.x) s_ty[q] = a.ty_f[q];
+  }
+  const double jit = r.jitter;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int W = kRoqMixThreads / 32;
+  if (threadIdx.x == 0) {
+    s_scal[0] = a.roq_hh[p];
+    s_scal[1] = r.dist / a.ref_dist;
+    // the samples inside the prior: t_j + jit in [t_min, t_max], tested as
+    // the float64 kernel tests them (the times increase)
+    const int64_t n = a.roq_tm_n;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (a.roq_tm_times[mid] + jit >= a.t_min) hi = mid; else lo = mid + 1;
+    }
+    int64_t lo2 = lo, hi2 = n;  // first sample past t_max
+    while (lo2 < hi2) {
+      const int64_t mid = (lo2 + hi2) / 2;
+      if (a.roq_tm_times[mid] + jit <= a.t_max) lo2 = mid + 1; else hi2 = mid;
+    }
+    s_j[0] = lo;
+    s_j[1] = lo2;
+  }
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + D) {
+    // detector d's grid index offset ((start_0 - start_d) + dt_d + jit) / dt, split
+    const int d = threadIdx.x - 32;
+    const double t0 = (double)a.roq_time_start * a.roq_dt;
+    const double space = (double)(a.roq_time_start + 1) * a.roq_dt - t0;
+    const double bd = (((a.det[0].start_time - a.det[d].start_time) + r.dt[d]) + jit) / space;
+    const double fb = floor(bd);
+    s_bi[d] = (int)fb;
+    s_bf[d] = (float)(bd - fb);
+  }
+  // ||h_d,s||_2 per node group, one warp per (detector, group), fixed order
+  for (int ds = warp; ds < D * kRoqSplits; ds += W) {
+    const int d = ds / kRoqSplits, sp = ds % kRoqSplits;
+    const float2* h = a.roq_h32 + ((size_t)d * cn + p) * a.roq_nl_pad + (size_t)sp * a.roq_ks;
+    float n2 = 0.f;
+    for (int q = lane; q < a.roq_ks; q += 32) n2 = __fmaf_rn(h[q].x, h[q].x, __fmaf_rn(h[q].y, h[q].y, n2));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+    if (lane == 0) s_hn[ds] = sqrtf(n2);
+  }
+  __syncthreads();
+  if (threadIdx.x < D) {
+    int64_t lo, n;
+    roq_row_range(a, s_j[0], s_j[1], s_bi[threadIdx.x], &lo, &n);
+    s_klo[threadIdx.x] = lo;
+    s_kn[threadIdx.x] = n;
+  }
+  const double hh = s_scal[0], sr = s_scal[1];
+  if (threadIdx.x == 32 && a.dist_marg) s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)(hh * sr * sr));
+  __syncthreads();
+  // the groups' partial rows summed in float-float, rounded once to float32
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int64_t klo = s_klo[d], kn = s_kn[d];
+    const float2* src = a.roq_d32 + ((size_t)d * kRoqSplits * cn + p) * nt + klo;
+    for (int64_t k = threadIdx.x; k < kn; k += blockDim.x) {
+      float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
+#pragma unroll
+      for (int sp = 0; sp < kRoqSplits; ++sp) {
+        const float2 v = src[(size_t)sp * cn * nt + k];
+        two_sum_acc(xh, xl, v.x);
+        two_sum_acc(yh, yl, v.y);
+      }
+      s_rows[(size_t)d * nt + k] = make_float2(__fadd_rn(xh, xl), __fadd_rn(yh, yl));
+    }
+  }
+  __syncthreads();
+  double m = -INFINITY, acc = 0.0;
+  float xmax = 0.f;
+  const int64_t j1 = s_j[1];
+  for (int64_t j = s_j[0] + threadIdx.x; j < j1; j += blockDim.x) {
+    const int2 g = a.roq_tm_g[j];
+    const float gf = __int_as_float(g.y);
+    float xr = 0.f, xi = 0.f;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      // grid index fc = floor(g + b_d) and fraction b, rows fc - 2 .. fc + 2
+      const float sf = gf + s_bf[d];
+      const int carry = sf >= 1.f ? 1 : 0;
+      const float b = sf - (float)carry;
+      const int64_t k = (int64_t)g.x + s_bi[d] + carry - 2;
+      if (k < 0 || k + 4 > nt - 1) {
+        ok = false;  // outside the weight grid
+        continue;
+      }
+      const float2* Dd = s_rows + (size_t)d * nt + (k - s_klo[d]);
+      const float2 m2 = Dd[0], m1 = Dd[1], c0 = Dd[2], p1 = Dd[3], p2 = Dd[4];
+      const float a1 = 1.f - b;
+      const float c = (a1 * a1 * a1 - a1) * (1.f / 6.f), dd = (b * b * b - b) * (1.f / 6.f);
+      const float r1r = (-m2.x + 8.f * m1.x - 14.f * c0.x + 8.f * p1.x - p2.x) * 0.25f;
+      const float r1i = (-m2.y + 8.f * m1.y - 14.f * c0.y + 8.f * p1.y - p2.y) * 0.25f;
+      const float r2r = c0.x - 2.f * p1.x + p2.x, r2i = c0.y - 2.f * p1.y + p2.y;
+      xr += a1 * c0.x + b * p1.x + c * r1r + dd * r2r;
+      xi += a1 * c0.y + b * p1.y + c * r1i + dd * r2i;
+    }
+    if (!ok) continue;
+    double lw = 0.0;
+    if (a.tm_prior) {
+      const float pw = tm_prior_density_f(a, a.roq_tm_times[j] + jit);  // base.py:807, prior(t_j)
+      if (!(pw > 0.f)) continue;
+      lw = (double)__logf(pw);
+    }
+    const double l = tm_lnl_mixed(a, xr, xi, hh, sr, s_tx, s_row) + lw;
+    xmax = fmaxf(xmax, sqrtf(xr * xr + xi * xi));
+    tm_lse_push<true>(l, m, acc);
+  }
+  // the block's logsumexp: the float32 maximum of the threads' m (any
+  // reference near the maximum serves), then sum acc_t exp(m_t - M), both by
+  // xor-shuffles within warps and a fixed-order sum over the warps
+  float mf = (float)m, xm = xmax;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
+    xm = fmaxf(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+  }
+  if (lane == 0) {
+    redf[warp] = mf;
+    redf[W + warp] = xm;
+  }
+  __syncthreads();
+  float M = redf[0];
+  for (int w = 1; w < W; ++w) M = fmaxf(M, redf[w]);
+  float sm = 0.f;
+  if (isfinite(M) && isfinite(m)) sm = (float)acc * __expf((float)(m - (double)M));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
+  if (lane == 0) redf[2 * W + warp] = sm;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float total = 0.f, xp = 0.f;
+    for (int w = 0; w < W; ++w) {
+      total += redf[2 * W + w];
+      xp = fmaxf(xp, redf[W + w]);
+    }
+    const double prob = 1.0 / (a.t_max - a.t_min);
+    const double tot = (double)total * (a.tm_prior ? 1.0 : prob) * a.delta_tc;
+    double lnl;
+    if (!r.valid) lnl = -1.7976931348623157e308;
+    else if (!isfinite(M)) lnl = (double)M;
+    else lnl = (double)M + (double)logf((float)tot);
+    a.out[i] = lnl;
+    if (a.rf_tol > 0 && a.rf_count && a.rf_list && r.valid) {
+      double gemm = 0.0;
+      for (int d = 0; d < D; ++d) {
+        double c2 = 0.0;
+        for (int sp = 0; sp < kRoqSplits; ++sp) {
+          const double c = (double)a.roq_wnorm[d][sp] * (double)s_hn[d * kRoqSplits + sp];
+          c2 += c * c;
+        }
+        gemm += sqrt(c2);
+      }
+      const double err =
+          tm_sensitivity(a, (double)xp, sr, s_tx, s_row) * (kRoqErrNorm * gemm + kRoqErrPeak * (double)xp);
+      if (!(err <= a.rf_tol)) a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
+    }
+  }
+}
+
+size_t roq_tm_mixed_smem(const LaunchArgs& a) {
+  const size_t knots = a.dist_marg ? (size_t)((a.nx + a.ny + 3) & ~3) * sizeof(float) : 0;
+  return knots + (size_t)a.n_det * (size_t)a.roq_n_time * sizeof(float2);
+}
+
+bool roq_tm_mixed_fits(const LaunchArgs& a) { return roq_tm_mixed_smem(a) <= (size_t)200 * 1024; }
+
+template <int D>
+static cudaError_t launch_roq_nodes32_d(const LaunchArgs& a, cudaStream_t s) {
+  k_roq_nodes32<D><<<(unsigned)a.roq_cn, kRoqNodeThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roq_nodes32(const LaunchArgs& a, cudaStream_t s) {
+  if (a.roq_cn < 1) return cudaSuccess;
+  switch (a.n_det) {
+    case 1: return launch_roq_nodes32_d<1>(a, s);
+    case 2: return launch_roq_nodes32_d<2>(a, s);
+    case 3: return launch_roq_nodes32_d<3>(a, s);
+    default: return launch_roq_nodes32_d<4>(a, s);
+  }
+}
+
+template <int D>
+static cudaError_t launch_roq_tm_mixed_d(const LaunchArgs& a, cudaStream_t s) {
+  const size_t smem = roq_tm_mixed_smem(a);  // the opt-in covers the dynamic part
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_roq_tm_mixed<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_roq_tm_mixed<D><<<(unsigned)a.roq_cn, kRoqMixThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roq_tm_mixed(const LaunchArgs& a, cudaStream_t s) {
+  if (a.roq_cn < 1) return cudaSuccess;
+  if (!roq_tm_mixed_fits(a)) return cudaErrorInvalidValue;  // checked on the host first
+  switch (a.n_det) {
+    case 1: return launch_roq_tm_mixed_d<1>(a, s);
+    case 2: return launch_roq_tm_mixed_d<2>(a, s);
+    case 3: return launch_roq_tm_mixed_d<3>(a, s);
+    default: return launch_roq_tm_mixed_d<4>(a, s);
   }
 }
 

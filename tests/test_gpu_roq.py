@@ -102,6 +102,56 @@ def test_lnl_matches_the_reference(gpu, tmp_path, combo):
 
 
 
+def marginalized_points(params, priors, combo, jitter):
+    """Prior draws as the marginalised likelihood takes them: the marginalised
+    parameters at the values the constructor fixed in the priors."""
+    pts = {k: np.asarray(v, dtype=np.float64).copy() for k, v in params.items()}
+    n = len(pts["mass_1"])
+    pts["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+    pts["time_jitter"] = np.asarray(jitter, dtype=np.float64)
+    if "p" in combo:
+        pts["phase"] = np.zeros(n)
+    if "d" in combo:
+        pts["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+    return pts
+
+
+@pytest.mark.parametrize("combo", ["t", "tpd"])
+def test_mixed_time_marginalized_matches_the_reference(gpu, tmp_path, combo):
+    """Mixed precision (float32 weight-row products and marginalisation, the
+    points over the error bound recomputed in float64): |dlnL| <= 1e-3 from
+    the reference's values."""
+    like, priors, z = make(combo, tmp_path)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = marginalized_points(params, priors, combo, z["time_jitter"])
+    got = like.log_likelihood_ratio_batch(pts, precision="mixed")
+    ref = z["lnl_" + combo]
+    assert np.all(np.abs(got - ref) <= 1e-3), got - ref
+
+
+def test_mixed_time_marginalized_over_prior_draws(gpu, tmp_path):
+    """5000 prior draws (three chunks of the mixed launch) and 64 templates
+    near the injection, time, phase and distance marginalised: every mixed
+    result within 1e-3 of the float64 kernel's."""
+    from bilby_gb300.workloads import draw_points
+    like, priors, z = make("tpd", tmp_path)
+    w = WORKLOADS["tf2_marg_8s_2k"]
+    rng = np.random.default_rng(11)
+    p = draw_points(w, 5000, rng)
+    loud = {k: np.full(64, float(w.injection[k])) for k in w.injection}
+    loud["mass_1"] = loud["mass_1"] * (1 + rng.uniform(-2e-3, 2e-3, 64))
+    for k in ("chi_1", "chi_2"):
+        loud[k] = np.full(64, float(w.injection.get(k, 0.0)))
+    p = {k: np.concatenate([np.asarray(p[k], dtype=np.float64), loud[k] if k in loud else p[k][:64]]) for k in p}
+    pts = marginalized_points(p, priors, "tpd", p["time_jitter"])
+    fp64 = like.log_likelihood_ratio_batch(pts, precision="fp64")
+    mixed = like.log_likelihood_ratio_batch(pts, precision="mixed")
+    refined = like.analysis.last_refined()
+    assert np.all(np.isfinite(fp64))
+    err = np.abs(mixed - fp64)
+    assert np.all(err <= 1e-3), (err.max(), int(np.argmax(err)), refined)
+
+
 def test_time_marginalized_with_many_nodes(gpu, tmp_path):
     """300 linear nodes: the nodes and each chunk's weight rows take more than
     48 KB of shared memory together with the kernel's static arrays."""
