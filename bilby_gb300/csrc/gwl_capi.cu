@@ -372,6 +372,15 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.nx = a->nx;
   L.ny = a->ny;
   for (int q = 0; q < 4; ++q) L.bbox[q] = a->bbox[q];
+  {
+    // the x bounds as float32 that give the same test of a float32 x:
+    // bbox[0] rounded up, bbox[1] rounded down
+    float lo = (float)a->bbox[0], hi = (float)a->bbox[1];
+    if ((double)lo < a->bbox[0]) lo = std::nextafter(lo, INFINITY);
+    if ((double)hi > a->bbox[1]) hi = std::nextafter(hi, -INFINITY);
+    L.bbox_x_f[0] = lo;
+    L.bbox_x_f[1] = hi;
+  }
   L.ref_dist = a->ref_dist;
   L.tm_step = a->duration / (double)(a->n_bins - 1);  // linspace(0, T, L + 1) spacing, L = n_bins - 1
   L.tm_inv_step = (double)(a->n_bins - 1) / a->duration;
@@ -788,6 +797,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
       GWL_CUDA(launch_mixed(P, s));
     }
     GWL_CUDA(launch_time_marginalized(L, s));
+    if (marks) GWL_CUDA(launch_time_marg_marks(L, s));
     if (marks && (rc = launch_window_refine(a, L, s, share))) return rc;
     if (a->profiling) {
       GWL_CUDA(cudaEventRecord(a->ev_end, s));

@@ -58,6 +58,15 @@ struct PointRec {
   int64_t k_start, k_end;            // TaylorF2 band [k_start, k_end) on the analysis grid
   int32_t valid;                     // 0: waveform undefined (lnL = nan_to_num(-inf))
   int32_t refine;                    // TaylorF2 mixed: error bound above the tolerance (LaunchArgs::rf_tol)
+  // mixed time-marginalised kernel over the full grid (k_time_marg): per-point
+  // scalars from the float64 prologue, so that the kernel runs no float64 per
+  // point before its transform nor per time sample
+  float tm_coef[2 * kMaxDet];        // detector response coefficients of the integrand
+  double tm_hh;                      // TaylorF2 <h|h>
+  int64_t tm_j0, tm_j1;              // FFT indices of the first and last time sample inside the prior
+  int32_t tm_row_ly, tm_row_in;      // TaylorF2 with the distance table: the spline's row at this <h|h>
+  float tm_row_hy[4];                // (SplineRowF: interval, inside the table, basis values)
+  float tm_xp, tm_zs;                // the kernel's largest |X| over the window and ||z||_2, for the error bound
 };
 
 // Relative binning, per grid index: its bin and the offset of its frequency
@@ -136,6 +145,8 @@ struct LaunchArgs {
   int64_t n_fft;                        // time-marginalisation FFT length (n_bins - 1)
   const double* tx; const double* ty; const double* tc;  // distance spline
   const float* tx_f; const float* ty_f; const float* tc_f; // float32 copy (mixed precision)
+  float bbox_x_f[2];                    // bbox[0] rounded up and bbox[1] rounded down to float32: the same
+                                        // test of a float32 x as against the float64 bounds
   int nx, ny;
   double bbox[4];
   double ref_dist;
@@ -309,6 +320,9 @@ void order_layout(int64_t n_chunks, int* keys, int* shift);
 void ordering_with_marks(LaunchArgs& L);
 void ordering_by_peak(LaunchArgs& L);
 cudaError_t launch_time_marginalized(const LaunchArgs& a, cudaStream_t s);
+// The mixed full-grid time-marginalised kernel's error bounds, from what it
+// stored in the point records: marks the points over the tolerance.
+cudaError_t launch_time_marg_marks(const LaunchArgs& a, cudaStream_t s);
 // Relative binning / multi-banding with time marginalisation by the windowed
 // four-step transform (gwl_marg_window.cu): whether this launch's shared
 // memory fits, and the launch (mixed precision: relative binning only).

@@ -14,6 +14,7 @@
 
 #include "gwl_device.cuh"
 #include "gwl_internal.h"
+#include "gwl_marg_common.cuh"
 #include "gwl_math.cuh"
 #include "gwl_phase.cuh"
 
@@ -185,6 +186,51 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
       atomicAdd(a.rf_count, 1);
       if (a.rf_total) atomicAdd(a.rf_total, 1);
     }
+  }
+  if (a.time_marg && a.precision == GWL_PRECISION_MIXED && a.n_fft > 0 && !a.relbin && !a.mb_tm && !a.roq) {
+    // the mixed full-grid time-marginalised kernel's per-point scalars:
+    // integrand coefficients, the TaylorF2 <h|h> and the exact sample window
+    const double norm = 4.0 / a.duration;
+    double hh = 0.0;
+    for (int d = 0; d < a.n_det; ++d) {
+      if (a.model == GWL_MODEL_TAYLORF2) {
+        const double ci = r.cos_i;
+        const double s = norm * r.amp * a.w_scale[d];
+        r.tm_coef[2 * d] = (float)(s * r.fp[d] * (1.0 + ci * ci) / 2.0);
+        r.tm_coef[2 * d + 1] = (float)(-s * r.fx[d] * ci);
+        const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
+        const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
+        hh += norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
+      } else {
+        r.tm_coef[2 * d] = (float)(norm * a.w_scale[d] * r.fp[d] * r.amp);
+        r.tm_coef[2 * d + 1] = (float)(norm * a.w_scale[d] * r.fx[d] * r.amp2);
+      }
+    }
+    r.tm_hh = hh;
+    if (a.model == GWL_MODEL_TAYLORF2 && a.dist_marg) {
+      // the distance spline's row at this point's <h|h> (base.py:775-784)
+      const double sr = r.dist * a.inv_ref_dist;
+      const SplineRowF row = bicubic_row_f(a.ty_f, a.ny, a.bbox, (float)(hh * sr * sr));
+      r.tm_row_ly = row.Ly;
+      r.tm_row_in = row.inside;
+      for (int q = 0; q < 4; ++q) r.tm_row_hy[q] = row.hy[q];
+    }
+    // samples j with t_j = start + (j + 1) T / L + jitter inside [t_min, t_max]
+    // (base.py:1027-1035), tested as the float64 kernel tests them; t_j
+    // increases with j
+    const int64_t L = a.n_fft;
+    int64_t lo = 0, hi = L;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (tm_sample_time(a, mid, L, a.tm_step, r.jitter) >= a.t_min) hi = mid; else lo = mid + 1;
+    }
+    int64_t lo2 = lo, hi2 = L;
+    while (lo2 < hi2) {
+      const int64_t mid = (lo2 + hi2) / 2;
+      if (tm_sample_time(a, mid, L, a.tm_step, r.jitter) <= a.t_max) lo2 = mid + 1; else hi2 = mid;
+    }
+    r.tm_j0 = lo;
+    r.tm_j1 = lo2 - 1;
   }
   a.rec[i] = r;
   if (a.order_hist) atomicAdd(&a.order_hist[order_key(a, r)], 1);

@@ -42,9 +42,10 @@ constexpr int kTmTwiddleRows = 128;
 // per-bin errors and the float32 transform's rounding as ||z||_2 where the
 // outputs are noise, the transform's coherent rounding as |X| at a peak.
 // Measured on tf2_marg_8s (8192 prior draws and loud templates at 20-800 Mpc
-// with |X| up to 3e4): |dX| <= 2e-6 ||z||_2 + 1.3e-7 |X|max.
+// with |X| up to 3e4): |dX| <= 2e-6 ||z||_2 + 1.3e-7 |X|max; the per-sample
+// lnL in float32 adds one rounding of about 6e-8 |X|.
 constexpr double kTmErrNorm = 2e-6;
-constexpr double kTmErrPeak = 2.5e-7;
+constexpr double kTmErrPeak = 3e-7;
 
 // Block-wide reductions over kTmThreads threads in a fixed tree order.
 __device__ double block_max(double v, double* red) {
@@ -159,20 +160,8 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     double hh_part = 0.0;
     float z2 = 0.f;  // mixed TaylorF2: sum of |z_k|^2 over this thread's bins (error bound)
     if constexpr (MIXED) {
-      // per-point float32 coefficients, computed once (float64 issues slowly) and shared
-      if (threadIdx.x == 0) {
-        for (int d = 0; d < D; ++d) {
-          if (a.model == GWL_MODEL_TAYLORF2) {
-            const double ci = r.cos_i;
-            const double s = norm * r.amp * a.w_scale[d];
-            s_coef[2 * d] = (float)(s * r.fp[d] * (1.0 + ci * ci) / 2.0);
-            s_coef[2 * d + 1] = (float)(-s * r.fx[d] * ci);
-          } else {
-            s_coef[2 * d] = (float)(norm * a.w_scale[d] * r.fp[d] * r.amp);
-            s_coef[2 * d + 1] = (float)(norm * a.w_scale[d] * r.fx[d] * r.amp2);
-          }
-        }
-      }
+      // per-point float32 coefficients, computed by the float64 prologue
+      if (threadIdx.x < 2 * D) s_coef[threadIdx.x] = r.tm_coef[threadIdx.x];
       __syncthreads();
       float gre[D], gim[D], cre[D], cim[D];
       uint32_t xl[D], xh[D];
@@ -201,16 +190,22 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         const int lr = log2N - 4;
         const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
         const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
+        // ceil(x / R) for 0 < x < 2^32 (R = m_odd 2^lr: a shift when m_odd = 1),
+        // in 32-bit arithmetic
+        const auto cdiv_R = [&](int64_t x) -> int {
+          const uint32_t n = (uint32_t)x + (uint32_t)R - 1u;
+          return (int)(m_odd == 1 ? n >> lr : n / (uint32_t)R);
+        };
         for (int64_t bb = threadIdx.x; bb < R; bb += blockDim.x) {
           // block bb / R2 of the m_odd transforms: bins q + j L / 16 with
-          // q = (bb / R2) + m_odd bitrev(bb mod R2)
-          const int64_t q = bb / R2 + m_odd * (int64_t)bit_reverse((uint32_t)(bb % R2), lr);
+          // q = (bb / R2) + m_odd bitrev(bb mod R2), R2 = 2^lr
+          const int64_t q = (bb >> lr) + m_odd * (int64_t)bit_reverse((uint32_t)(bb & (R2 - 1)), lr);
           float yr[16], yi[16];
 #pragma unroll
           for (int v = 0; v < 16; ++v) yr[v] = yi[v] = 0.f;
           // in-band j: ks <= q + j R < ke
-          const int j0 = r.valid ? (int)max((int64_t)0, (ks - q + R - 1) / R) : 16;
-          const int j1 = r.valid ? (int)min((int64_t)16, (ke - q + R - 1) / R) : 0;
+          const int j0 = r.valid ? (ks > q ? cdiv_R(ks - q) : 0) : 16;
+          const int j1 = r.valid ? (ke > q ? min(16, cdiv_R(ke - q)) : 0) : 0;
           for (int j = j0; j < j1; ++j) {
             const int64_t k = q + (int64_t)j * R;
             float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
@@ -427,13 +422,10 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
     }
     if (MIXED && threadIdx.x == 0) {
-      // this point's candidate window of FFT indices (checked exactly in C):
-      // the last FFT stages compute only the outputs inside it
-      const double jit = r.jitter;
-      const double jl = floor((a.t_min - a.start_time0 - jit) * a.tm_inv_step) - 3.0;
-      const double jh = ceil((a.t_max - a.start_time0 - jit) * a.tm_inv_step) + 2.0;
-      s_jr[0] = (long long)fmax(0.0, jl);
-      s_jr[1] = (long long)fmin((double)(L - 1), jh);
+      // this point's window of FFT indices inside the prior (exact, from the
+      // prologue): the last FFT stages compute only the outputs inside it
+      s_jr[0] = r.tm_j0;
+      s_jr[1] = r.tm_j1;
     }
     __syncthreads();
     // ---- B: in-place FFT, radix-4 passes (two radix-2 stages each) -------
@@ -473,7 +465,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
 #pragma unroll
           for (int j = 0; j < RB; ++j) {
             // exp(-2 pi i (pos + m h0) L / (2 h0 2^j) / L) = tw(pos stride) * exp(-2 pi i m / 2^(j+1))
-            const int64_t stride = L / (2 * (h0 << j));
+            const int64_t stride = L >> (stage + j);  // L / (2 h0 2^j), L = m_odd 2^log2N
             C w[MIXED ? 8 : 1];
             if constexpr (MIXED) {
               const C w0 = tw(pos * stride);
@@ -515,7 +507,10 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       const bool prune = MIXED && stage + 1 == log2N && n_win > 0 && n_win <= h;
       const int64_t n_bf = prune ? n_win * m_odd : L / 4;
       for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
-        const int64_t bf = prune ? ((t / n_win) * h + ((s_jr[0] + t % n_win) & (h - 1))) : t;
+        // pruned: butterfly (s_jr[0] + t mod n_win) mod h of transform t / n_win (32-bit division, none for m_odd = 1)
+        const uint32_t tq = (prune && m_odd != 1) ? (uint32_t)t / (uint32_t)n_win : 0u;
+        const int64_t tr_ = prune ? (int64_t)((uint32_t)t - tq * (uint32_t)n_win) : 0;
+        const int64_t bf = prune ? ((int64_t)tq * h + ((s_jr[0] + tr_) & (h - 1))) : t;
         const int64_t pos = bf & (h - 1);
         const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
         const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
@@ -542,8 +537,11 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       const bool prune = MIXED && n_win > 0 && n_win <= h;  // only the window's butterflies
       const int64_t n_bf = prune ? n_win * m_odd : L / 2;
       for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
-        const int64_t l = prune ? ((s_jr[0] + t % n_win) & (h - 1)) : t % h;
-        const int64_t q = (prune ? t / n_win : t / h) * N2 + l;
+        // t / n_win (pruned, 32-bit; none for m_odd = 1) or t / h (h = 2^(log2N - 1))
+        const uint32_t tq = prune ? (m_odd == 1 ? 0u : (uint32_t)t / (uint32_t)n_win) : (uint32_t)(t >> (log2N - 1));
+        // (prune implies n_win > 0)
+        const int64_t l = prune ? ((s_jr[0] + (int64_t)((uint32_t)t - tq * (uint32_t)n_win)) & (h - 1)) : (t & (h - 1));
+        const int64_t q = (int64_t)tq * N2 + l;
         const C w = tw(l * m_odd);
         const C x0 = buf[P(q)], x1 = buf[P(q + h)];
         const R tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
@@ -571,22 +569,12 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
     }
     const double jit = r.jitter;
-    // per-point scalars, computed once (float64 issues slowly) and shared
-    if (MIXED && a.model == GWL_MODEL_TAYLORF2 && threadIdx.x < D) {
-      // <h|h> of detector d from the prefix sums, one thread per detector
-      const int d = threadIdx.x;
-      const double ci = r.cos_i;
-      const double qr = r.fp[d] * (1.0 + ci * ci) / 2.0, qi = -r.fx[d] * ci;
-      const int64_t k1 = min(r.k_end, a.n_bins), k0 = min(r.k_start, k1);
-      red[d] = norm * r.amp * r.amp * (qr * qr + qi * qi) * (a.hh_prefix[d][k1] - a.hh_prefix[d][k0]);
-    }
-    if (MIXED && a.model == GWL_MODEL_TAYLORF2) __syncthreads();
+    // per-point scalars: the TaylorF2 <h|h> from the prologue
+    if (MIXED && a.model == GWL_MODEL_TAYLORF2) hh = r.tm_hh;
     if (MIXED && (threadIdx.x == 0 || threadIdx.x == 32)) {
       // the divisions precomputed on the host (LaunchArgs::tm_step ...);
-      // thread 0 the scalars and the window, thread 32 (another warp) the
-      // distance spline's row at this point's <h|h>, at the same time
-      if (a.model == GWL_MODEL_TAYLORF2)
-        for (int d = 0; d < D; ++d) hh += red[d];
+      // thread 0 the scalars, thread 32 (another warp) the distance spline's
+      // row at this point's <h|h>, at the same time
       const double sr = r.dist * a.inv_ref_dist;
       const double hh_ref = hh * sr * sr;
       if (threadIdx.x == 0) {
@@ -595,9 +583,15 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         s_scal[2] = sr;
         s_scal[3] = a.tm_step;
         s_scal[4] = a.tm_prob;
-        // the candidate window (s_jr) was set before the FFT
+        // the window (s_jr) was set before the FFT
       } else if (a.dist_marg) {
-        s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)hh_ref);
+        if (a.model == GWL_MODEL_TAYLORF2) {  // computed by the prologue
+          s_row.Ly = r.tm_row_ly;
+          s_row.inside = r.tm_row_in;
+          for (int q = 0; q < 4; ++q) s_row.hy[q] = r.tm_row_hy[q];
+        } else {
+          s_row = bicubic_row_f(s_ty, a.ny, a.bbox, (float)hh_ref);
+        }
       }
     }
     if (!MIXED && threadIdx.x == 0) {
@@ -620,19 +614,47 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     // one pass: running (max, sum of exp(l - max)) per thread, then a fixed-order block combination
     double m = -INFINITY, acc = 0.0;
     float xmax = 0.f;  // mixed: the largest |X| over this thread's samples (error bound)
-    for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
-      const double t = tm_sample_time(a, j, L, step, jit);
-      double lw;
-      if (!tm_log_weight<MIXED>(a, t, lw)) continue;
-      const C x = out_at(buf, j);
-      double l;
-      if constexpr (MIXED) {
-        l = tm_lnl_mixed(a, x.x, x.y, hh, sr, s_tx, s_row);
-        xmax = fmaxf(xmax, sqrtf(x.x * x.x + x.y * x.y));
-      } else {
-        l = tm_lnl_fp64(a, x.x, x.y, hh, hh_ref, sr);
+    float mf32 = -INFINITY, acc32 = 0.f;  // mixed: the same in float32, without the point's constant -<h|h>/2
+    if constexpr (MIXED) {
+      // every sample of [j_lo, j_hi] is inside the prior; the per-sample lnL
+      // without the constant term (-<h|h>/2 unless the distance table holds
+      // it), in float32 throughout
+      const float srf = (float)sr;
+      for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
+        float lw = 0.f;
+        if (a.tm_prior) {
+          const float pw = tm_prior_density_f(a, tm_sample_time(a, j, L, step, jit));  // base.py:807, prior(t_j)
+          if (!(pw > 0.f)) continue;
+          lw = __logf(pw);
+        }
+        const C x = out_at(buf, j);
+        const float ax = sqrtf(x.x * x.x + x.y * x.y);
+        float l;
+        if (a.dist_marg) {
+          l = bicubic_eval_row_ff(s_tx, a.nx, a.ny, a.tc_f, a.bbox_x_f, (a.phase_marg ? ax : x.x) * srf, s_row);
+        } else if (a.phase_marg) {
+          l = ax + ln_i0_minus_x(ax);
+        } else {
+          l = x.x;
+        }
+        l += lw;
+        xmax = fmaxf(xmax, ax);
+        if (l > mf32) {
+          acc32 = mf32 > -INFINITY ? acc32 * __expf(mf32 - l) + 1.f : 1.f;
+          mf32 = l;
+        } else if (isfinite(l)) {
+          acc32 += __expf(l - mf32);
+        }
       }
-      tm_lse_push<MIXED>(l + lw, m, acc);
+    } else {
+      for (int64_t j = j_lo + threadIdx.x; j <= j_hi; j += blockDim.x) {
+        const double t = tm_sample_time(a, j, L, step, jit);
+        double lw;
+        if (!tm_log_weight<MIXED>(a, t, lw)) continue;
+        const C x = out_at(buf, j);
+        const double l = tm_lnl_fp64(a, x.x, x.y, hh, hh_ref, sr);
+        tm_lse_push<MIXED>(l + lw, m, acc);
+      }
     }
     // combine (m, acc) pairs over the block in a fixed order
     double* redm = red;
@@ -642,7 +664,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       // near the maximum serves), then sum acc_t exp(m_t - M) in float32; both
       // by xor-shuffles within warps and a fixed-order sum of the 16 warps
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      float mf = (float)m, zz = z2, xm = xmax;
+      float mf = mf32, zz = z2, xm = xmax;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
@@ -659,7 +681,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       float M = redf[0];
       for (int w = 1; w < kTmThreads / 32; ++w) M = fmaxf(M, redf[w]);
       float sm = 0.f;
-      if (isfinite(M) && isfinite(m)) sm = (float)acc * __expf((float)(m - (double)M));
+      if (isfinite(M) && isfinite(mf32)) sm = acc32 * __expf(mf32 - M);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
       __syncthreads();
@@ -696,7 +718,10 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       }
     }
     if (threadIdx.x == 0) {
-      const double amax = redm[0], total = reds[0] * (a.tm_prior ? 1.0 : prob) * a.delta_tc;
+      // mixed: the maximum is of the per-sample lnL without the point's
+      // constant, added here in float64
+      const double c0 = MIXED && !a.dist_marg ? -hh / 2 : 0.0;
+      const double amax = redm[0] + c0, total = reds[0] * (a.tm_prior ? 1.0 : prob) * a.delta_tc;
       double lnl;
       if (!r.valid) lnl = -1.7976931348623157e308;
       else if (!isfinite(amax)) lnl = amax;
@@ -704,17 +729,43 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
       else lnl = amax + (MIXED ? (double)logf((float)total) : log(total));
       a.out[i] = lnl;
       if (MIXED && a.model == GWL_MODEL_TAYLORF2 && a.rf_tol > 0 && a.rf_count && a.rf_list && r.valid) {
-        // |dlnL| <= s (kTmErrNorm ||z||_2 + kTmErrPeak max|X|): points over the
-        // tolerance are listed for the float64 recomputation
-        const double err = tm_sensitivity(a, redm[2], sr, s_tx, s_row) * (kTmErrNorm * redm[1] + kTmErrPeak * redm[2]);
-        if (!(err <= a.rf_tol)) {
-          a.rec[i].refine = 1;
-          a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
-        }
+        // the error bound's inputs, for k_tm_marks (so that no thread of this
+        // CTA holds the others up with the distance table's sensitivity)
+        a.rec[i].tm_xp = (float)redm[2];
+        a.rec[i].tm_zs = (float)redm[1];
       }
     }
     __syncthreads();
   }
+}
+
+// The mixed full-grid kernel's error bounds, one thread per point:
+// |dlnL| <= s (kTmErrNorm ||z||_2 + kTmErrPeak max|X|), s the distance table's
+// sensitivity at the window's peak (tm_sensitivity); points over the
+// tolerance are listed for the float64 recomputation.
+__global__ void k_tm_marks(LaunchArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.B) return;
+  const PointRec& r = a.rec[i];
+  if (!r.valid) return;
+  SplineRowF row;
+  row.Ly = r.tm_row_ly;
+  row.inside = r.tm_row_in;
+  for (int q = 0; q < 4; ++q) row.hy[q] = r.tm_row_hy[q];
+  const double xp = (double)r.tm_xp, sr = r.dist * a.inv_ref_dist;
+  const double err = tm_sensitivity(a, xp, sr, a.tx_f, row) * (kTmErrNorm * (double)r.tm_zs + kTmErrPeak * xp);
+  if (!(err <= a.rf_tol)) {
+    a.rec[i].refine = 1;
+    a.rf_list[atomicAdd(a.rf_count, 1)] = (int32_t)i;
+  }
+}
+
+cudaError_t launch_time_marg_marks(const LaunchArgs& a, cudaStream_t s) {
+  if (a.precision != GWL_PRECISION_MIXED || a.model != GWL_MODEL_TAYLORF2 || !(a.rf_tol > 0) || !a.rf_count ||
+      !a.rf_list || a.B <= 0)
+    return cudaSuccess;
+  k_tm_marks<<<(unsigned)((a.B + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

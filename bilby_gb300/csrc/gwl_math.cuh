@@ -173,9 +173,32 @@ __device__ inline SplineRowF bicubic_row_f(const float* ty, int ny, const double
   return row;
 }
 
+// ... with the table's x bounds as float32 (bx[0] = bbox[0] rounded up,
+// bx[1] = bbox[1] rounded down, so that the test of a float32 x is the same
+// as against the float64 bounds, without float64 arithmetic)
+__device__ inline float bicubic_eval_row_ff(const float* tx, int nx, int ny, const float* c, const float* bx, float x,
+                                            const SplineRowF& row);
+
 __device__ inline float bicubic_eval_row_f(const float* tx, int nx, int ny, const float* c, const double* bbox,
                                            float x, const SplineRowF& row) {
   if (!((double)x >= bbox[0] && (double)x <= bbox[1] && row.inside)) return -INFINITY;
+  const int Lx = bspline_interval_f(tx, nx, 3, x);
+  float hx[4];
+  bspline_values_f(tx, 3, x, Lx, hx);
+  const int ncy = ny - 4;
+  float s = 0.0f;
+  for (int i = 0; i < 4; ++i) {
+    const float* rowc = c + (size_t)(Lx - 3 + i) * ncy + (row.Ly - 3);
+    float r = 0.0f;
+    for (int j = 0; j < 4; ++j) r += rowc[j] * row.hy[j];
+    s += r * hx[i];
+  }
+  return s;
+}
+
+__device__ inline float bicubic_eval_row_ff(const float* tx, int nx, int ny, const float* c, const float* bx, float x,
+                                            const SplineRowF& row) {
+  if (!(x >= bx[0] && x <= bx[1] && row.inside)) return -INFINITY;
   const int Lx = bspline_interval_f(tx, nx, 3, x);
   float hx[4];
   bspline_values_f(tx, 3, x, Lx, hx);
