@@ -739,6 +739,319 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed TaylorF2 time marginalisation in two half-length transforms.  With
+// L = 2 M (M a power of two, at least 32), X[j] = E[j mod M] +
+// e^{-2 pi i j / L} O[j mod M], E and O the length-M transforms of the even
+// and the odd bins (the last radix-2 stage of a decimation in time).  One CTA
+// of 256 threads per point runs E, keeps its values at the prior window's
+// samples, then O in the same shared buffer, and combines them there: the
+// buffer is half of k_time_marg's, so two CTAs (two points, each in its own
+// phase of the work) share an SM.  Each half runs as k_time_marg<D, true>
+// runs its transform: the integrand fused with the first four stages, radix-16
+// passes in registers, the last passes only for the window's outputs; then
+// the window in float32 and the error bound's inputs, as there.
+// ---------------------------------------------------------------------------
+constexpr int kTmHalfThreads = 256;
+
+template <int D>
+__global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, const float2* twiddle, int log2L,
+                                                               int n_win_cap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float s_coef[2 * kMaxDet];
+  __shared__ SplineRowF s_row;
+  __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
+  __shared__ float2 s_w16[16];
+  constexpr int W = kTmHalfThreads / 32;
+  __shared__ float redf[4 * W];
+  __shared__ double s_lnl[2];
+  const int64_t L = a.n_fft, M = L >> 1;
+  const int lM = log2L - 1;
+  for (int q = threadIdx.x; q < kTmTwiddleRows; q += blockDim.x) {
+    const int64_t qh = (int64_t)q * kTmTwiddleRows;
+    tw_hi[q] = qh < M ? twiddle[qh] : make_float2(1.f, 0.f);
+    tw_lo[q] = q < M ? twiddle[q] : make_float2(1.f, 0.f);
+  }
+  if (threadIdx.x < 8) {  // the 16th roots of unity exp(-2 pi i m / 16)
+    const float2 t = twiddle[(int64_t)threadIdx.x * (L / 16)];
+    s_w16[threadIdx.x] = t;
+    s_w16[threadIdx.x + 8] = make_float2(-t.x, -t.y);
+  }
+  float2* buf = reinterpret_cast<float2*>(smem);  // [M + M / 16], padded every 16
+  float2* s_ew = buf + (M + (M >> 4));            // [n_win_cap] the window's values
+  float* s_tx = reinterpret_cast<float*>(s_ew + n_win_cap);
+  float* s_ty = s_tx + a.nx;
+  if (a.dist_marg) {
+    for (int q = threadIdx.x; q < a.nx; q += blockDim.x) s_tx[q] = a.tx_f[q];
+    for (int q = threadIdx.x; q < a.ny; q += blockDim.x) s_ty[q] = a.ty_f[q];
+  }
+  __syncthreads();
+  // exp(-2 pi i q / L), q < L / 2, from the two tables
+  const auto tw = [&](int64_t q) -> float2 {
+    const float2 h = tw_hi[q / kTmTwiddleRows], l = tw_lo[q % kTmTwiddleRows];
+    return make_float2(h.x * l.x - h.y * l.y, h.x * l.y + h.y * l.x);
+  };
+  const auto P = [](int64_t q) -> int64_t { return q + (q >> 4); };
+  const float4* basis4 = reinterpret_cast<const float4*>(a.basis);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t i = blockIdx.x; i < a.B; i += gridDim.x) {
+    const PointRec& r = a.rec[i];
+    if (threadIdx.x < 2 * D) s_coef[threadIdx.x] = r.tm_coef[threadIdx.x];
+    const int64_t j_lo = r.tm_j0;
+    int64_t n_win = r.tm_j1 - r.tm_j0 + 1;
+    if (n_win > n_win_cap) {  // cannot happen: the host sizes the window from the prior's width
+      if (threadIdx.x == 0 && a.status) atomicExch(a.status, kDevStatusBadInput);
+      n_win = n_win_cap;
+    }
+    __syncthreads();
+    float gre[D], gim[D];
+    uint32_t xl[D], xh[D];
+    float ch[kNumBasis + 1], cl[kNumBasis + 1];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      xl[d] = r.xfix[d][0];
+      xh[d] = r.xfix[d][1];
+      gre[d] = s_coef[2 * d];
+      gim[d] = s_coef[2 * d + 1];
+    }
+#pragma unroll
+    for (int b = 0; b <= kNumBasis; ++b) {
+      ch[b] = r.c_hi[b];
+      cl[b] = r.c_lo[b];
+    }
+    const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
+    float z2 = 0.f;  // sum of |z_k|^2 over this thread's bins (error bound)
+    for (int par = 0; par < 2; ++par) {
+      // ---- A: bins k = 2 k' + par, fused with the first four stages: after
+      // them positions 16 b .. 16 b + 15 hold the 16-point DFT of the bins
+      // k' = q + j M / 16 (j < 16), q = bitrev(b) over log2(M) - 4 bits
+      const int64_t R = M >> 4;
+      const int lr = lM - 4;
+      const int64_t ka = (ks - par + 1) >> 1, kb = (ke - par + 1) >> 1;  // in-band k' in [ka, kb)
+      for (int64_t bb = threadIdx.x; bb < R; bb += blockDim.x) {
+        const int64_t q = (int64_t)bit_reverse((uint32_t)bb, lr);
+        float yr[16], yi[16];
+#pragma unroll
+        for (int v = 0; v < 16; ++v) yr[v] = yi[v] = 0.f;
+        const int j0 = r.valid ? (ka > q ? (int)(((uint32_t)(ka - q) + (uint32_t)R - 1u) >> lr) : 0) : 16;
+        const int j1 = r.valid ? (kb > q ? min(16, (int)(((uint32_t)(kb - q) + (uint32_t)R - 1u) >> lr)) : 0) : 0;
+        for (int j = j0; j < j1; ++j) {
+          const int64_t k = 2 * (q + (int64_t)j * R) + par;
+          float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
+#pragma unroll
+          for (int qq = 0; qq < kNumBasis / 2; ++qq) {
+            const float4 v = __ldg(basis4 + k * (kNumBasis / 2) + qq);
+            ff_mac(s_hi, s_lo, ch[2 * qq], cl[2 * qq], v.x, v.y);
+            ff_mac(s_hi, s_lo, ch[2 * qq + 1], cl[2 * qq + 1], v.z, v.w);
+          }
+          const float base = __fadd_rn(__fsub_rn(s_hi, rintf(s_hi)), s_lo);
+          float zr = 0.f, zi = 0.f;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const uint32_t top = (uint32_t)k * xh[d] + __umulhi((uint32_t)k, xl[d]);
+            float ph = base + __int2float_rn((int)top) * 2.3283064365386963e-10f;
+            ph -= rintf(ph);
+            float sn, cs;
+            __sincosf(ph * 6.283185307179586f, &sn, &cs);
+            const float2 w = __ldg(a.w[d] + k);
+            const float er = w.x * cs - w.y * sn, ei = w.x * sn + w.y * cs;
+            // h conj(d) / S = G conj(e^{i Phi} w)
+            zr += gre[d] * er + gim[d] * ei;
+            zi += gim[d] * er - gre[d] * ei;
+          }
+          z2 += zr * zr + zi * zi;
+#pragma unroll
+          for (int v = 0; v < 16; ++v) {
+            const float2 t = s_w16[(j * v) & 15];
+            yr[v] += zr * t.x - zi * t.y;
+            yi[v] += zr * t.y + zi * t.x;
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 16; ++v) buf[P(16 * bb + v)] = make_float2(yr[v], yi[v]);
+      }
+      __syncthreads();
+      // ---- B: stages 5 .. log2(M); a stage of half-length h has twiddles
+      // exp(-2 pi i pos / (2 h)) = tw(pos L / (2 h))
+      int stage = 5;
+      for (; stage + 3 <= lM; stage += 4) {
+        const int64_t h0 = (int64_t)1 << (stage - 1);
+        for (int64_t gi = threadIdx.x; gi < (M >> 4); gi += blockDim.x) {
+          const int64_t pos = gi & (h0 - 1);
+          const int64_t b0 = ((gi >> (stage - 1)) << (stage + 3)) + pos;
+          float2 x[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) x[k] = buf[P(b0 + k * h0)];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float2 w0 = tw(pos * (L >> (stage + j)));
+            float2 w[8];
+            w[0] = w0;
+#pragma unroll
+            for (int m = 1; m < (1 << j); ++m) {
+              const float2 u = s_w16[m << (3 - j)];
+              w[m] = make_float2(w0.x * u.x - w0.y * u.y, w0.x * u.y + w0.y * u.x);
+            }
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              if (k & (1 << j)) continue;
+              const int k2 = k | (1 << j);
+              const float2 ww = w[k & ((1 << j) - 1)];
+              const float tr = ww.x * x[k2].x - ww.y * x[k2].y, ti = ww.x * x[k2].y + ww.y * x[k2].x;
+              x[k2].x = x[k].x - tr;
+              x[k2].y = x[k].y - ti;
+              x[k].x = x[k].x + tr;
+              x[k].y = x[k].y + ti;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 16; ++k) buf[P(b0 + k * h0)] = x[k];
+        }
+        __syncthreads();
+      }
+      for (; stage < lM; stage += 2) {
+        const int64_t h = (int64_t)1 << (stage - 1);
+        const int64_t s1 = L >> stage, s2 = L >> (stage + 1);  // L / (2 h), L / (4 h)
+        // the last two stages: output j comes from the butterfly at j mod h alone
+        const bool prune = stage + 1 == lM && n_win > 0 && n_win <= h;
+        const int64_t n_bf = prune ? n_win : (M >> 2);
+        for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
+          const int64_t bf = prune ? ((j_lo + t) & (h - 1)) : t;
+          const int64_t pos = bf & (h - 1);
+          const int64_t i0 = ((bf >> (stage - 1)) << (stage + 1)) + pos;
+          const int64_t i1 = i0 + h, i2 = i0 + 2 * h, i3 = i0 + 3 * h;
+          const float2 w1 = tw(pos * s1), w2 = tw(pos * s2), w3 = tw((pos + h) * s2);
+          const float2 x0 = buf[P(i0)], x1 = buf[P(i1)], x2 = buf[P(i2)], x3 = buf[P(i3)];
+          float2 a0, a1, a2, a3, y0, y1, y2, y3;
+          float tr = w1.x * x1.x - w1.y * x1.y, ti = w1.x * x1.y + w1.y * x1.x;
+          a0.x = x0.x + tr; a0.y = x0.y + ti; a1.x = x0.x - tr; a1.y = x0.y - ti;
+          tr = w1.x * x3.x - w1.y * x3.y; ti = w1.x * x3.y + w1.y * x3.x;
+          a2.x = x2.x + tr; a2.y = x2.y + ti; a3.x = x2.x - tr; a3.y = x2.y - ti;
+          tr = w2.x * a2.x - w2.y * a2.y; ti = w2.x * a2.y + w2.y * a2.x;
+          y0.x = a0.x + tr; y0.y = a0.y + ti; y2.x = a0.x - tr; y2.y = a0.y - ti;
+          tr = w3.x * a3.x - w3.y * a3.y; ti = w3.x * a3.y + w3.y * a3.x;
+          y1.x = a1.x + tr; y1.y = a1.y + ti; y3.x = a1.x - tr; y3.y = a1.y - ti;
+          buf[P(i0)] = y0;
+          buf[P(i1)] = y1;
+          buf[P(i2)] = y2;
+          buf[P(i3)] = y3;
+        }
+        __syncthreads();
+      }
+      if (stage == lM) {  // a last radix-2 stage, half-length M / 2, twiddle exp(-2 pi i l / M) = tw(2 l)
+        const int64_t h = M >> 1;
+        const bool prune = n_win > 0 && n_win <= h;
+        const int64_t n_bf = prune ? n_win : h;
+        for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
+          const int64_t l = prune ? ((j_lo + t) & (h - 1)) : t;
+          const float2 w = tw(2 * l);
+          const float2 x0 = buf[P(l)], x1 = buf[P(l + h)];
+          const float tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
+          buf[P(l)] = make_float2(x0.x + tr, x0.y + ti);
+          buf[P(l + h)] = make_float2(x0.x - tr, x0.y - ti);
+        }
+        __syncthreads();
+      }
+      // the window's values: E kept, then X = E + exp(-2 pi i j / L) O
+      for (int64_t t = threadIdx.x; t < n_win; t += blockDim.x) {
+        const int64_t j = j_lo + t;
+        const float2 v = buf[P(j & (M - 1))];
+        if (par == 0) {
+          s_ew[t] = v;
+        } else {
+          float2 w = j < M ? tw(j) : tw(j - M);
+          if (j >= M) w = make_float2(-w.x, -w.y);
+          const float2 e = s_ew[t];
+          s_ew[t] = make_float2(e.x + (w.x * v.x - w.y * v.y), e.y + (w.x * v.y + w.y * v.x));
+        }
+      }
+      __syncthreads();
+    }
+    // ---- C: the prior window, per sample in float32 without the point's
+    // constant -<h|h>/2 (added once at the end), and a logsumexp
+    const double hh = r.tm_hh, sr = r.dist * a.inv_ref_dist;
+    if (a.dist_marg && threadIdx.x == 0) {
+      s_row.Ly = r.tm_row_ly;
+      s_row.inside = r.tm_row_in;
+      for (int q = 0; q < 4; ++q) s_row.hy[q] = r.tm_row_hy[q];
+    }
+    __syncthreads();
+    const float srf = (float)sr;
+    const double jit = r.jitter, step = a.tm_step;
+    float mf32 = -INFINITY, acc32 = 0.f, xmax = 0.f;
+    for (int64_t t = threadIdx.x; t < n_win; t += blockDim.x) {
+      float lw = 0.f;
+      if (a.tm_prior) {
+        const float pw = tm_prior_density_f(a, tm_sample_time(a, j_lo + t, L, step, jit));  // base.py:807
+        if (!(pw > 0.f)) continue;
+        lw = __logf(pw);
+      }
+      const float2 x = s_ew[t];
+      const float ax = sqrtf(x.x * x.x + x.y * x.y);
+      float l;
+      if (a.dist_marg) {
+        l = bicubic_eval_row_ff(s_tx, a.nx, a.ny, a.tc_f, a.bbox_x_f, (a.phase_marg ? ax : x.x) * srf, s_row);
+      } else if (a.phase_marg) {
+        l = ax + ln_i0_minus_x(ax);
+      } else {
+        l = x.x;
+      }
+      l += lw;
+      xmax = fmaxf(xmax, ax);
+      if (l > mf32) {
+        acc32 = mf32 > -INFINITY ? acc32 * __expf(mf32 - l) + 1.f : 1.f;
+        mf32 = l;
+      } else if (isfinite(l)) {
+        acc32 += __expf(l - mf32);
+      }
+    }
+    // the block's logsumexp: the float32 maximum, then sum acc_t exp(m_t - M),
+    // xor-shuffles within warps and a fixed-order sum over the warps
+    float mf = mf32, zz = z2, xm = xmax;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mf = fmaxf(mf, __shfl_xor_sync(0xffffffffu, mf, o));
+      zz += __shfl_xor_sync(0xffffffffu, zz, o);
+      xm = fmaxf(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+    }
+    if (lane == 0) {
+      redf[warp] = mf;
+      redf[W + warp] = zz;
+      redf[2 * W + warp] = xm;
+    }
+    __syncthreads();
+    float Mx = redf[0];
+    for (int w = 1; w < W; ++w) Mx = fmaxf(Mx, redf[w]);
+    float sm = 0.f;
+    if (isfinite(Mx) && isfinite(mf32)) sm = acc32 * __expf(mf32 - Mx);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    if (lane == 0) redf[3 * W + warp] = sm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float total = 0.f, zs = 0.f, xp = 0.f;
+      for (int w = 0; w < W; ++w) {
+        total += redf[3 * W + w];
+        zs += redf[W + w];
+        xp = fmaxf(xp, redf[2 * W + w]);
+      }
+      const double c0 = a.dist_marg ? 0.0 : -hh / 2;
+      const double amax = (isfinite(Mx) ? (double)Mx : -INFINITY) + c0;
+      const double tot = (double)total * (a.tm_prior ? 1.0 : a.tm_prob) * a.delta_tc;
+      double lnl;
+      if (!r.valid) lnl = -1.7976931348623157e308;
+      else if (!isfinite(amax)) lnl = amax;
+      else lnl = amax + (double)logf((float)tot);
+      a.out[i] = lnl;
+      if (a.rf_tol > 0 && a.rf_count && a.rf_list && r.valid) {
+        a.rec[i].tm_xp = xp;
+        a.rec[i].tm_zs = sqrtf(zs);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // The mixed full-grid kernel's error bounds, one thread per point:
 // |dlnL| <= s (kTmErrNorm ||z||_2 + kTmErrPeak max|X|), s the distance table's
 // sensitivity at the window's peak (tm_sensitivity); points over the
@@ -1349,8 +1662,27 @@ size_t time_marg_work_bytes(const LaunchArgs& a) {
   return (size_t)tm_grid_fp64() * (size_t)a.n_fft * sizeof(double2);
 }
 
+// shared memory of k_tm_half: the half-length buffer, the window's values, the spline's knots
+static size_t tm_half_smem(const LaunchArgs& a, int* n_win_cap) {
+  const double width = (a.t_max - a.t_min) / a.tm_step;
+  *n_win_cap = (int)std::ceil(width > 0.0 && width < 1e7 ? width : 0.0) + 8;
+  const int64_t M = a.n_fft / 2;
+  return (size_t)(M + M / 16) * sizeof(float2) + (size_t)*n_win_cap * sizeof(float2) +
+         (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0);
+}
+
 template <int D>
 static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2N, int m_odd, const TwiddleTables& tw) {
+  int n_win_cap = 0;
+  if (a.precision == GWL_PRECISION_MIXED && a.model == GWL_MODEL_TAYLORF2 && m_odd == 1 && log2N >= 6 &&
+      tm_half_smem(a, &n_win_cap) <= (size_t)100 * 1024) {
+    // two half-length transforms per point, two CTAs per SM
+    const size_t smem = tm_half_smem(a, &n_win_cap);
+    cudaError_t e = cudaFuncSetAttribute(k_tm_half<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tm_half<D><<<(unsigned)a.B, kTmHalfThreads, smem, s>>>(a, tw.d32, log2N, n_win_cap);
+    return cudaGetLastError();
+  }
   if (a.precision == GWL_PRECISION_MIXED) {
     // the FFT buffer, then the distance spline's knots
     const size_t smem = (size_t)(a.n_fft + a.n_fft / 16) * sizeof(float2) +
