@@ -752,25 +752,28 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
 // passes in registers, the last passes only for the window's outputs; then
 // the window in float32 and the error bound's inputs, as there.
 // ---------------------------------------------------------------------------
-constexpr int kTmHalfThreads = 256;
+// LS = 1 splits the transform in two (256 threads per CTA, two CTAs per SM),
+// LS = 2 in four (X[j] = sum_r e^{-2 pi i j r / L} Y_r[j mod L/4], Y_r over the
+// bins k = 4 k' + r; 128 threads, four CTAs per SM).
+constexpr int kTmHalfLs = 2;
 
-template <int D>
-__global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, const float2* twiddle, int log2L,
-                                                               int n_win_cap) {
+template <int D, int LS>
+__global__ void __launch_bounds__(512 >> LS, 1 << LS) k_tm_half(LaunchArgs a, const float2* twiddle, int log2L,
+                                                                  int n_win_cap) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float s_coef[2 * kMaxDet];
   __shared__ SplineRowF s_row;
   __shared__ float2 tw_hi[kTmTwiddleRows], tw_lo[kTmTwiddleRows];
   __shared__ float2 s_w16[16];
-  constexpr int W = kTmHalfThreads / 32;
+  constexpr int W = (512 >> LS) / 32;
   __shared__ float redf[4 * W];
-  __shared__ double s_lnl[2];
-  const int64_t L = a.n_fft, M = L >> 1;
-  const int lM = log2L - 1;
+  const int64_t L = a.n_fft, M = L >> LS;
+  const int lM = log2L - LS;
+  const int64_t hL = L >> 1;  // the table holds exp(-2 pi i q / L) for q < L / 2
   for (int q = threadIdx.x; q < kTmTwiddleRows; q += blockDim.x) {
     const int64_t qh = (int64_t)q * kTmTwiddleRows;
-    tw_hi[q] = qh < M ? twiddle[qh] : make_float2(1.f, 0.f);
-    tw_lo[q] = q < M ? twiddle[q] : make_float2(1.f, 0.f);
+    tw_hi[q] = qh < hL ? twiddle[qh] : make_float2(1.f, 0.f);
+    tw_lo[q] = q < hL ? twiddle[q] : make_float2(1.f, 0.f);
   }
   if (threadIdx.x < 8) {  // the 16th roots of unity exp(-2 pi i m / 16)
     const float2 t = twiddle[(int64_t)threadIdx.x * (L / 16)];
@@ -821,13 +824,14 @@ __global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, con
     }
     const int64_t ks = max(r.k_start, a.k_lo), ke = min(min(r.k_end, a.k_hi), L);
     float z2 = 0.f;  // sum of |z_k|^2 over this thread's bins (error bound)
-    for (int par = 0; par < 2; ++par) {
-      // ---- A: bins k = 2 k' + par, fused with the first four stages: after
+    for (int par = 0; par < (1 << LS); ++par) {
+      // ---- A: bins k = 2^LS k' + par, fused with the first four stages: after
       // them positions 16 b .. 16 b + 15 hold the 16-point DFT of the bins
       // k' = q + j M / 16 (j < 16), q = bitrev(b) over log2(M) - 4 bits
       const int64_t R = M >> 4;
       const int lr = lM - 4;
-      const int64_t ka = (ks - par + 1) >> 1, kb = (ke - par + 1) >> 1;  // in-band k' in [ka, kb)
+      // in-band k' in [ka, kb)
+      const int64_t ka = (ks - par + (1 << LS) - 1) >> LS, kb = (ke - par + (1 << LS) - 1) >> LS;
       for (int64_t bb = threadIdx.x; bb < R; bb += blockDim.x) {
         const int64_t q = (int64_t)bit_reverse((uint32_t)bb, lr);
         float yr[16], yi[16];
@@ -836,7 +840,7 @@ __global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, con
         const int j0 = r.valid ? (ka > q ? (int)(((uint32_t)(ka - q) + (uint32_t)R - 1u) >> lr) : 0) : 16;
         const int j1 = r.valid ? (kb > q ? min(16, (int)(((uint32_t)(kb - q) + (uint32_t)R - 1u) >> lr)) : 0) : 0;
         for (int j = j0; j < j1; ++j) {
-          const int64_t k = 2 * (q + (int64_t)j * R) + par;
+          const int64_t k = ((q + (int64_t)j * R) << LS) + par;
           float s_hi = ch[kNumBasis], s_lo = cl[kNumBasis];
 #pragma unroll
           for (int qq = 0; qq < kNumBasis / 2; ++qq) {
@@ -938,13 +942,13 @@ __global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, con
         }
         __syncthreads();
       }
-      if (stage == lM) {  // a last radix-2 stage, half-length M / 2, twiddle exp(-2 pi i l / M) = tw(2 l)
+      if (stage == lM) {  // a last radix-2 stage, half-length M / 2, twiddle exp(-2 pi i l / M) = tw(2^LS l)
         const int64_t h = M >> 1;
         const bool prune = n_win > 0 && n_win <= h;
         const int64_t n_bf = prune ? n_win : h;
         for (int64_t t = threadIdx.x; t < n_bf; t += blockDim.x) {
           const int64_t l = prune ? ((j_lo + t) & (h - 1)) : t;
-          const float2 w = tw(2 * l);
+          const float2 w = tw(l << LS);
           const float2 x0 = buf[P(l)], x1 = buf[P(l + h)];
           const float tr = w.x * x1.x - w.y * x1.y, ti = w.x * x1.y + w.y * x1.x;
           buf[P(l)] = make_float2(x0.x + tr, x0.y + ti);
@@ -952,15 +956,16 @@ __global__ void __launch_bounds__(kTmHalfThreads, 2) k_tm_half(LaunchArgs a, con
         }
         __syncthreads();
       }
-      // the window's values: E kept, then X = E + exp(-2 pi i j / L) O
+      // the window's values: X = sum over the parts of exp(-2 pi i j par / L) Y_par
       for (int64_t t = threadIdx.x; t < n_win; t += blockDim.x) {
         const int64_t j = j_lo + t;
         const float2 v = buf[P(j & (M - 1))];
         if (par == 0) {
           s_ew[t] = v;
         } else {
-          float2 w = j < M ? tw(j) : tw(j - M);
-          if (j >= M) w = make_float2(-w.x, -w.y);
+          const int64_t qq = (j * par) & (L - 1);
+          float2 w = qq < hL ? tw(qq) : tw(qq - hL);
+          if (qq >= hL) w = make_float2(-w.x, -w.y);
           const float2 e = s_ew[t];
           s_ew[t] = make_float2(e.x + (w.x * v.x - w.y * v.y), e.y + (w.x * v.y + w.y * v.x));
         }
@@ -1666,7 +1671,7 @@ size_t time_marg_work_bytes(const LaunchArgs& a) {
 static size_t tm_half_smem(const LaunchArgs& a, int* n_win_cap) {
   const double width = (a.t_max - a.t_min) / a.tm_step;
   *n_win_cap = (int)std::ceil(width > 0.0 && width < 1e7 ? width : 0.0) + 8;
-  const int64_t M = a.n_fft / 2;
+  const int64_t M = a.n_fft >> kTmHalfLs;
   return (size_t)(M + M / 16) * sizeof(float2) + (size_t)*n_win_cap * sizeof(float2) +
          (a.dist_marg ? (size_t)(a.nx + a.ny) * sizeof(float) : 0);
 }
@@ -1674,13 +1679,14 @@ static size_t tm_half_smem(const LaunchArgs& a, int* n_win_cap) {
 template <int D>
 static cudaError_t launch_tm_d(const LaunchArgs& a, cudaStream_t s, int log2N, int m_odd, const TwiddleTables& tw) {
   int n_win_cap = 0;
-  if (a.precision == GWL_PRECISION_MIXED && a.model == GWL_MODEL_TAYLORF2 && m_odd == 1 && log2N >= 6 &&
-      tm_half_smem(a, &n_win_cap) <= (size_t)100 * 1024) {
-    // two half-length transforms per point, two CTAs per SM
+  if (a.precision == GWL_PRECISION_MIXED && a.model == GWL_MODEL_TAYLORF2 && m_odd == 1 && log2N >= 5 + kTmHalfLs &&
+      tm_half_smem(a, &n_win_cap) <= ((size_t)200 * 1024 >> kTmHalfLs)) {
+    // 2^kTmHalfLs shorter transforms per point, as many CTAs per SM
     const size_t smem = tm_half_smem(a, &n_win_cap);
-    cudaError_t e = cudaFuncSetAttribute(k_tm_half<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_tm_half<D, kTmHalfLs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_tm_half<D><<<(unsigned)a.B, kTmHalfThreads, smem, s>>>(a, tw.d32, log2N, n_win_cap);
+    k_tm_half<D, kTmHalfLs><<<(unsigned)a.B, 512 >> kTmHalfLs, smem, s>>>(a, tw.d32, log2N, n_win_cap);
     return cudaGetLastError();
   }
   if (a.precision == GWL_PRECISION_MIXED) {
