@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB_PATH = os.path.join(OUT_DIR, "libgwlnl.so")
-SOURCES = ["gwl_capi.cu", "gwl_kernels.cu", "gwl_marg.cu", "gwl_marg_window.cu", "gwl_source.cu", "gwl_noalloc.cu", "gwl_priors.cu"]
+SOURCES = ["gwl_capi.cu", "gwl_kernels.cu", "gwl_marg.cu", "gwl_marg_window.cu", "gwl_mb_fft.cu", "gwl_source.cu",
+           "gwl_noalloc.cu", "gwl_priors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]

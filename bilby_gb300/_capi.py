@@ -101,6 +101,8 @@ SIGNATURES = {
     "gwl_set_relative_binning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32,
                                                 ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                                 ctypes.POINTER(ctypes.c_double)]),
+    "gwl_set_multiband_ifft_fft": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                  c_double_p, c_double_p, c_double_p]),
     "gwl_set_multiband": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),

@@ -202,6 +202,29 @@ class Analysis:
                     "gwl_set_multiband")
         self.multiband = True
 
+    def set_multiband_ifft_fft(self, enable: bool, ks=None, m=None, scale=None, sqrt_window=None,
+                               odd_weights=None):
+        """Multi-banding with the IFFT-FFT <h|h>, after :meth:`set_multiband`:
+        per band b >= 1 the transform length ``m[b]`` (``m[0] = 0``), its first
+        bin ``ks[b]``, ``scale[b] = 4 / That_b``; ``sqrt_window`` [K] the
+        roots of the band windows; ``odd_weights`` [n_det, sum_b m[b] / 2]
+        the odd-bin weights Re I_b[2j + 1], band after band."""
+        if not enable:
+            _capi.check(self._lib.gwl_set_multiband_ifft_fft(self._h, 0, None, None, None, None, None),
+                        "gwl_set_multiband_ifft_fft")
+            return
+        ks = np.ascontiguousarray(ks, dtype=np.int32)
+        m = np.ascontiguousarray(m, dtype=np.int32)
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        sw = np.ascontiguousarray(sqrt_window, dtype=np.float64)
+        od = np.ascontiguousarray(odd_weights, dtype=np.float64)
+        n_odd = int(np.sum(m[1:] // 2))
+        if len(ks) != len(m) or len(sc) != len(m) or od.size != self.n_detectors * n_odd:
+            raise ValueError("IFFT-FFT tables do not match the bands and detectors")
+        _capi.check(self._lib.gwl_set_multiband_ifft_fft(
+            self._h, 1, ks.ctypes.data_as(ctypes.c_void_p), m.ctypes.data_as(ctypes.c_void_p), _capi.dptr(sc),
+            _capi.dptr(sw), _capi.dptr(od)), "gwl_set_multiband_ifft_fft")
+
     def set_roq(self, enable: bool, nodes_linear=None, nodes_quadratic=None, time_start_index=0, time_step=0.0,
                 linear_weights=None, quadratic_weights=None):
         """Reduced-order quadrature: ``linear_weights`` [n_det, n_time,

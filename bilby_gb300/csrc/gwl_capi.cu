@@ -122,6 +122,21 @@ struct gwl_analysis {
   double mb_tm_delta_tc = 0.0, mb_tm_antenna_time = 0.0;
   int32_t* mb_tm_ptr = nullptr;
   int32_t* mb_tm_src = nullptr;
+  // multi-banding with the IFFT-FFT <h|h>: per band b >= 1 its transform's
+  // parameters (pointers into the tables below), the slab of odd-bin parts
+  // and, for transforms too long for shared memory, one global slot per CTA
+  int mb_fft = 0;
+  std::vector<int64_t> mb_band_start_h;
+  std::vector<MbFftBand> mbf_bands;
+  double* mbf_sqrtw = nullptr;
+  double* mbf_odd[kMaxDet] = {};
+  double2* mbf_tw = nullptr;
+  int mbf_log2m_max = 0;
+  double* d_mbf_hh = nullptr;
+  size_t mbf_hh_count = 0;
+  double2* d_mbf_scratch = nullptr;
+  size_t mbf_scratch_count = 0;  // double2 elements
+  int64_t mbf_slots = 0;
   int roq_tm = 0;  // ROQ time-marginalisation grid set for these weights
   int64_t roq_tm_n = 0, roq_tm_chunk = 0, roq_tm_rows = 0;
   double roq_tm_delta_tc = 0.0, roq_tm_antenna_time = 0.0;
@@ -228,6 +243,12 @@ void free_workspace(gwl_analysis* a) {
   a->d_roq_h32 = a->d_roq_d32 = nullptr;
   a->d_roq_hh = nullptr;
   a->roq_ws_points = 0;
+  cudaFree(a->d_mbf_hh);
+  cudaFree(a->d_mbf_scratch);
+  a->d_mbf_hh = nullptr;
+  a->d_mbf_scratch = nullptr;
+  a->mbf_hh_count = a->mbf_scratch_count = 0;
+  a->mbf_slots = 0;
 }
 
 float2 split_ff(double x) {
@@ -623,6 +644,41 @@ int run_roq_tm_mixed(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
   return GWL_OK;
 }
 
+// Multi-banding with the IFFT-FFT <h|h>: the odd-bin transforms of every band
+// b >= 1 into the slab that the multi-banding kernels add to <h|h>.
+int run_mb_fft(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
+  const size_t need = (size_t)a->mb_bands * a->n_det * L.B;
+  bool glob = false;
+  for (const MbFftBand& bd : a->mbf_bands) glob = glob || !bd.in_smem;
+  const int64_t slots = glob ? (int64_t)sm_count() : 0;
+  const size_t scratch = glob ? ((size_t)slots << a->mbf_log2m_max) : 0;
+  if (need > a->mbf_hh_count || scratch > a->mbf_scratch_count) {
+    GWL_CUDA(cudaStreamSynchronize(s));
+    int rc;
+    if (need > a->mbf_hh_count) {
+      cudaFree(a->d_mbf_hh);
+      a->d_mbf_hh = nullptr;
+      a->mbf_hh_count = 0;
+      if ((rc = dev_alloc(a, &a->d_mbf_hh, need, false))) return rc;
+      a->mbf_hh_count = need;
+    }
+    if (scratch > a->mbf_scratch_count) {
+      cudaFree(a->d_mbf_scratch);
+      a->d_mbf_scratch = nullptr;
+      a->mbf_scratch_count = 0;
+      if ((rc = dev_alloc(a, &a->d_mbf_scratch, scratch, false))) return rc;
+      a->mbf_scratch_count = scratch;
+    }
+  }
+  a->mbf_slots = glob ? slots : 0;
+  for (MbFftBand bd : a->mbf_bands) {
+    bd.out = a->d_mbf_hh;
+    GWL_CUDA(launch_mb_hh_fft(L, bd, a->d_mbf_scratch, a->mbf_slots, s));
+  }
+  L.mb_fft_hh = a->d_mbf_hh;
+  return GWL_OK;
+}
+
 int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, double* d_out, double* d_dh,
              double* d_hh, cudaStream_t s, double* d_series = nullptr) {
   if (precision != GWL_PRECISION_FP64 && precision != GWL_PRECISION_MIXED) {
@@ -702,6 +758,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     if (mixed && (rc = ensure_window_shares(a, L, s, &share))) return rc;
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+    if (a->multiband && a->mb_fft && (rc = run_mb_fft(a, L, s))) return rc;
     if (window) {
       if ((rc = launch_window_marg(a, L, s, mixed, share))) return rc;
     } else {
@@ -720,6 +777,7 @@ int run_eval(gwl_analysis* a, const double* d_params, int64_t B, int precision, 
     L.rf_tol = 0.0;
     GWL_CUDA(launch_prologue(L, s));
     if (a->profiling) GWL_CUDA(cudaEventRecord(a->ev_begin, s));
+    if (a->multiband && a->mb_fft && (rc = run_mb_fft(a, L, s))) return rc;
     if (a->relbin) {
       GWL_CUDA(launch_relbin(L, s));
     } else if (a->multiband) {
@@ -1542,6 +1600,7 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   std::lock_guard<std::mutex> g(a->mu);
   if (!enable) {
     a->multiband = 0;
+    a->mb_fft = 0;
     return GWL_OK;
   }
   if (a->relbin || a->roq) {
@@ -1627,11 +1686,105 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   std::vector<int64_t> bs(band_start, band_start + n_bands + 1);
   std::vector<double> bd(band_df, band_df + n_bands);
   if ((rc = upload(a, &a->mb_band_start, bs))) return rc;
+  a->mb_band_start_h = bs;
+  a->mb_fft = 0;  // new bands need new IFFT-FFT tables
   if ((rc = upload(a, &a->mb_band_df, bd))) return rc;
   a->mb_bands = n_bands;
   a->mb_points = n_points;
   a->mb_tm = 0;  // new bands need new time-marginalisation tables
   a->multiband = 1;
+  return GWL_OK;
+}
+
+int gwl_set_multiband_ifft_fft(gwl_analysis* a, int enable, const int32_t* ks, const int32_t* m,
+                               const double* scale, const double* sqrt_window, const double* odd_weights) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  if (!enable) {
+    a->mb_fft = 0;
+    return GWL_OK;
+  }
+  if (!a->multiband) {
+    set_error("set the bands first (gwl_set_multiband)");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (!ks || !m || !scale || !sqrt_window || !odd_weights) {
+    set_error("the IFFT-FFT <h|h> needs K_s, M, the scales, the window roots and the odd-bin weights of every band");
+    return GWL_ERR_ARGUMENT;
+  }
+  const int nb = a->mb_bands;
+  if (m[0] != 0) {
+    set_error("band 0's <h|h> is in the quadratic coefficients: m[0] must be 0");
+    return GWL_ERR_ARGUMENT;
+  }
+  int64_t total = 0;
+  int log2m_max = 2;
+  for (int b = 1; b < nb; ++b) {
+    const int64_t M = m[b], nk = a->mb_band_start_h[b + 1] - a->mb_band_start_h[b];
+    if (M < 4 || M > ((int64_t)1 << 22) || (M & (M - 1)) != 0) {
+      set_error("each band's M must be a power of two between 4 and 2^22");
+      return GWL_ERR_ARGUMENT;
+    }
+    // the band's bins m = K_s .. K_s + n - 1 and their mirrors M - m must be
+    // distinct and exclude 0 and M / 2
+    if (nk > 0 && (ks[b] < 1 || (int64_t)ks[b] + nk - 1 >= M / 2)) {
+      set_error("each band's bins must satisfy 1 <= K_s and K_s + n_points - 1 < M / 2");
+      return GWL_ERR_ARGUMENT;
+    }
+    if (!(scale[b] >= 0) || !std::isfinite(scale[b])) {
+      set_error("the band scales 4 / That must be finite and non-negative");
+      return GWL_ERR_ARGUMENT;
+    }
+    int l = 0;
+    while ((int64_t)1 << l < M) ++l;
+    log2m_max = std::max(log2m_max, l);
+    total += M / 2;
+  }
+  int rc;
+  std::vector<double> sw(sqrt_window, sqrt_window + a->mb_points);
+  for (double v : sw) {
+    if (!std::isfinite(v)) {
+      set_error("the window roots must be finite");
+      return GWL_ERR_ARGUMENT;
+    }
+  }
+  if ((rc = upload(a, &a->mbf_sqrtw, sw))) return rc;
+  for (int d = 0; d < a->n_det; ++d) {
+    std::vector<double> od(odd_weights + (size_t)d * total, odd_weights + (size_t)(d + 1) * total);
+    if ((rc = upload(a, &a->mbf_odd[d], od))) return rc;
+  }
+  // exp(-i pi k / 2^log2m_max), k < 2^log2m_max
+  const int64_t n_tw = (int64_t)1 << log2m_max;
+  std::vector<double2> tw((size_t)n_tw);
+  for (int64_t k = 0; k < n_tw; ++k) {
+    const double th = M_PI * (double)k / (double)n_tw;
+    tw[(size_t)k] = make_double2(std::cos(th), -std::sin(th));
+  }
+  if ((rc = upload(a, &a->mbf_tw, tw))) return rc;
+  a->mbf_log2m_max = log2m_max;
+  a->mbf_bands.clear();
+  int64_t off = 0;
+  for (int b = 1; b < nb; ++b) {
+    MbFftBand bd;
+    std::memset(&bd, 0, sizeof(bd));
+    bd.band = b;
+    bd.ks = ks[b];
+    int l = 0;
+    while (((int64_t)1 << l) < m[b]) ++l;
+    bd.log2m = l;
+    bd.log2m_max = log2m_max;
+    bd.in_smem = mb_hh_fft_smem(l) > 0;
+    bd.scale = scale[b];
+    for (int d = 0; d < a->n_det; ++d) bd.odd[d] = a->mbf_odd[d] + off;
+    bd.sqrtw = a->mbf_sqrtw;
+    bd.tw = a->mbf_tw;
+    a->mbf_bands.push_back(bd);
+    off += m[b] / 2;
+  }
+  a->mb_fft = nb > 1;
   return GWL_OK;
 }
 

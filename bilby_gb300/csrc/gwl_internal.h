@@ -213,6 +213,11 @@ struct LaunchArgs {
   int mb_tm;
   const int32_t* mb_tm_ptr;             // [n_fft + 1]
   const int32_t* mb_tm_src;             // [mb_points]
+  // multi-banding with the IFFT-FFT <h|h> (multiband.py:613-650, 760-779):
+  // the odd-bin part of band b >= 1 of detector d at point i,
+  // mb_fft_hh[(b * n_det + d) * B + i], written by k_mb_hh_fft before the
+  // kernels that add it to <h|h> (band 0 is wholly in mb_quad); null without it
+  const double* mb_fft_hh;
   // reduced-order quadrature: the model at the linear and quadratic nodes,
   // time-dependent linear weights on the grid (t_start + k) dt, k < n_time
   int roq;
@@ -338,6 +343,26 @@ cudaError_t launch_time_marg_window(const LaunchArgs& a, cudaStream_t s);
 constexpr int kTmMaxOddFactor = 127;
 bool fft_length_supported(int64_t L, int* m_odd, int* log2N);
 size_t time_marg_work_bytes(const LaunchArgs& a);
+// Multi-banding with the IFFT-FFT <h|h> (gwl_mb_fft.cu): one band's odd-bin
+// transform.  Transforms of at most 2^kMbFftSmemLog2 samples run in shared
+// memory, longer ones in a global slot of 2^log2m double2 per CTA.
+constexpr int kMbFftSmemLog2 = 13;
+struct MbFftBand {
+  int band;                      // b >= 1
+  int ks;                        // K_s: grid index of the band's first banded point
+  int log2m;                     // M = Mbs[b] = 2^log2m samples
+  int log2m_max;                 // twiddle table length 2^log2m_max >= M
+  int in_smem;                   // 1: the transform in shared memory
+  double scale;                  // 4 / That_b
+  const double* odd[kMaxDet];    // [M / 2] Re I_(2j+1) of each detector
+  const double* sqrtw;           // [mb_points] square roots of the band windows
+  const double2* tw;             // [2^log2m_max] exp(-i pi k / 2^log2m_max)
+  double* out;                   // the mb_fft_hh slab
+};
+size_t mb_hh_fft_smem(int log2m);  // dynamic shared memory of a transform in shared memory, 0 if it does not fit
+int mb_hh_fft_threads();
+cudaError_t launch_mb_hh_fft(const LaunchArgs& a, const MbFftBand& band, double2* scratch, int64_t scratch_slots,
+                             cudaStream_t s);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,
                                         double fmin, double* plus, double* cross, cudaStream_t s);
 cudaError_t launch_detector_response(const DetGeom& g, const double* freq, int64_t n, const double* plus,

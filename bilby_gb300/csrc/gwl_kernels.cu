@@ -1720,6 +1720,7 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband(LaunchArgs a) {
       hh += __shfl_xor_sync(0xffffffffu, hh, off);
     }
   }
+  if (lane == 0 && r.valid) hh += mb_fft_hh_total(a, i);
   // <d|h> = conj(sum s L)
   if (lane == 0) finish_point(a, r, i, sr, -si, hh);
 }
@@ -1862,6 +1863,7 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArg
       }
     }
   }
+  if (lane == 0 && r.valid) hh += mb_fft_hh_total(a, i);
   // <d|h> = conj(sum h L)
   if (lane == 0) finish_point(a, r, i, sr, -si, hh);
 }

@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
     C* buf = MIXED ? reinterpret_cast<C*>(smem) : reinterpret_cast<C*>(a.tm_work) + (size_t)blockIdx.x * L;
     const PointRec& r = a.rec[i];
     // ---- A: integrand --------------------------------------------------
-    double hh_part = 0.0;
+    // (multi-banding with the IFFT-FFT <h|h>: its odd-bin part, once)
+    double hh_part = threadIdx.x == 0 ? mb_fft_hh_total(a, i) : 0.0;
     float z2 = 0.f;  // mixed TaylorF2: sum of |z_k|^2 over this thread's bins (error bound)
     if constexpr (MIXED) {
       // per-point float32 coefficients, computed by the float64 prologue

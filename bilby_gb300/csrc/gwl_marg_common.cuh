@@ -58,6 +58,16 @@ struct TmTypes<false> {
 
 __device__ __forceinline__ uint32_t bit_reverse(uint32_t k, int log2n) { return __brev(k) >> (32 - log2n); }
 
+// Multi-banding with the IFFT-FFT <h|h>: the odd-bin part of point i summed
+// over the bands b >= 1 and the detectors (zero without it).
+__device__ __forceinline__ double mb_fft_hh_total(const LaunchArgs& a, int64_t i) {
+  double s = 0.0;
+  if (a.mb_fft_hh)
+    for (int b = 1; b < a.mb_bands; ++b)
+      for (int d = 0; d < a.n_det; ++d) s += a.mb_fft_hh[((int64_t)b * a.n_det + d) * a.B + i];
+  return s;
+}
+
 // float64 source polarisations of the plain kernels at one frequency.
 __device__ __forceinline__ bool plain_pols(const LaunchArgs& a, const PointRec& r, double f, double2& hp, double2& hx) {
   if (a.model == GWL_MODEL_SINEGAUSSIAN) {

@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
       s_scal[0] = step;
     }
     // ---- per-point set-up ----------------------------------------------
-    double hh_part = 0.0;
+    // (multi-banding with the IFFT-FFT <h|h>: its odd-bin part, once)
+    double hh_part = MB && part_c == 0 && threadIdx.x == 0 ? mb_fft_hh_total(a, i) : 0.0;
     float z2 = 0.f;  // mixed: sum of |z_k|^2 (error bound)
     double2* rat = reinterpret_cast<double2*>(smem + lay.off_rat);  // relative binning: [D][nE]
     float4* coef = reinterpret_cast<float4*>(smem + lay.off_coef);  // mixed: [D][nB] {r0, r1}, then [D][nB] lo(r0)

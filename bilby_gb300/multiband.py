@@ -16,9 +16,16 @@ time-marginalised kernel scatters the banded strain times the linear
 coefficients to the full-resolution grid, transforms it and marginalises
 over time (``gwl_set_multiband_time_marginalization``).
 
-Not built: the IFFT-FFT evaluation of <h|h> (``linear_interpolation=False``),
-which raises NotImplementedError; weights files need h5py, as in the
-reference.
+With ``linear_interpolation=False`` <h|h> is the reference's IFFT-FFT sum
+(multiband.py:613-650, 760-779): band 0 by direct weights, each later band b
+by an inverse FFT of sqrt(w) h over M_b samples, zero-padding to 2 M_b and an
+FFT weighted by the band's truncated inverse-PSD spectrum I_b.  Its even bins
+equal the banded values themselves, so their weights join the quadratic
+coefficients; the odd bins run on the GPU as one packed complex transform
+per point, detector pair and band (``k_mb_hh_fft``, behind
+``gwl_set_multiband_ifft_fft``).
+
+Weights files need h5py, as in the reference.
 """
 from __future__ import annotations
 
@@ -82,10 +89,8 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
                  distance_marginalization=False, phase_marginalization=False, priors=None,
                  time_marginalization=False, jitter_time=True, distance_marginalization_lookup_table=None,
                  reference_frame="sky", time_reference="geocenter", precision="fp64"):
-        if not linear_interpolation:
-            raise NotImplementedError("the IFFT-FFT evaluation of <h|h> has no GPU kernel; "
-                                      "use linear_interpolation=True")
         self._mb = None
+        self._mb_fft = None
         self._mb_tm = None
         super().__init__(interferometers, waveform_generator, priors=priors,
                          time_marginalization=time_marginalization,
@@ -258,12 +263,15 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
     # set-up (host, float64)
     # ------------------------------------------------------------------
     def setup_multibanding(self):
-        """multiband.py:317-326 (linear interpolation of <h|h>)."""
+        """multiband.py:317-326."""
         self._setup_frequency_bands()
         self._setup_integers()
         self._setup_waveform_frequency_points()
         self._setup_linear_coefficients()
-        self._setup_quadratic_coefficients_linear_interp()
+        if self.linear_interpolation:
+            self._setup_quadratic_coefficients_linear_interp()
+        else:
+            self._setup_quadratic_coefficients_ifft_fft()
 
     def _tau(self, f):
         """0PN time to merger (multiband.py:328-344)."""
@@ -431,21 +439,94 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
         for name in self.quadratic_coeffs:
             self.quadratic_coeffs[name] = np.concatenate(self.quadratic_coeffs[name])
 
+    def _setup_quadratic_coefficients_ifft_fft(self):
+        """multiband.py:613-650: per band the zero-padded length
+        Nhat_b = min(2 M_b, N_b) and duration That_b = T Nhat_b / N_b, and per
+        detector I_b = rfft of the inverse PSD's inverse FFT at N_b samples
+        truncated to lags |n| <= Nhat_b / 2 (wrapped to Nhat_b samples); the
+        band windows and their square roots."""
+        N = int(self.Nbs[-1])
+        nhat = [min(2 * int(mb), int(nb)) for mb, nb in zip(self.Mbs, self.Nbs)]
+        self.Tbhats = [self._ifo_duration * nh / int(nb) for nb, nh in zip(self.Nbs, nhat)]
+        self.Ibcs = dict((ifo.name, []) for ifo in self.interferometers)
+        self.hbcs = dict((ifo.name, []) for ifo in self.interferometers)
+        self.wths = dict((ifo.name, []) for ifo in self.interferometers)
+        for ifo in self.interferometers:
+            psd = np.asarray(ifo.power_spectral_density_array)
+            mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+            inv = np.zeros(N // 2 + 1)
+            n = min(len(psd), len(inv))
+            m = mask[:n]
+            inv[:n][m] = 1.0 / psd[:n][m]
+            for b in range(self.number_of_bands):
+                imb = np.fft.irfft(inv[:int(self.Nbs[b]) // 2 + 1])
+                h = nhat[b] // 2
+                self.Ibcs[ifo.name].append(np.fft.rfft(np.concatenate([imb[:h + 1], imb[len(imb) - (nhat[b] - h - 1):]])))
+                self.hbcs[ifo.name].append(np.zeros(nhat[b]))
+                self.wths[ifo.name].append(np.zeros(int(self.Mbs[b]) // 2 + 1, dtype=complex))
+        ws = []
+        for b in range(self.number_of_bands):
+            ks, ke = self.Ks_Ke[b]
+            ws.append(self._window(1. / self.durations[b], ks, ke - ks + 1, b))
+        self.windows = np.concatenate(ws)
+        self.square_root_windows = np.sqrt(self.windows)
+
+    def _ifft_fft_tables(self):
+        """The GPU form of the IFFT-FFT <h|h> (multiband.py:760-779): the
+        quadratic coefficients [n_det, K] (band 0: (4/T) mask w / S; band
+        b >= 1: the even bins, (4/That_b) w_k Re I_b[2 m_k] at grid index
+        m_k = K_s + k - k_b), and per band b >= 1 K_s, M_b, 4 / That_b and the
+        odd-bin weights Re I_b[2j + 1], j < M_b / 2."""
+        T = float(self._ifo_duration)
+        nb = self.number_of_bands
+        quad = np.zeros((len(self.interferometers), len(self.banded_frequency_points)))
+        odd = [[] for _ in self.interferometers]
+        ks_out, m_out, scale = np.zeros(nb, dtype=np.int32), np.zeros(nb, dtype=np.int32), np.zeros(nb)
+        for b in range(nb):
+            ks, ke = (int(x) for x in self.Ks_Ke[b])
+            s, e = (int(x) for x in self.start_end_idxs[b])
+            w = np.asarray(self.windows[s:e + 1])
+            for q, ifo in enumerate(self.interferometers):
+                if b == 0:
+                    psd = np.asarray(ifo.power_spectral_density_array)
+                    mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        quad[q, s:e + 1] = (4. / T) * mask[ks:ke + 1] * w / psd[ks:ke + 1]
+                else:
+                    ibc = np.asarray(self.Ibcs[ifo.name][b]).real
+                    quad[q, s:e + 1] = (4. / self.Tbhats[b]) * w * ibc[2 * np.arange(ks, ke + 1)]
+                    odd[q].append(ibc[1::2][:int(self.Mbs[b]) // 2])
+            if b > 0:
+                mb = int(self.Mbs[b])
+                if 2 * mb != min(2 * mb, int(self.Nbs[b])) or ks < 1 or ke >= mb // 2:
+                    raise ValueError(f"band {b}: the IFFT-FFT <h|h> needs Nhat = 2 M and 1 <= K_s <= K_e < M / 2")
+                ks_out[b], m_out[b], scale[b] = ks, mb, 4. / self.Tbhats[b]
+        odd = np.stack([np.concatenate(o) if o else np.zeros(0) for o in odd])
+        return quad, (ks_out, m_out, scale, np.asarray(self.square_root_windows, dtype=np.float64), odd)
+
     @property
     def weights(self):
-        out = {key: getattr(self, key) for key in WEIGHT_KEYS}
+        """multiband.py:652-671."""
+        keys = WEIGHT_KEYS if self.linear_interpolation else [k for k in WEIGHT_KEYS if k != "quadratic_coeffs"]
+        out = {key: getattr(self, key) for key in keys}
         out["waveform_frequencies"] = self.waveform_generator.waveform_arguments["frequencies"]
+        if not self.linear_interpolation:
+            for key in ("Tbhats", "windows", "square_root_windows"):
+                out[key] = getattr(self, key)
+            for key in ("wths", "hbcs", "Ibcs"):
+                out[key] = {name: dict((str(b), v) for b, v in enumerate(data))
+                            for name, data in getattr(self, key).items()}
         return out
 
     def setup_multibanding_from_weights(self, weights):
-        """multiband.py:656-681 (linear interpolation weights)."""
+        """multiband.py:687-712."""
         weights = dict(weights)
-        if not bool(weights.get("linear_interpolation", True)):
-            raise NotImplementedError("IFFT-FFT weights have no GPU kernel")
         self.reference_chirp_mass = weights.pop("reference_chirp_mass")
         for key, value in weights.items():
             if key == "waveform_frequencies":
                 self.waveform_generator.waveform_arguments["frequencies"] = value
+            elif key in ("wths", "hbcs", "Ibcs"):
+                setattr(self, key, {name: [data[str(b)] for b in range(len(data))] for name, data in value.items()})
             elif key in ("highest_mode", "linear_interpolation", "accuracy_factor", "time_offset", "delta_f_end",
                          "maximum_banding_frequency", "minimum_banding_duration"):
                 setattr(self, "_" + key, value)
@@ -486,6 +567,9 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
                 an.set_time_marginalization(True, False, tp.minimum, tp.maximum)
             freqs, lin, quad, band_start, band_df = self._mb
             an.set_multiband(True, freqs, lin[k:k + 1], quad[k:k + 1], band_start, band_df)
+            if self._mb_fft is not None:
+                ks, m, scale, sw, odd = self._mb_fft
+                an.set_multiband_ifft_fft(True, ks, m, scale, sw, odd[k:k + 1])
             if self._mb_tm is not None:
                 an.set_multiband_time_marginalization(*self._mb_tm)
             self._detector_analyses[name] = an
@@ -516,7 +600,11 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
     def _upload(self):
         names = [ifo.name for ifo in self.interferometers]
         lin = np.stack([np.asarray(self.linear_coeffs[n]) for n in names])
-        quad = np.stack([np.asarray(self.quadratic_coeffs[n]) for n in names])
+        if self.linear_interpolation:
+            quad = np.stack([np.asarray(self.quadratic_coeffs[n]) for n in names])
+            self._mb_fft = None
+        else:
+            quad, self._mb_fft = self._ifft_fft_tables()
         band_start = np.append(np.asarray(self.start_end_idxs)[:, 0], np.asarray(self.start_end_idxs)[-1, 1] + 1)
         self._mb = (np.asarray(self.banded_frequency_points, dtype=np.float64), lin, quad, band_start,
                     1.0 / np.asarray(self.durations, dtype=np.float64))
@@ -524,6 +612,8 @@ class MBGravitationalWaveTransient(GravitationalWaveTransient):
 
     def _set_bands(self, an):
         an.set_multiband(True, *self._mb)
+        if self._mb_fft is not None:
+            an.set_multiband_ifft_fft(True, *self._mb_fft)
         if self._mb_tm is not None:
             an.set_multiband_time_marginalization(*self._mb_tm)
 

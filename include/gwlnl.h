@@ -329,6 +329,23 @@ int gwl_set_multiband(gwl_analysis *a, int enable, int64_t n_points, const doubl
 int gwl_set_multiband_time_marginalization(gwl_analysis *a, int64_t n_fft, const int32_t *index_start,
                                            const int32_t *source, double delta_tc, double antenna_time);
 
+/* Multi-banding with the IFFT-FFT <h|h> (replaces the linear_interpolation=
+ * False branch of MBGravitationalWaveTransient.calculate_snrs,
+ * bilby/gw/likelihood/multiband.py:760-779, set up by
+ * _setup_quadratic_coefficients_ifft_fft 613-650).  Call after
+ * gwl_set_multiband (whose quadratic coefficients then hold band 0's direct
+ * weights (4/T) mask w / S and, for bands b >= 1, the even bins' weights
+ * (4/That_b) w_k Re I_b[2 m_k], m_k = K_s + k - k_b).  Per band b >= 1 and
+ * detector every evaluation transforms W = sqrt(w) s over M = m[b] samples
+ * and adds scale[b] sum_j |Z_j|^2 Re I_b[2j + 1] (the odd bins) to <h|h>, in
+ * float64 for either precision.  ks[b] and m[b] ([n_bands], m[0] = 0, m[b] a
+ * power of two with 1 <= ks[b] and ks[b] + n_b - 1 < m[b] / 2), scale[b] =
+ * 4 / That_b, sqrt_window [n_points] the square roots of the band windows,
+ * odd_weights [n_det][sum over b >= 1 of m[b] / 2] (Re I_b[2j + 1], band
+ * after band).  enable = 0 switches it off; a new gwl_set_multiband does too. */
+int gwl_set_multiband_ifft_fft(gwl_analysis *a, int enable, const int32_t *ks, const int32_t *m, const double *scale,
+                               const double *sqrt_window, const double *odd_weights);
+
 /* Reduced-order quadrature (replaces ROQGravitationalWaveTransient.
  * calculate_snrs for one linear and one quadratic basis without time
  * marginalisation, bilby/gw/likelihood/roq.py:467-602; the weights of

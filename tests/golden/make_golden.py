@@ -37,6 +37,11 @@ Outputs
     frequencies, linear and quadratic coefficients and lnL ratios without
     marginalisation, with phase, with distance, with time, and with time,
     phase and distance marginalisation.
+``tests/golden/tf2_128s_multiband_ifft.npz``
+    The same likelihood with the IFFT-FFT <h|h> (``linear_interpolation=False``):
+    lnL ratios without marginalisation, with phase, with time, and with time,
+    phase and distance marginalisation, its Tbhats, the sum of its windows and
+    a strided sample of each detector's per-band Ibcs.
 ``tests/golden/tf2_marg_8s_2k_roq.npz``
     The reference's ``ROQGravitationalWaveTransient`` on tf2_marg_8s_2k with the
     seeded synthetic basis of ``oracle/roq_basis.py``: its time grid, the rows
@@ -313,6 +318,62 @@ def run_multiband(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87):
                 out[f"mb_quadratic_coeffs_{q}"] = np.asarray(like.quadratic_coeffs[ifo.name])
             out["checksum"] = strain_checksum(ifos)
     np.savez_compressed(os.path.join(HERE, f"{name}_multiband.npz"), **out)
+
+
+MB_IFFT_COMBOS = ["none", "p", "t", "tpd"]
+
+
+def run_multiband_ifft(bilby, name, n_fixed, n_random, reference_chirp_mass=0.87, stride=61):
+    """The reference's MBGravitationalWaveTransient with the IFFT-FFT <h|h>
+    (linear_interpolation=False, multiband.py:613-650, 760-779): lnL ratios
+    under four marginalisation combinations, its Tbhats, its windows' sum and
+    every ``stride``-th entry of each detector's per-band Ibcs (the full
+    arrays are 1.4 MB)."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 5)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    n = n_fixed + n_random
+    jitter = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
+    out = {"p_" + k: v for k, v in params.items()}
+    out["time_jitter"] = jitter
+    for combo in MB_IFFT_COMBOS:
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_frequency_sequence,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency))
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, t, p, d)
+        like = bilby.gw.likelihood.MBGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, reference_chirp_mass=reference_chirp_mass,
+            priors=priors if (t or p or d) else None, time_marginalization=t, phase_marginalization=p,
+            distance_marginalization=d, linear_interpolation=False)
+        t0 = time.perf_counter()
+        vals = []
+        for i in range(n):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+                q["time_jitter"] = float(jitter[i])
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} multiband IFFT-FFT[{combo}]: {(time.perf_counter() - t0) / n * 1e3:.2f} ms/eval")
+        if combo == "none":
+            out["mb_Tbhats"] = np.asarray(like.Tbhats, dtype=np.float64)
+            out["mb_windows_sum"] = float(np.sum(like.windows))
+            out["mb_n_banded"] = len(like.banded_frequency_points)
+            out["ibc_stride"] = stride
+            for q, ifo in enumerate(ifos):
+                for b, ibc in enumerate(like.Ibcs[ifo.name]):
+                    out[f"mb_Ibcs_{q}_{b}"] = np.asarray(ibc)[::stride]
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}_multiband_ifft.npz"), **out)
 
 
 def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
@@ -847,6 +908,7 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--relbin-only", action="store_true")
     ap.add_argument("--multiband-only", action="store_true")
+    ap.add_argument("--multiband-ifft-only", action="store_true")
     ap.add_argument("--frames-only", action="store_true")
     ap.add_argument("--priors-only", action="store_true")
     ap.add_argument("--roq-only", action="store_true")
@@ -906,6 +968,15 @@ def main():
     if args.frames_only:
         run_frames(bilby)
         return
+    if args.multiband_ifft_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_multiband_ifft(bilby, "tf2_128s", 4, 4)
+            finally:
+                os.chdir(cwd)
+        return
     if args.multiband_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -940,6 +1011,7 @@ def main():
                 run_time_prior(bilby)
                 run_relbin(bilby, "tf2_128s", 8, 8)
                 run_multiband(bilby, "tf2_128s", 8, 8)
+                run_multiband_ifft(bilby, "tf2_128s", 4, 4)
                 run_roq(bilby)
                 run_roq_multibasis(bilby)
                 run_snrs(bilby)

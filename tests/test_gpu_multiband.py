@@ -83,9 +83,82 @@ def test_weights_round_trip(gpu, tmp_path):
     assert np.array_equal(a, b)
 
 
-def test_unsupported_options_are_refused(gpu, tmp_path):
-    with pytest.raises(NotImplementedError):
-        make("none", tmp_path, linear_interpolation=False)
+def _golden_points(z, priors, combo):
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = float(z["time_jitter"][i])
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        pts.append(q)
+    return pts
+
+
+@pytest.mark.parametrize("combo", ["none", "p", "t", "tpd"])
+def test_ifft_fft_lnl_matches_the_reference(gpu, tmp_path, combo):
+    """linear_interpolation=False: <h|h> by the IFFT-FFT sum (band 0 direct,
+    even bins in the quadratic coefficients, odd bins by k_mb_hh_fft) against
+    the reference's lnL (tests/golden/tf2_128s_multiband_ifft.npz), float64:
+    |dlnL| <= 1e-9 max(1, |lnL|) (1e-8 with the distance table); batch equals
+    single."""
+    like, priors = make(combo, tmp_path, linear_interpolation=False)
+    z = golden("tf2_128s_multiband_ifft")
+    pts = _golden_points(z, priors, combo)
+    ref = z["lnl_" + combo]
+    single = np.array([like.log_likelihood_ratio(q) for q in pts])
+    batch = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    assert np.array_equal(single, batch)
+    rtol = 1e-8 if "d" in combo else 1e-9
+    assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
+
+
+@pytest.mark.parametrize("combo", ["none", "tpd"])
+def test_ifft_fft_mixed_precision_matches_float64(gpu, tmp_path, combo):
+    """The mixed-precision multi-banded kernels with the IFFT-FFT <h|h> (its
+    odd bins in float64 for either precision) against the float64 ones on
+    512 prior draws and on the golden points: |dlnL| <= 1e-3."""
+    from bilby_gb300.analysis import params_block
+    from bilby_gb300.workloads import draw_points
+    w = WORKLOADS["tf2_128s"]
+    like, priors = make(combo, tmp_path, linear_interpolation=False, precision="mixed")
+    z = golden("tf2_128s_multiband_ifft")
+    rng = np.random.default_rng(53)
+    draws = draw_points(w, 512, rng)
+    n = 512
+    if "t" in combo:
+        draws["geocent_time"] = np.full(n, float(priors["geocent_time"]))
+        draws["time_jitter"] = rng.uniform(-1 / w.sampling_frequency, 1 / w.sampling_frequency, n)
+    if "p" in combo:
+        draws["phase"] = np.zeros(n)
+    if "d" in combo:
+        draws["luminosity_distance"] = np.full(n, float(priors["luminosity_distance"]))
+    block = params_block(like._prepare(draws))
+    mixed = like.analysis.log_likelihood_ratio_host(block, "mixed")
+    fp64 = like.analysis.log_likelihood_ratio_host(block, "fp64")
+    err = np.abs(mixed - fp64)
+    assert np.all(np.isfinite(mixed)) and np.all(err <= 1e-3), (err.max(), fp64[np.argmax(err)])
+    pts = _golden_points(z, priors, combo)
+    got = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    assert np.all(np.abs(got - z["lnl_" + combo]) <= 1e-3), got - z["lnl_" + combo]
+
+
+def test_ifft_fft_weights_round_trip(gpu, tmp_path):
+    """The IFFT-FFT weights dictionary (Tbhats, windows, wths, hbcs, Ibcs by
+    band) rebuilds a likelihood with identical results."""
+    from bilby_gb300.multiband import MBGravitationalWaveTransient
+    like, _ = make("none", tmp_path, linear_interpolation=False)
+    weights = like.weights
+    assert "quadratic_coeffs" not in weights and set(weights["Ibcs"]) == {i.name for i in like.interferometers}
+    again = MBGravitationalWaveTransient(like.interferometers, like.waveform_generator, weights=weights)
+    assert not again.linear_interpolation
+    z = golden("tf2_128s_multiband_ifft")
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    assert np.array_equal(like.log_likelihood_ratio_batch(params), again.log_likelihood_ratio_batch(params))
 
 
 @pytest.mark.parametrize("combo", ["none", "p", "d"])
