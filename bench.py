@@ -692,13 +692,24 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     tm["max_abs_dlnl_mixed_vs_fp64"] = float((outs["mixed"] - outs["fp64"]).abs().max().item())
     for ifo in base.interferometers:  # the MB time set-up fixes the antenna time on the interferometers
         ifo.reference_time = None
+    # the IFFT-FFT <h|h> (linear_interpolation=False, multiband.py:760-779):
+    # the odd-bin float64 transforms of bands 1.. per point and detector pair
+    like_f = MBGravitationalWaveTransient(base.interferometers, base.waveform_generator, reference_chirp_mass=0.87,
+                                          linear_interpolation=False)
+    bf = 2048
+    block_f = torch.from_numpy(params_block(draw_points(w, bf, rng))).cuda()
+    ifft = {"batch": bf, "transform_lengths": [int(m) for m in like_f.Mbs[1:]],
+            "launch": "prologue + k_mb_hh_fft per band (float64, packed detector pairs) + the multi-banding kernel"}
+    for precision in ("fp64", "mixed"):
+        ms_f, finite = time_launches(like_f.analysis, block_f, bf, steps, warmup, precision=precision)
+        ifft[precision] = {"value": bf / (ms_f / 1e3), "unit": "evals/s", "ms_per_launch": ms_f, "finite": finite}
     return {"workload": name, "bands": int(like.number_of_bands),
             "banded_frequencies": int(len(like.banded_frequency_points)), "batch": batch,
             "value": res["fp64"]["value"], "unit": "evals/s", "ms_per_launch": res["fp64"]["ms_per_launch"],
             "precision": "fp64", "mixed": res["mixed"], "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
             "max_abs_dlnl_mixed_vs_fp64": float((omx - o64).abs().max().item()), "setup_s": setup_s,
             "launch": "prologue + one warp per point over the banded frequencies",
-            "time_marginalized": tm}
+            "time_marginalized": tm, "ifft_fft": ifft}
 
 
 def eim_basis(f, n_linear, n_quadratic, n_train, seed, fmin, mass_range=(10.0, 40.0)):

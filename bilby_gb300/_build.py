@@ -3,6 +3,12 @@
 The translation units compile in parallel; the library lands in
 ``bilby_gb300/_lib/``.  ``python -m bilby_gb300._build`` builds it from the
 command line; ``__graft_entry__.build()`` calls :func:`build`.
+
+``build(checked=True)`` (``--checked``) builds the debug variant
+``libgwlnl_check.so`` with ``-DGWL_CHECK``: the kernels test the indices they
+read from host-built tables before each access and report a failed test as
+GWL_ERR_CHECK.  Setting ``GWL_CHECKED=1`` in the environment makes
+``bilby_gb300._capi`` load that variant.
 """
 from __future__ import annotations
 
@@ -17,6 +23,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB_PATH = os.path.join(OUT_DIR, "libgwlnl.so")
+CHECKED_LIB_PATH = os.path.join(OUT_DIR, "libgwlnl_check.so")
 SOURCES = ["gwl_capi.cu", "gwl_kernels.cu", "gwl_marg.cu", "gwl_marg_window.cu", "gwl_mb_fft.cu", "gwl_source.cu",
            "gwl_noalloc.cu", "gwl_priors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -31,8 +38,8 @@ def nvcc() -> str:
     return path
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra: list[str], obj_dir: str = OBJ_DIR) -> str:
+    obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -40,31 +47,35 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB_PATH):
+def _stale(lib: str = LIB_PATH) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "gwlnl.h"), __file__]
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 
-def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
-    """Compile every translation unit and link ``libgwlnl.so``; returns its path."""
-    if not force and not _stale() and not extra:
-        return LIB_PATH
-    os.makedirs(OBJ_DIR, exist_ok=True)
-    extra = list(extra or [])
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None,
+          checked: bool = False) -> str:
+    """Compile every translation unit and link ``libgwlnl.so`` (with
+    ``checked``, ``libgwlnl_check.so``); returns its path."""
+    lib = CHECKED_LIB_PATH if checked else LIB_PATH
+    obj_dir = OBJ_DIR + "_check" if checked else OBJ_DIR
+    if not force and not _stale(lib) and not extra:
+        return lib
+    os.makedirs(obj_dir, exist_ok=True)
+    extra = list(extra or []) + (["-DGWL_CHECK"] if checked else [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcudart", "-lcublas"]
+        objs = list(ex.map(lambda s: _compile(s, extra, obj_dir), SOURCES))
+    cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lcublas", "-ldl"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     if verbose:
-        print(f"built {LIB_PATH}")
-    return LIB_PATH
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True,
-          extra=["-Xptxas", "-v"] if "--ptxas-v" in sys.argv else None)
+          extra=["-Xptxas", "-v"] if "--ptxas-v" in sys.argv else None, checked="--checked" in sys.argv)

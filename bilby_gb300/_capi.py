@@ -21,6 +21,7 @@ GWL_ERR_MEMORY = 3
 GWL_ERR_UNSUPPORTED = 4
 GWL_ERR_TIMEOUT = 5
 GWL_ERR_STATE = 6
+GWL_ERR_CHECK = 7
 
 MODEL_SINEGAUSSIAN = 1
 MODEL_TAYLORF2 = 2
@@ -135,6 +136,8 @@ SIGNATURES = {
     "gwl_batcher_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "gwl_last_error": (ctypes.c_char_p, []),
     "gwl_version": (ctypes.c_char_p, []),
+    "gwl_trace_push": (ctypes.c_int, [ctypes.c_char_p]),
+    "gwl_trace_pop": (ctypes.c_int, []),
 }
 
 _LIB = None
@@ -142,7 +145,9 @@ _LOCK = threading.Lock()
 
 
 def library_path() -> str:
-    return _build.LIB_PATH
+    """``libgwlnl.so``, or the index-checked debug build ``libgwlnl_check.so``
+    when the environment sets ``GWL_CHECKED=1``."""
+    return _build.CHECKED_LIB_PATH if os.environ.get("GWL_CHECKED") == "1" else _build.LIB_PATH
 
 
 def load():

@@ -2,6 +2,7 @@
 // analysis, owns its work space and sequences the kernels of one evaluation.
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -643,6 +644,16 @@ int run_roq_tm_mixed(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
   }
   return GWL_OK;
 }
+
+// An NVTX range over a scope (a no-op unless a profiler is attached): the
+// entry points mark their launch sequences, the host paths also their
+// copies.
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // Multi-banding with the IFFT-FFT <h|h>: the odd-bin transforms of every band
 // b >= 1 into the slab that the multi-banding kernels add to <h|h>.
@@ -1978,12 +1989,23 @@ int gwl_set_roq_time_marginalization(gwl_analysis* a, int64_t n_times, const dou
   return GWL_OK;
 }
 
+int gwl_trace_push(const char* name) {
+  nvtxRangePushA(name ? name : "gwl");
+  return GWL_OK;
+}
+
+int gwl_trace_pop(void) {
+  nvtxRangePop();
+  return GWL_OK;
+}
+
 int gwl_eval_device(gwl_analysis* a, const double* params, int64_t B, int32_t precision, double* out, void* stream) {
   if (!a || (B > 0 && (!params || !out))) {
     set_error("null argument");
     return GWL_ERR_ARGUMENT;
   }
   std::lock_guard<std::mutex> g(a->mu);
+  TraceRange tr("gwl_eval_device");
   return run_eval(a, params, B, precision, out, nullptr, nullptr, static_cast<cudaStream_t>(stream));
 }
 
@@ -2030,16 +2052,31 @@ namespace {
 // h_out (the caller holds the analysis lock): upload, launch sequence,
 // download of the results and the device status word, one synchronisation.
 int eval_staged(gwl_analysis* a, int64_t B, int32_t precision) {
-  GWL_CUDA(cudaMemcpyAsync(a->d_params, a->h_params, sizeof(double) * GWL_NPARAM * B, cudaMemcpyHostToDevice,
-                           a->stream));
-  int rc = run_eval(a, a->d_params, B, precision, a->d_out, nullptr, nullptr, a->stream);
-  if (rc) return rc;
-  GWL_CUDA(cudaMemcpyAsync(a->h_out, a->d_out, sizeof(double) * B, cudaMemcpyDeviceToHost, a->stream));
+  TraceRange tr("gwl_eval_host");
+  {
+    TraceRange t1("h2d");
+    GWL_CUDA(cudaMemcpyAsync(a->d_params, a->h_params, sizeof(double) * GWL_NPARAM * B, cudaMemcpyHostToDevice,
+                             a->stream));
+  }
+  {
+    TraceRange t2("launch");
+    int rc = run_eval(a, a->d_params, B, precision, a->d_out, nullptr, nullptr, a->stream);
+    if (rc) return rc;
+  }
   int* h_status = reinterpret_cast<int*>(a->h_out + B);
-  GWL_CUDA(cudaMemcpyAsync(h_status, a->d_status, sizeof(int), cudaMemcpyDeviceToHost, a->stream));
-  GWL_CUDA(cudaStreamSynchronize(a->stream));
+  {
+    TraceRange t3("readback");
+    GWL_CUDA(cudaMemcpyAsync(a->h_out, a->d_out, sizeof(double) * B, cudaMemcpyDeviceToHost, a->stream));
+    GWL_CUDA(cudaMemcpyAsync(h_status, a->d_status, sizeof(int), cudaMemcpyDeviceToHost, a->stream));
+    GWL_CUDA(cudaStreamSynchronize(a->stream));
+  }
   if (*h_status != kDevStatusOk) {
+    const int code = *h_status;
     cudaMemset(a->d_status, 0, sizeof(int));
+    if (code == kDevStatusIndex) {
+      set_error("an index check of the checked build failed (the access was skipped)");
+      return GWL_ERR_CHECK;
+    }
     set_error("a bounded device wait gave up (bulk copy did not complete)");
     return GWL_ERR_TIMEOUT;
   }
@@ -2242,6 +2279,7 @@ int gwl_batcher_eval(gwl_batcher* b, const gwl_batch_item* items, int32_t n, int
     return GWL_ERR_ARGUMENT;
   }
   if (n == 0) return GWL_OK;
+  TraceRange tr("gwl_batcher_eval");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   bool fused = precision == GWL_PRECISION_MIXED;
   for (int q = 0; q < n; ++q) {

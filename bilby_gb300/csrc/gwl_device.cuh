@@ -247,6 +247,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Checked builds (-DGWL_CHECK): the gathers and scatters whose indices come
+// from host-built tables (scatter lists, bin maps, transform bins) test the
+// index first; a failed test records kDevStatusIndex in the status word and
+// the access is skipped, so that a bad table reads back as GWL_ERR_CHECK
+// instead of touching memory out of bounds.  Ordinary builds compile the
+// test away.
+#ifdef GWL_CHECK
+__device__ __forceinline__ bool index_ok(int64_t i, int64_t n, int* status) {
+  if (i >= 0 && i < n) return true;
+  if (status) atomicExch(status, kDevStatusIndex);
+  return false;
+}
+#define GWL_INDEX_OK(i, n, status) ::gwl::index_ok((int64_t)(i), (int64_t)(n), (status))
+#else
+#define GWL_INDEX_OK(i, n, status) true
+#endif
+
 // Bounded wait: gives up after `limit` polls, records the failure in the
 // device status word and returns false.  Each poll suspends for a
 // hardware-defined time slice, so the limit bounds the wait to well under a

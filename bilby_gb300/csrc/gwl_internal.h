@@ -28,6 +28,7 @@ constexpr int kOrderMaxKeys = 4096;    // buckets of the point ordering by band 
 constexpr int kDevStatusOk = 0;
 constexpr int kDevStatusTimeout = 1;
 constexpr int kDevStatusBadInput = 2;
+constexpr int kDevStatusIndex = 3;  // checked builds (-DGWL_CHECK): an index check failed, the access was skipped
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a bulk-copy barrier before giving up
 // Refinement of the TaylorF2 mixed-precision result (see LaunchArgs::rf_tol):
 // the error bound of a point is kRefineL2 * L2 + kRefineL1 * L1, with L2 the

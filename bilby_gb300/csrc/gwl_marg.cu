@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         double zr = 0.0, zi = 0.0;
         if (r.valid && k >= k0 && k <= k1) {
           const int b = a.rb_bin[k - k0];
+          if (!GWL_INDEX_OK(b, nE - 1, a.status)) continue;
           const double fb0 = a.rb_freq[b], fb1 = a.rb_freq[b + 1];
           const double x = a.freq[k] - (fb1 + fb0) / 2, width = fb1 - fb0;
 #pragma unroll
@@ -350,6 +351,7 @@ __global__ void __launch_bounds__(kTmThreads) k_time_marg(LaunchArgs a, const ty
         for (int32_t c = a.mb_tm_ptr[k]; r.valid && c < c1; ++c) {
           const int32_t code = a.mb_tm_src[c];
           const int64_t j = code >= 0 ? (int64_t)code : -(int64_t)code - 1;
+          if (!GWL_INDEX_OK(j, a.mb_points, a.status)) continue;
           const double f = a.mb_freq[j];
           double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
           if (!(tf2 ? tf2_pols_t(a, r, a.mb_pow[j], f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx)))

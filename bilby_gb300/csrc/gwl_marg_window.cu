@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
           if (k < k0 || k > k1) return z;
           // relative.py:380-396: h0_d(f) (r0_b + r1_b (f - f_b)) of bin b
           const int b = a.rb_bin[k - k0];
+          if (!GWL_INDEX_OK(b, nE - 1, a.status)) return z;
           const double fb0 = a.rb_freq[b], fb1 = a.rb_freq[b + 1];
           const double x = a.freq[k] - (fb1 + fb0) / 2, width = fb1 - fb0;
 #pragma unroll
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         const int32_t c1 = a.mb_tm_ptr[k + 1];
         for (int32_t c = a.mb_tm_ptr[k]; c < c1; ++c) {
           const int32_t code = a.mb_tm_src[c];
-          if (code >= 0) {
+          if (code >= 0 && GWL_INDEX_OK(code, a.mb_points, a.status)) {
             const float2 v = zb[code];
             z.x += v.x;
             z.y += v.y;
@@ -513,6 +514,7 @@ __global__ void __launch_bounds__(kWinThreads, MIXED ? 2 : 1)
         for (int32_t c = a.mb_tm_ptr[k]; c < c1; ++c) {
           const int32_t code = a.mb_tm_src[c];
           const int64_t jb = code >= 0 ? (int64_t)code : -(int64_t)code - 1;
+          if (!GWL_INDEX_OK(jb, a.mb_points, a.status)) continue;
           const double f = a.mb_freq[jb];
           double2 hp = make_double2(0.0, 0.0), hx = make_double2(0.0, 0.0);
           if (!(tf2 ? tf2_pols_t(a, r, a.mb_pow[jb], f, u, lnu, pu5, hp, hx) : plain_pols(a, r, f, hp, hx))) continue;

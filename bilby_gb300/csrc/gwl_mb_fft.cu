@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(kMbFftThreads) k_mb_hh_fft(LaunchArgs a, MbFft
           w[e] = make_double2(sw * (sre * cs + sim * sn), sw * (sim * cs - sre * sn));
         }
         const uint32_t m = (uint32_t)(bd.ks + t);  // 1 <= m < M / 2 (checked on the host)
+        if (!GWL_INDEX_OK((int64_t)m - 1, half - 1, a.status)) continue;
         buf[m] = make_double2(w[0].x - w[1].y, w[0].y + w[1].x);
         buf[M - m] = make_double2(w[0].x + w[1].y, w[1].x - w[0].y);
       }

@@ -22,6 +22,7 @@ admission and failure paths be tested without a GPU.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import contextlib
 import threading
 import time
 from collections import deque
@@ -96,6 +97,17 @@ class GpuBackend:
         self._arenas = [None] * n_slots
 
     @staticmethod
+    @contextlib.contextmanager
+    def trace(name: str):
+        """An NVTX range (a no-op unless a profiler is attached)."""
+        lib = _capi.load()
+        lib.gwl_trace_push(name.encode())
+        try:
+            yield
+        finally:
+            lib.gwl_trace_pop()
+
+    @staticmethod
     def resident_bytes(analysis) -> int:
         return analysis.resident_bytes()
 
@@ -135,11 +147,14 @@ class GpuBackend:
             off += n
         stream = self.streams[slot]
         with torch.cuda.stream(stream):
-            dev_in[:_capi.NPARAM * off].copy_(pin_in[:_capi.NPARAM * off], non_blocking=True)
-            self.batchers[slot].eval_device(raw, self.precision, stream.cuda_stream)
-            pin_out[:off].copy_(dev_out[:off], non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(stream)
+            with self.trace("h2d"):
+                dev_in[:_capi.NPARAM * off].copy_(pin_in[:_capi.NPARAM * off], non_blocking=True)
+            with self.trace("launch"):
+                self.batchers[slot].eval_device(raw, self.precision, stream.cuda_stream)
+            with self.trace("readback"):
+                pin_out[:off].copy_(dev_out[:off], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(stream)
         return (ev, spans, pin_out, None, slot)
 
     @staticmethod
@@ -320,7 +335,9 @@ class LikelihoodServer:
             with self.cv:
                 if len(self.inflight) < self.n_streams and self.pending:
                     slot = min(set(range(self.n_streams)) - self._busy_slots)
-                    take, pts = self._take()
+                    trace = getattr(self.backend, "trace", None)
+                    with trace("admission") if trace else contextlib.nullcontext():
+                        take, pts = self._take()
                     if take:
                         self._busy_slots.add(slot)
                     else:

@@ -42,7 +42,8 @@ typedef enum {
   GWL_ERR_MEMORY = 3,        /* device allocation failed or HBM budget exceeded */
   GWL_ERR_UNSUPPORTED = 4,   /* model / option not implemented (NotImplementedError) */
   GWL_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
-  GWL_ERR_STATE = 6          /* handle not configured for the request */
+  GWL_ERR_STATE = 6,         /* handle not configured for the request */
+  GWL_ERR_CHECK = 7          /* checked builds (-DGWL_CHECK): a device index check failed */
 } gwl_status;
 
 typedef enum {
@@ -343,6 +344,13 @@ int gwl_set_multiband_time_marginalization(gwl_analysis *a, int64_t n_fft, const
  * 4 / That_b, sqrt_window [n_points] the square roots of the band windows,
  * odd_weights [n_det][sum over b >= 1 of m[b] / 2] (Re I_b[2j + 1], band
  * after band).  enable = 0 switches it off; a new gwl_set_multiband does too. */
+/* NVTX ranges (no-ops unless a profiler is attached).  The library marks
+ * its entry points (gwl_eval_device, gwl_eval_host with its h2d / launch /
+ * readback steps, gwl_batcher_eval); a caller marks its own phases, e.g. a
+ * server's admission, with these.  No counterpart in the reference. */
+int gwl_trace_push(const char *name);
+int gwl_trace_pop(void);
+
 int gwl_set_multiband_ifft_fft(gwl_analysis *a, int enable, const int32_t *ks, const int32_t *m, const double *scale,
                                const double *sqrt_window, const double *odd_weights);
 

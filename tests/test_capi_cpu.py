@@ -115,3 +115,11 @@ def test_twiddle_tables_are_keyed_by_device_and_length(tmp_path):
                     str(exe), "-pthread"], check=True)
     res = subprocess.run([str(exe)], capture_output=True, text=True)
     assert res.returncode == 0 and res.stdout.strip() == "ok", (res.returncode, res.stdout)
+
+
+def test_trace_ranges_need_no_profiler(lib):
+    """The NVTX entry points are no-ops without a profiler attached (no GPU
+    needed) and balance."""
+    for name in (b"admission", b"launch"):
+        assert lib.gwl_trace_push(name) == _capi.GWL_OK
+        assert lib.gwl_trace_pop() == _capi.GWL_OK
