@@ -23,8 +23,13 @@ Every pair of bases a batch uses gets its own device-resident analysis (the
 same data, that pair's nodes and weights); a batch is grouped by pair,
 evaluated pair by pair and put back in order.
 
-Not built: multi-banded ROQ weights (NotImplementedError); hdf5 files need
-h5py, as in the reference.
+Bases come as arrays, .npy files, or a mapping laid out as an ROQ basis file
+(``basis_<type>``, and optionally ``prior_range_<type>``,
+``multiband_<type>``, ``durations_s_<type>``,
+``start_end_frequency_bins_<type>``): bases outside the prior are dropped
+(roq.py:368-400, 771-791), and a multi-banded basis gets its weights from the
+band-wise down-sampled data and inverse PSD (roq.py:920-974, 1007-1055).
+Basis files themselves need h5py, as in the reference.
 """
 from __future__ import annotations
 
@@ -249,7 +254,13 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
     @staticmethod
     def _parse_basis(basis, basis_type):
         """roq.py:333-366: an array (n_frequencies x n_basis) or a .npy file
-        (n_basis x n_frequencies) -> {basis_<type>: {"0": {"basis": n_basis x n_frequencies}}}."""
+        (n_basis x n_frequencies) -> {basis_<type>: {"0": {"basis": n_basis x n_frequencies}}}.
+        A mapping with the layout of a basis file (what h5py would open) is
+        taken as it is."""
+        if hasattr(basis, "keys") and not isinstance(basis, np.ndarray):
+            if f"basis_{basis_type}" not in basis:
+                raise ValueError(f"a {basis_type} basis mapping needs the key basis_{basis_type}")
+            return basis
         if isinstance(basis, str):
             fmt = basis.split(".")[-1]
             if fmt == "npy":
@@ -317,8 +328,23 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         n = int(2 ** np.ceil(np.log2(n)))
         return duration / n
 
+    def _select_prior_ranges(self, prior_ranges):
+        """roq.py:368-400: the bases whose prior ranges meet the priors."""
+        names = list(prior_ranges)
+        n = len(prior_ranges[names[0]])
+        keep = np.ones(n, dtype=bool)
+        for name in names:
+            if self.priors is None or name not in self.priors:
+                continue
+            pr = np.asarray(prior_ranges[name])
+            keep &= (pr[:, 1] >= self.priors[name].minimum) & (pr[:, 0] <= self.priors[name].maximum)
+        idx = np.arange(n)[keep]
+        return idx, {name: np.asarray(prior_ranges[name])[idx] for name in names}
+
     def _set_weights(self, linear_matrix, quadratic_matrix):
-        """roq.py:736-1005 for one basis of each kind, no multi-banding."""
+        """roq.py:736-847: the time grid, the bases inside the prior and their
+        frequency nodes, then the linear and quadratic weights of each basis
+        (multi-banded or on the data's own frequencies)."""
         ifos = self.interferometers
         duration = float(ifos[0].strain_data.duration)
         start_time = float(ifos[0].strain_data.start_time)
@@ -329,38 +355,159 @@ class ROQGravitationalWaveTransient(GravitationalWaveTransient):
         start_idx = max(0, int(np.floor((tp.minimum - crossing - start_time) / time_space)))
         end_idx = min(n_time - 1, int(np.ceil((tp.maximum + crossing - start_time) / time_space)))
         self.weights["time_samples"] = np.arange(start_idx, end_idx + 1) * float(time_space)
-        lin = np.asarray(linear_matrix["basis_linear"]["0"]["basis"])
-        quad = np.asarray(quadratic_matrix["basis_quadratic"]["0"]["basis"]).real
+        selected = {}
         for key, matrix in (("linear", linear_matrix), ("quadratic", quadratic_matrix)):
-            node = matrix[f"basis_{key}"]["0"]
-            if "frequency_nodes" in node:
-                self.weights[f"frequency_nodes_{key}"] = [np.asarray(node["frequency_nodes"]) * self.roq_scale_factor]
-        for ifo in ifos:
-            mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
-            fm = np.asarray(ifo.strain_data.frequency_array)[mask]
-            if self.roq_params is not None:
-                fmax = self.roq_params["fhigh"] * self.roq_scale_factor
-                seglen = self.roq_params["seglen"] / self.roq_scale_factor
-                roq_f = np.linspace(0, fmax, int(np.round(fmax * seglen)) + 1)
-                roq_f = roq_f[roq_f >= self.roq_params["flow"] * self.roq_scale_factor]
-                _, ifo_idxs, roq_idxs = np.intersect1d(fm, roq_f, return_indices=True)
+            pr_key = f"prior_range_{key}"
+            if pr_key in matrix:
+                ranges = {}
+                for name in matrix[pr_key]:
+                    attrs = getattr(matrix[pr_key][name], "attrs", {})
+                    power = attrs["roq_scale_power"] if "roq_scale_power" in attrs else None
+                    scale = self.roq_scale_factor ** power if power is not None else 1.
+                    ranges[name] = np.asarray(matrix[pr_key][name][()]) * scale
+                idx, sel = self._select_prior_ranges(ranges)
+                if len(idx) == 0:
+                    raise BilbyROQParamsRangeError(f"There are no {key} ROQ bases within the prior range.")
+                self.weights[pr_key] = sel
+                selected[key] = [int(i) for i in idx]
             else:
-                roq_idxs = np.arange(lin.shape[1], dtype=int)
-                ifo_idxs = np.arange(int(mask.sum()))
-                if len(ifo_idxs) != len(roq_idxs):
-                    raise ValueError(f"Mismatch between ROQ basis and frequency array for {ifo.name}")
-            nonzero = ifo_idxs + int(ifo.minimum_frequency * duration)
-            d_over_s = (np.asarray(ifo.strain_data.frequency_domain_strain)[mask][ifo_idxs]
-                        / np.asarray(ifo.power_spectral_density_array)[mask][ifo_idxs])
-            rows = []
-            for c0 in range(0, lin.shape[0], 16):  # inverse FFTs of 16 basis elements at a time
-                block = np.zeros((min(16, lin.shape[0] - c0), n_time), dtype=complex)
-                block[:, nonzero] = d_over_s * np.conj(lin[c0:c0 + 16][:, roq_idxs])
-                rows.append(np.fft.ifft(block, axis=1)[:, start_idx:end_idx + 1])
-            w = np.concatenate(rows).T * (4. * n_time / duration)
-            self.weights[ifo.name + "_linear"] = [w]
-            inv_psd = 1 / np.asarray(ifo.power_spectral_density_array)[mask][ifo_idxs]
-            self.weights[ifo.name + "_quadratic"] = [4. / duration * quad[:, roq_idxs] @ inv_psd]
+                selected[key] = [0]
+            if "frequency_nodes" in matrix[f"basis_{key}"][str(selected[key][0])]:
+                self.weights[f"frequency_nodes_{key}"] = [
+                    np.asarray(matrix[f"basis_{key}"][str(i)]["frequency_nodes"][()]) * self.roq_scale_factor
+                    for i in selected[key]]
+        mb_lin = bool(np.asarray(linear_matrix["multiband_linear"][()])) if "multiband_linear" in linear_matrix \
+            else False
+        mb_quad = bool(np.asarray(quadratic_matrix["multiband_quadratic"][()])) \
+            if "multiband_quadratic" in quadratic_matrix else False
+        idxs = None
+        if not (mb_lin and mb_quad):
+            n_basis_f = np.asarray(linear_matrix["basis_linear"][str(selected["linear"][0])]["basis"]).shape[1]
+            idxs = {ifo.name: self._overlap_indices(ifo, n_basis_f) for ifo in ifos}
+        if mb_lin:
+            self._set_weights_linear_multiband(linear_matrix, selected["linear"])
+        else:
+            self._set_weights_linear(linear_matrix, selected["linear"], idxs, n_time, start_idx, end_idx)
+        if mb_quad:
+            self._set_weights_quadratic_multiband(quadratic_matrix, selected["quadratic"])
+        else:
+            self._set_weights_quadratic(quadratic_matrix, selected["quadratic"], idxs)
+
+    def _overlap_indices(self, ifo, n_basis_frequencies):
+        """roq.py:802-837: (indices into the data's masked frequencies, indices
+        into the basis' frequencies) of the frequencies both share."""
+        mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+        fm = np.asarray(ifo.strain_data.frequency_array)[mask]
+        if self.roq_params is not None:
+            fmax = self.roq_params["fhigh"] * self.roq_scale_factor
+            seglen = self.roq_params["seglen"] / self.roq_scale_factor
+            roq_f = np.linspace(0, fmax, int(np.round(fmax * seglen)) + 1)
+            roq_f = roq_f[roq_f >= self.roq_params["flow"] * self.roq_scale_factor]
+            _, ifo_idxs, roq_idxs = np.intersect1d(fm, roq_f, return_indices=True)
+        else:
+            roq_idxs = np.arange(n_basis_frequencies, dtype=int)
+            ifo_idxs = np.arange(int(mask.sum()))
+            if len(ifo_idxs) != len(roq_idxs):
+                raise ValueError(f"Mismatch between ROQ basis and frequency array for {ifo.name}")
+        return ifo_idxs, roq_idxs
+
+    def _set_weights_linear(self, linear_matrix, basis_idxs, idxs, n_time, start_idx, end_idx):
+        """roq.py:849-918: per basis and detector, the inverse FFT of d/S times
+        each conjugated basis element, kept on the time grid."""
+        duration = float(self.interferometers[0].strain_data.duration)
+        for ifo in self.interferometers:
+            self.weights[ifo.name + "_linear"] = []
+        for i in basis_idxs:
+            lin = np.asarray(linear_matrix["basis_linear"][str(i)]["basis"][()])
+            for ifo in self.interferometers:
+                ifo_idxs, roq_idxs = idxs[ifo.name]
+                mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+                nonzero = ifo_idxs + int(ifo.minimum_frequency * duration)
+                d_over_s = (np.asarray(ifo.strain_data.frequency_domain_strain)[mask][ifo_idxs]
+                            / np.asarray(ifo.power_spectral_density_array)[mask][ifo_idxs])
+                rows = []
+                for c0 in range(0, lin.shape[0], 16):  # inverse FFTs of 16 basis elements at a time
+                    block = np.zeros((min(16, lin.shape[0] - c0), n_time), dtype=complex)
+                    block[:, nonzero] = d_over_s * np.conj(lin[c0:c0 + 16][:, roq_idxs])
+                    rows.append(np.fft.ifft(block, axis=1)[:, start_idx:end_idx + 1])
+                self.weights[ifo.name + "_linear"].append(np.concatenate(rows).T * (4. * n_time / duration))
+
+    def _set_weights_quadratic(self, quadratic_matrix, basis_idxs, idxs):
+        """roq.py:976-1005: (4/T) basis times 1/S per basis and detector."""
+        for ifo in self.interferometers:
+            self.weights[ifo.name + "_quadratic"] = []
+        for i in basis_idxs:
+            quad = np.asarray(quadratic_matrix["basis_quadratic"][str(i)]["basis"][()]).real
+            for ifo in self.interferometers:
+                ifo_idxs, roq_idxs = idxs[ifo.name]
+                mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+                inv_psd = 1 / np.asarray(ifo.power_spectral_density_array)[mask][ifo_idxs]
+                self.weights[ifo.name + "_quadratic"].append(
+                    4. / float(ifo.strain_data.duration) * quad[:, roq_idxs] @ inv_psd)
+
+    @staticmethod
+    def _band_layout(matrix, basis_type, scale):
+        tbs = np.asarray(matrix[f"durations_s_{basis_type}"][()], dtype=np.float64) / scale
+        se = np.asarray(matrix[f"start_end_frequency_bins_{basis_type}"][()]).astype(np.int64)
+        return tbs, se, int(np.sum(se[:, 1] - se[:, 0] + 1)), float(np.max(se[:, 1] / tbs))
+
+    def _set_weights_linear_multiband(self, linear_matrix, basis_idxs):
+        """roq.py:920-974: d/S (zero outside the mask) up to the basis' top
+        frequency to the time domain, each band's last 2 f_high T_b samples
+        back to its frequencies k / T_b, times (4 / T_b) exp(2 pi i f (t - T +
+        T_b)) on the time grid; the weights are the conjugated basis times
+        that, per detector."""
+        tbs, se, dim, fhigh = self._band_layout(linear_matrix, "linear", self.roq_scale_factor)
+        ts = np.asarray(self.weights["time_samples"], dtype=np.float64)
+        for ifo in self.interferometers:
+            self.weights[ifo.name + "_linear"] = []
+        bases = [np.asarray(linear_matrix["basis_linear"][str(i)]["basis"][()]) for i in basis_idxs]
+        for ifo in self.interferometers:
+            T = float(ifo.strain_data.duration)
+            mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+            strain = np.asarray(ifo.strain_data.frequency_domain_strain)
+            psd = np.asarray(ifo.power_spectral_density_array)
+            data = np.zeros(int(fhigh * T) + 1, dtype=complex)
+            data[np.arange(len(strain))[mask]] = strain[mask] / psd[mask]
+            td = np.fft.irfft(data)
+            shifted = np.zeros((dim, len(ts)), dtype=complex)
+            off = 0
+            for b, tb in enumerate(tbs):
+                s0, e0 = (int(x) for x in se[b])
+                fs = np.arange(s0, e0 + 1) / tb
+                db = np.fft.rfft(td[-int(2. * fhigh * tb):])[s0:e0 + 1]
+                shifted[off:off + e0 - s0 + 1] = 4. / tb * db[:, None] * np.exp(
+                    2. * np.pi * 1j * fs[:, None] * (ts[None, :] - T + tb))
+                off += e0 - s0 + 1
+            for basis in bases:
+                self.weights[ifo.name + "_linear"].append((basis.conj() @ shifted).T)
+            del shifted
+
+    def _set_weights_quadratic_multiband(self, quadratic_matrix, basis_idxs):
+        """roq.py:1007-1055: 1/S (zero outside the mask) up to the basis' top
+        frequency to the time domain, truncated to lags |n| < f_high T_b and
+        back to each band's frequencies, times 4 / T_b; the weights are the
+        basis times that, per detector."""
+        tbs, se, dim, fhigh = self._band_layout(quadratic_matrix, "quadratic", self.roq_scale_factor)
+        for ifo in self.interferometers:
+            self.weights[ifo.name + "_quadratic"] = []
+        bases = [np.asarray(quadratic_matrix["basis_quadratic"][str(i)]["basis"][()]).real for i in basis_idxs]
+        for ifo in self.interferometers:
+            T = float(ifo.strain_data.duration)
+            mask = np.asarray(ifo.strain_data.frequency_mask, dtype=bool)
+            psd = np.asarray(ifo.power_spectral_density_array)
+            inv = np.zeros(int(fhigh * T) + 1)
+            inv[np.arange(len(psd))[mask]] = 1. / psd[mask]
+            td = np.fft.irfft(inv)
+            v = np.zeros(dim)
+            off = 0
+            for b, tb in enumerate(tbs):
+                s0, e0 = (int(x) for x in se[b])
+                h = int(fhigh * tb)
+                v[off:off + e0 - s0 + 1] = 4. / tb * np.fft.rfft(np.concatenate([td[:h], td[-h:]]))[s0:e0 + 1].real
+                off += e0 - s0 + 1
+            for basis in bases:
+                self.weights[ifo.name + "_quadratic"].append(basis @ v)
 
     def _setup_time_marginalization(self):
         """roq.py:320-331: delta_tc from the constructor or the ROQ time

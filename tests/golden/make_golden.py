@@ -55,6 +55,12 @@ Outputs
     dictionary merged from single-basis weights): the sampler-style draws,
     the basis pair the reference selected for each, and its lnL ratios
     without and with time marginalisation.
+``tests/golden/tf2_marg_8s_2k_roq_multiband.npz``
+    The reference's ROQ weights built from a seeded multi-banded basis
+    (``oracle/roq_basis.build_multiband``: three bands of 8, 4 and 2 s) -- the
+    rows of the linear weights the stored points read and the quadratic
+    weights -- and its lnL ratios without marginalisation, with time, and with
+    time, phase and distance marginalisation.
 ``tests/golden/priors.npz``
     The reference's ``PriorDict.rescale`` of fixed unit-cube samples for the
     GW prior kinds the device rescaler supports, followed by
@@ -442,6 +448,82 @@ def run_roq(bilby, name="tf2_marg_8s_2k", n_fixed=8, n_random=8):
                 out[f"roq_quadratic_{q}"] = np.asarray(like.weights[ifo.name + "_quadratic"][0])
             out["checksum"] = strain_checksum(ifos)
     np.savez_compressed(os.path.join(HERE, f"{name}_roq.npz"), **out)
+
+
+def run_roq_multiband(bilby, name="tf2_marg_8s_2k", n_fixed=6, n_random=6):
+    """The reference's ROQ likelihood with a seeded multi-banded basis
+    (roq.py:793-1055, _set_weights_linear_multiband and
+    _set_weights_quadratic_multiband; oracle/roq_basis.build_multiband).  The
+    reference reads such a basis from an hdf5 file only, so its _set_weights
+    runs here on the basis dictionary, and a likelihood built from the
+    resulting weights gives the lnL ratios without marginalisation, with
+    time, and with time, phase and distance marginalisation."""
+    from oracle import roq_basis
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.draw_seed + 7)
+    pf = draw_points(w, n_fixed, rng, fixed_extrinsic=True)
+    pr = draw_points(w, n_random, rng, fixed_extrinsic=False)
+    params = {k: np.concatenate([pf[k], pr[k]]) for k in pf}
+    params.pop("time_jitter", None)
+    n = n_fixed + n_random
+    jitter = rng.uniform(-1.0 / w.sampling_frequency, 1.0 / w.sampling_frequency, n)
+    out = {"p_" + k: v for k, v in params.items()}
+    out["time_jitter"] = jitter
+    lin, quad = roq_basis.build_multiband(minimum_frequency=w.minimum_frequency)
+    nl = lin["basis_linear"]["0"]["frequency_nodes"]
+    nq = quad["basis_quadratic"]["0"]["frequency_nodes"]
+    weights = None
+    for combo in ("none", "t", "tpd"):
+        ifos, _ = build_reference(bilby, w, taylorf2_aligned)
+        wfg = bilby.gw.waveform_generator.WaveformGenerator(
+            duration=w.duration, sampling_frequency=w.sampling_frequency, start_time=w.start_time,
+            frequency_domain_source_model=taylorf2_aligned_roq,
+            waveform_arguments=dict(minimum_frequency=w.minimum_frequency, frequency_nodes_linear=nl,
+                                    frequency_nodes_quadratic=nq))
+        t, p, d = "t" in combo, "p" in combo, "d" in combo
+        priors = make_priors(bilby, w, True, p, d)
+        if weights is None:
+            fm = ifos[0].frequency_array[ifos[0].frequency_mask]
+            _, bl0, _, bq0 = roq_basis.build(fm, n_linear=4, n_quadratic=2, n_train=20,
+                                             minimum_frequency=w.minimum_frequency)
+            seed_like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+                interferometers=ifos, waveform_generator=wfg, priors=priors, linear_matrix=bl0.T,
+                quadratic_matrix=bq0.T)
+            seed_like.weights = dict()
+            seed_like._set_weights(linear_matrix=lin, quadratic_matrix=quad)
+            weights = seed_like.weights
+        like = bilby.gw.likelihood.ROQGravitationalWaveTransient(
+            interferometers=ifos, waveform_generator=wfg, priors=priors, weights=weights,
+            time_marginalization=t, phase_marginalization=p, distance_marginalization=d)
+        vals = []
+        for i in range(n):
+            q = point(params, i)
+            if t:
+                q["geocent_time"] = float(priors["geocent_time"])
+                q["time_jitter"] = float(jitter[i])
+            if p:
+                q["phase"] = 0.0
+            if d:
+                q["luminosity_distance"] = float(priors["luminosity_distance"])
+            vals.append(like.log_likelihood_ratio(q))
+        out["lnl_" + combo] = np.array(vals)
+        print(f"{name} multi-banded roq[{combo}]: {out['lnl_' + combo][:4]}")
+        if combo == "none":
+            ts = np.asarray(weights["time_samples"])
+            out["roq_time_meta"] = np.array([ts[0], ts[1] - ts[0], len(ts)])
+            for q, ifo in enumerate(ifos):
+                rows = set()
+                for i in range(n):
+                    pt = point(params, i)
+                    dt = ifo.time_delay_from_geocenter(pt["ra"], pt["dec"], pt["geocent_time"])
+                    c = int(np.floor((pt["geocent_time"] - ifo.strain_data.start_time + dt - ts[0]) / (ts[1] - ts[0])))
+                    rows.update(min(max(c + k, 0), len(ts) - 1) for k in range(-2, 3))
+                rows = np.array(sorted(rows))
+                out[f"roq_linear_rows_{q}"] = rows
+                out[f"roq_linear_{q}"] = np.asarray(weights[ifo.name + "_linear"][0])[rows]
+                out[f"roq_quadratic_{q}"] = np.asarray(weights[ifo.name + "_quadratic"][0])
+            out["checksum"] = strain_checksum(ifos)
+    np.savez_compressed(os.path.join(HERE, f"{name}_roq_multiband.npz"), **out)
 
 
 # two seeded synthetic bases over overlapping chirp-mass ranges; the
@@ -916,8 +998,18 @@ def main():
     ap.add_argument("--marg-only", action="store_true")
     ap.add_argument("--time-prior-only", action="store_true")
     ap.add_argument("--roq-multibasis-only", action="store_true")
+    ap.add_argument("--roq-multiband-only", action="store_true")
     args = ap.parse_args()
     bilby = ref_harness.import_bilby()
+    if args.roq_multiband_only:
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as tmp:
+            os.chdir(tmp)
+            try:
+                run_roq_multiband(bilby)
+            finally:
+                os.chdir(cwd)
+        return
     if args.roq_multibasis_only or args.time_prior_only:
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as tmp:
@@ -1014,6 +1106,7 @@ def main():
                 run_multiband_ifft(bilby, "tf2_128s", 4, 4)
                 run_roq(bilby)
                 run_roq_multibasis(bilby)
+                run_roq_multiband(bilby)
                 run_snrs(bilby)
                 run_fast_snrs(bilby)
                 run_roq_snrs(bilby)

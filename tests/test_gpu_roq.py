@@ -60,7 +60,14 @@ def make(combo, tmp_path, **kw):
                                                  DISTANCE_PRIOR["maximum"])
     z = golden("tf2_marg_8s_2k_roq")
     from_basis = kw.pop("basis", False)
-    if "t" in combo or from_basis:
+    if kw.pop("multiband", False):
+        from oracle import roq_basis
+        lin, quad = roq_basis.build_multiband(minimum_frequency=w.minimum_frequency)
+        wfg.waveform_arguments.update(frequency_nodes_linear=lin["basis_linear"]["0"]["frequency_nodes"],
+                                      frequency_nodes_quadratic=quad["basis_quadratic"]["0"]["frequency_nodes"])
+        source = dict(linear_matrix=lin, quadratic_matrix=quad)
+        z = golden("tf2_marg_8s_2k_roq_multiband")
+    elif "t" in combo or from_basis:
         from oracle import roq_basis
         fm = ifos[0].frequency_array[ifos[0].frequency_mask]
         nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
@@ -100,6 +107,31 @@ def test_lnl_matches_the_reference(gpu, tmp_path, combo):
     rtol = 1e-8 if "d" in combo else 1e-9
     assert np.all(np.abs(single - ref) <= rtol * np.maximum(1.0, np.abs(ref))), single - ref
 
+
+
+@pytest.mark.parametrize("combo", ["none", "t", "tpd"])
+def test_multiband_basis_matches_the_reference(gpu, tmp_path, combo):
+    """Weights built from a multi-banded basis (roq.py:920-974, 1007-1055; the
+    seeded three-band basis of oracle/roq_basis.build_multiband) give the
+    reference's lnL ratios (tests/golden/tf2_marg_8s_2k_roq_multiband.npz),
+    without marginalisation, with time, and with time, phase and distance."""
+    like, priors, z = make(combo, tmp_path, multiband=True)
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    pts = []
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        if "t" in combo:
+            q["geocent_time"] = float(priors["geocent_time"])
+            q["time_jitter"] = float(z["time_jitter"][i])
+        if "p" in combo:
+            q["phase"] = 0.0
+        if "d" in combo:
+            q["luminosity_distance"] = float(priors["luminosity_distance"])
+        pts.append(q)
+    ref = z["lnl_" + combo]
+    got = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
+    rtol = 1e-8 if "d" in combo else 1e-9
+    assert np.all(np.abs(got - ref) <= rtol * np.maximum(1.0, np.abs(ref))), got - ref
 
 
 def marginalized_points(params, priors, combo, jitter):

@@ -1,8 +1,11 @@
 """The host construction of the GPU ROQ likelihood's weights
 (bilby/gw/likelihood/roq.py:736-1005: time grid, linear weights by inverse
 FFTs, quadratic weights) reproduces the reference's weights for the same
-seeded synthetic basis (tests/golden/tf2_marg_8s_2k_roq.npz).  No GPU."""
+seeded synthetic basis (tests/golden/tf2_marg_8s_2k_roq.npz), and for a
+multi-banded basis (tests/golden/tf2_marg_8s_2k_roq_multiband.npz); bases
+outside the prior are dropped.  No GPU."""
 import numpy as np
+import pytest
 
 from tests.conftest import golden
 from oracle import data as OD
@@ -35,7 +38,9 @@ class _Uniform:
         self.minimum, self.maximum = lo, hi
 
 
-def test_weights_match_the_reference():
+def _host_likelihood():
+    """The product's ROQ class with the oracle's data of tf2_marg_8s_2k and
+    its time prior, ready for _set_weights (no GPU)."""
     from bilby_gb300.roq import ROQGravitationalWaveTransient
     w = WORKLOADS["tf2_marg_8s_2k"]
     dets = OD.build_workload(w)
@@ -48,8 +53,6 @@ def test_weights_match_the_reference():
         m = d.mask
         snr = np.sqrt(R.noise_weighted_inner_product(s[m], s[m], d.psd[m], d.duration).real)
         ifos.append(_Ifo(d, snr))
-    fm = dets[0].frequency[dets[0].mask]
-    nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
     like = object.__new__(ROQGravitationalWaveTransient)
     like.interferometers = ifos
     tc = w.injection["geocent_time"]
@@ -58,8 +61,10 @@ def test_weights_match_the_reference():
     like.roq_params = None
     like.roq_scale_factor = 1
     like.weights = {}
-    like._set_weights(like._parse_basis(bl.T, "linear"), like._parse_basis(bq.T, "quadratic"))
-    z = golden("tf2_marg_8s_2k_roq")
+    return like, w, dets, ifos
+
+
+def _check_weights(like, ifos, z):
     ts = like.weights["time_samples"]
     t0, dt, n = z["roq_time_meta"]
     assert len(ts) == int(n) and ts[0] == t0 and ts[1] - ts[0] == dt
@@ -69,6 +74,49 @@ def test_weights_match_the_reference():
         assert np.max(np.abs(lin - ref)) <= 1e-10 * np.max(np.abs(ref))
         quad = like.weights[ifo.name + "_quadratic"][0]
         assert np.max(np.abs(quad - z[f"roq_quadratic_{q}"])) <= 1e-12 * np.max(np.abs(quad))
+
+
+def test_multiband_weights_match_the_reference():
+    """A multi-banded basis (three bands of 8, 4 and 2 s) through
+    _set_weights_linear_multiband / _set_weights_quadratic_multiband
+    (roq.py:920-974, 1007-1055) gives the reference's weights."""
+    like, w, dets, ifos = _host_likelihood()
+    lin, quad = roq_basis.build_multiband(minimum_frequency=w.minimum_frequency)
+    like._set_weights(like._parse_basis(lin, "linear"), like._parse_basis(quad, "quadratic"))
+    assert np.array_equal(like.weights["frequency_nodes_linear"][0], lin["basis_linear"]["0"]["frequency_nodes"])
+    _check_weights(like, ifos, golden("tf2_marg_8s_2k_roq_multiband"))
+
+
+def test_weights_match_the_reference():
+    like, w, dets, ifos = _host_likelihood()
+    fm = dets[0].frequency[dets[0].mask]
+    nl, bl, nq, bq = roq_basis.build(fm, minimum_frequency=w.minimum_frequency)
+    like._set_weights(like._parse_basis(bl.T, "linear"), like._parse_basis(bq.T, "quadratic"))
+    _check_weights(like, ifos, golden("tf2_marg_8s_2k_roq"))
+
+
+def test_bases_outside_the_prior_are_dropped():
+    """roq.py:368-400, 771-791: with prior ranges in the basis mapping only
+    the bases whose ranges meet the priors are built, their ranges and nodes
+    kept in that order; none inside raises."""
+    from bilby_gb300.roq import BilbyROQParamsRangeError
+    like, w, dets, ifos = _host_likelihood()
+    fm = dets[0].frequency[dets[0].mask]
+    _, bl, _, bq = roq_basis.build(fm, n_linear=4, n_quadratic=2, n_train=20, minimum_frequency=w.minimum_frequency)
+    lin = {"basis_linear": {str(i): {"basis": bl * (i + 1), "frequency_nodes": fm[:4] + i} for i in range(3)},
+           "prior_range_linear": {"chirp_mass": np.array([[5., 10.], [10., 20.], [20., 40.]])}}
+    quad = {"basis_quadratic": {"0": {"basis": bq, "frequency_nodes": fm[:2]}}}
+    like._prior["chirp_mass"] = _Uniform(12.0, 30.0)
+    like._set_weights(like._parse_basis(lin, "linear"), like._parse_basis(quad, "quadratic"))
+    assert np.array_equal(like.weights["prior_range_linear"]["chirp_mass"], [[10., 20.], [20., 40.]])
+    assert [float(n[0]) for n in like.weights["frequency_nodes_linear"]] == [fm[0] + 1, fm[0] + 2]
+    for ifo in ifos:
+        a, b = like.weights[ifo.name + "_linear"]
+        np.testing.assert_allclose(b, a * 1.5, rtol=1e-12)
+    like._prior["chirp_mass"] = _Uniform(50.0, 60.0)
+    like.weights = {}
+    with pytest.raises(BilbyROQParamsRangeError):
+        like._set_weights(like._parse_basis(lin, "linear"), like._parse_basis(quad, "quadratic"))
 
 
 def _reference_update_basis(weights, n_bases, basis_type, parameters):
