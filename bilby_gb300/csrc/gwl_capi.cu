@@ -1767,10 +1767,11 @@ int gwl_set_multiband_ifft_fft(gwl_analysis* a, int enable, const int32_t* ks, c
     std::vector<double> od(odd_weights + (size_t)d * total, odd_weights + (size_t)(d + 1) * total);
     if ((rc = upload(a, &a->mbf_odd[d], od))) return rc;
   }
-  // exp(-i pi k / 2^log2m_max), k < 2^log2m_max
+  // exp(-i pi k / 2^log2m_max), k < 2^(log2m_max + 1): the whole circle, as
+  // the radix-4 passes read up to 3/2 of the half circle
   const int64_t n_tw = (int64_t)1 << log2m_max;
-  std::vector<double2> tw((size_t)n_tw);
-  for (int64_t k = 0; k < n_tw; ++k) {
+  std::vector<double2> tw((size_t)(2 * n_tw));
+  for (int64_t k = 0; k < 2 * n_tw; ++k) {
     const double th = M_PI * (double)k / (double)n_tw;
     tw[(size_t)k] = make_double2(std::cos(th), -std::sin(th));
   }

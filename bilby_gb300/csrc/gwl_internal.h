@@ -357,7 +357,7 @@ struct MbFftBand {
   double scale;                  // 4 / That_b
   const double* odd[kMaxDet];    // [M / 2] Re I_(2j+1) of each detector
   const double* sqrtw;           // [mb_points] square roots of the band windows
-  const double2* tw;             // [2^log2m_max] exp(-i pi k / 2^log2m_max)
+  const double2* tw;             // [2^(log2m_max + 1)] exp(-i pi k / 2^log2m_max)
   double* out;                   // the mb_fft_hh slab
 };
 size_t mb_hh_fft_smem(int log2m);  // dynamic shared memory of a transform in shared memory, 0 if it does not fit

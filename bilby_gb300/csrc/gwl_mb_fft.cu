@@ -22,7 +22,8 @@
 //   natural out): F = Z_d1 + i Z_d2;
 //   Z_d1,j = (F_j + conj F_(M-1-j)) / 2, Z_d2,j = (F_j - conj F_(M-1-j)) / 2i
 //   (a real y has Z_(M-1-j) = conj Z_j), for j < M / 2.
-// float64 throughout, radix-2 stages in place.  The transform lives in
+// float64 throughout, in place, radix-4 passes (one radix-2 stage more for
+// an odd log2 M).  The transform lives in
 // shared memory up to 2^kMbFftSmemLog2 samples, above that in a global slot per
 // CTA (a persistent grid of one CTA per SM, whose slots stay in L2).  The
 // partner detector of a point is fixed (d, d + 1), so a point's result does
@@ -91,15 +92,37 @@ __global__ void __launch_bounds__(kMbFftThreads) k_mb_hh_fft(LaunchArgs a, MbFft
     }
     __syncthreads();
     // ---- inverse DFT, decimation in frequency ----------------------------
-    for (int lh = log2m - 1; lh >= 0; --lh) {
-      const uint32_t h = 1u << lh;
+    // radix-4 passes, each two radix-2 stages (half-sizes h and q = h / 2) on
+    // {x0, x1, x2, x3} at i0 + {0, q, 2q, 3q} with W = exp(i pi j / h):
+    //   z0 = (x0 + x2) + (x1 + x3)      z1 = W^2 ((x0 + x2) - (x1 + x3))
+    //   z2 = W ((x0 - x2) + i (x1 - x3))  z3 = W^3 ((x0 - x2) - i (x1 - x3))
+    // then, for odd log2 M, the radix-2 stage h = 1
+    int lh = log2m - 1;
+    for (; lh >= 1; lh -= 2) {
+      const int lq = lh - 1;
+      const uint32_t q = 1u << lq;
+      for (uint32_t t = threadIdx.x; t < (M >> 2); t += blockDim.x) {
+        const uint32_t j = t & (q - 1), i0 = ((t >> lq) << (lq + 2)) + j;
+        const double2 x0 = buf[i0], x1 = buf[i0 + q], x2 = buf[i0 + 2 * q], x3 = buf[i0 + 3 * q];
+        const int s = sh - lh;
+        const double2 w1 = bd.tw[(size_t)j << s], w2 = bd.tw[(size_t)(2 * j) << s], w3 = bd.tw[(size_t)(3 * j) << s];
+        const double ar = x0.x + x2.x, ai = x0.y + x2.y, br = x1.x + x3.x, bi = x1.y + x3.y;
+        const double cr = x0.x - x2.x, ci = x0.y - x2.y, dr = x1.x - x3.x, di = x1.y - x3.y;
+        buf[i0] = make_double2(ar + br, ai + bi);
+        const double er = ar - br, ei = ai - bi;        // times conj(w2)
+        buf[i0 + q] = make_double2(er * w2.x + ei * w2.y, ei * w2.x - er * w2.y);
+        const double fr = cr - di, fi = ci + dr;        // (x0 - x2) + i (x1 - x3), times conj(w1)
+        buf[i0 + 2 * q] = make_double2(fr * w1.x + fi * w1.y, fi * w1.x - fr * w1.y);
+        const double gr = cr + di, gi = ci - dr;        // (x0 - x2) - i (x1 - x3), times conj(w3)
+        buf[i0 + 3 * q] = make_double2(gr * w3.x + gi * w3.y, gi * w3.x - gr * w3.y);
+      }
+      __syncthreads();
+    }
+    if (lh == 0) {
       for (uint32_t t = threadIdx.x; t < half; t += blockDim.x) {
-        const uint32_t j = t & (h - 1), i0 = ((t >> lh) << (lh + 1)) + j, i1 = i0 + h;
-        const double2 x0 = buf[i0], x1 = buf[i1];
-        const double2 w = bd.tw[(size_t)j << (sh - lh)];  // exp(-i pi j / h)
-        const double dx = x0.x - x1.x, dy = x0.y - x1.y;
-        buf[i0] = make_double2(x0.x + x1.x, x0.y + x1.y);
-        buf[i1] = make_double2(dx * w.x + dy * w.y, dy * w.x - dx * w.y);  // times conj(w)
+        const double2 x0 = buf[2 * t], x1 = buf[2 * t + 1];
+        buf[2 * t] = make_double2(x0.x + x1.x, x0.y + x1.y);
+        buf[2 * t + 1] = make_double2(x0.x - x1.x, x0.y - x1.y);
       }
       __syncthreads();
     }
@@ -113,15 +136,37 @@ __global__ void __launch_bounds__(kMbFftThreads) k_mb_hh_fft(LaunchArgs a, MbFft
     }
     __syncthreads();
     // ---- forward DFT, decimation in time ---------------------------------
-    for (int lh = 0; lh < log2m; ++lh) {
-      const uint32_t h = 1u << lh;
+    // for odd log2 M the radix-2 stage h = 1 first, then radix-4 passes, each
+    // two radix-2 stages (h and 2h) on {x0, x1, x2, x3} at i0 + {0, h, 2h, 3h}
+    // with U = exp(-i pi j / 2h), a = x0, b = U^2 x1, c = U x2, d = U^3 x3:
+    //   z0 = (a + b) + (c + d)    z2 = (a + b) - (c + d)
+    //   z1 = (a - b) - i (c - d)  z3 = (a - b) + i (c - d)
+    lh = 0;
+    if (log2m & 1) {
       for (uint32_t t = threadIdx.x; t < half; t += blockDim.x) {
-        const uint32_t j = t & (h - 1), i0 = ((t >> lh) << (lh + 1)) + j, i1 = i0 + h;
-        const double2 x0 = buf[i0], x1 = buf[i1];
-        const double2 w = bd.tw[(size_t)j << (sh - lh)];
-        const double vx = x1.x * w.x - x1.y * w.y, vy = x1.x * w.y + x1.y * w.x;
-        buf[i0] = make_double2(x0.x + vx, x0.y + vy);
-        buf[i1] = make_double2(x0.x - vx, x0.y - vy);
+        const double2 x0 = buf[2 * t], x1 = buf[2 * t + 1];
+        buf[2 * t] = make_double2(x0.x + x1.x, x0.y + x1.y);
+        buf[2 * t + 1] = make_double2(x0.x - x1.x, x0.y - x1.y);
+      }
+      __syncthreads();
+      lh = 1;
+    }
+    for (; lh + 1 < log2m; lh += 2) {
+      const uint32_t h = 1u << lh;
+      for (uint32_t t = threadIdx.x; t < (M >> 2); t += blockDim.x) {
+        const uint32_t j = t & (h - 1), i0 = ((t >> lh) << (lh + 2)) + j;
+        const double2 x0 = buf[i0], x1 = buf[i0 + h], x2 = buf[i0 + 2 * h], x3 = buf[i0 + 3 * h];
+        const int s = sh - lh - 1;
+        const double2 u1 = bd.tw[(size_t)j << s], u2 = bd.tw[(size_t)(2 * j) << s], u3 = bd.tw[(size_t)(3 * j) << s];
+        const double br = x1.x * u2.x - x1.y * u2.y, bi = x1.x * u2.y + x1.y * u2.x;
+        const double cr = x2.x * u1.x - x2.y * u1.y, ci = x2.x * u1.y + x2.y * u1.x;
+        const double dr = x3.x * u3.x - x3.y * u3.y, di = x3.x * u3.y + x3.y * u3.x;
+        const double pr = x0.x + br, pi = x0.y + bi, mr = x0.x - br, mi = x0.y - bi;
+        const double sr = cr + dr, si = ci + di, tr = cr - dr, ti = ci - di;
+        buf[i0] = make_double2(pr + sr, pi + si);
+        buf[i0 + 2 * h] = make_double2(pr - sr, pi - si);
+        buf[i0 + h] = make_double2(mr + ti, mi - tr);      // (a - b) - i (c - d)
+        buf[i0 + 3 * h] = make_double2(mr - ti, mi + tr);  // (a - b) + i (c - d)
       }
       __syncthreads();
     }
