@@ -402,39 +402,85 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
     * ``("spec", key, None)``: the registered likelihood's parameter
       preparation (``ParameterPreparer``), so that the client converts;
 
-    and receives ``("ok", results)`` or ``("error", message)``.  Returns the
-    listener (close it to stop accepting)."""
-    from multiprocessing.connection import Listener
+    and receives ``("ok", results)`` or ``("error", message)``.  One thread
+    accepts connections; one thread waits on all of them at once, reads each
+    request and queues it; the reply is sent when its result is set (from the
+    thread that retires the step), so no thread per client waits on a
+    future.  A client has at most one request in flight, so each connection
+    has one writer at a time.  Returns the listener (close it to stop
+    accepting)."""
+    import socket
+    from multiprocessing.connection import Listener, wait
     listener = Listener(address, authkey=authkey)
+    lock = threading.Lock()
+    watched = {}                      # connection -> client token
+    wake_r, wake_w = socket.socketpair()
+    wake_r.setblocking(False)
 
-    def handle(conn):
-        token = object()
+    def reply(conn, fut):
         try:
-            while True:
-                msg = conn.recv()
-                if not isinstance(msg, tuple) or len(msg) != 3 or \
-                        msg[0] not in ("eval", "eval_parameters", "noise", "spec"):
-                    conn.send(("error", "malformed message"))
-                    continue
-                if msg[0] in ("noise", "spec"):
-                    try:
-                        what = server.noise_log_likelihood if msg[0] == "noise" else server.preparer
-                        conn.send(("ok", what(msg[1])))
-                    except Exception as e:
-                        conn.send(("error", f"{type(e).__name__}: {e}"))
-                    continue
-                if msg[0] == "eval":
-                    fut = server.submit(msg[1], msg[2], client=token)
-                else:
-                    fut = server.submit_parameters(msg[1], msg[2], client=token)
-                try:
-                    conn.send(("ok", fut.result()))
-                except Exception as e:
-                    conn.send(("error", f"{type(e).__name__}: {e}"))
-        except (EOFError, OSError):
+            try:
+                msg = ("ok", fut.result())
+            except Exception as e:
+                msg = ("error", f"{type(e).__name__}: {e}")
+            conn.send(msg)
+        except (OSError, ValueError):
+            pass                       # the client went away; the receiver drops it
+
+    def drop(conn):
+        with lock:
+            token = watched.pop(conn, None)
+        if token is not None:
             server.cancel_client(token)   # the client went away mid-request
-        finally:
+        try:
             conn.close()
+        except OSError:
+            pass
+
+    def handle(conn, msg):
+        if not isinstance(msg, tuple) or len(msg) != 3 or \
+                msg[0] not in ("eval", "eval_parameters", "noise", "spec"):
+            conn.send(("error", "malformed message"))
+            return
+        if msg[0] in ("noise", "spec"):
+            try:
+                what = server.noise_log_likelihood if msg[0] == "noise" else server.preparer
+                conn.send(("ok", what(msg[1])))
+            except Exception as e:
+                conn.send(("error", f"{type(e).__name__}: {e}"))
+            return
+        token = watched.get(conn)
+        if msg[0] == "eval":
+            fut = server.submit(msg[1], msg[2], client=token)
+        else:
+            fut = server.submit_parameters(msg[1], msg[2], client=token)
+        fut.add_done_callback(lambda f, c=conn: reply(c, f))
+
+    def receive():
+        while True:
+            with lock:
+                conns = list(watched)
+            try:
+                ready = wait(conns + [wake_r], timeout=0.5)
+            except OSError:
+                ready = []
+            for conn in ready:
+                if conn is wake_r:
+                    try:
+                        while wake_r.recv(64):
+                            pass
+                    except (BlockingIOError, OSError):
+                        pass
+                    continue
+                try:
+                    msg = conn.recv()
+                except (EOFError, OSError):
+                    drop(conn)
+                    continue
+                try:
+                    handle(conn, msg)
+                except (OSError, ValueError):
+                    drop(conn)
 
     def accept():
         while True:
@@ -442,8 +488,14 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
                 conn = listener.accept()
             except OSError:
                 return
-            threading.Thread(target=handle, args=(conn,), daemon=True).start()
+            with lock:
+                watched[conn] = object()
+            try:
+                wake_w.send(b"x")
+            except OSError:
+                pass
 
+    threading.Thread(target=receive, daemon=True).start()
     threading.Thread(target=accept, daemon=True).start()
     return listener
 
