@@ -699,10 +699,20 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     bf = 2048
     block_f = torch.from_numpy(params_block(draw_points(w, bf, rng))).cuda()
     ifft = {"batch": bf, "transform_lengths": [int(m) for m in like_f.Mbs[1:]],
-            "launch": "prologue + k_mb_hh_fft per band (float64, packed detector pairs) + the multi-banding kernel"}
+            "launch": "prologue + per band k_mb_hh_fft (float64) or k_mb_hh_fft32 (float32 with an error bound, "
+                      "the marked points recomputed by k_mb_hh_fft), packed detector pairs, + the multi-banding "
+                      "kernel"}
+    outs_f = {}
     for precision in ("fp64", "mixed"):
         ms_f, finite = time_launches(like_f.analysis, block_f, bf, steps, warmup, precision=precision)
         ifft[precision] = {"value": bf / (ms_f / 1e3), "unit": "evals/s", "ms_per_launch": ms_f, "finite": finite}
+        o = torch.empty(bf, dtype=torch.float64, device="cuda")
+        like_f.analysis.log_likelihood_ratio_device(block_f.data_ptr(), bf, o.data_ptr(), precision,
+                                                    stream.cuda_stream)
+        torch.cuda.synchronize()
+        outs_f[precision] = o
+    ifft["mixed_over_fp64"] = ifft["mixed"]["value"] / ifft["fp64"]["value"]
+    ifft["max_abs_dlnl_mixed_vs_fp64"] = float((outs_f["mixed"] - outs_f["fp64"]).abs().max().item())
     return {"workload": name, "bands": int(like.number_of_bands),
             "banded_frequencies": int(len(like.banded_frequency_points)), "batch": batch,
             "value": res["fp64"]["value"], "unit": "evals/s", "ms_per_launch": res["fp64"]["ms_per_launch"],

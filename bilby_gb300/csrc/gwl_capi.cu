@@ -138,6 +138,15 @@ struct gwl_analysis {
   double2* d_mbf_scratch = nullptr;
   size_t mbf_scratch_count = 0;  // double2 elements
   int64_t mbf_slots = 0;
+  // mixed precision (TaylorF2): float32 twiddles and amplitude table, the
+  // error slab and the list of points for the float64 recomputation
+  float2* mbf_tw32 = nullptr;
+  float2* mbf_odd32[kMaxDet] = {};
+  float* mbf_aw = nullptr;
+  double mbf_aw_scale = 1.0;
+  double* d_mbf_err = nullptr;
+  int32_t* d_mbf_list = nullptr;  // [B + 1]: the count, then the listed points
+  std::vector<double> mb_freq_h;
   int roq_tm = 0;  // ROQ time-marginalisation grid set for these weights
   int64_t roq_tm_n = 0, roq_tm_chunk = 0, roq_tm_rows = 0;
   double roq_tm_delta_tc = 0.0, roq_tm_antenna_time = 0.0;
@@ -246,8 +255,12 @@ void free_workspace(gwl_analysis* a) {
   a->roq_ws_points = 0;
   cudaFree(a->d_mbf_hh);
   cudaFree(a->d_mbf_scratch);
+  cudaFree(a->d_mbf_err);
+  cudaFree(a->d_mbf_list);
   a->d_mbf_hh = nullptr;
   a->d_mbf_scratch = nullptr;
+  a->d_mbf_err = nullptr;
+  a->d_mbf_list = nullptr;
   a->mbf_hh_count = a->mbf_scratch_count = 0;
   a->mbf_slots = 0;
 }
@@ -656,21 +669,31 @@ struct TraceRange {
 };
 
 // Multi-banding with the IFFT-FFT <h|h>: the odd-bin transforms of every band
-// b >= 1 into the slab that the multi-banding kernels add to <h|h>.
+// b >= 1 into the slab that the multi-banding kernels add to <h|h>.  Mixed
+// precision with TaylorF2: float32 transforms with an error bound, then the
+// float64 kernel over the points whose bound exceeds the tolerance.
 int run_mb_fft(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
+  const bool mixed = L.precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2;
   const size_t need = (size_t)a->mb_bands * a->n_det * L.B;
   bool glob = false;
-  for (const MbFftBand& bd : a->mbf_bands) glob = glob || !bd.in_smem;
-  const int64_t slots = glob ? (int64_t)sm_count() : 0;
-  const size_t scratch = glob ? ((size_t)slots << a->mbf_log2m_max) : 0;
+  for (const MbFftBand& bd : a->mbf_bands)
+    glob = glob || !bd.in_smem || (mixed && !mb_hh_fft32_in_smem(bd.log2m));
+  // one global slot per resident CTA (two per SM for the float32 kernel)
+  const int64_t slots = glob ? (int64_t)(mixed ? 2 : 1) * sm_count() : 0;
+  const size_t scratch = glob ? ((size_t)slots << a->mbf_log2m_max) : 0;  // double2 elements
   if (need > a->mbf_hh_count || scratch > a->mbf_scratch_count) {
     GWL_CUDA(cudaStreamSynchronize(s));
     int rc;
     if (need > a->mbf_hh_count) {
       cudaFree(a->d_mbf_hh);
-      a->d_mbf_hh = nullptr;
+      cudaFree(a->d_mbf_err);
+      cudaFree(a->d_mbf_list);
+      a->d_mbf_hh = a->d_mbf_err = nullptr;
+      a->d_mbf_list = nullptr;
       a->mbf_hh_count = 0;
       if ((rc = dev_alloc(a, &a->d_mbf_hh, need, false))) return rc;
+      if ((rc = dev_alloc(a, &a->d_mbf_err, need, false))) return rc;
+      if ((rc = dev_alloc(a, &a->d_mbf_list, (size_t)L.B + 1, false))) return rc;
       a->mbf_hh_count = need;
     }
     if (scratch > a->mbf_scratch_count) {
@@ -682,9 +705,29 @@ int run_mb_fft(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
     }
   }
   a->mbf_slots = glob ? slots : 0;
-  for (MbFftBand bd : a->mbf_bands) {
-    bd.out = a->d_mbf_hh;
-    GWL_CUDA(launch_mb_hh_fft(L, bd, a->d_mbf_scratch, a->mbf_slots, s));
+  if (!mixed) {
+    for (MbFftBand bd : a->mbf_bands) {
+      bd.out = a->d_mbf_hh;
+      GWL_CUDA(launch_mb_hh_fft(L, bd, a->d_mbf_scratch, a->mbf_slots, false, s));
+    }
+  } else {
+    for (MbFftBand bd : a->mbf_bands) {
+      bd.out = a->d_mbf_hh;
+      bd.err = a->d_mbf_err;
+      bd.in_smem = mb_hh_fft32_in_smem(bd.log2m);
+      GWL_CUDA(launch_mb_hh_fft(L, bd, a->d_mbf_scratch, a->mbf_slots, true, s));
+    }
+    if (a->refine_tol > 0) {
+      int32_t* count = a->d_mbf_list;
+      GWL_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t), s));
+      GWL_CUDA(launch_mb_fft_marks(L, a->d_mbf_err, a->refine_tol, count + 1, count, s));
+      for (MbFftBand bd : a->mbf_bands) {
+        bd.out = a->d_mbf_hh;
+        bd.list = count + 1;
+        bd.list_count = count;
+        GWL_CUDA(launch_mb_hh_fft(L, bd, a->d_mbf_scratch, a->mbf_slots, false, s));
+      }
+    }
   }
   L.mb_fft_hh = a->d_mbf_hh;
   return GWL_OK;
@@ -1698,6 +1741,7 @@ int gwl_set_multiband(gwl_analysis* a, int enable, int64_t n_points, const doubl
   std::vector<double> bd(band_df, band_df + n_bands);
   if ((rc = upload(a, &a->mb_band_start, bs))) return rc;
   a->mb_band_start_h = bs;
+  a->mb_freq_h = fr;
   a->mb_fft = 0;  // new bands need new IFFT-FFT tables
   if ((rc = upload(a, &a->mb_band_df, bd))) return rc;
   a->mb_bands = n_bands;
@@ -1767,6 +1811,28 @@ int gwl_set_multiband_ifft_fft(gwl_analysis* a, int enable, const int32_t* ks, c
     std::vector<double> od(odd_weights + (size_t)d * total, odd_weights + (size_t)(d + 1) * total);
     if ((rc = upload(a, &a->mbf_odd[d], od))) return rc;
   }
+  // mixed precision: the odd-bin weights as float-float pairs over each band's largest
+  std::vector<double> odd_scale((size_t)nb, 1.0);
+  {
+    int64_t off0 = 0;
+    for (int b = 1; b < nb; ++b) {
+      double mx = 0.0;
+      for (int d = 0; d < a->n_det; ++d)
+        for (int64_t j = 0; j < m[b] / 2; ++j) mx = std::max(mx, std::fabs(odd_weights[(size_t)d * total + off0 + j]));
+      odd_scale[(size_t)b] = mx > 0 ? mx : 1.0;
+      off0 += m[b] / 2;
+    }
+    for (int d = 0; d < a->n_det; ++d) {
+      std::vector<float2> o32((size_t)total);
+      int64_t off1 = 0;
+      for (int b = 1; b < nb; ++b) {
+        for (int64_t j = 0; j < m[b] / 2; ++j)
+          o32[(size_t)(off1 + j)] = split_ff(odd_weights[(size_t)d * total + off1 + j] / odd_scale[(size_t)b]);
+        off1 += m[b] / 2;
+      }
+      if ((rc = upload(a, &a->mbf_odd32[d], o32))) return rc;
+    }
+  }
   // exp(-i pi k / 2^log2m_max), k < 2^(log2m_max + 1): the whole circle, as
   // the radix-4 passes read up to 3/2 of the half circle
   const int64_t n_tw = (int64_t)1 << log2m_max;
@@ -1776,6 +1842,21 @@ int gwl_set_multiband_ifft_fft(gwl_analysis* a, int enable, const int32_t* ks, c
     tw[(size_t)k] = make_double2(std::cos(th), -std::sin(th));
   }
   if ((rc = upload(a, &a->mbf_tw, tw))) return rc;
+  std::vector<float2> tw32(tw.size());
+  for (size_t k = 0; k < tw.size(); ++k) tw32[k] = make_float2((float)tw[k].x, (float)tw[k].y);
+  if ((rc = upload(a, &a->mbf_tw32, tw32))) return rc;
+  // mixed precision: sqrt(w_k) f_k^(-7/6), scaled to at most one
+  std::vector<double> awd(sw.size(), 0.0);
+  double aw_max = 0.0;
+  for (size_t k = 0; k < sw.size(); ++k) {
+    const double f = k < a->mb_freq_h.size() ? a->mb_freq_h[k] : 0.0;
+    if (f > 0 && std::isfinite(f)) awd[k] = sw[k] * std::pow(f, -7.0 / 6.0);
+    aw_max = std::max(aw_max, std::fabs(awd[k]));
+  }
+  a->mbf_aw_scale = aw_max > 0 ? aw_max : 1.0;
+  std::vector<float> aw(sw.size());
+  for (size_t k = 0; k < sw.size(); ++k) aw[k] = (float)(awd[k] / a->mbf_aw_scale);
+  if ((rc = upload(a, &a->mbf_aw, aw))) return rc;
   a->mbf_log2m_max = log2m_max;
   a->mbf_bands.clear();
   int64_t off = 0;
@@ -1790,9 +1871,16 @@ int gwl_set_multiband_ifft_fft(gwl_analysis* a, int enable, const int32_t* ks, c
     bd.log2m_max = log2m_max;
     bd.in_smem = mb_hh_fft_smem(l) > 0;
     bd.scale = scale[b];
-    for (int d = 0; d < a->n_det; ++d) bd.odd[d] = a->mbf_odd[d] + off;
+    for (int d = 0; d < a->n_det; ++d) {
+      bd.odd[d] = a->mbf_odd[d] + off;
+      bd.odd32[d] = a->mbf_odd32[d] + off;
+    }
+    bd.odd32_scale = odd_scale[(size_t)b];
     bd.sqrtw = a->mbf_sqrtw;
     bd.tw = a->mbf_tw;
+    bd.tw32 = a->mbf_tw32;
+    bd.aw = a->mbf_aw;
+    bd.aw_scale = a->mbf_aw_scale;
     a->mbf_bands.push_back(bd);
     off += m[b] / 2;
   }

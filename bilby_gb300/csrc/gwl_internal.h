@@ -359,11 +359,30 @@ struct MbFftBand {
   const double* sqrtw;           // [mb_points] square roots of the band windows
   const double2* tw;             // [2^(log2m_max + 1)] exp(-i pi k / 2^log2m_max)
   double* out;                   // the mb_fft_hh slab
+  // float64 kernel: only the listed points (list_count of them), or all
+  const int32_t* list;
+  const int32_t* list_count;
+  // float32 kernel (TaylorF2, mixed precision): the twiddles in float32, the
+  // banded amplitude table sqrt(w_k) f_k^(-7/6) / aw_scale, and the error slab
+  // (same layout as out)
+  const float2* tw32;
+  const float* aw;
+  double aw_scale;
+  const float2* odd32[kMaxDet];  // [M / 2] float-float Re I_(2j+1) / odd32_scale
+  double odd32_scale;            // the band's largest |Re I_(2j+1)|
+  double* err;
 };
-size_t mb_hh_fft_smem(int log2m);  // dynamic shared memory of a transform in shared memory, 0 if it does not fit
+size_t mb_hh_fft_smem(int log2m);  // dynamic shared memory of a float64 transform in shared memory, 0 if it does not fit
+bool mb_hh_fft32_in_smem(int log2m);
 int mb_hh_fft_threads();
-cudaError_t launch_mb_hh_fft(const LaunchArgs& a, const MbFftBand& band, double2* scratch, int64_t scratch_slots,
-                             cudaStream_t s);
+// one band's transforms: float64 (mixed = false; all points or the listed
+// ones) or float32 with the error bound (mixed = true); scratch holds
+// scratch_slots slots of 2^log2m complex values of that precision
+cudaError_t launch_mb_hh_fft(const LaunchArgs& a, const MbFftBand& band, void* scratch, int64_t scratch_slots,
+                             bool mixed, cudaStream_t s);
+// the points whose float32 error, summed over bands and detectors, exceeds tol
+cudaError_t launch_mb_fft_marks(const LaunchArgs& a, const double* err, double tol, int32_t* list, int32_t* count,
+                                cudaStream_t s);
 cudaError_t launch_source_polarizations(int model, const double* freq, int64_t n, const double* params,
                                         double fmin, double* plus, double* cross, cudaStream_t s);
 cudaError_t launch_detector_response(const DetGeom& g, const double* freq, int64_t n, const double* plus,

@@ -120,8 +120,9 @@ def test_ifft_fft_lnl_matches_the_reference(gpu, tmp_path, combo):
 @pytest.mark.parametrize("combo", ["none", "tpd"])
 def test_ifft_fft_mixed_precision_matches_float64(gpu, tmp_path, combo):
     """The mixed-precision multi-banded kernels with the IFFT-FFT <h|h> (its
-    odd bins in float64 for either precision) against the float64 ones on
-    512 prior draws and on the golden points: |dlnL| <= 1e-3."""
+    odd bins by float32 transforms with an error bound, the points over it
+    recomputed in float64) against the float64 ones on 512 prior draws and
+    on the golden points: |dlnL| <= 1e-3."""
     from bilby_gb300.analysis import params_block
     from bilby_gb300.workloads import draw_points
     w = WORKLOADS["tf2_128s"]
@@ -145,6 +146,27 @@ def test_ifft_fft_mixed_precision_matches_float64(gpu, tmp_path, combo):
     pts = _golden_points(z, priors, combo)
     got = like.log_likelihood_ratio_batch({k: np.array([q[k] for q in pts]) for k in pts[0]})
     assert np.all(np.abs(got - z["lnl_" + combo]) <= 1e-3), got - z["lnl_" + combo]
+
+
+def test_ifft_fft_mixed_refines_loud_templates(gpu, tmp_path):
+    """The float32 odd-bin transforms on templates up to 10^4 times louder
+    than the prior draws (5-120 Mpc, and 0.05-2 Mpc, at the injection's
+    masses and sky position): the error bound sends the points it cannot
+    hold to the float64 kernel, and every result stays within 1e-3 of
+    float64."""
+    from bilby_gb300.analysis import params_block
+    w = WORKLOADS["tf2_128s"]
+    like, _ = make("none", tmp_path, linear_interpolation=False, precision="mixed")
+    rng = np.random.default_rng(59)
+    for lo, hi in ((5.0, 120.0), (0.05, 2.0)):
+        loud = {k: np.full(512, float(v)) for k, v in w.injection.items()}
+        loud["luminosity_distance"] = 10 ** rng.uniform(np.log10(lo), np.log10(hi), 512)
+        loud["theta_jn"] = rng.uniform(0.0, np.pi, 512)
+        block = params_block(like._prepare(loud))
+        mixed = like.analysis.log_likelihood_ratio_host(block, "mixed")
+        fp64 = like.analysis.log_likelihood_ratio_host(block, "fp64")
+        err = np.abs(mixed - fp64)
+        assert np.all(np.isfinite(mixed)) and np.all(err <= 1e-3), (lo, err.max(), fp64[np.argmax(err)])
 
 
 def test_ifft_fft_weights_round_trip(gpu, tmp_path):
