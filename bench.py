@@ -696,16 +696,18 @@ def bench_multiband(name, steps, warmup, batch=16384, seed=37):
     # the odd-bin float64 transforms of bands 1.. per point and detector pair
     like_f = MBGravitationalWaveTransient(base.interferometers, base.waveform_generator, reference_chirp_mass=0.87,
                                           linear_interpolation=False)
-    bf = 2048
+    bf, bfm = 2048, 8192
     block_f = torch.from_numpy(params_block(draw_points(w, bf, rng))).cuda()
-    ifft = {"batch": bf, "transform_lengths": [int(m) for m in like_f.Mbs[1:]],
+    block_fm = torch.from_numpy(params_block(draw_points(w, bfm, rng))).cuda()
+    ifft = {"batch": bf, "batch_mixed": bfm, "transform_lengths": [int(m) for m in like_f.Mbs[1:]],
             "launch": "prologue + per band k_mb_hh_fft (float64) or k_mb_hh_fft32 (float32 with an error bound, "
                       "the marked points recomputed by k_mb_hh_fft), packed detector pairs, + the multi-banding "
                       "kernel"}
     outs_f = {}
     for precision in ("fp64", "mixed"):
-        ms_f, finite = time_launches(like_f.analysis, block_f, bf, steps, warmup, precision=precision)
-        ifft[precision] = {"value": bf / (ms_f / 1e3), "unit": "evals/s", "ms_per_launch": ms_f, "finite": finite}
+        blk, nb = (block_f, bf) if precision == "fp64" else (block_fm, bfm)
+        ms_f, finite = time_launches(like_f.analysis, blk, nb, steps, warmup, precision=precision)
+        ifft[precision] = {"value": nb / (ms_f / 1e3), "unit": "evals/s", "ms_per_launch": ms_f, "finite": finite}
         o = torch.empty(bf, dtype=torch.float64, device="cuda")
         like_f.analysis.log_likelihood_ratio_device(block_f.data_ptr(), bf, o.data_ptr(), precision,
                                                     stream.cuda_stream)
