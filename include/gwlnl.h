@@ -338,21 +338,23 @@ int gwl_set_multiband_time_marginalization(gwl_analysis *a, int64_t n_fft, const
  * weights (4/T) mask w / S and, for bands b >= 1, the even bins' weights
  * (4/That_b) w_k Re I_b[2 m_k], m_k = K_s + k - k_b).  Per band b >= 1 and
  * detector every evaluation transforms W = sqrt(w) s over M = m[b] samples
- * and adds scale[b] sum_j |Z_j|^2 Re I_b[2j + 1] (the odd bins) to <h|h>, in
- * float64 for either precision.  ks[b] and m[b] ([n_bands], m[0] = 0, m[b] a
+ * and adds scale[b] sum_j |Z_j|^2 Re I_b[2j + 1] (the odd bins) to <h|h>:
+ * in float64, or with GWL_PRECISION_MIXED and TaylorF2 in float32 with an
+ * error bound per point, the points over the refinement tolerance
+ * recomputed in float64.  ks[b] and m[b] ([n_bands], m[0] = 0, m[b] a
  * power of two with 1 <= ks[b] and ks[b] + n_b - 1 < m[b] / 2), scale[b] =
  * 4 / That_b, sqrt_window [n_points] the square roots of the band windows,
  * odd_weights [n_det][sum over b >= 1 of m[b] / 2] (Re I_b[2j + 1], band
  * after band).  enable = 0 switches it off; a new gwl_set_multiband does too. */
+int gwl_set_multiband_ifft_fft(gwl_analysis *a, int enable, const int32_t *ks, const int32_t *m, const double *scale,
+                               const double *sqrt_window, const double *odd_weights);
+
 /* NVTX ranges (no-ops unless a profiler is attached).  The library marks
  * its entry points (gwl_eval_device, gwl_eval_host with its h2d / launch /
  * readback steps, gwl_batcher_eval); a caller marks its own phases, e.g. a
  * server's admission, with these.  No counterpart in the reference. */
 int gwl_trace_push(const char *name);
 int gwl_trace_pop(void);
-
-int gwl_set_multiband_ifft_fft(gwl_analysis *a, int enable, const int32_t *ks, const int32_t *m, const double *scale,
-                               const double *sqrt_window, const double *odd_weights);
 
 /* Reduced-order quadrature (replaces ROQGravitationalWaveTransient.
  * calculate_snrs for one linear and one quadratic basis without time
