@@ -374,7 +374,6 @@ struct MbFftBand {
 };
 size_t mb_hh_fft_smem(int log2m);  // dynamic shared memory of a float64 transform in shared memory, 0 if it does not fit
 bool mb_hh_fft32_in_smem(int log2m);
-int mb_hh_fft_threads();
 // one band's transforms: float64 (mixed = false; all points or the listed
 // ones) or float32 with the error bound (mixed = true); scratch holds
 // scratch_slots slots of 2^log2m complex values of that precision

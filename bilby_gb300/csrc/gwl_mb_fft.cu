@@ -549,8 +549,6 @@ size_t mb_hh_fft_smem(int log2m) {
 
 bool mb_hh_fft32_in_smem(int log2m) { return log2m <= kMbFft32SmemLog2; }
 
-int mb_hh_fft_threads() { return kMbFftThreads; }
-
 cudaError_t launch_mb_hh_fft(const LaunchArgs& a, const MbFftBand& bd, void* scratch, int64_t scratch_slots,
                              bool mixed, cudaStream_t s) {
   switch (a.n_det) {

@@ -396,6 +396,10 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
     (host, port)).  Each connection sends one of
 
     * ``("eval", key, block)``: a packed [NPARAM, B] block;
+    * ``("eval_raw", key, B)`` followed by the block's raw float64 bytes
+      (``send_bytes``): the same without pickling, received straight into a
+      buffer the connection reuses (its one request in flight keeps it
+      until the step has copied it);
     * ``("eval_parameters", key, parameters)``: a sampler's dictionary,
       prepared by the registered likelihood (``submit_parameters``);
     * ``("noise", key, None)``: the analysis's noise log-likelihood;
@@ -414,6 +418,7 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
     listener = Listener(address, authkey=authkey)
     lock = threading.Lock()
     watched = {}                      # connection -> client token
+    buffers = {}                      # connection -> its receive buffer (float64)
     wake_r, wake_w = socket.socketpair()
     wake_r.setblocking(False)
 
@@ -428,6 +433,7 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
             pass                       # the client went away; the receiver drops it
 
     def drop(conn):
+        buffers.pop(conn, None)
         with lock:
             token = watched.pop(conn, None)
         if token is not None:
@@ -439,8 +445,20 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
 
     def handle(conn, msg):
         if not isinstance(msg, tuple) or len(msg) != 3 or \
-                msg[0] not in ("eval", "eval_parameters", "noise", "spec"):
+                msg[0] not in ("eval", "eval_raw", "eval_parameters", "noise", "spec"):
             conn.send(("error", "malformed message"))
+            return
+        if msg[0] == "eval_raw":
+            n = int(msg[2])
+            if not 0 < n <= (1 << 26):
+                raise ValueError("eval_raw: bad batch size")   # the stream is out of step: drop the client
+            buf = buffers.get(conn)
+            if buf is None or buf.size < _capi.NPARAM * n:
+                buf = buffers[conn] = np.empty(_capi.NPARAM * max(n, 1024), dtype=np.float64)
+            view = buf[:_capi.NPARAM * n]
+            conn.recv_bytes_into(view)
+            fut = server.submit(msg[1], view.reshape(_capi.NPARAM, n), client=watched.get(conn))
+            fut.add_done_callback(lambda f, c=conn: reply(c, f))
             return
         if msg[0] in ("noise", "spec"):
             try:
@@ -479,7 +497,7 @@ def serve_ipc(server: LikelihoodServer, address, authkey: bytes = b"gwlnl"):
                     continue
                 try:
                     handle(conn, msg)
-                except (OSError, ValueError):
+                except (OSError, ValueError, EOFError):
                     drop(conn)
 
     def accept():
@@ -551,7 +569,17 @@ class ServedLikelihood:
 
     def log_likelihood_ratio_batch(self, parameters) -> np.ndarray:
         if self.convert_on_client:
-            return self._call("eval", self.preparer.block(parameters))
+            # the packed block as raw bytes after a small header (no pickling)
+            block = np.ascontiguousarray(self.preparer.block(parameters), dtype=np.float64)
+            conn = self._connection()
+            conn.send(("eval_raw", self.key, int(block.shape[1])))
+            conn.send_bytes(block)
+            status, result = conn.recv()
+            if status != "ok":
+                if result.startswith("KeyError"):
+                    raise KeyError(result)
+                raise RuntimeError(result)
+            return result
         return self._call("eval_parameters", {k: (v if isinstance(v, str) else np.asarray(v, dtype=np.float64))
                                               for k, v in dict(parameters).items()})
 
