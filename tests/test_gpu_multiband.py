@@ -169,6 +169,27 @@ def test_ifft_fft_mixed_refines_loud_templates(gpu, tmp_path):
         assert np.all(np.isfinite(mixed)) and np.all(err <= 1e-3), (lo, err.max(), fp64[np.argmax(err)])
 
 
+def test_ifft_fft_per_detector_snrs_sum_to_the_likelihood(gpu, tmp_path):
+    """calculate_snrs per detector (one-detector analyses: the transform has
+    no partner detector) gives <h|h> values whose sum is the three-detector
+    analysis's <h|h> (detectors packed in pairs), and the lnL that
+    compute_log_likelihood_from_snrs forms from them is the likelihood's."""
+    like, priors = make("none", tmp_path, linear_interpolation=False)
+    z = golden("tf2_128s_multiband_ifft")
+    params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
+    from bilby_gb300.analysis import params_block
+    block = params_block(like._prepare({k: np.asarray(v, dtype=float) for k, v in params.items()}))
+    _, hh_all = like.analysis.inner_products_host(block, "fp64")
+    for i in range(len(params["mass_1"])):
+        q = point(params, i)
+        snrs = [like.calculate_snrs(None, ifo, parameters=dict(q)) for ifo in like.interferometers]
+        hh = sum(float(s.optimal_snr_squared) for s in snrs)
+        assert abs(hh - hh_all[i]) <= 1e-10 * max(1.0, abs(hh_all[i])), (i, hh, hh_all[i])
+        dh = sum(complex(s.d_inner_h) for s in snrs)
+        lnl = dh.real - hh / 2
+        assert abs(lnl - z["lnl_none"][i]) <= 1e-9 * max(1.0, abs(z["lnl_none"][i])), (i, lnl, z["lnl_none"][i])
+
+
 def test_ifft_fft_weights_round_trip(gpu, tmp_path):
     """The IFFT-FFT weights dictionary (Tbhats, windows, wths, hbcs, Ibcs by
     band) rebuilds a likelihood with identical results."""
