@@ -6,8 +6,9 @@ from many concurrent sampler clients with continuous batching.
   refused with ``MemoryError``.
 * Requests (analysis, batch of points) queue up; whenever one of the
   ``n_streams`` step slots is free the scheduler packs pending requests (FIFO,
-  up to ``max_points_per_step`` points and the remaining work-space budget)
-  into one step: one batched launch over all their analyses on that slot's
+  up to ``max_points_per_step`` points -- ``backlog_points_per_step`` while
+  more than that many wait -- and the remaining work-space budget) into one
+  step: one batched launch over all their analyses on that slot's
   CUDA stream.  Requests that arrive while steps are running are admitted as
   slots free up; up to ``n_streams`` steps are on the device at once.
 * Each request's result is bit-identical whether it ran alone or in a mix
@@ -171,9 +172,13 @@ class GpuBackend:
 
 class LikelihoodServer:
     def __init__(self, hbm_budget_bytes: float = 160e9, max_points_per_step: int = 1 << 15, n_streams: int = 3,
-                 backend=None, precision: str = "mixed", use_graphs: bool = False, poll_s: float = 5e-5):
+                 backend=None, precision: str = "mixed", use_graphs: bool = False, poll_s: float = 5e-5,
+                 backlog_points_per_step: int | None = None):
         self.budget = float(hbm_budget_bytes)
         self.max_points = int(max_points_per_step)
+        # while more points than this wait, a step may take this many: larger
+        # steps under a backlog (fewer per-step costs), short ones otherwise
+        self.backlog_points = int(backlog_points_per_step or 2 * self.max_points)
         self.n_streams = int(n_streams)
         self.backend = backend if backend is not None else GpuBackend(n_streams, precision, use_graphs)
         self.poll_s = poll_s
@@ -181,6 +186,7 @@ class LikelihoodServer:
         self.likelihoods: dict = {}
         self.resident = 0
         self.pending: deque = deque()
+        self._pending_points = 0          # points of the queued requests
         self.inflight: list = []
         self.cv = threading.Condition()
         self.stats = ServerStats()
@@ -255,6 +261,7 @@ class LikelihoodServer:
         req = Request(key, block, fut, time.perf_counter(), client)
         with self.cv:
             self.pending.append(req)
+            self._pending_points += req.n
             self.cv.notify()
         return fut
 
@@ -281,24 +288,30 @@ class LikelihoodServer:
             for r in self.pending:
                 if r.client is client:
                     r.future.cancel()
+                    self._pending_points -= r.n
                 else:
                     keep.append(r)
             self.pending = keep
 
     # -- scheduler ---------------------------------------------------------
     def _take(self):
-        """FIFO requests for one step, within the point and work-space limits."""
+        """FIFO requests for one step, within the point and work-space
+        limits: max_points_per_step, or backlog_points_per_step while more
+        points than that are queued."""
         take, pts, ws = [], 0, 0
         room = self.budget - self.resident
+        limit = self.backlog_points if self._pending_points > self.backlog_points else self.max_points
         while self.pending:
             r = self.pending[0]
             if r.future.cancelled():
                 self.pending.popleft()
+                self._pending_points -= r.n
                 continue
             need = self.backend.step_bytes(self.analyses[r.key], r.n)
-            if take and (pts + r.n > self.max_points or ws + need > room):
+            if take and (pts + r.n > limit or ws + need > room):
                 break
             self.pending.popleft()
+            self._pending_points -= r.n
             take.append(r)
             pts += r.n
             ws += need

@@ -88,6 +88,26 @@ def test_continuous_batching_packs_arrivals_during_a_step():
     assert {slot for slot, _ in be.launches} == {0, 1}
 
 
+def test_steps_grow_under_a_backlog():
+    """Steps take up to max_points_per_step points, and up to
+    backlog_points_per_step while more than that many wait; every request
+    still gets its own results."""
+    be = FakeBackend(delay=0.05)
+    srv = LikelihoodServer(hbm_budget_bytes=1e9, backend=be, n_streams=1, max_points_per_step=100,
+                           backlog_points_per_step=200)
+    srv.add_analysis("a", FakeAnalysis(10, 1.0))
+    futs = [srv.submit("a", block(20, q)) for q in range(30)]   # 600 points queued before the loop starts
+    srv.start()
+    for q, f in enumerate(futs):
+        assert np.array_equal(f.result(5), expected(FakeAnalysis(10, 1.0), block(20, q)))
+    srv.stop()
+    sizes = [sum(n) for _, n in be.launches]
+    assert sum(sizes) == 600 and max(sizes) <= 200
+    assert sizes[0] == 200          # 600 waiting: a backlog step
+    assert sizes[-1] <= 100         # the last 100 or fewer: an ordinary step
+    assert srv._pending_points == 0
+
+
 def test_admission_by_hbm_budget():
     srv = LikelihoodServer(hbm_budget_bytes=10_000, backend=FakeBackend())
     srv.add_analysis("a", FakeAnalysis(5_000, 1.0))
