@@ -209,6 +209,55 @@ def test_ipc_front_end_with_client_processes():
     srv.stop()
 
 
+def _raw_client(address, key, seed, conn):
+    """Packed blocks as raw bytes after an ``eval_raw`` header, twice the
+    same connection (its receive buffer reused), then a header whose size
+    does not match what follows."""
+    from multiprocessing.connection import Client
+    c = Client(address, authkey=b"gwlnl")
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in (7, 3, 1500):
+        b = rng.normal(size=(_capi.NPARAM, n))
+        c.send(("eval_raw", key, n))
+        c.send_bytes(np.ascontiguousarray(b))
+        out.append((b, c.recv()[1]))
+    conn.send(out)
+    c.send(("eval_raw", key, -4))   # malformed: the server drops this connection
+    try:
+        c.recv()
+        dropped = False
+    except (EOFError, OSError):
+        dropped = True
+    conn.send(dropped)
+
+
+def test_ipc_raw_blocks_and_a_malformed_header():
+    be = FakeBackend(delay=0.005)
+    srv = LikelihoodServer(hbm_budget_bytes=1e9, backend=be).start()
+    srv.add_analysis("a", FakeAnalysis(10, 2.0))
+    path = os.path.join(tempfile.mkdtemp(), "gwl.sock")
+    listener = serve_ipc(srv, path)
+    ctx = mp.get_context("spawn")
+    r, w = ctx.Pipe(duplex=False)
+    p = ctx.Process(target=_raw_client, args=(path, "a", 5, w))
+    p.start()
+    for b, got in r.recv():
+        assert np.array_equal(got, 2.0 * b.sum(axis=0))
+    assert r.recv() is True
+    p.join(30)
+    assert p.exitcode == 0
+    # the server still serves other clients
+    r2, w2 = ctx.Pipe(duplex=False)
+    p2 = ctx.Process(target=_client_proc, args=(path, "a", 9, w2))
+    p2.start()
+    for b, got in r2.recv():
+        assert np.array_equal(got, 2.0 * b.sum(axis=0))
+    p2.join(30)
+    listener.close()
+    srv.stop()
+
+
 class _HostOnlyLikelihood:
     """A real likelihood's parameter preparation with a fake device analysis."""
 
