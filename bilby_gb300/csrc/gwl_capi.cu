@@ -671,9 +671,13 @@ struct TraceRange {
 // Multi-banding with the IFFT-FFT <h|h>: the odd-bin transforms of every band
 // b >= 1 into the slab that the multi-banding kernels add to <h|h>.  Mixed
 // precision with TaylorF2: float32 transforms with an error bound, then the
-// float64 kernel over the points whose bound exceeds the tolerance.
+// float64 kernel over the points whose bound exceeds the tolerance.  The
+// bound holds for lnL = f(<d|h>) - <h|h> / 2 (no marginalisation, phase, time),
+// whose slope in <h|h> is -1/2; with the distance table the slope is
+// -E[(d_ref / d)^2] / 2, unbounded by the tolerance's terms, so distance
+// marginalisation keeps the float64 transforms.
 int run_mb_fft(gwl_analysis* a, LaunchArgs& L, cudaStream_t s) {
-  const bool mixed = L.precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2;
+  const bool mixed = L.precision == GWL_PRECISION_MIXED && a->model == GWL_MODEL_TAYLORF2 && !a->dist_marg;
   const size_t need = (size_t)a->mb_bands * a->n_det * L.B;
   bool glob = false;
   for (const MbFftBand& bd : a->mbf_bands)

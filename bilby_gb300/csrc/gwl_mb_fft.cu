@@ -38,7 +38,8 @@
 // (independent rounding of the banded values and of the two transforms;
 // Cauchy-Schwarz on the weighted sum); a point whose bound, summed over bands
 // and detectors, exceeds the tolerance is listed and recomputed by the
-// float64 kernel.
+// float64 kernel.  The bound is on <h|h>/2, the lnL's change without the
+// distance table; with it the float64 transforms run instead.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -495,8 +496,8 @@ __global__ void __launch_bounds__(kMbFftThreads, 2) k_mb_hh_fft32(LaunchArgs a, 
       const double eta = kFft32Err * kU32 * sqrt((double)(log2m + 2));
       const int64_t o = (int64_t)bd.band * D * a.B;
       bd.out[o + (int64_t)d1 * a.B + i] = gs * v[0];
-      // |d lnL| <= |d <h|h>| / 2 (with the distance table, at most that as well: the
-      // marginalised lnL's slope in <h|h> is below 1/2 in magnitude)
+      // |d lnL| <= |d <h|h>| / 2: the lnL's slope in <h|h> is -1/2 without
+      // the distance table (with it the host keeps the float64 transforms)
       bd.err[o + (int64_t)d1 * a.B + i] = 0.5 * gs * eta * sqrt(v[1]) * sqrt(v[2]);
       if (d2 < D) {
         bd.out[o + (int64_t)d2 * a.B + i] = gs * v[3];
