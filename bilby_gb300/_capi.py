@@ -136,6 +136,7 @@ SIGNATURES = {
     "gwl_batcher_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "gwl_last_error": (ctypes.c_char_p, []),
     "gwl_version": (ctypes.c_char_p, []),
+    "gwl_set_distance_slope": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "gwl_trace_push": (ctypes.c_int, [ctypes.c_char_p]),
     "gwl_trace_pop": (ctypes.c_int, []),
 }

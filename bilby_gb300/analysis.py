@@ -107,6 +107,11 @@ class Analysis:
         _capi.check(self._lib.gwl_set_phase_marginalization(self._h, int(enable)), "gwl_set_phase_marginalization")
         self.phase_marginalization = bool(enable)
 
+    def set_distance_slope(self, max_slope: float):
+        """The bound d_ref / d_min on the distance-marginalised lnL's slope in
+        <d|h>, by which the mixed kernels scale their error bounds."""
+        _capi.check(self._lib.gwl_set_distance_slope(self._h, float(max_slope)), "gwl_set_distance_slope")
+
     def set_distance_marginalization(self, enable: bool, tx=None, ty=None, coeffs=None, bbox=None,
                                      reference_distance=0.0):
         if not enable:

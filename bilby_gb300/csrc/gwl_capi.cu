@@ -76,6 +76,7 @@ struct gwl_analysis {
   double w_scale[kMaxDet] = {}, v_scale[kMaxDet] = {};
   // marginalisation
   int time_marg = 0, jitter = 0, phase_marg = 0, dist_marg = 0;
+  double dist_slope = 1.0;  // d_ref / d_min of the distance prior (gwl_set_distance_slope)
   double t_min = 0, t_max = 0;
   double* tm_prior = nullptr;  // time prior density on a uniform grid (nullptr: Uniform)
   float* tm_prior_f = nullptr;
@@ -379,6 +380,7 @@ LaunchArgs make_args(gwl_analysis* a, int64_t B, int precision) {
   L.time_marg = a->time_marg;
   L.phase_marg = a->phase_marg;
   L.dist_marg = a->dist_marg;
+  L.dist_slope = a->dist_marg && !a->time_marg ? a->dist_slope : 1.0;
   L.jitter = a->jitter;
   L.t_min = a->t_min;
   L.t_max = a->t_max;
@@ -1525,6 +1527,20 @@ int gwl_set_phase_marginalization(gwl_analysis* a, int enable) {
   }
   std::lock_guard<std::mutex> g(a->mu);
   a->phase_marg = enable ? 1 : 0;
+  return GWL_OK;
+}
+
+int gwl_set_distance_slope(gwl_analysis* a, double max_slope) {
+  if (!a) {
+    set_error("null argument");
+    return GWL_ERR_ARGUMENT;
+  }
+  if (!(max_slope >= 1.0) || !std::isfinite(max_slope)) {
+    set_error("the distance slope bound d_ref / d_min must be finite and at least 1");
+    return GWL_ERR_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> g(a->mu);
+  a->dist_slope = max_slope;
   return GWL_OK;
 }
 

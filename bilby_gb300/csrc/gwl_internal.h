@@ -219,6 +219,12 @@ struct LaunchArgs {
   // mb_fft_hh[(b * n_det + d) * B + i], written by k_mb_hh_fft before the
   // kernels that add it to <h|h> (band 0 is wholly in mb_quad); null without it
   const double* mb_fft_hh;
+  // distance marginalisation without time marginalisation: a bound r_max =
+  // d_ref / d_min on the lnL's slope E[d_ref / d] in <d|h> (and r_max^2 / 2 in
+  // <h|h>), by which the mixed kernels scale their error bounds; values <= 1
+  // (no distance table, or time marginalisation with its own sensitivities)
+  // leave them as they are
+  double dist_slope;
   // reduced-order quadrature: the model at the linear and quadratic nodes,
   // time-dependent linear weights on the grid (t_start + k) dt, k < n_time
   int roq;

@@ -181,7 +181,9 @@ __device__ __noinline__ void prologue_point(const LaunchArgs& a, int64_t i) {
       l2 += s * s * (a.rf_p2[d][k1] - a.rf_p2[d][k0]);
       l1 += s * (a.rf_p1[d][k1] - a.rf_p1[d][k0]);
     }
-    if (kRefineL2 * sqrt(fmax(l2, 0.0)) + kRefineL1 * l1 > a.rf_tol) {
+    // (times the distance slope bound: the lnL's change per unit <d|h>)
+    const double slope = a.dist_slope > 1.0 ? a.dist_slope : 1.0;
+    if (slope * (kRefineL2 * sqrt(fmax(l2, 0.0)) + kRefineL1 * l1) > a.rf_tol) {
       r.refine = 1;
       atomicAdd(a.rf_count, 1);
       if (a.rf_total) atomicAdd(a.rf_total, 1);
@@ -1393,9 +1395,11 @@ __device__ __noinline__ void finalize_point(const LaunchArgs& a, int64_t i, int6
   detector_totals(a, i, G, r, &dr, &di, &hh, sg_bound ? &err : nullptr);
   finish_point(a, r, i, dr, di, hh);
   if (sg_bound) {
-    err += kSgCoherentErr * (fabs(dr) + fabs(di)) + kSgHhErr * hh;
     // the bound holds for Re <d|h> - <h|h> / 2 and, as ln I0 has slope at
-    // most one, for the phase-marginalised ln I0(|<d|h>|) - <h|h> / 2
+    // most one, for the phase-marginalised ln I0(|<d|h>|) - <h|h> / 2; with
+    // the distance table the slopes are at most r and r^2 / 2 (r = dist_slope)
+    const double slope = a.dist_slope > 1.0 ? a.dist_slope : 1.0;
+    err = slope * (err + kSgCoherentErr * (fabs(dr) + fabs(di))) + slope * slope * kSgHhErr * hh;
     if (!(err <= a.rf_tol)) {
       a.rec[i].refine = 1;
       atomicAdd(a.rf_count, 1);
@@ -1857,6 +1861,8 @@ __global__ void __launch_bounds__(32 * kRelbinWarps) k_multiband_mixed(LaunchArg
         err += kMbRandomErr * r.amp * hypot(qr, qi) * a.mb_lw_scale[d] *
                sqrt(fmax(a.mb_l2prefix[d][kb1] - a.mb_l2prefix[d][kb0], 0.0));
       }
+      // (times the distance slope bound: the lnL's change per unit <d|h>)
+      if (a.dist_slope > 1.0) err *= a.dist_slope;
       if (a.rf_tol > 0 && a.rf_count && !(err <= a.rf_tol)) {
         a.rec[i].refine = 1;
         atomicAdd(a.rf_count, 1);

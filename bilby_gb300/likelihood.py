@@ -409,6 +409,8 @@ class GravitationalWaveTransient(_Base):
         if self.distance_marginalization:
             tx, ty, c = self._spline_tck
             an.set_distance_marginalization(True, tx, ty, c, self._spline_bbox, self._ref_dist)
+            # E[d_ref / d] under any distance posterior is at most d_ref / d_min
+            an.set_distance_slope(max(1.0, float(self._ref_dist) / float(self._distance_array[0])))
 
     # ------------------------------------------------------------------
     # pickling: the device handle is rebuilt in the receiving process

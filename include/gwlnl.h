@@ -143,6 +143,14 @@ int gwl_set_distance_marginalization(gwl_analysis *a, int enable, const double *
                                      const double *ty, int32_t ny, const double *c,
                                      const double bbox[4], double reference_distance);
 
+/* The bound r_max = d_ref / d_min (at least 1) on the slope E[d_ref / d] of
+ * the distance-marginalised lnL in <d|h> (base.py:775-784): with distance
+ * and without time marginalisation the mixed-precision kernels scale their
+ * <d|h> error bounds by r_max and their <h|h> ones by r_max^2 / 2 before
+ * comparing them with the refinement tolerance, so that |dlnL| stays below
+ * it for every point.  Default 1. */
+int gwl_set_distance_slope(gwl_analysis *a, double max_slope);
+
 /* log_likelihood_ratio for B points.
  *   params: device pointer to a [GWL_NPARAM][B] float64 block (slot-major)
  *   out:    device pointer to B float64 results
